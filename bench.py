@@ -1,0 +1,352 @@
+#!/usr/bin/env python
+"""Benchmark: 65,536 uneven glyph-like paths rasterised to Matte8 masks (NonZero).
+
+One step = one pass of the fill path over the whole batch (65,536 independent
+Plotter::fill calls, each on its own canvas of side 16..256).
+
+  value  Mpx/s with ops and masks resident in HBM: the prepared batch replays its
+         CUDA graph (persistent kernel) K times, timed with CUDA events.
+  e2e    the same metric through the C ABI call with host buffers
+         (ft_fill_batch, FT_HOST): ops and rasters copied in, masks copied out,
+         inside the timed region.
+  cpu_baseline  the CPU oracle (a C++ restatement of footile's Plotter) on the
+         host cores, one Plotter per path, on a bounded sample.
+
+`--impl reference` times the CPU implementation alone (the reference is a Rust
+crate and cannot be built here; its restatement is the timed CPU code).
+
+Multi-GPU (torchrun): every rank renders its own 65,536-path batch (weak
+scaling, no collective on the data path); value = all ranks' pixels / max time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mpx/s"
+WORKLOAD = "glyphs_65536"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n-paths", type=int, default=65536)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
+    ap.add_argument("--per-path-sample", type=int, default=4096)
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def config(args, world):
+    return {"workload": WORKLOAD, "paths_per_gpu": args.n_paths, "canvas_side": "16..256 log-uniform",
+            "segments": "4..400 log-uniform, 70% quad / 20% cubic / 10% line", "fill_rule": "NonZero",
+            "format": "Matte8", "seed": "3 + rank", "parallelism": f"replicas x{world} (paths per rank)",
+            "l2": "inputs larger than L2 (ops 185 MB + masks 780 MB per step)"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of the rasteriser from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "k_raster_glyphs_65536.txt")
+    try:
+        for line in open(p):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_baseline(ops, paths, nbytes, seconds, threads):
+    """Time the oracle on a bounded sample of the workload (all host threads)."""
+    import oracle
+    from footile_gb300 import _abi
+    px = paths["width"].astype(np.int64) * paths["height"]
+    probe = min(512, len(paths))
+    r = np.zeros(nbytes, np.uint8)
+    t0 = time.perf_counter()
+    oracle.fill_batch(0, _abi.NONZERO, ops, paths[:probe], _abi.MATTE8, r, n_threads=threads)
+    dt = time.perf_counter() - t0
+    rate = probe / max(dt, 1e-6)
+    n = int(min(len(paths), max(probe, rate * seconds)))
+    t0 = time.perf_counter()
+    oracle.fill_batch(0, _abi.NONZERO, ops, paths[:n], _abi.MATTE8, r, n_threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": float(px[:n].sum() / dt / 1e6), "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"first {n} of {len(paths)} paths ({int(px[:n].sum())} px), one Plotter per path",
+            "paths_per_s": n / dt, "seconds": dt}
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    from footile_gb300 import workloads
+    ops, paths, nbytes = workloads.glyphs(args.n_paths, seed=3)
+    threads = os.cpu_count() or 1
+    px = paths["width"].astype(np.int64) * paths["height"]
+    import oracle
+    from footile_gb300 import _abi
+    # each step: a bounded sample of the workload sized so the run stays within minutes
+    r = np.zeros(nbytes, np.uint8)
+    probe = min(256, len(paths))
+    t0 = time.perf_counter()
+    oracle.fill_batch(0, _abi.NONZERO, ops, paths[:probe], _abi.MATTE8, r, n_threads=threads)
+    rate = probe / max(time.perf_counter() - t0, 1e-6)
+    budget = 120.0 / max(args.steps + args.warmup, 1)
+    n = int(min(len(paths), max(probe, rate * budget)))
+    sample = paths[:n]
+    for _ in range(args.warmup):
+        oracle.fill_batch(0, _abi.NONZERO, ops, sample, _abi.MATTE8, r, n_threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.fill_batch(0, _abi.NONZERO, ops, sample, _abi.MATTE8, r, n_threads=threads)
+    dt = (time.perf_counter() - t0) / max(args.steps, 1)
+    val = float(px[:n].sum() / dt / 1e6)
+    desc = f"first {n} of {len(paths)} paths per step ({int(px[:n].sum())} px)"
+    out = {"metric": METRIC, "value": val, "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "int32 (16.16 fixed) + f32", "data": "synthetic",
+           "config": config(args, world),
+           "cpu_baseline": {"value": val, "unit": METRIC, "cores": threads, "kind": "port", "sample": desc},
+           "e2e": {"value": val, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "note": "footile is a Rust crate; no cargo/rustc in this image, so the timed CPU code is its C++ "
+                   "restatement (oracle/footile_oracle.cpp), one Plotter per path on all host threads"}
+    print(json.dumps(out), flush=True)
+
+
+def run_ours(args):
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from footile_gb300 import _abi, workloads
+    from footile_gb300._lib import Context
+    from footile_gb300.plotter import PreparedBatch
+
+    ops, paths, nbytes = workloads.glyphs(args.n_paths, seed=3 + rank)
+    px_total = int((paths["width"].astype(np.int64) * paths["height"]).sum())
+    n_ops = len(ops)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    ctx = Context(local)
+    ctx.set_stream(stream.cuda_stream)
+    ops_d = torch.from_numpy(ops.view(np.uint8)).to(dev)
+    ras_d = torch.zeros(nbytes, dtype=torch.uint8, device=dev)
+    batch = PreparedBatch(ctx, paths, _abi.MATTE8)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        batch.launch(ops_d, ras_d)
+    st = batch.status()
+    assert (st == 0).all(), f"path status errors: {np.unique(st)}"
+
+    # ---- device-resident throughput (value)
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    launches0 = ctx.launch_count()
+    e0.record(stream)
+    for _ in range(args.steps):
+        batch.launch(ops_d, ras_d)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    launches = ctx.launch_count() - launches0
+    ms = e0.elapsed_time(e1) / max(args.steps, 1)
+    # per-launch device time of the graph (memsets + rasteriser), library events
+    kms = []
+    for _ in range(args.steps):
+        batch.launch(ops_d, ras_d)
+        kms.append(ctx.last_ms())
+    clk = clocks.stop()
+    ms_max = ms
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+    value = px_total * world / (ms_max * 1e-3) / 1e6
+
+    # ---- end to end through the C ABI with host buffers (e2e)
+    from footile_gb300.plotter import fill_batch
+    ops_h = torch.from_numpy(ops.view(np.uint8)).pin_memory()
+    ras_h = torch.zeros(nbytes, dtype=torch.uint8).pin_memory()
+    ops_np = ops_h.numpy().view(_abi.OP_DTYPE)
+    ras_np = ras_h.numpy()
+    ctx2 = Context(local)
+    fill_batch(ctx2, ops_np, paths, _abi.MATTE8, ras_np)  # warm (allocations)
+    barrier()
+    t0 = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, 5))
+    for _ in range(e2e_steps):
+        fill_batch(ctx2, ops_np, paths, _abi.MATTE8, ras_np)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    barrier()
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_val = px_total * world / e2e_s / 1e6
+    # masks of the e2e path must equal the device path's
+    same = bool(np.array_equal(ras_np, ras_d.cpu().numpy()))
+
+    # ---- one launch per path (ft_fill, device mode), on a sample
+    per_path = None
+    if rank == 0 and args.per_path_sample > 0:
+        import ctypes
+        n = min(args.per_path_sample, len(paths))
+        sub_px = int((paths["width"][:n].astype(np.int64) * paths["height"][:n]).sum())
+        L = ctx.L
+        base_o, base_r = ops_d.data_ptr(), ras_d.data_ptr()
+        clr = (ctypes.c_uint8 * 4)(0, 0, 0, 0)
+
+        def one(i):
+            d = paths[i]
+            rc = L.ft_fill(ctx.h, _abi.NONZERO, ctypes.c_void_p(base_o + 32 * int(d["op_begin"])), int(d["n_ops"]),
+                           _abi.MATTE8, clr, ctypes.c_void_p(base_r + int(d["raster_offset"])), int(d["width"]),
+                           int(d["height"]), int(d["stride"]), _abi.DEVICE)
+            ctx.check(rc)
+        for i in range(min(64, n)):
+            one(i)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(n):
+            one(i)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        per_path = {"paths_per_s": n / dt, "mpx_per_s": sub_px / dt / 1e6, "sample_paths": n,
+                    "launches_per_path": 1}
+
+    # ---- CPU baseline (rank 0, N=1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(ops, paths, nbytes, args.cpu_seconds, os.cpu_count() or 1)
+
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peak_hbm()
+    alg_bytes = px_total + 32 * n_ops + 40 * len(paths)
+    kmean = float(np.mean(kms)) if kms else ms
+    achieved = alg_bytes / (kmean * 1e-3) / 1e9
+    out = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32 (16.16 fixed) + f32", "data": "synthetic",
+        "config": config(args, world),
+        "paths_per_s": len(paths) * world / (ms_max * 1e-3),
+        "e2e": {"value": e2e_val, "unit": METRIC, "h2d_bytes_per_step": int(32 * n_ops + nbytes + 40 * len(paths)),
+                "d2h_bytes_per_step": int(nbytes), "ms_per_step": e2e_s * 1e3, "masks_equal_device_path": same},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": profiled_traffic(), "peak_kind": peak_kind,
+                     "kernel": "ftk::k_raster (graph: 2 memsets + rasteriser)", "kernel_ms": kmean,
+                     "algorithmic_bytes_per_launch": int(alg_bytes)},
+        "cpu_baseline": cpu,
+        "modes": {"batched_paths_per_s": len(paths) / (ms_max * 1e-3), "per_path_launch": per_path,
+                  "batched_over_per_path": (len(paths) / (ms_max * 1e-3) / per_path["paths_per_s"]) if per_path else None},
+        "clocks": clk,
+        "gpu_launches": int(launches),
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,139 @@
+"""ctypes binding of libfootile_gpu.so (the C ABI in include/footile_gpu.h).
+
+The library is built in-tree by `footile_gb300._build`.  There is no CPU
+fallback: if the shared library is missing or no GPU is present, every call
+raises.
+"""
+import ctypes
+import os
+import threading
+
+from . import _abi
+from ._build import LIB, build, up_to_date
+
+_lock = threading.Lock()
+_lib = None
+
+
+class FootileError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{_abi.STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+def load(auto_build=True):
+    """Load libfootile_gpu.so, compiling it first when it is missing or stale."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not up_to_date():
+            if not auto_build:
+                raise RuntimeError(f"{LIB} is missing; run footile_gb300._build.build()")
+            build()
+        L = ctypes.CDLL(LIB)
+        P = ctypes.c_void_p
+        i32, u32, u64, f32 = ctypes.c_int32, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_float
+        sig = {
+            "ft_ctx_create": ([ctypes.c_int, ctypes.POINTER(P)], ctypes.c_int),
+            "ft_ctx_destroy": ([P], None),
+            "ft_set_stream": ([P, P], ctypes.c_int),
+            "ft_set_tolerance": ([P, f32], ctypes.c_int),
+            "ft_set_transform": ([P, P], ctypes.c_int),
+            "ft_set_join": ([P, i32, f32], ctypes.c_int),
+            "ft_set_pen_width": ([P, f32], ctypes.c_int),
+            "ft_get_pen_width": ([P, ctypes.POINTER(f32)], ctypes.c_int),
+            "ft_fill": ([P, i32, P, u32, i32, P, P, u32, u32, u32, i32], ctypes.c_int),
+            "ft_stroke": ([P, P, u32, i32, P, P, u32, u32, u32, i32], ctypes.c_int),
+            "ft_fill_batch": ([P, i32, i32, P, u32, P, u32, i32, P, u64, i32], ctypes.c_int),
+            "ft_batch_status": ([P, P, u32], ctypes.c_int),
+            "ft_sync": ([P], ctypes.c_int),
+            "ft_last_error": ([P], ctypes.c_char_p),
+            "ft_last_timings": ([P, ctypes.POINTER(f32)], ctypes.c_int),
+            "ft_launch_count": ([P], u64),
+            "ft_batch_create": ([P, i32, i32, P, u32, i32, ctypes.POINTER(P)], ctypes.c_int),
+            "ft_batch_launch": ([P, P, P, u32, P, u64], ctypes.c_int),
+            "ft_batch_launch_status": ([P, P, P, u32], ctypes.c_int),
+            "ft_batch_destroy": ([P], None),
+        }
+        for name, (args, res) in sig.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+        return _lib
+
+
+def exported_symbols():
+    """Names of the C ABI functions declared in include/footile_gpu.h."""
+    return [n for n in (
+        "ft_ctx_create", "ft_ctx_destroy", "ft_set_stream", "ft_set_tolerance", "ft_set_transform",
+        "ft_set_join", "ft_set_pen_width", "ft_get_pen_width", "ft_fill", "ft_stroke", "ft_fill_batch",
+        "ft_batch_status", "ft_sync", "ft_last_error", "ft_last_timings", "ft_launch_count",
+        "ft_batch_create", "ft_batch_launch", "ft_batch_launch_status", "ft_batch_destroy")]
+
+
+class Context:
+    """One `ft_ctx`: footile's Plotter settings plus device buffers and a stream."""
+
+    def __init__(self, device=0):
+        self.L = load()
+        h = ctypes.c_void_p()
+        rc = self.L.ft_ctx_create(device, ctypes.byref(h))
+        if rc != _abi.OK:
+            raise FootileError(rc, "ft_ctx_create failed (no usable CUDA device?)")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.ft_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, rc):
+        if rc != _abi.OK:
+            raise FootileError(rc, self.L.ft_last_error(self.h).decode())
+        return rc
+
+    def set_tolerance(self, t):
+        self.check(self.L.ft_set_tolerance(self.h, t))
+
+    def set_transform(self, m):
+        arr = (ctypes.c_float * 6)(*[float(v) for v in m])
+        self.check(self.L.ft_set_transform(self.h, arr))
+
+    def set_join(self, kind, limit):
+        self.check(self.L.ft_set_join(self.h, kind, limit))
+
+    def set_pen_width(self, w):
+        self.check(self.L.ft_set_pen_width(self.h, w))
+
+    def pen_width(self):
+        v = ctypes.c_float()
+        self.check(self.L.ft_get_pen_width(self.h, ctypes.byref(v)))
+        return v.value
+
+    def set_stream(self, stream_ptr):
+        self.check(self.L.ft_set_stream(self.h, ctypes.c_void_p(stream_ptr)))
+
+    def sync(self):
+        self.check(self.L.ft_sync(self.h))
+
+    def last_ms(self):
+        v = ctypes.c_float()
+        self.check(self.L.ft_last_timings(self.h, ctypes.byref(v)))
+        return v.value
+
+    def launch_count(self):
+        return int(self.L.ft_launch_count(self.h))
+
+    def batch_status(self, n):
+        import numpy as np
+        st = np.zeros(n, dtype=np.int32)
+        self.check(self.L.ft_batch_status(self.h, st.ctypes.data_as(ctypes.c_void_p), n))
+        return st

@@ -1,0 +1,597 @@
+// ft_capi.cu — the C ABI of include/footile_gpu.h: context state (footile's
+// Plotter settings), device buffers, work-item planning and kernel launches.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ft_kernels.cuh"
+
+namespace {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= cap) return cudaSuccess;
+        if (p) {
+            cudaDeviceSynchronize();  // earlier asynchronous work may still use the old buffer
+            cudaFree(p);
+        }
+        p = nullptr;
+        cap = 0;
+        size_t want = std::max(bytes, (size_t)256);
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+}  // namespace
+
+struct ft_batch;
+
+struct ft_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    // Plotter state (plotter.rs:96-115)
+    float tolerance = 0.3f;
+    float xf[6] = {1, 0, 0, 0, 1, 0};
+    int join = FT_JOIN_MITER;
+    float miter_limit = 4.0f;
+    float s_width = 1.0f;   // host copy, valid unless sw_on_device
+    bool sw_on_device = false;
+    // device buffers
+    DevBuf ops, paths, items, status, sw_out, rasters, queue, scratch, sw_chain;
+    std::vector<ftk::WorkItem> h_items;
+    uint32_t last_n_paths = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bool timed = false;
+    uint64_t launches = 0;
+    int sm_count = 0;
+    int max_smem = 0;
+    std::string err;
+};
+
+namespace {
+
+int fail(ft_ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+int cuda_fail(ft_ctx* c, cudaError_t e, const char* what) {
+    return fail(c, e == cudaErrorMemoryAllocation ? FT_ERR_NOMEM : FT_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define FT_CU(call, what)                                 \
+    do {                                                  \
+        cudaError_t _e = (call);                          \
+        if (_e != cudaSuccess) return cuda_fail(c, _e, what); \
+    } while (0)
+
+// Dynamic shared memory for a batch whose widest raster row is `max_w` pixels.
+int choose_smem(const ft_ctx* c, uint32_t max_w) {
+    const int wp = (int)((max_w + 3) & ~3u);
+    const char* env = getenv("FT_SMEM_BYTES");
+    int smem;
+    if (env) {
+        smem = atoi(env);
+    } else if (wp <= 512) {
+        smem = 64 * 1024;
+    } else {
+        smem = ftk::RASTER_FIXED_SMEM + 16 * wp * 4;
+    }
+    smem = std::max(smem, ftk::RASTER_FIXED_SMEM + wp * 4);
+    smem = std::max(smem, (int)(40 * 1024));  // room for the build-phase buffers
+    smem = std::min(smem, c->max_smem);
+    return smem;
+}
+
+// Split each path into work items of whole bands (host side of the device queue).
+void plan_items(ft_ctx* c, const ft_path_desc* paths, uint32_t n_paths, int smem, std::vector<ftk::WorkItem>& out) {
+    out.clear();
+    out.reserve(n_paths);
+    const int area_bytes = smem - ftk::RASTER_FIXED_SMEM;
+    std::vector<std::pair<uint64_t, uint32_t>> order;
+    const char* env = getenv("FT_SPLIT_PX");
+    const uint64_t split_px = env ? strtoull(env, nullptr, 10) : (uint64_t)(1u << 20);
+    for (uint32_t i = 0; i < n_paths; i++) {
+        const ft_path_desc& d = paths[i];
+        const uint32_t wp = (d.width + 3) & ~3u;
+        uint32_t R = wp ? (uint32_t)(area_bytes / (int)(wp * 4)) : 1;
+        R = std::max(1u, std::min(R, std::max(d.height, 1u)));
+        uint32_t rows_per_item = std::max(d.height, 1u);
+        if ((uint64_t)d.width * d.height >= split_px && c->sm_count > 0) {
+            uint32_t target = (d.height + (uint32_t)c->sm_count - 1) / (uint32_t)c->sm_count;
+            rows_per_item = std::max(R, ((target + R - 1) / R) * R);
+        }
+        for (uint32_t r = 0; r < std::max(d.height, 1u); r += rows_per_item) {
+            ftk::WorkItem w;
+            w.path = i;
+            w.row_begin = r;
+            w.row_end = std::min(d.height, r + rows_per_item);
+            w.band_rows = R;
+            out.push_back(w);
+        }
+    }
+    // longest items first: ops drive the build, pixels the bands
+    std::vector<uint64_t> cost(out.size());
+    for (size_t k = 0; k < out.size(); k++) {
+        const ft_path_desc& d = paths[out[k].path];
+        cost[k] = (uint64_t)d.n_ops * 64 + (uint64_t)d.width * (out[k].row_end - out[k].row_begin) / 8;
+    }
+    std::vector<uint32_t> idx(out.size());
+    for (size_t k = 0; k < idx.size(); k++) idx[k] = (uint32_t)k;
+    std::stable_sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) { return cost[a] > cost[b]; });
+    std::vector<ftk::WorkItem> sorted(out.size());
+    for (size_t k = 0; k < idx.size(); k++) sorted[k] = out[idx[k]];
+    out.swap(sorted);
+    (void)order;
+}
+
+int check_path(ft_ctx* c, const ft_path_desc& d, int fmt, uint64_t raster_bytes, uint64_t n_ops_total) {
+    const uint32_t bpp = fmt == FT_RGBA8P ? 4 : 1;
+    if (d.width > FT_MAX_WIDTH) return fail(c, FT_ERR_CAP, "raster wider than FT_MAX_WIDTH");
+    if ((uint64_t)d.op_begin + d.n_ops > n_ops_total) return fail(c, FT_ERR_ARG, "path ops out of range");
+    if (d.height > 0 && d.width > 0) {
+        if ((uint64_t)d.stride < (uint64_t)d.width * bpp) return fail(c, FT_ERR_ARG, "stride smaller than a row");
+        const uint64_t end = d.raster_offset + (uint64_t)(d.height - 1) * d.stride + (uint64_t)d.width * bpp;
+        if (end > raster_bytes) return fail(c, FT_ERR_ARG, "raster region out of range");
+        if (fmt == FT_RGBA8P && ((d.raster_offset | d.stride) & 3))
+            return fail(c, FT_ERR_ARG, "Rgba8p rasters need 4-byte aligned rows");
+    }
+    return FT_OK;
+}
+
+// Kernel parameters for a planned launch.
+void fill_params(ft_ctx* c, ftk::KParams& p, int stroke, int rule, int fmt, int smem) {
+    memset(&p, 0, sizeof(p));
+    for (int i = 0; i < 6; i++) p.xf[i] = c->xf[i];
+    const float t = std::max(c->tolerance, 0.01f);
+    p.tol_sq = t * t;
+    p.join = c->join;
+    p.miter_limit = c->miter_limit;
+    p.rule = rule;
+    p.fmt = fmt;
+    p.stroke = stroke;
+    p.smem_bytes = smem;
+}
+
+int grid_for(ft_ctx* c, int smem, uint32_t n_items) {
+    const int per_sm = ftk::raster_blocks_per_sm(smem);
+    const char* genv = getenv("FT_GRID");
+    int grid = genv ? atoi(genv) : c->sm_count * per_sm;
+    return std::max(1, std::min(grid, (int)std::max(n_items, 1u)));
+}
+
+// Queue, statuses, launch.  `ops_d` / `rasters_d` are device pointers.
+int run(ft_ctx* c, int stroke, int rule, const ft_op* ops_d, const ft_path_desc* paths, uint32_t n_paths, int fmt,
+        uint8_t* rasters_d, const float* sw_chain, float* sw_out) {
+    uint32_t max_w = 1;
+    for (uint32_t i = 0; i < n_paths; i++) max_w = std::max(max_w, paths[i].width);
+    const int smem = choose_smem(c, max_w);
+    plan_items(c, paths, n_paths, smem, c->h_items);
+    const uint32_t n_items = (uint32_t)c->h_items.size();
+    FT_CU(c->paths.ensure(sizeof(ft_path_desc) * std::max(n_paths, 1u)), "alloc paths");
+    FT_CU(c->items.ensure(sizeof(ftk::WorkItem) * std::max(n_items, 1u)), "alloc items");
+    FT_CU(c->status.ensure(sizeof(int32_t) * std::max(n_paths, 1u)), "alloc status");
+    FT_CU(c->queue.ensure(256), "alloc queue");
+    const int grid = grid_for(c, smem, n_items);
+    FT_CU(c->scratch.ensure(ftk::SCRATCH_BYTES_PER_CTA * (size_t)grid), "alloc scratch");
+    FT_CU(cudaMemcpyAsync(c->paths.p, paths, sizeof(ft_path_desc) * n_paths, cudaMemcpyHostToDevice, c->stream),
+          "upload paths");
+    FT_CU(cudaMemcpyAsync(c->items.p, c->h_items.data(), sizeof(ftk::WorkItem) * n_items, cudaMemcpyHostToDevice,
+                          c->stream),
+          "upload items");
+    FT_CU(cudaMemsetAsync(c->queue.p, 0, 256, c->stream), "reset queue");
+    FT_CU(cudaMemsetAsync(c->status.p, 0, sizeof(int32_t) * std::max(n_paths, 1u), c->stream), "reset status");
+    c->last_n_paths = n_paths;
+    if (n_items == 0) return FT_OK;
+    ftk::KParams p;
+    fill_params(c, p, stroke, rule, fmt, smem);
+    p.ops = ops_d;
+    p.paths = static_cast<const ft_path_desc*>(c->paths.p);
+    p.items = static_cast<const ftk::WorkItem*>(c->items.p);
+    p.n_items = n_items;
+    p.queue = static_cast<uint32_t*>(c->queue.p);
+    p.rasters = rasters_d;
+    p.status = static_cast<int32_t*>(c->status.p);
+    p.sw_out = sw_out;
+    p.sw_chain = sw_chain;
+    p.scratch = static_cast<unsigned char*>(c->scratch.p);
+    FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
+    FT_CU(ftk::launch_raster(p, grid, smem, c->stream), "launch rasteriser");
+    c->launches++;
+    FT_CU(cudaEventRecord(c->ev1, c->stream), "event");
+    c->timed = true;
+    return FT_OK;
+}
+
+bool valid_ops_host(const ft_op* ops, uint64_t n) {
+    for (uint64_t i = 0; i < n; i++)
+        if (ops[i].kind < FT_OP_CLOSE || ops[i].kind > FT_OP_PEN_WIDTH) return false;
+    return true;
+}
+
+int single(ft_ctx* c, int stroke, int32_t rule, const ft_op* ops, uint32_t n_ops, int32_t fmt, const uint8_t clr[4],
+           uint8_t* raster, uint32_t w, uint32_t h, uint32_t stride, int32_t where) {
+    if (!c) return FT_ERR_ARG;
+    if ((rule != FT_NONZERO && rule != FT_EVENODD) || (fmt != FT_MATTE8 && fmt != FT_RGBA8P) ||
+        (where != FT_HOST && where != FT_DEVICE))
+        return fail(c, FT_ERR_ARG, "bad rule, format or location");
+    if ((n_ops && !ops) || (w && h && !raster)) return fail(c, FT_ERR_ARG, "null buffer");
+    if (stroke) return fail(c, FT_ERR_ARG, "stroke is not available in this build");
+    FT_CU(cudaSetDevice(c->device), "set device");
+    ft_path_desc d;
+    memset(&d, 0, sizeof(d));
+    d.op_begin = 0;
+    d.n_ops = n_ops;
+    d.width = w;
+    d.height = h;
+    d.raster_offset = 0;
+    d.stride = stride;
+    d.s_width = c->s_width;
+    if (clr) memcpy(d.clr, clr, 4);
+    const uint32_t bpp = fmt == FT_RGBA8P ? 4 : 1;
+    const uint64_t raster_bytes = h ? (uint64_t)(h - 1) * stride + (uint64_t)w * bpp : 0;
+    int st = check_path(c, d, fmt, raster_bytes, n_ops);
+    if (st != FT_OK) return st;
+    // pen-width chain: [0] current value, [1] value after this call
+    FT_CU(c->sw_chain.ensure(2 * sizeof(float)), "alloc pen width");
+    float* swd = static_cast<float*>(c->sw_chain.p);
+    if (!c->sw_on_device) {
+        FT_CU(cudaMemcpyAsync(swd, &c->s_width, sizeof(float), cudaMemcpyHostToDevice, c->stream), "pen width");
+        c->sw_on_device = true;
+    }
+    const ft_op* ops_d = ops;
+    uint8_t* ras_d = raster;
+    if (where == FT_HOST) {
+        if (!valid_ops_host(ops, n_ops)) return fail(c, FT_ERR_ARG, "unknown path op kind");
+        FT_CU(c->ops.ensure(sizeof(ft_op) * std::max(n_ops, 1u)), "alloc ops");
+        FT_CU(c->rasters.ensure(std::max(raster_bytes, (uint64_t)1)), "alloc raster");
+        if (n_ops)
+            FT_CU(cudaMemcpyAsync(c->ops.p, ops, sizeof(ft_op) * n_ops, cudaMemcpyHostToDevice, c->stream),
+                  "upload ops");
+        if (raster_bytes)
+            FT_CU(cudaMemcpyAsync(c->rasters.p, raster, raster_bytes, cudaMemcpyHostToDevice, c->stream),
+                  "upload raster");
+        ops_d = static_cast<const ft_op*>(c->ops.p);
+        ras_d = static_cast<uint8_t*>(c->rasters.p);
+    } else if ((reinterpret_cast<uintptr_t>(ops) & 15) || (fmt == FT_RGBA8P && (reinterpret_cast<uintptr_t>(raster) & 3))) {
+        return fail(c, FT_ERR_ARG, "device ops need 16-byte alignment, Rgba8p rasters 4-byte alignment");
+    }
+    st = run(c, stroke, rule, ops_d, &d, 1, fmt, ras_d, swd, swd + 1);
+    if (st != FT_OK) return st;
+    FT_CU(cudaMemcpyAsync(swd, swd + 1, sizeof(float), cudaMemcpyDeviceToDevice, c->stream), "pen width");
+    if (where == FT_HOST) {
+        if (raster_bytes)
+            FT_CU(cudaMemcpyAsync(raster, c->rasters.p, raster_bytes, cudaMemcpyDeviceToHost, c->stream),
+                  "download raster");
+        FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
+        int32_t s0 = 0;
+        FT_CU(cudaMemcpy(&s0, c->status.p, sizeof(int32_t), cudaMemcpyDeviceToHost), "status");
+        if (s0 != FT_OK) return fail(c, s0, s0 == FT_ERR_DEPTH ? "subdivision depth cap reached"
+                                                               : "non-finite curve control point or bad op");
+    }
+    return FT_OK;
+}
+
+}  // namespace
+
+
+struct ft_batch {
+    int stroke = 0, rule = 0, fmt = 0, smem = 0, grid = 0;
+    uint32_t n_paths = 0, n_items = 0;
+    uint64_t ops_needed = 0, bytes_needed = 0;
+    DevBuf paths, items, status, queue, scratch;
+    ftk::KParams params;
+    const void* g_ops = nullptr;
+    void* g_ras = nullptr;
+    cudaStream_t g_stream = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    void release() {
+        if (exec) cudaGraphExecDestroy(exec);
+        exec = nullptr;
+        paths.release();
+        items.release();
+        status.release();
+        queue.release();
+        scratch.release();
+    }
+};
+
+extern "C" {
+
+FT_API int ft_batch_create(ft_ctx* c, int32_t stroke, int32_t rule, const ft_path_desc* paths, uint32_t n_paths,
+                           int32_t fmt, ft_batch** out) {
+    if (!c || !out) return FT_ERR_ARG;
+    *out = nullptr;
+    if ((rule != FT_NONZERO && rule != FT_EVENODD) || (fmt != FT_MATTE8 && fmt != FT_RGBA8P))
+        return fail(c, FT_ERR_ARG, "bad rule or format");
+    if (stroke) return fail(c, FT_ERR_ARG, "stroke is not available in this build");
+    if (n_paths && !paths) return fail(c, FT_ERR_ARG, "null path list");
+    FT_CU(cudaSetDevice(c->device), "set device");
+    ft_batch* b = new ft_batch();
+    b->stroke = stroke;
+    b->rule = rule;
+    b->fmt = fmt;
+    b->n_paths = n_paths;
+    uint32_t max_w = 1;
+    const uint32_t bpp = fmt == FT_RGBA8P ? 4 : 1;
+    for (uint32_t i = 0; i < n_paths; i++) {
+        const ft_path_desc& d = paths[i];
+        int st = check_path(c, d, fmt, UINT64_MAX, UINT64_MAX);
+        if (st != FT_OK) {
+            delete b;
+            return st;
+        }
+        max_w = std::max(max_w, d.width);
+        b->ops_needed = std::max(b->ops_needed, (uint64_t)d.op_begin + d.n_ops);
+        if (d.width && d.height)
+            b->bytes_needed = std::max(b->bytes_needed, d.raster_offset + (uint64_t)(d.height - 1) * d.stride +
+                                                            (uint64_t)d.width * bpp);
+    }
+    b->smem = choose_smem(c, max_w);
+    std::vector<ftk::WorkItem> items;
+    plan_items(c, paths, n_paths, b->smem, items);
+    b->n_items = (uint32_t)items.size();
+    b->grid = grid_for(c, b->smem, b->n_items);
+    cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = b->paths.ensure(sizeof(ft_path_desc) * std::max(n_paths, 1u));
+    if (e == cudaSuccess) e = b->items.ensure(sizeof(ftk::WorkItem) * std::max(b->n_items, 1u));
+    if (e == cudaSuccess) e = b->status.ensure(sizeof(int32_t) * std::max(n_paths, 1u));
+    if (e == cudaSuccess) e = b->queue.ensure(256);
+    if (e == cudaSuccess) e = b->scratch.ensure(ftk::SCRATCH_BYTES_PER_CTA * (size_t)b->grid);
+    if (e == cudaSuccess && n_paths)
+        e = cudaMemcpyAsync(b->paths.p, paths, sizeof(ft_path_desc) * n_paths, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess && b->n_items)
+        e = cudaMemcpyAsync(b->items.p, items.data(), sizeof(ftk::WorkItem) * b->n_items, cudaMemcpyHostToDevice,
+                            c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        b->release();
+        delete b;
+        return cuda_fail(c, e, "batch setup");
+    }
+    fill_params(c, b->params, stroke, rule, fmt, b->smem);
+    b->params.paths = static_cast<const ft_path_desc*>(b->paths.p);
+    b->params.items = static_cast<const ftk::WorkItem*>(b->items.p);
+    b->params.n_items = b->n_items;
+    b->params.queue = static_cast<uint32_t*>(b->queue.p);
+    b->params.status = static_cast<int32_t*>(b->status.p);
+    b->params.scratch = static_cast<unsigned char*>(b->scratch.p);
+    ftk::raster_blocks_per_sm(b->smem);  // sets the kernel's shared-memory attribute outside capture
+    *out = b;
+    return FT_OK;
+}
+
+FT_API int ft_batch_launch(ft_ctx* c, ft_batch* b, const ft_op* ops, uint32_t n_ops_total, uint8_t* rasters,
+                           uint64_t raster_bytes) {
+    if (!c || !b) return FT_ERR_ARG;
+    if (n_ops_total < b->ops_needed || raster_bytes < b->bytes_needed)
+        return fail(c, FT_ERR_ARG, "ops or raster buffer smaller than the batch needs");
+    if ((reinterpret_cast<uintptr_t>(ops) & 15) || (b->fmt == FT_RGBA8P && (reinterpret_cast<uintptr_t>(rasters) & 3)))
+        return fail(c, FT_ERR_ARG, "device ops need 16-byte alignment, Rgba8p rasters 4-byte alignment");
+    FT_CU(cudaSetDevice(c->device), "set device");
+    if (!b->exec || b->g_ops != ops || b->g_ras != rasters || b->g_stream != c->stream) {
+        if (b->exec) cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+        b->params.ops = ops;
+        b->params.rasters = rasters;
+        cudaGraph_t g = nullptr;
+        FT_CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+        cudaError_t e1 = cudaMemsetAsync(b->queue.p, 0, 256, c->stream);
+        cudaError_t e2 = cudaMemsetAsync(b->status.p, 0, sizeof(int32_t) * std::max(b->n_paths, 1u), c->stream);
+        cudaError_t e3 = b->n_items ? ftk::launch_raster(b->params, b->grid, b->smem, c->stream) : cudaSuccess;
+        cudaError_t e4 = cudaStreamEndCapture(c->stream, &g);
+        if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess || e4 != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return cuda_fail(c, e1 != cudaSuccess ? e1 : e2 != cudaSuccess ? e2 : e3 != cudaSuccess ? e3 : e4,
+                             "capture batch graph");
+        }
+        cudaError_t e5 = cudaGraphInstantiate(&b->exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e5 != cudaSuccess) return cuda_fail(c, e5, "instantiate batch graph");
+        b->g_ops = ops;
+        b->g_ras = rasters;
+        b->g_stream = c->stream;
+    }
+    FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
+    FT_CU(cudaGraphLaunch(b->exec, c->stream), "launch batch graph");
+    FT_CU(cudaEventRecord(c->ev1, c->stream), "event");
+    c->timed = true;
+    if (b->n_items) c->launches++;
+    return FT_OK;
+}
+
+FT_API int ft_batch_launch_status(ft_ctx* c, ft_batch* b, int32_t* status, uint32_t n) {
+    if (!c || !b || (n && !status)) return FT_ERR_ARG;
+    FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
+    const uint32_t k = std::min(n, b->n_paths);
+    if (k) FT_CU(cudaMemcpy(status, b->status.p, sizeof(int32_t) * k, cudaMemcpyDeviceToHost), "status");
+    for (uint32_t i = k; i < n; i++) status[i] = FT_OK;
+    return FT_OK;
+}
+
+FT_API void ft_batch_destroy(ft_batch* b) {
+    if (!b) return;
+    b->release();
+    delete b;
+}
+
+
+FT_API int ft_ctx_create(int device, ft_ctx** out) {
+    if (!out) return FT_ERR_ARG;
+    *out = nullptr;
+    ft_ctx* c = new ft_ctx();
+    c->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (e != cudaSuccess) {
+        delete c;
+        return FT_ERR_CUDA;
+    }
+    c->own_stream = true;
+    c->max_smem = ftk::raster_max_smem();
+    *out = c;
+    return FT_OK;
+}
+
+FT_API void ft_ctx_destroy(ft_ctx* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    DevBuf* bufs[] = {&c->ops, &c->paths, &c->items, &c->status, &c->sw_out,
+                      &c->rasters, &c->queue, &c->scratch, &c->sw_chain};
+    for (DevBuf* b : bufs) b->release();
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+FT_API int ft_set_stream(ft_ctx* c, void* s) {
+    if (!c) return FT_ERR_ARG;
+    if (c->own_stream && c->stream) {
+        cudaStreamSynchronize(c->stream);
+        cudaStreamDestroy(c->stream);
+    }
+    c->stream = static_cast<cudaStream_t>(s);
+    c->own_stream = false;
+    return FT_OK;
+}
+
+FT_API int ft_set_tolerance(ft_ctx* c, float t) {
+    if (!c) return FT_ERR_ARG;
+    c->tolerance = std::max(t, 0.01f);
+    return FT_OK;
+}
+
+FT_API int ft_set_transform(ft_ctx* c, const float m[6]) {
+    if (!c || !m) return FT_ERR_ARG;
+    for (int i = 0; i < 6; i++) c->xf[i] = m[i];
+    return FT_OK;
+}
+
+FT_API int ft_set_join(ft_ctx* c, int32_t join, float miter_limit) {
+    if (!c || join < FT_JOIN_MITER || join > FT_JOIN_ROUND) return FT_ERR_ARG;
+    c->join = join;
+    c->miter_limit = miter_limit;
+    return FT_OK;
+}
+
+FT_API int ft_set_pen_width(ft_ctx* c, float w) {
+    if (!c) return FT_ERR_ARG;
+    c->s_width = w;
+    c->sw_on_device = false;
+    return FT_OK;
+}
+
+FT_API int ft_get_pen_width(ft_ctx* c, float* w) {
+    if (!c || !w) return FT_ERR_ARG;
+    if (c->sw_on_device && c->sw_chain.p) {
+        FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
+        FT_CU(cudaMemcpy(&c->s_width, c->sw_chain.p, sizeof(float), cudaMemcpyDeviceToHost), "pen width");
+    }
+    *w = c->s_width;
+    return FT_OK;
+}
+
+FT_API int ft_fill(ft_ctx* c, int32_t rule, const ft_op* ops, uint32_t n_ops, int32_t fmt, const uint8_t clr[4],
+                   uint8_t* raster, uint32_t w, uint32_t h, uint32_t stride, int32_t where) {
+    return single(c, 0, rule, ops, n_ops, fmt, clr, raster, w, h, stride, where);
+}
+
+FT_API int ft_stroke(ft_ctx* c, const ft_op* ops, uint32_t n_ops, int32_t fmt, const uint8_t clr[4],
+                     uint8_t* raster, uint32_t w, uint32_t h, uint32_t stride, int32_t where) {
+    return single(c, 1, FT_NONZERO, ops, n_ops, fmt, clr, raster, w, h, stride, where);
+}
+
+FT_API int ft_fill_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* ops, uint32_t n_ops_total,
+                         const ft_path_desc* paths, uint32_t n_paths, int32_t fmt, uint8_t* rasters,
+                         uint64_t raster_bytes, int32_t where) {
+    if (!c) return FT_ERR_ARG;
+    if ((rule != FT_NONZERO && rule != FT_EVENODD) || (fmt != FT_MATTE8 && fmt != FT_RGBA8P) ||
+        (where != FT_HOST && where != FT_DEVICE))
+        return fail(c, FT_ERR_ARG, "bad rule, format or location");
+    if (stroke) return fail(c, FT_ERR_ARG, "stroke is not available in this build");
+    if (n_paths && !paths) return fail(c, FT_ERR_ARG, "null path list");
+    FT_CU(cudaSetDevice(c->device), "set device");
+    for (uint32_t i = 0; i < n_paths; i++) {
+        int st = check_path(c, paths[i], fmt, raster_bytes, n_ops_total);
+        if (st != FT_OK) return st;
+    }
+    const ft_op* ops_d = ops;
+    uint8_t* ras_d = rasters;
+    if (where == FT_HOST) {
+        if (!valid_ops_host(ops, n_ops_total)) return fail(c, FT_ERR_ARG, "unknown path op kind");
+        FT_CU(c->ops.ensure(sizeof(ft_op) * std::max<uint64_t>(n_ops_total, 1)), "alloc ops");
+        FT_CU(c->rasters.ensure(std::max<uint64_t>(raster_bytes, 1)), "alloc rasters");
+        if (n_ops_total)
+            FT_CU(cudaMemcpyAsync(c->ops.p, ops, sizeof(ft_op) * n_ops_total, cudaMemcpyHostToDevice, c->stream),
+                  "upload ops");
+        if (raster_bytes)
+            FT_CU(cudaMemcpyAsync(c->rasters.p, rasters, raster_bytes, cudaMemcpyHostToDevice, c->stream),
+                  "upload rasters");
+        ops_d = static_cast<const ft_op*>(c->ops.p);
+        ras_d = static_cast<uint8_t*>(c->rasters.p);
+    } else if ((reinterpret_cast<uintptr_t>(ops) & 15) || (fmt == FT_RGBA8P && (reinterpret_cast<uintptr_t>(rasters) & 3))) {
+        return fail(c, FT_ERR_ARG, "device ops need 16-byte alignment, Rgba8p rasters 4-byte alignment");
+    }
+    int st = run(c, stroke, rule, ops_d, paths, n_paths, fmt, ras_d, nullptr, nullptr);
+    if (st != FT_OK) return st;
+    if (where == FT_HOST) {
+        if (raster_bytes)
+            FT_CU(cudaMemcpyAsync(rasters, c->rasters.p, raster_bytes, cudaMemcpyDeviceToHost, c->stream),
+                  "download rasters");
+        FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
+    }
+    return FT_OK;
+}
+
+FT_API int ft_batch_status(ft_ctx* c, int32_t* status, uint32_t n) {
+    if (!c || (n && !status)) return FT_ERR_ARG;
+    FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
+    const uint32_t k = std::min(n, c->last_n_paths);
+    if (k) FT_CU(cudaMemcpy(status, c->status.p, sizeof(int32_t) * k, cudaMemcpyDeviceToHost), "status");
+    for (uint32_t i = k; i < n; i++) status[i] = FT_OK;
+    return FT_OK;
+}
+
+FT_API int ft_sync(ft_ctx* c) {
+    if (!c) return FT_ERR_ARG;
+    FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
+    return FT_OK;
+}
+
+FT_API const char* ft_last_error(ft_ctx* c) {
+    if (!c) return "null context";
+    return c->err.c_str();
+}
+
+FT_API int ft_last_timings(ft_ctx* c, float* kernel_ms) {
+    if (!c || !kernel_ms) return FT_ERR_ARG;
+    *kernel_ms = 0.f;
+    if (!c->timed) return FT_OK;
+    FT_CU(cudaEventSynchronize(c->ev1), "event sync");
+    FT_CU(cudaEventElapsedTime(kernel_ms, c->ev0, c->ev1), "event time");
+    return FT_OK;
+}
+
+FT_API uint64_t ft_launch_count(ft_ctx* c) { return c ? c->launches : 0; }
+
+}  // extern "C"

@@ -1,0 +1,897 @@
+// ft_kernels.cu — the GB300 fill/stroke rasteriser (sm_103a).
+//
+// One persistent kernel drains a device queue of work items (a path and a range
+// of its raster rows).  For each item one CTA of 256 threads:
+//
+//  1. walks the path ops in chunks of 256 (footile plotter.rs:175-224): two block
+//     max-scans give every op its pen, pen width and "starts a new sub-figure"
+//     flag, so each thread then flattens its own op independently;
+//  2. flattens quads / cubics by recursive De Casteljau subdivision
+//     (plotter.rs:248-265, 311-332) with an explicit per-thread stack, IEEE f32
+//     without contraction, in the reference's depth-first leaf order: a count
+//     pass, a block scan, then an emit pass into a shared-memory window;
+//  3. builds the figure (fig.rs:428-461): warp 0 drops coincident vertices, pops
+//     a closing vertex equal to the sub-figure start and applies the 65,535-vertex
+//     cap, with ballots over 32 vertices at a time;
+//  4. finds the top vertex (min (y, x, id), the head of footile's stable (Y,X)
+//     sort, fig.rs:493-496) and the figure direction (fig.rs:402-411), and turns
+//     every non-horizontal segment into an edge (fig.rs:179-201) — each segment
+//     yields exactly the edge the active-edge sweep would add;
+//  5. rasterises bands of rows: every (edge, row) pair is independent (x at the
+//     bottom of row k is x_bot0 + k*inv_slope, wrapping), and its per-cell
+//     coverage (fig.rs:285-321) has a closed form, so threads take (edge, row)
+//     items and add signed cell areas into a shared-memory i32 band buffer with
+//     atomics.  i16 wrapping sums commute, so the i32 sums truncated to i16 equal
+//     footile's;
+//  6. resolves each band row with a warp scan (__shfl_up_sync) and the NonZero /
+//     EvenOdd rule (imgbuf.rs:38-199), then overwrites Matte8 rows or composites
+//     premultiplied RGBA with pix SrcOver (fig.rs:629-665).
+//
+// Rows footile writes: from max(top_row, 0) to the bottom of the raster, raster
+// row r receiving scan row r + min(top_row, 0) (fig.rs:496-499, 536-553).
+#include <cstdio>
+
+#include "ft_device.cuh"
+#include "ft_kernels.cuh"
+
+namespace ftk {
+
+constexpr unsigned FULL = 0xFFFFFFFFu;
+
+// ------------------------------------------------------------ block scans
+__device__ __forceinline__ int warp_incl_sum(int v) {
+    int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(FULL, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+__device__ __forceinline__ unsigned warp_incl_sum_u(unsigned v) {
+    int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned t = __shfl_up_sync(FULL, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+__device__ __forceinline__ int warp_incl_max(int v) {
+    int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(FULL, v, o);
+        if (lane >= o) v = max(v, t);
+    }
+    return v;
+}
+// Exclusive block sum; `total` receives the block total.  tmp: NWARP ints.
+__device__ int block_excl_sum(int v, int* tmp, int& total) {
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int inc = warp_incl_sum(v);
+    if (lane == 31) tmp[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        int t = lane < NWARP ? tmp[lane] : 0;
+        t = warp_incl_sum(t);
+        if (lane < NWARP) tmp[lane] = t;
+    }
+    __syncthreads();
+    int base = w > 0 ? tmp[w - 1] : 0;
+    total = tmp[NWARP - 1];
+    __syncthreads();
+    return base + inc - v;
+}
+// Inclusive block max.
+__device__ int block_incl_max(int v, int* tmp) {
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int inc = warp_incl_max(v);
+    if (lane == 31) tmp[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        int t = lane < NWARP ? tmp[lane] : -1;
+        t = warp_incl_max(t);
+        if (lane < NWARP) tmp[lane] = t;
+    }
+    __syncthreads();
+    int r = w > 0 ? max(inc, tmp[w - 1]) : inc;
+    __syncthreads();
+    return r;
+}
+// Inclusive and exclusive block max (identity -1) in one pass.
+__device__ void block_max_scan(int v, int* tmp, int& incl, int& excl) {
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int inc = warp_incl_max(v);
+    int wex = __shfl_up_sync(FULL, inc, 1);
+    if (lane == 0) wex = -1;
+    if (lane == 31) tmp[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        int t = lane < NWARP ? tmp[lane] : -1;
+        t = warp_incl_max(t);
+        if (lane < NWARP) tmp[lane] = t;
+    }
+    __syncthreads();
+    int carry = w > 0 ? tmp[w - 1] : -1;
+    incl = max(inc, carry);
+    excl = max(wex, carry);
+    __syncthreads();
+}
+
+// ------------------------------------------------- De Casteljau flattening
+// Walk the subdivision of a quad (plotter.rs:248-265) in depth-first order.
+// Leaves with index in [lo, hi) go to emit(index, point, width).  Returns the
+// number of leaves walked (the total when hi == INT_MAX).
+template <bool W, class Emit>
+__device__ int quad_walk(P2 a, P2 b, P2 c, float wa, float wb, float wc, float tol_sq, int lo, int hi,
+                         int* depth_hit, Emit emit) {
+    struct Fr {
+        P2 a, b, c;
+        float wa, wb, wc;
+        int d;
+    };
+    Fr st[FT_MAX_DEPTH + 1];
+    int sp = 0, leaf = 0, d = 0;
+    for (;;) {
+        P2 ab = pmid(a, b), bc = pmid(b, c), abbc = pmid(ab, bc), ac = pmid(a, c);
+        bool within = pdist_sq(abbc, ac) <= tol_sq;
+        if (within || d >= FT_MAX_DEPTH) {
+            if (!within) *depth_hit = 1;
+            if (leaf >= lo && leaf < hi) emit(leaf, c, wc);
+            leaf++;
+            if (leaf >= hi || sp == 0) break;
+            --sp;
+            a = st[sp].a;
+            b = st[sp].b;
+            c = st[sp].c;
+            if (W) {
+                wa = st[sp].wa;
+                wb = st[sp].wb;
+                wc = st[sp].wc;
+            }
+            d = st[sp].d;
+        } else {
+            float wab = 0, wbc = 0, wabbc = 0;
+            if (W) {
+                wab = fmid(wa, wb);
+                wbc = fmid(wb, wc);
+                wabbc = fmid(wab, wbc);
+            }
+            st[sp].a = abbc;
+            st[sp].b = bc;
+            st[sp].c = c;
+            if (W) {
+                st[sp].wa = wabbc;
+                st[sp].wb = wbc;
+                st[sp].wc = wc;
+            }
+            st[sp].d = d + 1;
+            sp++;
+            b = ab;
+            c = abbc;
+            if (W) {
+                wb = wab;
+                wc = wabbc;
+            }
+            d++;
+        }
+    }
+    return leaf;
+}
+
+// The same for a cubic (plotter.rs:311-332).
+template <bool W, class Emit>
+__device__ int cubic_walk(P2 a, P2 b, P2 c, P2 e, float wa, float wb, float wc, float we, float tol_sq, int lo,
+                          int hi, int* depth_hit, Emit emit) {
+    struct Fr {
+        P2 a, b, c, e;
+        float wa, wb, wc, we;
+        int d;
+    };
+    Fr st[FT_MAX_DEPTH + 1];
+    int sp = 0, leaf = 0, d = 0;
+    for (;;) {
+        P2 ab = pmid(a, b), bc = pmid(b, c), cd = pmid(c, e);
+        P2 abbc = pmid(ab, bc), bccd = pmid(bc, cd);
+        P2 pe = pmid(abbc, bccd);
+        P2 ad = pmid(a, e);
+        bool within = pdist_sq(pe, ad) <= tol_sq;
+        if (within || d >= FT_MAX_DEPTH) {
+            if (!within) *depth_hit = 1;
+            if (leaf >= lo && leaf < hi) emit(leaf, e, we);
+            leaf++;
+            if (leaf >= hi || sp == 0) break;
+            --sp;
+            a = st[sp].a;
+            b = st[sp].b;
+            c = st[sp].c;
+            e = st[sp].e;
+            if (W) {
+                wa = st[sp].wa;
+                wb = st[sp].wb;
+                wc = st[sp].wc;
+                we = st[sp].we;
+            }
+            d = st[sp].d;
+        } else {
+            float wab = 0, wbc = 0, wcd = 0, wabbc = 0, wbccd = 0, wpe = 0;
+            if (W) {
+                wab = fmid(wa, wb);
+                wbc = fmid(wb, wc);
+                wcd = fmid(wc, we);
+                wabbc = fmid(wab, wbc);
+                wbccd = fmid(wbc, wcd);
+                wpe = fmid(wabbc, wbccd);
+            }
+            st[sp].a = pe;
+            st[sp].b = bccd;
+            st[sp].c = cd;
+            st[sp].e = e;
+            if (W) {
+                st[sp].wa = wpe;
+                st[sp].wb = wbccd;
+                st[sp].wc = wcd;
+                st[sp].we = we;
+            }
+            st[sp].d = d + 1;
+            sp++;
+            b = ab;
+            c = abbc;
+            e = pe;
+            if (W) {
+                wb = wab;
+                wc = wabbc;
+                we = wpe;
+            }
+            d++;
+        }
+    }
+    return leaf;
+}
+
+// ------------------------------------------------------------- CTA state
+struct CState {
+    // path walk carried between op chunks
+    float pen_x, pen_y, pen_w, sw;
+    int last_pc_kind;  // kind of the last Move/Line/Quad/Cubic/Close op, -1 none
+    // figure builder
+    int count;
+    int has_prev, prev_x, prev_y;  // previous raw vertex
+    int rf_x, rf_y, rf_pos;        // first vertex of the current sub-figure and its id
+    int capped;
+    int flags;  // 1: depth cap reached, 2: bad argument
+    // figure summary
+    int top_row;
+    int dir;  // 0 forward, 1 reverse
+    int last_pw;
+};
+
+struct BuildSmem {
+    int kind[BLOCK];
+    float pwval[BLOCK];
+    float penx[BLOCK], peny[BLOCK], penw[BLOCK];
+    int scan[2 * NWARP + 2];
+    int2 raw[RAW_CAP];
+    unsigned char rs[RAW_CAP];
+};
+
+struct RasterSmem {
+    EdgeRec edges[BLOCK];
+    int ya[BLOCK];
+    int off[BLOCK + 1];
+    int scan[2 * NWARP + 2];
+};
+
+// ------------------------------------------------------------ figure builder
+// Sequential restatement of Fig::add_point / Fig::close (fig.rs:373-461) for one
+// group of raw vertices; used for the group in which the 65,535 cap is reached.
+__device__ void seq_group(CState& S, const int2* raw, const unsigned char* rsf, int n, int2* pts, int* ss) {
+    int count = S.count, has_prev = S.has_prev;
+    int px = S.prev_x, py = S.prev_y, rfx = S.rf_x, rfy = S.rf_y, rf_pos = S.rf_pos;
+    for (int l = 0; l < n; l++) {
+        int2 p = raw[l];
+        int rs = rsf[l];
+        // a close event precedes a vertex that starts a sub-figure: pop when the
+        // last vertex equals the sub-figure start (fig.rs:373-383)
+        if (rs && has_prev && rfx == px && rfy == py) count -= 1;
+        if (count >= PT_CAP) {
+            // add_point is ignored from here on (fig.rs:430).  The next close —
+            // an explicit one or the one Plotter::fill ends with — pops the last
+            // vertex if it equals the open sub-figure's start.
+            if (!rs && rfx == px && rfy == py) count -= 1;
+            S.capped = 1;
+            break;
+        }
+        if (rs) {
+            rfx = p.x;
+            rfy = p.y;
+            rf_pos = count;
+            pts[count] = p;
+            ss[count] = count;
+            count++;
+        } else if (p.x != px || p.y != py) {
+            pts[count] = p;
+            ss[count] = rf_pos;
+            count++;
+        }
+        px = p.x;
+        py = p.y;
+        has_prev = 1;
+    }
+    S.count = count;
+    S.has_prev = has_prev;
+    S.prev_x = px;
+    S.prev_y = py;
+    S.rf_x = rfx;
+    S.rf_y = rfy;
+    S.rf_pos = rf_pos;
+}
+
+// Warp 0: append one window of raw vertices to the figure.  A vertex is kept when
+// it starts a sub-figure or differs from the previous raw vertex; a sub-figure
+// whose last vertex equals its first loses that vertex when it is closed.
+__device__ void compact_window(CState& S, const int2* raw, const unsigned char* rsf, int m, int2* pts, int* ss) {
+    int lane = threadIdx.x & 31;
+    for (int base = 0; base < m; base += 32) {
+        int k = base + lane;
+        bool valid = k < m;
+        int2 p = valid ? raw[k] : make_int2(0, 0);
+        int rs = valid ? rsf[k] : 0;
+        int count = S.count, has_prev = S.has_prev;
+        int prevx = S.prev_x, prevy = S.prev_y;
+        int rfx0 = S.rf_x, rfy0 = S.rf_y, rf_pos0 = S.rf_pos;
+        unsigned vmask = __ballot_sync(FULL, valid);
+        unsigned RS = __ballot_sync(FULL, valid && rs);
+        // close of the run that ended with the previous group
+        int count_g = count;
+        if ((RS & 1u) && has_prev && rfx0 == prevx && rfy0 == prevy) count_g -= 1;
+        int qx = __shfl_up_sync(FULL, p.x, 1), qy = __shfl_up_sync(FULL, p.y, 1);
+        if (lane == 0) {
+            qx = prevx;
+            qy = prevy;
+        }
+        bool keep = valid && (rs || p.x != qx || p.y != qy);
+        unsigned K = __ballot_sync(FULL, keep);
+        unsigned E = (RS >> 1) & vmask;  // lane l ends its run when lane l+1 starts one
+        unsigned le = (lane == 31) ? FULL : ((2u << lane) - 1u);
+        unsigned rsl = RS & le;
+        int jf = rsl ? 31 - __clz(rsl) : -1;
+        int src = jf < 0 ? 0 : jf;
+        int rfx = __shfl_sync(FULL, p.x, src), rfy = __shfl_sync(FULL, p.y, src);
+        if (jf < 0) {
+            rfx = rfx0;
+            rfy = rfy0;
+        }
+        bool pop = ((E >> lane) & 1u) && p.x == rfx && p.y == rfy;
+        unsigned PM = __ballot_sync(FULL, pop);
+        unsigned below = (1u << lane) - 1u;
+        int pos = count_g + __popc(K & below) - __popc(PM & below);
+        unsigned capm = __ballot_sync(FULL, keep && pos >= PT_CAP);
+        if (capm) {
+            if (lane == 0) seq_group(S, raw + base, rsf + base, min(32, m - base), pts, ss);
+            __syncwarp();
+            return;
+        }
+        bool write = keep;
+        unsigned Ege = E & ~below;
+        if (keep && Ege) {
+            int e = __ffs(Ege) - 1;
+            if ((PM >> e) & 1u) {
+                unsigned upto_e = (e == 31) ? FULL : ((2u << e) - 1u);
+                if ((K & upto_e & ~le) == 0) write = false;  // the popped vertex
+            }
+        }
+        int posj = __shfl_sync(FULL, pos, src);
+        int ssv = jf < 0 ? rf_pos0 : posj;
+        if (write) {
+            pts[pos] = p;
+            ss[pos] = ssv;
+        }
+        int last = 31 - __clz(vmask);
+        int nprevx = __shfl_sync(FULL, p.x, last), nprevy = __shfl_sync(FULL, p.y, last);
+        int lrs = RS ? 31 - __clz(RS) : 0;
+        int nrfx = __shfl_sync(FULL, p.x, lrs), nrfy = __shfl_sync(FULL, p.y, lrs);
+        int nrfpos = __shfl_sync(FULL, pos, lrs);
+        __syncwarp();
+        if (lane == 0) {
+            S.count = count_g + __popc(K) - __popc(PM);
+            S.prev_x = nprevx;
+            S.prev_y = nprevy;
+            S.has_prev = 1;
+            if (RS) {
+                S.rf_x = nrfx;
+                S.rf_y = nrfy;
+                S.rf_pos = nrfpos;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Path walk + flattening + figure building for a fill (Plotter::fill, plotter.rs:339-350).
+// Leaves the figure in pts[0..S.count) / ss[].
+__device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, unsigned char* smem, CState& S,
+                           int2* pts, int* ss) {
+    BuildSmem& B = *reinterpret_cast<BuildSmem*>(smem);
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        S.pen_x = 0.f;
+        S.pen_y = 0.f;
+        S.pen_w = sw0;
+        S.sw = sw0;
+        S.last_pc_kind = -1;
+        S.count = 0;
+        S.has_prev = 0;
+        S.prev_x = S.prev_y = 0;
+        S.rf_x = S.rf_y = 0;
+        S.rf_pos = 0;
+        S.capped = 0;
+        S.flags = 0;
+    }
+    __syncthreads();
+    const ft_op* ops = P.ops + d.op_begin;
+    const int n_ops = (int)d.n_ops;
+    const float tol_sq = P.tol_sq;
+    for (int c0 = 0; c0 < n_ops; c0 += BLOCK) {
+        const int i = c0 + tid;
+        const bool valid = i < n_ops;
+        ft_op op;
+        if (valid) {
+            const int4* src = reinterpret_cast<const int4*>(ops + i);
+            int4 q0 = __ldg(src), q1 = __ldg(src + 1);
+            op.kind = q0.x;
+            op.v[0] = __int_as_float(q0.y);
+            op.v[1] = __int_as_float(q0.z);
+            op.v[2] = __int_as_float(q0.w);
+            op.v[3] = __int_as_float(q1.x);
+            op.v[4] = __int_as_float(q1.y);
+            op.v[5] = __int_as_float(q1.z);
+        } else {
+            op.kind = -1;
+            for (int j = 0; j < 6; j++) op.v[j] = 0.f;
+        }
+        int kind = op.kind;
+        if (kind < -1 || kind > FT_OP_PEN_WIDTH) {
+            atomicOr(&S.flags, 2);
+            kind = -1;
+        }
+        const bool isPW = kind == FT_OP_PEN_WIDTH;
+        const bool isPC = kind >= FT_OP_CLOSE && kind <= FT_OP_CUBIC;
+        B.kind[tid] = kind;
+        B.pwval[tid] = op.v[0];
+        // pen width in effect at this op (last PenWidth at or before it)
+        int lpw = block_incl_max(isPW ? tid : -1, B.scan);
+        const float sw_i = lpw >= 0 ? B.pwval[lpw] : S.sw;
+        if (isPC) {
+            float ex = 0.f, ey = 0.f;  // Close resets the pen to the origin (plotter.rs:200-203)
+            if (kind == FT_OP_MOVE || kind == FT_OP_LINE) {
+                ex = op.v[0];
+                ey = op.v[1];
+            } else if (kind == FT_OP_QUAD) {
+                ex = op.v[2];
+                ey = op.v[3];
+            } else if (kind == FT_OP_CUBIC) {
+                ex = op.v[4];
+                ey = op.v[5];
+            }
+            B.penx[tid] = ex;
+            B.peny[tid] = ey;
+            B.penw[tid] = sw_i;
+        }
+        // pen before this op = pen after the last Move/Line/Quad/Cubic/Close before it
+        int lpc_inc, lpc;
+        block_max_scan(isPC ? tid : -1, B.scan, lpc_inc, lpc);
+        float pen_x, pen_y, pen_w;
+        int prev_pc_kind;
+        if (lpc >= 0) {
+            pen_x = B.penx[lpc];
+            pen_y = B.peny[lpc];
+            pen_w = B.penw[lpc];
+            prev_pc_kind = B.kind[lpc];
+        } else {
+            pen_x = S.pen_x;
+            pen_y = S.pen_y;
+            pen_w = S.pen_w;
+            prev_pc_kind = S.last_pc_kind;
+        }
+        (void)pen_w;
+        // the first vertex of this op starts a sub-figure after a close event
+        const int rs = (kind == FT_OP_MOVE) || prev_pc_kind == FT_OP_CLOSE || prev_pc_kind == -1;
+
+        // ---- count the vertices this op adds
+        int n = 0;
+        int depth_hit = 0;
+        bool nonfinite = false;
+        P2 A = p2(0, 0), Bq = p2(0, 0), C = p2(0, 0), D = p2(0, 0);
+        if (kind == FT_OP_MOVE || kind == FT_OP_LINE) {
+            A = xform(P.xf, p2(op.v[0], op.v[1]));
+            n = 1;
+        } else if (kind == FT_OP_QUAD) {
+            A = xform(P.xf, p2(pen_x, pen_y));
+            Bq = xform(P.xf, p2(op.v[0], op.v[1]));
+            C = xform(P.xf, p2(op.v[2], op.v[3]));
+            if (!pfinite(A) || !pfinite(Bq) || !pfinite(C)) {
+                nonfinite = true;
+                n = 1;
+            } else {
+                n = quad_walk<false>(A, Bq, C, 0.f, 0.f, 0.f, tol_sq, 0, INT_MAX, &depth_hit,
+                                     [](int, P2, float) {});
+            }
+        } else if (kind == FT_OP_CUBIC) {
+            A = xform(P.xf, p2(pen_x, pen_y));
+            Bq = xform(P.xf, p2(op.v[0], op.v[1]));
+            C = xform(P.xf, p2(op.v[2], op.v[3]));
+            D = xform(P.xf, p2(op.v[4], op.v[5]));
+            if (!pfinite(A) || !pfinite(Bq) || !pfinite(C) || !pfinite(D)) {
+                nonfinite = true;
+                n = 1;
+            } else {
+                n = cubic_walk<false>(A, Bq, C, D, 0.f, 0.f, 0.f, 0.f, tol_sq, 0, INT_MAX, &depth_hit,
+                                      [](int, P2, float) {});
+            }
+        }
+        if (depth_hit) atomicOr(&S.flags, 1);
+        if (nonfinite) atomicOr(&S.flags, 2);
+        int total;
+        const int off = block_excl_sum(n, B.scan, total);
+        // carry the path-walk state to the next chunk (everyone has read S by now)
+        if (tid == BLOCK - 1) {
+            S.sw = sw_i;
+            int last_pc = isPC ? tid : lpc;
+            if (last_pc >= 0) {
+                S.pen_x = B.penx[last_pc];
+                S.pen_y = B.peny[last_pc];
+                S.pen_w = B.penw[last_pc];
+                S.last_pc_kind = B.kind[last_pc];
+            }
+        }
+        // ---- emit and compact window by window
+        for (int w0 = 0; w0 < total; w0 += RAW_CAP) {
+            const int w1 = min(w0 + RAW_CAP, total);
+            if (n > 0 && off < w1 && off + n > w0) {
+                const int lo = max(w0, off) - off, hi = min(w1, off + n) - off;
+                auto emit = [&](int k, P2 q, float) {
+                    int idx = off + k - w0;
+                    B.raw[idx] = make_int2(f2fx(q.x), f2fx(q.y));
+                    B.rs[idx] = (k == 0) ? (unsigned char)rs : (unsigned char)0;
+                };
+                if (kind == FT_OP_MOVE || kind == FT_OP_LINE) {
+                    emit(0, A, 0.f);
+                } else if (nonfinite) {
+                    emit(0, kind == FT_OP_QUAD ? C : D, 0.f);
+                } else if (kind == FT_OP_QUAD) {
+                    int dh = 0;
+                    quad_walk<false>(A, Bq, C, 0.f, 0.f, 0.f, tol_sq, lo, hi, &dh, emit);
+                } else {
+                    int dh = 0;
+                    cubic_walk<false>(A, Bq, C, D, 0.f, 0.f, 0.f, 0.f, tol_sq, lo, hi, &dh, emit);
+                }
+            }
+            __syncthreads();
+            if (tid < 32) compact_window(S, B.raw, B.rs, w1 - w0, pts, ss);
+            __syncthreads();
+            if (S.capped) break;
+        }
+        __syncthreads();
+        if (S.capped) break;
+    }
+    // Plotter::fill ends with fig.close() (plotter.rs:347)
+    if (tid == 0 && !S.capped && S.has_prev && S.rf_x == S.prev_x && S.rf_y == S.prev_y) S.count -= 1;
+    __syncthreads();
+}
+
+// Top vertex (min (y, x, id)) and figure direction (fig.rs:402-411, 493-496).
+__device__ void top_and_dir(CState& S, const int2* pts, const int* ss, int* tmp3) {
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int count = S.count;
+    int by = INT_MAX, bx = INT_MAX, bi = INT_MAX;
+    for (int i = tid; i < count; i += BLOCK) {
+        int2 p = pts[i];
+        if (p.y < by || (p.y == by && (p.x < bx || (p.x == bx && i < bi)))) {
+            by = p.y;
+            bx = p.x;
+            bi = i;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        int oy = __shfl_down_sync(FULL, by, o), ox = __shfl_down_sync(FULL, bx, o), oi = __shfl_down_sync(FULL, bi, o);
+        if (oy < by || (oy == by && (ox < bx || (ox == bx && oi < bi)))) {
+            by = oy;
+            bx = ox;
+            bi = oi;
+        }
+    }
+    if (lane == 0) {
+        tmp3[3 * w] = by;
+        tmp3[3 * w + 1] = bx;
+        tmp3[3 * w + 2] = bi;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        for (int k = 1; k < NWARP; k++) {
+            int oy = tmp3[3 * k], ox = tmp3[3 * k + 1], oi = tmp3[3 * k + 2];
+            if (oy < by || (oy == by && (ox < bx || (ox == bx && oi < bi)))) {
+                by = oy;
+                bx = ox;
+                bi = oi;
+            }
+        }
+        const int top = bi;
+        const int s = ss[top];
+        const int nf = (top + 1 < count && ss[top + 1] == s) ? top + 1 : s;
+        int nr;
+        if (top > s) {
+            nr = top - 1;
+        } else {
+            // last vertex of the sub-figure: ss[] is non-decreasing
+            int lo = top, hi = count - 1;
+            while (lo < hi) {
+                int mid = (lo + hi + 1) >> 1;
+                if (ss[mid] == s)
+                    lo = mid;
+                else
+                    hi = mid - 1;
+            }
+            nr = lo;
+        }
+        int2 p = pts[top], p0 = pts[nf], p1 = pts[nr];
+        int ax = wsub(p1.x, p.x), ay = wsub(p1.y, p.y);
+        int cx = wsub(p0.x, p.x), cy = wsub(p0.y, p.y);
+        // (p1 - p).widdershins(p0 - p) -> Forward   (fig.rs:116-119)
+        S.dir = (fxmul(ax, cy) > fxmul(cx, ay)) ? 0 : 1;
+        S.top_row = by >> 16;
+    }
+    __syncthreads();
+}
+
+// One edge per non-horizontal segment (fig.rs:179-201, 576-600).
+__device__ void build_edges(const CState& S, const int2* pts, const int* ss, EdgeRec* edges) {
+    const int count = S.count, figdir = S.dir;
+    for (int i = threadIdx.x; i < count; i += BLOCK) {
+        const int s = ss[i];
+        const int nx = (i + 1 < count && ss[i + 1] == s) ? i + 1 : s;
+        EdgeRec e;
+        e.ed = 0;
+        e.y_upper = e.y_lower = e.x_bot0 = e.inv_slope = e.step_pix = e.start_row = e.end_row = 0;
+        if (nx != i) {
+            int2 a = pts[i], b = pts[nx];
+            if (a.y != b.y) {
+                int2 up, lo;
+                int edir;
+                if (b.y > a.y) {
+                    up = a;
+                    lo = b;
+                    edir = 0;
+                } else {
+                    up = b;
+                    lo = a;
+                    edir = 1;
+                }
+                const int dx = wsub(lo.x, up.x), dy = wsub(lo.y, up.y);
+                const int step = dx != 0 ? min(fxabs(fxdiv(dy, dx)), FX_ONE) : 0;
+                const int inv = fxdiv(dx, dy);
+                const int ybot = wsub(fxfloor(wadd(up.y, FX_ONE)), up.y);
+                e.y_upper = up.y;
+                e.y_lower = lo.y;
+                e.x_bot0 = wadd(up.x, fxmul(inv, ybot));
+                e.inv_slope = inv;
+                e.step_pix = step;
+                e.ed = (edir == figdir) ? 1 : -1;
+                e.start_row = up.y >> 16;
+                e.end_row = lo.y >> 16;
+            }
+        }
+        edges[i] = e;
+    }
+}
+
+// Signed cell areas of one edge on one scan row (fig.rs:238-321), added into
+// `area` (the band row of width W).
+__device__ __forceinline__ void scan_item(const EdgeRec& E, int y, int* area, int W) {
+    const int k = y - E.start_row;
+    const int x_bot = wadd(E.x_bot0, wmul(k, E.inv_slope));
+    const bool st = (y == E.start_row), en = (y == E.end_row);
+    const int ccov = en ? pixel_cov(fxfract(E.y_lower)) : 256;
+    const int cov = st ? ccov - pixel_cov(fxfract(E.y_upper)) : ccov;
+    if (cov <= 0) return;
+    const int x0 = st ? wsub(x_bot, fxmul(E.inv_slope, wsub(FX_ONE, fxfract(E.y_upper)))) : wsub(x_bot, E.inv_slope);
+    const int x1 = en ? wsub(x_bot, fxmul(E.inv_slope, wsub(fxceil(E.y_lower), E.y_lower))) : x_bot;
+    const int mnx = min(x0, x1), mxx = max(x0, x1);
+    const int minp = mnx >> 16, maxp = mxx >> 16;
+    if (minp >= W) return;
+    const int full = cov << 8;
+    const int r = (minp == maxp) ? fxmul(wsub(FX_ONE, fxfract(fxavg(mxx, mnx))), full)
+                                 : fxmul(wsub(FX_ONE, fxfract(mnx)), FX_HALF);
+    const int first = E.step_pix > 0 ? fxmul(r, E.step_pix) : r;
+    const int step = E.step_pix > 0 ? E.step_pix : FX_ONE;
+    // x_pix(j) = min(pixel_cov(min(first + j*step, ONE)), cov) reaches cov at j = jend
+    const int thr = cov * 256 - 128;
+    const int jend = first >= thr ? 0 : (thr - first + step - 1) / step;
+    const int jlast = min(jend, W - 1 - minp);
+    const int ed = E.ed;
+    int j = 0, prevpix = 0;
+    if (minp < 0) {
+        // cells left of the raster all land in cell 0 (fig.rs:295)
+        const int jz = min(-minp, jlast);
+        const int v = jz >= jend ? cov : pixel_cov(first + jz * step);
+        if (v) atomicAdd(&area[0], ed * v);
+        prevpix = v;
+        j = jz + 1;
+    }
+    for (; j <= jlast; j++) {
+        const int v = j >= jend ? cov : pixel_cov(first + j * step);
+        const int p = v - prevpix;
+        prevpix = v;
+        if (p) atomicAdd(&area[minp + j], ed * p);
+    }
+}
+
+// Resolve one band row and write it (fig.rs:621-665, imgbuf.rs:38-199).
+__device__ __forceinline__ void resolve_row(const int* arow, int W, int Wp, uint8_t* drow, int rule, int fmt,
+                                            unsigned clr) {
+    const int lane = threadIdx.x & 31;
+    unsigned carry = 0;
+    for (int x0 = 0; x0 < W; x0 += 128) {
+        const int x = x0 + lane * 4;
+        int4 a = make_int4(0, 0, 0, 0);
+        if (x < Wp) a = *reinterpret_cast<const int4*>(arow + x);
+        const unsigned s0 = (unsigned)a.x;
+        const unsigned s1 = s0 + (unsigned)a.y;
+        const unsigned s2 = s1 + (unsigned)a.z;
+        const unsigned s3 = s2 + (unsigned)a.w;
+        const unsigned inc = warp_incl_sum_u(s3);
+        const unsigned ex = inc - s3 + carry;
+        carry += __shfl_sync(FULL, inc, 31);
+        const unsigned v0 = resolve_cov(s0 + ex, rule), v1 = resolve_cov(s1 + ex, rule);
+        const unsigned v2 = resolve_cov(s2 + ex, rule), v3 = resolve_cov(s3 + ex, rule);
+        if (x >= W) continue;
+        if (fmt == FT_MATTE8) {
+            uint8_t* dp = drow + x;
+            if (x + 3 < W && ((reinterpret_cast<uintptr_t>(dp) & 3) == 0)) {
+                *reinterpret_cast<unsigned*>(dp) = v0 | (v1 << 8) | (v2 << 16) | (v3 << 24);
+            } else {
+                dp[0] = (uint8_t)v0;
+                if (x + 1 < W) dp[1] = (uint8_t)v1;
+                if (x + 2 < W) dp[2] = (uint8_t)v2;
+                if (x + 3 < W) dp[3] = (uint8_t)v3;
+            }
+        } else {
+            unsigned* dp = reinterpret_cast<unsigned*>(drow) + x;
+            const unsigned vv[4] = {v0, v1, v2, v3};
+#pragma unroll
+            for (int c = 0; c < 4; c++)
+                if (x + c < W) dp[c] = srcover_rgba(dp[c], clr, vv[c]);
+        }
+    }
+}
+
+// Rasterise rows [lo, hi) of the built figure, `R` rows per band.
+__device__ void raster_rows(const KParams& P, const ft_path_desc& d, const CState& S, const EdgeRec* edges, int lo,
+                            int hi, int R, unsigned char* smem) {
+    RasterSmem& Rs = *reinterpret_cast<RasterSmem*>(smem);
+    int* area = reinterpret_cast<int*>(smem + ((sizeof(RasterSmem) + 15) & ~(size_t)15));
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int W = (int)d.width;
+    const int Wp = (W + 3) & ~3;
+    const int tmin = min(S.top_row, 0);
+    const int count = S.count;
+    const unsigned clr = (unsigned)d.clr[0] | ((unsigned)d.clr[1] << 8) | ((unsigned)d.clr[2] << 16) |
+                         ((unsigned)d.clr[3] << 24);
+    uint8_t* base = P.rasters + d.raster_offset;
+    for (int r0 = lo; r0 < hi; r0 += R) {
+        const int r1 = min(r0 + R, hi);
+        const int nr = r1 - r0;
+        int4* a4 = reinterpret_cast<int4*>(area);
+        for (int i = tid; i < nr * Wp / 4; i += BLOCK) a4[i] = make_int4(0, 0, 0, 0);
+        __syncthreads();
+        const int yb0 = r0 + tmin, yb1 = r1 + tmin;
+        for (int e0 = 0; e0 < count; e0 += BLOCK) {
+            const int e = e0 + tid;
+            int nrow = 0, ya = 0;
+            EdgeRec E;
+            E.ed = 0;
+            if (e < count) {
+                E = edges[e];
+                if (E.ed) {
+                    ya = max(E.start_row, yb0);
+                    const int yb = min(E.end_row, yb1 - 1);
+                    nrow = max(yb - ya + 1, 0);
+                }
+            }
+            Rs.edges[tid] = E;
+            Rs.ya[tid] = ya;
+            int tot;
+            const int o = block_excl_sum(nrow, Rs.scan, tot);
+            Rs.off[tid] = o;
+            __syncthreads();
+            for (int it = tid; it < tot; it += BLOCK) {
+                int lo_j = 0, hi_j = BLOCK - 1;
+                while (lo_j < hi_j) {
+                    int mid = (lo_j + hi_j + 1) >> 1;
+                    if (Rs.off[mid] <= it)
+                        lo_j = mid;
+                    else
+                        hi_j = mid - 1;
+                }
+                // skip edges with no rows in this band (equal offsets)
+                const EdgeRec& Ej = Rs.edges[lo_j];
+                const int y = Rs.ya[lo_j] + (it - Rs.off[lo_j]);
+                scan_item(Ej, y, area + (size_t)(y - yb0) * Wp, W);
+            }
+            __syncthreads();
+        }
+        for (int rr = r0 + warp; rr < r1; rr += NWARP)
+            resolve_row(area + (size_t)(rr - r0) * Wp, W, Wp, base + (size_t)rr * d.stride, P.rule, P.fmt, clr);
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(BLOCK) k_raster(KParams P) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ CState S;
+    __shared__ int s_item;
+    __shared__ int s_tmp3[3 * NWARP];
+    const int tid = threadIdx.x;
+    unsigned char* scr = P.scratch + (size_t)blockIdx.x * SCRATCH_BYTES_PER_CTA;
+    int2* pts = reinterpret_cast<int2*>(scr + SCR_PTS);
+    int* ss = reinterpret_cast<int*>(scr + SCR_SS);
+    EdgeRec* edges = reinterpret_cast<EdgeRec*>(scr + SCR_EDGES);
+    for (;;) {
+        if (tid == 0) s_item = (int)atomicAdd(P.queue, 1u);
+        __syncthreads();
+        const int it = s_item;
+        __syncthreads();
+        if (it >= (int)P.n_items) break;
+        const WorkItem wi = P.items[it];
+        const ft_path_desc d = P.paths[wi.path];
+        const float sw0 = P.sw_chain ? *P.sw_chain : d.s_width;
+        build_fill(P, d, sw0, smem, S, pts, ss);
+        if (S.count > 0) {
+            top_and_dir(S, pts, ss, s_tmp3);
+            build_edges(S, pts, ss, edges);
+            __syncthreads();
+            const int row_begin = max(S.top_row, 0);
+            const int lo = max((int)wi.row_begin, row_begin);
+            const int hi = min((int)wi.row_end, (int)d.height);
+            if (lo < hi && d.width > 0) raster_rows(P, d, S, edges, lo, hi, (int)wi.band_rows, smem);
+        }
+        // pen width after the call: the last PenWidth op of the path
+        if (P.sw_out && wi.row_begin == 0) {
+            int lp = -1;
+            for (int i = tid; i < (int)d.n_ops; i += BLOCK)
+                if (P.ops[d.op_begin + i].kind == FT_OP_PEN_WIDTH) lp = max(lp, i);
+            lp = block_incl_max(lp, reinterpret_cast<BuildSmem*>(smem)->scan);
+            if (tid == BLOCK - 1) P.sw_out[wi.path] = lp >= 0 ? P.ops[d.op_begin + lp].v[0] : sw0;
+        }
+        if (tid == 0 && S.flags) atomicMax(&P.status[wi.path], (S.flags & 1) ? FT_ERR_DEPTH : FT_ERR_ARG);
+        __syncthreads();
+    }
+}
+
+cudaError_t launch_raster(const KParams& p, int grid, int smem_bytes, cudaStream_t s) {
+    cudaError_t e = cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+    if (e != cudaSuccess) return e;
+    k_raster<<<grid, BLOCK, smem_bytes, s>>>(p);
+    return cudaGetLastError();
+}
+
+int raster_blocks_per_sm(int smem_bytes) {
+    cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_raster, BLOCK, smem_bytes) != cudaSuccess) return 1;
+    return n > 0 ? n : 1;
+}
+
+int raster_max_smem() {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa;
+    int stat = 0;
+    if (cudaFuncGetAttributes(&fa, k_raster) == cudaSuccess) stat = (int)fa.sharedSizeBytes;
+    return v - stat;
+}
+
+}  // namespace ftk

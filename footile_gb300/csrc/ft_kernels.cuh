@@ -1,0 +1,87 @@
+// ft_kernels.cuh — launch interface between the C ABI (ft_capi.cu) and the kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/footile_gpu.h"
+
+namespace ftk {
+
+constexpr int BLOCK = 256;                 // threads per CTA
+constexpr int NWARP = BLOCK / 32;
+constexpr int RAW_CAP = 2048;              // raw (pre-dedupe) vertices per compaction window
+constexpr int PT_CAP = FT_MAX_POINTS;      // vertices kept per figure (u16 vertex ids)
+constexpr int OUT_CAP = 2 * RAW_CAP;       // stroke outline points staged per window
+
+// One unit of the device work queue: rows [row_begin, row_end) of one path's
+// raster, rasterised `band_rows` rows at a time.
+struct WorkItem {
+    uint32_t path;
+    uint32_t row_begin;
+    uint32_t row_end;
+    uint32_t band_rows;
+};
+
+// One non-horizontal edge of a figure (footile fig.rs:47-66), 32 bytes.  `ed` is
+// +1 when the edge direction equals the figure direction, -1 otherwise, 0 for
+// "no edge" (horizontal or degenerate segment).
+struct EdgeRec {
+    int y_upper, y_lower, x_bot0, inv_slope;
+    int step_pix, ed, start_row, end_row;
+};
+
+// One stroke sub-path (stroker.rs:31-40).
+struct SubRec {
+    int start;   // first stroke point
+    int n;       // points
+    int joined;  // joined ends
+    int len;     // SubStroke::len() (u16 arithmetic)
+};
+
+// Per-CTA scratch in global memory, private to one resident CTA and reused for
+// every work item it takes (stays L2-resident for small figures).  Every array
+// starts on a 256-byte boundary.
+constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+constexpr size_t SCR_PTS = 0;                                                   // int2[PT_CAP] vertices
+constexpr size_t SCR_SS = align256(SCR_PTS + (size_t)PT_CAP * sizeof(int2));    // int[PT_CAP] sub-figure starts
+constexpr size_t SCR_EDGES = align256(SCR_SS + (size_t)PT_CAP * sizeof(int));   // EdgeRec[PT_CAP]
+constexpr size_t SCR_SPTS = align256(SCR_EDGES + (size_t)PT_CAP * sizeof(EdgeRec));  // float4[PT_CAP] stroke points
+constexpr size_t SCR_SUBS = align256(SCR_SPTS + (size_t)PT_CAP * sizeof(float4));    // SubRec[PT_CAP] sub-strokes
+constexpr size_t SCR_SOFF = align256(SCR_SUBS + (size_t)PT_CAP * sizeof(SubRec));    // int[2*PT_CAP+8] offsets
+constexpr size_t SCRATCH_BYTES_PER_CTA = align256(SCR_SOFF + (size_t)(2 * PT_CAP + 8) * sizeof(int));
+
+struct KParams {
+    const ft_op* ops;
+    const ft_path_desc* paths;
+    const WorkItem* items;
+    uint32_t n_items;
+    uint32_t* queue;         // [0]: next work item
+    uint8_t* rasters;
+    int32_t* status;         // per path, atomicMax of FT_ERR_* codes
+    float* sw_out;           // per path pen width after the call (nullable)
+    const float* sw_chain;   // nullable: initial pen width of every path
+    unsigned char* scratch;  // gridDim.x * SCRATCH_BYTES_PER_CTA bytes
+    float xf[6];
+    float tol_sq;
+    int join;
+    float miter_limit;
+    int rule;
+    int fmt;
+    int stroke;
+    int smem_bytes;
+};
+
+// Static shared memory of the kernel besides the dynamic area buffer.
+constexpr int RASTER_FIXED_SMEM = BLOCK * (int)sizeof(EdgeRec) + 3 * BLOCK * 4 + 256;
+
+// Launch the persistent rasteriser.  Returns the CUDA error of the launch.
+cudaError_t launch_raster(const KParams& p, int grid, int smem_bytes, cudaStream_t s);
+
+// Resident CTAs per SM for `smem_bytes` of dynamic shared memory.
+int raster_blocks_per_sm(int smem_bytes);
+
+// Maximum dynamic shared memory the kernel may be configured for.
+int raster_max_smem();
+
+}  // namespace ftk

@@ -1,0 +1,178 @@
+/*
+ * footile_gpu.h — C ABI of the GB300 (sm_103a) fill/stroke rasterisation path.
+ *
+ * This library replaces the body of footile's `Plotter::fill` / `Plotter::stroke`
+ * (src/plotter.rs:339-365) — path walk, De Casteljau flattening, stroking, the
+ * fixed-point `Fig` rasteriser and the 8-bit resolve/composite — with CUDA kernels.
+ * Results are bit-identical to the CPU algorithm (16.16 fixed point, release-mode
+ * wrapping arithmetic, IEEE f32 without contraction in the float stages).
+ *
+ * Plain C types only: pointers, sizes and small structs.  Every call returns an
+ * `int` status (FT_OK or an FT_ERR_* code); `ft_last_error` gives a message.
+ * The caller owns every buffer it passes; the library never frees them.
+ * One context per host thread; a context issues all work on one CUDA stream.
+ */
+#ifndef FOOTILE_GPU_H
+#define FOOTILE_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define FT_API __declspec(dllexport)
+#else
+#define FT_API __attribute__((visibility("default")))
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+enum {
+    FT_OK = 0,
+    FT_ERR_ARG = 1,      /* bad argument, or a curve with a non-finite control point */
+    FT_ERR_DEPTH = 2,    /* curve / arc subdivision reached FT_MAX_DEPTH levels       */
+    FT_ERR_CAP = 3,      /* a size limit of the library was exceeded                  */
+    FT_ERR_TIMEOUT = 4,  /* a bounded device wait gave up                             */
+    FT_ERR_CUDA = 5,     /* a CUDA runtime call failed                                */
+    FT_ERR_NOMEM = 6     /* device or pinned host allocation failed                   */
+};
+
+/* Maximum De Casteljau / round-join arc recursion depth.  footile recurses without
+ * a limit (README.md:32-33); deeper subdivisions are emitted as leaves and flagged. */
+#define FT_MAX_DEPTH 22
+
+/* Vertices kept per figure, from `Vid(u16)` (src/vid.rs:9-18, src/fig.rs:428-442). */
+#define FT_MAX_POINTS 65535
+
+/* Widest raster row the band rasteriser accepts (one row of i32 cell areas must fit
+ * in shared memory). */
+#define FT_MAX_WIDTH 16384
+
+/* ---- path operations: footile `PathOp` (src/path.rs:18-31) ------------- */
+enum {
+    FT_OP_CLOSE = 0,     /* PathOp::Close()                        */
+    FT_OP_MOVE = 1,      /* PathOp::Move(p)           v[0..2] = p  */
+    FT_OP_LINE = 2,      /* PathOp::Line(p)           v[0..2] = p  */
+    FT_OP_QUAD = 3,      /* PathOp::Quad(b, c)        v[0..4]      */
+    FT_OP_CUBIC = 4,     /* PathOp::Cubic(b, c, d)    v[0..6]      */
+    FT_OP_PEN_WIDTH = 5  /* PathOp::PenWidth(w)       v[0] = w     */
+};
+
+/* One path operation, 32 bytes.  Points are absolute (Path2D resolves relative
+ * coordinates while building, src/path.rs:80-86). */
+typedef struct ft_op {
+    int32_t kind;
+    float v[6];
+    int32_t reserved;
+} ft_op;
+
+/* ---- fill rules, joins, pixel formats -------------------------------- */
+enum { FT_NONZERO = 0, FT_EVENODD = 1 };                         /* FillRule, src/path.rs:8-14  */
+enum { FT_JOIN_MITER = 0, FT_JOIN_BEVEL = 1, FT_JOIN_ROUND = 2 }; /* JoinStyle, src/stroker.rs:13-20 */
+enum {
+    FT_MATTE8 = 0,  /* pix Matte8: 1 byte / pixel; fill overwrites rows (src/fig.rs:629-636) */
+    FT_RGBA8P = 1   /* pix Rgba8p: 4 bytes / pixel premultiplied; SrcOver (src/fig.rs:637-643) */
+};
+enum { FT_HOST = 0, FT_DEVICE = 1 };  /* where the ops / raster pointers live */
+
+/* One path of a batch.  Each path is an independent Plotter call onto its own
+ * raster (or region of one).  40 bytes. */
+typedef struct ft_path_desc {
+    uint32_t op_begin;       /* index of the first op of this path in `ops`          */
+    uint32_t n_ops;          /* number of ops                                          */
+    uint32_t width;          /* raster width in pixels                                 */
+    uint32_t height;         /* raster height in pixels                                */
+    uint64_t raster_offset;  /* byte offset of the raster in the raster buffer         */
+    uint32_t stride;         /* bytes per raster row                                   */
+    float s_width;           /* Plotter pen width when the call starts (plotter.rs:52) */
+    uint8_t clr[4];          /* fill colour (premultiplied Rgba8p); ignored for Matte8  */
+    uint32_t reserved;
+} ft_path_desc;
+
+typedef struct ft_ctx ft_ctx;
+
+/* ---- context (Plotter state: tolerance, transform, join, pen width) ---- */
+
+/* Plotter::new defaults (src/plotter.rs:96-115): tolerance 0.3, identity transform,
+ * JoinStyle::Miter(4.0), pen width 1.0. */
+FT_API int ft_ctx_create(int device, ft_ctx** out);
+FT_API void ft_ctx_destroy(ft_ctx* ctx);
+/* Issue work on `cuda_stream` (a cudaStream_t) instead of the context's own stream. */
+FT_API int ft_set_stream(ft_ctx* ctx, void* cuda_stream);
+/* Plotter::set_tolerance (src/plotter.rs:133-137): clamps to >= 0.01, stores t*t. */
+FT_API int ft_set_tolerance(ft_ctx* ctx, float t);
+/* Plotter::set_transform (src/plotter.rs:140-143): x' = m0*x + m1*y + m2,
+ * y' = m3*x + m4*y + m5. */
+FT_API int ft_set_transform(ft_ctx* ctx, const float m[6]);
+/* Plotter::set_join (src/plotter.rs:158-161). */
+FT_API int ft_set_join(ft_ctx* ctx, int32_t join, float miter_limit);
+/* Plotter::pen_width state (src/plotter.rs:151-153); PenWidth ops update it and it
+ * persists from call to call, as in footile. */
+FT_API int ft_set_pen_width(ft_ctx* ctx, float w);
+FT_API int ft_get_pen_width(ft_ctx* ctx, float* w);
+
+/* ---- single-path calls ------------------------------------------------ */
+
+/* Plotter::fill (src/plotter.rs:339-350).  `raster` is `h` rows of `stride` bytes in
+ * `fmt`; it is read and written in place.  `clr` is the premultiplied RGBA colour
+ * (ignored for FT_MATTE8, as footile ignores it, src/fig.rs:633).  With
+ * where == FT_HOST the call copies, runs and copies back before returning; with
+ * FT_DEVICE `ops` and `raster` are device pointers and the call is asynchronous on
+ * the context stream. */
+FT_API int ft_fill(ft_ctx* ctx, int32_t rule, const ft_op* ops, uint32_t n_ops,
+                   int32_t fmt, const uint8_t clr[4], uint8_t* raster, uint32_t w,
+                   uint32_t h, uint32_t stride, int32_t where);
+
+/* Plotter::stroke (src/plotter.rs:356-365): stroke outline, then NonZero fill. */
+FT_API int ft_stroke(ft_ctx* ctx, const ft_op* ops, uint32_t n_ops, int32_t fmt,
+                     const uint8_t clr[4], uint8_t* raster, uint32_t w, uint32_t h,
+                     uint32_t stride, int32_t where);
+
+/* ---- batches: many independent Plotter calls in one persistent launch ---- */
+
+/* Fill (stroke == 0) or stroke (stroke == 1) every path of `paths` onto its own
+ * raster region.  `ops` holds all ops (n_ops_total), `rasters` all rasters
+ * (raster_bytes).  `paths` is always a host array; `ops` / `rasters` live where
+ * `where` says.  The per-path status of the last batch is read with
+ * ft_batch_status.  The raster regions of the paths must not overlap. */
+FT_API int ft_fill_batch(ft_ctx* ctx, int32_t stroke, int32_t rule, const ft_op* ops,
+                         uint32_t n_ops_total, const ft_path_desc* paths,
+                         uint32_t n_paths, int32_t fmt, uint8_t* rasters,
+                         uint64_t raster_bytes, int32_t where);
+
+/* Prepared batches: the path descriptors and the planned work queue stay on the
+ * device, and each launch replays a captured CUDA graph (queue reset, status reset,
+ * persistent rasteriser).  `ops` / `rasters` given to ft_batch_launch are device
+ * pointers; the launch is asynchronous on the context stream.  A batch owns its
+ * scratch memory and may be launched any number of times. */
+typedef struct ft_batch ft_batch;
+FT_API int ft_batch_create(ft_ctx* ctx, int32_t stroke, int32_t rule, const ft_path_desc* paths,
+                           uint32_t n_paths, int32_t fmt, ft_batch** out);
+FT_API int ft_batch_launch(ft_ctx* ctx, ft_batch* batch, const ft_op* ops, uint32_t n_ops_total,
+                           uint8_t* rasters, uint64_t raster_bytes);
+/* Per-path status codes of the last launch of `batch` (synchronises). */
+FT_API int ft_batch_launch_status(ft_ctx* ctx, ft_batch* batch, int32_t* status, uint32_t n);
+FT_API void ft_batch_destroy(ft_batch* batch);
+
+/* Per-path status codes of the last batch (synchronises the context stream). */
+FT_API int ft_batch_status(ft_ctx* ctx, int32_t* status, uint32_t n);
+
+/* Wait for all work of the context. */
+FT_API int ft_sync(ft_ctx* ctx);
+
+/* Message for the last error of this context (static storage, never NULL). */
+FT_API const char* ft_last_error(ft_ctx* ctx);
+
+/* Device time in milliseconds of the last call's kernels (CUDA events). */
+FT_API int ft_last_timings(ft_ctx* ctx, float* kernel_ms);
+
+/* Number of kernel launches the library has issued since the context was created. */
+FT_API uint64_t ft_launch_count(ft_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FOOTILE_GPU_H */

@@ -1,0 +1,193 @@
+"""TEST INFRASTRUCTURE ONLY — ctypes wrapper of the CPU oracle (footile_oracle.cpp).
+
+The oracle is a sequential C++ restatement of footile's fill/stroke path.  Only
+tests/, __graft_entry__.smoke() and bench.py (cpu_baseline leg and the
+`--impl reference` arm) use it, as the checker / CPU baseline.  The shipped
+library (footile_gb300) never imports it.
+"""
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+from footile_gb300 import _abi
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_SO = os.path.join(_HERE, "_build", "libfootile_oracle.so")
+_lock = threading.Lock()
+_lib = None
+
+
+def build():
+    """Compile the oracle (g++, a few seconds)."""
+    subprocess.check_call(["make", "-s", "-C", _HERE])
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("tolerance", ctypes.c_float), ("transform", ctypes.c_float * 6),
+                ("join", ctypes.c_int32), ("miter_limit", ctypes.c_float)]
+
+
+def make_params(tolerance=0.3, transform=_abi.IDENTITY, join=_abi.JOIN_MITER, miter_limit=4.0):
+    p = Params()
+    p.tolerance = tolerance
+    for i in range(6):
+        p.transform[i] = transform[i]
+    p.join = join
+    p.miter_limit = miter_limit
+    return p
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            src = os.path.join(_HERE, "footile_oracle.cpp")
+            if not os.path.exists(_SO) or os.path.getmtime(_SO) < os.path.getmtime(src):
+                build()
+            L = ctypes.CDLL(_SO)
+            P = ctypes.c_void_p
+            i32, u32 = ctypes.c_int32, ctypes.c_uint32
+            L.orc_fill.argtypes = [i32, P, u32, i32, P, P, u32, u32, u32, ctypes.POINTER(Params),
+                                   ctypes.POINTER(ctypes.c_float)]
+            L.orc_fill.restype = ctypes.c_int
+            L.orc_stroke.argtypes = [P, u32, i32, P, P, u32, u32, u32, ctypes.POINTER(Params),
+                                     ctypes.POINTER(ctypes.c_float)]
+            L.orc_stroke.restype = ctypes.c_int
+            L.orc_stroke_outline.argtypes = [P, u32, ctypes.POINTER(Params), ctypes.c_float, P, u32]
+            L.orc_stroke_outline.restype = u32
+            L.orc_fig_points.argtypes = [P, u32, ctypes.POINTER(Params), P, u32]
+            L.orc_fig_points.restype = u32
+            L.orc_accumulate.argtypes = [i32, P, P, u32]
+            L.orc_accumulate.restype = None
+            L.orc_fx_from_f32.argtypes = [ctypes.c_float]
+            L.orc_fx_from_f32.restype = i32
+            L.orc_fx_from_int.argtypes = [i32]
+            L.orc_fx_from_int.restype = i32
+            L.orc_fx_to_f32.argtypes = [i32]
+            L.orc_fx_to_f32.restype = ctypes.c_float
+            L.orc_fx_to_int.argtypes = [i32]
+            L.orc_fx_to_int.restype = i32
+            L.orc_fx_op.argtypes = [i32, i32, i32]
+            L.orc_fx_op.restype = i32
+            L.orc_widdershins.argtypes = [i32, i32, i32, i32]
+            L.orc_widdershins.restype = i32
+            L.orc_atan2f.argtypes = [ctypes.c_float, ctypes.c_float]
+            L.orc_atan2f.restype = ctypes.c_float
+            L.orc_sinf.argtypes = [ctypes.c_float]
+            L.orc_sinf.restype = ctypes.c_float
+            L.orc_fill_batch.argtypes = [i32, i32, P, P, u32, i32, P, ctypes.POINTER(Params), P, i32]
+            L.orc_fill_batch.restype = ctypes.c_int
+            _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def _clr(clr):
+    return np.ascontiguousarray(np.asarray(clr if clr is not None else (0, 0, 0, 0), dtype=np.uint8))
+
+
+def fill(rule, ops, raster, fmt, clr=None, s_width=1.0, **params):
+    """Plotter::fill on `raster` (modified in place).  Returns (status, s_width)."""
+    ops = np.ascontiguousarray(ops, dtype=_abi.OP_DTYPE)
+    assert raster.flags.c_contiguous
+    h = raster.shape[0]
+    w = raster.shape[1]
+    stride = raster.strides[0]
+    c = _clr(clr)
+    sw = ctypes.c_float(s_width)
+    st = lib().orc_fill(rule, _ptr(ops), len(ops), fmt, _ptr(c), _ptr(raster), w, h, stride,
+                        ctypes.byref(make_params(**params)), ctypes.byref(sw))
+    return st, sw.value
+
+
+def stroke(ops, raster, fmt, clr=None, s_width=1.0, **params):
+    """Plotter::stroke on `raster` (modified in place).  Returns (status, s_width)."""
+    ops = np.ascontiguousarray(ops, dtype=_abi.OP_DTYPE)
+    h = raster.shape[0]
+    w = raster.shape[1]
+    stride = raster.strides[0]
+    c = _clr(clr)
+    sw = ctypes.c_float(s_width)
+    st = lib().orc_stroke(_ptr(ops), len(ops), fmt, _ptr(c), _ptr(raster), w, h, stride,
+                          ctypes.byref(make_params(**params)), ctypes.byref(sw))
+    return st, sw.value
+
+
+def stroke_outline(ops, s_width=1.0, **params):
+    ops = np.ascontiguousarray(ops, dtype=_abi.OP_DTYPE)
+    cap = 1 << 16
+    while True:
+        out = np.zeros(cap, dtype=_abi.OP_DTYPE)
+        n = lib().orc_stroke_outline(_ptr(ops), len(ops), ctypes.byref(make_params(**params)), s_width,
+                                     _ptr(out), cap)
+        if n <= cap:
+            return out[:n]
+        cap = n
+
+
+def fig_points(ops, **params):
+    """The Fixed (16.16) vertices footile's Fig holds after the path walk."""
+    ops = np.ascontiguousarray(ops, dtype=_abi.OP_DTYPE)
+    xy = np.zeros((_abi.MAX_POINTS, 2), dtype=np.int32)
+    n = lib().orc_fig_points(_ptr(ops), len(ops), ctypes.byref(make_params(**params)), _ptr(xy),
+                             _abi.MAX_POINTS)
+    return xy[:n].copy()
+
+
+def accumulate(rule, src):
+    """imgbuf accumulate_non_zero / accumulate_even_odd: returns (dst, src_after)."""
+    s = np.ascontiguousarray(np.array(src, dtype=np.int16))
+    d = np.zeros(len(s), dtype=np.uint8)
+    lib().orc_accumulate(rule, _ptr(s), _ptr(d), len(s))
+    return d, s
+
+
+def fill_batch(stroke, rule, ops, paths, fmt, rasters, n_threads=1, **params):
+    ops = np.ascontiguousarray(ops, dtype=_abi.OP_DTYPE)
+    paths = np.ascontiguousarray(paths, dtype=_abi.PATH_DTYPE)
+    status = np.zeros(len(paths), dtype=np.int32)
+    lib().orc_fill_batch(stroke, rule, _ptr(ops), _ptr(paths), len(paths), fmt, _ptr(rasters),
+                         ctypes.byref(make_params(**params)), _ptr(status), n_threads)
+    return status
+
+
+# Fixed (16.16) arithmetic of fixed.rs, for the known-answer tests
+FX_ADD, FX_SUB, FX_MUL, FX_DIV, FX_SHL, FX_SHR, FX_ABS, FX_FLOOR, FX_CEIL, FX_ROUND, FX_TRUNC, \
+    FX_FRACT, FX_AVG = range(13)
+
+
+def fx(v):
+    """Fixed::from(f32) for floats, Fixed::from(i32) for ints."""
+    if isinstance(v, (int, np.integer)):
+        return lib().orc_fx_from_int(int(v))
+    return lib().orc_fx_from_f32(float(v))
+
+
+def fx_op(op, a, b=0):
+    return lib().orc_fx_op(op, a, b)
+
+
+def fx_to_f32(v):
+    return lib().orc_fx_to_f32(v)
+
+
+def fx_to_int(v):
+    return lib().orc_fx_to_int(v)
+
+
+def widdershins(a, b):
+    return bool(lib().orc_widdershins(a[0], a[1], b[0], b[1]))
+
+
+def atan2f(y, x):
+    return lib().orc_atan2f(y, x)
+
+
+def sinf(x):
+    return lib().orc_sinf(x)
