@@ -209,7 +209,8 @@ def run_ours(args):
     px_total = int((paths["width"].astype(np.int64) * paths["height"]).sum())
     n_ops = len(ops)
     dev = torch.device("cuda", local)
-    stream = torch.cuda.current_stream(dev)
+    stream = torch.cuda.Stream(dev)  # a capturable stream for the batch's CUDA graph
+    torch.cuda.set_stream(stream)
     ctx = Context(local)
     ctx.set_stream(stream.cuda_stream)
     ops_d = torch.from_numpy(ops.view(np.uint8)).to(dev)

@@ -384,11 +384,24 @@ FT_API int ft_batch_launch(ft_ctx* c, ft_batch* b, const ft_op* ops, uint32_t n_
     if ((reinterpret_cast<uintptr_t>(ops) & 15) || (b->fmt == FT_RGBA8P && (reinterpret_cast<uintptr_t>(rasters) & 3)))
         return fail(c, FT_ERR_ARG, "device ops need 16-byte alignment, Rgba8p rasters 4-byte alignment");
     FT_CU(cudaSetDevice(c->device), "set device");
+    b->params.ops = ops;
+    b->params.rasters = rasters;
+    if (c->stream == nullptr || c->stream == cudaStreamLegacy || c->stream == cudaStreamPerThread) {
+        // the legacy and per-thread default streams cannot be captured: launch directly
+        FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
+        FT_CU(cudaMemsetAsync(b->queue.p, 0, 256, c->stream), "reset queue");
+        FT_CU(cudaMemsetAsync(b->status.p, 0, sizeof(int32_t) * std::max(b->n_paths, 1u), c->stream), "reset status");
+        if (b->n_items) {
+            FT_CU(ftk::launch_raster(b->params, b->grid, b->smem, c->stream), "launch rasteriser");
+            c->launches++;
+        }
+        FT_CU(cudaEventRecord(c->ev1, c->stream), "event");
+        c->timed = true;
+        return FT_OK;
+    }
     if (!b->exec || b->g_ops != ops || b->g_ras != rasters || b->g_stream != c->stream) {
         if (b->exec) cudaGraphExecDestroy(b->exec);
         b->exec = nullptr;
-        b->params.ops = ops;
-        b->params.rasters = rasters;
         cudaGraph_t g = nullptr;
         FT_CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
         cudaError_t e1 = cudaMemsetAsync(b->queue.p, 0, 256, c->stream);

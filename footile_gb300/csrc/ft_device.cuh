@@ -60,8 +60,9 @@ __device__ __forceinline__ P2 p2(float x, float y) { return P2{x, y}; }
 __device__ __forceinline__ P2 padd(P2 a, P2 b) { return p2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y)); }
 __device__ __forceinline__ P2 psub(P2 a, P2 b) { return p2(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y)); }
 __device__ __forceinline__ P2 pscale(P2 a, float s) { return p2(__fmul_rn(a.x, s), __fmul_rn(a.y, s)); }
-// Pt::midpoint: ((a + b) / 2)
-__device__ __forceinline__ float fmid(float a, float b) { return __fdiv_rn(__fadd_rn(a, b), 2.0f); }
+// Pt::midpoint, (a + b) / 2: halving is an exact power-of-two scaling, so the product with 0.5
+// rounds to the same bits as the IEEE quotient.
+__device__ __forceinline__ float fmid(float a, float b) { return __fmul_rn(__fadd_rn(a, b), 0.5f); }
 __device__ __forceinline__ P2 pmid(P2 a, P2 b) { return p2(fmid(a.x, b.x), fmid(a.y, b.y)); }
 // Pt::distance_sq
 __device__ __forceinline__ float pdist_sq(P2 a, P2 b) {

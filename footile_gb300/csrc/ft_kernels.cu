@@ -37,6 +37,8 @@
 namespace ftk {
 
 constexpr unsigned FULL = 0xFFFFFFFFu;
+constexpr int LEAF_CACHE = 16;  // curve leaves kept from the count pass
+constexpr bool BLOCK_COMPACT = true;  // figure building by the whole CTA (false: warp 0)
 
 // ------------------------------------------------------------ block scans
 __device__ __forceinline__ int warp_incl_sum(int v) {
@@ -276,12 +278,16 @@ struct BuildSmem {
     unsigned char rs[RAW_CAP];
 };
 
+constexpr int MAP_CAP = 4096;  // (edge, row) items mapped per round
+
 struct RasterSmem {
     EdgeRec edges[BLOCK];
     int ya[BLOCK];
     int off[BLOCK + 1];
     int scan[2 * NWARP + 2];
+    unsigned char map[MAP_CAP];  // item -> edge slot of the current chunk
 };
+static_assert(((sizeof(RasterSmem) + 15) & ~(size_t)15) <= (size_t)RASTER_FIXED_SMEM, "raster smem layout");
 
 // ------------------------------------------------------------ figure builder
 // Sequential restatement of Fig::add_point / Fig::close (fig.rs:373-461) for one
@@ -409,6 +415,117 @@ __device__ void compact_window(CState& S, const int2* raw, const unsigned char* 
     }
 }
 
+// Block-wide variant of compact_window: 256 raw vertices per step, one per thread.
+// Cross-lane questions (latest sub-figure start at or before a vertex, next kept
+// vertex, next run end) are answered from per-warp ballot masks in shared memory.
+struct CompactSmem {
+    unsigned rsm[NWARP], km[NWARP], em[NWARP], pm[NWARP];
+    int posv[BLOCK];
+    int scan[2 * NWARP + 2];
+};
+
+// first set bit of the block-wide mask at index >= i (block-local), or BLOCK
+__device__ __forceinline__ int mask_next(const unsigned* m, int i) {
+    int w = i >> 5;
+    unsigned bits = m[w] & (0xFFFFFFFFu << (i & 31));
+    while (!bits) {
+        if (++w >= NWARP) return BLOCK;
+        bits = m[w];
+    }
+    return (w << 5) + __ffs(bits) - 1;
+}
+// last set bit at index <= i (block-local), or -1
+__device__ __forceinline__ int mask_prev(const unsigned* m, int i) {
+    int w = i >> 5;
+    int sh = i & 31;
+    unsigned bits = m[w] & (sh == 31 ? 0xFFFFFFFFu : ((2u << sh) - 1u));
+    while (!bits) {
+        if (--w < 0) return -1;
+        bits = m[w];
+    }
+    return (w << 5) + 31 - __clz(bits);
+}
+
+__device__ void compact_window_block(CState& S, const int2* raw, const unsigned char* rsf, int m, int2* pts,
+                                     int* ss, CompactSmem& C) {
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    for (int base = 0; base < m; base += BLOCK) {
+        const int k = base + tid;
+        const bool valid = k < m;
+        const int2 p = valid ? raw[k] : make_int2(0, 0);
+        const int rs = valid ? rsf[k] : 0;
+        const int count0 = S.count, has_prev = S.has_prev;
+        const int prevx = S.prev_x, prevy = S.prev_y, rfx0 = S.rf_x, rfy0 = S.rf_y, rfpos0 = S.rf_pos;
+        const int nb = min(BLOCK, m - base);  // vertices in this step
+        // close of the run that ended with the previous step (pop if it returned to its start)
+        int count_b = count0;
+        if (rsf[base] && has_prev && rfx0 == prevx && rfy0 == prevy) count_b -= 1;
+        int2 q = make_int2(prevx, prevy);
+        if (tid > 0 && valid) q = raw[k - 1];
+        const bool keep = valid && (rs || p.x != q.x || p.y != q.y);
+        // runs ending at the step's last vertex are closed at the next step (as above)
+        const bool endk = valid && (tid + 1 < nb) && rsf[k + 1];
+        const unsigned RS = __ballot_sync(FULL, valid && rs), K = __ballot_sync(FULL, keep),
+                       E = __ballot_sync(FULL, endk);
+        if (lane == 0) {
+            C.rsm[w] = RS;
+            C.km[w] = K;
+            C.em[w] = E;
+        }
+        __syncthreads();
+        const int jf = mask_prev(C.rsm, tid);  // first vertex of this vertex's run, in this block
+        int rfx = rfx0, rfy = rfy0;
+        if (jf >= 0) {
+            const int2 f = raw[base + jf];
+            rfx = f.x;
+            rfy = f.y;
+        }
+        const bool pop = endk && p.x == rfx && p.y == rfy;
+        const unsigned PM = __ballot_sync(FULL, pop);
+        if (lane == 0) C.pm[w] = PM;
+        int tot;
+        const int ex = block_excl_sum((keep ? 1 : 0) - (pop ? 1 : 0), C.scan, tot);
+        const int pos = count_b + ex;
+        C.posv[tid] = pos;
+        const int capped = __syncthreads_or(keep && pos >= PT_CAP);
+        if (capped) {
+            if (tid == 0) seq_group(S, raw + base, rsf + base, nb, pts, ss);
+            __syncthreads();
+            return;
+        }
+        // a vertex disappears when it is the last kept one of a run that pops in this block
+        bool write = keep;
+        if (keep) {
+            const int e = mask_next(C.em, tid);
+            if (e < BLOCK && ((C.pm[e >> 5] >> (e & 31)) & 1u)) {
+                const int nk = tid < BLOCK - 1 ? mask_next(C.km, tid + 1) : BLOCK;
+                if (nk > e) write = false;
+            }
+        }
+        if (write) {
+            pts[pos] = p;
+            ss[pos] = jf >= 0 ? C.posv[jf] : rfpos0;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            const int n = nb;
+            S.count = count_b + tot;
+            const int2 l = raw[base + n - 1];
+            S.prev_x = l.x;
+            S.prev_y = l.y;
+            S.has_prev = 1;
+            const int lr = mask_prev(C.rsm, n - 1);
+            if (lr >= 0) {
+                const int2 f = raw[base + lr];
+                S.rf_x = f.x;
+                S.rf_y = f.y;
+                S.rf_pos = C.posv[lr];
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // Path walk + flattening + figure building for a fill (Plotter::fill, plotter.rs:339-350).
 // Leaves the figure in pts[0..S.count) / ss[].
 __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, unsigned char* smem, CState& S,
@@ -503,6 +620,10 @@ __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, u
         int n = 0;
         int depth_hit = 0;
         bool nonfinite = false;
+        int2 cache[LEAF_CACHE];  // leaves of the count pass, reused by the emit pass
+        auto keep_leaf = [&](int k, P2 q, float) {
+            if (k < LEAF_CACHE) cache[k] = make_int2(f2fx(q.x), f2fx(q.y));
+        };
         P2 A = p2(0, 0), Bq = p2(0, 0), C = p2(0, 0), D = p2(0, 0);
         if (kind == FT_OP_MOVE || kind == FT_OP_LINE) {
             A = xform(P.xf, p2(op.v[0], op.v[1]));
@@ -515,8 +636,7 @@ __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, u
                 nonfinite = true;
                 n = 1;
             } else {
-                n = quad_walk<false>(A, Bq, C, 0.f, 0.f, 0.f, tol_sq, 0, INT_MAX, &depth_hit,
-                                     [](int, P2, float) {});
+                n = quad_walk<false>(A, Bq, C, 0.f, 0.f, 0.f, tol_sq, 0, INT_MAX, &depth_hit, keep_leaf);
             }
         } else if (kind == FT_OP_CUBIC) {
             A = xform(P.xf, p2(pen_x, pen_y));
@@ -528,7 +648,7 @@ __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, u
                 n = 1;
             } else {
                 n = cubic_walk<false>(A, Bq, C, D, 0.f, 0.f, 0.f, 0.f, tol_sq, 0, INT_MAX, &depth_hit,
-                                      [](int, P2, float) {});
+                                      keep_leaf);
             }
         }
         if (depth_hit) atomicOr(&S.flags, 1);
@@ -560,6 +680,12 @@ __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, u
                     emit(0, A, 0.f);
                 } else if (nonfinite) {
                     emit(0, kind == FT_OP_QUAD ? C : D, 0.f);
+                } else if (n <= LEAF_CACHE) {
+                    for (int k = lo; k < hi; k++) {
+                        const int idx = off + k - w0;
+                        B.raw[idx] = cache[k];
+                        B.rs[idx] = (k == 0) ? (unsigned char)rs : (unsigned char)0;
+                    }
                 } else if (kind == FT_OP_QUAD) {
                     int dh = 0;
                     quad_walk<false>(A, Bq, C, 0.f, 0.f, 0.f, tol_sq, lo, hi, &dh, emit);
@@ -569,7 +695,12 @@ __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, u
                 }
             }
             __syncthreads();
-            if (tid < 32) compact_window(S, B.raw, B.rs, w1 - w0, pts, ss);
+            if (BLOCK_COMPACT) {
+                CompactSmem& Cs = *reinterpret_cast<CompactSmem*>(smem + ((sizeof(BuildSmem) + 15) & ~(size_t)15));
+                compact_window_block(S, B.raw, B.rs, w1 - w0, pts, ss, Cs);
+            } else if (tid < 32) {
+                compact_window(S, B.raw, B.rs, w1 - w0, pts, ss);
+            }
             __syncthreads();
             if (S.capped) break;
         }
@@ -706,25 +837,33 @@ __device__ __forceinline__ void scan_item(const EdgeRec& E, int y, int* area, in
                                  : fxmul(wsub(FX_ONE, fxfract(mnx)), FX_HALF);
     const int first = E.step_pix > 0 ? fxmul(r, E.step_pix) : r;
     const int step = E.step_pix > 0 ? E.step_pix : FX_ONE;
-    // x_pix(j) = min(pixel_cov(min(first + j*step, ONE)), cov) reaches cov at j = jend
-    const int thr = cov * 256 - 128;
-    const int jend = first >= thr ? 0 : (thr - first + step - 1) / step;
-    const int jlast = min(jend, W - 1 - minp);
     const int ed = E.ed;
-    int j = 0, prevpix = 0;
+    // fig.rs:292-301: x_cov runs first, first + step, ... capped at ONE; each cell
+    // gets the growth of min(pixel_cov(x_cov), cov) until it reaches cov
+    const int jmax = W - 1 - minp;  // the loop also stops at the raster's last cell
+    int j, prev, x_cov;
     if (minp < 0) {
-        // cells left of the raster all land in cell 0 (fig.rs:295)
-        const int jz = min(-minp, jlast);
-        const int v = jz >= jend ? cov : pixel_cov(first + jz * step);
-        if (v) atomicAdd(&area[0], ed * v);
-        prevpix = v;
-        j = jz + 1;
+        // cells left of the raster all land in cell 0 (fig.rs:295): their sum telescopes
+        j = -minp;
+        long long v = (long long)first + (long long)j * step;
+        x_cov = v > FX_ONE ? FX_ONE : (int)v;
+        prev = min(pixel_cov(x_cov), cov);
+        if (prev) atomicAdd(&area[0], ed * prev);
+        if (prev >= cov) return;
+        j++;
+        x_cov = min(x_cov + step, FX_ONE);
+    } else {
+        j = 0;
+        prev = 0;
+        x_cov = first;
     }
-    for (; j <= jlast; j++) {
-        const int v = j >= jend ? cov : pixel_cov(first + j * step);
-        const int p = v - prevpix;
-        prevpix = v;
+    for (; j <= jmax; j++) {
+        const int v = min(pixel_cov(x_cov), cov);
+        const int p = v - prev;
+        prev = v;
         if (p) atomicAdd(&area[minp + j], ed * p);
+        if (v >= cov) break;
+        x_cov = min(x_cov + step, FX_ONE);
     }
 }
 
@@ -805,22 +944,20 @@ __device__ void raster_rows(const KParams& P, const ft_path_desc& d, const CStat
             int tot;
             const int o = block_excl_sum(nrow, Rs.scan, tot);
             Rs.off[tid] = o;
-            __syncthreads();
-            for (int it = tid; it < tot; it += BLOCK) {
-                int lo_j = 0, hi_j = BLOCK - 1;
-                while (lo_j < hi_j) {
-                    int mid = (lo_j + hi_j + 1) >> 1;
-                    if (Rs.off[mid] <= it)
-                        lo_j = mid;
-                    else
-                        hi_j = mid - 1;
+            // spread the chunk's (edge, row) items over the threads: each edge writes
+            // its slot into a run of the item map, then every thread takes items
+            for (int m0 = 0; m0 < tot; m0 += MAP_CAP) {
+                const int ia = max(o, m0), ib = min(o + nrow, m0 + MAP_CAP);
+                for (int k = ia; k < ib; k++) Rs.map[k - m0] = (unsigned char)tid;
+                __syncthreads();
+                const int n = min(MAP_CAP, tot - m0);
+                for (int it = tid; it < n; it += BLOCK) {
+                    const int jj = Rs.map[it];
+                    const int y = Rs.ya[jj] + (m0 + it - Rs.off[jj]);
+                    scan_item(Rs.edges[jj], y, area + (size_t)(y - yb0) * Wp, W);
                 }
-                // skip edges with no rows in this band (equal offsets)
-                const EdgeRec& Ej = Rs.edges[lo_j];
-                const int y = Rs.ya[lo_j] + (it - Rs.off[lo_j]);
-                scan_item(Ej, y, area + (size_t)(y - yb0) * Wp, W);
+                __syncthreads();
             }
-            __syncthreads();
         }
         for (int rr = r0 + warp; rr < r1; rr += NWARP)
             resolve_row(area + (size_t)(rr - r0) * Wp, W, Wp, base + (size_t)rr * d.stride, P.rule, P.fmt, clr);

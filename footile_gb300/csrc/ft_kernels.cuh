@@ -73,7 +73,7 @@ struct KParams {
 };
 
 // Static shared memory of the kernel besides the dynamic area buffer.
-constexpr int RASTER_FIXED_SMEM = BLOCK * (int)sizeof(EdgeRec) + 3 * BLOCK * 4 + 256;
+constexpr int RASTER_FIXED_SMEM = BLOCK * (int)sizeof(EdgeRec) + 3 * BLOCK * 4 + 256 + 4096;
 
 // Launch the persistent rasteriser.  Returns the CUDA error of the launch.
 cudaError_t launch_raster(const KParams& p, int grid, int smem_bytes, cudaStream_t s);
