@@ -51,8 +51,8 @@ struct ft_ctx {
     float s_width = 1.0f;   // host copy, valid unless sw_on_device
     bool sw_on_device = false;
     // device buffers
-    DevBuf ops, paths, items, status, sw_out, rasters, queue, scratch, sw_chain;
-    std::vector<ftk::WorkItem> h_items;
+    DevBuf ops, paths, items, items_w, overflow, status, sw_out, rasters, queue, scratch, sw_chain;
+    std::vector<ftk::WorkItem> h_items, h_items_w;
     uint32_t last_n_paths = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool timed = false;
@@ -88,7 +88,7 @@ int choose_smem(const ft_ctx* c, uint32_t max_w) {
     if (env) {
         smem = atoi(env);
     } else if (wp <= 512) {
-        smem = 64 * 1024;
+        smem = 48 * 1024;  // four CTAs per SM
     } else {
         smem = ftk::RASTER_FIXED_SMEM + 16 * wp * 4;
     }
@@ -98,46 +98,54 @@ int choose_smem(const ft_ctx* c, uint32_t max_w) {
     return smem;
 }
 
-// Split each path into work items of whole bands (host side of the device queue).
-void plan_items(ft_ctx* c, const ft_path_desc* paths, uint32_t n_paths, int smem, std::vector<ftk::WorkItem>& out) {
+// Largest canvas side the warp rasteriser takes (FT_WARP_MAX_SIDE, 0 disables it).
+int warp_max_side() {
+    const char* env = getenv("FT_WARP_MAX_SIDE");
+    int v = env ? atoi(env) : ftk::WARP_MAX_SIDE;
+    return std::max(0, std::min(v, ftk::WARP_MAX_SIDE));
+}
+
+// Work items of the device queues: small paths go whole to the warp rasteriser,
+// large paths are split into row ranges of whole bands for the CTA rasteriser.
+// Both lists are ordered longest first.
+void plan_items(ft_ctx* c, const ft_path_desc* paths, uint32_t n_paths, int smem, std::vector<ftk::WorkItem>& out,
+                std::vector<ftk::WorkItem>& out_w) {
     out.clear();
-    out.reserve(n_paths);
+    out_w.clear();
     const int area_bytes = smem - ftk::RASTER_FIXED_SMEM;
-    std::vector<std::pair<uint64_t, uint32_t>> order;
     const char* env = getenv("FT_SPLIT_PX");
     const uint64_t split_px = env ? strtoull(env, nullptr, 10) : (uint64_t)(1u << 20);
+    const uint32_t wside = (uint32_t)warp_max_side();
     for (uint32_t i = 0; i < n_paths; i++) {
         const ft_path_desc& d = paths[i];
         const uint32_t wp = (d.width + 3) & ~3u;
         uint32_t R = wp ? (uint32_t)(area_bytes / (int)(wp * 4)) : 1;
         R = std::max(1u, std::min(R, std::max(d.height, 1u)));
+        if (d.width <= wside && d.height <= wside) {
+            out_w.push_back(ftk::WorkItem{i, 0, d.height, R});
+            continue;
+        }
         uint32_t rows_per_item = std::max(d.height, 1u);
         if ((uint64_t)d.width * d.height >= split_px && c->sm_count > 0) {
             uint32_t target = (d.height + (uint32_t)c->sm_count - 1) / (uint32_t)c->sm_count;
             rows_per_item = std::max(R, ((target + R - 1) / R) * R);
         }
-        for (uint32_t r = 0; r < std::max(d.height, 1u); r += rows_per_item) {
-            ftk::WorkItem w;
-            w.path = i;
-            w.row_begin = r;
-            w.row_end = std::min(d.height, r + rows_per_item);
-            w.band_rows = R;
-            out.push_back(w);
+        for (uint32_t r = 0; r < std::max(d.height, 1u); r += rows_per_item)
+            out.push_back(ftk::WorkItem{i, r, std::min(d.height, r + rows_per_item), R});
+    }
+    auto order = [&](std::vector<ftk::WorkItem>& v) {
+        std::vector<std::pair<uint64_t, uint32_t>> key(v.size());
+        for (size_t k = 0; k < v.size(); k++) {
+            const ft_path_desc& d = paths[v[k].path];
+            key[k] = {(uint64_t)d.n_ops * 64 + (uint64_t)d.width * (v[k].row_end - v[k].row_begin) / 8, (uint32_t)k};
         }
-    }
-    // longest items first: ops drive the build, pixels the bands
-    std::vector<uint64_t> cost(out.size());
-    for (size_t k = 0; k < out.size(); k++) {
-        const ft_path_desc& d = paths[out[k].path];
-        cost[k] = (uint64_t)d.n_ops * 64 + (uint64_t)d.width * (out[k].row_end - out[k].row_begin) / 8;
-    }
-    std::vector<uint32_t> idx(out.size());
-    for (size_t k = 0; k < idx.size(); k++) idx[k] = (uint32_t)k;
-    std::stable_sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) { return cost[a] > cost[b]; });
-    std::vector<ftk::WorkItem> sorted(out.size());
-    for (size_t k = 0; k < idx.size(); k++) sorted[k] = out[idx[k]];
-    out.swap(sorted);
-    (void)order;
+        std::stable_sort(key.begin(), key.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
+        std::vector<ftk::WorkItem> sorted(v.size());
+        for (size_t k = 0; k < v.size(); k++) sorted[k] = v[key[k].second];
+        v.swap(sorted);
+    };
+    order(out);
+    order(out_w);
 }
 
 int check_path(ft_ctx* c, const ft_path_desc& d, int fmt, uint64_t raster_bytes, uint64_t n_ops_total) {
@@ -175,35 +183,71 @@ int grid_for(ft_ctx* c, int smem, uint32_t n_items) {
     return std::max(1, std::min(grid, (int)std::max(n_items, 1u)));
 }
 
+// Grid of the warp rasteriser.
+int grid_for_warp(ft_ctx* c, uint32_t n_items_w) {
+    const int per_sm = ftk::raster_warp_blocks_per_sm();
+    const char* genv = getenv("FT_GRID");
+    int grid = genv ? atoi(genv) : c->sm_count * per_sm;
+    const int need = (int)((n_items_w + ftk::NWARP - 1) / ftk::NWARP);
+    return std::max(1, std::min(grid, std::max(need, 1)));
+}
+
+// Enqueue the two rasterisers for prepared parameters: warps for small paths,
+// then CTAs for large paths and for small ones a warp could not hold.
+cudaError_t enqueue(const ftk::KParams& p, int grid_b, int grid_w, int smem, cudaStream_t st, uint64_t* launches) {
+    cudaError_t e = cudaSuccess;
+    if (p.n_items_w) {
+        e = ftk::launch_raster_warp(p, grid_w, st);
+        if (e != cudaSuccess) return e;
+        (*launches)++;
+    }
+    if (p.n_items || p.n_items_w) {
+        e = ftk::launch_raster(p, grid_b, smem, st);
+        if (e == cudaSuccess) (*launches)++;
+    }
+    return e;
+}
+
 // Queue, statuses, launch.  `ops_d` / `rasters_d` are device pointers.
 int run(ft_ctx* c, int stroke, int rule, const ft_op* ops_d, const ft_path_desc* paths, uint32_t n_paths, int fmt,
         uint8_t* rasters_d, const float* sw_chain, float* sw_out) {
     uint32_t max_w = 1;
     for (uint32_t i = 0; i < n_paths; i++) max_w = std::max(max_w, paths[i].width);
     const int smem = choose_smem(c, max_w);
-    plan_items(c, paths, n_paths, smem, c->h_items);
-    const uint32_t n_items = (uint32_t)c->h_items.size();
+    plan_items(c, paths, n_paths, smem, c->h_items, c->h_items_w);
+    const uint32_t n_items = (uint32_t)c->h_items.size(), n_items_w = (uint32_t)c->h_items_w.size();
     FT_CU(c->paths.ensure(sizeof(ft_path_desc) * std::max(n_paths, 1u)), "alloc paths");
     FT_CU(c->items.ensure(sizeof(ftk::WorkItem) * std::max(n_items, 1u)), "alloc items");
+    FT_CU(c->items_w.ensure(sizeof(ftk::WorkItem) * std::max(n_items_w, 1u)), "alloc items");
+    FT_CU(c->overflow.ensure(sizeof(uint32_t) * std::max(n_items_w, 1u)), "alloc overflow list");
     FT_CU(c->status.ensure(sizeof(int32_t) * std::max(n_paths, 1u)), "alloc status");
     FT_CU(c->queue.ensure(256), "alloc queue");
-    const int grid = grid_for(c, smem, n_items);
-    FT_CU(c->scratch.ensure(ftk::SCRATCH_BYTES_PER_CTA * (size_t)grid), "alloc scratch");
+    const int grid = n_items_w ? std::max(grid_for(c, smem, n_items), c->sm_count) : grid_for(c, smem, n_items);
+    const int grid_w = grid_for_warp(c, n_items_w);
+    FT_CU(c->scratch.ensure(ftk::SCRATCH_BYTES_PER_CTA * (size_t)std::max(grid, grid_w)), "alloc scratch");
     FT_CU(cudaMemcpyAsync(c->paths.p, paths, sizeof(ft_path_desc) * n_paths, cudaMemcpyHostToDevice, c->stream),
           "upload paths");
-    FT_CU(cudaMemcpyAsync(c->items.p, c->h_items.data(), sizeof(ftk::WorkItem) * n_items, cudaMemcpyHostToDevice,
-                          c->stream),
-          "upload items");
+    if (n_items)
+        FT_CU(cudaMemcpyAsync(c->items.p, c->h_items.data(), sizeof(ftk::WorkItem) * n_items, cudaMemcpyHostToDevice,
+                              c->stream),
+              "upload items");
+    if (n_items_w)
+        FT_CU(cudaMemcpyAsync(c->items_w.p, c->h_items_w.data(), sizeof(ftk::WorkItem) * n_items_w,
+                              cudaMemcpyHostToDevice, c->stream),
+              "upload items");
     FT_CU(cudaMemsetAsync(c->queue.p, 0, 256, c->stream), "reset queue");
     FT_CU(cudaMemsetAsync(c->status.p, 0, sizeof(int32_t) * std::max(n_paths, 1u), c->stream), "reset status");
     c->last_n_paths = n_paths;
-    if (n_items == 0) return FT_OK;
+    if (n_items == 0 && n_items_w == 0) return FT_OK;
     ftk::KParams p;
     fill_params(c, p, stroke, rule, fmt, smem);
     p.ops = ops_d;
     p.paths = static_cast<const ft_path_desc*>(c->paths.p);
     p.items = static_cast<const ftk::WorkItem*>(c->items.p);
     p.n_items = n_items;
+    p.items_w = static_cast<const ftk::WorkItem*>(c->items_w.p);
+    p.n_items_w = n_items_w;
+    p.overflow = static_cast<uint32_t*>(c->overflow.p);
     p.queue = static_cast<uint32_t*>(c->queue.p);
     p.rasters = rasters_d;
     p.status = static_cast<int32_t*>(c->status.p);
@@ -211,8 +255,7 @@ int run(ft_ctx* c, int stroke, int rule, const ft_op* ops_d, const ft_path_desc*
     p.sw_chain = sw_chain;
     p.scratch = static_cast<unsigned char*>(c->scratch.p);
     FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
-    FT_CU(ftk::launch_raster(p, grid, smem, c->stream), "launch rasteriser");
-    c->launches++;
+    FT_CU(enqueue(p, grid, grid_w, smem, c->stream, &c->launches), "launch rasteriser");
     FT_CU(cudaEventRecord(c->ev1, c->stream), "event");
     c->timed = true;
     return FT_OK;
@@ -291,10 +334,10 @@ int single(ft_ctx* c, int stroke, int32_t rule, const ft_op* ops, uint32_t n_ops
 
 
 struct ft_batch {
-    int stroke = 0, rule = 0, fmt = 0, smem = 0, grid = 0;
-    uint32_t n_paths = 0, n_items = 0;
+    int stroke = 0, rule = 0, fmt = 0, smem = 0, grid = 0, grid_w = 0;
+    uint32_t n_paths = 0, n_items = 0, n_items_w = 0;
     uint64_t ops_needed = 0, bytes_needed = 0;
-    DevBuf paths, items, status, queue, scratch;
+    DevBuf paths, items, items_w, overflow, status, queue, scratch;
     ftk::KParams params;
     const void* g_ops = nullptr;
     void* g_ras = nullptr;
@@ -305,6 +348,8 @@ struct ft_batch {
         exec = nullptr;
         paths.release();
         items.release();
+        items_w.release();
+        overflow.release();
         status.release();
         queue.release();
         scratch.release();
@@ -343,21 +388,28 @@ FT_API int ft_batch_create(ft_ctx* c, int32_t stroke, int32_t rule, const ft_pat
                                                             (uint64_t)d.width * bpp);
     }
     b->smem = choose_smem(c, max_w);
-    std::vector<ftk::WorkItem> items;
-    plan_items(c, paths, n_paths, b->smem, items);
+    std::vector<ftk::WorkItem> items, items_w;
+    plan_items(c, paths, n_paths, b->smem, items, items_w);
     b->n_items = (uint32_t)items.size();
-    b->grid = grid_for(c, b->smem, b->n_items);
+    b->n_items_w = (uint32_t)items_w.size();
+    b->grid = b->n_items_w ? std::max(grid_for(c, b->smem, b->n_items), c->sm_count) : grid_for(c, b->smem, b->n_items);
+    b->grid_w = grid_for_warp(c, b->n_items_w);
     cudaError_t e = cudaSuccess;
     if (e == cudaSuccess) e = b->paths.ensure(sizeof(ft_path_desc) * std::max(n_paths, 1u));
     if (e == cudaSuccess) e = b->items.ensure(sizeof(ftk::WorkItem) * std::max(b->n_items, 1u));
+    if (e == cudaSuccess) e = b->items_w.ensure(sizeof(ftk::WorkItem) * std::max(b->n_items_w, 1u));
+    if (e == cudaSuccess) e = b->overflow.ensure(sizeof(uint32_t) * std::max(b->n_items_w, 1u));
     if (e == cudaSuccess) e = b->status.ensure(sizeof(int32_t) * std::max(n_paths, 1u));
     if (e == cudaSuccess) e = b->queue.ensure(256);
-    if (e == cudaSuccess) e = b->scratch.ensure(ftk::SCRATCH_BYTES_PER_CTA * (size_t)b->grid);
+    if (e == cudaSuccess) e = b->scratch.ensure(ftk::SCRATCH_BYTES_PER_CTA * (size_t)std::max(b->grid, b->grid_w));
     if (e == cudaSuccess && n_paths)
         e = cudaMemcpyAsync(b->paths.p, paths, sizeof(ft_path_desc) * n_paths, cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess && b->n_items)
         e = cudaMemcpyAsync(b->items.p, items.data(), sizeof(ftk::WorkItem) * b->n_items, cudaMemcpyHostToDevice,
                             c->stream);
+    if (e == cudaSuccess && b->n_items_w)
+        e = cudaMemcpyAsync(b->items_w.p, items_w.data(), sizeof(ftk::WorkItem) * b->n_items_w,
+                            cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) {
         b->release();
@@ -368,10 +420,14 @@ FT_API int ft_batch_create(ft_ctx* c, int32_t stroke, int32_t rule, const ft_pat
     b->params.paths = static_cast<const ft_path_desc*>(b->paths.p);
     b->params.items = static_cast<const ftk::WorkItem*>(b->items.p);
     b->params.n_items = b->n_items;
+    b->params.items_w = static_cast<const ftk::WorkItem*>(b->items_w.p);
+    b->params.n_items_w = b->n_items_w;
+    b->params.overflow = static_cast<uint32_t*>(b->overflow.p);
     b->params.queue = static_cast<uint32_t*>(b->queue.p);
     b->params.status = static_cast<int32_t*>(b->status.p);
     b->params.scratch = static_cast<unsigned char*>(b->scratch.p);
-    ftk::raster_blocks_per_sm(b->smem);  // sets the kernel's shared-memory attribute outside capture
+    ftk::raster_blocks_per_sm(b->smem);  // sets the kernels' shared-memory attributes outside capture
+    ftk::raster_warp_blocks_per_sm();
     *out = b;
     return FT_OK;
 }
@@ -391,10 +447,7 @@ FT_API int ft_batch_launch(ft_ctx* c, ft_batch* b, const ft_op* ops, uint32_t n_
         FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
         FT_CU(cudaMemsetAsync(b->queue.p, 0, 256, c->stream), "reset queue");
         FT_CU(cudaMemsetAsync(b->status.p, 0, sizeof(int32_t) * std::max(b->n_paths, 1u), c->stream), "reset status");
-        if (b->n_items) {
-            FT_CU(ftk::launch_raster(b->params, b->grid, b->smem, c->stream), "launch rasteriser");
-            c->launches++;
-        }
+        FT_CU(enqueue(b->params, b->grid, b->grid_w, b->smem, c->stream, &c->launches), "launch rasteriser");
         FT_CU(cudaEventRecord(c->ev1, c->stream), "event");
         c->timed = true;
         return FT_OK;
@@ -406,7 +459,8 @@ FT_API int ft_batch_launch(ft_ctx* c, ft_batch* b, const ft_op* ops, uint32_t n_
         FT_CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
         cudaError_t e1 = cudaMemsetAsync(b->queue.p, 0, 256, c->stream);
         cudaError_t e2 = cudaMemsetAsync(b->status.p, 0, sizeof(int32_t) * std::max(b->n_paths, 1u), c->stream);
-        cudaError_t e3 = b->n_items ? ftk::launch_raster(b->params, b->grid, b->smem, c->stream) : cudaSuccess;
+        uint64_t nl = 0;
+        cudaError_t e3 = enqueue(b->params, b->grid, b->grid_w, b->smem, c->stream, &nl);
         cudaError_t e4 = cudaStreamEndCapture(c->stream, &g);
         if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess || e4 != cudaSuccess) {
             if (g) cudaGraphDestroy(g);
@@ -424,7 +478,7 @@ FT_API int ft_batch_launch(ft_ctx* c, ft_batch* b, const ft_op* ops, uint32_t n_
     FT_CU(cudaGraphLaunch(b->exec, c->stream), "launch batch graph");
     FT_CU(cudaEventRecord(c->ev1, c->stream), "event");
     c->timed = true;
-    if (b->n_items) c->launches++;
+    c->launches += (b->n_items_w ? 1 : 0) + ((b->n_items || b->n_items_w) ? 1 : 0);
     return FT_OK;
 }
 
@@ -468,8 +522,8 @@ FT_API void ft_ctx_destroy(ft_ctx* c) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
-    DevBuf* bufs[] = {&c->ops, &c->paths, &c->items, &c->status, &c->sw_out,
-                      &c->rasters, &c->queue, &c->scratch, &c->sw_chain};
+    DevBuf* bufs[] = {&c->ops,     &c->paths,   &c->items, &c->items_w, &c->overflow, &c->status,
+                      &c->sw_out, &c->rasters, &c->queue, &c->scratch, &c->sw_chain};
     for (DevBuf* b : bufs) b->release();
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);

@@ -121,6 +121,40 @@ __device__ void block_max_scan(int v, int* tmp, int& incl, int& excl) {
     __syncthreads();
 }
 
+// Thread-group policies: the figure builder runs either on a whole CTA (large
+// paths) or on one warp (small paths, many per CTA, no block barriers).
+struct BlockG {
+    static constexpr int N = BLOCK;
+    static constexpr int RAW = RAW_CAP;
+    __device__ static int rank() { return threadIdx.x; }
+    __device__ static void sync() { __syncthreads(); }
+    __device__ static int excl_sum(int v, int* tmp, int& total) { return block_excl_sum(v, tmp, total); }
+    __device__ static int incl_max(int v, int* tmp) { return block_incl_max(v, tmp); }
+    __device__ static void max_scan(int v, int* tmp, int& incl, int& excl) { block_max_scan(v, tmp, incl, excl); }
+};
+struct WarpG {
+    static constexpr int N = 32;
+    static constexpr int RAW = 256;
+    __device__ static int rank() { return threadIdx.x & 31; }
+    __device__ static void sync() { __syncwarp(); }
+    __device__ static int excl_sum(int v, int*, int& total) {
+        __syncwarp();
+        const int inc = warp_incl_sum(v);
+        total = __shfl_sync(FULL, inc, 31);
+        return inc - v;
+    }
+    __device__ static int incl_max(int v, int*) {
+        __syncwarp();
+        return warp_incl_max(v);
+    }
+    __device__ static void max_scan(int v, int*, int& incl, int& excl) {
+        __syncwarp();
+        incl = warp_incl_max(v);
+        excl = __shfl_up_sync(FULL, incl, 1);
+        if ((threadIdx.x & 31) == 0) excl = -1;
+    }
+};
+
 // ------------------------------------------------- De Casteljau flattening
 // Walk the subdivision of a quad (plotter.rs:248-265) in depth-first order.
 // Leaves with index in [lo, hi) go to emit(index, point, width).  Returns the
@@ -262,21 +296,25 @@ struct CState {
     int has_prev, prev_x, prev_y;  // previous raw vertex
     int rf_x, rf_y, rf_pos;        // first vertex of the current sub-figure and its id
     int capped;
-    int flags;  // 1: depth cap reached, 2: bad argument
+    int overflow;  // the figure outgrew the warp's scratch: hand the path to a CTA
+    int flags;     // 1: depth cap reached, 2: bad argument
     // figure summary
     int top_row;
     int dir;  // 0 forward, 1 reverse
     int last_pw;
 };
 
-struct BuildSmem {
-    int kind[BLOCK];
-    float pwval[BLOCK];
-    float penx[BLOCK], peny[BLOCK], penw[BLOCK];
+template <int N, int RAW>
+struct BuildSmemT {
+    int kind[N];
+    float pwval[N];
+    float penx[N], peny[N], penw[N];
     int scan[2 * NWARP + 2];
-    int2 raw[RAW_CAP];
-    unsigned char rs[RAW_CAP];
+    int2 raw[RAW];
+    unsigned char rs[RAW];
 };
+using BuildSmem = BuildSmemT<BLOCK, RAW_CAP>;
+using WarpBuildSmem = BuildSmemT<32, 256>;
 
 constexpr int MAP_CAP = 4096;  // (edge, row) items mapped per round
 
@@ -337,7 +375,8 @@ __device__ void seq_group(CState& S, const int2* raw, const unsigned char* rsf, 
 // Warp 0: append one window of raw vertices to the figure.  A vertex is kept when
 // it starts a sub-figure or differs from the previous raw vertex; a sub-figure
 // whose last vertex equals its first loses that vertex when it is closed.
-__device__ void compact_window(CState& S, const int2* raw, const unsigned char* rsf, int m, int2* pts, int* ss) {
+__device__ void compact_window(CState& S, const int2* raw, const unsigned char* rsf, int m, int2* pts, int* ss,
+                               int limit) {
     int lane = threadIdx.x & 31;
     for (int base = 0; base < m; base += 32) {
         int k = base + lane;
@@ -373,6 +412,12 @@ __device__ void compact_window(CState& S, const int2* raw, const unsigned char* 
         unsigned PM = __ballot_sync(FULL, pop);
         unsigned below = (1u << lane) - 1u;
         int pos = count_g + __popc(K & below) - __popc(PM & below);
+        if (__any_sync(FULL, keep && pos >= limit)) {
+            // more vertices than this warp's scratch holds
+            if (lane == 0) S.overflow = 1;
+            __syncwarp();
+            return;
+        }
         unsigned capm = __ballot_sync(FULL, keep && pos >= PT_CAP);
         if (capm) {
             if (lane == 0) seq_group(S, raw + base, rsf + base, min(32, m - base), pts, ss);
@@ -526,12 +571,14 @@ __device__ void compact_window_block(CState& S, const int2* raw, const unsigned 
     }
 }
 
-// Path walk + flattening + figure building for a fill (Plotter::fill, plotter.rs:339-350).
-// Leaves the figure in pts[0..S.count) / ss[].
-__device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, unsigned char* smem, CState& S,
-                           int2* pts, int* ss) {
-    BuildSmem& B = *reinterpret_cast<BuildSmem*>(smem);
-    const int tid = threadIdx.x;
+// Path walk + flattening + figure building for a fill (Plotter::fill, plotter.rs:339-350),
+// by the thread group G.  Leaves the figure in pts[0..S.count) / ss[].  `limit` is
+// the vertex capacity of pts/ss (a warp stops with S.overflow set beyond it).
+template <class G>
+__device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, BuildSmemT<G::N, G::RAW>& B,
+                           CompactSmem* Cs, CState& S, int2* pts, int* ss, int limit) {
+    constexpr int N = G::N;
+    const int tid = G::rank();
     if (tid == 0) {
         S.pen_x = 0.f;
         S.pen_y = 0.f;
@@ -544,13 +591,14 @@ __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, u
         S.rf_x = S.rf_y = 0;
         S.rf_pos = 0;
         S.capped = 0;
+        S.overflow = 0;
         S.flags = 0;
     }
-    __syncthreads();
+    G::sync();
     const ft_op* ops = P.ops + d.op_begin;
     const int n_ops = (int)d.n_ops;
     const float tol_sq = P.tol_sq;
-    for (int c0 = 0; c0 < n_ops; c0 += BLOCK) {
+    for (int c0 = 0; c0 < n_ops; c0 += N) {
         const int i = c0 + tid;
         const bool valid = i < n_ops;
         ft_op op;
@@ -578,7 +626,8 @@ __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, u
         B.kind[tid] = kind;
         B.pwval[tid] = op.v[0];
         // pen width in effect at this op (last PenWidth at or before it)
-        int lpw = block_incl_max(isPW ? tid : -1, B.scan);
+        const int lpw = G::incl_max(isPW ? tid : -1, B.scan);
+        G::sync();
         const float sw_i = lpw >= 0 ? B.pwval[lpw] : S.sw;
         if (isPC) {
             float ex = 0.f, ey = 0.f;  // Close resets the pen to the origin (plotter.rs:200-203)
@@ -598,21 +647,19 @@ __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, u
         }
         // pen before this op = pen after the last Move/Line/Quad/Cubic/Close before it
         int lpc_inc, lpc;
-        block_max_scan(isPC ? tid : -1, B.scan, lpc_inc, lpc);
-        float pen_x, pen_y, pen_w;
+        G::max_scan(isPC ? tid : -1, B.scan, lpc_inc, lpc);
+        G::sync();
+        float pen_x, pen_y;
         int prev_pc_kind;
         if (lpc >= 0) {
             pen_x = B.penx[lpc];
             pen_y = B.peny[lpc];
-            pen_w = B.penw[lpc];
             prev_pc_kind = B.kind[lpc];
         } else {
             pen_x = S.pen_x;
             pen_y = S.pen_y;
-            pen_w = S.pen_w;
             prev_pc_kind = S.last_pc_kind;
         }
-        (void)pen_w;
         // the first vertex of this op starts a sub-figure after a close event
         const int rs = (kind == FT_OP_MOVE) || prev_pc_kind == FT_OP_CLOSE || prev_pc_kind == -1;
 
@@ -654,9 +701,9 @@ __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, u
         if (depth_hit) atomicOr(&S.flags, 1);
         if (nonfinite) atomicOr(&S.flags, 2);
         int total;
-        const int off = block_excl_sum(n, B.scan, total);
+        const int off = G::excl_sum(n, B.scan, total);
         // carry the path-walk state to the next chunk (everyone has read S by now)
-        if (tid == BLOCK - 1) {
+        if (tid == N - 1) {
             S.sw = sw_i;
             int last_pc = isPC ? tid : lpc;
             if (last_pc >= 0) {
@@ -667,8 +714,8 @@ __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, u
             }
         }
         // ---- emit and compact window by window
-        for (int w0 = 0; w0 < total; w0 += RAW_CAP) {
-            const int w1 = min(w0 + RAW_CAP, total);
+        for (int w0 = 0; w0 < total; w0 += G::RAW) {
+            const int w1 = min(w0 + G::RAW, total);
             if (n > 0 && off < w1 && off + n > w0) {
                 const int lo = max(w0, off) - off, hi = min(w1, off + n) - off;
                 auto emit = [&](int k, P2 q, float) {
@@ -694,30 +741,33 @@ __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, u
                     cubic_walk<false>(A, Bq, C, D, 0.f, 0.f, 0.f, 0.f, tol_sq, lo, hi, &dh, emit);
                 }
             }
-            __syncthreads();
-            if (BLOCK_COMPACT) {
-                CompactSmem& Cs = *reinterpret_cast<CompactSmem*>(smem + ((sizeof(BuildSmem) + 15) & ~(size_t)15));
-                compact_window_block(S, B.raw, B.rs, w1 - w0, pts, ss, Cs);
+            G::sync();
+            if (N == 32) {
+                compact_window(S, B.raw, B.rs, w1 - w0, pts, ss, limit);
+            } else if (BLOCK_COMPACT) {
+                compact_window_block(S, B.raw, B.rs, w1 - w0, pts, ss, *Cs);
             } else if (tid < 32) {
-                compact_window(S, B.raw, B.rs, w1 - w0, pts, ss);
+                compact_window(S, B.raw, B.rs, w1 - w0, pts, ss, limit);
             }
-            __syncthreads();
-            if (S.capped) break;
+            G::sync();
+            if (S.capped || S.overflow) break;
         }
-        __syncthreads();
-        if (S.capped) break;
+        G::sync();
+        if (S.capped || S.overflow) break;
     }
     // Plotter::fill ends with fig.close() (plotter.rs:347)
-    if (tid == 0 && !S.capped && S.has_prev && S.rf_x == S.prev_x && S.rf_y == S.prev_y) S.count -= 1;
-    __syncthreads();
+    if (tid == 0 && !S.capped && !S.overflow && S.has_prev && S.rf_x == S.prev_x && S.rf_y == S.prev_y)
+        S.count -= 1;
+    G::sync();
 }
 
 // Top vertex (min (y, x, id)) and figure direction (fig.rs:402-411, 493-496).
+template <class G>
 __device__ void top_and_dir(CState& S, const int2* pts, const int* ss, int* tmp3) {
-    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int tid = G::rank(), lane = threadIdx.x & 31, w = tid >> 5;
     const int count = S.count;
     int by = INT_MAX, bx = INT_MAX, bi = INT_MAX;
-    for (int i = tid; i < count; i += BLOCK) {
+    for (int i = tid; i < count; i += G::N) {
         int2 p = pts[i];
         if (p.y < by || (p.y == by && (p.x < bx || (p.x == bx && i < bi)))) {
             by = p.y;
@@ -734,14 +784,16 @@ __device__ void top_and_dir(CState& S, const int2* pts, const int* ss, int* tmp3
             bi = oi;
         }
     }
-    if (lane == 0) {
-        tmp3[3 * w] = by;
-        tmp3[3 * w + 1] = bx;
-        tmp3[3 * w + 2] = bi;
+    if (G::N > 32) {
+        if (lane == 0) {
+            tmp3[3 * w] = by;
+            tmp3[3 * w + 1] = bx;
+            tmp3[3 * w + 2] = bi;
+        }
+        G::sync();
     }
-    __syncthreads();
     if (tid == 0) {
-        for (int k = 1; k < NWARP; k++) {
+        for (int k = 1; k < G::N / 32; k++) {
             int oy = tmp3[3 * k], ox = tmp3[3 * k + 1], oi = tmp3[3 * k + 2];
             if (oy < by || (oy == by && (ox < bx || (ox == bx && oi < bi)))) {
                 by = oy;
@@ -774,13 +826,14 @@ __device__ void top_and_dir(CState& S, const int2* pts, const int* ss, int* tmp3
         S.dir = (fxmul(ax, cy) > fxmul(cx, ay)) ? 0 : 1;
         S.top_row = by >> 16;
     }
-    __syncthreads();
+    G::sync();
 }
 
 // One edge per non-horizontal segment (fig.rs:179-201, 576-600).
+template <class G>
 __device__ void build_edges(const CState& S, const int2* pts, const int* ss, EdgeRec* edges) {
     const int count = S.count, figdir = S.dir;
-    for (int i = threadIdx.x; i < count; i += BLOCK) {
+    for (int i = G::rank(); i < count; i += G::N) {
         const int s = ss[i];
         const int nx = (i + 1 < count && ss[i + 1] == s) ? i + 1 : s;
         EdgeRec e;
@@ -868,14 +921,18 @@ __device__ __forceinline__ void scan_item(const EdgeRec& E, int y, int* area, in
 }
 
 // Resolve one band row and write it (fig.rs:621-665, imgbuf.rs:38-199).
-__device__ __forceinline__ void resolve_row(const int* arow, int W, int Wp, uint8_t* drow, int rule, int fmt,
+template <bool ZERO = false>
+__device__ __forceinline__ void resolve_row(int* arow, int W, int Wp, uint8_t* drow, int rule, int fmt,
                                             unsigned clr) {
     const int lane = threadIdx.x & 31;
     unsigned carry = 0;
     for (int x0 = 0; x0 < W; x0 += 128) {
         const int x = x0 + lane * 4;
         int4 a = make_int4(0, 0, 0, 0);
-        if (x < Wp) a = *reinterpret_cast<const int4*>(arow + x);
+        if (x < Wp) {
+            a = *reinterpret_cast<const int4*>(arow + x);
+            if (ZERO) *reinterpret_cast<int4*>(arow + x) = make_int4(0, 0, 0, 0);
+        }
         const unsigned s0 = (unsigned)a.x;
         const unsigned s1 = s0 + (unsigned)a.y;
         const unsigned s2 = s1 + (unsigned)a.z;
@@ -965,6 +1022,135 @@ __device__ void raster_rows(const KParams& P, const ft_path_desc& d, const CStat
     }
 }
 
+// ---------------------------------------------------------------------------
+// Warp rasteriser: one warp per small path.  After building the figure, the warp
+// sweeps the scan rows top to bottom like footile's Scanner (fig.rs:536-617):
+// edges are bucketed by their first row, each row processes the active edges one
+// per lane into a one-row i32 buffer, then resolves and writes the row.
+struct WarpSmem {
+    CState S;
+    int tmp3[4];
+    union {
+        WarpBuildSmem B;
+        int hist[WARP_MAX_SIDE];
+    } u;
+    int row[WARP_MAX_SIDE];
+};
+
+__device__ void raster_sweep_warp(const KParams& P, const ft_path_desc& d, const CState& S, const EdgeRec* edges,
+                                  int* sorted, int* active, int* hist, int* row) {
+    const int lane = threadIdx.x & 31;
+    const int count = S.count, H = (int)d.height, W = (int)d.width, Wp = (W + 3) & ~3;
+    const int top_row = S.top_row, row_begin = max(top_row, 0);
+    const int nrows = H - row_begin;
+    const unsigned clr = (unsigned)d.clr[0] | ((unsigned)d.clr[1] << 8) | ((unsigned)d.clr[2] << 16) |
+                         ((unsigned)d.clr[3] << 24);
+    uint8_t* base = P.rasters + d.raster_offset;
+    // bucket the edges by their first scan row (edges below the last row never start)
+    for (int b = lane; b < nrows; b += 32) hist[b] = 0;
+    __syncwarp();
+    for (int e = lane; e < count; e += 32) {
+        const EdgeRec& E = edges[e];
+        if (E.ed) {
+            const long long b = (long long)E.start_row - top_row;
+            if (b < nrows) atomicAdd(&hist[b], 1);
+        }
+    }
+    __syncwarp();
+    int carry = 0;
+    for (int b0 = 0; b0 < nrows; b0 += 32) {
+        const int b = b0 + lane;
+        const int v = b < nrows ? hist[b] : 0;
+        const int inc = warp_incl_sum(v);
+        if (b < nrows) hist[b] = carry + inc - v;
+        carry += __shfl_sync(FULL, inc, 31);
+    }
+    __syncwarp();
+    for (int e = lane; e < count; e += 32) {
+        const EdgeRec& E = edges[e];
+        if (E.ed) {
+            const long long b = (long long)E.start_row - top_row;
+            if (b < nrows) sorted[atomicAdd(&hist[b], 1)] = e;
+        }
+    }
+    for (int x = lane; x < Wp; x += 32) row[x] = 0;
+    __syncwarp();
+    // hist[b] now ends bucket b
+    int n_act = 0;
+    for (int s = 0; s < nrows; s++) {
+        const int y = top_row + s;
+        const int bs = s == 0 ? 0 : hist[s - 1], be = hist[s];
+        for (int k = lane; k < be - bs; k += 32) active[n_act + k] = sorted[bs + k];
+        n_act += be - bs;
+        __syncwarp();
+        int nn = 0;
+        for (int a0 = 0; a0 < n_act; a0 += 32) {
+            const int idx = a0 + lane;
+            const bool v = idx < n_act;
+            int e = 0, end_row = INT_MIN;
+            if (v) {
+                e = active[idx];
+                const EdgeRec E = edges[e];
+                end_row = E.end_row;
+                scan_item(E, y, row, W);
+            }
+            // an edge leaves the active list after its last row (fig.rs:582, 603-617)
+            const bool keep = v && end_row > y;
+            const unsigned km = __ballot_sync(FULL, keep);
+            if (keep) active[nn + __popc(km & ((1u << lane) - 1u))] = e;
+            nn += __popc(km);
+        }
+        n_act = nn;
+        __syncwarp();
+        resolve_row<true>(row, W, Wp, base + (size_t)(row_begin + s) * d.stride, P.rule, P.fmt, clr);
+        __syncwarp();
+    }
+}
+
+__global__ void __launch_bounds__(BLOCK) k_raster_warp(KParams P) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    WarpSmem& M = reinterpret_cast<WarpSmem*>(smem)[warp];
+    unsigned char* scr = P.scratch + (size_t)blockIdx.x * SCRATCH_BYTES_PER_CTA + (size_t)warp * WS_BYTES;
+    int2* pts = reinterpret_cast<int2*>(scr + WS_PTS);
+    int* ss = reinterpret_cast<int*>(scr + WS_SS);
+    EdgeRec* edges = reinterpret_cast<EdgeRec*>(scr + WS_EDGES);
+    int* sorted = reinterpret_cast<int*>(scr + WS_SORT);
+    int* active = reinterpret_cast<int*>(scr + WS_ACT);
+    for (;;) {
+        int it = 0;
+        if (lane == 0) it = (int)atomicAdd(&P.queue[1], 1u);
+        it = __shfl_sync(FULL, it, 0);
+        if (it >= (int)P.n_items_w) break;
+        const WorkItem wi = P.items_w[it];
+        const ft_path_desc d = P.paths[wi.path];
+        const float sw0 = P.sw_chain ? *P.sw_chain : d.s_width;
+        build_fill<WarpG>(P, d, sw0, M.u.B, nullptr, M.S, pts, ss, WARP_CAP);
+        if (M.S.overflow) {
+            // too many vertices for a warp: a CTA of the next kernel redoes this path
+            if (lane == 0) P.overflow[atomicAdd(&P.queue[2], 1u)] = wi.path;
+            __syncwarp();
+            continue;
+        }
+        if (M.S.count > 0) {
+            top_and_dir<WarpG>(M.S, pts, ss, M.tmp3);
+            build_edges<WarpG>(M.S, pts, ss, edges);
+            __syncwarp();
+            if (max(M.S.top_row, 0) < (int)d.height && d.width > 0)
+                raster_sweep_warp(P, d, M.S, edges, sorted, active, M.u.hist, M.row);
+        }
+        if (P.sw_out) {
+            int lp = -1;
+            for (int i = lane; i < (int)d.n_ops; i += 32)
+                if (P.ops[d.op_begin + i].kind == FT_OP_PEN_WIDTH) lp = max(lp, i);
+            lp = warp_incl_max(lp);
+            if (lane == 31) P.sw_out[wi.path] = lp >= 0 ? P.ops[d.op_begin + lp].v[0] : sw0;
+        }
+        if (lane == 0 && M.S.flags) atomicMax(&P.status[wi.path], (M.S.flags & 1) ? FT_ERR_DEPTH : FT_ERR_ARG);
+        __syncwarp();
+    }
+}
+
 __global__ void __launch_bounds__(BLOCK) k_raster(KParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ CState S;
@@ -975,19 +1161,35 @@ __global__ void __launch_bounds__(BLOCK) k_raster(KParams P) {
     int2* pts = reinterpret_cast<int2*>(scr + SCR_PTS);
     int* ss = reinterpret_cast<int*>(scr + SCR_SS);
     EdgeRec* edges = reinterpret_cast<EdgeRec*>(scr + SCR_EDGES);
+    // paths the warp rasteriser handed over (it ran before this kernel)
+    const int n_over = P.overflow ? (int)*(volatile uint32_t*)&P.queue[2] : 0;
     for (;;) {
-        if (tid == 0) s_item = (int)atomicAdd(P.queue, 1u);
+        if (tid == 0) s_item = (int)atomicAdd(&P.queue[0], 1u);
         __syncthreads();
         const int it = s_item;
         __syncthreads();
-        if (it >= (int)P.n_items) break;
-        const WorkItem wi = P.items[it];
+        if (it >= (int)P.n_items + n_over) break;
+        WorkItem wi;
+        if (it < (int)P.n_items) {
+            wi = P.items[it];
+        } else {
+            wi.path = P.overflow[it - (int)P.n_items];
+            wi.row_begin = 0;
+            wi.row_end = P.paths[wi.path].height;
+            wi.band_rows = 0;
+        }
         const ft_path_desc d = P.paths[wi.path];
+        if (wi.band_rows == 0) {
+            const int wp4 = (int)(((d.width + 3) & ~3u) * 4);
+            wi.band_rows = (uint32_t)max(1, min((P.smem_bytes - RASTER_FIXED_SMEM) / max(wp4, 4), (int)d.height));
+        }
         const float sw0 = P.sw_chain ? *P.sw_chain : d.s_width;
-        build_fill(P, d, sw0, smem, S, pts, ss);
+        BuildSmem& B = *reinterpret_cast<BuildSmem*>(smem);
+        CompactSmem* Cs = reinterpret_cast<CompactSmem*>(smem + ((sizeof(BuildSmem) + 15) & ~(size_t)15));
+        build_fill<BlockG>(P, d, sw0, B, Cs, S, pts, ss, PT_CAP);
         if (S.count > 0) {
-            top_and_dir(S, pts, ss, s_tmp3);
-            build_edges(S, pts, ss, edges);
+            top_and_dir<BlockG>(S, pts, ss, s_tmp3);
+            build_edges<BlockG>(S, pts, ss, edges);
             __syncthreads();
             const int row_begin = max(S.top_row, 0);
             const int lo = max((int)wi.row_begin, row_begin);
@@ -1018,6 +1220,24 @@ int raster_blocks_per_sm(int smem_bytes) {
     cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_raster, BLOCK, smem_bytes) != cudaSuccess) return 1;
+    return n > 0 ? n : 1;
+}
+
+cudaError_t launch_raster_warp(const KParams& p, int grid, cudaStream_t s) {
+    const int smem = raster_warp_smem();
+    cudaError_t e = cudaFuncSetAttribute(k_raster_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    k_raster_warp<<<grid, BLOCK, smem, s>>>(p);
+    return cudaGetLastError();
+}
+
+int raster_warp_smem() { return (int)(NWARP * sizeof(WarpSmem)); }
+
+int raster_warp_blocks_per_sm() {
+    const int smem = raster_warp_smem();
+    cudaFuncSetAttribute(k_raster_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_raster_warp, BLOCK, smem) != cudaSuccess) return 1;
     return n > 0 ? n : 1;
 }
 

@@ -51,12 +51,26 @@ constexpr size_t SCR_SUBS = align256(SCR_SPTS + (size_t)PT_CAP * sizeof(float4))
 constexpr size_t SCR_SOFF = align256(SCR_SUBS + (size_t)PT_CAP * sizeof(SubRec));    // int[2*PT_CAP+8] offsets
 constexpr size_t SCRATCH_BYTES_PER_CTA = align256(SCR_SOFF + (size_t)(2 * PT_CAP + 8) * sizeof(int));
 
+// Warp rasteriser (one warp per small path): per-warp share of the CTA scratch.
+constexpr int WARP_CAP = 8191;        // vertices a warp holds; larger figures go to a CTA
+constexpr int WARP_MAX_SIDE = 512;    // canvases up to this width and height use the warp rasteriser
+constexpr size_t WS_PTS = 0;
+constexpr size_t WS_SS = align256(WS_PTS + (size_t)WARP_CAP * sizeof(int2));
+constexpr size_t WS_EDGES = align256(WS_SS + (size_t)WARP_CAP * sizeof(int));
+constexpr size_t WS_SORT = align256(WS_EDGES + (size_t)WARP_CAP * sizeof(EdgeRec));
+constexpr size_t WS_ACT = align256(WS_SORT + (size_t)WARP_CAP * sizeof(int));
+constexpr size_t WS_BYTES = align256(WS_ACT + (size_t)WARP_CAP * sizeof(int));
+static_assert(NWARP * WS_BYTES <= SCRATCH_BYTES_PER_CTA, "warp scratch layout");
+
 struct KParams {
     const ft_op* ops;
     const ft_path_desc* paths;
-    const WorkItem* items;
+    const WorkItem* items;   // CTA work items (large paths, row ranges)
     uint32_t n_items;
-    uint32_t* queue;         // [0]: next work item
+    const WorkItem* items_w; // warp work items (small paths, whole rasters)
+    uint32_t n_items_w;
+    uint32_t* overflow;      // paths a warp handed over to the CTA kernel
+    uint32_t* queue;         // [0]: next CTA item, [1]: next warp item, [2]: overflow count
     uint8_t* rasters;
     int32_t* status;         // per path, atomicMax of FT_ERR_* codes
     float* sw_out;           // per path pen width after the call (nullable)
@@ -77,6 +91,10 @@ constexpr int RASTER_FIXED_SMEM = BLOCK * (int)sizeof(EdgeRec) + 3 * BLOCK * 4 +
 
 // Launch the persistent rasteriser.  Returns the CUDA error of the launch.
 cudaError_t launch_raster(const KParams& p, int grid, int smem_bytes, cudaStream_t s);
+// Launch the warp rasteriser (small paths).  Its dynamic shared memory is fixed.
+cudaError_t launch_raster_warp(const KParams& p, int grid, cudaStream_t s);
+int raster_warp_smem();
+int raster_warp_blocks_per_sm();
 
 // Resident CTAs per SM for `smem_bytes` of dynamic shared memory.
 int raster_blocks_per_sm(int smem_bytes);

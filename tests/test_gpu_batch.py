@@ -21,8 +21,10 @@ def _compare_paths(got, want, paths, which):
         assert_same(a, b, f"path {i} ({d['n_ops']} ops, {d['width']}x{d['height']})")
 
 
+@pytest.mark.parametrize("warp", ["512", "0"])
 @pytest.mark.parametrize("rule", [_abi.NONZERO, _abi.EVENODD])
-def test_glyph_batch_host(ctx, rule):
+def test_glyph_batch_host(ctx, rule, warp, monkeypatch):
+    monkeypatch.setenv("FT_WARP_MAX_SIDE", warp)
     ops, paths, nbytes = workloads.glyphs(3000, seed=31)
     want = np.zeros(nbytes, np.uint8)
     st_o = oracle.fill_batch(0, rule, ops, paths, _abi.MATTE8, want, n_threads=8)

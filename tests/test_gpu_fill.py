@@ -21,6 +21,15 @@ from test_oracle_golden import FIG_CASES
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(params=["warp", "cta"])
+def rasteriser(request, monkeypatch):
+    """Small canvases go to the warp rasteriser by default; FT_WARP_MAX_SIDE=0
+    sends every path to the CTA rasteriser, so both kernels are checked."""
+    if request.param == "cta":
+        monkeypatch.setenv("FT_WARP_MAX_SIDE", "0")
+    return request.param
+
+
 @pytest.mark.parametrize("name", sorted(FIG_CASES))
 def test_fig_known_answers(ctx, name):
     pts, w, h, want = FIG_CASES[name]
@@ -40,7 +49,7 @@ def test_fig_3x3_rgba8p(ctx):
 
 @pytest.mark.parametrize("seed", range(12))
 @pytest.mark.parametrize("rule", [_abi.NONZERO, _abi.EVENODD])
-def test_random_paths_matte8(ctx, seed, rule):
+def test_random_paths_matte8(ctx, rasteriser, seed, rule):
     rng = np.random.default_rng(100 + seed)
     w = int(rng.integers(1, 300))
     h = int(rng.integers(1, 300))
@@ -53,7 +62,7 @@ def test_random_paths_matte8(ctx, seed, rule):
 
 
 @pytest.mark.parametrize("seed", range(6))
-def test_random_paths_rgba8p(ctx, seed):
+def test_random_paths_rgba8p(ctx, rasteriser, seed):
     rng = np.random.default_rng(200 + seed)
     w, h = int(rng.integers(1, 200)), int(rng.integers(1, 200))
     ops = workloads.random_path(rng, max(w, h), 40, n_sub=2)
@@ -67,7 +76,7 @@ def test_random_paths_rgba8p(ctx, seed):
     assert_same(got, want, f"rgba seed {seed}")
 
 
-def test_single_path_256(ctx):
+def test_single_path_256(ctx, rasteriser):
     ops, w, h, clr = workloads.single_path_256()
     got, want, st, _, err = gpu_vs_oracle(ctx, ops, w, h)
     assert err is None
@@ -76,7 +85,7 @@ def test_single_path_256(ctx):
     assert_same(got, want, "rgba")
 
 
-def test_empty_and_degenerate(ctx):
+def test_empty_and_degenerate(ctx, rasteriser):
     for ops in [ops_array([]), ops_array([PathOp.Move(3, 3)]), ops_array([PathOp.Close(), PathOp.Close()]),
                 fig_ops([(1, 1), (1, 1), (1, 1)]), fig_ops([(1, 1), (5, 1), (9, 1)]),
                 ops_array([PathOp.PenWidth(3.0)])]:
@@ -85,7 +94,7 @@ def test_empty_and_degenerate(ctx):
         assert_same(got, want, str(ops["kind"].tolist()))
 
 
-def test_negative_top_row_shift(ctx):
+def test_negative_top_row_shift(ctx, rasteriser):
     # fig.rs:496-499: raster row 0 receives scan row top_row when top_row < 0
     ops = fig_ops([(2.5, -5.25), (20.0, 3.0), (6.0, 14.5), (1.0, 9.0)])
     got, want, st, _, err = gpu_vs_oracle(ctx, ops, 24, 16, init=3)
@@ -102,7 +111,7 @@ def test_rows_above_top_untouched(ctx):
     assert_same(got, want, "rows above top")
 
 
-def test_x_out_of_bounds(ctx):
+def test_x_out_of_bounds(ctx, rasteriser):
     for pts in [[(-30.0, 0.0), (-20.0, 9.0), (5.5, 4.5)], [(10.0, 0.0), (60.0, 9.0), (45.5, 4.5)],
                 [(-1e6, 0.5), (1e6, 7.25), (3.0, 9.0)]]:
         got, want, *_ = gpu_vs_oracle(ctx, fig_ops(pts), 17, 11)
@@ -116,7 +125,7 @@ def test_wrapping_widdershins_long_edges(ctx):
     assert_same(got, want, "wrapping direction")
 
 
-def test_close_pops_start_point(ctx):
+def test_close_pops_start_point(ctx, rasteriser):
     # a sub-figure that returns to its start loses the closing vertex
     pts = [(2.0, 2.0), (12.0, 3.0), (8.0, 11.0), (2.0, 2.0)]
     ops = ops_array([PathOp.Move(*pts[0])] + [PathOp.Line(*p) for p in pts[1:]] + [PathOp.Close()] +
@@ -157,7 +166,7 @@ def test_pen_width_persists(ctx):
     assert p.pen_width() == 5.5
 
 
-def test_vertex_cap_65535(ctx):
+def test_vertex_cap_65535(ctx, rasteriser):
     # more than 65,535 vertices: footile keeps the first 65,535 (fig.rs:428-442)
     rng = np.random.default_rng(11)
     n = 70000
@@ -196,3 +205,20 @@ def test_scene_4096_capped(ctx):
     for rule in (_abi.NONZERO, _abi.EVENODD):
         got, want, *_ = gpu_vs_oracle(ctx, ops, w, h, rule=rule)
         assert_same(got, want, f"scene rule {rule}")
+
+
+def test_warp_overflow_hands_path_to_cta(ctx):
+    # 9,000 vertices on a small canvas: more than a warp holds, so the CTA kernel
+    # redraws the path; the result must not change
+    rng = np.random.default_rng(21)
+    n = 9000
+    ang = np.sort(rng.random(n)) * 2 * np.pi
+    rad = 20 + 10 * rng.random(n)
+    ops = np.zeros(n + 1, dtype=_abi.OP_DTYPE)
+    ops["kind"][0] = _abi.OP_MOVE
+    ops["kind"][1:n] = _abi.OP_LINE
+    ops["v"][:n, 0] = 32 + rad * np.cos(ang)
+    ops["v"][:n, 1] = 32 + rad * np.sin(ang)
+    ops["kind"][n] = _abi.OP_CLOSE
+    got, want, *_ = gpu_vs_oracle(ctx, ops, 64, 64)
+    assert_same(got, want, "overflow")
