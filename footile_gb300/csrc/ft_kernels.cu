@@ -29,7 +29,9 @@
 //
 // Rows footile writes: from max(top_row, 0) to the bottom of the raster, raster
 // row r receiving scan row r + min(top_row, 0) (fig.rs:496-499, 536-553).
+#include <algorithm>
 #include <cstdio>
+#include <cstring>
 
 #include "ft_device.cuh"
 #include "ft_kernels.cuh"
@@ -1252,3 +1254,108 @@ int raster_max_smem() {
 }
 
 }  // namespace ftk
+
+// ===========================================================================
+// Allocation-free single-path fill (ft_fill_noalloc).
+//
+// For callers that cannot allocate device memory: code running inside a stream
+// capture, under a fixed memory budget, or in a process whose allocator belongs to
+// another runtime.  The figure scratch of one CTA lives in a file-scope device
+// array that every GPU loading this library holds until the process exits; the
+// caller passes only inputs and outputs.  One CTA rasterises the whole path.
+namespace ftk {
+
+// vertices, sub-figure starts and edges of one figure of up to FT_MAX_POINTS vertices
+constexpr size_t NOALLOC_SCRATCH_BYTES = align256(SCR_EDGES + (size_t)PT_CAP * sizeof(EdgeRec));
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+__global__ void __launch_bounds__(BLOCK) k_fill_noalloc(KParams P, ft_path_desc d, unsigned char* scratch,
+                                                        int32_t* status_out) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ CState S;
+    __shared__ int s_tmp3[3 * NWARP];
+    int2* pts = reinterpret_cast<int2*>(scratch + SCR_PTS);
+    int* ss = reinterpret_cast<int*>(scratch + SCR_SS);
+    EdgeRec* edges = reinterpret_cast<EdgeRec*>(scratch + SCR_EDGES);
+    BuildSmem& B = *reinterpret_cast<BuildSmem*>(smem);
+    CompactSmem* Cs = reinterpret_cast<CompactSmem*>(smem + ((sizeof(BuildSmem) + 15) & ~(size_t)15));
+    build_fill<BlockG>(P, d, d.s_width, B, Cs, S, pts, ss, PT_CAP);
+    if (S.count > 0) {
+        top_and_dir<BlockG>(S, pts, ss, s_tmp3);
+        build_edges<BlockG>(S, pts, ss, edges);
+        __syncthreads();
+        const int lo = max(S.top_row, 0), hi = (int)d.height;
+        const int wp4 = (int)(((d.width + 3) & ~3u) * 4);
+        const int R = max(1, min((P.smem_bytes - RASTER_FIXED_SMEM) / max(wp4, 4), max(hi, 1)));
+        if (lo < hi && d.width > 0) raster_rows(P, d, S, edges, lo, hi, R, smem);
+    }
+    if (threadIdx.x == 0 && status_out)
+        *status_out = S.flags ? ((S.flags & 1) ? FT_ERR_DEPTH : FT_ERR_ARG) : FT_OK;
+}
+
+}  // namespace ftk
+
+#include <mutex>
+
+namespace {
+// device address of g_noalloc_scratch, looked up once per device
+constexpr int NOALLOC_MAX_DEVICES = 64;
+void* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {nullptr};
+std::mutex g_noalloc_mu;
+}  // namespace
+
+extern "C" FT_API int ft_fill_noalloc(int32_t rule, const ft_op* ops, uint32_t n_ops, int32_t fmt,
+                                      const uint8_t clr[4], uint8_t* raster, uint32_t w, uint32_t h,
+                                      uint32_t stride, const float transform[6], float tolerance, float pen_width,
+                                      int32_t* status, void* stream) {
+    if ((rule != FT_NONZERO && rule != FT_EVENODD) || (fmt != FT_MATTE8 && fmt != FT_RGBA8P)) return FT_ERR_ARG;
+    if ((n_ops && !ops) || (w && h && !raster)) return FT_ERR_ARG;
+    if (w > FT_MAX_WIDTH) return FT_ERR_CAP;  // one band row of cell areas must fit in shared memory
+    const uint32_t bpp = fmt == FT_RGBA8P ? 4 : 1;
+    if (h && stride < (uint64_t)w * bpp) return FT_ERR_ARG;
+    if ((reinterpret_cast<uintptr_t>(ops) & 15) ||
+        (fmt == FT_RGBA8P && ((reinterpret_cast<uintptr_t>(raster) | stride) & 3)))
+        return FT_ERR_ARG;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES) return FT_ERR_CUDA;
+    void* scratch = nullptr;
+    {
+        // first call on this device: find the array's device address (before any stream capture)
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            void* p = nullptr;
+            if (cudaGetSymbolAddress(&p, ftk::g_noalloc_scratch) != cudaSuccess || !p) return FT_ERR_CUDA;
+            g_noalloc_ptr[dev] = p;
+        }
+        scratch = g_noalloc_ptr[dev];
+    }
+    ft_path_desc d;
+    memset(&d, 0, sizeof(d));
+    d.n_ops = n_ops;
+    d.width = w;
+    d.height = h;
+    d.stride = stride;
+    d.s_width = pen_width;
+    if (clr) memcpy(d.clr, clr, 4);
+    ftk::KParams p;
+    memset(&p, 0, sizeof(p));
+    p.ops = ops;
+    p.rasters = raster;
+    p.rule = rule;
+    p.fmt = fmt;
+    static const float ident[6] = {1, 0, 0, 0, 1, 0};
+    for (int i = 0; i < 6; i++) p.xf[i] = transform ? transform[i] : ident[i];
+    const float t = tolerance > 0.01f ? tolerance : 0.01f;
+    p.tol_sq = t * t;
+    int optin = 0;
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return FT_ERR_CUDA;
+    const int wp = (int)((w + 3) & ~3u);
+    int smem = std::max(ftk::RASTER_FIXED_SMEM + 16 * wp * 4, 40 * 1024);
+    smem = std::min(smem, optin - 1024);
+    p.smem_bytes = smem;
+    if (cudaFuncSetAttribute(ftk::k_fill_noalloc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+        return FT_ERR_CUDA;
+    ftk::k_fill_noalloc<<<1, ftk::BLOCK, smem, static_cast<cudaStream_t>(stream)>>>(p, d, static_cast<unsigned char*>(scratch),
+                                                                                 status);
+    return cudaGetLastError() == cudaSuccess ? FT_OK : FT_ERR_CUDA;
+}

@@ -156,6 +156,26 @@ FT_API int ft_batch_launch(ft_ctx* ctx, ft_batch* batch, const ft_op* ops, uint3
 FT_API int ft_batch_launch_status(ft_ctx* ctx, ft_batch* batch, int32_t* status, uint32_t n);
 FT_API void ft_batch_destroy(ft_batch* batch);
 
+/* Allocation-free fill of one path — this entry point has no counterpart in footile.
+ * For callers that cannot allocate device memory: work recorded into a CUDA graph
+ * while a stream is being captured, processes under a fixed device-memory budget,
+ * or hosts whose device allocator belongs to another runtime.  It needs no
+ * context and calls no allocator: the figure scratch (vertices, sub-figure starts
+ * and edges of one figure, about 2.9 MB) is a file-scope device array that every
+ * GPU which loads this library holds until the process exits.  All pointers are
+ * device pointers; `ops` must be 16-byte aligned, Rgba8p rows 4-byte aligned.
+ * `transform` may be NULL (identity); `status` (device int, may be NULL) receives
+ * FT_OK, FT_ERR_DEPTH or FT_ERR_ARG.  The call is asynchronous on `stream`.  The
+ * first call on each device looks up the array's device address; make that first
+ * call before any stream capture.  Every call shares the one array, so calls that
+ * overlap on the GPU race: serialise them on one stream.  Widths above
+ * FT_MAX_WIDTH return FT_ERR_CAP; figures are capped at FT_MAX_POINTS vertices as
+ * in footile, so every path fits the array. */
+FT_API int ft_fill_noalloc(int32_t rule, const ft_op* ops, uint32_t n_ops, int32_t fmt,
+                           const uint8_t clr[4], uint8_t* raster, uint32_t w, uint32_t h,
+                           uint32_t stride, const float transform[6], float tolerance,
+                           float pen_width, int32_t* status, void* stream);
+
 /* Per-path status codes of the last batch (synchronises the context stream). */
 FT_API int ft_batch_status(ft_ctx* ctx, int32_t* status, uint32_t n);
 
