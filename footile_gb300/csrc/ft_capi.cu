@@ -109,13 +109,13 @@ int warp_max_side() {
 // large paths are split into row ranges of whole bands for the CTA rasteriser.
 // Both lists are ordered longest first.
 void plan_items(ft_ctx* c, const ft_path_desc* paths, uint32_t n_paths, int smem, std::vector<ftk::WorkItem>& out,
-                std::vector<ftk::WorkItem>& out_w) {
+                std::vector<ftk::WorkItem>& out_w, bool stroke) {
     out.clear();
     out_w.clear();
     const int area_bytes = smem - ftk::RASTER_FIXED_SMEM;
     const char* env = getenv("FT_SPLIT_PX");
     const uint64_t split_px = env ? strtoull(env, nullptr, 10) : (uint64_t)(1u << 20);
-    const uint32_t wside = (uint32_t)warp_max_side();
+    const uint32_t wside = stroke ? 0u : (uint32_t)warp_max_side();  // strokes use the CTA kernel
     for (uint32_t i = 0; i < n_paths; i++) {
         const ft_path_desc& d = paths[i];
         const uint32_t wp = (d.width + 3) & ~3u;
@@ -176,8 +176,8 @@ void fill_params(ft_ctx* c, ftk::KParams& p, int stroke, int rule, int fmt, int 
     p.smem_bytes = smem;
 }
 
-int grid_for(ft_ctx* c, int smem, uint32_t n_items) {
-    const int per_sm = ftk::raster_blocks_per_sm(smem);
+int grid_for(ft_ctx* c, int smem, uint32_t n_items, bool stroke) {
+    const int per_sm = ftk::raster_blocks_per_sm(smem, stroke);
     const char* genv = getenv("FT_GRID");
     int grid = genv ? atoi(genv) : c->sm_count * per_sm;
     return std::max(1, std::min(grid, (int)std::max(n_items, 1u)));
@@ -214,7 +214,7 @@ int run(ft_ctx* c, int stroke, int rule, const ft_op* ops_d, const ft_path_desc*
     uint32_t max_w = 1;
     for (uint32_t i = 0; i < n_paths; i++) max_w = std::max(max_w, paths[i].width);
     const int smem = choose_smem(c, max_w);
-    plan_items(c, paths, n_paths, smem, c->h_items, c->h_items_w);
+    plan_items(c, paths, n_paths, smem, c->h_items, c->h_items_w, stroke != 0);
     const uint32_t n_items = (uint32_t)c->h_items.size(), n_items_w = (uint32_t)c->h_items_w.size();
     FT_CU(c->paths.ensure(sizeof(ft_path_desc) * std::max(n_paths, 1u)), "alloc paths");
     FT_CU(c->items.ensure(sizeof(ftk::WorkItem) * std::max(n_items, 1u)), "alloc items");
@@ -222,7 +222,8 @@ int run(ft_ctx* c, int stroke, int rule, const ft_op* ops_d, const ft_path_desc*
     FT_CU(c->overflow.ensure(sizeof(uint32_t) * std::max(n_items_w, 1u)), "alloc overflow list");
     FT_CU(c->status.ensure(sizeof(int32_t) * std::max(n_paths, 1u)), "alloc status");
     FT_CU(c->queue.ensure(256), "alloc queue");
-    const int grid = n_items_w ? std::max(grid_for(c, smem, n_items), c->sm_count) : grid_for(c, smem, n_items);
+    const int grid = n_items_w ? std::max(grid_for(c, smem, n_items, stroke), c->sm_count)
+                               : grid_for(c, smem, n_items, stroke);
     const int grid_w = grid_for_warp(c, n_items_w);
     FT_CU(c->scratch.ensure(ftk::SCRATCH_BYTES_PER_CTA * (size_t)std::max(grid, grid_w)), "alloc scratch");
     FT_CU(cudaMemcpyAsync(c->paths.p, paths, sizeof(ft_path_desc) * n_paths, cudaMemcpyHostToDevice, c->stream),
@@ -274,7 +275,6 @@ int single(ft_ctx* c, int stroke, int32_t rule, const ft_op* ops, uint32_t n_ops
         (where != FT_HOST && where != FT_DEVICE))
         return fail(c, FT_ERR_ARG, "bad rule, format or location");
     if ((n_ops && !ops) || (w && h && !raster)) return fail(c, FT_ERR_ARG, "null buffer");
-    if (stroke) return fail(c, FT_ERR_ARG, "stroke is not available in this build");
     FT_CU(cudaSetDevice(c->device), "set device");
     ft_path_desc d;
     memset(&d, 0, sizeof(d));
@@ -364,7 +364,7 @@ FT_API int ft_batch_create(ft_ctx* c, int32_t stroke, int32_t rule, const ft_pat
     *out = nullptr;
     if ((rule != FT_NONZERO && rule != FT_EVENODD) || (fmt != FT_MATTE8 && fmt != FT_RGBA8P))
         return fail(c, FT_ERR_ARG, "bad rule or format");
-    if (stroke) return fail(c, FT_ERR_ARG, "stroke is not available in this build");
+    if (stroke) rule = FT_NONZERO;  // Plotter::stroke fills the outline NonZero (plotter.rs:364)
     if (n_paths && !paths) return fail(c, FT_ERR_ARG, "null path list");
     FT_CU(cudaSetDevice(c->device), "set device");
     ft_batch* b = new ft_batch();
@@ -389,10 +389,11 @@ FT_API int ft_batch_create(ft_ctx* c, int32_t stroke, int32_t rule, const ft_pat
     }
     b->smem = choose_smem(c, max_w);
     std::vector<ftk::WorkItem> items, items_w;
-    plan_items(c, paths, n_paths, b->smem, items, items_w);
+    plan_items(c, paths, n_paths, b->smem, items, items_w, stroke != 0);
     b->n_items = (uint32_t)items.size();
     b->n_items_w = (uint32_t)items_w.size();
-    b->grid = b->n_items_w ? std::max(grid_for(c, b->smem, b->n_items), c->sm_count) : grid_for(c, b->smem, b->n_items);
+    b->grid = b->n_items_w ? std::max(grid_for(c, b->smem, b->n_items, stroke), c->sm_count)
+                           : grid_for(c, b->smem, b->n_items, stroke);
     b->grid_w = grid_for_warp(c, b->n_items_w);
     cudaError_t e = cudaSuccess;
     if (e == cudaSuccess) e = b->paths.ensure(sizeof(ft_path_desc) * std::max(n_paths, 1u));
@@ -426,7 +427,7 @@ FT_API int ft_batch_create(ft_ctx* c, int32_t stroke, int32_t rule, const ft_pat
     b->params.queue = static_cast<uint32_t*>(b->queue.p);
     b->params.status = static_cast<int32_t*>(b->status.p);
     b->params.scratch = static_cast<unsigned char*>(b->scratch.p);
-    ftk::raster_blocks_per_sm(b->smem);  // sets the kernels' shared-memory attributes outside capture
+    ftk::raster_blocks_per_sm(b->smem, stroke != 0);  // sets the kernels' shared-memory attributes outside capture
     ftk::raster_warp_blocks_per_sm();
     *out = b;
     return FT_OK;
@@ -595,7 +596,7 @@ FT_API int ft_fill_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* o
     if ((rule != FT_NONZERO && rule != FT_EVENODD) || (fmt != FT_MATTE8 && fmt != FT_RGBA8P) ||
         (where != FT_HOST && where != FT_DEVICE))
         return fail(c, FT_ERR_ARG, "bad rule, format or location");
-    if (stroke) return fail(c, FT_ERR_ARG, "stroke is not available in this build");
+    if (stroke) rule = FT_NONZERO;  // Plotter::stroke fills the outline NonZero (plotter.rs:364)
     if (n_paths && !paths) return fail(c, FT_ERR_ARG, "null path list");
     FT_CU(cudaSetDevice(c->device), "set device");
     for (uint32_t i = 0; i < n_paths; i++) {

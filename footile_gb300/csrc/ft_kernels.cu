@@ -30,6 +30,7 @@
 // Rows footile writes: from max(top_row, 0) to the bottom of the raster, raster
 // row r receiving scan row r + min(top_row, 0) (fig.rs:496-499, 536-553).
 #include <algorithm>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 
@@ -41,6 +42,7 @@ namespace ftk {
 constexpr unsigned FULL = 0xFFFFFFFFu;
 constexpr int LEAF_CACHE = 16;  // curve leaves kept from the count pass
 constexpr bool BLOCK_COMPACT = true;  // figure building by the whole CTA (false: warp 0)
+constexpr int SRAW = 1024;            // stroke points per window (float4 in the raw window's bytes)
 
 // ------------------------------------------------------------ block scans
 __device__ __forceinline__ int warp_incl_sum(int v) {
@@ -304,6 +306,10 @@ struct CState {
     int top_row;
     int dir;  // 0 forward, 1 reverse
     int last_pw;
+    // stroke points (stroker.rs:204-236)
+    int s_count, s_nsubs, s_capped, s_last_op, s_has_prev;
+    float s_prev_x, s_prev_y;
+    int s_items;  // outline items of all sub-strokes
 };
 
 template <int N, int RAW>
@@ -312,7 +318,8 @@ struct BuildSmemT {
     float pwval[N];
     float penx[N], peny[N], penw[N];
     int scan[2 * NWARP + 2];
-    int2 raw[RAW];
+    // 16-byte aligned: stroke points are stored here as float4
+    __align__(16) int2 raw[RAW];
     unsigned char rs[RAW];
 };
 using BuildSmem = BuildSmemT<BLOCK, RAW_CAP>;
@@ -328,6 +335,9 @@ struct RasterSmem {
     unsigned char map[MAP_CAP];  // item -> edge slot of the current chunk
 };
 static_assert(((sizeof(RasterSmem) + 15) & ~(size_t)15) <= (size_t)RASTER_FIXED_SMEM, "raster smem layout");
+static_assert(sizeof(int2) * RAW_CAP >= sizeof(float4) * SRAW && RAW_CAP >= 2 * SRAW, "stroke window layout");
+static_assert(offsetof(BuildSmem, raw) % 16 == 0 && sizeof(BuildSmem) % 16 == 0, "build smem alignment");
+static_assert(offsetof(WarpBuildSmem, raw) % 8 == 0, "warp build smem alignment");
 
 // ------------------------------------------------------------ figure builder
 // Sequential restatement of Fig::add_point / Fig::close (fig.rs:373-461) for one
@@ -573,12 +583,284 @@ __device__ void compact_window_block(CState& S, const int2* raw, const unsigned 
     }
 }
 
-// Path walk + flattening + figure building for a fill (Plotter::fill, plotter.rs:339-350),
-// by the thread group G.  Leaves the figure in pts[0..S.count) / ss[].  `limit` is
-// the vertex capacity of pts/ss (a warp stops with S.overflow set beyond it).
-template <class G>
+// Stroke points, block-wide (Stroke::add_point / close, stroker.rs:204-236): a point is
+// kept when it starts a sub-stroke or its f32 position differs from the previous raw
+// point; no closing point is popped; points past 65,535 are dropped and start nothing.
+// `jpf[k]` is the `joined` value the close events before a sub-stroke start leave on
+// the previous sub-stroke (false after a Move, true after a Close).
+__device__ void compact_stroke_block(CState& S, const float4* raw, const unsigned char* rsf,
+                                     const unsigned char* jpf, const int* opi, int m, float4* spts, SubRec* subs,
+                                     CompactSmem& C) {
+    const int tid = threadIdx.x;
+    for (int base = 0; base < m; base += BLOCK) {
+        const int k = base + tid;
+        const bool valid = k < m;
+        const int nb = min(BLOCK, m - base);
+        float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+        int rs = 0;
+        if (valid) {
+            p = raw[k];
+            rs = rsf[k];
+        }
+        const int count0 = S.s_count, nsub0 = S.s_nsubs;
+        float qx = S.s_prev_x, qy = S.s_prev_y;
+        if (tid > 0 && valid) {
+            qx = raw[k - 1].x;
+            qy = raw[k - 1].y;
+        }
+        const bool keep = valid && (rs || !(p.x == qx && p.y == qy));
+        int tot;
+        const int pos = count0 + block_excl_sum(keep ? 1 : 0, C.scan, tot);
+        const bool acc = keep && pos < PT_CAP;
+        int tot_rs;
+        const int sid = nsub0 + block_excl_sum((acc && rs) ? 1 : 0, C.scan, tot_rs);
+        if (acc) spts[pos] = p;
+        if (acc && rs) {
+            subs[sid].start = pos;
+            if (sid > 0) subs[sid - 1].joined = jpf[k];  // the last sub-stroke's is set by finish_subs
+        }
+        const int la = block_incl_max(acc ? tid : -1, C.scan);  // last accepted point of the step
+        const int capped = __syncthreads_or(keep && pos >= PT_CAP);
+        if (tid == BLOCK - 1) {
+            S.s_count = min(count0 + tot, PT_CAP);
+            S.s_nsubs = nsub0 + tot_rs;
+            const float4 l = raw[base + nb - 1];
+            S.s_prev_x = l.x;
+            S.s_prev_y = l.y;
+            S.s_has_prev = 1;
+            if (la >= 0) S.s_last_op = opi[base + la];
+            if (capped) S.s_capped = 1;
+        }
+        __syncthreads();
+        if (capped) return;
+    }
+}
+
+// Sizes of the sub-strokes and their outline items (stroker.rs:87-96, 239-262).  The
+// last sub-stroke is joined when the last close event after its last point was a
+// Close; when the 65,535 cap stopped the point stream, that is the last Close or Move
+// op after the op of the last kept point.
+__device__ void finish_subs(const KParams& P, const ft_path_desc& d, CState& S, SubRec* subs, int* tmp) {
+    const int tid = threadIdx.x;
+    const int nsub = S.s_nsubs, count = S.s_count;
+    if (S.s_capped) {
+        int last = -1;
+        for (int i = S.s_last_op + 1 + tid; i < (int)d.n_ops; i += BLOCK) {
+            const int kd = P.ops[d.op_begin + i].kind;
+            if (kd == FT_OP_CLOSE || kd == FT_OP_MOVE) last = max(last, i);
+        }
+        last = block_incl_max(last, tmp);
+        if (tid == BLOCK - 1 && nsub > 0)
+            subs[nsub - 1].joined = last >= 0 ? (P.ops[d.op_begin + last].kind == FT_OP_CLOSE) : 0;
+    } else if (tid == 0 && nsub > 0) {
+        subs[nsub - 1].joined = S.last_pc_kind == FT_OP_CLOSE;
+    }
+    __syncthreads();
+    int carry = 0;
+    for (int s0 = 0; s0 < nsub; s0 += BLOCK) {
+        const int si = s0 + tid;
+        int items = 0;
+        if (si < nsub) {
+            SubRec r = subs[si];
+            r.n = (si + 1 < nsub ? subs[si + 1].start : count) - r.start;
+            // SubStroke::len with u16 arithmetic: n + 1 wraps at 65,536
+            r.len = r.joined ? ((r.n + 1) & 0xFFFF) : (r.n > 0 ? r.n - 1 : 0);
+            items = r.len > 0 ? 2 * r.len + 2 : 0;
+            subs[si].n = r.n;
+            subs[si].len = r.len;
+        }
+        int tot;
+        const int off = block_excl_sum(items, tmp, tot);
+        if (si < nsub) subs[si].item_off = carry + off;
+        carry += tot;
+    }
+    if (tid == 0) S.s_items = carry;
+    __syncthreads();
+}
+
+// stroke_offset (stroker.rs:301-309): both ends of segment (p0, p1) moved right by w/2
+__device__ __forceinline__ void seg_offset(float4 p0, float4 p1, P2* r0, P2* r1) {
+    const P2 vr = pnormalize(pright(psub(p2(p1.x, p1.y), p2(p0.x, p0.y))));
+    *r0 = padd(p2(p0.x, p0.y), pscale(vr, __fmul_rn(p0.z, 0.5f)));
+    *r1 = padd(p2(p1.x, p1.y), pscale(vr, __fmul_rn(p1.z, 0.5f)));
+}
+
+// Round-join arc (stroker.rs:399-416) walked depth first; leaves in [lo, hi) go to
+// emit(index, point).  Returns the leaves walked.
+template <class Emit>
+__device__ int arc_walk(float4 p, P2 a, P2 b, float tol_sq, int lo, int hi, int* depth_hit, Emit emit) {
+    struct Fr {
+        P2 a, b;
+        int d;
+    };
+    Fr st[FT_MAX_DEPTH + 1];
+    int sp = 0, leaf = 0, d = 0;
+    const float hw = __fmul_rn(p.z, 0.5f);
+    for (;;) {
+        const P2 vr = pnormalize(pright(psub(b, a)));
+        const P2 c = padd(p2(p.x, p.y), pscale(vr, hw));
+        const P2 ab = pmid(a, b);
+        const bool leafy = !pfinite(c) || pdist_sq(c, ab) <= tol_sq;
+        if (leafy || d >= FT_MAX_DEPTH) {
+            if (!leafy) *depth_hit = 1;
+            if (leaf >= lo && leaf < hi) emit(leaf, b);
+            leaf++;
+            if (leaf >= hi || sp == 0) break;
+            --sp;
+            a = st[sp].a;
+            b = st[sp].b;
+            d = st[sp].d;
+        } else {
+            st[sp].a = c;
+            st[sp].b = b;
+            st[sp].d = d + 1;
+            sp++;
+            b = c;
+            d++;
+        }
+    }
+    return leaf;
+}
+
+// One outline item of a sub-stroke: the start point, one join, or the end point of a
+// side (stroker.rs:265-295, 323-396).  Emits its points in order through emit(k, pt)
+// for k in [lo, hi) and returns how many it has.
+template <class Emit>
+__device__ int outline_item(const KParams& P, const float4* spts, const SubRec& sr, int u, int lo, int hi,
+                            int* depth_hit, Emit emit) {
+    const int len = sr.len, n = sr.n, s = sr.start;
+    const bool joined = sr.joined != 0;
+    const bool rev = u > len;
+    const int j = rev ? u - len - 1 : u;  // iteration on this side; j == len is the end item
+    auto v0 = [&](int jj) { return rev ? s + ((n - 1 - jj) % n + n) % n : s + (jj % n); };
+    auto v1 = [&](int jj) { return rev ? s + ((n - 2 - jj) % n + n) % n : s + ((jj + 1) % n); };
+    auto seg = [&](int jj, P2* r0, P2* r1) { seg_offset(spts[v0(jj)], spts[v1(jj)], r0, r1); };
+    if (j == len) {  // end of an open side: the last offset point
+        if (joined) return 0;
+        P2 r0, r1;
+        seg(len - 1, &r0, &r1);
+        if (lo <= 0 && 0 < hi) emit(0, r1);
+        return 1;
+    }
+    if (j == 0) {  // start of an open side: butt end
+        if (joined) return 0;
+        P2 r0, r1;
+        seg(0, &r0, &r1);
+        if (lo <= 0 && 0 < hi) emit(0, r0);
+        return 1;
+    }
+    P2 a0, a1, b0, b1;
+    seg(j - 1, &a0, &a1);
+    seg(j, &b0, &b1);
+    if (P.join == FT_JOIN_MITER) {  // stroker.rs:340-367
+        const float ml = P.miter_limit;
+        if (ml > 0.0f) {
+            const float sm_min = __fdiv_rn(1.0f, ml);
+            const float th = pangle_rel(psub(a1, a0), psub(b0, b1));
+            const float sm = fabsf(ft_sinf(__fmul_rn(th, 0.5f)));
+            P2 xp;
+            if (sm >= sm_min && sm < 1.0f && pline_x(a0, a1, b0, b1, &xp)) {
+                if (lo <= 0 && 0 < hi) emit(0, xp);
+                return 1;
+            }
+        }
+    } else if (P.join == FT_JOIN_ROUND) {  // stroker.rs:380-396
+        const float th = pangle_rel(psub(a1, a0), psub(b0, b1));
+        if (th > 0.0f) {
+            if (lo <= 0 && 0 < hi) emit(0, a1);
+            const int na = arc_walk(spts[v0(j)], a1, b0, P.tol_sq, max(lo - 1, 0), hi - 1, depth_hit,
+                                    [&](int k, P2 q) { emit(k + 1, q); });
+            return 1 + na;
+        }
+    }
+    // bevel (stroker.rs:370-373)
+    if (lo <= 0 && 0 < hi) emit(0, a1);
+    if (lo <= 1 && 1 < hi) emit(1, b0);
+    return 2;
+}
+
+// Stroke outline -> figure: outline items in chunks of BLOCK (count, scan, then emit
+// window by window through the second transform, plotter.rs:356-365 / 219-224) into
+// the same figure builder a fill uses.
+__device__ void build_outline(const KParams& P, CState& S, const float4* spts, const SubRec* subs, BuildSmem& B,
+                              CompactSmem& Cs, int2* pts, int* ss) {
+    const int tid = threadIdx.x;
+    const int total_items = S.s_items, nsub = S.s_nsubs;
+    if (tid == 0) {
+        S.count = 0;
+        S.has_prev = 0;
+        S.prev_x = S.prev_y = 0;
+        S.rf_x = S.rf_y = 0;
+        S.rf_pos = 0;
+        S.capped = 0;
+    }
+    __syncthreads();
+    for (int t0 = 0; t0 < total_items; t0 += BLOCK) {
+        const int t = t0 + tid;
+        int n = 0, si = -1, u = 0, rsk = -1;  // rsk: index of this item's point that starts a figure run
+        SubRec sr;
+        int depth_hit = 0;
+        if (t < total_items) {
+            // the last sub-stroke with item_off <= t owns item t (empty ones share the
+            // next one's offset and come before it)
+            int lo = 0, hi = nsub - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (subs[mid].item_off <= t)
+                    lo = mid;
+                else
+                    hi = mid - 1;
+            }
+            si = lo;
+            sr = subs[si];
+            u = t - sr.item_off;
+            n = outline_item(P, spts, sr, u, INT_MAX, INT_MAX, &depth_hit, [](int, P2) {});
+            // a figure run starts at each side's first point after a Close: the forward
+            // side always (after the previous sub-stroke's Close, or first), the reverse
+            // side when the sub-stroke is joined (stroker.rs:255-260)
+            const bool rev = u > sr.len;
+            const int j = rev ? u - sr.len - 1 : u;
+            const bool joined = sr.joined != 0;
+            if (!rev && ((!joined && j == 0) || (joined && j == 1))) rsk = 0;
+            if (rev && joined && j == 1) rsk = 0;
+        }
+        if (depth_hit) atomicOr(&S.flags, 1);
+        int total;
+        const int off = block_excl_sum(n, B.scan, total);
+        for (int w0 = 0; w0 < total; w0 += RAW_CAP) {
+            const int w1 = min(w0 + RAW_CAP, total);
+            if (n > 0 && off < w1 && off + n > w0) {
+                const int lo = max(w0, off) - off, hi = min(w1, off + n) - off;
+                int dh = 0;
+                outline_item(P, spts, sr, u, lo, hi, &dh, [&](int k, P2 q) {
+                    const int idx = off + k - w0;
+                    const P2 tq = xform(P.xf, q);  // the outline is transformed again (F9)
+                    B.raw[idx] = make_int2(f2fx(tq.x), f2fx(tq.y));
+                    B.rs[idx] = (k == rsk) ? (unsigned char)1 : (unsigned char)0;
+                });
+            }
+            __syncthreads();
+            compact_window_block(S, B.raw, B.rs, w1 - w0, pts, ss, Cs);
+            __syncthreads();
+            if (S.capped) break;
+        }
+        __syncthreads();
+        if (S.capped) break;
+    }
+    // Plotter::fill ends with fig.close() (plotter.rs:347)
+    if (tid == 0 && !S.capped && S.has_prev && S.rf_x == S.prev_x && S.rf_y == S.prev_y) S.count -= 1;
+    __syncthreads();
+}
+
+// Path walk + flattening by the thread group G.
+// Fill (Plotter::fill, plotter.rs:339-350): builds the figure in pts[0..S.count) / ss[];
+// `limit` is the vertex capacity of pts/ss (a warp stops with S.overflow set beyond it).
+// STROKE (Plotter::stroke, plotter.rs:356-365, first half): collects the stroke points
+// with their widths in spts[0..S.s_count) and the sub-strokes in subs[0..S.s_nsubs).
+template <class G, bool STROKE = false>
 __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, BuildSmemT<G::N, G::RAW>& B,
-                           CompactSmem* Cs, CState& S, int2* pts, int* ss, int limit) {
+                           CompactSmem* Cs, CState& S, int2* pts, int* ss, int limit, float4* spts = nullptr,
+                           SubRec* subs = nullptr, int* opi = nullptr) {
     constexpr int N = G::N;
     const int tid = G::rank();
     if (tid == 0) {
@@ -595,8 +877,12 @@ __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, B
         S.capped = 0;
         S.overflow = 0;
         S.flags = 0;
+        S.s_count = S.s_nsubs = S.s_capped = S.s_has_prev = 0;
+        S.s_last_op = -1;
+        S.s_prev_x = S.s_prev_y = 0.f;
     }
     G::sync();
+    constexpr int WIN = STROKE ? SRAW : G::RAW;
     const ft_op* ops = P.ops + d.op_begin;
     const int n_ops = (int)d.n_ops;
     const float tol_sq = P.tol_sq;
@@ -651,16 +937,29 @@ __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, B
         int lpc_inc, lpc;
         G::max_scan(isPC ? tid : -1, B.scan, lpc_inc, lpc);
         G::sync();
-        float pen_x, pen_y;
+        float pen_x, pen_y, pen_w;
         int prev_pc_kind;
         if (lpc >= 0) {
             pen_x = B.penx[lpc];
             pen_y = B.peny[lpc];
+            pen_w = B.penw[lpc];
             prev_pc_kind = B.kind[lpc];
         } else {
             pen_x = S.pen_x;
             pen_y = S.pen_y;
+            pen_w = S.pen_w;
             prev_pc_kind = S.last_pc_kind;
+        }
+        // widths of a curve's control points (plotter.rs:235-236, 294-298)
+        float wa = pen_w, wb = 0.f, wc = 0.f, wd = sw_i;
+        if (STROKE) {
+            if (kind == FT_OP_QUAD) {
+                wb = __fmul_rn(__fadd_rn(pen_w, sw_i), 0.5f);
+                wc = sw_i;
+            } else if (kind == FT_OP_CUBIC) {
+                wb = __fadd_rn(sw_i, __fmul_rn(__fsub_rn(pen_w, sw_i), 1.0f / 3.0f));
+                wc = __fadd_rn(sw_i, __fmul_rn(__fsub_rn(pen_w, sw_i), 2.0f / 3.0f));
+            }
         }
         // the first vertex of this op starts a sub-figure after a close event
         const int rs = (kind == FT_OP_MOVE) || prev_pc_kind == FT_OP_CLOSE || prev_pc_kind == -1;
@@ -684,6 +983,8 @@ __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, B
             if (!pfinite(A) || !pfinite(Bq) || !pfinite(C)) {
                 nonfinite = true;
                 n = 1;
+            } else if (STROKE) {
+                n = quad_walk<true>(A, Bq, C, wa, wb, wc, tol_sq, 0, INT_MAX, &depth_hit, [](int, P2, float) {});
             } else {
                 n = quad_walk<false>(A, Bq, C, 0.f, 0.f, 0.f, tol_sq, 0, INT_MAX, &depth_hit, keep_leaf);
             }
@@ -695,6 +996,9 @@ __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, B
             if (!pfinite(A) || !pfinite(Bq) || !pfinite(C) || !pfinite(D)) {
                 nonfinite = true;
                 n = 1;
+            } else if (STROKE) {
+                n = cubic_walk<true>(A, Bq, C, D, wa, wb, wc, wd, tol_sq, 0, INT_MAX, &depth_hit,
+                                     [](int, P2, float) {});
             } else {
                 n = cubic_walk<false>(A, Bq, C, D, 0.f, 0.f, 0.f, 0.f, tol_sq, 0, INT_MAX, &depth_hit,
                                       keep_leaf);
@@ -716,35 +1020,62 @@ __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, B
             }
         }
         // ---- emit and compact window by window
-        for (int w0 = 0; w0 < total; w0 += G::RAW) {
-            const int w1 = min(w0 + G::RAW, total);
+        for (int w0 = 0; w0 < total; w0 += WIN) {
+            const int w1 = min(w0 + WIN, total);
             if (n > 0 && off < w1 && off + n > w0) {
                 const int lo = max(w0, off) - off, hi = min(w1, off + n) - off;
-                auto emit = [&](int k, P2 q, float) {
-                    int idx = off + k - w0;
-                    B.raw[idx] = make_int2(f2fx(q.x), f2fx(q.y));
-                    B.rs[idx] = (k == 0) ? (unsigned char)rs : (unsigned char)0;
-                };
-                if (kind == FT_OP_MOVE || kind == FT_OP_LINE) {
-                    emit(0, A, 0.f);
-                } else if (nonfinite) {
-                    emit(0, kind == FT_OP_QUAD ? C : D, 0.f);
-                } else if (n <= LEAF_CACHE) {
-                    for (int k = lo; k < hi; k++) {
+                if (STROKE) {
+                    // stroke points keep f32 coordinates and their width (stroker.rs:204-225)
+                    float4* raw4 = reinterpret_cast<float4*>(B.raw);
+                    auto emit = [&](int k, P2 q, float w) {
                         const int idx = off + k - w0;
-                        B.raw[idx] = cache[k];
+                        raw4[idx] = make_float4(q.x, q.y, w, 0.f);
                         B.rs[idx] = (k == 0) ? (unsigned char)rs : (unsigned char)0;
+                        // a Move closes the previous sub-stroke open, a Close joined (F7)
+                        B.rs[SRAW + idx] = (unsigned char)(kind != FT_OP_MOVE);
+                        opi[idx] = i;
+                    };
+                    if (kind == FT_OP_MOVE || kind == FT_OP_LINE) {
+                        emit(0, A, sw_i);
+                    } else if (nonfinite) {
+                        emit(0, kind == FT_OP_QUAD ? C : D, kind == FT_OP_QUAD ? wc : wd);
+                    } else if (kind == FT_OP_QUAD) {
+                        int dh = 0;
+                        quad_walk<true>(A, Bq, C, wa, wb, wc, tol_sq, lo, hi, &dh, emit);
+                    } else {
+                        int dh = 0;
+                        cubic_walk<true>(A, Bq, C, D, wa, wb, wc, wd, tol_sq, lo, hi, &dh, emit);
                     }
-                } else if (kind == FT_OP_QUAD) {
-                    int dh = 0;
-                    quad_walk<false>(A, Bq, C, 0.f, 0.f, 0.f, tol_sq, lo, hi, &dh, emit);
                 } else {
-                    int dh = 0;
-                    cubic_walk<false>(A, Bq, C, D, 0.f, 0.f, 0.f, 0.f, tol_sq, lo, hi, &dh, emit);
+                    auto emit = [&](int k, P2 q, float) {
+                        int idx = off + k - w0;
+                        B.raw[idx] = make_int2(f2fx(q.x), f2fx(q.y));
+                        B.rs[idx] = (k == 0) ? (unsigned char)rs : (unsigned char)0;
+                    };
+                    if (kind == FT_OP_MOVE || kind == FT_OP_LINE) {
+                        emit(0, A, 0.f);
+                    } else if (nonfinite) {
+                        emit(0, kind == FT_OP_QUAD ? C : D, 0.f);
+                    } else if (n <= LEAF_CACHE) {
+                        for (int k = lo; k < hi; k++) {
+                            const int idx = off + k - w0;
+                            B.raw[idx] = cache[k];
+                            B.rs[idx] = (k == 0) ? (unsigned char)rs : (unsigned char)0;
+                        }
+                    } else if (kind == FT_OP_QUAD) {
+                        int dh = 0;
+                        quad_walk<false>(A, Bq, C, 0.f, 0.f, 0.f, tol_sq, lo, hi, &dh, emit);
+                    } else {
+                        int dh = 0;
+                        cubic_walk<false>(A, Bq, C, D, 0.f, 0.f, 0.f, 0.f, tol_sq, lo, hi, &dh, emit);
+                    }
                 }
             }
             G::sync();
-            if (N == 32) {
+            if (STROKE) {
+                compact_stroke_block(S, reinterpret_cast<const float4*>(B.raw), B.rs, B.rs + SRAW, opi, w1 - w0,
+                                     spts, subs, *Cs);
+            } else if (N == 32) {
                 compact_window(S, B.raw, B.rs, w1 - w0, pts, ss, limit);
             } else if (BLOCK_COMPACT) {
                 compact_window_block(S, B.raw, B.rs, w1 - w0, pts, ss, *Cs);
@@ -752,10 +1083,14 @@ __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, B
                 compact_window(S, B.raw, B.rs, w1 - w0, pts, ss, limit);
             }
             G::sync();
-            if (S.capped || S.overflow) break;
+            if (S.capped || S.overflow || S.s_capped) break;
         }
         G::sync();
-        if (S.capped || S.overflow) break;
+        if (S.capped || S.overflow || S.s_capped) break;
+    }
+    if (STROKE) {
+        G::sync();
+        return;
     }
     // Plotter::fill ends with fig.close() (plotter.rs:347)
     if (tid == 0 && !S.capped && !S.overflow && S.has_prev && S.rf_x == S.prev_x && S.rf_y == S.prev_y)
@@ -1032,12 +1367,13 @@ __device__ void raster_rows(const KParams& P, const ft_path_desc& d, const CStat
 struct WarpSmem {
     CState S;
     int tmp3[4];
-    union {
+    union __align__(16) {
         WarpBuildSmem B;
         int hist[WARP_MAX_SIDE];
     } u;
-    int row[WARP_MAX_SIDE];
+    __align__(16) int row[WARP_MAX_SIDE];  // read and cleared as int4 by resolve_row
 };
+static_assert(offsetof(WarpSmem, row) % 16 == 0 && sizeof(WarpSmem) % 16 == 0, "warp smem alignment");
 
 __device__ void raster_sweep_warp(const KParams& P, const ft_path_desc& d, const CState& S, const EdgeRec* edges,
                                   int* sorted, int* active, int* hist, int* row) {
@@ -1153,6 +1489,7 @@ __global__ void __launch_bounds__(BLOCK) k_raster_warp(KParams P) {
     }
 }
 
+template <bool STROKE>
 __global__ void __launch_bounds__(BLOCK) k_raster(KParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ CState S;
@@ -1163,6 +1500,8 @@ __global__ void __launch_bounds__(BLOCK) k_raster(KParams P) {
     int2* pts = reinterpret_cast<int2*>(scr + SCR_PTS);
     int* ss = reinterpret_cast<int*>(scr + SCR_SS);
     EdgeRec* edges = reinterpret_cast<EdgeRec*>(scr + SCR_EDGES);
+    float4* spts = reinterpret_cast<float4*>(scr + SCR_SPTS);
+    SubRec* subs = reinterpret_cast<SubRec*>(scr + SCR_SUBS);
     // paths the warp rasteriser handed over (it ran before this kernel)
     const int n_over = P.overflow ? (int)*(volatile uint32_t*)&P.queue[2] : 0;
     for (;;) {
@@ -1187,8 +1526,17 @@ __global__ void __launch_bounds__(BLOCK) k_raster(KParams P) {
         }
         const float sw0 = P.sw_chain ? *P.sw_chain : d.s_width;
         BuildSmem& B = *reinterpret_cast<BuildSmem*>(smem);
-        CompactSmem* Cs = reinterpret_cast<CompactSmem*>(smem + ((sizeof(BuildSmem) + 15) & ~(size_t)15));
-        build_fill<BlockG>(P, d, sw0, B, Cs, S, pts, ss, PT_CAP);
+        const size_t cs_off = (sizeof(BuildSmem) + 15) & ~(size_t)15;
+        CompactSmem* Cs = reinterpret_cast<CompactSmem*>(smem + cs_off);
+        if (STROKE) {
+            // Plotter::stroke: stroke points, sub-strokes, outline, then the NonZero fill
+            int* opi = reinterpret_cast<int*>(smem + cs_off + ((sizeof(CompactSmem) + 15) & ~(size_t)15));
+            build_fill<BlockG, true>(P, d, sw0, B, Cs, S, pts, ss, PT_CAP, spts, subs, opi);
+            finish_subs(P, d, S, subs, B.scan);
+            build_outline(P, S, spts, subs, B, *Cs, pts, ss);
+        } else {
+            build_fill<BlockG>(P, d, sw0, B, Cs, S, pts, ss, PT_CAP);
+        }
         if (S.count > 0) {
             top_and_dir<BlockG>(S, pts, ss, s_tmp3);
             build_edges<BlockG>(S, pts, ss, edges);
@@ -1212,16 +1560,18 @@ __global__ void __launch_bounds__(BLOCK) k_raster(KParams P) {
 }
 
 cudaError_t launch_raster(const KParams& p, int grid, int smem_bytes, cudaStream_t s) {
-    cudaError_t e = cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+    auto kern = p.stroke ? k_raster<true> : k_raster<false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
     if (e != cudaSuccess) return e;
-    k_raster<<<grid, BLOCK, smem_bytes, s>>>(p);
+    kern<<<grid, BLOCK, smem_bytes, s>>>(p);
     return cudaGetLastError();
 }
 
-int raster_blocks_per_sm(int smem_bytes) {
-    cudaFuncSetAttribute(k_raster, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+int raster_blocks_per_sm(int smem_bytes, bool stroke) {
+    auto kern = stroke ? k_raster<true> : k_raster<false>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_raster, BLOCK, smem_bytes) != cudaSuccess) return 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, BLOCK, smem_bytes) != cudaSuccess) return 1;
     return n > 0 ? n : 1;
 }
 
@@ -1249,7 +1599,7 @@ int raster_max_smem() {
     cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     cudaFuncAttributes fa;
     int stat = 0;
-    if (cudaFuncGetAttributes(&fa, k_raster) == cudaSuccess) stat = (int)fa.sharedSizeBytes;
+    if (cudaFuncGetAttributes(&fa, k_raster<true>) == cudaSuccess) stat = (int)fa.sharedSizeBytes;
     return v - stat;
 }
 

@@ -33,10 +33,12 @@ struct EdgeRec {
 
 // One stroke sub-path (stroker.rs:31-40).
 struct SubRec {
-    int start;   // first stroke point
-    int n;       // points
-    int joined;  // joined ends
-    int len;     // SubStroke::len() (u16 arithmetic)
+    int start;     // first stroke point
+    int n;         // points
+    int joined;    // joined ends
+    int len;       // SubStroke::len() (u16 arithmetic)
+    int item_off;  // first outline item of this sub-stroke
+    int pad[3];
 };
 
 // Per-CTA scratch in global memory, private to one resident CTA and reused for
@@ -97,7 +99,7 @@ int raster_warp_smem();
 int raster_warp_blocks_per_sm();
 
 // Resident CTAs per SM for `smem_bytes` of dynamic shared memory.
-int raster_blocks_per_sm(int smem_bytes);
+int raster_blocks_per_sm(int smem_bytes, bool stroke);
 
 // Maximum dynamic shared memory the kernel may be configured for.
 int raster_max_smem();
