@@ -217,10 +217,10 @@ def run_ours(args):
     ras_d = torch.zeros(nbytes, dtype=torch.uint8, device=dev)
     batch = PreparedBatch(ctx, paths, _abi.MATTE8)
 
+    from footile_gb300 import replicas
+
     def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
+        replicas.barrier()
 
     for _ in range(args.warmup):
         batch.launch(ops_d, ras_d)
@@ -250,13 +250,10 @@ def run_ours(args):
         batch.launch(ops_d, ras_d)
         kms.append(ctx.last_ms())
     clk = clocks.stop()
-    ms_max = ms
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_max = float(t.item())
-    value = px_total * world / (ms_max * 1e-3) / 1e6
+    # every rank renders its own batch: job pixels over the slowest rank's time
+    ms_max = replicas.reduce_max(ms, dev)
+    job_px = replicas.reduce_sum(px_total, dev)
+    value = job_px / (ms_max * 1e-3) / 1e6
 
     # ---- end to end through the C ABI with host buffers (e2e)
     from footile_gb300.plotter import fill_batch
@@ -273,12 +270,8 @@ def run_ours(args):
         fill_batch(ctx2, ops_np, paths, _abi.MATTE8, ras_np)
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     barrier()
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_val = px_total * world / e2e_s / 1e6
+    e2e_s = replicas.reduce_max(e2e_s, dev)
+    e2e_val = job_px / e2e_s / 1e6
     # masks of the e2e path must equal the device path's
     same = bool(np.array_equal(ras_np, ras_d.cpu().numpy()))
 
