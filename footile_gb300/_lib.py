@@ -55,6 +55,7 @@ def load(auto_build=True):
             "ft_batch_launch": ([P, P, P, u32, P, u64], ctypes.c_int),
             "ft_batch_launch_status": ([P, P, P, u32], ctypes.c_int),
             "ft_batch_destroy": ([P], None),
+            "ft_composite_batch": ([P, i32, i32, P, u32, P, u32, i32, P, u32, u32, u32, i32], ctypes.c_int),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -70,7 +71,8 @@ def exported_symbols():
         "ft_ctx_create", "ft_ctx_destroy", "ft_set_stream", "ft_set_tolerance", "ft_set_transform",
         "ft_set_join", "ft_set_pen_width", "ft_get_pen_width", "ft_fill", "ft_stroke", "ft_fill_batch",
         "ft_batch_status", "ft_sync", "ft_last_error", "ft_last_timings", "ft_launch_count",
-        "ft_batch_create", "ft_batch_launch", "ft_batch_launch_status", "ft_batch_destroy")]
+        "ft_batch_create", "ft_batch_launch", "ft_batch_launch_status", "ft_batch_destroy",
+        "ft_composite_batch")]
 
 
 class Context:

@@ -52,6 +52,7 @@ struct ft_ctx {
     bool sw_on_device = false;
     // device buffers
     DevBuf ops, paths, items, items_w, overflow, status, sw_out, rasters, queue, scratch, sw_chain;
+    DevBuf pool, pool_used, bandoff, crec;  // ordered composite
     std::vector<ftk::WorkItem> h_items, h_items_w;
     uint32_t last_n_paths = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -523,8 +524,9 @@ FT_API void ft_ctx_destroy(ft_ctx* c) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
-    DevBuf* bufs[] = {&c->ops,     &c->paths,   &c->items, &c->items_w, &c->overflow, &c->status,
-                      &c->sw_out, &c->rasters, &c->queue, &c->scratch, &c->sw_chain};
+    DevBuf* bufs[] = {&c->ops,     &c->paths,   &c->items,   &c->items_w, &c->overflow,
+                      &c->status,  &c->sw_out,  &c->rasters, &c->queue,   &c->scratch,
+                      &c->sw_chain, &c->pool,   &c->pool_used, &c->bandoff, &c->crec};
     for (DevBuf* b : bufs) b->release();
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
@@ -629,6 +631,143 @@ FT_API int ft_fill_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* o
         FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
     }
     return FT_OK;
+}
+
+// Rows per band of the ordered composite: the band count should fill the GPU in
+// one wave of CTAs while each band stays as tall as possible.
+static int composite_band_rows(ft_ctx* c, uint32_t w, uint32_t h) {
+    const char* env = getenv("FT_BAND_ROWS");
+    if (env) return std::max(1, std::min(atoi(env), ftk::NWARP));
+    int best = 1;
+    double best_cost = 1e30;
+    for (int R = ftk::NWARP; R >= 1; R--) {
+        const int smem = ftk::composite_bands_smem(R, (int)w);
+        if (smem > c->max_smem) continue;
+        const int per_sm = std::max(1, (c->max_smem + 1024) / (smem + 1024));
+        const int slots = std::max(1, c->sm_count * per_sm);
+        const int bands = (int)((h + R - 1) / R);
+        const int waves = (bands + slots - 1) / slots;
+        const double cost = (double)waves * R;
+        if (cost < best_cost) {
+            best_cost = cost;
+            best = R;
+        }
+    }
+    return best;
+}
+
+FT_API int ft_composite_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* ops, uint32_t n_ops_total,
+                              const ft_path_desc* paths, uint32_t n_paths, int32_t fmt, uint8_t* raster, uint32_t w,
+                              uint32_t h, uint32_t stride, int32_t where) {
+    if (!c) return FT_ERR_ARG;
+    if ((rule != FT_NONZERO && rule != FT_EVENODD) || (fmt != FT_MATTE8 && fmt != FT_RGBA8P) ||
+        (where != FT_HOST && where != FT_DEVICE))
+        return fail(c, FT_ERR_ARG, "bad rule, format or location");
+    if (stroke) rule = FT_NONZERO;
+    if ((n_paths && !paths) || (n_ops_total && !ops) || (w && h && !raster)) return fail(c, FT_ERR_ARG, "null buffer");
+    if (w > FT_MAX_WIDTH) return fail(c, FT_ERR_CAP, "raster wider than FT_MAX_WIDTH");
+    const uint32_t bpp = fmt == FT_RGBA8P ? 4 : 1;
+    if (h && stride < (uint64_t)w * bpp) return fail(c, FT_ERR_ARG, "stride smaller than a row");
+    if (fmt == FT_RGBA8P && (stride & 3)) return fail(c, FT_ERR_ARG, "Rgba8p rasters need 4-byte aligned rows");
+    for (uint32_t i = 0; i < n_paths; i++)
+        if ((uint64_t)paths[i].op_begin + paths[i].n_ops > n_ops_total)
+            return fail(c, FT_ERR_ARG, "path ops out of range");
+    FT_CU(cudaSetDevice(c->device), "set device");
+    const uint64_t raster_bytes = h ? (uint64_t)(h - 1) * stride + (uint64_t)w * bpp : 0;
+    const ft_op* ops_d = ops;
+    uint8_t* ras_d = raster;
+    if (where == FT_HOST) {
+        if (!valid_ops_host(ops, n_ops_total)) return fail(c, FT_ERR_ARG, "unknown path op kind");
+        FT_CU(c->ops.ensure(sizeof(ft_op) * std::max<uint64_t>(n_ops_total, 1)), "alloc ops");
+        FT_CU(c->rasters.ensure(std::max<uint64_t>(raster_bytes, 1)), "alloc raster");
+        if (n_ops_total)
+            FT_CU(cudaMemcpyAsync(c->ops.p, ops, sizeof(ft_op) * n_ops_total, cudaMemcpyHostToDevice, c->stream),
+                  "upload ops");
+        if (raster_bytes)
+            FT_CU(cudaMemcpyAsync(c->rasters.p, raster, raster_bytes, cudaMemcpyHostToDevice, c->stream),
+                  "upload raster");
+        ops_d = static_cast<const ft_op*>(c->ops.p);
+        ras_d = static_cast<uint8_t*>(c->rasters.p);
+    } else if ((reinterpret_cast<uintptr_t>(ops) & 15) || (fmt == FT_RGBA8P && (reinterpret_cast<uintptr_t>(raster) & 3))) {
+        return fail(c, FT_ERR_ARG, "device ops need 16-byte alignment, Rgba8p rasters 4-byte alignment");
+    }
+    const int R = composite_band_rows(c, w, h);
+    const int n_bands = (int)((h + R - 1) / R);
+    const int smem_b = ftk::composite_bands_smem(R, (int)w);
+    if (smem_b > c->max_smem) return fail(c, FT_ERR_CAP, "raster too wide for the band compositor");
+    const int smem_a = choose_smem(c, 1);
+    if ((size_t)(n_bands + 1) * sizeof(int) > (size_t)smem_a)
+        return fail(c, FT_ERR_CAP, "raster too tall for the band compositor");
+    FT_CU(c->paths.ensure(sizeof(ft_path_desc) * std::max(n_paths, 1u)), "alloc paths");
+    FT_CU(c->status.ensure(sizeof(int32_t) * std::max(n_paths, 1u)), "alloc status");
+    FT_CU(c->queue.ensure(256), "alloc queue");
+    FT_CU(c->crec.ensure(sizeof(int4) * std::max(n_paths, 1u)), "alloc path records");
+    FT_CU(c->bandoff.ensure(sizeof(int) * (size_t)std::max(n_paths, 1u) * (n_bands + 1)), "alloc band offsets");
+    FT_CU(c->pool_used.ensure(sizeof(unsigned long long)), "alloc pool counter");
+    const int grid = std::max(1, std::min((int)std::max(n_paths, 1u),
+                                          c->sm_count * ftk::composite_build_blocks_per_sm(smem_a, stroke != 0)));
+    FT_CU(c->scratch.ensure(ftk::SCRATCH_BYTES_PER_CTA * (size_t)grid), "alloc scratch");
+    if (n_paths)
+        FT_CU(cudaMemcpyAsync(c->paths.p, paths, sizeof(ft_path_desc) * n_paths, cudaMemcpyHostToDevice, c->stream),
+              "upload paths");
+    // edge pool: grows until every path's binned edges fit
+    const char* penv = getenv("FT_POOL_EDGES");  // first pool size in edges (it grows on demand)
+    uint64_t want = penv ? std::max<uint64_t>(strtoull(penv, nullptr, 10), 1)
+                         : std::max<uint64_t>((uint64_t)n_ops_total * 64, 1u << 20);
+    for (int attempt = 0; attempt < 4; attempt++) {
+        if (!penv || attempt > 0) want = std::max<uint64_t>(want, c->pool.cap / sizeof(ftk::EdgeRec));
+        if (penv && attempt == 0 && c->pool.cap > want * sizeof(ftk::EdgeRec)) c->pool.release();
+        FT_CU(c->pool.ensure(want * sizeof(ftk::EdgeRec)), "alloc edge pool");
+        FT_CU(cudaMemsetAsync(c->queue.p, 0, 256, c->stream), "reset queue");
+        FT_CU(cudaMemsetAsync(c->status.p, 0, sizeof(int32_t) * std::max(n_paths, 1u), c->stream), "reset status");
+        FT_CU(cudaMemsetAsync(c->pool_used.p, 0, sizeof(unsigned long long), c->stream), "reset pool");
+        ftk::KParams p;
+        fill_params(c, p, stroke, rule, fmt, smem_a);
+        p.ops = ops_d;
+        p.paths = static_cast<const ft_path_desc*>(c->paths.p);
+        p.n_items = n_paths;
+        p.queue = static_cast<uint32_t*>(c->queue.p);
+        p.status = static_cast<int32_t*>(c->status.p);
+        p.scratch = static_cast<unsigned char*>(c->scratch.p);
+        p.rasters = ras_d;
+        p.canvas_w = w;
+        p.canvas_h = h;
+        p.canvas_stride = stride;
+        p.band_rows = R;
+        p.n_bands = n_bands;
+        p.pool = static_cast<ftk::EdgeRec*>(c->pool.p);
+        p.pool_used = static_cast<unsigned long long*>(c->pool_used.p);
+        p.pool_cap = c->pool.cap / sizeof(ftk::EdgeRec);
+        p.bandoff = static_cast<int*>(c->bandoff.p);
+        p.crec = static_cast<int4*>(c->crec.p);
+        FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
+        if (n_paths) {
+            FT_CU(ftk::launch_composite_build(p, grid, smem_a, c->stream), "launch composite build");
+            c->launches++;
+        }
+        unsigned long long used = 0;
+        FT_CU(cudaMemcpyAsync(&used, c->pool_used.p, sizeof(used), cudaMemcpyDeviceToHost, c->stream), "pool size");
+        FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
+        if (used > p.pool_cap) {
+            want = used + used / 4;
+            continue;
+        }
+        if (n_paths && n_bands) {
+            FT_CU(ftk::launch_composite_bands(p, smem_b, c->stream), "launch band compositor");
+            c->launches++;
+        }
+        FT_CU(cudaEventRecord(c->ev1, c->stream), "event");
+        c->timed = true;
+        c->last_n_paths = n_paths;
+        if (where == FT_HOST) {
+            if (raster_bytes)
+                FT_CU(cudaMemcpyAsync(raster, c->rasters.p, raster_bytes, cudaMemcpyDeviceToHost, c->stream),
+                      "download raster");
+            FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
+        }
+        return FT_OK;
+    }
+    return fail(c, FT_ERR_NOMEM, "edge pool did not converge");
 }
 
 FT_API int ft_batch_status(ft_ctx* c, int32_t* status, uint32_t n) {

@@ -1605,6 +1605,308 @@ int raster_max_smem() {
 
 }  // namespace ftk
 
+namespace ftk {
+
+// ===========================================================================
+// Ordered composite of many paths onto one raster: footile's repeated
+// Plotter::fill / Plotter::stroke calls on one Plotter (plotter.rs:339-365).
+//
+// k_cbuild: one CTA per path builds its figure and edges as k_raster does, then
+// bins the edges by raster band into a device pool.  k_cbands: one CTA per band
+// walks the paths in call order; for each it accumulates the band's cell areas,
+// resolves its rows and composites.  Every call of footile composites every pixel
+// from its top row down, alpha 0 included, and SrcOver with alpha 0 maps each
+// premultiplied channel d to ch8_mul(d, 255), which changes only d in 1..15 and
+// is the identity after 15 applications.  So a band keeps, per row, the number of
+// calls so far and, per pixel, the call count at its last covering call: a covered
+// pixel first takes the pending alpha-0 maps from a 16-entry table of powers,
+// uncovered pixels are not touched, and the band ends with one pending flush.
+
+// Bin the built figure's edges by raster band into the pool (block-wide).
+__device__ void bin_edges(const KParams& P, uint32_t path, const CState& S, const EdgeRec* edges, int* hist,
+                          int* tmp) {
+    const int tid = threadIdx.x;
+    const int count = S.count, H = (int)P.canvas_h, R = P.band_rows, nb = P.n_bands;
+    const int tmin = min(S.top_row, 0);
+    const int rb = count > 0 ? max(S.top_row, 0) : H;  // first raster row footile writes
+    for (int b = tid; b < nb; b += BLOCK) hist[b] = 0;
+    __syncthreads();
+    for (int e = tid; e < count; e += BLOCK) {
+        const EdgeRec E = edges[e];
+        if (!E.ed) continue;
+        const int lo = max(E.start_row - tmin, rb), hi = min(E.end_row - tmin, H - 1);
+        for (int b = lo / R; lo <= hi && b <= hi / R; b++) atomicAdd(&hist[b], 1);
+    }
+    __syncthreads();
+    int carry = 0;
+    for (int b0 = 0; b0 < nb; b0 += BLOCK) {
+        const int b = b0 + tid;
+        int tot;
+        const int off = block_excl_sum(b < nb ? hist[b] : 0, tmp, tot);
+        if (b < nb) hist[b] = carry + off;
+        carry += tot;
+    }
+    __shared__ unsigned long long s_base;
+    if (tid == 0) s_base = atomicAdd(P.pool_used, (unsigned long long)carry);
+    __syncthreads();
+    const unsigned long long base = s_base;
+    const bool fits = base + (unsigned long long)carry <= P.pool_cap;
+    int* boff = P.bandoff + (size_t)path * (nb + 1);
+    for (int b = tid; b <= nb; b += BLOCK) boff[b] = fits ? (b < nb ? hist[b] : carry) : 0;
+    if (tid == 0) {
+        P.crec[path] = make_int4(rb, tmin, (int)(unsigned)(base & 0xFFFFFFFFull), (int)(unsigned)(base >> 32));
+        if (!fits) atomicMax(&P.status[path], FT_ERR_CAP);  // the host grows the pool and runs again
+    }
+    __syncthreads();
+    if (fits) {
+        for (int e = tid; e < count; e += BLOCK) {
+            const EdgeRec E = edges[e];
+            if (!E.ed) continue;
+            const int lo = max(E.start_row - tmin, rb), hi = min(E.end_row - tmin, H - 1);
+            for (int b = lo / R; lo <= hi && b <= hi / R; b++) P.pool[base + (unsigned)atomicAdd(&hist[b], 1)] = E;
+        }
+    }
+    __syncthreads();
+}
+
+template <bool STROKE>
+__global__ void __launch_bounds__(BLOCK) k_cbuild(KParams P) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ CState S;
+    __shared__ int s_item;
+    __shared__ int s_tmp3[3 * NWARP];
+    const int tid = threadIdx.x;
+    unsigned char* scr = P.scratch + (size_t)blockIdx.x * SCRATCH_BYTES_PER_CTA;
+    int2* pts = reinterpret_cast<int2*>(scr + SCR_PTS);
+    int* ss = reinterpret_cast<int*>(scr + SCR_SS);
+    EdgeRec* edges = reinterpret_cast<EdgeRec*>(scr + SCR_EDGES);
+    float4* spts = reinterpret_cast<float4*>(scr + SCR_SPTS);
+    SubRec* subs = reinterpret_cast<SubRec*>(scr + SCR_SUBS);
+    BuildSmem& B = *reinterpret_cast<BuildSmem*>(smem);
+    const size_t cs_off = (sizeof(BuildSmem) + 15) & ~(size_t)15;
+    CompactSmem* Cs = reinterpret_cast<CompactSmem*>(smem + cs_off);
+    for (;;) {
+        if (tid == 0) s_item = (int)atomicAdd(&P.queue[0], 1u);
+        __syncthreads();
+        const int it = s_item;
+        __syncthreads();
+        if (it >= (int)P.n_items) break;
+        const ft_path_desc d = P.paths[it];
+        if (STROKE) {
+            int* opi = reinterpret_cast<int*>(smem + cs_off + ((sizeof(CompactSmem) + 15) & ~(size_t)15));
+            build_fill<BlockG, true>(P, d, d.s_width, B, Cs, S, pts, ss, PT_CAP, spts, subs, opi);
+            finish_subs(P, d, S, subs, B.scan);
+            build_outline(P, S, spts, subs, B, *Cs, pts, ss);
+        } else {
+            build_fill<BlockG>(P, d, d.s_width, B, Cs, S, pts, ss, PT_CAP);
+        }
+        if (S.count > 0) {
+            top_and_dir<BlockG>(S, pts, ss, s_tmp3);
+            build_edges<BlockG>(S, pts, ss, edges);
+        }
+        __syncthreads();
+        bin_edges(P, (uint32_t)it, S, edges, reinterpret_cast<int*>(smem), s_tmp3);
+        if (tid == 0 && S.flags) atomicMax(&P.status[it], (S.flags & 1) ? FT_ERR_DEPTH : FT_ERR_ARG);
+        __syncthreads();
+    }
+}
+
+// Shared memory of k_cbands.
+struct BandSmem {
+    RasterSmem Rs;
+    int G[NWARP];                    // calls so far per band row
+    int rb[BLOCK], tmin[BLOCK], o0[BLOCK], o1[BLOCK];
+    unsigned clr[BLOCK];
+    unsigned long long base[BLOCK];
+    unsigned char ftab[16 * 256];    // ftab[k][d] = d after k alpha-0 SrcOver composites
+};
+
+__device__ __forceinline__ unsigned ftab4(const unsigned char* ftab, unsigned d, int k) {
+    const unsigned char* t = ftab + (k << 8);
+    return (unsigned)t[d & 0xFF] | ((unsigned)t[(d >> 8) & 0xFF] << 8) | ((unsigned)t[(d >> 16) & 0xFF] << 16) |
+           ((unsigned)t[d >> 24] << 24);
+}
+
+// Accumulate the cell areas of `n` edges on scan rows [ylo, yhi) of a band whose
+// first scan row is yb0 (area row = y - yb0).  Block-wide.
+__device__ void band_items(const EdgeRec* edges, int n, int yb0, int ylo, int yhi, int* area, int Wp, int W,
+                           RasterSmem& Rs) {
+    const int tid = threadIdx.x;
+    for (int e0 = 0; e0 < n; e0 += BLOCK) {
+        const int e = e0 + tid;
+        int nrow = 0, ya = 0;
+        EdgeRec E;
+        E.ed = 0;
+        if (e < n) {
+            E = edges[e];
+            ya = max(E.start_row, ylo);
+            nrow = max(min(E.end_row, yhi - 1) - ya + 1, 0);
+        }
+        Rs.edges[tid] = E;
+        Rs.ya[tid] = ya;
+        int tot;
+        const int o = block_excl_sum(nrow, Rs.scan, tot);
+        Rs.off[tid] = o;
+        for (int m0 = 0; m0 < tot; m0 += MAP_CAP) {
+            const int ia = max(o, m0), ib = min(o + nrow, m0 + MAP_CAP);
+            for (int k = ia; k < ib; k++) Rs.map[k - m0] = (unsigned char)tid;
+            __syncthreads();
+            const int cnt = min(MAP_CAP, tot - m0);
+            for (int it = tid; it < cnt; it += BLOCK) {
+                const int jj = Rs.map[it];
+                const int y = Rs.ya[jj] + (m0 + it - Rs.off[jj]);
+                scan_item(Rs.edges[jj], y, area + (size_t)(y - yb0) * Wp, W);
+            }
+            __syncthreads();
+        }
+    }
+}
+
+__global__ void __launch_bounds__(BLOCK) k_cbands(KParams P) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    BandSmem& M = *reinterpret_cast<BandSmem*>(smem);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int W = (int)P.canvas_w, H = (int)P.canvas_h, Wp = (W + 3) & ~3;
+    const int R = P.band_rows, nb = P.n_bands, b = blockIdx.x;
+    const int r0 = b * R, r1 = min(r0 + R, H);
+    int* area = reinterpret_cast<int*>(smem + ((sizeof(BandSmem) + 15) & ~(size_t)15));
+    unsigned short* last = reinterpret_cast<unsigned short*>(area + (size_t)R * Wp);
+    for (int i = tid; i < R * Wp / 4; i += BLOCK) reinterpret_cast<int4*>(area)[i] = make_int4(0, 0, 0, 0);
+    for (int i = tid; i < R * Wp; i += BLOCK) last[i] = 0;
+    for (int i = tid; i < 16 * 256; i += BLOCK) {
+        unsigned v = (unsigned)(i & 255);
+        for (int k = 0; k < (i >> 8); k++) v = ch8_mul(v, 255u);
+        M.ftab[i] = (unsigned char)v;
+    }
+    if (tid < NWARP) M.G[tid] = 0;
+    __syncthreads();
+    const bool rgba = P.fmt == FT_RGBA8P;
+    const int n_paths = (int)P.n_items;
+    for (int c0 = 0; c0 < n_paths; c0 += BLOCK) {
+        const int i = c0 + tid;
+        if (i < n_paths) {
+            const int4 cr = P.crec[i];
+            const int* boff = P.bandoff + (size_t)i * (nb + 1);
+            M.rb[tid] = cr.x;
+            M.tmin[tid] = cr.y;
+            M.base[tid] = (unsigned long long)(unsigned)cr.z | ((unsigned long long)(unsigned)cr.w << 32);
+            M.o0[tid] = boff[b];
+            M.o1[tid] = boff[b + 1];
+            const ft_path_desc& d = P.paths[i];
+            M.clr[tid] = (unsigned)d.clr[0] | ((unsigned)d.clr[1] << 8) | ((unsigned)d.clr[2] << 16) |
+                         ((unsigned)d.clr[3] << 24);
+        }
+        __syncthreads();
+        const int nk = min(BLOCK, n_paths - c0);
+        for (int k = 0; k < nk; k++) {
+            const int rb = M.rb[k];
+            if (rb >= r1) continue;  // this call writes no row of the band
+            const int ya = max(r0, rb);
+            const int ne = M.o1[k] - M.o0[k];
+            if (rgba && ne == 0) {
+                // only alpha 0 on these rows: one more pending map per row
+                if (lane == 0 && r0 + warp < r1 && r0 + warp >= ya) M.G[warp]++;
+                continue;
+            }
+            const int tmin = M.tmin[k];
+            if (ne > 0)
+                band_items(P.pool + M.base[k] + M.o0[k], ne, r0 + tmin, ya + tmin, r1 + tmin, area, Wp, W, M.Rs);
+            // resolve and composite the rows from ya (one warp per row)
+            const int rr = r0 + warp;
+            if (rr < r1) {
+                int* arow = area + (size_t)warp * Wp;
+                unsigned short* lrow = last + (size_t)warp * Wp;
+                uint8_t* drow = P.rasters + (size_t)rr * P.canvas_stride;
+                const int G = M.G[warp];
+                const unsigned clr = M.clr[k];
+                if (rr >= ya) {
+                    unsigned carry = 0;
+                    for (int x0 = 0; x0 < W; x0 += 128) {
+                        const int x = x0 + lane * 4;
+                        int4 a = make_int4(0, 0, 0, 0);
+                        if (x < Wp) {
+                            a = *reinterpret_cast<const int4*>(arow + x);
+                            *reinterpret_cast<int4*>(arow + x) = make_int4(0, 0, 0, 0);
+                        }
+                        const unsigned s0 = (unsigned)a.x, s1 = s0 + (unsigned)a.y, s2 = s1 + (unsigned)a.z,
+                                       s3 = s2 + (unsigned)a.w;
+                        const unsigned inc = warp_incl_sum_u(s3);
+                        const unsigned ex = inc - s3 + carry;
+                        carry += __shfl_sync(FULL, inc, 31);
+                        const unsigned av[4] = {resolve_cov(s0 + ex, P.rule), resolve_cov(s1 + ex, P.rule),
+                                                resolve_cov(s2 + ex, P.rule), resolve_cov(s3 + ex, P.rule)};
+#pragma unroll
+                        for (int c = 0; c < 4; c++) {
+                            const int xc = x + c;
+                            if (xc >= W) break;
+                            if (!rgba) {
+                                drow[xc] = (uint8_t)av[c];  // Matte8 rows are overwritten (fig.rs:629-636)
+                            } else if (av[c]) {
+                                unsigned* dp = reinterpret_cast<unsigned*>(drow) + xc;
+                                unsigned dv = *dp;
+                                const int kk = min(G - (int)lrow[xc], 15);
+                                if (kk) dv = ftab4(M.ftab, dv, kk);
+                                *dp = srcover_rgba(dv, clr, av[c]);
+                                lrow[xc] = (unsigned short)(G + 1);
+                            }
+                        }
+                    }
+                    if (lane == 0) M.G[warp] = G + 1;
+                } else if (ne > 0) {
+                    // rows above this call's top row: no composite, clear any areas
+                    for (int x = lane * 4; x < Wp; x += 128)
+                        *reinterpret_cast<int4*>(arow + x) = make_int4(0, 0, 0, 0);
+                }
+            }
+            __syncthreads();
+        }
+        __syncthreads();
+    }
+    if (rgba) {
+        // the alpha-0 composites still pending since each pixel's last cover
+        const int rr = r0 + warp;
+        if (rr < r1) {
+            const int G = M.G[warp];
+            unsigned short* lrow = last + (size_t)warp * Wp;
+            unsigned* drow = reinterpret_cast<unsigned*>(P.rasters + (size_t)rr * P.canvas_stride);
+            for (int x = lane; x < W; x += 32) {
+                const int kk = min(G - (int)lrow[x], 15);
+                if (kk) drow[x] = ftab4(M.ftab, drow[x], kk);
+            }
+        }
+    }
+}
+
+int composite_bands_smem(int band_rows, int width) {
+    const int wp = (width + 3) & ~3;
+    return (int)(((sizeof(BandSmem) + 15) & ~(size_t)15) + (size_t)band_rows * wp * (4 + 2));
+}
+
+cudaError_t launch_composite_build(const KParams& p, int grid, int smem_bytes, cudaStream_t s) {
+    auto kern = p.stroke ? k_cbuild<true> : k_cbuild<false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+    if (e != cudaSuccess) return e;
+    kern<<<grid, BLOCK, smem_bytes, s>>>(p);
+    return cudaGetLastError();
+}
+
+int composite_build_blocks_per_sm(int smem_bytes, bool stroke) {
+    auto kern = stroke ? k_cbuild<true> : k_cbuild<false>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, BLOCK, smem_bytes) != cudaSuccess) return 1;
+    return n > 0 ? n : 1;
+}
+
+cudaError_t launch_composite_bands(const KParams& p, int smem_bytes, cudaStream_t s) {
+    cudaError_t e = cudaFuncSetAttribute(k_cbands, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+    if (e != cudaSuccess) return e;
+    k_cbands<<<p.n_bands, BLOCK, smem_bytes, s>>>(p);
+    return cudaGetLastError();
+}
+
+}  // namespace ftk
+
 // ===========================================================================
 // Allocation-free single-path fill (ft_fill_noalloc).
 //

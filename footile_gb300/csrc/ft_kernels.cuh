@@ -86,7 +86,22 @@ struct KParams {
     int fmt;
     int stroke;
     int smem_bytes;
+    // ordered composite of all paths onto one raster (ft_composite_batch)
+    uint32_t canvas_w, canvas_h, canvas_stride;
+    int band_rows;               // rows per band
+    int n_bands;
+    EdgeRec* pool;               // binned edges of all paths
+    unsigned long long* pool_used;  // bump counter (edges)
+    unsigned long long pool_cap;    // edges
+    int* bandoff;                // per path: n_bands + 1 offsets into its pool run
+    int4* crec;                  // per path: rowbegin, tmin, pool offset lo, pool offset hi
 };
+
+// Ordered composite: per-path figure build and edge binning, then one CTA per band.
+cudaError_t launch_composite_build(const KParams& p, int grid, int smem_bytes, cudaStream_t s);
+cudaError_t launch_composite_bands(const KParams& p, int smem_bytes, cudaStream_t s);
+int composite_bands_smem(int band_rows, int width);
+int composite_build_blocks_per_sm(int smem_bytes, bool stroke);
 
 // Static shared memory of the kernel besides the dynamic area buffer.
 constexpr int RASTER_FIXED_SMEM = BLOCK * (int)sizeof(EdgeRec) + 3 * BLOCK * 4 + 256 + 4096;

@@ -229,3 +229,51 @@ class PreparedBatch:
             self.close()
         except Exception:
             pass
+
+
+def pen_width_chain(ops, paths, s_width=1.0):
+    """Pen width at the start of each call of a sequence of Plotter calls: footile
+    keeps the last PenWidth from call to call (plotter.rs:151-153)."""
+    ops = np.asarray(ops, dtype=_abi.OP_DTYPE)
+    out = np.empty(len(paths), np.float32)
+    pw = np.flatnonzero(ops["kind"] == _abi.OP_PEN_WIDTH)
+    cur = np.float32(s_width)
+    for i, d in enumerate(paths):
+        out[i] = cur
+        b, n = int(d["op_begin"]), int(d["n_ops"])
+        k = np.searchsorted(pw, b + n) - 1
+        if k >= 0 and pw[k] >= b:
+            cur = ops["v"][pw[k], 0]
+    return out, cur
+
+
+def composite_batch(ctx, ops, paths, fmt, raster, rule=FillRule.NonZero, stroke=False, s_width=None):
+    """Draw every path onto one raster in order (`ft_composite_batch`), as a
+    sequence of Plotter::fill / Plotter::stroke calls on one Plotter would.
+
+    `raster` is an (h, w) Matte8 or (h, w, 4) Rgba8p numpy array (host) or CUDA
+    tensor (device).  Path colours come from `paths["clr"]`.  With host ops the pen
+    width chain is computed here, starting from the context's pen width (or
+    `s_width`); the context's pen width is left at the sequence's final value.
+    Returns the per-path status array."""
+    paths = np.array(paths, dtype=_abi.PATH_DTYPE)
+    h, w = int(raster.shape[0]), int(raster.shape[1])
+    if _is_torch_cuda(raster):
+        where = _abi.DEVICE
+        optr, n_ops = ops.data_ptr(), ops.numel() * ops.element_size() // 32
+        rptr = raster.data_ptr()
+        stride = int(raster.stride(0)) * raster.element_size()
+    else:
+        where = _abi.HOST
+        ops = np.ascontiguousarray(ops, dtype=_abi.OP_DTYPE)
+        optr, n_ops = ops.ctypes.data, len(ops)
+        rptr = raster.ctypes.data
+        stride = int(raster.strides[0])
+        start = ctx.pen_width() if s_width is None else s_width
+        paths["s_width"], last = pen_width_chain(ops, paths, start)
+        ctx.set_pen_width(float(last))
+    rc = ctx.L.ft_composite_batch(ctx.h, int(bool(stroke)), int(rule), ctypes.c_void_p(optr), n_ops,
+                                  paths.ctypes.data_as(ctypes.c_void_p), len(paths), fmt, ctypes.c_void_p(rptr),
+                                  w, h, stride, where)
+    ctx.check(rc)
+    return ctx.batch_status(len(paths))

@@ -142,6 +142,20 @@ FT_API int ft_fill_batch(ft_ctx* ctx, int32_t stroke, int32_t rule, const ft_op*
                          uint32_t n_paths, int32_t fmt, uint8_t* rasters,
                          uint64_t raster_bytes, int32_t where);
 
+/* Ordered composite: footile's sequence of Plotter calls on ONE raster.  Path i is
+ * filled (stroke == 0, with `rule`) or stroked (stroke == 1) onto `raster` after
+ * paths 0..i-1, with its own colour `paths[i].clr` and starting pen width
+ * `paths[i].s_width` (footile carries the pen width from call to call, so set it to
+ * the last PenWidth of the calls before, as the Python and C++ mirrors do).  The
+ * width/height/offset/stride fields of `paths` are ignored: every path draws on the
+ * w x h raster with `stride`.  Bit-identical to the calls made one after another,
+ * including the alpha-0 SrcOver every call applies from its top row down.
+ * Per-path status as for batches (ft_batch_status). */
+FT_API int ft_composite_batch(ft_ctx* ctx, int32_t stroke, int32_t rule, const ft_op* ops,
+                              uint32_t n_ops_total, const ft_path_desc* paths, uint32_t n_paths,
+                              int32_t fmt, uint8_t* raster, uint32_t w, uint32_t h, uint32_t stride,
+                              int32_t where);
+
 /* Prepared batches: the path descriptors and the planned work queue stay on the
  * device, and each launch replays a captured CUDA graph (queue reset, status reset,
  * persistent rasteriser).  `ops` / `rasters` given to ft_batch_launch are device

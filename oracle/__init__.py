@@ -80,6 +80,9 @@ def lib():
             L.orc_sinf.restype = ctypes.c_float
             L.orc_fill_batch.argtypes = [i32, i32, P, P, u32, i32, P, ctypes.POINTER(Params), P, i32]
             L.orc_fill_batch.restype = ctypes.c_int
+            L.orc_composite.argtypes = [i32, i32, P, P, u32, i32, P, u32, u32, u32, ctypes.POINTER(Params),
+                                        ctypes.POINTER(ctypes.c_float), P]
+            L.orc_composite.restype = ctypes.c_int
             _lib = L
     return _lib
 
@@ -191,3 +194,15 @@ def atan2f(y, x):
 
 def sinf(x):
     return lib().orc_sinf(x)
+
+
+def composite(stroke, rule, ops, paths, fmt, raster, s_width=1.0, **params):
+    """Plotter calls one after another on one raster; returns (status array, s_width)."""
+    ops = np.ascontiguousarray(ops, dtype=_abi.OP_DTYPE)
+    paths = np.ascontiguousarray(paths, dtype=_abi.PATH_DTYPE)
+    status = np.zeros(len(paths), dtype=np.int32)
+    sw = ctypes.c_float(s_width)
+    h, w = raster.shape[0], raster.shape[1]
+    lib().orc_composite(stroke, rule, _ptr(ops), _ptr(paths), len(paths), fmt, _ptr(raster), w, h,
+                        raster.strides[0], ctypes.byref(make_params(**params)), ctypes.byref(sw), _ptr(status))
+    return status, sw.value

@@ -899,6 +899,24 @@ __attribute__((visibility("default"))) int32_t orc_widdershins(int32_t ax, int32
 __attribute__((visibility("default"))) float orc_atan2f(float y, float x) { return ft_atan2f(y, x); }
 __attribute__((visibility("default"))) float orc_sinf(float x) { return ft_sinf(x); }
 
+// A sequence of Plotter calls on one raster (ft_composite_batch semantics): path i
+// draws after paths 0..i-1 with its own colour; the pen width carries from call to
+// call starting at *s_width_inout.
+__attribute__((visibility("default"))) int orc_composite(int32_t stroke, int32_t rule, const ft_op* ops,
+                                                         const ft_path_desc* paths, uint32_t n_paths, int32_t fmt,
+                                                         uint8_t* raster, uint32_t w, uint32_t h, uint32_t stride,
+                                                         const orc_params* prm, float* s_width_inout,
+                                                         int32_t* status) {
+    float sw = s_width_inout ? *s_width_inout : 1.0f;
+    for (uint32_t i = 0; i < n_paths; i++) {
+        const ft_path_desc& d = paths[i];
+        int st = orc_run(stroke, rule, ops + d.op_begin, d.n_ops, fmt, d.clr, raster, w, h, stride, prm, &sw);
+        if (status) status[i] = st;
+    }
+    if (s_width_inout) *s_width_inout = sw;
+    return 0;
+}
+
 // A batch of independent Plotter calls (ft_fill_batch semantics) on `n_threads`
 // host threads, one Plotter per path.  Statuses go to `status` (may be NULL).
 __attribute__((visibility("default"))) int orc_fill_batch(int32_t stroke, int32_t rule, const ft_op* ops,

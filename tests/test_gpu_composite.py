@@ -1,0 +1,95 @@
+"""Ordered composite: many Plotter calls on ONE raster, in order (footile's
+Plotter::stroke / Plotter::fill called repeatedly, plotter.rs:339-365), on the GPU
+against the oracle's calls one after another, bit-exact.  Every call composites all
+pixels from its top row down (alpha 0 too, fig.rs:637-643), so the test canvases
+start with random bytes and colours with small channel values, where SrcOver with
+alpha 0 changes the destination."""
+import numpy as np
+import pytest
+
+import oracle
+from footile_gb300 import _abi, workloads
+from footile_gb300.path import PathOp, ops_array
+from footile_gb300.plotter import composite_batch, pack_batch
+from helpers import assert_same
+
+pytestmark = pytest.mark.gpu
+
+
+def _scene(seed, n_paths, w, h, stroke, small_colours=True):
+    rng = np.random.default_rng(seed)
+    paths_ops, clrs = [], []
+    for i in range(n_paths):
+        o = workloads.random_path(rng, max(w, h), int(rng.integers(1, 12)), close=not stroke or bool(i % 3 == 0),
+                                  probs=(0.2, 0.3, 0.5))
+        if stroke and i % 4 != 3:
+            o = np.concatenate([ops_array([PathOp.PenWidth(float(rng.uniform(1, 12)))]), o])
+        paths_ops.append(o)
+        a = int(rng.integers(64, 256))
+        rgb = rng.integers(0, 24 if small_colours else 256, 3)
+        clrs.append([int(v) * a // 255 for v in rgb] + [a])
+    ops, paths, _ = pack_batch(paths_ops, [(w, h)] * n_paths, _abi.RGBA8P, clrs)
+    init = rng.integers(0, 256, (h, w, 4)).astype(np.uint8)
+    return ops, paths, init
+
+
+@pytest.mark.parametrize("stroke", [True, False])
+@pytest.mark.parametrize("seed", range(3))
+def test_composite_rgba(ctx, stroke, seed):
+    ops, paths, init = _scene(40 + seed, 48, 200 + 13 * seed, 150, stroke)
+    want = init.copy()
+    st_o, sw_o = oracle.composite(int(stroke), _abi.NONZERO, ops, paths, _abi.RGBA8P, want, s_width=1.0)
+    got = init.copy()
+    ctx.set_pen_width(1.0)
+    st = composite_batch(ctx, ops, paths, _abi.RGBA8P, got, stroke=stroke)
+    assert (st == st_o).all()
+    assert_same(got, want, f"stroke={stroke} seed={seed}")
+    assert ctx.pen_width() == sw_o
+
+
+@pytest.mark.parametrize("band_rows", ["1", "3", "8"])
+def test_composite_band_heights(ctx, band_rows, monkeypatch):
+    monkeypatch.setenv("FT_BAND_ROWS", band_rows)
+    ops, paths, init = _scene(7, 30, 97, 61, True)
+    want = init.copy()
+    oracle.composite(1, _abi.NONZERO, ops, paths, _abi.RGBA8P, want)
+    got = init.copy()
+    ctx.set_pen_width(1.0)
+    composite_batch(ctx, ops, paths, _abi.RGBA8P, got, stroke=True)
+    assert_same(got, want, f"band rows {band_rows}")
+
+
+def test_composite_matte8_evenodd(ctx):
+    ops, paths, _ = _scene(3, 40, 120, 90, False)
+    init = np.random.default_rng(1).integers(0, 256, (90, 120)).astype(np.uint8)
+    want = init.copy()
+    oracle.composite(0, _abi.EVENODD, ops, paths, _abi.MATTE8, want)
+    got = init.copy()
+    composite_batch(ctx, ops, paths, _abi.MATTE8, got, rule=_abi.EVENODD)
+    assert_same(got, want, "matte8 even-odd")
+
+
+def test_composite_pool_grows(ctx, monkeypatch):
+    # a tiny first edge pool forces the build to overflow and run again
+    monkeypatch.setenv("FT_POOL_EDGES", "500")
+    ops, paths, init = _scene(11, 24, 150, 110, True)
+    want = init.copy()
+    oracle.composite(1, _abi.NONZERO, ops, paths, _abi.RGBA8P, want)
+    got = init.copy()
+    ctx.set_pen_width(1.0)
+    st = composite_batch(ctx, ops, paths, _abi.RGBA8P, got, stroke=True)
+    assert (st == 0).all()
+    assert_same(got, want, "pool growth")
+
+
+def test_composite_device_buffers(ctx):
+    torch = pytest.importorskip("torch")
+    ops, paths, init = _scene(21, 64, 256, 256, True, small_colours=False)
+    want = init.copy()
+    _, sw = oracle.composite(1, _abi.NONZERO, ops, paths, _abi.RGBA8P, want)
+    from footile_gb300.plotter import pen_width_chain
+    paths["s_width"], _ = pen_width_chain(ops, paths, 1.0)
+    ops_d = torch.from_numpy(ops.view(np.uint8)).cuda()
+    ras_d = torch.from_numpy(init).cuda()
+    composite_batch(ctx, ops_d, paths, _abi.RGBA8P, ras_d, stroke=True)
+    assert_same(ras_d.cpu().numpy(), want, "device composite")
