@@ -46,7 +46,136 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
     ap.add_argument("--per-path-sample", type=int, default=4096)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the secondary workloads")
+    ap.add_argument("--only", choices=["single", "scene", "strokes"],
+                    help="run one secondary workload alone (for profiling) and print its line")
     return ap.parse_args()
+
+
+def _events_ms(stream, fn, reps):
+    """Mean device time of fn() over `reps` calls, CUDA events on `stream`."""
+    import torch
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def extra_single(ctx, stream, dev, cpu=True):
+    """One closed 64-segment path on 256x256 (Matte8 and Rgba8p), per call."""
+    import ctypes
+    import torch
+    from footile_gb300 import _abi, workloads
+    ops, w, h, clr = workloads.single_path_256()
+    ops_d = torch.from_numpy(ops.view(np.uint8)).to(dev)
+    m_d = torch.zeros((h, w), dtype=torch.uint8, device=dev)
+    r_d = torch.zeros((h, w, 4), dtype=torch.uint8, device=dev)
+    c = (ctypes.c_uint8 * 4)(*[int(v) for v in clr])
+    L = ctx.L
+
+    def fill(fmt, buf, stride):
+        ctx.check(L.ft_fill(ctx.h, _abi.NONZERO, ctypes.c_void_p(ops_d.data_ptr()), len(ops), fmt, c,
+                            ctypes.c_void_p(buf.data_ptr()), w, h, stride, _abi.DEVICE))
+    for _ in range(5):
+        fill(_abi.MATTE8, m_d, w)
+    out = {"workload": "single_path_256 (64 mixed segments, 256x256, NonZero)",
+           "matte8_us_per_call": 1e3 * _events_ms(stream, lambda: fill(_abi.MATTE8, m_d, w), 50),
+           "rgba8p_us_per_call": 1e3 * _events_ms(stream, lambda: fill(_abi.RGBA8P, r_d, 4 * w), 50)}
+    if cpu:
+        import oracle
+        r = np.zeros((h, w), np.uint8)
+        t0 = time.perf_counter()
+        for _ in range(50):
+            oracle.fill(_abi.NONZERO, ops, r, _abi.MATTE8)
+        out["cpu_oracle_us_per_call_1thread"] = (time.perf_counter() - t0) / 50 * 1e6
+    return out
+
+
+def extra_scene(ctx, stream, dev, cpu=True):
+    """One 4096x4096 scene of 1,000 sub-paths x 100 segments: NonZero, EvenOdd, stroke."""
+    import ctypes
+    import torch
+    from footile_gb300 import _abi, workloads
+    from footile_gb300.path import PathOp, ops_array
+    ops, w, h, clr = workloads.scene_4096()
+    sops = np.concatenate([ops_array([PathOp.PenWidth(8.0)]), ops])
+    ops_d = torch.from_numpy(ops.view(np.uint8)).to(dev)
+    sops_d = torch.from_numpy(sops.view(np.uint8)).to(dev)
+    m_d = torch.zeros((h, w), dtype=torch.uint8, device=dev)
+    r_d = torch.zeros((h, w, 4), dtype=torch.uint8, device=dev)
+    c = (ctypes.c_uint8 * 4)(*[int(v) for v in clr])
+    L = ctx.L
+
+    def fill(rule, fmt, buf, stride):
+        ctx.check(L.ft_fill(ctx.h, rule, ctypes.c_void_p(ops_d.data_ptr()), len(ops), fmt, c,
+                            ctypes.c_void_p(buf.data_ptr()), w, h, stride, _abi.DEVICE))
+
+    def stroke():
+        ctx.check(L.ft_stroke(ctx.h, ctypes.c_void_p(sops_d.data_ptr()), len(sops), _abi.MATTE8, c,
+                              ctypes.c_void_p(m_d.data_ptr()), w, h, w, _abi.DEVICE))
+    fill(_abi.NONZERO, _abi.MATTE8, m_d, w)
+    out = {"workload": "scene_4096 (1,000 sub-paths x 100 segments; 65,535-vertex figure cap)",
+           "nonzero_matte8_ms": _events_ms(stream, lambda: fill(_abi.NONZERO, _abi.MATTE8, m_d, w), 5),
+           "evenodd_matte8_ms": _events_ms(stream, lambda: fill(_abi.EVENODD, _abi.MATTE8, m_d, w), 5),
+           "nonzero_rgba8p_ms": _events_ms(stream, lambda: fill(_abi.NONZERO, _abi.RGBA8P, r_d, 4 * w), 5)}
+    ctx.set_join(_abi.JOIN_ROUND, 0.0)
+    stroke()
+    out["stroke_w8_round_matte8_ms"] = _events_ms(stream, stroke, 3)
+    ctx.set_join(_abi.JOIN_MITER, 4.0)
+    # composite bytes: every Rgba8p pixel from the top row down is read and written
+    out["rgba8p_composite_GBps"] = (w * h * 8) / (out["nonzero_rgba8p_ms"] * 1e-3) / 1e9
+    if cpu:
+        import oracle
+        m = np.zeros((h, w), np.uint8)
+        t0 = time.perf_counter()
+        oracle.fill(_abi.NONZERO, ops, m, _abi.MATTE8)
+        out["cpu_oracle_nonzero_ms_1thread"] = (time.perf_counter() - t0) * 1e3
+        t0 = time.perf_counter()
+        oracle.stroke(sops, m, _abi.MATTE8, join=_abi.JOIN_ROUND, miter_limit=0.0)
+        out["cpu_oracle_stroke_ms_1thread"] = (time.perf_counter() - t0) * 1e3
+    return out
+
+
+def extra_strokes(ctx, stream, dev, cpu=True, reps=2):
+    """16,384 open cubic strokes (pen width 1..12, Miter(4)) composited in order onto
+    one 2048x2048 Rgba8p canvas (ft_composite_batch)."""
+    import torch
+    from footile_gb300 import _abi, workloads
+    from footile_gb300.plotter import composite_batch, pack_batch, pen_width_chain
+    paths_ops, widths, clrs, side = workloads.strokes_16384()
+    ops, paths, _ = pack_batch(paths_ops, [side] * len(paths_ops), _abi.RGBA8P, clrs)
+    paths["s_width"], _ = pen_width_chain(ops, paths, 1.0)
+    ops_d = torch.from_numpy(ops.view(np.uint8)).to(dev)
+    ras_d = torch.zeros((side, side, 4), dtype=torch.uint8, device=dev)
+    ctx.set_join(_abi.JOIN_MITER, 4.0)
+
+    def run():
+        composite_batch(ctx, ops_d, paths, _abi.RGBA8P, ras_d, stroke=True)
+    run()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        run()
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) / reps * 1e3
+    out = {"workload": "strokes_16384 (8..64 cubics each, width 1..12, ordered SrcOver on 2048x2048 Rgba8p)",
+           "ms_per_composite": ms, "paths_per_s": len(paths) / (ms * 1e-3),
+           "canvas_Mpx_per_s": side * side / (ms * 1e-3) / 1e6}
+    if cpu:
+        # the reference composites every pixel from each call's top row down: time a few calls
+        import oracle
+        n = 8
+        canvas = np.zeros((side, side, 4), np.uint8)
+        t0 = time.perf_counter()
+        oracle.composite(1, _abi.NONZERO, ops, paths[:n], _abi.RGBA8P, canvas)
+        per = (time.perf_counter() - t0) / n
+        out["cpu_oracle_ms_per_call_1thread"] = per * 1e3
+        out["cpu_oracle_estimated_s_for_all_16384"] = per * len(paths)
+    return out
 
 
 def dist_env():
@@ -194,6 +323,18 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def run_only(args):
+    import torch
+    from footile_gb300._lib import Context
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    ctx = Context(0)
+    ctx.set_stream(stream.cuda_stream)
+    fn = {"single": extra_single, "scene": extra_scene, "strokes": extra_strokes}[args.only]
+    print(json.dumps(fn(ctx, stream, dev, cpu=not args.no_cpu)), flush=True)
+
+
 def run_ours(args):
     import torch
     rank, world, local = dist_env()
@@ -302,6 +443,17 @@ def run_ours(args):
         per_path = {"paths_per_s": n / dt, "mpx_per_s": sub_px / dt / 1e6, "sample_paths": n,
                     "launches_per_path": 1}
 
+    # ---- the other configurations, on rank 0 (device time, CUDA events)
+    extras = None
+    if rank == 0 and not args.no_extras:
+        extras = {}
+        for name, fn in (("single_path_256", extra_single), ("scene_4096", extra_scene),
+                         ("strokes_16384", extra_strokes)):
+            try:
+                extras[name] = fn(ctx, stream, dev, cpu=(world == 1 and not args.no_cpu))
+            except Exception as e:  # report, never hide, a failing secondary workload
+                extras[name] = {"error": repr(e)}
+
     # ---- CPU baseline (rank 0, N=1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -330,6 +482,7 @@ def run_ours(args):
                   "batched_over_per_path": (len(paths) / (ms_max * 1e-3) / per_path["paths_per_s"]) if per_path else None},
         "clocks": clk,
         "gpu_launches": int(launches),
+        "workloads": extras,
     }
     print(json.dumps(out), flush=True)
 
@@ -338,6 +491,8 @@ def main():
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.only:
+        run_only(args)
     else:
         run_ours(args)
 

@@ -63,6 +63,10 @@ struct ft_ctx {
     std::string err;
 };
 
+static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* ops, uint32_t n_ops_total,
+                          const ft_path_desc* paths, uint32_t n_paths, int32_t fmt, uint8_t* raster, uint32_t w,
+                          uint32_t h, uint32_t stride, int32_t where, float* sw_out);
+
 namespace {
 
 int fail(ft_ctx* c, int code, const std::string& msg) {
@@ -116,7 +120,9 @@ void plan_items(ft_ctx* c, const ft_path_desc* paths, uint32_t n_paths, int smem
     const int area_bytes = smem - ftk::RASTER_FIXED_SMEM;
     const char* env = getenv("FT_SPLIT_PX");
     const uint64_t split_px = env ? strtoull(env, nullptr, 10) : (uint64_t)(1u << 20);
-    const uint32_t wside = stroke ? 0u : (uint32_t)warp_max_side();  // strokes use the CTA kernel
+    // few paths cannot fill the GPU one warp or one CTA each: split their rows instead
+    const bool few = n_paths < (uint32_t)std::max(2 * c->sm_count, 1);
+    const uint32_t wside = (stroke || few) ? 0u : (uint32_t)warp_max_side();  // strokes use the CTA kernel
     for (uint32_t i = 0; i < n_paths; i++) {
         const ft_path_desc& d = paths[i];
         const uint32_t wp = (d.width + 3) & ~3u;
@@ -130,6 +136,10 @@ void plan_items(ft_ctx* c, const ft_path_desc* paths, uint32_t n_paths, int smem
         if ((uint64_t)d.width * d.height >= split_px && c->sm_count > 0) {
             uint32_t target = (d.height + (uint32_t)c->sm_count - 1) / (uint32_t)c->sm_count;
             rows_per_item = std::max(R, ((target + R - 1) / R) * R);
+        } else if (few && c->sm_count > 0) {
+            // every item rebuilds the figure, so keep items at least 16 rows tall
+            const uint32_t parts = std::max(1u, (uint32_t)(2 * c->sm_count) / std::max(n_paths, 1u));
+            rows_per_item = std::max(16u, (d.height + parts - 1) / parts);
         }
         for (uint32_t r = 0; r < std::max(d.height, 1u); r += rows_per_item)
             out.push_back(ftk::WorkItem{i, r, std::min(d.height, r + rows_per_item), R});
@@ -315,7 +325,19 @@ int single(ft_ctx* c, int stroke, int32_t rule, const ft_op* ops, uint32_t n_ops
     } else if ((reinterpret_cast<uintptr_t>(ops) & 15) || (fmt == FT_RGBA8P && (reinterpret_cast<uintptr_t>(raster) & 3))) {
         return fail(c, FT_ERR_ARG, "device ops need 16-byte alignment, Rgba8p rasters 4-byte alignment");
     }
-    st = run(c, stroke, rule, ops_d, &d, 1, fmt, ras_d, swd, swd + 1);
+    const char* env = getenv("FT_SPLIT_PX");
+    const uint64_t big_px = env ? strtoull(env, nullptr, 10) : (uint64_t)(1u << 20);
+    if ((uint64_t)w * h >= big_px && ftk::composite_bands_smem(1, (int)w) <= c->max_smem) {
+        // a large canvas: build the figure once and bin its edges, then one CTA per
+        // band of rows (the ordered compositor with a single call)
+        float sw0 = c->s_width;
+        FT_CU(cudaMemcpyAsync(&sw0, swd, sizeof(float), cudaMemcpyDeviceToHost, c->stream), "pen width");
+        FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
+        d.s_width = sw0;
+        st = composite_impl(c, stroke, rule, ops_d, n_ops, &d, 1, fmt, ras_d, w, h, stride, FT_DEVICE, swd + 1);
+    } else {
+        st = run(c, stroke, rule, ops_d, &d, 1, fmt, ras_d, swd, swd + 1);
+    }
     if (st != FT_OK) return st;
     FT_CU(cudaMemcpyAsync(swd, swd + 1, sizeof(float), cudaMemcpyDeviceToDevice, c->stream), "pen width");
     if (where == FT_HOST) {
@@ -633,32 +655,28 @@ FT_API int ft_fill_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* o
     return FT_OK;
 }
 
-// Rows per band of the ordered composite: the band count should fill the GPU in
-// one wave of CTAs while each band stays as tall as possible.
+// Rows per band of the ordered composite = warps of a compositor CTA (one row each):
+// as many as the shared memory holds, at most eight.
 static int composite_band_rows(ft_ctx* c, uint32_t w, uint32_t h) {
+    (void)h;
     const char* env = getenv("FT_BAND_ROWS");
-    if (env) return std::max(1, std::min(atoi(env), ftk::NWARP));
-    int best = 1;
-    double best_cost = 1e30;
-    for (int R = ftk::NWARP; R >= 1; R--) {
-        const int smem = ftk::composite_bands_smem(R, (int)w);
-        if (smem > c->max_smem) continue;
-        const int per_sm = std::max(1, (c->max_smem + 1024) / (smem + 1024));
-        const int slots = std::max(1, c->sm_count * per_sm);
-        const int bands = (int)((h + R - 1) / R);
-        const int waves = (bands + slots - 1) / slots;
-        const double cost = (double)waves * R;
-        if (cost < best_cost) {
-            best_cost = cost;
-            best = R;
-        }
-    }
-    return best;
+    int R = env ? std::max(1, std::min(atoi(env), ftk::NWARP)) : ftk::NWARP;
+    while (R > 1 && ftk::composite_bands_smem(R, (int)w) > c->max_smem) R--;
+    return R;
 }
 
 FT_API int ft_composite_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* ops, uint32_t n_ops_total,
                               const ft_path_desc* paths, uint32_t n_paths, int32_t fmt, uint8_t* raster, uint32_t w,
                               uint32_t h, uint32_t stride, int32_t where) {
+    return composite_impl(c, stroke, rule, ops, n_ops_total, paths, n_paths, fmt, raster, w, h, stride, where,
+                          nullptr);
+}
+
+}  // extern "C"
+
+static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* ops, uint32_t n_ops_total,
+                          const ft_path_desc* paths, uint32_t n_paths, int32_t fmt, uint8_t* raster, uint32_t w,
+                          uint32_t h, uint32_t stride, int32_t where, float* sw_out) {
     if (!c) return FT_ERR_ARG;
     if ((rule != FT_NONZERO && rule != FT_EVENODD) || (fmt != FT_MATTE8 && fmt != FT_RGBA8P) ||
         (where != FT_HOST && where != FT_DEVICE))
@@ -740,6 +758,7 @@ FT_API int ft_composite_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_
         p.pool_cap = c->pool.cap / sizeof(ftk::EdgeRec);
         p.bandoff = static_cast<int*>(c->bandoff.p);
         p.crec = static_cast<int4*>(c->crec.p);
+        p.sw_out = sw_out;
         FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
         if (n_paths) {
             FT_CU(ftk::launch_composite_build(p, grid, smem_a, c->stream), "launch composite build");
@@ -769,6 +788,8 @@ FT_API int ft_composite_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_
     }
     return fail(c, FT_ERR_NOMEM, "edge pool did not converge");
 }
+
+extern "C" {
 
 FT_API int ft_batch_status(ft_ctx* c, int32_t* status, uint32_t n) {
     if (!c || (n && !status)) return FT_ERR_ARG;

@@ -1210,7 +1210,8 @@ __device__ void build_edges(const CState& S, const int2* pts, const int* ss, Edg
 
 // Signed cell areas of one edge on one scan row (fig.rs:238-321), added into
 // `area` (the band row of width W).
-__device__ __forceinline__ void scan_item(const EdgeRec& E, int y, int* area, int W) {
+// With `spans`, the 128-pixel spans holding the touched cells are marked too.
+__device__ __forceinline__ void scan_item(const EdgeRec& E, int y, int* area, int W, unsigned* spans = nullptr) {
     const int k = y - E.start_row;
     const int x_bot = wadd(E.x_bot0, wmul(k, E.inv_slope));
     const bool st = (y == E.start_row), en = (y == E.end_row);
@@ -1232,6 +1233,8 @@ __device__ __forceinline__ void scan_item(const EdgeRec& E, int y, int* area, in
     // gets the growth of min(pixel_cov(x_cov), cov) until it reaches cov
     const int jmax = W - 1 - minp;  // the loop also stops at the raster's last cell
     int j, prev, x_cov;
+    const int cell0 = max(minp, 0);
+    int cell1 = cell0;
     if (minp < 0) {
         // cells left of the raster all land in cell 0 (fig.rs:295): their sum telescopes
         j = -minp;
@@ -1239,7 +1242,6 @@ __device__ __forceinline__ void scan_item(const EdgeRec& E, int y, int* area, in
         x_cov = v > FX_ONE ? FX_ONE : (int)v;
         prev = min(pixel_cov(x_cov), cov);
         if (prev) atomicAdd(&area[0], ed * prev);
-        if (prev >= cov) return;
         j++;
         x_cov = min(x_cov + step, FX_ONE);
     } else {
@@ -1247,14 +1249,19 @@ __device__ __forceinline__ void scan_item(const EdgeRec& E, int y, int* area, in
         prev = 0;
         x_cov = first;
     }
-    for (; j <= jmax; j++) {
-        const int v = min(pixel_cov(x_cov), cov);
-        const int p = v - prev;
-        prev = v;
-        if (p) atomicAdd(&area[minp + j], ed * p);
-        if (v >= cov) break;
-        x_cov = min(x_cov + step, FX_ONE);
+    if (prev < cov) {
+        for (; j <= jmax; j++) {
+            const int v = min(pixel_cov(x_cov), cov);
+            const int p = v - prev;
+            prev = v;
+            if (p) atomicAdd(&area[minp + j], ed * p);
+            cell1 = minp + j;
+            if (v >= cov) break;
+            x_cov = min(x_cov + step, FX_ONE);
+        }
     }
+    if (spans)
+        for (int sp = cell0 >> 7; sp <= (cell1 >> 7); sp++) atomicOr(&spans[sp >> 5], 1u << (sp & 31));
 }
 
 // Resolve one band row and write it (fig.rs:621-665, imgbuf.rs:38-199).
@@ -1706,20 +1713,17 @@ __global__ void __launch_bounds__(BLOCK) k_cbuild(KParams P) {
         }
         __syncthreads();
         bin_edges(P, (uint32_t)it, S, edges, reinterpret_cast<int*>(smem), s_tmp3);
+        if (P.sw_out) {  // pen width after the call: the last PenWidth op of the path
+            int lp = -1;
+            for (int i = tid; i < (int)d.n_ops; i += BLOCK)
+                if (P.ops[d.op_begin + i].kind == FT_OP_PEN_WIDTH) lp = max(lp, i);
+            lp = block_incl_max(lp, s_tmp3);
+            if (tid == BLOCK - 1) P.sw_out[it] = lp >= 0 ? P.ops[d.op_begin + lp].v[0] : d.s_width;
+        }
         if (tid == 0 && S.flags) atomicMax(&P.status[it], (S.flags & 1) ? FT_ERR_DEPTH : FT_ERR_ARG);
         __syncthreads();
     }
 }
-
-// Shared memory of k_cbands.
-struct BandSmem {
-    RasterSmem Rs;
-    int G[NWARP];                    // calls so far per band row
-    int rb[BLOCK], tmin[BLOCK], o0[BLOCK], o1[BLOCK];
-    unsigned clr[BLOCK];
-    unsigned long long base[BLOCK];
-    unsigned char ftab[16 * 256];    // ftab[k][d] = d after k alpha-0 SrcOver composites
-};
 
 __device__ __forceinline__ unsigned ftab4(const unsigned char* ftab, unsigned d, int k) {
     const unsigned char* t = ftab + (k << 8);
@@ -1727,160 +1731,163 @@ __device__ __forceinline__ unsigned ftab4(const unsigned char* ftab, unsigned d,
            ((unsigned)t[d >> 24] << 24);
 }
 
-// Accumulate the cell areas of `n` edges on scan rows [ylo, yhi) of a band whose
-// first scan row is yb0 (area row = y - yb0).  Block-wide.
-__device__ void band_items(const EdgeRec* edges, int n, int yb0, int ylo, int yhi, int* area, int Wp, int W,
-                           RasterSmem& Rs) {
-    const int tid = threadIdx.x;
-    for (int e0 = 0; e0 < n; e0 += BLOCK) {
-        const int e = e0 + tid;
-        int nrow = 0, ya = 0;
-        EdgeRec E;
-        E.ed = 0;
-        if (e < n) {
-            E = edges[e];
-            ya = max(E.start_row, ylo);
-            nrow = max(min(E.end_row, yhi - 1) - ya + 1, 0);
-        }
-        Rs.edges[tid] = E;
-        Rs.ya[tid] = ya;
-        int tot;
-        const int o = block_excl_sum(nrow, Rs.scan, tot);
-        Rs.off[tid] = o;
-        for (int m0 = 0; m0 < tot; m0 += MAP_CAP) {
-            const int ia = max(o, m0), ib = min(o + nrow, m0 + MAP_CAP);
-            for (int k = ia; k < ib; k++) Rs.map[k - m0] = (unsigned char)tid;
-            __syncthreads();
-            const int cnt = min(MAP_CAP, tot - m0);
-            for (int it = tid; it < cnt; it += BLOCK) {
-                const int jj = Rs.map[it];
-                const int y = Rs.ya[jj] + (m0 + it - Rs.off[jj]);
-                scan_item(Rs.edges[jj], y, area + (size_t)(y - yb0) * Wp, W);
-            }
-            __syncthreads();
-        }
+constexpr int FTAB_BYTES = 16 * 256;  // ftab[k][d]: d after k alpha-0 SrcOver composites
+
+// Per-warp shared memory of the band compositor for rows of `width` pixels.
+__host__ __device__ constexpr int row_smem_bytes(int width) {
+    return (int)align256((size_t)((width + 3) & ~3) * (4 + 2) + (size_t)(((width + 127) / 128 + 31) / 32) * 4);
+}
+
+// Accumulate the cells of the `ne` band edges that cross scan row y into `row`
+// (one warp; each lane takes edges), marking the touched 128-pixel spans.
+__device__ __forceinline__ void row_items(const EdgeRec* edges, int ne, int y, int* row, int W, unsigned* spans) {
+    const int lane = threadIdx.x & 31;
+    for (int e = lane; e < ne; e += 32) {
+        const EdgeRec E = edges[e];
+        if (E.start_row <= y && y <= E.end_row) scan_item(E, y, row, W, spans);
     }
 }
 
+// Resolve one row and write it: Matte8 overwrites every pixel; Rgba8p composites
+// the covered pixels after their pending alpha-0 maps (see above).  Spans that no
+// cell touched keep the running sum, so when that sum resolves to alpha 0 the
+// whole span is skipped.  Clears the row buffer and the span marks.
+__device__ __forceinline__ void composite_row(int* row, unsigned short* last, unsigned* spans, int W, int Wp,
+                                              uint8_t* drow, int rule, bool rgba, unsigned clr, int G,
+                                              const unsigned char* ftab, bool skip_spans) {
+    const int lane = threadIdx.x & 31;
+    unsigned carry = 0;
+    for (int x0 = 0; x0 < W; x0 += 128) {
+        const int sp = x0 >> 7;
+        const bool touched = (spans[sp >> 5] >> (sp & 31)) & 1u;
+        if (skip_spans && !touched && resolve_cov(carry, rule) == 0) continue;
+        const int x = x0 + lane * 4;
+        int4 a = make_int4(0, 0, 0, 0);
+        if (touched && x < Wp) {
+            a = *reinterpret_cast<const int4*>(row + x);
+            *reinterpret_cast<int4*>(row + x) = make_int4(0, 0, 0, 0);
+        }
+        const unsigned s0 = (unsigned)a.x, s1 = s0 + (unsigned)a.y, s2 = s1 + (unsigned)a.z, s3 = s2 + (unsigned)a.w;
+        const unsigned inc = warp_incl_sum_u(s3);
+        const unsigned ex = inc - s3 + carry;
+        carry += __shfl_sync(FULL, inc, 31);
+        const unsigned av[4] = {resolve_cov(s0 + ex, rule), resolve_cov(s1 + ex, rule), resolve_cov(s2 + ex, rule),
+                                resolve_cov(s3 + ex, rule)};
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            const int xc = x + c;
+            if (xc >= W) break;
+            if (!rgba) {
+                drow[xc] = (uint8_t)av[c];  // Matte8 rows are overwritten (fig.rs:629-636)
+            } else if (av[c]) {
+                unsigned* dp = reinterpret_cast<unsigned*>(drow) + xc;
+                unsigned dv = *dp;
+                const int kk = min(G - (int)last[xc], 15);
+                if (kk) dv = ftab4(ftab, dv, kk);
+                *dp = srcover_rgba(dv, clr, av[c]);
+                last[xc] = (unsigned short)(G + 1);
+            }
+        }
+    }
+    __syncwarp();
+    const int n_words = ((W + 127) / 128 + 31) / 32;
+    for (int k = lane; k < n_words; k += 32) spans[k] = 0;
+    __syncwarp();
+}
+
+// One CTA per band of P.band_rows rows, one warp per row.  Each warp walks the calls
+// in order with warp-level steps only (no block barriers after set-up).
 __global__ void __launch_bounds__(BLOCK) k_cbands(KParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
-    BandSmem& M = *reinterpret_cast<BandSmem*>(smem);
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int W = (int)P.canvas_w, H = (int)P.canvas_h, Wp = (W + 3) & ~3;
     const int R = P.band_rows, nb = P.n_bands, b = blockIdx.x;
-    const int r0 = b * R, r1 = min(r0 + R, H);
-    int* area = reinterpret_cast<int*>(smem + ((sizeof(BandSmem) + 15) & ~(size_t)15));
-    unsigned short* last = reinterpret_cast<unsigned short*>(area + (size_t)R * Wp);
-    for (int i = tid; i < R * Wp / 4; i += BLOCK) reinterpret_cast<int4*>(area)[i] = make_int4(0, 0, 0, 0);
-    for (int i = tid; i < R * Wp; i += BLOCK) last[i] = 0;
-    for (int i = tid; i < 16 * 256; i += BLOCK) {
+    const int r = b * R + warp;  // this warp's raster row
+    unsigned char* ftab = smem;
+    for (int i = threadIdx.x; i < FTAB_BYTES; i += BLOCK) {
         unsigned v = (unsigned)(i & 255);
         for (int k = 0; k < (i >> 8); k++) v = ch8_mul(v, 255u);
-        M.ftab[i] = (unsigned char)v;
+        ftab[i] = (unsigned char)v;
     }
-    if (tid < NWARP) M.G[tid] = 0;
     __syncthreads();
+    if (warp >= R || r >= H) return;
+    unsigned char* mine = smem + FTAB_BYTES + (size_t)warp * row_smem_bytes(W);
+    int* row = reinterpret_cast<int*>(mine);
+    unsigned short* last = reinterpret_cast<unsigned short*>(row + Wp);
+    unsigned* spans = reinterpret_cast<unsigned*>(last + Wp);
+    const int n_words = ((W + 127) / 128 + 31) / 32;
+    for (int x = lane * 4; x < Wp; x += 128) *reinterpret_cast<int4*>(row + x) = make_int4(0, 0, 0, 0);
+    for (int x = lane; x < Wp; x += 32) last[x] = 0;
+    for (int k = lane; k < n_words; k += 32) spans[k] = 0;
+    __syncwarp();
+    uint8_t* drow = P.rasters + (size_t)r * P.canvas_stride;
     const bool rgba = P.fmt == FT_RGBA8P;
-    const int n_paths = (int)P.n_items;
-    for (int c0 = 0; c0 < n_paths; c0 += BLOCK) {
-        const int i = c0 + tid;
-        if (i < n_paths) {
-            const int4 cr = P.crec[i];
-            const int* boff = P.bandoff + (size_t)i * (nb + 1);
-            M.rb[tid] = cr.x;
-            M.tmin[tid] = cr.y;
-            M.base[tid] = (unsigned long long)(unsigned)cr.z | ((unsigned long long)(unsigned)cr.w << 32);
-            M.o0[tid] = boff[b];
-            M.o1[tid] = boff[b + 1];
-            const ft_path_desc& d = P.paths[i];
-            M.clr[tid] = (unsigned)d.clr[0] | ((unsigned)d.clr[1] << 8) | ((unsigned)d.clr[2] << 16) |
-                         ((unsigned)d.clr[3] << 24);
+    const int n = (int)P.n_items;
+    // a call's record: band edge range, scan-row offset and colour
+    struct Call {
+        unsigned long long first;  // pool index of the call's first edge in this band
+        int ne, tmin;
+        unsigned clr;
+    };
+    auto fetch = [&](int i) {
+        Call c;
+        const int4 cr = P.crec[i];
+        const int* boff = P.bandoff + (size_t)i * (nb + 1);
+        const int o0 = boff[b], o1 = boff[b + 1];
+        c.first = ((unsigned long long)(unsigned)cr.z | ((unsigned long long)(unsigned)cr.w << 32)) + o0;
+        c.ne = o1 - o0;
+        c.tmin = cr.y;
+        const ft_path_desc& d = P.paths[i];
+        c.clr = (unsigned)d.clr[0] | ((unsigned)d.clr[1] << 8) | ((unsigned)d.clr[2] << 16) |
+                ((unsigned)d.clr[3] << 24);
+        return c;
+    };
+    auto draw = [&](const Call& c, int G, bool skip) {
+        row_items(P.pool + c.first, c.ne, r + c.tmin, row, W, spans);
+        __syncwarp();
+        composite_row(row, last, spans, W, Wp, drow, P.rule, rgba, c.clr, G, ftab, skip);
+    };
+    if (!rgba) {
+        // Matte8: every call overwrites its rows, so only the last call reaching this row shows
+        int found = -1;
+        for (int c1 = n; c1 > 0 && found < 0; c1 -= 32) {
+            const int i = c1 - 32 + lane;
+            const bool hit = i >= 0 && P.crec[i].x <= r;
+            const unsigned m = __ballot_sync(FULL, hit);
+            if (m) found = c1 - 32 + 31 - __clz(m);
         }
-        __syncthreads();
-        const int nk = min(BLOCK, n_paths - c0);
-        for (int k = 0; k < nk; k++) {
-            const int rb = M.rb[k];
-            if (rb >= r1) continue;  // this call writes no row of the band
-            const int ya = max(r0, rb);
-            const int ne = M.o1[k] - M.o0[k];
-            if (rgba && ne == 0) {
-                // only alpha 0 on these rows: one more pending map per row
-                if (lane == 0 && r0 + warp < r1 && r0 + warp >= ya) M.G[warp]++;
-                continue;
-            }
-            const int tmin = M.tmin[k];
-            if (ne > 0)
-                band_items(P.pool + M.base[k] + M.o0[k], ne, r0 + tmin, ya + tmin, r1 + tmin, area, Wp, W, M.Rs);
-            // resolve and composite the rows from ya (one warp per row)
-            const int rr = r0 + warp;
-            if (rr < r1) {
-                int* arow = area + (size_t)warp * Wp;
-                unsigned short* lrow = last + (size_t)warp * Wp;
-                uint8_t* drow = P.rasters + (size_t)rr * P.canvas_stride;
-                const int G = M.G[warp];
-                const unsigned clr = M.clr[k];
-                if (rr >= ya) {
-                    unsigned carry = 0;
-                    for (int x0 = 0; x0 < W; x0 += 128) {
-                        const int x = x0 + lane * 4;
-                        int4 a = make_int4(0, 0, 0, 0);
-                        if (x < Wp) {
-                            a = *reinterpret_cast<const int4*>(arow + x);
-                            *reinterpret_cast<int4*>(arow + x) = make_int4(0, 0, 0, 0);
-                        }
-                        const unsigned s0 = (unsigned)a.x, s1 = s0 + (unsigned)a.y, s2 = s1 + (unsigned)a.z,
-                                       s3 = s2 + (unsigned)a.w;
-                        const unsigned inc = warp_incl_sum_u(s3);
-                        const unsigned ex = inc - s3 + carry;
-                        carry += __shfl_sync(FULL, inc, 31);
-                        const unsigned av[4] = {resolve_cov(s0 + ex, P.rule), resolve_cov(s1 + ex, P.rule),
-                                                resolve_cov(s2 + ex, P.rule), resolve_cov(s3 + ex, P.rule)};
-#pragma unroll
-                        for (int c = 0; c < 4; c++) {
-                            const int xc = x + c;
-                            if (xc >= W) break;
-                            if (!rgba) {
-                                drow[xc] = (uint8_t)av[c];  // Matte8 rows are overwritten (fig.rs:629-636)
-                            } else if (av[c]) {
-                                unsigned* dp = reinterpret_cast<unsigned*>(drow) + xc;
-                                unsigned dv = *dp;
-                                const int kk = min(G - (int)lrow[xc], 15);
-                                if (kk) dv = ftab4(M.ftab, dv, kk);
-                                *dp = srcover_rgba(dv, clr, av[c]);
-                                lrow[xc] = (unsigned short)(G + 1);
-                            }
-                        }
-                    }
-                    if (lane == 0) M.G[warp] = G + 1;
-                } else if (ne > 0) {
-                    // rows above this call's top row: no composite, clear any areas
-                    for (int x = lane * 4; x < Wp; x += 128)
-                        *reinterpret_cast<int4*>(arow + x) = make_int4(0, 0, 0, 0);
-                }
-            }
-            __syncthreads();
-        }
-        __syncthreads();
+        if (found >= 0) draw(fetch(found), 0, false);
+        return;
     }
-    if (rgba) {
-        // the alpha-0 composites still pending since each pixel's last cover
-        const int rr = r0 + warp;
-        if (rr < r1) {
-            const int G = M.G[warp];
-            unsigned short* lrow = last + (size_t)warp * Wp;
-            unsigned* drow = reinterpret_cast<unsigned*>(P.rasters + (size_t)rr * P.canvas_stride);
-            for (int x = lane; x < W; x += 32) {
-                const int kk = min(G - (int)lrow[x], 15);
-                if (kk) drow[x] = ftab4(M.ftab, drow[x], kk);
-            }
+    int G = 0;  // calls so far that reach this row
+    for (int c0 = 0; c0 < n; c0 += 32) {
+        // 32 calls' records at once, one per lane, then handed out by shuffles
+        const int i = c0 + lane;
+        const int rb = i < n ? P.crec[i].x : INT_MAX;
+        unsigned reach = __ballot_sync(FULL, rb <= r);
+        Call mine_c{0ull, 0, 0, 0u};
+        if (rb <= r) mine_c = fetch(i);
+        while (reach) {
+            const int j = __ffs(reach) - 1;
+            reach &= reach - 1;
+            Call c;
+            c.first = __shfl_sync(FULL, mine_c.first, j);
+            c.ne = __shfl_sync(FULL, mine_c.ne, j);
+            c.tmin = __shfl_sync(FULL, mine_c.tmin, j);
+            c.clr = __shfl_sync(FULL, mine_c.clr, j);
+            draw(c, G, true);
+            G++;
         }
+    }
+    // the alpha-0 composites still pending since each pixel's last cover
+    unsigned* dp = reinterpret_cast<unsigned*>(drow);
+    for (int x = lane; x < W; x += 32) {
+        const int kk = min(G - (int)last[x], 15);
+        if (kk) dp[x] = ftab4(ftab, dp[x], kk);
     }
 }
 
-int composite_bands_smem(int band_rows, int width) {
-    const int wp = (width + 3) & ~3;
-    return (int)(((sizeof(BandSmem) + 15) & ~(size_t)15) + (size_t)band_rows * wp * (4 + 2));
-}
+int composite_bands_smem(int band_rows, int width) { return FTAB_BYTES + band_rows * row_smem_bytes(width); }
 
 cudaError_t launch_composite_build(const KParams& p, int grid, int smem_bytes, cudaStream_t s) {
     auto kern = p.stroke ? k_cbuild<true> : k_cbuild<false>;

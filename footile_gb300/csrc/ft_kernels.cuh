@@ -26,7 +26,7 @@ struct WorkItem {
 // One non-horizontal edge of a figure (footile fig.rs:47-66), 32 bytes.  `ed` is
 // +1 when the edge direction equals the figure direction, -1 otherwise, 0 for
 // "no edge" (horizontal or degenerate segment).
-struct EdgeRec {
+struct __align__(16) EdgeRec {
     int y_upper, y_lower, x_bot0, inv_slope;
     int step_pix, ed, start_row, end_row;
 };

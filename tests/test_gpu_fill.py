@@ -208,17 +208,31 @@ def test_scene_4096_capped(ctx):
 
 
 def test_warp_overflow_hands_path_to_cta(ctx):
-    # 9,000 vertices on a small canvas: more than a warp holds, so the CTA kernel
-    # redraws the path; the result must not change
+    # a batch large enough for the warp rasteriser, where a few figures have more
+    # vertices than a warp holds (9,000): those warps hand their paths to the CTA
+    # kernel; nothing may change in the result
+    from footile_gb300.plotter import fill_batch, pack_batch
     rng = np.random.default_rng(21)
-    n = 9000
-    ang = np.sort(rng.random(n)) * 2 * np.pi
-    rad = 20 + 10 * rng.random(n)
-    ops = np.zeros(n + 1, dtype=_abi.OP_DTYPE)
-    ops["kind"][0] = _abi.OP_MOVE
-    ops["kind"][1:n] = _abi.OP_LINE
-    ops["v"][:n, 0] = 32 + rad * np.cos(ang)
-    ops["v"][:n, 1] = 32 + rad * np.sin(ang)
-    ops["kind"][n] = _abi.OP_CLOSE
-    got, want, *_ = gpu_vs_oracle(ctx, ops, 64, 64)
-    assert_same(got, want, "overflow")
+    paths_ops, sizes = [], []
+    for i in range(400):
+        if i % 100 == 7:
+            n = 9000
+            ang = np.sort(rng.random(n)) * 2 * np.pi
+            rad = 20 + 10 * rng.random(n)
+            ops = np.zeros(n + 1, dtype=_abi.OP_DTYPE)
+            ops["kind"][0] = _abi.OP_MOVE
+            ops["kind"][1:n] = _abi.OP_LINE
+            ops["v"][:n, 0] = 32 + rad * np.cos(ang)
+            ops["v"][:n, 1] = 32 + rad * np.sin(ang)
+            ops["kind"][n] = _abi.OP_CLOSE
+        else:
+            ops = workloads.random_path(rng, 64, int(rng.integers(2, 20)))
+        paths_ops.append(ops)
+        sizes.append(64)
+    ops, paths, nbytes = pack_batch(paths_ops, sizes)
+    want = np.zeros(nbytes, np.uint8)
+    oracle.fill_batch(0, _abi.NONZERO, ops, paths, _abi.MATTE8, want, n_threads=8)
+    got = np.zeros(nbytes, np.uint8)
+    st = fill_batch(ctx, ops, paths, _abi.MATTE8, got)
+    assert (st == 0).all()
+    assert_same(got, want, "overflow batch")
