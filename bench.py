@@ -255,7 +255,7 @@ def measured_peak_hbm():
 
 def profiled_traffic():
     """DRAM bytes per launch of the rasteriser from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "k_raster_glyphs_65536.txt")
+    p = os.path.join(ROOT, "profiles", "k_raster_warp_glyphs_65536.txt")
     try:
         for line in open(p):
             if line.startswith("traffic_bytes_per_launch:"):
@@ -475,7 +475,7 @@ def run_ours(args):
                 "d2h_bytes_per_step": int(nbytes), "ms_per_step": e2e_s * 1e3, "masks_equal_device_path": same},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": profiled_traffic(), "peak_kind": peak_kind,
-                     "kernel": "ftk::k_raster (graph: 2 memsets + rasteriser)", "kernel_ms": kmean,
+                     "kernel": "ftk::k_raster_warp + ftk::k_raster (graph: 2 memsets, warp rasteriser, CTA rasteriser)", "kernel_ms": kmean,
                      "algorithmic_bytes_per_launch": int(alg_bytes)},
         "cpu_baseline": cpu,
         "modes": {"batched_paths_per_s": len(paths) / (ms_max * 1e-3), "per_path_launch": per_path,
