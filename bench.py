@@ -47,7 +47,7 @@ def parse_args():
     ap.add_argument("--per-path-sample", type=int, default=4096)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the secondary workloads")
-    ap.add_argument("--only", choices=["single", "scene", "strokes"],
+    ap.add_argument("--only", choices=["single", "scene", "strokes", "adjoint"],
                     help="run one secondary workload alone (for profiling) and print its line")
     return ap.parse_args()
 
@@ -323,6 +323,94 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def extra_adjoint(ctx, stream, dev, cpu=True, reps=10, check_paths=32, fd_paths=2):
+    """Coverage adjoint on 1,024 closed 32-cubic paths (128x128 f32 coverage each):
+    forward and backward device time, and the gradient's error against the FP64 oracle
+    and against central differences (h = 1e-2 px) of the FP64 coverage."""
+    import torch
+    from footile_gb300 import _abi, workloads
+    from footile_gb300.adjoint import Adjoint
+    ops, paths, cov_bytes, target = workloads.cubics_1024_coverage()
+    n_px = cov_bytes // 4
+    ops_d = torch.from_numpy(ops.view(np.uint8).copy()).to(dev)
+    tgt_d = torch.from_numpy(target).to(dev)
+    cov_d = torch.empty(n_px, dtype=torch.float32, device=dev)
+    gops_d = torch.empty((len(ops), 6), dtype=torch.float32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # larger than L2
+    adj = Adjoint(ctx)
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    fwd, bwd, fwd_k, bwd_k = [], [], [], []
+    for it in range(reps + 3):
+        flush.zero_()
+        e[0].record(stream)
+        adj.forward(_abi.NONZERO, ops_d, paths, cov_d)
+        e[1].record(stream)
+        fk = ctx.last_ms()
+        g_cov = 2.0 * (cov_d - tgt_d)  # dLoss/dcov of sum((cov - target)^2), outside both timings
+        flush.zero_()
+        e[2].record(stream)
+        adj.backward(g_cov, gops_d)
+        e[3].record(stream)
+        bk = ctx.last_ms()
+        torch.cuda.synchronize()
+        if it >= 3:
+            fwd.append(e[0].elapsed_time(e[1]))
+            bwd.append(e[2].elapsed_time(e[3]))
+            fwd_k.append(fk)
+            bwd_k.append(bk)
+    st = adj.status()
+    out = {"workload": "cubics_1024 coverage adjoint (1,024 closed paths x 32 cubics, 128x128 f32, L2 loss)",
+           "fwd_ms": float(np.median(fwd)), "bwd_ms": float(np.median(bwd)),
+           "fwd_kernel_ms": float(np.median(fwd_k)), "bwd_kernel_ms": float(np.median(bwd_k)),
+           "bwd_over_fwd": float(np.median(bwd) / np.median(fwd)), "paths_status_ok": int((st == 0).sum()),
+           "l2_flushed_between_calls": True}
+    if cpu:
+        import oracle
+        cov = cov_d.cpu().numpy()
+        g = gops_d.cpu().numpy().astype(np.float64)
+        gc = (2.0 * (cov.astype(np.float64) - target)).astype(np.float32).astype(np.float64)
+        num, den = 0.0, 0.0
+        t0 = time.perf_counter()
+        for p in paths[:check_paths]:
+            b, n = int(p["op_begin"]), int(p["n_ops"])
+            o = ops[b:b + n]
+            c64, area, _ = oracle.adj_forward(_abi.NONZERO, o, 128, 128)
+            off = int(p["raster_offset"]) // 4
+            r = oracle.adj_backward(_abi.NONZERO, o, 128, 128, area, gc[off:off + 128 * 128].reshape(128, 128))
+            num = max(num, float(np.abs(g[b:b + n] - r).max()))
+            den = max(den, float(np.abs(r).max()))
+        out["cpu_fp64_oracle_ms_per_path_fwd_bwd"] = (time.perf_counter() - t0) / check_paths * 1e3
+        out["max_rel_err_vs_fp64"] = num / den
+        out["rel_err_definition"] = "max|g - g64| / max|g64| over the op floats of the first %d paths" % check_paths
+        # central differences of the FP64 loss (subdivision tree held), all 198 floats of a path
+        fd_num, fd_den = 0.0, 0.0
+        for p in paths[:fd_paths]:
+            b, n = int(p["op_begin"]), int(p["n_ops"])
+            o = ops[b:b + n]
+            off = int(p["raster_offset"]) // 4
+            tg = target[off:off + 128 * 128].reshape(128, 128).astype(np.float64)
+            c64, area, _ = oracle.adj_forward(_abi.NONZERO, o, 128, 128)
+            r = oracle.adj_backward(_abi.NONZERO, o, 128, 128, area, 2 * (c64 - tg))
+            base = np.array([x["v"] for x in o], dtype=np.float64)
+            fd = np.zeros_like(base)
+            for i in range(n):
+                for k in range(6):
+                    if o[i]["kind"] in (_abi.OP_CLOSE, _abi.OP_PEN_WIDTH) or (o[i]["kind"] != _abi.OP_CUBIC and k >= 2):
+                        continue
+                    vp, vm = base.copy(), base.copy()
+                    vp[i, k] += 1e-2
+                    vm[i, k] -= 1e-2
+                    lp = ((oracle.adj_forward(_abi.NONZERO, o, 128, 128, val=vp)[0] - tg) ** 2).sum()
+                    lm = ((oracle.adj_forward(_abi.NONZERO, o, 128, 128, val=vm)[0] - tg) ** 2).sum()
+                    fd[i, k] = (lp - lm) / 2e-2
+            fd_num = max(fd_num, float(np.abs(g[b:b + n] - fd).max()))
+            fd_den = max(fd_den, float(np.abs(fd).max()))
+        out["max_rel_err_vs_central_fd_h1e-2"] = fd_num / fd_den
+        out["fd_paths"] = fd_paths
+    adj.close()
+    return out
+
+
 def run_only(args):
     import torch
     from footile_gb300._lib import Context
@@ -331,7 +419,7 @@ def run_only(args):
     torch.cuda.set_stream(stream)
     ctx = Context(0)
     ctx.set_stream(stream.cuda_stream)
-    fn = {"single": extra_single, "scene": extra_scene, "strokes": extra_strokes}[args.only]
+    fn = {"single": extra_single, "scene": extra_scene, "strokes": extra_strokes, "adjoint": extra_adjoint}[args.only]
     print(json.dumps(fn(ctx, stream, dev, cpu=not args.no_cpu)), flush=True)
 
 
@@ -448,7 +536,7 @@ def run_ours(args):
     if rank == 0 and not args.no_extras:
         extras = {}
         for name, fn in (("single_path_256", extra_single), ("scene_4096", extra_scene),
-                         ("strokes_16384", extra_strokes)):
+                         ("strokes_16384", extra_strokes), ("adjoint_cubics_1024", extra_adjoint)):
             try:
                 extras[name] = fn(ctx, stream, dev, cpu=(world == 1 and not args.no_cpu))
             except Exception as e:  # report, never hide, a failing secondary workload

@@ -14,8 +14,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libfootile_gpu.so")
 
-SOURCES = ["ft_kernels.cu", "ft_capi.cu"]
-HEADERS = ["ft_device.cuh", "ft_kernels.cuh"]
+SOURCES = ["ft_kernels.cu", "ft_adjoint.cu", "ft_capi.cu"]
+HEADERS = ["ft_device.cuh", "ft_kernels.cuh", "ft_adjoint.cuh"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Bit-exact float stages: no FMA contraction, IEEE division and square root.
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-prec-div=true", "-prec-sqrt=true",

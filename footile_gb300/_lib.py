@@ -56,6 +56,10 @@ def load(auto_build=True):
             "ft_batch_launch_status": ([P, P, P, u32], ctypes.c_int),
             "ft_batch_destroy": ([P], None),
             "ft_composite_batch": ([P, i32, i32, P, u32, P, u32, i32, P, u32, u32, u32, i32], ctypes.c_int),
+            "ft_adjoint_forward": ([P, i32, P, u32, P, u32, P, u64, i32, ctypes.POINTER(P)], ctypes.c_int),
+            "ft_adjoint_backward": ([P, P, P, P, P, i32], ctypes.c_int),
+            "ft_adjoint_status": ([P, P, P, u32], ctypes.c_int),
+            "ft_adjoint_destroy": ([P], None),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -72,7 +76,8 @@ def exported_symbols():
         "ft_set_join", "ft_set_pen_width", "ft_get_pen_width", "ft_fill", "ft_stroke", "ft_fill_batch",
         "ft_batch_status", "ft_sync", "ft_last_error", "ft_last_timings", "ft_launch_count",
         "ft_batch_create", "ft_batch_launch", "ft_batch_launch_status", "ft_batch_destroy",
-        "ft_composite_batch")]
+        "ft_composite_batch", "ft_fill_noalloc", "ft_adjoint_forward", "ft_adjoint_backward", "ft_adjoint_status",
+        "ft_adjoint_destroy")]
 
 
 class Context:
@@ -85,6 +90,7 @@ class Context:
         if rc != _abi.OK:
             raise FootileError(rc, "ft_ctx_create failed (no usable CUDA device?)")
         self.h = h
+        self.stream_ptr = None  # the context's own stream until set_stream
 
     def close(self):
         if getattr(self, "h", None):
@@ -122,6 +128,19 @@ class Context:
 
     def set_stream(self, stream_ptr):
         self.check(self.L.ft_set_stream(self.h, ctypes.c_void_p(stream_ptr)))
+        self.stream_ptr = int(stream_ptr)
+
+    def torch_fence(self):
+        """Order a call on CUDA tensors after the work torch has queued for them: a
+        no-op when the context runs on torch's current stream, otherwise the host
+        waits for that stream.  Returns True when the caller must also wait for the
+        context (`sync`) before torch reads the results."""
+        import torch
+        cur = torch.cuda.current_stream()
+        if self.stream_ptr == int(cur.cuda_stream):
+            return False
+        cur.synchronize()
+        return True
 
     def sync(self):
         self.check(self.L.ft_sync(self.h))

@@ -1,0 +1,710 @@
+// ft_adjoint.cu — differentiable FP32 coverage of fills and its adjoint.
+//
+// The forward covers the flattened polygon of every path analytically: the path walk
+// and De Casteljau subdivision of Plotter::fill (plotter.rs:175-332, same f32 tree as
+// the integer rasteriser), sub-figures as Fig builds them (fig.rs:428-461), and the
+// cell-area scheme of fig.rs:285-321 without its 16.16 / 1/256 quantisation: each edge
+// adds, per raster row and cell, dir * h * (c + 1 - xmid) to cell c and the rest of h
+// to cell c + 1 (all of h to cell 0 left of the raster); the row prefix sum
+// (imgbuf.rs:38-51) times the figure's direction sign (fig_sign) is the winding area
+// S; NonZero gives clamp(S, 0, 1), EvenOdd the period-2 triangle wave.  The integer rasteriser stays the shipped forward; this one
+// exists to be differentiated.
+//
+// The backward recomputes the flattening and the edges (nothing but the winding area
+// is kept from the forward) and takes, per edge P0->P1, the boundary integral
+//   dS_p/dP0 = (-dy, dx) * int_{s in p} (1 - s) ds,  dS_p/dP1 = (-dy, dx) * int_{s in p} s ds
+// weighted by g_p = dL/dcov_p * dcov/dS_p, then chains vertex gradients to the op
+// floats through the Bernstein weights of each leaf's end parameter and the
+// transpose of the transform's linear part.  The subdivision tree is held fixed
+// (it is piecewise constant in the control points).
+//
+// One CTA per path: a 256-thread walk over the ops in chunks (block scans give each
+// op its pen, vertex offset and sub-figure start), then bands of rows in a 64 KB
+// shared buffer, (edge, row) items spread over the threads.
+#include <climits>
+
+#include "ft_adjoint.cuh"
+#include "ft_device.cuh"
+
+namespace fta {
+
+using ftk::P2;
+using ftk::p2;
+using ftk::pdist_sq;
+using ftk::pfinite;
+using ftk::pmid;
+using ftk::xform;
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int NW = ABLOCK / 32;
+constexpr int EPT = 4;                 // edges per thread per edge chunk
+constexpr int ECHUNK = ABLOCK * EPT;
+
+struct ASmem {
+    int wsum[NW];
+    int wmax[NW];
+    int wmax2[NW];
+    int wmax3[NW];
+    int off[ECHUNK + 1];
+    int carry_pen, carry_close, carry_base, carry_sub;
+    int status;
+    int total;
+    unsigned long long top_key;
+    int top, nxt, prv, sub_last;
+    float sign;
+};
+
+__device__ __forceinline__ int warp_incl_sum(int v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(FULL, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+__device__ __forceinline__ int warp_incl_max(int v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(FULL, v, o);
+        if (lane >= o) v = max(v, t);
+    }
+    return v;
+}
+
+// Block-wide exclusive sum; `total` gets the block's sum.  Every thread must call.
+__device__ int block_excl_sum(int v, int* wsum, int& total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int inc = warp_incl_sum(v);
+    if (lane == 31) wsum[w] = inc;
+    __syncthreads();
+    int pre = 0, tot = 0;
+#pragma unroll
+    for (int i = 0; i < NW; i++) {
+        int x = wsum[i];
+        pre += i < w ? x : 0;
+        tot += x;
+    }
+    __syncthreads();
+    total = tot;
+    return pre + inc - v;
+}
+
+// Block-wide max scan: inclusive and exclusive (INT_MIN before the first thread).
+__device__ void block_max_scan(int v, int* wmax, int& incl, int& excl) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int inc = warp_incl_max(v);
+    int ex = __shfl_up_sync(FULL, inc, 1);
+    if (lane == 0) ex = INT_MIN;
+    if (lane == 31) wmax[w] = inc;
+    __syncthreads();
+    int pre = INT_MIN;
+#pragma unroll
+    for (int i = 0; i < NW; i++) pre = i < w ? max(pre, wmax[i]) : pre;
+    __syncthreads();
+    incl = max(pre, inc);
+    excl = max(pre, ex);
+}
+
+__device__ __forceinline__ float pow2neg(int d) { return __int_as_float((127 - d) << 23); }  // 2^-d, d <= 126
+
+// De Casteljau walk of one quad (plotter.rs:248-265) or cubic (plotter.rs:311-332) in
+// depth-first order; leaf(index, end point, end parameter t).  Returns the leaf count.
+template <bool CUBIC, class Leaf>
+__device__ int curve_walk(P2 a, P2 b, P2 c, P2 d, float tol_sq, int* depth_hit, Leaf leaf) {
+    struct Fr {
+        P2 a, b, c, d;
+        int dep;
+    };
+    Fr st[FT_MAX_DEPTH + 1];
+    int sp = 0, n = 0, dep = 0;
+    float t = 0.0f;
+    for (;;) {
+        bool within;
+        P2 l1, l2, m, r1, r2;
+        if (CUBIC) {
+            P2 ab = pmid(a, b), bc = pmid(b, c), cd = pmid(c, d);
+            P2 abbc = pmid(ab, bc), bccd = pmid(bc, cd);
+            m = pmid(abbc, bccd);
+            within = pdist_sq(m, pmid(a, d)) <= tol_sq;
+            l1 = ab;
+            l2 = abbc;
+            r1 = bccd;
+            r2 = cd;
+        } else {
+            P2 ab = pmid(a, b), bc = pmid(b, c);
+            m = pmid(ab, bc);
+            within = pdist_sq(m, pmid(a, c)) <= tol_sq;
+            l1 = ab;
+            l2 = m;
+            r1 = bc;
+            r2 = c;
+        }
+        if (within || dep >= FT_MAX_DEPTH) {
+            if (!within) *depth_hit = 1;
+            t = __fadd_rn(t, pow2neg(dep));  // dyadic, exact
+            leaf(n, CUBIC ? d : c, t);
+            n++;
+            if (sp == 0) break;
+            --sp;
+            a = st[sp].a;
+            b = st[sp].b;
+            c = st[sp].c;
+            d = st[sp].d;
+            dep = st[sp].dep;
+        } else {
+            if (CUBIC) {
+                st[sp] = Fr{m, r1, r2, d, dep + 1};
+                b = l1;
+                c = l2;
+                d = m;
+            } else {
+                st[sp] = Fr{m, r1, r2, r2, dep + 1};
+                b = l1;
+                c = l2;
+            }
+            sp++;
+            dep++;
+        }
+    }
+    return n;
+}
+
+__device__ __forceinline__ int end_slot(int kind) { return kind == FT_OP_CUBIC ? 2 : (kind == FT_OP_QUAD ? 1 : 0); }
+
+__device__ __forceinline__ P2 op_pt(const ft_op& o, int slot) { return p2(o.v[2 * slot], o.v[2 * slot + 1]); }
+
+__device__ __forceinline__ ft_op load_op(const ft_op* ops, int i) {
+    const float4* q = reinterpret_cast<const float4*>(ops + i);
+    float4 x = __ldg(q), y = __ldg(q + 1);
+    ft_op o;
+    o.kind = __float_as_int(x.x);
+    o.v[0] = x.y;
+    o.v[1] = x.z;
+    o.v[2] = x.w;
+    o.v[3] = y.x;
+    o.v[4] = y.y;
+    o.v[5] = y.z;
+    o.reserved = 0;
+    return o;
+}
+
+enum { WALK_EMIT = 0, WALK_GRAD = 1 };
+
+// The path walk of plotter.rs:175-224 over ops [0, n) in chunks of ABLOCK ops.
+// WALK_EMIT writes vertex positions and sub-figure starts (and zeroes vertex gradients
+// when `zero_grad`); WALK_GRAD chains vertex gradients to the op floats.  Returns the
+// vertex count.
+template <int MODE>
+__device__ int path_walk(const AParams& p, ASmem& sm, const ft_op* ops, int n, float2* vpos, int* vsub,
+                         float2* vgrad, bool zero_grad, float* gops) {
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        sm.carry_pen = -1;
+        sm.carry_close = -1;
+        sm.carry_base = 0;
+        sm.carry_sub = -1;
+    }
+    __syncthreads();
+    const float* m = p.xf;
+    for (int c0 = 0; c0 < n; c0 += ABLOCK) {
+        const int i = c0 + tid;
+        ft_op o;
+        o.kind = -1;
+        if (i < n) o = load_op(ops, i);
+        const int kind = o.kind;
+        const bool pen_setting = kind == FT_OP_MOVE || kind == FT_OP_LINE || kind == FT_OP_QUAD || kind == FT_OP_CUBIC;
+        int inc_pen, exc_pen, inc_close, exc_close;
+        block_max_scan(pen_setting ? i : -1, sm.wmax, inc_pen, exc_pen);
+        block_max_scan(kind == FT_OP_CLOSE ? i : -1, sm.wmax2, inc_close, exc_close);
+        const int carry_pen = sm.carry_pen, carry_close = sm.carry_close;
+        exc_pen = max(exc_pen, carry_pen);
+        exc_close = max(exc_close, carry_close);
+        const int prev_pen = exc_pen > exc_close ? exc_pen : -1;
+        // curve geometry (transformed) and leaf count
+        P2 A = p2(0.f, 0.f), B = A, C = A, D = A;
+        int cnt = 0, depth_hit = 0;
+        bool curve = false;
+        if (kind == FT_OP_MOVE || kind == FT_OP_LINE) {
+            cnt = 1;
+        } else if (kind == FT_OP_QUAD || kind == FT_OP_CUBIC) {
+            P2 pen = p2(0.f, 0.f);
+            if (prev_pen >= 0) {
+                ft_op q = load_op(ops, prev_pen);
+                pen = op_pt(q, end_slot(q.kind));
+            }
+            A = xform(m, pen);
+            B = xform(m, op_pt(o, 0));
+            C = xform(m, op_pt(o, 1));
+            D = kind == FT_OP_CUBIC ? xform(m, op_pt(o, 2)) : C;
+            if (!pfinite(A) || !pfinite(B) || !pfinite(C) || !pfinite(D)) {
+                cnt = 1;
+                atomicMax(&sm.status, (int)FT_ERR_ARG);
+            } else {
+                curve = true;
+                auto none = [](int, P2, float) {};
+                cnt = kind == FT_OP_CUBIC ? curve_walk<true>(A, B, C, D, p.tol_sq, &depth_hit, none)
+                                          : curve_walk<false>(A, B, C, D, p.tol_sq, &depth_hit, none);
+                if (depth_hit) atomicMax(&sm.status, (int)FT_ERR_DEPTH);
+            }
+        }
+        int chunk_total;
+        const int base = sm.carry_base + block_excl_sum(cnt, sm.wsum, chunk_total);
+        const bool starts = cnt > 0 && (kind == FT_OP_MOVE || prev_pen < 0);
+        int inc_sub, exc_sub;
+        block_max_scan(starts ? base : -1, sm.wmax3, inc_sub, exc_sub);
+        const int sub = max(inc_sub, sm.carry_sub);
+        if (MODE == WALK_EMIT) {
+            auto put = [&](int j, P2 q, float) {
+                const int k = base + j;
+                if (k < VCAP) {
+                    vpos[k] = make_float2(q.x, q.y);
+                    vsub[k] = sub;
+                    if (zero_grad) vgrad[k] = make_float2(0.f, 0.f);
+                }
+            };
+            if (curve) {
+                if (kind == FT_OP_CUBIC)
+                    curve_walk<true>(A, B, C, D, p.tol_sq, &depth_hit, put);
+                else
+                    curve_walk<false>(A, B, C, D, p.tol_sq, &depth_hit, put);
+            } else if (cnt == 1) {
+                put(0, xform(m, op_pt(o, end_slot(kind))), 1.0f);
+            }
+        } else if (cnt > 0) {
+            // back through the transform: d(m*p)/dp = [[m0, m1], [m3, m4]]
+            float* g = gops + (size_t)i * 6;
+            if (!curve) {
+                float2 gv = __ldcg(&vgrad[base]);  // written by L2 atomics
+                const int s = end_slot(kind);
+                atomicAdd(g + 2 * s, __fadd_rn(__fmul_rn(m[0], gv.x), __fmul_rn(m[3], gv.y)));
+                atomicAdd(g + 2 * s + 1, __fadd_rn(__fmul_rn(m[1], gv.x), __fmul_rn(m[4], gv.y)));
+            } else {
+                float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // pen, b, c, d
+                auto chain = [&](int j, P2, float t) {
+                    float2 gv = __ldcg(&vgrad[base + j]);
+                    const float gx = __fadd_rn(__fmul_rn(m[0], gv.x), __fmul_rn(m[3], gv.y));
+                    const float gy = __fadd_rn(__fmul_rn(m[1], gv.x), __fmul_rn(m[4], gv.y));
+                    const float u = __fsub_rn(1.0f, t);
+                    float w0, w1, w2, w3;
+                    if (kind == FT_OP_CUBIC) {
+                        w0 = __fmul_rn(__fmul_rn(u, u), u);
+                        w1 = __fmul_rn(__fmul_rn(3.0f, t), __fmul_rn(u, u));
+                        w2 = __fmul_rn(__fmul_rn(3.0f, t), __fmul_rn(t, u));
+                        w3 = __fmul_rn(__fmul_rn(t, t), t);
+                    } else {
+                        w0 = __fmul_rn(u, u);
+                        w1 = __fmul_rn(__fmul_rn(2.0f, t), u);
+                        w2 = __fmul_rn(t, t);
+                        w3 = 0.0f;
+                    }
+                    acc[0] = __fadd_rn(acc[0], __fmul_rn(w0, gx));
+                    acc[1] = __fadd_rn(acc[1], __fmul_rn(w0, gy));
+                    acc[2] = __fadd_rn(acc[2], __fmul_rn(w1, gx));
+                    acc[3] = __fadd_rn(acc[3], __fmul_rn(w1, gy));
+                    acc[4] = __fadd_rn(acc[4], __fmul_rn(w2, gx));
+                    acc[5] = __fadd_rn(acc[5], __fmul_rn(w2, gy));
+                    acc[6] = __fadd_rn(acc[6], __fmul_rn(w3, gx));
+                    acc[7] = __fadd_rn(acc[7], __fmul_rn(w3, gy));
+                };
+                if (kind == FT_OP_CUBIC)
+                    curve_walk<true>(A, B, C, D, p.tol_sq, &depth_hit, chain);
+                else
+                    curve_walk<false>(A, B, C, D, p.tol_sq, &depth_hit, chain);
+                const int nslot = kind == FT_OP_CUBIC ? 3 : 2;
+                for (int s = 0; s < nslot; s++) {
+                    atomicAdd(g + 2 * s, acc[2 + 2 * s]);
+                    atomicAdd(g + 2 * s + 1, acc[3 + 2 * s]);
+                }
+                if (prev_pen >= 0) {
+                    const int s = end_slot(load_op(ops, prev_pen).kind);
+                    float* gp = gops + (size_t)prev_pen * 6;
+                    atomicAdd(gp + 2 * s, acc[0]);
+                    atomicAdd(gp + 2 * s + 1, acc[1]);
+                }
+            }
+        }
+        __syncthreads();
+        if (tid == ABLOCK - 1) {
+            sm.carry_pen = max(inc_pen, carry_pen);
+            sm.carry_close = max(inc_close, carry_close);
+            sm.carry_base = base + cnt;
+            sm.carry_sub = sub;
+        }
+        __syncthreads();
+    }
+    return sm.carry_base;
+}
+
+__device__ __forceinline__ int2 fxp(const float2* vpos, int k) {
+    const float2 q = vpos[k];
+    return make_int2(ftk::f2fx(q.x), ftk::f2fx(q.y));
+}
+__device__ __forceinline__ bool fx_ne(int2 a, int2 b) { return a.x != b.x || a.y != b.y; }
+
+// The direction footile's Fig gives the figure (fig.rs:402-411, 493-494), as +1.0f
+// (Forward) or -1.0f: the top vertex is the kept vertex with the least (y, x, id) in
+// 16.16, where Fig::add_point drops a point equal to the previous one and Fig::close
+// drops a last point equal to the sub-figure's first (fig.rs:373-383, 428-451), so the
+// top is the first raw vertex with the least point outside sub-figures whose points
+// all coincide; its neighbours in the kept sub-figure decide widdershins with
+// wrapping Fixed products (fig.rs:116-119).  Edges count +1 in that direction, and
+// NonZero clamps the signed row sum at 0 (imgbuf.rs:54-61).
+__device__ float fig_sign(ASmem& sm, int V, const float2* vpos, const int* vsub, int* vflag) {
+    const int tid = threadIdx.x, lane = tid & 31;
+    if (tid == 0) {
+        sm.top_key = ~0ull;
+        sm.top = INT_MAX;
+        sm.nxt = INT_MAX;
+        sm.prv = -1;
+        sm.sub_last = -1;
+    }
+    for (int k = tid; k < V; k += ABLOCK) vflag[k] = 0;
+    __syncthreads();
+    for (int k = tid; k < V; k += ABLOCK) {
+        const int s0 = vsub[k];
+        if (fx_ne(fxp(vpos, k), fxp(vpos, s0))) vflag[s0] = 1;  // the sub-figure keeps a second point
+    }
+    __syncthreads();
+    unsigned long long best = ~0ull;
+    for (int k = tid; k < V; k += ABLOCK) {
+        const int s0 = vsub[k];
+        const int2 q = fxp(vpos, k);
+        const bool kept = k == s0 || fx_ne(q, fxp(vpos, k - 1));
+        if (!kept || !vflag[s0]) continue;
+        const unsigned long long key = ((unsigned long long)((unsigned)q.y ^ 0x80000000u) << 32) |
+                                       (unsigned long long)((unsigned)q.x ^ 0x80000000u);
+        best = key < best ? key : best;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long t = __shfl_down_sync(FULL, best, o);
+        best = t < best ? t : best;
+    }
+    if (lane == 0 && best != ~0ull) atomicMin(&sm.top_key, best);
+    __syncthreads();
+    const unsigned long long tk = sm.top_key;
+    if (tk == ~0ull) return 1.0f;
+    for (int k = tid; k < V; k += ABLOCK) {
+        const int s0 = vsub[k];
+        const int2 q = fxp(vpos, k);
+        const unsigned long long key = ((unsigned long long)((unsigned)q.y ^ 0x80000000u) << 32) |
+                                       (unsigned long long)((unsigned)q.x ^ 0x80000000u);
+        const bool kept = k == s0 || fx_ne(q, fxp(vpos, k - 1));
+        if (kept && vflag[s0] && key == tk) atomicMin(&sm.top, k);
+    }
+    __syncthreads();
+    const int top = sm.top, s0 = vsub[top];
+    const int2 qt = fxp(vpos, top), qs = fxp(vpos, s0);
+    for (int k = s0 + 1 + tid; k < V && vsub[k] == s0; k += ABLOCK) {
+        const int2 q = fxp(vpos, k);
+        if (k > top && fx_ne(q, qt)) atomicMin(&sm.nxt, k);
+        if (fx_ne(q, qs)) atomicMax(&sm.prv, k);
+    }
+    __syncthreads();
+    float sign = 1.0f;
+    if (tid == 0) {
+        const int2 n = sm.nxt != INT_MAX ? fxp(vpos, sm.nxt) : qs;
+        const int2 pv = top > s0 ? fxp(vpos, top - 1) : (sm.prv >= 0 ? fxp(vpos, sm.prv) : qt);
+        const int ax = ftk::wsub(pv.x, qt.x), ay = ftk::wsub(pv.y, qt.y);
+        const int bx = ftk::wsub(n.x, qt.x), by = ftk::wsub(n.y, qt.y);
+        sm.sign = ftk::fxmul(ax, by) > ftk::fxmul(bx, ay) ? 1.0f : -1.0f;
+    }
+    __syncthreads();
+    sign = sm.sign;
+    __syncthreads();
+    return sign;
+}
+
+// One edge, top end a, bottom end b (a.y < b.y).
+struct EdgeG {
+    P2 a, b;
+    float dy, dxdy, xlo, xhi;
+    float dir;   // +1 when the edge runs down (P0 on top), -1 up
+    P2 perp;     // (-dy, dx) of P1 - P0
+    int e, nxt;
+    bool ok;
+};
+
+__device__ __forceinline__ int next_vertex(const int* vsub, int V, int k) {
+    return (k + 1 < V && vsub[k + 1] == vsub[k]) ? k + 1 : vsub[k];
+}
+
+__device__ __forceinline__ EdgeG make_edge(const float2* vpos, const int* vsub, int V, int e) {
+    EdgeG E;
+    E.e = e;
+    E.nxt = next_vertex(vsub, V, e);
+    const float2 q0 = vpos[e], q1 = vpos[E.nxt];
+    const P2 p0 = p2(q0.x, q0.y), p1 = p2(q1.x, q1.y);
+    E.ok = pfinite(p0) && pfinite(p1) && p0.y != p1.y;
+    const bool down = p1.y > p0.y;
+    E.a = down ? p0 : p1;
+    E.b = down ? p1 : p0;
+    E.dir = down ? 1.0f : -1.0f;
+    E.dy = __fsub_rn(E.b.y, E.a.y);
+    E.dxdy = __fdiv_rn(__fsub_rn(E.b.x, E.a.x), E.dy);
+    E.xlo = fminf(E.a.x, E.b.x);
+    E.xhi = fmaxf(E.a.x, E.b.x);
+    E.perp = p2(-__fsub_rn(p1.y, p0.y), __fsub_rn(p1.x, p0.x));
+    return E;
+}
+
+// Rows of the edge inside rows [b0, b1]; first row in *r0.
+__device__ __forceinline__ int edge_rows(const EdgeG& E, int b0, int b1, int* r0) {
+    if (!E.ok) return 0;
+    const float f0 = fmaxf(floorf(E.a.y), (float)b0);
+    const float f1 = fminf(__fsub_rn(ceilf(E.b.y), 1.0f), (float)b1);
+    if (!(f0 <= f1)) return 0;
+    *r0 = (int)f0;
+    return (int)f1 - (int)f0 + 1;
+}
+
+// Pieces of the edge in raster row r, cell by cell: cb(cell, h, xmid, u0, u1); cell -1
+// is everything left of the raster; cells at or right of W are dropped.
+template <class CB>
+__device__ __forceinline__ void row_pieces(const EdgeG& E, int r, int W, CB cb) {
+    const float yt = fmaxf(E.a.y, (float)r), yb = fminf(E.b.y, (float)(r + 1));
+    if (!(yb > yt)) return;
+    const float xt = yt == E.a.y ? E.a.x
+                                 : fminf(fmaxf(__fadd_rn(E.a.x, __fmul_rn(__fsub_rn(yt, E.a.y), E.dxdy)), E.xlo), E.xhi);
+    const float xb = yb == E.b.y ? E.b.x
+                                 : fminf(fmaxf(__fadd_rn(E.a.x, __fmul_rn(__fsub_rn(yb, E.a.y), E.dxdy)), E.xlo), E.xhi);
+    const float ut = __fdiv_rn(__fsub_rn(yt, E.a.y), E.dy), ub = __fdiv_rn(__fsub_rn(yb, E.a.y), E.dy);
+    const float h = __fsub_rn(yb, yt);
+    const float xl = fminf(xt, xb), xr = fmaxf(xt, xb);
+    const bool rising = xt <= xb;
+    const float cl = floorf(xl), cr = floorf(xr);
+    if (cl == cr || xr == xl) {
+        if (cl < (float)W) cb(cl < 0.0f ? -1 : (int)cl, h, __fmul_rn(__fadd_rn(xl, xr), 0.5f), ut, ub);
+        return;
+    }
+    const float span = __fsub_rn(xr, xl), du = __fsub_rn(ub, ut);
+    auto piece = [&](float x0, float x1, int c) {
+        const float f0 = __fdiv_rn(__fsub_rn(x0, xl), span), f1 = __fdiv_rn(__fsub_rn(x1, xl), span);
+        const float u0 = rising ? __fadd_rn(ut, __fmul_rn(f0, du)) : __fsub_rn(ub, __fmul_rn(f1, du));
+        const float u1 = rising ? __fadd_rn(ut, __fmul_rn(f1, du)) : __fsub_rn(ub, __fmul_rn(f0, du));
+        cb(c, __fmul_rn(__fsub_rn(f1, f0), h), __fmul_rn(__fadd_rn(x0, x1), 0.5f), u0, u1);
+    };
+    float c = cl;
+    if (c < 0.0f) {
+        const float x1 = fminf(xr, 0.0f);
+        if (x1 > xl) piece(xl, x1, -1);
+        c = 0.0f;
+    }
+    const float cend = fminf(cr, (float)(W - 1));
+    for (; c <= cend; c = __fadd_rn(c, 1.0f)) {
+        const float x0 = fmaxf(xl, c), x1 = fminf(xr, __fadd_rn(c, 1.0f));
+        if (x1 > x0) piece(x0, x1, (int)c);
+    }
+}
+
+// All (edge, row) items of rows [b0, b0 + nb) of the path: forward adds cell areas to
+// the band, backward accumulates the edge integrals against the band's g values.
+template <bool BWD>
+__device__ void band_edges(ASmem& sm, float* band, int W, int b0, int nb, int V, const float2* vpos,
+                           const int* vsub, float2* vgrad) {
+    const int tid = threadIdx.x;
+    const int b1 = b0 + nb - 1;
+    for (int e0 = 0; e0 < V; e0 += ECHUNK) {
+        int cnt[EPT], sum = 0;
+#pragma unroll
+        for (int q = 0; q < EPT; q++) {
+            const int e = e0 + tid * EPT + q;
+            int r0;
+            cnt[q] = e < V ? edge_rows(make_edge(vpos, vsub, V, e), b0, b1, &r0) : 0;
+            sum += cnt[q];
+        }
+        int total;
+        int pre = block_excl_sum(sum, sm.wsum, total);
+#pragma unroll
+        for (int q = 0; q < EPT; q++) {
+            sm.off[tid * EPT + q] = pre;
+            pre += cnt[q];
+        }
+        if (tid == 0) sm.off[ECHUNK] = total;
+        __syncthreads();
+        const int per = (total + ABLOCK - 1) / ABLOCK;
+        const int beg = tid * per, end = min(total, beg + per);
+        if (beg < end) {
+            // last edge slot whose range starts at or before `beg`
+            int lo = 0, hi = ECHUNK - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (sm.off[mid] <= beg)
+                    lo = mid;
+                else
+                    hi = mid - 1;
+            }
+            int slot = lo;
+            EdgeG E = make_edge(vpos, vsub, V, e0 + slot);
+            int r0 = 0;
+            edge_rows(E, b0, b1, &r0);
+            float ga = 0.0f, gb = 0.0f;
+            for (int it = beg; it < end; it++) {
+                if (sm.off[slot + 1] <= it) {
+                    if (BWD) {
+                        atomicAdd(&vgrad[E.e].x, __fmul_rn(E.perp.x, ga));
+                        atomicAdd(&vgrad[E.e].y, __fmul_rn(E.perp.y, ga));
+                        atomicAdd(&vgrad[E.nxt].x, __fmul_rn(E.perp.x, gb));
+                        atomicAdd(&vgrad[E.nxt].y, __fmul_rn(E.perp.y, gb));
+                        ga = gb = 0.0f;
+                    }
+                    do {
+                        slot++;
+                    } while (sm.off[slot + 1] <= it);
+                    E = make_edge(vpos, vsub, V, e0 + slot);
+                    edge_rows(E, b0, b1, &r0);
+                }
+                const int r = r0 + (it - sm.off[slot]);
+                float* row = band + (size_t)(r - b0) * W;
+                if (!BWD) {
+                    row_pieces(E, r, W, [&](int c, float h, float xm, float, float) {
+                        const float dh = __fmul_rn(E.dir, h);
+                        if (c < 0) {
+                            atomicAdd(row, dh);
+                        } else {
+                            atomicAdd(row + c, __fmul_rn(dh, __fsub_rn((float)(c + 1), xm)));
+                            if (c + 1 < W) atomicAdd(row + c + 1, __fmul_rn(dh, __fsub_rn(xm, (float)c)));
+                        }
+                    });
+                } else {
+                    const bool down = E.dir > 0.0f;
+                    row_pieces(E, r, W, [&](int c, float, float, float u0, float u1) {
+                        if (c < 0) return;
+                        const float g = row[c];
+                        const float i1 = __fsub_rn(u1, u0);
+                        const float iu = __fmul_rn(__fmul_rn(0.5f, i1), __fadd_rn(u1, u0));
+                        const float i0 = __fsub_rn(i1, iu);
+                        ga = __fadd_rn(ga, __fmul_rn(g, down ? i0 : iu));
+                        gb = __fadd_rn(gb, __fmul_rn(g, down ? iu : i0));
+                    });
+                }
+            }
+            if (BWD) {
+                atomicAdd(&vgrad[E.e].x, __fmul_rn(E.perp.x, ga));
+                atomicAdd(&vgrad[E.e].y, __fmul_rn(E.perp.y, ga));
+                atomicAdd(&vgrad[E.nxt].x, __fmul_rn(E.perp.x, gb));
+                atomicAdd(&vgrad[E.nxt].y, __fmul_rn(E.perp.y, gb));
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ float cov_of(int rule, float s) {
+    if (rule == FT_NONZERO) return fminf(fmaxf(s, 0.0f), 1.0f);
+    const float m = __fsub_rn(s, __fmul_rn(2.0f, floorf(__fmul_rn(s, 0.5f))));
+    return m <= 1.0f ? m : __fsub_rn(2.0f, m);
+}
+__device__ __forceinline__ float cov_d(int rule, float s) {
+    if (rule == FT_NONZERO) return s > 0.0f && s < 1.0f ? 1.0f : 0.0f;
+    const float m = __fsub_rn(s, __fmul_rn(2.0f, floorf(__fmul_rn(s, 0.5f))));
+    return m < 1.0f ? 1.0f : -1.0f;
+}
+
+__device__ __forceinline__ float* px_at(float* base, const ft_path_desc& d, int r) {
+    return reinterpret_cast<float*>(reinterpret_cast<char*>(base) + d.raster_offset + (size_t)r * d.stride);
+}
+
+template <bool BWD>
+__global__ void __launch_bounds__(ABLOCK) k_adjoint(AParams p) {
+    extern __shared__ float band[];
+    __shared__ ASmem sm;
+    unsigned char* scr = p.scratch + (size_t)blockIdx.x * A_SCRATCH_PER_CTA;
+    float2* vpos = reinterpret_cast<float2*>(scr + AS_POS);
+    int* vsub = reinterpret_cast<int*>(scr + AS_SUB);
+    float2* vgrad = reinterpret_cast<float2*>(scr + AS_GRAD);
+    int* vflag = reinterpret_cast<int*>(scr + AS_FLAG);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (uint32_t path = blockIdx.x; path < p.n_paths; path += gridDim.x) {
+        const ft_path_desc d = p.paths[path];
+        const int W = (int)d.width, H = (int)d.height;
+        const ft_op* ops = p.ops + d.op_begin;
+        if (tid == 0) sm.status = FT_OK;
+        __syncthreads();
+        const int V = path_walk<WALK_EMIT>(p, sm, ops, (int)d.n_ops, vpos, vsub, vgrad, BWD, nullptr);
+        const bool cap = V > VCAP;
+        if (cap && tid == 0) atomicMax(&sm.status, (int)FT_ERR_CAP);
+        const float sign = cap ? 1.0f : fig_sign(sm, V, vpos, vsub, vflag);
+        const int rows_per_band = W > 0 ? max(1, BAND_FLOATS / W) : 1;
+        for (int b0 = 0; b0 < H && W > 0; b0 += rows_per_band) {
+            const int nb = min(rows_per_band, H - b0);
+            const int nc = nb * W;
+            if (!BWD) {
+                for (int i = tid; i < nc; i += ABLOCK) band[i] = 0.0f;
+            } else {
+                for (int i = tid; i < nc; i += ABLOCK) {
+                    const int r = b0 + i / W, c = i - (i / W) * W;
+                    const float g = px_at(const_cast<float*>(p.grad_cov), d, r)[c];
+                    band[i] = cap ? 0.0f : __fmul_rn(__fmul_rn(sign, g), cov_d(p.rule, px_at(p.area, d, r)[c]));
+                }
+            }
+            __syncthreads();
+            if (!cap) band_edges<BWD>(sm, band, W, b0, nb, V, vpos, vsub, vgrad);
+            if (!BWD) {
+                __syncthreads();
+                for (int rr = warp; rr < nb; rr += NW) {
+                    float* ar = px_at(p.area, d, b0 + rr);
+                    float* cv = px_at(p.cov, d, b0 + rr);
+                    const float* src = band + (size_t)rr * W;
+                    float carry = 0.0f;
+                    for (int c0 = 0; c0 < W; c0 += 32) {
+                        const int c = c0 + lane;
+                        float v = c < W ? src[c] : 0.0f;
+#pragma unroll
+                        for (int o = 1; o < 32; o <<= 1) {
+                            const float t = __shfl_up_sync(FULL, v, o);
+                            if (lane >= o) v = __fadd_rn(v, t);
+                        }
+                        v = __fadd_rn(v, carry);
+                        carry = __shfl_sync(FULL, v, 31);
+                        if (c < W) {
+                            const float sv = __fmul_rn(sign, v);
+                            ar[c] = sv;
+                            cv[c] = cov_of(p.rule, sv);
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        if (BWD && !cap) {
+            path_walk<WALK_GRAD>(p, sm, ops, (int)d.n_ops, vpos, vsub, vgrad, false,
+                                 p.grad_ops + (size_t)d.op_begin * 6);
+        }
+        if (tid == 0) p.status[path] = sm.status;
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+int adjoint_blocks_per_sm(bool backward) {
+    const int smem = BAND_FLOATS * (int)sizeof(float);
+    int n = 0;
+    if (backward) {
+        cudaFuncSetAttribute(k_adjoint<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_adjoint<true>, ABLOCK, smem);
+    } else {
+        cudaFuncSetAttribute(k_adjoint<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_adjoint<false>, ABLOCK, smem);
+    }
+    return n > 0 ? n : 1;
+}
+
+cudaError_t launch_adjoint(bool backward, const AParams& p, int grid, cudaStream_t s) {
+    const int smem = BAND_FLOATS * (int)sizeof(float);
+    if (backward) {
+        cudaFuncSetAttribute(k_adjoint<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        k_adjoint<true><<<grid, ABLOCK, smem, s>>>(p);
+    } else {
+        cudaFuncSetAttribute(k_adjoint<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        k_adjoint<false><<<grid, ABLOCK, smem, s>>>(p);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace fta

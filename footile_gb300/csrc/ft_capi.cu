@@ -8,6 +8,7 @@
 #include <string>
 #include <vector>
 
+#include "ft_adjoint.cuh"
 #include "ft_kernels.cuh"
 
 namespace {
@@ -789,7 +790,188 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
     return fail(c, FT_ERR_NOMEM, "edge pool did not converge");
 }
 
+// ------------------------------------------------------------ coverage adjoint
+// Saved state between ft_adjoint_forward and ft_adjoint_backward.
+struct ft_adjoint {
+    ft_ctx* ctx = nullptr;
+    DevBuf ops, paths, area, status, scratch, cov, gcov, gops, gwidth;
+    std::vector<ft_path_desc> h_paths;
+    uint32_t n_ops = 0, n_paths = 0;
+    uint64_t cov_bytes = 0;
+    int rule = FT_NONZERO;
+    float xf[6] = {1, 0, 0, 0, 1, 0};
+    float tol_sq = 0.09f;
+    int grid_f = 1, grid_b = 1;
+    bool ready = false;
+};
+
+static int adjoint_check_path(ft_ctx* c, const ft_path_desc& d, uint64_t cov_bytes, uint64_t n_ops_total) {
+    if ((uint64_t)d.op_begin + d.n_ops > n_ops_total) return fail(c, FT_ERR_ARG, "path ops out of range");
+    if (d.width > FT_MAX_WIDTH) return fail(c, FT_ERR_CAP, "coverage wider than FT_MAX_WIDTH");
+    if (d.width == 0 || d.height == 0) return FT_OK;
+    if ((d.raster_offset & 3) || (d.stride & 3)) return fail(c, FT_ERR_ARG, "coverage offset and stride need 4-byte alignment");
+    if ((uint64_t)d.stride < 4ull * d.width) return fail(c, FT_ERR_ARG, "coverage stride below 4 * width");
+    const uint64_t end = d.raster_offset + (uint64_t)d.stride * (d.height - 1) + 4ull * d.width;
+    if (end > cov_bytes) return fail(c, FT_ERR_ARG, "coverage outside the buffer");
+    return FT_OK;
+}
+
 extern "C" {
+
+FT_API int ft_adjoint_forward(ft_ctx* c, int32_t rule, const ft_op* ops, uint32_t n_ops_total,
+                              const ft_path_desc* paths, uint32_t n_paths, float* cov, uint64_t cov_bytes,
+                              int32_t where, ft_adjoint** saved) {
+    if (!c || !saved) return FT_ERR_ARG;
+    if ((rule != FT_NONZERO && rule != FT_EVENODD) || (where != FT_HOST && where != FT_DEVICE))
+        return fail(c, FT_ERR_ARG, "bad rule or location");
+    if ((n_paths && !paths) || (n_ops_total && !ops) || (cov_bytes && !cov))
+        return fail(c, FT_ERR_ARG, "null pointer");
+    for (uint32_t i = 0; i < n_paths; i++) {
+        int st = adjoint_check_path(c, paths[i], cov_bytes, n_ops_total);
+        if (st != FT_OK) return st;
+    }
+    if (where == FT_DEVICE && ((reinterpret_cast<uintptr_t>(ops) & 15) || (reinterpret_cast<uintptr_t>(cov) & 3)))
+        return fail(c, FT_ERR_ARG, "device ops need 16-byte alignment, coverage 4-byte alignment");
+    if (where == FT_HOST && !valid_ops_host(ops, n_ops_total)) return fail(c, FT_ERR_ARG, "unknown path op kind");
+    FT_CU(cudaSetDevice(c->device), "set device");
+    ft_adjoint* a = *saved;
+    if (!a) {
+        a = new ft_adjoint();
+        a->ctx = c;
+        *saved = a;
+    }
+    a->ready = false;
+    a->rule = rule;
+    a->n_ops = n_ops_total;
+    a->n_paths = n_paths;
+    a->cov_bytes = cov_bytes;
+    a->h_paths.assign(paths, paths + n_paths);
+    for (int k = 0; k < 6; k++) a->xf[k] = c->xf[k];
+    const float t = std::max(c->tolerance, 0.01f);
+    a->tol_sq = t * t;
+    FT_CU(a->ops.ensure(sizeof(ft_op) * std::max(n_ops_total, 1u)), "alloc ops");
+    FT_CU(a->paths.ensure(sizeof(ft_path_desc) * std::max(n_paths, 1u)), "alloc paths");
+    FT_CU(a->status.ensure(sizeof(int32_t) * std::max(n_paths, 1u)), "alloc status");
+    FT_CU(a->area.ensure(std::max<uint64_t>(cov_bytes, 4)), "alloc winding area");
+    const int bps_f = fta::adjoint_blocks_per_sm(false), bps_b = fta::adjoint_blocks_per_sm(true);
+    a->grid_f = (int)std::max(1u, std::min<uint32_t>(n_paths, (uint32_t)(bps_f * c->sm_count)));
+    a->grid_b = (int)std::max(1u, std::min<uint32_t>(n_paths, (uint32_t)(bps_b * c->sm_count)));
+    FT_CU(a->scratch.ensure(fta::A_SCRATCH_PER_CTA * (size_t)std::max(a->grid_f, a->grid_b)), "alloc scratch");
+    if (n_ops_total)
+        FT_CU(cudaMemcpyAsync(a->ops.p, ops, sizeof(ft_op) * n_ops_total,
+                              where == FT_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, c->stream),
+              "copy ops");
+    if (n_paths)
+        FT_CU(cudaMemcpyAsync(a->paths.p, paths, sizeof(ft_path_desc) * n_paths, cudaMemcpyHostToDevice, c->stream),
+              "upload paths");
+    FT_CU(cudaMemsetAsync(a->status.p, 0, sizeof(int32_t) * std::max(n_paths, 1u), c->stream), "reset status");
+    float* cov_d = cov;
+    if (where == FT_HOST) {
+        FT_CU(a->cov.ensure(std::max<uint64_t>(cov_bytes, 4)), "alloc coverage");
+        cov_d = static_cast<float*>(a->cov.p);
+    }
+    fta::AParams p{};
+    p.ops = static_cast<const ft_op*>(a->ops.p);
+    p.paths = static_cast<const ft_path_desc*>(a->paths.p);
+    p.n_paths = n_paths;
+    p.cov = cov_d;
+    p.area = static_cast<float*>(a->area.p);
+    p.status = static_cast<int*>(a->status.p);
+    p.scratch = static_cast<unsigned char*>(a->scratch.p);
+    for (int k = 0; k < 6; k++) p.xf[k] = a->xf[k];
+    p.tol_sq = a->tol_sq;
+    p.rule = rule;
+    FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
+    if (n_paths) {
+        FT_CU(fta::launch_adjoint(false, p, a->grid_f, c->stream), "launch adjoint forward");
+        c->launches++;
+    }
+    FT_CU(cudaEventRecord(c->ev1, c->stream), "event");
+    c->timed = true;
+    if (where == FT_HOST) {
+        if (cov_bytes) FT_CU(cudaMemcpyAsync(cov, cov_d, cov_bytes, cudaMemcpyDeviceToHost, c->stream), "download coverage");
+        FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
+    }
+    a->ready = true;
+    return FT_OK;
+}
+
+FT_API int ft_adjoint_backward(ft_ctx* c, ft_adjoint* a, const float* grad_cov, float* grad_ops, float* grad_width,
+                               int32_t where) {
+    if (!c || !a) return FT_ERR_ARG;
+    if (!a->ready) return fail(c, FT_ERR_ARG, "backward without a forward");
+    if (a->ctx != c) return fail(c, FT_ERR_ARG, "saved state belongs to another context");
+    if (where != FT_HOST && where != FT_DEVICE) return fail(c, FT_ERR_ARG, "bad location");
+    if ((a->cov_bytes && !grad_cov) || (a->n_ops && !grad_ops)) return fail(c, FT_ERR_ARG, "null pointer");
+    if (where == FT_DEVICE && (reinterpret_cast<uintptr_t>(grad_cov) & 3))
+        return fail(c, FT_ERR_ARG, "grad_cov needs 4-byte alignment");
+    FT_CU(cudaSetDevice(c->device), "set device");
+    const size_t gops_bytes = sizeof(float) * 6 * (size_t)a->n_ops;
+    const float* gcov_d = grad_cov;
+    float* gops_d = grad_ops;
+    if (where == FT_HOST) {
+        FT_CU(a->gcov.ensure(std::max<uint64_t>(a->cov_bytes, 4)), "alloc coverage gradient");
+        FT_CU(a->gops.ensure(std::max<size_t>(gops_bytes, 4)), "alloc op gradient");
+        if (a->cov_bytes)
+            FT_CU(cudaMemcpyAsync(a->gcov.p, grad_cov, a->cov_bytes, cudaMemcpyHostToDevice, c->stream),
+                  "upload coverage gradient");
+        gcov_d = static_cast<const float*>(a->gcov.p);
+        gops_d = static_cast<float*>(a->gops.p);
+    }
+    if (gops_bytes) FT_CU(cudaMemsetAsync(gops_d, 0, gops_bytes, c->stream), "reset op gradient");
+    fta::AParams p{};
+    p.ops = static_cast<const ft_op*>(a->ops.p);
+    p.paths = static_cast<const ft_path_desc*>(a->paths.p);
+    p.n_paths = a->n_paths;
+    p.area = static_cast<float*>(a->area.p);
+    p.grad_cov = gcov_d;
+    p.grad_ops = gops_d;
+    p.status = static_cast<int*>(a->status.p);
+    p.scratch = static_cast<unsigned char*>(a->scratch.p);
+    for (int k = 0; k < 6; k++) p.xf[k] = a->xf[k];
+    p.tol_sq = a->tol_sq;
+    p.rule = a->rule;
+    FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
+    if (a->n_paths) {
+        FT_CU(fta::launch_adjoint(true, p, a->grid_b, c->stream), "launch adjoint backward");
+        c->launches++;
+    }
+    FT_CU(cudaEventRecord(c->ev1, c->stream), "event");
+    c->timed = true;
+    if (grad_width && a->n_paths) {
+        if (where == FT_HOST)
+            std::fill(grad_width, grad_width + a->n_paths, 0.0f);
+        else
+            FT_CU(cudaMemsetAsync(grad_width, 0, sizeof(float) * a->n_paths, c->stream), "reset width gradient");
+    }
+    if (where == FT_HOST) {
+        if (gops_bytes)
+            FT_CU(cudaMemcpyAsync(grad_ops, gops_d, gops_bytes, cudaMemcpyDeviceToHost, c->stream),
+                  "download op gradient");
+        FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
+    }
+    return FT_OK;
+}
+
+FT_API int ft_adjoint_status(ft_ctx* c, ft_adjoint* a, int32_t* status, uint32_t n) {
+    if (!c || !a || (n && !status)) return FT_ERR_ARG;
+    FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
+    const uint32_t k = std::min(n, a->ready ? a->n_paths : 0u);
+    if (k) FT_CU(cudaMemcpy(status, a->status.p, sizeof(int32_t) * k, cudaMemcpyDeviceToHost), "status");
+    for (uint32_t i = k; i < n; i++) status[i] = FT_OK;
+    return FT_OK;
+}
+
+FT_API void ft_adjoint_destroy(ft_adjoint* a) {
+    if (!a) return;
+    if (a->ctx) {
+        cudaSetDevice(a->ctx->device);
+        if (a->ctx->stream) cudaStreamSynchronize(a->ctx->stream);
+    }
+    DevBuf* bufs[] = {&a->ops, &a->paths, &a->area, &a->status, &a->scratch, &a->cov, &a->gcov, &a->gops, &a->gwidth};
+    for (DevBuf* b : bufs) b->release();
+    delete a;
+}
 
 FT_API int ft_batch_status(ft_ctx* c, int32_t* status, uint32_t n) {
     if (!c || (n && !status)) return FT_ERR_ARG;

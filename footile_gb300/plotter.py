@@ -176,6 +176,7 @@ def fill_batch(ctx, ops, paths, fmt, rasters, rule=FillRule.NonZero, stroke=Fals
     paths = np.ascontiguousarray(paths, dtype=_abi.PATH_DTYPE)
     if _is_torch_cuda(rasters):
         where = _abi.DEVICE
+        ctx.torch_fence()
         optr, n_ops = ops.data_ptr(), ops.numel() * ops.element_size() // 32
         rptr, nbytes = rasters.data_ptr(), rasters.numel() * rasters.element_size()
     else:
@@ -260,6 +261,7 @@ def composite_batch(ctx, ops, paths, fmt, raster, rule=FillRule.NonZero, stroke=
     h, w = int(raster.shape[0]), int(raster.shape[1])
     if _is_torch_cuda(raster):
         where = _abi.DEVICE
+        ctx.torch_fence()
         optr, n_ops = ops.data_ptr(), ops.numel() * ops.element_size() // 32
         rptr = raster.data_ptr()
         stride = int(raster.stride(0)) * raster.element_size()

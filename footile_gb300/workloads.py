@@ -149,6 +149,18 @@ def cubics_1024(seed=4, n_paths=1024, n_seg=32, side=128):
     return ops, paths, nbytes
 
 
+def cubics_1024_coverage(seed=4, target_seed=5, n_paths=1024, n_seg=32, side=128):
+    """The closed-cubic batch of `cubics_1024` packed for the coverage adjoint: one f32
+    coverage plane per path, and a target of uniform [0, 1) values (seed 5) for the
+    L2 loss sum((cov - target)^2).  Returns (ops, paths, cov_bytes, target)."""
+    from .adjoint import pack_coverage
+    ops, paths, _ = cubics_1024(seed, n_paths, n_seg, side)
+    per_path = [ops[p["op_begin"]:p["op_begin"] + p["n_ops"]] for p in paths]
+    ops_c, paths_c, cov_bytes = pack_coverage(per_path, [side] * n_paths)
+    target = np.random.default_rng(target_seed).random(cov_bytes // 4, dtype=np.float32)
+    return ops_c, paths_c, cov_bytes, target
+
+
 def strokes_16384(seed=6, n_paths=16384, side=2048, min_seg=8, max_seg=64):
     """Open cubic paths with a PenWidth op each, premultiplied colours, one canvas."""
     rng = np.random.default_rng(seed)

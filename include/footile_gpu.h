@@ -190,6 +190,40 @@ FT_API int ft_fill_noalloc(int32_t rule, const ft_op* ops, uint32_t n_ops, int32
                            uint32_t stride, const float transform[6], float tolerance,
                            float pen_width, int32_t* status, void* stream);
 
+/* Coverage adjoint — no counterpart in footile, which has no gradients.  A
+ * differentiable FP32 coverage of a batch of fills and its backward pass, for a
+ * torch.autograd.Function (or any reverse-mode caller) to wrap.
+ *
+ * Coverage: the path walk and De Casteljau subdivision of Plotter::fill
+ * (plotter.rs:175-332, the same f32 subdivision tree as ft_fill), sub-figures as
+ * Fig builds them (fig.rs:428-461), covered with the cell-area scheme of
+ * fig.rs:285-321 in float without the 16.16 / 1/256 quantisation (the exact area of
+ * the flattened polygon in each pixel), the row prefix sum of imgbuf.rs:38-51 as the
+ * winding area S, then NonZero min(|S|, 1) or EvenOdd the triangle wave of period 2.
+ *
+ * ft_adjoint_forward writes the coverage of path i (width x height floats) into
+ * `cov` at paths[i].raster_offset bytes with paths[i].stride bytes per row (both
+ * multiples of 4, widths up to FT_MAX_WIDTH) and keeps in `*saved` (created when
+ * NULL, reused otherwise) a copy of the ops and paths and the winding area: 4 bytes
+ * per coverage byte.  ft_adjoint_backward takes dLoss/dcov in the layout of `cov`,
+ * recomputes the flattened edges and writes dLoss/d(op floats) to `grad_ops`
+ * (6 floats per op, the layout of ft_op.v: overwritten, zero for Close and for
+ * PenWidth in a fill) and zero to `grad_width` (one float per path: a fill's coverage
+ * does not depend on the pen width; may be NULL).  Gradients hold the subdivision
+ * tree fixed: it is piecewise constant in the control points.  The tolerance and
+ * transform are the context's at the forward call.  `where` is FT_HOST or FT_DEVICE
+ * for ops, cov, grad_cov, grad_ops and grad_width; path descriptors are host memory.
+ * Per-path status (FT_ERR_DEPTH, FT_ERR_ARG, FT_ERR_CAP for more than FT_MAX_POINTS
+ * flattened vertices: coverage zero, gradient zero) via ft_adjoint_status. */
+typedef struct ft_adjoint ft_adjoint;
+FT_API int ft_adjoint_forward(ft_ctx* ctx, int32_t rule, const ft_op* ops, uint32_t n_ops_total,
+                              const ft_path_desc* paths, uint32_t n_paths, float* cov,
+                              uint64_t cov_bytes, int32_t where, ft_adjoint** saved);
+FT_API int ft_adjoint_backward(ft_ctx* ctx, ft_adjoint* saved, const float* grad_cov, float* grad_ops,
+                               float* grad_width, int32_t where);
+FT_API int ft_adjoint_status(ft_ctx* ctx, ft_adjoint* saved, int32_t* status, uint32_t n);
+FT_API void ft_adjoint_destroy(ft_adjoint* saved);
+
 /* Per-path status codes of the last batch (synchronises the context stream). */
 FT_API int ft_batch_status(ft_ctx* ctx, int32_t* status, uint32_t n);
 

@@ -83,6 +83,12 @@ def lib():
             L.orc_composite.argtypes = [i32, i32, P, P, u32, i32, P, u32, u32, u32, ctypes.POINTER(Params),
                                         ctypes.POINTER(ctypes.c_float), P]
             L.orc_composite.restype = ctypes.c_int
+            D = ctypes.POINTER(ctypes.c_double)
+            L.orc_adj_forward.argtypes = [i32, P, u32, P, u32, u32, ctypes.c_float, P, P, P]
+            L.orc_adj_forward.restype = ctypes.c_int
+            L.orc_adj_backward.argtypes = [i32, P, u32, P, u32, u32, ctypes.c_float, P, P, P, P]
+            L.orc_adj_backward.restype = ctypes.c_int
+            del D
             _lib = L
     return _lib
 
@@ -206,3 +212,37 @@ def composite(stroke, rule, ops, paths, fmt, raster, s_width=1.0, **params):
     lib().orc_composite(stroke, rule, _ptr(ops), _ptr(paths), len(paths), fmt, _ptr(raster), w, h,
                         raster.strides[0], ctypes.byref(make_params(**params)), ctypes.byref(sw), _ptr(status))
     return status, sw.value
+
+
+# ------------------------------------------------------------ coverage adjoint (FP64)
+def _xf(transform):
+    return np.ascontiguousarray(np.asarray(transform, dtype=np.float32))
+
+
+def adj_forward(rule, ops, w, h, val=None, tolerance=0.3, transform=_abi.IDENTITY):
+    """FP64 analytic coverage of one fill: returns (cov, area, status), each (h, w) f64.
+
+    Without `val` the polygon is footile's f32 flattened polygon (the vertices Fig
+    receives), widened to double.  With `val` (n_ops x 6 f64) the vertices are the
+    Bernstein points of `val` on the subdivision tree the op floats decide (for
+    finite differences)."""
+    ops = np.ascontiguousarray(ops, dtype=_abi.OP_DTYPE)
+    cov = np.zeros((h, w), np.float64)
+    area = np.zeros((h, w), np.float64)
+    v = None if val is None else np.ascontiguousarray(val, dtype=np.float64)
+    xf = _xf(transform)
+    st = lib().orc_adj_forward(rule, _ptr(ops), len(ops), _ptr(v), w, h, tolerance, _ptr(xf), _ptr(cov), _ptr(area))
+    return cov, area, st
+
+
+def adj_backward(rule, ops, w, h, area, grad_cov, val=None, tolerance=0.3, transform=_abi.IDENTITY):
+    """FP64 gradient of sum(grad_cov * cov) with respect to the op floats: (n_ops, 6) f64."""
+    ops = np.ascontiguousarray(ops, dtype=_abi.OP_DTYPE)
+    area = np.ascontiguousarray(area, dtype=np.float64)
+    g = np.ascontiguousarray(grad_cov, dtype=np.float64)
+    out = np.zeros((len(ops), 6), np.float64)
+    v = None if val is None else np.ascontiguousarray(val, dtype=np.float64)
+    xf = _xf(transform)
+    lib().orc_adj_backward(rule, _ptr(ops), len(ops), _ptr(v), w, h, tolerance, _ptr(xf), _ptr(area), _ptr(g),
+                           _ptr(out))
+    return out

@@ -1,0 +1,132 @@
+"""CPU checks of the FP64 gradient oracle of the coverage adjoint.
+
+The oracle defines the differentiable coverage (exact area of the flattened polygon
+per pixel, NonZero / EvenOdd) and its gradient with respect to the op floats.  Here
+it is checked against itself by central differences with the subdivision tree held
+(vertices as Bernstein points of the perturbed floats), against supersampling, and
+against footile's integer masks (which approximate the same area)."""
+
+import numpy as np
+import pytest
+
+import oracle
+from footile_gb300 import _abi, workloads
+from footile_gb300.path import Path2D
+
+SHAPE = (Path2D().absolute().move_to(20.3, 10.1).line_to(100.7, 30.2).cubic_to(120, 80, 40, 120, 30.5, 90.25)
+         .quad_to(5, 60, 15.5, 40.5).close().finish())
+# two sub-figures, one crossing the left and bottom raster edges, and an open one
+MULTI = (Path2D().absolute().move_to(-10.5, 20.25).cubic_to(30, -5, 60, 70, 20.5, 60.75).line_to(-4, 50).close()
+         .move_to(40.2, 40.7).quad_to(90, 10, 70.3, 75.1).line_to(55.6, 70.2).cubic_to(50, 60, 45, 90, 30.1, 70.4)
+         .close().move_to(10, 5).line_to(60.5, 12.25).line_to(30.75, 20.5).finish())
+
+
+def values(ops):
+    return np.array([o["v"] for o in ops], dtype=np.float64)
+
+
+def test_bernstein_and_float_polygons_agree():
+    # the f32 De Casteljau vertices and the f64 Bernstein points of the same tree
+    base = values(SHAPE)
+    c32, _, _ = oracle.adj_forward(_abi.NONZERO, SHAPE, 128, 128)
+    c64, _, _ = oracle.adj_forward(_abi.NONZERO, SHAPE, 128, 128, val=base)
+    assert np.abs(c32 - c64).max() < 1e-4
+
+
+def fd_grad(rule, ops, w, h, target, h_step, transform=_abi.IDENTITY, entries=None):
+    base = values(ops)
+    fd = np.zeros_like(base)
+    idx = entries if entries is not None else [(i, k) for i in range(len(ops)) for k in range(6)]
+    for i, k in idx:
+        vp, vm = base.copy(), base.copy()
+        vp[i, k] += h_step
+        vm[i, k] -= h_step
+        lp = ((oracle.adj_forward(rule, ops, w, h, val=vp, transform=transform)[0] - target) ** 2).sum()
+        lm = ((oracle.adj_forward(rule, ops, w, h, val=vm, transform=transform)[0] - target) ** 2).sum()
+        fd[i, k] = (lp - lm) / (2 * h_step)
+    return fd
+
+
+@pytest.mark.parametrize("rule", [_abi.NONZERO, _abi.EVENODD])
+@pytest.mark.parametrize("shape", ["shape", "multi"])
+def test_oracle_gradient_matches_central_differences(rule, shape):
+    ops = SHAPE if shape == "shape" else MULTI
+    w = h = 96 if shape == "multi" else 128
+    target = np.random.default_rng(5).random((h, w))
+    base = values(ops)
+    cov, area, st = oracle.adj_forward(rule, ops, w, h, val=base)
+    assert st == 0
+    g = oracle.adj_backward(rule, ops, w, h, area, 2 * (cov - target), val=base)
+    # central differences converge to the analytic gradient as the step shrinks
+    fd = fd_grad(rule, ops, w, h, target, 1e-5)
+    scale = np.abs(g).max()
+    assert scale > 0
+    assert np.abs(g - fd).max() / scale < 2e-4
+    # Close and the unused slots of Move/Line/Quad take no gradient
+    for i, o in enumerate(ops):
+        used = {_abi.OP_MOVE: 2, _abi.OP_LINE: 2, _abi.OP_QUAD: 4, _abi.OP_CUBIC: 6}.get(int(o["kind"]), 0)
+        assert not g[i, used:].any()
+
+
+def test_oracle_gradient_at_the_specified_step():
+    # h = 1e-2 px: the loss is piecewise quadratic with kinks (|S| = 0 or 1), so central
+    # differences at this step agree to about 1 %
+    target = np.random.default_rng(5).random((128, 128))
+    base = values(SHAPE)
+    cov, area, _ = oracle.adj_forward(_abi.NONZERO, SHAPE, 128, 128, val=base)
+    g = oracle.adj_backward(_abi.NONZERO, SHAPE, 128, 128, area, 2 * (cov - target), val=base)
+    fd = fd_grad(_abi.NONZERO, SHAPE, 128, 128, target, 1e-2)
+    assert np.abs(g - fd).max() / np.abs(fd).max() < 3e-2
+
+
+def test_oracle_gradient_through_transform():
+    m = (0.9, 0.2, 5.0, -0.15, 1.1, -3.0)
+    target = np.random.default_rng(6).random((128, 128))
+    base = values(SHAPE)
+    cov, area, _ = oracle.adj_forward(_abi.NONZERO, SHAPE, 128, 128, val=base, transform=m)
+    g = oracle.adj_backward(_abi.NONZERO, SHAPE, 128, 128, area, 2 * (cov - target), val=base, transform=m)
+    fd = fd_grad(_abi.NONZERO, SHAPE, 128, 128, target, 1e-5, transform=m)
+    assert np.abs(g - fd).max() / np.abs(g).max() < 2e-4
+
+
+def test_oracle_coverage_is_the_polygon_area():
+    # 16 x 16 supersampling of the same flattened polygon (footile's Fixed vertices)
+    w = h = 128
+    cov, _, _ = oracle.adj_forward(_abi.NONZERO, SHAPE, w, h)
+    pts = oracle.fig_points(SHAPE).astype(np.float64) / 65536
+    s = 16
+    ys = (np.arange(h * s) + 0.5) / s
+    xs = (np.arange(w * s) + 0.5) / s
+    X, Y = np.meshgrid(xs, ys)
+    wn = np.zeros_like(X)
+    for i in range(len(pts)):
+        (x0, y0), (x1, y1) = pts[i], pts[(i + 1) % len(pts)]
+        if y0 == y1:
+            continue
+        xi = x0 + (Y - y0) * (x1 - x0) / (y1 - y0)
+        wn += ((y0 <= Y) & (Y < y1) & (X < xi)).astype(float) - ((y1 <= Y) & (Y < y0) & (X < xi)).astype(float)
+    ss = np.minimum(np.abs(wn), 1).reshape(h, s, w, s).mean(axis=(1, 3))
+    assert np.abs(cov - ss).max() < 4 / 255
+
+
+def test_oracle_coverage_tracks_footile_masks():
+    # footile's 16.16 cell walk approximates the same coverage: close on average
+    ops, paths, cov_bytes, _ = workloads.cubics_1024_coverage(n_paths=8)
+    for p in paths:
+        o = ops[p["op_begin"]:p["op_begin"] + p["n_ops"]]
+        cov, _, st = oracle.adj_forward(_abi.NONZERO, o, 128, 128)
+        m = np.zeros((128, 128), np.uint8)
+        oracle.fill(_abi.NONZERO, o, m, _abi.MATTE8, clr=(255, 255, 255, 255))
+        d = np.abs(cov * 255 - m)
+        assert st == 0 and d.mean() < 1.5 and np.median(d) < 1.0
+
+
+def test_oracle_vertex_cap_status():
+    n = 70000
+    ops = np.zeros(n + 2, dtype=_abi.OP_DTYPE)
+    ops["kind"][0] = _abi.OP_MOVE
+    ops["kind"][1:-1] = _abi.OP_LINE
+    ops["v"][:-1, :2] = np.random.default_rng(1).random((n + 1, 2)) * 50
+    ops["kind"][-1] = _abi.OP_CLOSE
+    cov, _, st = oracle.adj_forward(_abi.NONZERO, ops, 64, 64)
+    assert st == _abi.ERR_CAP and not cov.any()
