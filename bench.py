@@ -47,6 +47,8 @@ def parse_args():
     ap.add_argument("--per-path-sample", type=int, default=4096)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the secondary workloads")
+    ap.add_argument("--no-tune", action="store_true", help="use the built-in plan instead of the autotuner")
+    ap.add_argument("--tune-cache", default=None, help="autotuner cache file (looked up, then appended)")
     ap.add_argument("--only", choices=["single", "scene", "strokes", "adjoint"],
                     help="run one secondary workload alone (for profiling) and print its line")
     return ap.parse_args()
@@ -444,6 +446,28 @@ def run_ours(args):
     ctx.set_stream(stream.cuda_stream)
     ops_d = torch.from_numpy(ops.view(np.uint8)).to(dev)
     ras_d = torch.zeros(nbytes, dtype=torch.uint8, device=dev)
+    torch.cuda.synchronize()
+
+    # ---- plan: the built-in one, then the autotuner's choice (both outside the timed region)
+    def launch_ms(b, reps=5):
+        b.launch(ops_d, ras_d)
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        for _ in range(reps):
+            b.launch(ops_d, ras_d)
+        a1.record(stream)
+        torch.cuda.synchronize()
+        return a0.elapsed_time(a1) / reps
+    tune_info = {"autotuned": False}
+    if not args.no_tune:
+        b0 = PreparedBatch(ctx, paths, _abi.MATTE8)
+        tune_info["default_plan_ms"] = launch_ms(b0)
+        tune_info["default_plan"] = ctx.tuning()
+        b0.close()
+        t0 = time.perf_counter()
+        chosen, tms = ctx.autotune(ops_d, paths, _abi.MATTE8, ras_d, cache_path=args.tune_cache)
+        tune_info.update({"autotuned": True, "chosen_plan": chosen, "chosen_plan_ms_while_tuning": tms,
+                          "tuning_s": time.perf_counter() - t0})
     batch = PreparedBatch(ctx, paths, _abi.MATTE8)
 
     from footile_gb300 import replicas
@@ -491,6 +515,7 @@ def run_ours(args):
     ops_np = ops_h.numpy().view(_abi.OP_DTYPE)
     ras_np = ras_h.numpy()
     ctx2 = Context(local)
+    ctx2.set_tuning(ctx.tuning())
     fill_batch(ctx2, ops_np, paths, _abi.MATTE8, ras_np)  # warm (allocations)
     barrier()
     t0 = time.perf_counter()
@@ -533,6 +558,7 @@ def run_ours(args):
 
     # ---- the other configurations, on rank 0 (device time, CUDA events)
     extras = None
+    ctx.set_tuning(None)  # the other workloads use the built-in plans
     if rank == 0 and not args.no_extras:
         extras = {}
         for name, fn in (("single_path_256", extra_single), ("scene_4096", extra_scene),
@@ -570,6 +596,7 @@ def run_ours(args):
                   "batched_over_per_path": (len(paths) / (ms_max * 1e-3) / per_path["paths_per_s"]) if per_path else None},
         "clocks": clk,
         "gpu_launches": int(launches),
+        "plan": tune_info,
         "workloads": extras,
     }
     print(json.dumps(out), flush=True)

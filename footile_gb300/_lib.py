@@ -60,6 +60,10 @@ def load(auto_build=True):
             "ft_adjoint_backward": ([P, P, P, P, P, i32], ctypes.c_int),
             "ft_adjoint_status": ([P, P, P, u32], ctypes.c_int),
             "ft_adjoint_destroy": ([P], None),
+            "ft_set_tuning": ([P, P], ctypes.c_int),
+            "ft_get_tuning": ([P, P], ctypes.c_int),
+            "ft_autotune_batch": ([P, i32, i32, P, u32, P, u32, i32, P, u64, ctypes.c_char_p, P,
+                                   ctypes.POINTER(f32)], ctypes.c_int),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -77,7 +81,16 @@ def exported_symbols():
         "ft_batch_status", "ft_sync", "ft_last_error", "ft_last_timings", "ft_launch_count",
         "ft_batch_create", "ft_batch_launch", "ft_batch_launch_status", "ft_batch_destroy",
         "ft_composite_batch", "ft_fill_noalloc", "ft_adjoint_forward", "ft_adjoint_backward", "ft_adjoint_status",
-        "ft_adjoint_destroy")]
+        "ft_adjoint_destroy", "ft_set_tuning", "ft_get_tuning", "ft_autotune_batch")]
+
+
+class Tuning(ctypes.Structure):
+    """`ft_tuning`: the knobs of a batch plan (see include/footile_gpu.h)."""
+    _fields_ = [("warp_max_side", ctypes.c_int32), ("cta_smem_bytes", ctypes.c_int32),
+                ("split_px", ctypes.c_int32), ("grid_per_sm", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
 
 
 class Context:
@@ -152,6 +165,35 @@ class Context:
 
     def launch_count(self):
         return int(self.L.ft_launch_count(self.h))
+
+    def set_tuning(self, tuning=None):
+        """Set the plan knobs from a dict (or `Tuning`); None restores the defaults."""
+        if tuning is None:
+            self.check(self.L.ft_set_tuning(self.h, None))
+            return
+        t = tuning if isinstance(tuning, Tuning) else Tuning(**tuning)
+        self.check(self.L.ft_set_tuning(self.h, ctypes.byref(t)))
+
+    def tuning(self):
+        t = Tuning()
+        self.check(self.L.ft_get_tuning(self.h, ctypes.byref(t)))
+        return t.as_dict()
+
+    def autotune(self, ops_dev, paths, fmt, rasters_dev, rule=0, stroke=False, cache_path=None):
+        """Time candidate plans of a batch on device buffers (CUDA tensors) and keep the
+        fastest as this context's tuning.  Returns (tuning dict, ms or 0 from the cache)."""
+        import numpy as np
+        paths = np.ascontiguousarray(paths, dtype=_abi.PATH_DTYPE)
+        n_ops = ops_dev.numel() * ops_dev.element_size() // 32
+        nbytes = rasters_dev.numel() * rasters_dev.element_size()
+        t = Tuning()
+        ms = ctypes.c_float()
+        cp = cache_path.encode() if cache_path else None
+        self.check(self.L.ft_autotune_batch(self.h, int(bool(stroke)), int(rule), ctypes.c_void_p(ops_dev.data_ptr()),
+                                            n_ops, paths.ctypes.data_as(ctypes.c_void_p), len(paths), fmt,
+                                            ctypes.c_void_p(rasters_dev.data_ptr()), nbytes, cp, ctypes.byref(t),
+                                            ctypes.byref(ms)))
+        return t.as_dict(), ms.value
 
     def batch_status(self, n):
         import numpy as np

@@ -61,6 +61,8 @@ struct ft_ctx {
     uint64_t launches = 0;
     int sm_count = 0;
     int max_smem = 0;
+    ft_tuning tune{0, 0, 0, 0};
+    bool tuned = false;  // `tune` replaces the built-in plan defaults
     std::string err;
 };
 
@@ -86,6 +88,8 @@ int cuda_fail(ft_ctx* c, cudaError_t e, const char* what) {
         if (_e != cudaSuccess) return cuda_fail(c, _e, what); \
     } while (0)
 
+// Plan knobs: an environment variable overrides the context's tuning (ft_set_tuning /
+// ft_autotune_batch), which overrides the built-in default.
 // Dynamic shared memory for a batch whose widest raster row is `max_w` pixels.
 int choose_smem(const ft_ctx* c, uint32_t max_w) {
     const int wp = (int)((max_w + 3) & ~3u);
@@ -93,6 +97,8 @@ int choose_smem(const ft_ctx* c, uint32_t max_w) {
     int smem;
     if (env) {
         smem = atoi(env);
+    } else if (c->tuned && c->tune.cta_smem_bytes > 0) {
+        smem = c->tune.cta_smem_bytes;
     } else if (wp <= 512) {
         smem = 48 * 1024;  // four CTAs per SM
     } else {
@@ -105,10 +111,26 @@ int choose_smem(const ft_ctx* c, uint32_t max_w) {
 }
 
 // Largest canvas side the warp rasteriser takes (FT_WARP_MAX_SIDE, 0 disables it).
-int warp_max_side() {
+int warp_max_side(const ft_ctx* c) {
     const char* env = getenv("FT_WARP_MAX_SIDE");
-    int v = env ? atoi(env) : ftk::WARP_MAX_SIDE;
+    int v = env ? atoi(env) : (c->tuned ? c->tune.warp_max_side : ftk::WARP_MAX_SIDE);
     return std::max(0, std::min(v, ftk::WARP_MAX_SIDE));
+}
+
+// Paths of at least this many pixels are split into row ranges (FT_SPLIT_PX).
+uint64_t split_px(const ft_ctx* c) {
+    const char* env = getenv("FT_SPLIT_PX");
+    if (env) return strtoull(env, nullptr, 10);
+    if (c->tuned && c->tune.split_px > 0) return (uint64_t)c->tune.split_px;
+    return (uint64_t)(1u << 20);
+}
+
+// Resident CTAs per SM of the persistent rasterisers (FT_GRID sets the whole grid).
+int grid_cap(const ft_ctx* c, int per_sm) {
+    const char* genv = getenv("FT_GRID");
+    if (genv) return atoi(genv);
+    if (c->tuned && c->tune.grid_per_sm > 0) per_sm = std::min(per_sm, (int)c->tune.grid_per_sm);
+    return c->sm_count * per_sm;
 }
 
 // Work items of the device queues: small paths go whole to the warp rasteriser,
@@ -119,11 +141,10 @@ void plan_items(ft_ctx* c, const ft_path_desc* paths, uint32_t n_paths, int smem
     out.clear();
     out_w.clear();
     const int area_bytes = smem - ftk::RASTER_FIXED_SMEM;
-    const char* env = getenv("FT_SPLIT_PX");
-    const uint64_t split_px = env ? strtoull(env, nullptr, 10) : (uint64_t)(1u << 20);
+    const uint64_t big_px = split_px(c);
     // few paths cannot fill the GPU one warp or one CTA each: split their rows instead
     const bool few = n_paths < (uint32_t)std::max(2 * c->sm_count, 1);
-    const uint32_t wside = (stroke || few) ? 0u : (uint32_t)warp_max_side();  // strokes use the CTA kernel
+    const uint32_t wside = (stroke || few) ? 0u : (uint32_t)warp_max_side(c);  // strokes use the CTA kernel
     for (uint32_t i = 0; i < n_paths; i++) {
         const ft_path_desc& d = paths[i];
         const uint32_t wp = (d.width + 3) & ~3u;
@@ -134,7 +155,7 @@ void plan_items(ft_ctx* c, const ft_path_desc* paths, uint32_t n_paths, int smem
             continue;
         }
         uint32_t rows_per_item = std::max(d.height, 1u);
-        if ((uint64_t)d.width * d.height >= split_px && c->sm_count > 0) {
+        if ((uint64_t)d.width * d.height >= big_px && c->sm_count > 0) {
             uint32_t target = (d.height + (uint32_t)c->sm_count - 1) / (uint32_t)c->sm_count;
             rows_per_item = std::max(R, ((target + R - 1) / R) * R);
         } else if (few && c->sm_count > 0) {
@@ -189,17 +210,13 @@ void fill_params(ft_ctx* c, ftk::KParams& p, int stroke, int rule, int fmt, int 
 }
 
 int grid_for(ft_ctx* c, int smem, uint32_t n_items, bool stroke) {
-    const int per_sm = ftk::raster_blocks_per_sm(smem, stroke);
-    const char* genv = getenv("FT_GRID");
-    int grid = genv ? atoi(genv) : c->sm_count * per_sm;
+    const int grid = grid_cap(c, ftk::raster_blocks_per_sm(smem, stroke));
     return std::max(1, std::min(grid, (int)std::max(n_items, 1u)));
 }
 
 // Grid of the warp rasteriser.
 int grid_for_warp(ft_ctx* c, uint32_t n_items_w) {
-    const int per_sm = ftk::raster_warp_blocks_per_sm();
-    const char* genv = getenv("FT_GRID");
-    int grid = genv ? atoi(genv) : c->sm_count * per_sm;
+    const int grid = grid_cap(c, ftk::raster_warp_blocks_per_sm());
     const int need = (int)((n_items_w + ftk::NWARP - 1) / ftk::NWARP);
     return std::max(1, std::min(grid, std::max(need, 1)));
 }
@@ -326,9 +343,7 @@ int single(ft_ctx* c, int stroke, int32_t rule, const ft_op* ops, uint32_t n_ops
     } else if ((reinterpret_cast<uintptr_t>(ops) & 15) || (fmt == FT_RGBA8P && (reinterpret_cast<uintptr_t>(raster) & 3))) {
         return fail(c, FT_ERR_ARG, "device ops need 16-byte alignment, Rgba8p rasters 4-byte alignment");
     }
-    const char* env = getenv("FT_SPLIT_PX");
-    const uint64_t big_px = env ? strtoull(env, nullptr, 10) : (uint64_t)(1u << 20);
-    if ((uint64_t)w * h >= big_px && ftk::composite_bands_smem(1, (int)w) <= c->max_smem) {
+    if ((uint64_t)w * h >= split_px(c) && ftk::composite_bands_smem(1, (int)w) <= c->max_smem) {
         // a large canvas: build the figure once and bin its edges, then one CTA per
         // band of rows (the ordered compositor with a single call)
         float sw0 = c->s_width;
@@ -522,6 +537,32 @@ FT_API void ft_batch_destroy(ft_batch* b) {
     delete b;
 }
 
+
+FT_API int ft_set_tuning(ft_ctx* c, const ft_tuning* t) {
+    if (!c) return FT_ERR_ARG;
+    if (!t) {
+        c->tune = ft_tuning{0, 0, 0, 0};
+        c->tuned = false;
+        return FT_OK;
+    }
+    if (t->warp_max_side < 0 || t->warp_max_side > ftk::WARP_MAX_SIDE || t->cta_smem_bytes < 0 ||
+        (t->cta_smem_bytes && t->cta_smem_bytes < 40 * 1024) || t->cta_smem_bytes > c->max_smem ||
+        t->split_px < 0 || t->grid_per_sm < 0)
+        return fail(c, FT_ERR_ARG, "tuning out of range");
+    c->tune = *t;
+    c->tuned = true;
+    return FT_OK;
+}
+
+FT_API int ft_get_tuning(ft_ctx* c, ft_tuning* t) {
+    if (!c || !t) return FT_ERR_ARG;
+    if (c->tuned) {
+        *t = c->tune;
+    } else {
+        *t = ft_tuning{ftk::WARP_MAX_SIDE, 0, 1 << 20, 0};
+    }
+    return FT_OK;
+}
 
 FT_API int ft_ctx_create(int device, ft_ctx** out) {
     if (!out) return FT_ERR_ARG;
@@ -790,6 +831,51 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
     return fail(c, FT_ERR_NOMEM, "edge pool did not converge");
 }
 
+// ------------------------------------------------------------------ autotuner
+// Signature of a batch for the tuning cache: GPU, call kind and powers of two of the
+// path count, mean / largest canvas side and mean op count.
+static std::string tune_key(ft_ctx* c, int stroke, int rule, int fmt, const ft_path_desc* paths, uint32_t n_paths) {
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, c->device) != cudaSuccess) prop.name[0] = 0;
+    double side = 0.0, ops = 0.0;
+    uint32_t max_side = 0;
+    for (uint32_t i = 0; i < n_paths; i++) {
+        side += 0.5 * ((double)paths[i].width + paths[i].height);
+        ops += paths[i].n_ops;
+        max_side = std::max(max_side, std::max(paths[i].width, paths[i].height));
+    }
+    auto lg = [](double v) { return v >= 1.0 ? (int)std::floor(std::log2(v)) : -1; };
+    const double n = std::max(n_paths, 1u);
+    std::string name(prop.name);
+    for (char& ch : name)
+        if (ch == ' ') ch = '_';
+    char buf[512];
+    snprintf(buf, sizeof(buf), "%s/sm%d/k%d.r%d.f%d/n%d.s%d.m%d.o%d", name.c_str(), c->sm_count, stroke, rule, fmt,
+             lg(n_paths), lg(side / n), lg(max_side), lg(ops / n));
+    return std::string(buf);
+}
+
+static bool tune_lookup(const char* path, const std::string& key, ft_tuning* t) {
+    if (!path) return false;
+    FILE* f = fopen(path, "r");
+    if (!f) return false;
+    char line[1024];
+    bool found = false;
+    while (fgets(line, sizeof(line), f)) {
+        char k[600];
+        ft_tuning v;
+        float ms;
+        if (sscanf(line, "%599s %d %d %d %d %f", k, &v.warp_max_side, &v.cta_smem_bytes, &v.split_px,
+                   &v.grid_per_sm, &ms) == 6 &&
+            key == k) {
+            *t = v;  // the last entry for a key wins
+            found = true;
+        }
+    }
+    fclose(f);
+    return found;
+}
+
 // ------------------------------------------------------------ coverage adjoint
 // Saved state between ft_adjoint_forward and ft_adjoint_backward.
 struct ft_adjoint {
@@ -971,6 +1057,82 @@ FT_API void ft_adjoint_destroy(ft_adjoint* a) {
     DevBuf* bufs[] = {&a->ops, &a->paths, &a->area, &a->status, &a->scratch, &a->cov, &a->gcov, &a->gops, &a->gwidth};
     for (DevBuf* b : bufs) b->release();
     delete a;
+}
+
+FT_API int ft_autotune_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* ops, uint32_t n_ops_total,
+                             const ft_path_desc* paths, uint32_t n_paths, int32_t fmt, uint8_t* rasters,
+                             uint64_t raster_bytes, const char* cache_path, ft_tuning* chosen, float* ms_out) {
+    if (!c) return FT_ERR_ARG;
+    if (n_paths && !paths) return fail(c, FT_ERR_ARG, "null path list");
+    for (uint32_t i = 0; i < n_paths; i++) {
+        int st = check_path(c, paths[i], fmt, raster_bytes, n_ops_total);
+        if (st != FT_OK) return st;
+    }
+    if (ms_out) *ms_out = 0.0f;
+    const std::string key = tune_key(c, stroke, rule, fmt, paths, n_paths);
+    ft_tuning best{0, 0, 0, 0};
+    if (tune_lookup(cache_path, key, &best) && ft_set_tuning(c, &best) == FT_OK) {
+        if (chosen) *chosen = best;
+        return FT_OK;
+    }
+    const ft_tuning saved = c->tune;
+    const bool saved_tuned = c->tuned;
+    // candidate plans: canvas side of the warp/CTA split x CTA tile height (shared
+    // memory) x resident CTAs per SM
+    const int sides[] = {0, 64, 128, 256, 512};
+    const int smems[] = {40 * 1024, 48 * 1024, 64 * 1024, 96 * 1024};
+    const int grids[] = {0, 2};
+    float best_ms = 0.0f;
+    bool have = false;
+    cudaEvent_t e0, e1;
+    FT_CU(cudaEventCreate(&e0), "event");
+    FT_CU(cudaEventCreate(&e1), "event");
+    for (int ws : sides)
+        for (int sm : smems)
+            for (int gp : grids) {
+                if (sm > c->max_smem) continue;
+                c->tune = ft_tuning{ws, sm, 1 << 20, gp};
+                c->tuned = true;
+                ft_batch* b = nullptr;
+                if (ft_batch_create(c, stroke, rule, paths, n_paths, fmt, &b) != FT_OK) continue;
+                bool ok = ft_batch_launch(c, b, ops, n_ops_total, rasters, raster_bytes) == FT_OK;  // warm-up
+                float total = 0.0f;
+                const int reps = 3;
+                if (ok) ok = cudaEventRecord(e0, c->stream) == cudaSuccess;
+                for (int r = 0; ok && r < reps; r++)
+                    ok = ft_batch_launch(c, b, ops, n_ops_total, rasters, raster_bytes) == FT_OK;
+                if (ok)
+                    ok = cudaEventRecord(e1, c->stream) == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess &&
+                         cudaEventElapsedTime(&total, e0, e1) == cudaSuccess;
+                ft_batch_destroy(b);
+                if (!ok) continue;
+                const float ms = total / reps;
+                if (!have || ms < best_ms) {
+                    best_ms = ms;
+                    best = c->tune;
+                    have = true;
+                }
+            }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (!have) {
+        c->tune = saved;
+        c->tuned = saved_tuned;
+        return fail(c, FT_ERR_CUDA, "no candidate plan ran");
+    }
+    c->tune = best;
+    c->tuned = true;
+    if (cache_path) {
+        FILE* f = fopen(cache_path, "a");
+        if (f) {
+            fprintf(f, "%s %d %d %d %d %.4f\n", key.c_str(), best.warp_max_side, best.cta_smem_bytes, best.split_px,
+                    best.grid_per_sm, best_ms);
+            fclose(f);
+        }
+    }
+    if (chosen) *chosen = best;
+    if (ms_out) *ms_out = best_ms;
+    return FT_OK;
 }
 
 FT_API int ft_batch_status(ft_ctx* c, int32_t* status, uint32_t n) {

@@ -170,6 +170,38 @@ FT_API int ft_batch_launch(ft_ctx* ctx, ft_batch* batch, const ft_op* ops, uint3
 FT_API int ft_batch_launch_status(ft_ctx* ctx, ft_batch* batch, int32_t* status, uint32_t n);
 FT_API void ft_batch_destroy(ft_batch* batch);
 
+/* Plan tuning — no counterpart in footile (its CPU plotter has nothing to tune).
+ * The knobs of a batch plan: `warp_max_side`, the largest canvas side given whole to
+ * one warp (0..512, 0 sends every path to the CTA rasteriser); `cta_smem_bytes`, the
+ * CTA rasteriser's shared memory, which sets its tile: bands of as many full-width rows
+ * as fit (0 = built-in choice); `split_px`, paths of at least this many pixels are
+ * split into row ranges, the queue grain of large paths (0 = 1 Mpx); `grid_per_sm`,
+ * resident CTAs per SM of the persistent kernels (0 = occupancy maximum).  Results do
+ * not depend on the tuning.  ft_set_tuning(ctx, NULL) restores the defaults.
+ * Environment variables FT_WARP_MAX_SIDE, FT_SMEM_BYTES, FT_SPLIT_PX and FT_GRID
+ * override both. */
+typedef struct ft_tuning {
+    int32_t warp_max_side;
+    int32_t cta_smem_bytes;
+    int32_t split_px;
+    int32_t grid_per_sm;
+} ft_tuning;
+FT_API int ft_set_tuning(ft_ctx* ctx, const ft_tuning* tuning);
+FT_API int ft_get_tuning(ft_ctx* ctx, ft_tuning* tuning);
+
+/* Autotuner: times candidate plans of this batch (prepared batches, graph replay, CUDA
+ * events on the context stream) and keeps the fastest as the context's tuning.  With
+ * `cache_path` (may be NULL) the choice is looked up first and appended after tuning,
+ * keyed by the GPU (name, SM count), the call kind and a signature of the batch
+ * (path count, mean and largest canvas side, mean op count, in powers of two).  `ops`
+ * and `rasters` are device pointers; the rasters are overwritten while tuning.
+ * `chosen` (may be NULL) receives the tuning; `ms` (may be NULL) its launch time
+ * (0 when taken from the cache). */
+FT_API int ft_autotune_batch(ft_ctx* ctx, int32_t stroke, int32_t rule, const ft_op* ops,
+                             uint32_t n_ops_total, const ft_path_desc* paths, uint32_t n_paths,
+                             int32_t fmt, uint8_t* rasters, uint64_t raster_bytes,
+                             const char* cache_path, ft_tuning* chosen, float* ms);
+
 /* Allocation-free fill of one path — this entry point has no counterpart in footile.
  * For callers that cannot allocate device memory: work recorded into a CUDA graph
  * while a stream is being captured, processes under a fixed device-memory budget,
