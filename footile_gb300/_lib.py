@@ -56,7 +56,7 @@ def load(auto_build=True):
             "ft_batch_launch_status": ([P, P, P, u32], ctypes.c_int),
             "ft_batch_destroy": ([P], None),
             "ft_composite_batch": ([P, i32, i32, P, u32, P, u32, i32, P, u32, u32, u32, i32], ctypes.c_int),
-            "ft_adjoint_forward": ([P, i32, P, u32, P, u32, P, u64, i32, ctypes.POINTER(P)], ctypes.c_int),
+            "ft_adjoint_forward": ([P, i32, i32, P, u32, P, u32, P, u64, i32, ctypes.POINTER(P)], ctypes.c_int),
             "ft_adjoint_backward": ([P, P, P, P, P, i32], ctypes.c_int),
             "ft_adjoint_status": ([P, P, P, u32], ctypes.c_int),
             "ft_adjoint_destroy": ([P], None),

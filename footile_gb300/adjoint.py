@@ -17,9 +17,10 @@ from . import _abi
 from ._lib import Context, load
 
 
-def pack_coverage(paths_ops, sizes):
+def pack_coverage(paths_ops, sizes, s_width=1.0):
     """Pack per-path op arrays and canvas sizes: (ops, paths, cov_bytes), one f32
-    coverage plane per path, back to back (row stride 4 * width)."""
+    coverage plane per path, back to back (row stride 4 * width); every path starts
+    with pen width `s_width` (footile's default 1.0)."""
     n = len(paths_ops)
     paths = np.zeros(n, dtype=_abi.PATH_DTYPE)
     lens = np.array([len(o) for o in paths_ops], dtype=np.int64)
@@ -33,6 +34,7 @@ def pack_coverage(paths_ops, sizes):
         paths[i]["height"] = h
         paths[i]["raster_offset"] = off
         paths[i]["stride"] = 4 * w
+        paths[i]["s_width"] = s_width
         off += 4 * w * h
     ops = np.concatenate([np.ascontiguousarray(o, dtype=_abi.OP_DTYPE) for o in paths_ops]) if n else \
         np.zeros(0, dtype=_abi.OP_DTYPE)
@@ -56,10 +58,12 @@ class Adjoint:
         self.n_ops = 0
         self.n_paths = 0
 
-    def forward(self, rule, ops, paths, cov):
+    def forward(self, rule, ops, paths, cov, stroke=False):
         """Coverage of every path into `cov` (numpy f32 array, or a CUDA tensor with
-        `ops` a CUDA tensor of ft_op records); returns `cov`.  CUDA tensors are used on
-        the context's stream, ordered after torch's current stream (Context.torch_fence)."""
+        `ops` a CUDA tensor of ft_op records); returns `cov`.  With `stroke` the paths are
+        stroked (context join, paths["s_width"] as starting pen width).  CUDA tensors
+        are used on the context's stream, ordered after torch's current stream
+        (Context.torch_fence)."""
         paths = np.ascontiguousarray(paths, dtype=_abi.PATH_DTYPE)
         dev = hasattr(cov, "data_ptr")
         where = _abi.DEVICE if dev else _abi.HOST
@@ -70,8 +74,9 @@ class Adjoint:
             n_ops = len(ops)
         nbytes = cov.numel() * 4 if dev else cov.nbytes
         wait = self.ctx.torch_fence() if dev else False
-        self.ctx.check(self.ctx.L.ft_adjoint_forward(self.ctx.h, int(rule), _ptr(ops), n_ops, _ptr(paths), len(paths),
-                                                     _ptr(cov), nbytes, where, ctypes.byref(self.h)))
+        self.ctx.check(self.ctx.L.ft_adjoint_forward(self.ctx.h, int(bool(stroke)), int(rule), _ptr(ops), n_ops,
+                                                     _ptr(paths), len(paths), _ptr(cov), nbytes, where,
+                                                     ctypes.byref(self.h)))
         self.n_ops, self.n_paths = n_ops, len(paths)
         if wait:
             self.ctx.sync()

@@ -109,6 +109,13 @@ __device__ void block_max_scan(int v, int* wmax, int& incl, int& excl) {
     excl = max(pre, ex);
 }
 
+// What fixed.rs:88-93 makes of a coordinate, in pixels: NaN becomes 0 and values
+// saturate at the ends of the 16.16 range.  Coordinates it changes take no gradient.
+__device__ __forceinline__ float fx_range(float v) { return v != v ? 0.0f : fminf(fmaxf(v, -32768.0f), 32768.0f); }
+__device__ __forceinline__ float2 fx_pass(P2 raw, float2 g) {
+    return make_float2(fx_range(raw.x) == raw.x ? g.x : 0.0f, fx_range(raw.y) == raw.y ? g.y : 0.0f);
+}
+
 __device__ __forceinline__ float pow2neg(int d) { return __int_as_float((127 - d) << 23); }  // 2^-d, d <= 126
 
 // De Casteljau walk of one quad (plotter.rs:248-265) or cubic (plotter.rs:311-332) in
@@ -261,7 +268,7 @@ __device__ int path_walk(const AParams& p, ASmem& sm, const ft_op* ops, int n, f
             auto put = [&](int j, P2 q, float) {
                 const int k = base + j;
                 if (k < VCAP) {
-                    vpos[k] = make_float2(q.x, q.y);
+                    vpos[k] = make_float2(fx_range(q.x), fx_range(q.y));
                     vsub[k] = sub;
                     if (zero_grad) vgrad[k] = make_float2(0.f, 0.f);
                 }
@@ -278,14 +285,14 @@ __device__ int path_walk(const AParams& p, ASmem& sm, const ft_op* ops, int n, f
             // back through the transform: d(m*p)/dp = [[m0, m1], [m3, m4]]
             float* g = gops + (size_t)i * 6;
             if (!curve) {
-                float2 gv = __ldcg(&vgrad[base]);  // written by L2 atomics
+                const float2 gv = fx_pass(xform(m, op_pt(o, end_slot(kind))), __ldcg(&vgrad[base]));  // L2 atomics
                 const int s = end_slot(kind);
                 atomicAdd(g + 2 * s, __fadd_rn(__fmul_rn(m[0], gv.x), __fmul_rn(m[3], gv.y)));
                 atomicAdd(g + 2 * s + 1, __fadd_rn(__fmul_rn(m[1], gv.x), __fmul_rn(m[4], gv.y)));
             } else {
                 float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // pen, b, c, d
-                auto chain = [&](int j, P2, float t) {
-                    float2 gv = __ldcg(&vgrad[base + j]);
+                auto chain = [&](int j, P2 q, float t) {
+                    const float2 gv = fx_pass(q, __ldcg(&vgrad[base + j]));
                     const float gx = __fadd_rn(__fmul_rn(m[0], gv.x), __fmul_rn(m[3], gv.y));
                     const float gy = __fadd_rn(__fmul_rn(m[1], gv.x), __fmul_rn(m[4], gv.y));
                     const float u = __fsub_rn(1.0f, t);
@@ -594,6 +601,441 @@ __device__ void band_edges(ASmem& sm, float* band, int W, int b0, int nb, int V,
     }
 }
 
+
+// ------------------------------------------------------------------- strokes
+// Plotter::stroke (plotter.rs:356-365): stroke points with widths from the pen walk
+// (stroker.rs:204-236), the outline of every sub-stroke (stroker.rs:239-416) as
+// footile emits it, then the fill of the outline transformed a second time.  Thread 0
+// runs the stroker sequentially and records every outline point as a node over the
+// stroke points: an offset point, a miter intersection or an arc point.  The backward
+// reverses the nodes with their Jacobians (decisions held) and chains stroke points to
+// the op floats (Bernstein weights of the transformed curve) and widths to the
+// PenWidth ops (linear in t between the pen's width and the op's).
+
+struct SPt {
+    float x, y, w, t;
+    int op, form, pen, w0, w1, pad;  // provenance; w0 / w1: PenWidth op of the start / end width (-1: the call's)
+};
+struct SNd {
+    int kind, a, b, c, d;  // OFF: stroke points a -> b, c = 0 offsets a, 1 offsets b; MITER: nodes a0 a1 b0 b1;
+                           // ARC: stroke point a (centre, width), nodes b (from) and c (to)
+    float x, y;
+    int pad;
+};
+struct SSub {
+    int start, n, joined, done;
+};
+static_assert(sizeof(SPt) == SPT_BYTES && sizeof(SNd) == SND_BYTES && sizeof(SSub) == SSUB_BYTES, "layout");
+enum { N_OFF = 0, N_MITER = 1, N_ARC = 2 };
+enum { F_POINT = 0, F_QUAD = 1, F_CUBIC = 2 };
+
+// The De Casteljau walk carrying widths (geom.rs:31-35): leaf(index, point, width, t).
+template <bool CUBIC, class Leaf>
+__device__ int curve_walk_w(P2 a, P2 b, P2 c, P2 d, float wa, float wb, float wc, float wd, float tol_sq,
+                            int* depth_hit, Leaf leaf) {
+    struct Fr {
+        P2 a, b, c, d;
+        float wa, wb, wc, wd;
+        int dep;
+    };
+    Fr st[FT_MAX_DEPTH + 1];
+    int sp = 0, n = 0, dep = 0;
+    float t = 0.0f;
+    for (;;) {
+        bool within;
+        P2 l1, l2, m, r1, r2;
+        float wl1, wl2, wm, wr1, wr2;
+        if (CUBIC) {
+            P2 ab = pmid(a, b), bc = pmid(b, c), cd = pmid(c, d);
+            P2 abbc = pmid(ab, bc), bccd = pmid(bc, cd);
+            m = pmid(abbc, bccd);
+            float wab = ftk::fmid(wa, wb), wbc = ftk::fmid(wb, wc), wcd = ftk::fmid(wc, wd);
+            float wabbc = ftk::fmid(wab, wbc), wbccd = ftk::fmid(wbc, wcd);
+            wm = ftk::fmid(wabbc, wbccd);
+            within = pdist_sq(m, pmid(a, d)) <= tol_sq;
+            l1 = ab, l2 = abbc, r1 = bccd, r2 = cd;
+            wl1 = wab, wl2 = wabbc, wr1 = wbccd, wr2 = wcd;
+        } else {
+            P2 ab = pmid(a, b), bc = pmid(b, c);
+            m = pmid(ab, bc);
+            float wab = ftk::fmid(wa, wb), wbc = ftk::fmid(wb, wc);
+            wm = ftk::fmid(wab, wbc);
+            within = pdist_sq(m, pmid(a, c)) <= tol_sq;
+            l1 = ab, l2 = m, r1 = bc, r2 = c;
+            wl1 = wab, wl2 = wm, wr1 = wbc, wr2 = wc;
+        }
+        if (within || dep >= FT_MAX_DEPTH) {
+            if (!within) *depth_hit = 1;
+            t = __fadd_rn(t, pow2neg(dep));
+            if (CUBIC)
+                leaf(n, d, wd, t);
+            else
+                leaf(n, c, wc, t);
+            n++;
+            if (sp == 0) break;
+            --sp;
+            a = st[sp].a, b = st[sp].b, c = st[sp].c, d = st[sp].d;
+            wa = st[sp].wa, wb = st[sp].wb, wc = st[sp].wc, wd = st[sp].wd;
+            dep = st[sp].dep;
+        } else {
+            if (CUBIC) {
+                st[sp] = Fr{m, r1, r2, d, wm, wr1, wr2, wd, dep + 1};
+                b = l1, c = l2, d = m;
+                wb = wl1, wc = wl2, wd = wm;
+            } else {
+                st[sp] = Fr{m, r1, r2, r2, wm, wr1, wr2, wr2, dep + 1};
+                b = l1, c = l2;
+                wb = wl1, wc = wl2;
+            }
+            sp++;
+            dep++;
+        }
+    }
+    return n;
+}
+
+struct StrokeScr {
+    SPt* sp;
+    SSub* subs;
+    SNd* nd;
+    float2* ng;
+    float4* spg;
+    int* vnode;
+};
+
+__device__ __forceinline__ StrokeScr stroke_scr(unsigned char* scr) {
+    StrokeScr S;
+    S.sp = reinterpret_cast<SPt*>(scr + AS_SPT);
+    S.subs = reinterpret_cast<SSub*>(scr + AS_SSUB);
+    S.nd = reinterpret_cast<SNd*>(scr + AS_SND);
+    S.ng = reinterpret_cast<float2*>(scr + AS_NG);
+    S.spg = reinterpret_cast<float4*>(scr + AS_SPG);
+    S.vnode = reinterpret_cast<int*>(scr + AS_VNODE);
+    return S;
+}
+
+// Thread 0: stroke points, outline nodes and the outline polygon (vpos, vsub, vnode).
+// Returns the outline vertex count (may exceed VCAP: nothing beyond VCAP is written);
+// *n_nodes / *n_sp get the node and stroke point counts, *status the path status.
+__device__ int build_stroke_dev(const AParams& p, const ft_op* ops, int n, float sw0, const StrokeScr& S,
+                                float2* vpos, int* vsub, int* n_nodes, int* n_sp, int* status) {
+    const float* m = p.xf;
+    // ---- stroke points (plotter.rs:175-332 into Stroke::add_point / close)
+    float sw = sw0;
+    int cur_pw = -1, pen = -1, pen_wsrc = -1;
+    P2 penp = p2(0.0f, 0.0f);
+    float penw = sw0;
+    int ns = 0, nsub = 1;
+    S.subs[0] = SSub{0, 0, 0, 0};
+    auto close = [&](int joined) {
+        if (ns > 0) {
+            S.subs[nsub - 1].joined = joined;
+            S.subs[nsub - 1].done = 1;
+        }
+    };
+    auto add = [&](P2 q, float w, int op, int form, float t, int pn, int w0, int w1) {
+        if (ns >= VCAP) return;  // the stroke keeps 65,535 points (stroker.rs:204-216)
+        const int done = S.subs[nsub - 1].done;
+        if (done) S.subs[nsub++] = SSub{ns, 0, 0, 0};
+        const bool coincident = ns > 0 && S.sp[ns - 1].x == q.x && S.sp[ns - 1].y == q.y;
+        if (done || !coincident) {
+            S.sp[ns++] = SPt{q.x, q.y, w, t, op, form, pn, w0, w1, 0};
+            S.subs[nsub - 1].n++;
+        }
+    };
+    for (int i = 0; i < n; i++) {
+        const ft_op o = load_op(ops, i);
+        switch (o.kind) {
+            case FT_OP_CLOSE:
+                close(1);
+                pen = -1;
+                pen_wsrc = cur_pw;
+                penp = p2(0.0f, 0.0f);
+                penw = sw;
+                break;
+            case FT_OP_MOVE:
+            case FT_OP_LINE: {
+                const P2 q = op_pt(o, 0);
+                if (o.kind == FT_OP_MOVE) close(0);
+                add(xform(m, q), sw, i, F_POINT, 1.0f, -1, cur_pw, cur_pw);
+                pen = i;
+                pen_wsrc = cur_pw;
+                penp = q;
+                penw = sw;
+                break;
+            }
+            case FT_OP_QUAD:
+            case FT_OP_CUBIC: {
+                const bool cubic = o.kind == FT_OP_CUBIC;
+                const P2 A = xform(m, penp), B = xform(m, op_pt(o, 0)), C = xform(m, op_pt(o, 1));
+                const P2 D = cubic ? xform(m, op_pt(o, 2)) : C;
+                float wb, wc, wd;
+                if (cubic) {  // float_lerp (geom.rs:14-16)
+                    wb = __fadd_rn(sw, __fmul_rn(__fsub_rn(penw, sw), 1.0f / 3.0f));
+                    wc = __fadd_rn(sw, __fmul_rn(__fsub_rn(penw, sw), 2.0f / 3.0f));
+                    wd = sw;
+                } else {
+                    wb = ftk::fmid(penw, sw);
+                    wc = sw;
+                    wd = sw;
+                }
+                if (!pfinite(A) || !pfinite(B) || !pfinite(C) || !pfinite(D)) {
+                    *status = max(*status, (int)FT_ERR_ARG);
+                    add(D, sw, i, F_POINT, 1.0f, -1, cur_pw, cur_pw);
+                } else {
+                    int dh = 0;
+                    const int pn = pen, w0 = pen_wsrc, w1 = cur_pw;
+                    auto leaf = [&](int, P2 q, float w, float t) { add(q, w, i, cubic ? F_CUBIC : F_QUAD, t, pn, w0, w1); };
+                    if (cubic)
+                        curve_walk_w<true>(A, B, C, D, penw, wb, wc, wd, p.tol_sq, &dh, leaf);
+                    else
+                        curve_walk_w<false>(A, B, C, D, penw, wb, wc, wd, p.tol_sq, &dh, leaf);
+                    if (dh) *status = max(*status, (int)FT_ERR_DEPTH);
+                }
+                pen = i;
+                pen_wsrc = cur_pw;
+                penp = cubic ? op_pt(o, 2) : op_pt(o, 1);
+                penw = sw;
+                break;
+            }
+            case FT_OP_PEN_WIDTH:
+                sw = o.v[0];
+                cur_pw = i;
+                break;
+            default:
+                break;
+        }
+    }
+    *n_sp = ns;
+    // ---- outline (stroker.rs:239-416), filled as Line ops transformed again
+    int nn = 0, nv = 0, sub_start = 0;
+    bool fresh = true;
+    auto P = [&](int k) { return p2(S.sp[k].x, S.sp[k].y); };
+    auto N = [&](int i) { return i < NODE_CAP ? p2(S.nd[i].x, S.nd[i].y) : p2(0.0f, 0.0f); };
+    auto node = [&](int kind, int a, int b, int c, int d, P2 v) {
+        if (nn < NODE_CAP) S.nd[nn] = SNd{kind, a, b, c, d, v.x, v.y, 0};
+        return nn++;
+    };
+    auto emit = [&](int nd) {
+        if (nv < VCAP) {
+            if (fresh) sub_start = nv;
+            const P2 q = xform(m, N(nd));
+            vpos[nv] = make_float2(fx_range(q.x), fx_range(q.y));
+            vsub[nv] = sub_start;
+            S.vnode[nv] = nd;
+        }
+        fresh = false;
+        nv++;
+    };
+    auto off = [&](int k0, int k1, int which) {
+        const P2 vr = ftk::pnormalize(ftk::pright(ftk::psub(P(k1), P(k0))));
+        const int ks = which ? k1 : k0;
+        return node(N_OFF, k0, k1, which, 0, ftk::padd(P(ks), ftk::pscale(vr, __fmul_rn(S.sp[ks].w, 0.5f))));
+    };
+    const float tol_sq = p.tol_sq;
+    auto arc = [&](int k, int na0, int nb0) {
+        struct Fr {
+            int na, nb, dep;
+        };
+        Fr st[FT_MAX_DEPTH + 3];
+        int sp = 0;
+        st[sp++] = Fr{na0, nb0, 0};
+        while (sp > 0) {
+            const Fr f = st[--sp];
+            const P2 a = N(f.na), b = N(f.nb);
+            const P2 vr = ftk::pnormalize(ftk::pright(ftk::psub(b, a)));
+            const P2 c = ftk::padd(P(k), ftk::pscale(vr, __fmul_rn(S.sp[k].w, 0.5f)));
+            if (!pfinite(c) || pdist_sq(c, pmid(a, b)) <= tol_sq) {
+                emit(f.nb);
+            } else if (f.dep >= FT_MAX_DEPTH) {
+                *status = max(*status, (int)FT_ERR_DEPTH);
+                emit(f.nb);
+            } else {
+                const int nc = node(N_ARC, k, f.na, f.nb, 0, c);
+                st[sp++] = Fr{nc, f.nb, f.dep + 1};  // right half after the left
+                st[sp++] = Fr{f.na, nc, f.dep + 1};
+            }
+        }
+    };
+    auto join = [&](int k, int a0, int a1, int b0, int b1) {
+        const P2 A0 = N(a0), A1 = N(a1), B0 = N(b0), B1 = N(b1);
+        if (p.join == FT_JOIN_MITER) {
+            if (p.miter_limit > 0.0f) {
+                const float sm_min = __fdiv_rn(1.0f, p.miter_limit);
+                const float th = ftk::pangle_rel(ftk::psub(A1, A0), ftk::psub(B0, B1));
+                const float sm = fabsf(ft_sinf(__fdiv_rn(th, 2.0f)));
+                P2 xp;
+                if (sm >= sm_min && sm < 1.0f && ftk::pline_x(A0, A1, B0, B1, &xp)) {
+                    emit(node(N_MITER, a0, a1, b0, b1, xp));
+                    return;
+                }
+            }
+            emit(a1);
+            emit(b0);
+        } else if (p.join == FT_JOIN_BEVEL) {
+            emit(a1);
+            emit(b0);
+        } else {
+            const float th = ftk::pangle_rel(ftk::psub(A1, A0), ftk::psub(B0, B1));
+            emit(a1);
+            if (th <= 0.0f)
+                emit(b0);
+            else
+                arc(k, a1, b0);
+        }
+    };
+    for (int si = 0; si < nsub && nn <= NODE_CAP && nv <= VCAP; si++) {
+        const SSub sb = S.subs[si];
+        const int len = (sb.joined ? sb.n + 1 : (sb.n > 0 ? sb.n - 1 : 0)) & 0xFFFF;  // SubStroke::len (u16)
+        if (len == 0) continue;
+        auto nextv = [&](int v, bool fwd) {
+            if (fwd) return v + 1 < sb.start + sb.n ? v + 1 : sb.start;
+            return v > sb.start ? v - 1 : sb.start + sb.n - 1;
+        };
+        for (int side = 0; side < 2; side++) {
+            const bool fwd = side == 0;
+            int v0 = fwd ? sb.start : nextv(sb.start, false);
+            int v1 = nextv(v0, fwd);
+            bool have = false;
+            int x0 = 0, x1 = 0;
+            for (int k = 0; k < len; k++) {
+                const int o0 = off(v0, v1, 0), o1 = off(v0, v1, 1);
+                if (have)
+                    join(v0, x0, x1, o0, o1);
+                else if (!sb.joined)
+                    emit(o0);
+                have = true;
+                x0 = o0;
+                x1 = o1;
+                v0 = v1;
+                v1 = nextv(v1, fwd);
+            }
+            if (!sb.joined && have) emit(x1);
+            if (fwd && sb.joined) fresh = true;  // Close between the two sides
+        }
+        fresh = true;  // Close
+    }
+    if (nn > NODE_CAP || nv > VCAP) *status = max(*status, (int)FT_ERR_CAP);
+    *n_nodes = min(nn, NODE_CAP);
+    return nv;
+}
+
+// Thread 0, backward: outline vertex gradients (vgrad, in fill space) -> nodes ->
+// stroke points -> op floats and widths.
+__device__ void stroke_backward_dev(const AParams& p, const ft_op* ops, float* gops, float* gwidth, int V, int nn,
+                                    int ns, const StrokeScr& S, const float2* vgrad) {
+    const float* m = p.xf;
+    for (int i = 0; i < nn; i++) S.ng[i] = make_float2(0.0f, 0.0f);
+    for (int k = 0; k < ns; k++) S.spg[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    for (int j = 0; j < V; j++) {
+        const int nd = S.vnode[j];
+        const float2 g = fx_pass(xform(m, p2(S.nd[nd].x, S.nd[nd].y)), __ldcg(&vgrad[j]));
+        float2& t = S.ng[nd];
+        t.x += m[0] * g.x + m[3] * g.y;
+        t.y += m[1] * g.x + m[4] * g.y;
+    }
+    for (int i = nn - 1; i >= 0; i--) {
+        const SNd nd = S.nd[i];
+        const float2 g = S.ng[i];
+        if (g.x == 0.0f && g.y == 0.0f) continue;
+        if (nd.kind == N_OFF || nd.kind == N_ARC) {
+            float fx, fy, tx, ty;
+            if (nd.kind == N_OFF) {
+                fx = S.sp[nd.a].x, fy = S.sp[nd.a].y, tx = S.sp[nd.b].x, ty = S.sp[nd.b].y;
+            } else {
+                fx = S.nd[nd.b].x, fy = S.nd[nd.b].y, tx = S.nd[nd.c].x, ty = S.nd[nd.c].y;
+            }
+            const float ux = ty - fy, uy = -(tx - fx);
+            const float len = sqrtf(ux * ux + uy * uy);
+            const float vx = ux / len, vy = uy / len;
+            const int ks = nd.kind == N_OFF ? (nd.c ? nd.b : nd.a) : nd.a;
+            const float w = S.sp[ks].w;
+            float4& gs = S.spg[ks];
+            gs.x += g.x;
+            gs.y += g.y;
+            gs.z += 0.5f * (vx * g.x + vy * g.y);
+            const float gvx = g.x * w * 0.5f, gvy = g.y * w * 0.5f;
+            const float dv = vx * gvx + vy * gvy;
+            const float gux = (gvx - vx * dv) / len, guy = (gvy - vy * dv) / len;
+            const float gdx = -guy, gdy = gux;  // u = (d.y, -d.x)
+            if (nd.kind == N_OFF) {
+                S.spg[nd.b].x += gdx;
+                S.spg[nd.b].y += gdy;
+                S.spg[nd.a].x -= gdx;
+                S.spg[nd.a].y -= gdy;
+            } else {
+                S.ng[nd.c].x += gdx;
+                S.ng[nd.c].y += gdy;
+                S.ng[nd.b].x -= gdx;
+                S.ng[nd.b].y -= gdy;
+            }
+        } else {
+            // intersection of lines a0-a1 and b0-b1 in coordinates relative to a1 (well
+            // conditioned in float): x = a1 + (B / D) * (a1 - a0), u = a0 - a1,
+            // v3 = b0 - a1, v4 = b1 - a1, D = u x (v3 - v4), B = v3 x v4
+            const float ax = S.nd[nd.b].x, ay = S.nd[nd.b].y;
+            const float ux = S.nd[nd.a].x - ax, uy = S.nd[nd.a].y - ay;
+            const float v3x = S.nd[nd.c].x - ax, v3y = S.nd[nd.c].y - ay;
+            const float v4x = S.nd[nd.d].x - ax, v4y = S.nd[nd.d].y - ay;
+            const float den = ux * (v3y - v4y) - uy * (v3x - v4x);
+            const float bb = v3x * v4y - v3y * v4x;
+            const float q = bb / den;
+            float gux = -q * g.x, guy = -q * g.y;
+            const float gq = -(ux * g.x + uy * g.y);
+            const float gb = gq / den, gden = -gq * q / den;
+            float g3x = gb * v4y, g3y = -gb * v4x, g4x = -gb * v3y, g4y = gb * v3x;
+            gux += gden * (v3y - v4y);
+            guy -= gden * (v3x - v4x);
+            g3y += gden * ux;
+            g4y -= gden * ux;
+            g3x -= gden * uy;
+            g4x += gden * uy;
+            S.ng[nd.a].x += gux;
+            S.ng[nd.a].y += guy;
+            S.ng[nd.c].x += g3x;
+            S.ng[nd.c].y += g3y;
+            S.ng[nd.d].x += g4x;
+            S.ng[nd.d].y += g4y;
+            S.ng[nd.b].x += g.x - gux - g3x - g4x;
+            S.ng[nd.b].y += g.y - guy - g3y - g4y;
+        }
+    }
+    auto gw = [&](int src, float v) {
+        if (src < 0)
+            atomicAdd(gwidth, v);
+        else
+            atomicAdd(gops + (size_t)src * 6, v);
+    };
+    for (int k = 0; k < ns; k++) {
+        const SPt q = S.sp[k];
+        const float4 g = S.spg[k];
+        const float gx = m[0] * g.x + m[3] * g.y, gy = m[1] * g.x + m[4] * g.y;
+        const int kind = load_op(ops, q.op).kind;
+        auto add = [&](int j, int slot, float wgt) {
+            atomicAdd(gops + (size_t)j * 6 + 2 * slot, wgt * gx);
+            atomicAdd(gops + (size_t)j * 6 + 2 * slot + 1, wgt * gy);
+        };
+        if (q.form == F_POINT) {
+            add(q.op, end_slot(kind), 1.0f);
+            gw(q.w1, g.z);
+            continue;
+        }
+        const float t = q.t, u = 1.0f - t;
+        if (q.form == F_QUAD) {
+            if (q.pen >= 0) add(q.pen, end_slot(load_op(ops, q.pen).kind), u * u);
+            add(q.op, 0, 2.0f * t * u);
+            add(q.op, 1, t * t);
+        } else {
+            if (q.pen >= 0) add(q.pen, end_slot(load_op(ops, q.pen).kind), u * u * u);
+            add(q.op, 0, 3.0f * t * u * u);
+            add(q.op, 1, 3.0f * t * t * u);
+            add(q.op, 2, t * t * t);
+        }
+        gw(q.w0, u * g.z);
+        gw(q.w1, t * g.z);
+    }
+}
+
 __device__ __forceinline__ float cov_of(int rule, float s) {
     if (rule == FT_NONZERO) return fminf(fmaxf(s, 0.0f), 1.0f);
     const float m = __fsub_rn(s, __fmul_rn(2.0f, floorf(__fmul_rn(s, 0.5f))));
@@ -613,7 +1055,9 @@ template <bool BWD>
 __global__ void __launch_bounds__(ABLOCK) k_adjoint(AParams p) {
     extern __shared__ float band[];
     __shared__ ASmem sm;
-    unsigned char* scr = p.scratch + (size_t)blockIdx.x * A_SCRATCH_PER_CTA;
+    unsigned char* scr = p.scratch + (size_t)blockIdx.x * (p.stroke ? A_SCRATCH_STROKE : A_SCRATCH_PER_CTA);
+    const StrokeScr S = stroke_scr(scr);
+    __shared__ int s_counts[3];
     float2* vpos = reinterpret_cast<float2*>(scr + AS_POS);
     int* vsub = reinterpret_cast<int*>(scr + AS_SUB);
     float2* vgrad = reinterpret_cast<float2*>(scr + AS_GRAD);
@@ -625,8 +1069,24 @@ __global__ void __launch_bounds__(ABLOCK) k_adjoint(AParams p) {
         const ft_op* ops = p.ops + d.op_begin;
         if (tid == 0) sm.status = FT_OK;
         __syncthreads();
-        const int V = path_walk<WALK_EMIT>(p, sm, ops, (int)d.n_ops, vpos, vsub, vgrad, BWD, nullptr);
-        const bool cap = V > VCAP;
+        int V;
+        if (p.stroke) {
+            if (tid == 0) {
+                int st = FT_OK, nn = 0, ns = 0;
+                s_counts[0] = build_stroke_dev(p, ops, (int)d.n_ops, d.s_width, S, vpos, vsub, &nn, &ns, &st);
+                s_counts[1] = nn;
+                s_counts[2] = ns;
+                atomicMax(&sm.status, st);
+            }
+            __syncthreads();
+            V = s_counts[0];
+            if (BWD)
+                for (int k = tid; k < min(V, VCAP); k += ABLOCK) vgrad[k] = make_float2(0.0f, 0.0f);
+            __syncthreads();
+        } else {
+            V = path_walk<WALK_EMIT>(p, sm, ops, (int)d.n_ops, vpos, vsub, vgrad, BWD, nullptr);
+        }
+        const bool cap = V > VCAP || (p.stroke && sm.status == FT_ERR_CAP);
         if (cap && tid == 0) atomicMax(&sm.status, (int)FT_ERR_CAP);
         const float sign = cap ? 1.0f : fig_sign(sm, V, vpos, vsub, vflag);
         const int rows_per_band = W > 0 ? max(1, BAND_FLOATS / W) : 1;
@@ -672,8 +1132,15 @@ __global__ void __launch_bounds__(ABLOCK) k_adjoint(AParams p) {
             __syncthreads();
         }
         if (BWD && !cap) {
-            path_walk<WALK_GRAD>(p, sm, ops, (int)d.n_ops, vpos, vsub, vgrad, false,
-                                 p.grad_ops + (size_t)d.op_begin * 6);
+            if (p.stroke) {
+                __syncthreads();
+                if (tid == 0)
+                    stroke_backward_dev(p, ops, p.grad_ops + (size_t)d.op_begin * 6, p.grad_width + path, V,
+                                        s_counts[1], s_counts[2], S, vgrad);
+            } else {
+                path_walk<WALK_GRAD>(p, sm, ops, (int)d.n_ops, vpos, vsub, vgrad, false,
+                                     p.grad_ops + (size_t)d.op_begin * 6);
+            }
         }
         if (tid == 0) p.status[path] = sm.status;
         __syncthreads();

@@ -23,6 +23,19 @@ constexpr size_t AS_GRAD = a_align(AS_SUB + (size_t)VCAP * 4);            // flo
 constexpr size_t AS_FLAG = a_align(AS_GRAD + (size_t)VCAP * 8);           // int[VCAP]
 constexpr size_t A_SCRATCH_PER_CTA = a_align(AS_FLAG + (size_t)VCAP * 4);
 
+// Strokes add, after the fill arrays: the node of each outline vertex, stroke points,
+// sub-strokes, outline nodes (offset points, miter intersections, arc points) and
+// their gradients.
+constexpr int NODE_CAP = 200000;            // outline nodes per stroke
+constexpr size_t SPT_BYTES = 40, SND_BYTES = 32, SSUB_BYTES = 16;
+constexpr size_t AS_VNODE = A_SCRATCH_PER_CTA;                                   // int[VCAP]
+constexpr size_t AS_SPT = a_align(AS_VNODE + (size_t)VCAP * 4);                  // stroke points
+constexpr size_t AS_SSUB = a_align(AS_SPT + (size_t)VCAP * SPT_BYTES);           // sub-strokes
+constexpr size_t AS_SND = a_align(AS_SSUB + (size_t)(VCAP + 1) * SSUB_BYTES);    // nodes
+constexpr size_t AS_NG = a_align(AS_SND + (size_t)NODE_CAP * SND_BYTES);         // float2 node gradients
+constexpr size_t AS_SPG = a_align(AS_NG + (size_t)NODE_CAP * 8);                 // float4 stroke point gradients
+constexpr size_t A_SCRATCH_STROKE = a_align(AS_SPG + (size_t)VCAP * 16);
+
 struct AParams {
     const ft_op* ops;
     const ft_path_desc* paths;
@@ -32,10 +45,14 @@ struct AParams {
     const float* grad_cov;  // backward: dLoss/dcov (layout of cov)
     float* grad_ops;        // backward: 6 floats per op, zeroed by the host, accumulated
     int* status;            // per path
-    unsigned char* scratch; // A_SCRATCH_PER_CTA per CTA
+    unsigned char* scratch; // A_SCRATCH_PER_CTA (fills) or A_SCRATCH_STROKE (strokes) per CTA
+    float* grad_width;      // backward, strokes: d/d(starting pen width) per path, zeroed by the host
     float xf[6];
     float tol_sq;
     int rule;
+    int stroke;             // Plotter::stroke: the outline of each path is filled NonZero
+    int join;
+    float miter_limit;
 };
 
 cudaError_t launch_adjoint(bool backward, const AParams& p, int grid, cudaStream_t s);

@@ -885,6 +885,8 @@ struct ft_adjoint {
     uint32_t n_ops = 0, n_paths = 0;
     uint64_t cov_bytes = 0;
     int rule = FT_NONZERO;
+    int stroke = 0, join = FT_JOIN_MITER;
+    float miter_limit = 4.0f;
     float xf[6] = {1, 0, 0, 0, 1, 0};
     float tol_sq = 0.09f;
     int grid_f = 1, grid_b = 1;
@@ -904,10 +906,11 @@ static int adjoint_check_path(ft_ctx* c, const ft_path_desc& d, uint64_t cov_byt
 
 extern "C" {
 
-FT_API int ft_adjoint_forward(ft_ctx* c, int32_t rule, const ft_op* ops, uint32_t n_ops_total,
+FT_API int ft_adjoint_forward(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* ops, uint32_t n_ops_total,
                               const ft_path_desc* paths, uint32_t n_paths, float* cov, uint64_t cov_bytes,
                               int32_t where, ft_adjoint** saved) {
     if (!c || !saved) return FT_ERR_ARG;
+    if (stroke) rule = FT_NONZERO;  // Plotter::stroke fills the outline NonZero (plotter.rs:364)
     if ((rule != FT_NONZERO && rule != FT_EVENODD) || (where != FT_HOST && where != FT_DEVICE))
         return fail(c, FT_ERR_ARG, "bad rule or location");
     if ((n_paths && !paths) || (n_ops_total && !ops) || (cov_bytes && !cov))
@@ -928,6 +931,9 @@ FT_API int ft_adjoint_forward(ft_ctx* c, int32_t rule, const ft_op* ops, uint32_
     }
     a->ready = false;
     a->rule = rule;
+    a->stroke = stroke ? 1 : 0;
+    a->join = c->join;
+    a->miter_limit = c->miter_limit;
     a->n_ops = n_ops_total;
     a->n_paths = n_paths;
     a->cov_bytes = cov_bytes;
@@ -939,10 +945,13 @@ FT_API int ft_adjoint_forward(ft_ctx* c, int32_t rule, const ft_op* ops, uint32_
     FT_CU(a->paths.ensure(sizeof(ft_path_desc) * std::max(n_paths, 1u)), "alloc paths");
     FT_CU(a->status.ensure(sizeof(int32_t) * std::max(n_paths, 1u)), "alloc status");
     FT_CU(a->area.ensure(std::max<uint64_t>(cov_bytes, 4)), "alloc winding area");
-    const int bps_f = fta::adjoint_blocks_per_sm(false), bps_b = fta::adjoint_blocks_per_sm(true);
+    // strokes: the stroker runs on one thread per CTA over a 14 MB scratch, two CTAs per SM
+    const int bps_f = a->stroke ? 2 : fta::adjoint_blocks_per_sm(false);
+    const int bps_b = a->stroke ? 2 : fta::adjoint_blocks_per_sm(true);
     a->grid_f = (int)std::max(1u, std::min<uint32_t>(n_paths, (uint32_t)(bps_f * c->sm_count)));
     a->grid_b = (int)std::max(1u, std::min<uint32_t>(n_paths, (uint32_t)(bps_b * c->sm_count)));
-    FT_CU(a->scratch.ensure(fta::A_SCRATCH_PER_CTA * (size_t)std::max(a->grid_f, a->grid_b)), "alloc scratch");
+    const size_t per_cta = a->stroke ? fta::A_SCRATCH_STROKE : fta::A_SCRATCH_PER_CTA;
+    FT_CU(a->scratch.ensure(per_cta * (size_t)std::max(a->grid_f, a->grid_b)), "alloc scratch");
     if (n_ops_total)
         FT_CU(cudaMemcpyAsync(a->ops.p, ops, sizeof(ft_op) * n_ops_total,
                               where == FT_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, c->stream),
@@ -967,6 +976,9 @@ FT_API int ft_adjoint_forward(ft_ctx* c, int32_t rule, const ft_op* ops, uint32_
     for (int k = 0; k < 6; k++) p.xf[k] = a->xf[k];
     p.tol_sq = a->tol_sq;
     p.rule = rule;
+    p.stroke = a->stroke;
+    p.join = a->join;
+    p.miter_limit = a->miter_limit;
     FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
     if (n_paths) {
         FT_CU(fta::launch_adjoint(false, p, a->grid_f, c->stream), "launch adjoint forward");
@@ -1005,6 +1017,16 @@ FT_API int ft_adjoint_backward(ft_ctx* c, ft_adjoint* a, const float* grad_cov, 
         gops_d = static_cast<float*>(a->gops.p);
     }
     if (gops_bytes) FT_CU(cudaMemsetAsync(gops_d, 0, gops_bytes, c->stream), "reset op gradient");
+    float* gw_d = nullptr;  // the kernel accumulates starting-width gradients of strokes here
+    if (a->n_paths) {
+        if (where == FT_DEVICE && grad_width) {
+            gw_d = grad_width;
+        } else {
+            FT_CU(a->gwidth.ensure(sizeof(float) * a->n_paths), "alloc width gradient");
+            gw_d = static_cast<float*>(a->gwidth.p);
+        }
+        FT_CU(cudaMemsetAsync(gw_d, 0, sizeof(float) * a->n_paths, c->stream), "reset width gradient");
+    }
     fta::AParams p{};
     p.ops = static_cast<const ft_op*>(a->ops.p);
     p.paths = static_cast<const ft_path_desc*>(a->paths.p);
@@ -1017,6 +1039,10 @@ FT_API int ft_adjoint_backward(ft_ctx* c, ft_adjoint* a, const float* grad_cov, 
     for (int k = 0; k < 6; k++) p.xf[k] = a->xf[k];
     p.tol_sq = a->tol_sq;
     p.rule = a->rule;
+    p.stroke = a->stroke;
+    p.join = a->join;
+    p.miter_limit = a->miter_limit;
+    p.grad_width = gw_d;
     FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
     if (a->n_paths) {
         FT_CU(fta::launch_adjoint(true, p, a->grid_b, c->stream), "launch adjoint backward");
@@ -1024,13 +1050,10 @@ FT_API int ft_adjoint_backward(ft_ctx* c, ft_adjoint* a, const float* grad_cov, 
     }
     FT_CU(cudaEventRecord(c->ev1, c->stream), "event");
     c->timed = true;
-    if (grad_width && a->n_paths) {
-        if (where == FT_HOST)
-            std::fill(grad_width, grad_width + a->n_paths, 0.0f);
-        else
-            FT_CU(cudaMemsetAsync(grad_width, 0, sizeof(float) * a->n_paths, c->stream), "reset width gradient");
-    }
     if (where == FT_HOST) {
+        if (grad_width && a->n_paths)
+            FT_CU(cudaMemcpyAsync(grad_width, gw_d, sizeof(float) * a->n_paths, cudaMemcpyDeviceToHost, c->stream),
+                  "download width gradient");
         if (gops_bytes)
             FT_CU(cudaMemcpyAsync(grad_ops, gops_d, gops_bytes, cudaMemcpyDeviceToHost, c->stream),
                   "download op gradient");

@@ -246,11 +246,21 @@ FT_API int ft_fill_noalloc(int32_t rule, const ft_op* ops, uint32_t n_ops, int32
  * transform are the context's at the forward call.  `where` is FT_HOST or FT_DEVICE
  * for ops, cov, grad_cov, grad_ops and grad_width; path descriptors are host memory.
  * Per-path status (FT_ERR_DEPTH, FT_ERR_ARG, FT_ERR_CAP for more than FT_MAX_POINTS
- * flattened vertices: coverage zero, gradient zero) via ft_adjoint_status. */
+ * flattened vertices: coverage zero, gradient zero) via ft_adjoint_status.
+ *
+ * With `stroke` = 1 each path is Plotter::stroke'd (plotter.rs:356-365) with the
+ * context's join and paths[i].s_width as the pen width at the call's start: the
+ * coverage is that of footile's outline (stroker.rs:204-416: the same stroke points,
+ * offsets, joins and arcs in f32, transformed a second time) filled NonZero, `rule` is
+ * ignored, and the backward also differentiates the outline (offset points, miter
+ * intersections, arc points; the miter and arc decisions held): gradients reach the
+ * control points, the PenWidth ops (slot 0 of their grad_ops row) and, per path, the
+ * starting pen width (`grad_width`).  Strokes whose outline needs more than
+ * FT_MAX_POINTS vertices or 200,000 outline nodes report FT_ERR_CAP. */
 typedef struct ft_adjoint ft_adjoint;
-FT_API int ft_adjoint_forward(ft_ctx* ctx, int32_t rule, const ft_op* ops, uint32_t n_ops_total,
-                              const ft_path_desc* paths, uint32_t n_paths, float* cov,
-                              uint64_t cov_bytes, int32_t where, ft_adjoint** saved);
+FT_API int ft_adjoint_forward(ft_ctx* ctx, int32_t stroke, int32_t rule, const ft_op* ops,
+                              uint32_t n_ops_total, const ft_path_desc* paths, uint32_t n_paths,
+                              float* cov, uint64_t cov_bytes, int32_t where, ft_adjoint** saved);
 FT_API int ft_adjoint_backward(ft_ctx* ctx, ft_adjoint* saved, const float* grad_cov, float* grad_ops,
                                float* grad_width, int32_t where);
 FT_API int ft_adjoint_status(ft_ctx* ctx, ft_adjoint* saved, int32_t* status, uint32_t n);

@@ -88,6 +88,14 @@ def lib():
             L.orc_adj_forward.restype = ctypes.c_int
             L.orc_adj_backward.argtypes = [i32, P, u32, P, u32, u32, ctypes.c_float, P, P, P, P]
             L.orc_adj_backward.restype = ctypes.c_int
+            d = ctypes.c_double
+            L.orc_adj_stroke_forward.argtypes = [P, u32, P, d, u32, u32, ctypes.c_float, P, i32, ctypes.c_float, P, P]
+            L.orc_adj_stroke_forward.restype = ctypes.c_int
+            L.orc_adj_stroke_backward.argtypes = [P, u32, P, d, u32, u32, ctypes.c_float, P, i32, ctypes.c_float, P, P,
+                                                  P, ctypes.POINTER(d)]
+            L.orc_adj_stroke_backward.restype = ctypes.c_int
+            L.orc_adj_stroke_outline.argtypes = [P, u32, ctypes.c_float, P, i32, ctypes.c_float, ctypes.c_float, P, u32]
+            L.orc_adj_stroke_outline.restype = u32
             del D
             _lib = L
     return _lib
@@ -246,3 +254,48 @@ def adj_backward(rule, ops, w, h, area, grad_cov, val=None, tolerance=0.3, trans
     lib().orc_adj_backward(rule, _ptr(ops), len(ops), _ptr(v), w, h, tolerance, _ptr(xf), _ptr(area), _ptr(g),
                            _ptr(out))
     return out
+
+
+def adj_stroke_forward(ops, w, h, val=None, s_width=1.0, tolerance=0.3, transform=_abi.IDENTITY,
+                       join=_abi.JOIN_MITER, miter_limit=4.0):
+    """FP64 analytic coverage of Plotter::stroke's outline: (cov, area, status).
+    With `val` the stroke points are Bernstein points of `val` and widths follow the
+    PenWidth values in val[:, 0] (and `s_width`), on the decisions the op floats make."""
+    ops = np.ascontiguousarray(ops, dtype=_abi.OP_DTYPE)
+    cov = np.zeros((h, w), np.float64)
+    area = np.zeros((h, w), np.float64)
+    v = None if val is None else np.ascontiguousarray(val, dtype=np.float64)
+    xf = _xf(transform)
+    st = lib().orc_adj_stroke_forward(_ptr(ops), len(ops), _ptr(v), s_width, w, h, tolerance, _ptr(xf), join,
+                                      miter_limit, _ptr(cov), _ptr(area))
+    return cov, area, st
+
+
+def adj_stroke_backward(ops, w, h, area, grad_cov, val=None, s_width=1.0, tolerance=0.3, transform=_abi.IDENTITY,
+                        join=_abi.JOIN_MITER, miter_limit=4.0):
+    """FP64 gradient of sum(grad_cov * cov) for a stroke: ((n_ops, 6) op-float gradient,
+    with PenWidth ops in column 0, and the gradient for the starting pen width)."""
+    ops = np.ascontiguousarray(ops, dtype=_abi.OP_DTYPE)
+    area = np.ascontiguousarray(area, dtype=np.float64)
+    g = np.ascontiguousarray(grad_cov, dtype=np.float64)
+    out = np.zeros((len(ops), 6), np.float64)
+    gsw = ctypes.c_double(0.0)
+    v = None if val is None else np.ascontiguousarray(val, dtype=np.float64)
+    xf = _xf(transform)
+    lib().orc_adj_stroke_backward(_ptr(ops), len(ops), _ptr(v), s_width, w, h, tolerance, _ptr(xf), join, miter_limit,
+                                  _ptr(area), _ptr(g), _ptr(out), ctypes.byref(gsw))
+    return out, gsw.value
+
+
+def adj_stroke_outline(ops, s_width=1.0, tolerance=0.3, transform=_abi.IDENTITY, join=_abi.JOIN_MITER,
+                       miter_limit=4.0):
+    ops = np.ascontiguousarray(ops, dtype=_abi.OP_DTYPE)
+    xf = _xf(transform)
+    cap = 1 << 16
+    while True:
+        out = np.zeros(cap, dtype=_abi.OP_DTYPE)
+        n = lib().orc_adj_stroke_outline(_ptr(ops), len(ops), tolerance, _ptr(xf), join, miter_limit, s_width,
+                                         _ptr(out), cap)
+        if n <= cap:
+            return out[:n]
+        cap = n

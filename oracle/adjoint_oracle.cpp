@@ -29,10 +29,12 @@
 #include <algorithm>
 #include <cmath>
 #include <climits>
+#include <functional>
 #include <cstdint>
 #include <vector>
 
 #include "../include/footile_gpu.h"
+#include "../include/ft_fmath.h"
 
 namespace adj {
 
@@ -190,6 +192,14 @@ struct D2 {
     double x, y;
 };
 
+// What fixed.rs:88-93 makes of a coordinate, in pixels: NaN becomes 0 and values
+// saturate at the ends of the 16.16 range.  Coordinates it changes take no gradient.
+static inline double fx_range(double v) { return std::isnan(v) ? 0.0 : std::clamp(v, -32768.0, 32768.0); }
+static inline D2 fx_range(D2 p) { return D2{fx_range(p.x), fx_range(p.y)}; }
+static inline D2 fx_pass(D2 raw, D2 g) {
+    return D2{fx_range(raw.x) == raw.x ? g.x : 0.0, fx_range(raw.y) == raw.y ? g.y : 0.0};
+}
+
 // Vertex positions in f64.  Without `val`: the f32 points of the De Casteljau walk, the
 // polygon footile's Fig receives (and the CUDA coverage covers), widened to double.
 // With `val` (6 per op, the layout of ft_op.v): the Bernstein points B(t) of the same
@@ -198,7 +208,7 @@ static std::vector<D2> positions(const Poly& P, const ft_op* ops, const double* 
     std::vector<D2> out(P.v.size());
     if (!val) {
         for (size_t k = 0; k < P.v.size(); k++) out[k] = D2{(double)P.f[k].x, (double)P.f[k].y};
-        return out;
+        return out;  // raw: callers apply fx_range
     }
     auto cp = [&](int j, int slot) { return D2{val[6 * j + 2 * slot], val[6 * j + 2 * slot + 1]}; };
     for (size_t k = 0; k < P.v.size(); k++) {
@@ -334,6 +344,66 @@ static inline double coverage_d(int rule, double s) {
     return m < 1.0 ? 1.0 : -1.0;
 }
 
+// Coverage of a polygon (positions `pos`, sub-figures and sign of P): area and cov.
+static void cover(const Poly& P, const std::vector<D2>& pos, int rule, uint32_t w, uint32_t h, double* cov,
+                  double* area) {
+    std::vector<double> acc((size_t)w * h, 0.0);
+    for (int k = 0; k < (int)pos.size(); k++) {
+        D2 p0 = pos[k], p1 = pos[next_vertex(P, k)];
+        double dir = p1.y > p0.y ? 1.0 : -1.0;
+        edge_pieces(p0, p1, (int)w, (int)h, [&](int r, int c, double hh, double xm, double, double) {
+            double* row = &acc[(size_t)r * w];
+            if (c < 0) {
+                row[0] += dir * hh;
+            } else if (c < (int)w) {
+                row[c] += dir * hh * (c + 1 - xm);
+                if (c + 1 < (int)w) row[c + 1] += dir * hh * (xm - c);
+            }
+        });
+    }
+    const double sg = P.sign;
+    for (uint32_t r = 0; r < h; r++) {
+        double s = 0.0;
+        for (uint32_t c = 0; c < w; c++) {
+            s += sg * acc[(size_t)r * w + c];
+            if (area) area[(size_t)r * w + c] = s;
+            cov[(size_t)r * w + c] = coverage(rule, s);
+        }
+    }
+}
+
+// Gradient of sum(grad_cov * cov) with respect to the polygon's vertex positions.
+static std::vector<D2> vertex_grads(const Poly& P, const std::vector<D2>& pos, int rule, uint32_t w, uint32_t h,
+                                    const double* area, const double* grad_cov) {
+    std::vector<double> gs((size_t)w * h);
+    for (size_t i = 0; i < gs.size(); i++) gs[i] = P.sign * grad_cov[i] * coverage_d(rule, area[i]);
+    std::vector<D2> gp(pos.size(), D2{0.0, 0.0});
+    for (int k = 0; k < (int)pos.size(); k++) {
+        int nk = next_vertex(P, k);
+        D2 p0 = pos[k], p1 = pos[nk];
+        bool down = p1.y > p0.y;  // P0 is the top end: s = u
+        double ga = 0.0, gb = 0.0;
+        edge_pieces(p0, p1, (int)w, (int)h, [&](int r, int c, double, double, double u0, double u1) {
+            if (c < 0 || c >= (int)w) return;
+            double g = gs[(size_t)r * w + c];
+            double i1 = u1 - u0, iu = 0.5 * (u1 * u1 - u0 * u0);
+            if (down) {
+                ga += g * (i1 - iu);
+                gb += g * iu;
+            } else {
+                ga += g * iu;
+                gb += g * (i1 - iu);
+            }
+        });
+        double px = -(p1.y - p0.y), py = p1.x - p0.x;
+        gp[k].x += px * ga;
+        gp[k].y += py * ga;
+        gp[nk].x += px * gb;
+        gp[nk].y += py * gb;
+    }
+    return gp;
+}
+
 struct Setup {
     Poly P;
     std::vector<double> val;
@@ -353,6 +423,446 @@ static Setup setup(const ft_op* ops, uint32_t n, const double* val, const float*
     return S;
 }
 
+
+// ===================================================================== strokes
+// The stroke of Plotter::stroke (plotter.rs:356-365): stroke points from the pen walk
+// with widths (stroker.rs:204-236), the outline of each sub-stroke (stroker.rs:239-416)
+// and the fill of that outline, NonZero, transformed a second time.  The f32 pass
+// makes footile's decisions (coincident points, joins, miter limit, arc subdivision)
+// and records each outline point as a node over the stroke points: an offset point,
+// a miter intersection or an arc point.  The nodes are then evaluated and
+// differentiated in double with the decisions held.
+
+static inline F2 f2sub(F2 a, F2 b) { return F2{a.x - b.x, a.y - b.y}; }
+static inline F2 f2add(F2 a, F2 b) { return F2{a.x + b.x, a.y + b.y}; }
+static inline F2 f2mul(F2 a, float s) { return F2{a.x * s, a.y * s}; }
+static inline F2 f2right(F2 v) { return F2{v.y, -v.x}; }
+static inline F2 f2norm(F2 v) {
+    float m = sqrtf(v.x * v.x + v.y * v.y);
+    return F2{v.x / m, v.y / m};
+}
+static inline float f2angle_rel(F2 a, F2 b) {
+    float th = ft_atan2f(a.y, a.x) - ft_atan2f(b.y, b.x);
+    const float PI = 3.14159265358979323846f;
+    if (th < -PI) return th + 2.0f * PI;
+    if (th > PI) return th - 2.0f * PI;
+    return th;
+}
+static inline bool f2line_x(F2 a0, F2 a1, F2 b0, F2 b1, F2* out) {
+    float x1 = a0.x, y1 = a0.y, x2 = a1.x, y2 = a1.y, x3 = b0.x, y3 = b0.y, x4 = b1.x, y4 = b1.y;
+    float den = (x1 - x2) * (y3 - y4) - (y1 - y2) * (x3 - x4);
+    if (den == 0.0f) return false;
+    float a = x1 * y2 - y1 * x2, b = x3 * y4 - y3 * x4;
+    *out = F2{(a * (x3 - x4) - (x1 - x2) * b) / den, (a * (y3 - y4) - (y1 - y2) * b) / den};
+    return true;
+}
+
+struct WP {
+    F2 p;
+    float w;
+};
+static inline WP wpmid(WP a, WP b) { return WP{fmidp(a.p, b.p), (a.w + b.w) / 2.0f}; }
+
+// Leaves of the width-carrying subdivision (the same tree as quad_tree / cubic_tree).
+static void quad_wtree(WP a, WP b, WP c, float tol_sq, int depth, double t0, std::vector<double>& ts,
+                       std::vector<WP>& pts, int& st) {
+    WP ab = wpmid(a, b), bc = wpmid(b, c), abbc = wpmid(ab, bc), ac = wpmid(a, c);
+    bool within = fdist_sq(abbc.p, ac.p) <= tol_sq;
+    if (within || depth >= FT_MAX_DEPTH) {
+        if (!within) st = std::max(st, (int)FT_ERR_DEPTH);
+        ts.push_back(t0 + std::ldexp(1.0, -depth));
+        pts.push_back(c);
+        return;
+    }
+    quad_wtree(a, ab, abbc, tol_sq, depth + 1, t0, ts, pts, st);
+    quad_wtree(abbc, bc, c, tol_sq, depth + 1, t0 + std::ldexp(1.0, -depth - 1), ts, pts, st);
+}
+static void cubic_wtree(WP a, WP b, WP c, WP d, float tol_sq, int depth, double t0, std::vector<double>& ts,
+                        std::vector<WP>& pts, int& st) {
+    WP ab = wpmid(a, b), bc = wpmid(b, c), cd = wpmid(c, d);
+    WP abbc = wpmid(ab, bc), bccd = wpmid(bc, cd), pe = wpmid(abbc, bccd), ad = wpmid(a, d);
+    bool within = fdist_sq(pe.p, ad.p) <= tol_sq;
+    if (within || depth >= FT_MAX_DEPTH) {
+        if (!within) st = std::max(st, (int)FT_ERR_DEPTH);
+        ts.push_back(t0 + std::ldexp(1.0, -depth));
+        pts.push_back(d);
+        return;
+    }
+    cubic_wtree(a, ab, abbc, pe, tol_sq, depth + 1, t0, ts, pts, st);
+    cubic_wtree(pe, bccd, cd, d, tol_sq, depth + 1, t0 + std::ldexp(1.0, -depth - 1), ts, pts, st);
+}
+
+enum { N_OFF = 0, N_MITER = 1, N_ARC = 2 };
+struct SNode {
+    int kind;
+    int a, b, c, d;  // OFF: stroke points a -> b, c = 0 offsets a, 1 offsets b; MITER: nodes a0 a1 b0 b1;
+                     // ARC: stroke point a (centre, width), nodes b (from) and c (to)
+    F2 f;            // f32 value (footile's outline point)
+};
+
+struct StrokeFig {
+    Poly cl;                  // stroke points (provenance, f32 points in cl.f)
+    std::vector<float> wf;    // f32 widths of the stroke points
+    std::vector<int> wsrc0;   // width source of the curve start (PenWidth op, -1: the call's width)
+    std::vector<int> wsrc1;   // width source of the op's own width
+    std::vector<SNode> nodes;
+    std::vector<int> verts;   // outline vertex -> node
+    Poly fig;                 // the outline polygon as the fill sees it (f32, transformed again)
+    int status = 0;
+};
+
+static StrokeFig build_stroke(const ft_op* ops, uint32_t n, const float* m, float tol_sq, int join, float ml,
+                              float sw0) {
+    StrokeFig S;
+    Poly& P = S.cl;
+    P.pen_src.assign(n, -1);
+    float sw = sw0;
+    int cur_pw = -1;                // PenWidth op in force
+    int pen = -1, pen_wsrc = -1;    // op holding the pen, width source of the pen
+    WP penp{F2{0.0f, 0.0f}, sw0};
+    struct Sub {
+        int start, n;
+        bool joined, done;
+    };
+    std::vector<Sub> subs{Sub{0, 0, false, false}};
+    auto close = [&](bool joined) {
+        if (!P.v.empty()) {
+            subs.back().joined = joined;
+            subs.back().done = true;
+        }
+    };
+    auto add = [&](WP q, int op, int form, double t, int w0, int w1) {  // Stroke::add_point
+        if (P.v.size() >= FT_MAX_POINTS) return;
+        bool done = subs.back().done;
+        if (done) subs.push_back(Sub{(int)P.v.size(), 0, false, false});
+        bool coincident = !P.f.empty() && P.f.back().x == q.p.x && P.f.back().y == q.p.y;
+        if (done || !coincident) {
+            P.v.push_back(Vert{op, form, t});
+            P.f.push_back(q.p);
+            P.sub.push_back(subs.back().start);
+            S.wf.push_back(q.w);
+            S.wsrc0.push_back(w0);
+            S.wsrc1.push_back(w1);
+            subs.back().n++;
+        }
+    };
+    auto ptf = [&](int j, int slot) { return F2{ops[j].v[2 * slot], ops[j].v[2 * slot + 1]}; };
+    std::vector<double> ts;
+    std::vector<WP> pts;
+    for (uint32_t i = 0; i < n; i++) {
+        const ft_op& o = ops[i];
+        switch (o.kind) {
+            case FT_OP_CLOSE:
+                close(true);
+                pen = -1;
+                pen_wsrc = cur_pw;
+                penp = WP{F2{0.0f, 0.0f}, sw};
+                break;
+            case FT_OP_MOVE:
+            case FT_OP_LINE: {
+                WP q{ptf(i, 0), sw};
+                if (o.kind == FT_OP_MOVE) close(false);
+                add(WP{fxform(m, q.p), q.w}, (int)i, V_POINT, 1.0, cur_pw, cur_pw);
+                pen = (int)i;
+                pen_wsrc = cur_pw;
+                penp = q;
+                break;
+            }
+            case FT_OP_QUAD:
+            case FT_OP_CUBIC: {
+                P.pen_src[i] = pen;
+                const bool cubic = o.kind == FT_OP_CUBIC;
+                WP a{fxform(m, penp.p), penp.w}, b, c, d;
+                if (cubic) {
+                    float w0 = sw + (penp.w - sw) * (1.0f / 3.0f);  // float_lerp, geom.rs:14-16
+                    float w1 = sw + (penp.w - sw) * (2.0f / 3.0f);
+                    b = WP{fxform(m, ptf(i, 0)), w0};
+                    c = WP{fxform(m, ptf(i, 1)), w1};
+                    d = WP{fxform(m, ptf(i, 2)), sw};
+                } else {
+                    b = WP{fxform(m, ptf(i, 0)), (penp.w + sw) / 2.0f};
+                    c = WP{fxform(m, ptf(i, 1)), sw};
+                    d = c;
+                }
+                if (!ffinite(a.p) || !ffinite(b.p) || !ffinite(c.p) || !ffinite(d.p)) {
+                    S.status = std::max(S.status, (int)FT_ERR_ARG);
+                    add(d, (int)i, V_POINT, 1.0, cur_pw, cur_pw);
+                } else {
+                    ts.clear();
+                    pts.clear();
+                    if (cubic)
+                        cubic_wtree(a, b, c, d, tol_sq, 0, 0.0, ts, pts, S.status);
+                    else
+                        quad_wtree(a, b, c, tol_sq, 0, 0.0, ts, pts, S.status);
+                    for (size_t j = 0; j < ts.size(); j++)
+                        add(pts[j], (int)i, cubic ? V_CUBIC : V_QUAD, ts[j], pen_wsrc, cur_pw);
+                }
+                pen = (int)i;
+                pen_wsrc = cur_pw;
+                penp = WP{cubic ? ptf(i, 2) : ptf(i, 1), sw};
+                break;
+            }
+            case FT_OP_PEN_WIDTH:
+                sw = o.v[0];
+                cur_pw = (int)i;
+                break;
+            default:
+                break;
+        }
+    }
+    // outline (stroker.rs:239-295)
+    std::vector<char> is_close;  // per outline op: 1 = Close
+    auto emit = [&](int node) {
+        S.verts.push_back(node);
+        is_close.push_back(0);
+    };
+    auto emit_close = [&]() {
+        S.verts.push_back(-1);
+        is_close.push_back(1);
+    };
+    auto off = [&](int k0, int k1, int which) {
+        F2 vr = f2norm(f2right(f2sub(P.f[k1], P.f[k0])));
+        int ks = which ? k1 : k0;
+        F2 v = f2add(P.f[ks], f2mul(vr, S.wf[ks] / 2.0f));
+        S.nodes.push_back(SNode{N_OFF, k0, k1, which, 0, v});
+        return (int)S.nodes.size() - 1;
+    };
+    std::function<void(int, int, int, int)> arc = [&](int k, int na, int nb, int depth) {
+        F2 a = S.nodes[na].f, b = S.nodes[nb].f;
+        F2 vr = f2norm(f2right(f2sub(b, a)));
+        F2 c = f2add(P.f[k], f2mul(vr, S.wf[k] / 2.0f));
+        F2 ab = fmidp(a, b);
+        if (!ffinite(c) || fdist_sq(c, ab) <= tol_sq) {
+            emit(nb);
+        } else if (depth >= FT_MAX_DEPTH) {
+            S.status = std::max(S.status, (int)FT_ERR_DEPTH);
+            emit(nb);
+        } else {
+            S.nodes.push_back(SNode{N_ARC, k, na, nb, 0, c});
+            int nc = (int)S.nodes.size() - 1;
+            arc(k, na, nc, depth + 1);
+            arc(k, nc, nb, depth + 1);
+        }
+    };
+    auto do_join = [&](int k, int a0, int a1, int b0, int b1) {
+        F2 A0 = S.nodes[a0].f, A1 = S.nodes[a1].f, B0 = S.nodes[b0].f, B1 = S.nodes[b1].f;
+        if (join == FT_JOIN_MITER) {
+            if (ml > 0.0f) {
+                float sm_min = 1.0f / ml;
+                float th = f2angle_rel(f2sub(A1, A0), f2sub(B0, B1));
+                float sm = fabsf(ft_sinf(th / 2.0f));
+                F2 xp;
+                if (sm >= sm_min && sm < 1.0f && f2line_x(A0, A1, B0, B1, &xp)) {
+                    S.nodes.push_back(SNode{N_MITER, a0, a1, b0, b1, xp});
+                    emit((int)S.nodes.size() - 1);
+                    return;
+                }
+            }
+            emit(a1);
+            emit(b0);
+        } else if (join == FT_JOIN_BEVEL) {
+            emit(a1);
+            emit(b0);
+        } else {
+            float th = f2angle_rel(f2sub(A1, A0), f2sub(B0, B1));
+            if (th <= 0.0f) {
+                emit(a1);
+                emit(b0);
+            } else {
+                emit(a1);
+                arc(k, a1, b0, 0);
+            }
+        }
+    };
+    for (const Sub& sb : subs) {
+        const int len = sb.joined ? sb.n + 1 : (sb.n > 0 ? sb.n - 1 : 0);  // SubStroke::len (u16)
+        const int lenw = len & 0xFFFF;
+        if (lenw == 0) continue;
+        auto nextv = [&](int v, bool fwd) {
+            if (fwd) return v + 1 < sb.start + sb.n ? v + 1 : sb.start;
+            return v > sb.start ? v - 1 : sb.start + sb.n - 1;
+        };
+        for (int side = 0; side < 2; side++) {
+            const bool fwd = side == 0;
+            int v0 = fwd ? sb.start : nextv(sb.start, false);
+            int v1 = nextv(v0, fwd);
+            bool have = false;
+            int x0 = -1, x1 = -1;
+            for (int k = 0; k < lenw; k++) {
+                int o0 = off(v0, v1, 0), o1 = off(v0, v1, 1);
+                if (have)
+                    do_join(v0, x0, x1, o0, o1);
+                else if (!sb.joined)
+                    emit(o0);
+                have = true;
+                x0 = o0;
+                x1 = o1;
+                v0 = v1;
+                v1 = nextv(v1, fwd);
+            }
+            if (!sb.joined && have) emit(x1);
+            if (fwd && sb.joined) emit_close();
+        }
+        emit_close();
+    }
+    // the fill of the outline: Line points transformed again, sub-figures between Closes
+    Poly& F = S.fig;
+    bool fresh = true;
+    int sub_start = 0;
+    std::vector<int> vmap;
+    for (size_t j = 0; j < S.verts.size(); j++) {
+        if (is_close[j]) {
+            fresh = true;
+            continue;
+        }
+        if (fresh) {
+            sub_start = (int)F.v.size();
+            fresh = false;
+        }
+        F.v.push_back(Vert{S.verts[j], V_POINT, 1.0});
+        F.f.push_back(fxform(m, S.nodes[S.verts[j]].f));
+        F.sub.push_back(sub_start);
+    }
+    if (F.v.size() > FT_MAX_POINTS) S.status = std::max(S.status, (int)FT_ERR_CAP);
+    F.sign = fig_sign(F);
+    return S;
+}
+
+struct StrokeEval {
+    std::vector<D2> P;   // stroke points (transformed once)
+    std::vector<double> W;
+    std::vector<D2> N;   // node values
+    std::vector<D2> V;   // outline vertices (transformed again)
+};
+
+static inline D2 d2right(D2 v) { return D2{v.y, -v.x}; }
+
+// Node values in double from stroke points (P, W).
+static void eval_nodes(const StrokeFig& S, StrokeEval& E) {
+    E.N.resize(S.nodes.size());
+    for (size_t i = 0; i < S.nodes.size(); i++) {
+        const SNode& nd = S.nodes[i];
+        if (nd.kind == N_OFF || nd.kind == N_ARC) {
+            D2 from = nd.kind == N_OFF ? E.P[nd.a] : E.N[nd.b];
+            D2 to = nd.kind == N_OFF ? E.P[nd.b] : E.N[nd.c];
+            D2 u = d2right(D2{to.x - from.x, to.y - from.y});
+            double len = std::sqrt(u.x * u.x + u.y * u.y);
+            D2 vr{u.x / len, u.y / len};
+            int ks = nd.kind == N_OFF ? (nd.c ? nd.b : nd.a) : nd.a;
+            E.N[i] = D2{E.P[ks].x + vr.x * E.W[ks] / 2, E.P[ks].y + vr.y * E.W[ks] / 2};
+        } else {
+            D2 a0 = E.N[nd.a], a1 = E.N[nd.b], b0 = E.N[nd.c], b1 = E.N[nd.d];
+            double x1 = a0.x, y1 = a0.y, x2 = a1.x, y2 = a1.y, x3 = b0.x, y3 = b0.y, x4 = b1.x, y4 = b1.y;
+            double den = (x1 - x2) * (y3 - y4) - (y1 - y2) * (x3 - x4);
+            double a = x1 * y2 - y1 * x2, b = x3 * y4 - y3 * x4;
+            E.N[i] = D2{(a * (x3 - x4) - (x1 - x2) * b) / den, (a * (y3 - y4) - (y1 - y2) * b) / den};
+        }
+    }
+}
+
+// Stroke points, nodes and outline in double.  Without `val`: footile's f32 stroke
+// points and outline widened (the polygon the CUDA path covers); with `val` (6 per
+// op) and `sw0`: Bernstein points and linear widths of the held tree.
+static StrokeEval evaluate(const StrokeFig& S, const ft_op* ops, const double* val, double sw0, const double* m) {
+    StrokeEval E;
+    const size_t ns = S.cl.v.size();
+    E.P.resize(ns);
+    E.W.resize(ns);
+    if (!val) {
+        for (size_t k = 0; k < ns; k++) {
+            E.P[k] = D2{(double)S.cl.f[k].x, (double)S.cl.f[k].y};
+            E.W[k] = S.wf[k];
+        }
+    } else {
+        E.P = positions(S.cl, ops, val, m);
+        auto wv = [&](int src) { return src < 0 ? sw0 : val[6 * src]; };
+        for (size_t k = 0; k < ns; k++) {
+            const Vert& v = S.cl.v[k];
+            E.W[k] = v.form == V_POINT ? wv(S.wsrc1[k]) : (1.0 - v.t) * wv(S.wsrc0[k]) + v.t * wv(S.wsrc1[k]);
+        }
+    }
+    eval_nodes(S, E);
+    E.V.resize(S.fig.v.size());
+    for (size_t j = 0; j < S.fig.v.size(); j++) {
+        if (!val) {
+            E.V[j] = D2{(double)S.fig.f[j].x, (double)S.fig.f[j].y};
+        } else {
+            D2 q = E.N[S.fig.v[j].op];
+            E.V[j] = D2{m[0] * q.x + m[1] * q.y + m[2], m[3] * q.x + m[4] * q.y + m[5]};
+        }
+    }
+    return E;
+}
+
+// Reverse pass over the nodes: outline vertex gradients gV -> stroke point position
+// and width gradients (gP, gW).
+static void backprop_nodes(const StrokeFig& S, const StrokeEval& E, const std::vector<D2>& gV, const double* m,
+                           std::vector<D2>& gP, std::vector<double>& gW) {
+    std::vector<D2> gN(S.nodes.size(), D2{0.0, 0.0});
+    for (size_t j = 0; j < gV.size(); j++) {
+        D2& g = gN[S.fig.v[j].op];
+        g.x += m[0] * gV[j].x + m[3] * gV[j].y;
+        g.y += m[1] * gV[j].x + m[4] * gV[j].y;
+    }
+    gP.assign(E.P.size(), D2{0.0, 0.0});
+    gW.assign(E.P.size(), 0.0);
+    for (int i = (int)S.nodes.size() - 1; i >= 0; i--) {
+        const SNode& nd = S.nodes[i];
+        const D2 g = gN[i];
+        if (g.x == 0.0 && g.y == 0.0) continue;
+        if (nd.kind == N_OFF || nd.kind == N_ARC) {
+            D2 from = nd.kind == N_OFF ? E.P[nd.a] : E.N[nd.b];
+            D2 to = nd.kind == N_OFF ? E.P[nd.b] : E.N[nd.c];
+            D2 u = d2right(D2{to.x - from.x, to.y - from.y});
+            double len = std::sqrt(u.x * u.x + u.y * u.y);
+            D2 vr{u.x / len, u.y / len};
+            int ks = nd.kind == N_OFF ? (nd.c ? nd.b : nd.a) : nd.a;
+            gP[ks].x += g.x;
+            gP[ks].y += g.y;
+            gW[ks] += 0.5 * (vr.x * g.x + vr.y * g.y);
+            D2 gvr{g.x * E.W[ks] / 2, g.y * E.W[ks] / 2};
+            double dv = vr.x * gvr.x + vr.y * gvr.y;
+            D2 gu{(gvr.x - vr.x * dv) / len, (gvr.y - vr.y * dv) / len};
+            D2 gd{-gu.y, gu.x};  // u = (d.y, -d.x)
+            if (nd.kind == N_OFF) {
+                gP[nd.b].x += gd.x;
+                gP[nd.b].y += gd.y;
+                gP[nd.a].x -= gd.x;
+                gP[nd.a].y -= gd.y;
+            } else {
+                gN[nd.c].x += gd.x;
+                gN[nd.c].y += gd.y;
+                gN[nd.b].x -= gd.x;
+                gN[nd.b].y -= gd.y;
+            }
+        } else {
+            D2 a0 = E.N[nd.a], a1 = E.N[nd.b], b0 = E.N[nd.c], b1 = E.N[nd.d];
+            double x1 = a0.x, y1 = a0.y, x2 = a1.x, y2 = a1.y, x3 = b0.x, y3 = b0.y, x4 = b1.x, y4 = b1.y;
+            double den = (x1 - x2) * (y3 - y4) - (y1 - y2) * (x3 - x4);
+            double a = x1 * y2 - y1 * x2, b = x3 * y4 - y3 * x4;
+            double x = (a * (x3 - x4) - (x1 - x2) * b) / den, y = (a * (y3 - y4) - (y1 - y2) * b) / den;
+            double gNx = g.x / den, gNy = g.y / den, gden = -(g.x * x + g.y * y) / den;
+            double ga = gNx * (x3 - x4) + gNy * (y3 - y4), gb = -gNx * (x1 - x2) - gNy * (y1 - y2);
+            double gx1 = -gNx * b + ga * y2 + gden * (y3 - y4);
+            double gx2 = gNx * b - ga * y1 - gden * (y3 - y4);
+            double gy1 = -gNy * b - ga * x2 - gden * (x3 - x4);
+            double gy2 = gNy * b + ga * x1 + gden * (x3 - x4);
+            double gx3 = gNx * a + gb * y4 - gden * (y1 - y2);
+            double gx4 = -gNx * a - gb * y3 + gden * (y1 - y2);
+            double gy3 = gNy * a - gb * x4 + gden * (x1 - x2);
+            double gy4 = -gNy * a + gb * x3 - gden * (x1 - x2);
+            gN[nd.a].x += gx1;
+            gN[nd.a].y += gy1;
+            gN[nd.b].x += gx2;
+            gN[nd.b].y += gy2;
+            gN[nd.c].x += gx3;
+            gN[nd.c].y += gy3;
+            gN[nd.d].x += gx4;
+            gN[nd.d].y += gy4;
+        }
+    }
+}
+
 }  // namespace adj
 
 extern "C" {
@@ -366,32 +876,10 @@ __attribute__((visibility("default"))) int orc_adj_forward(int32_t rule, const f
                                                            const double* val, uint32_t w, uint32_t h, float tol,
                                                            const float* xf, double* cov, double* area) {
     adj::Setup S = adj::setup(ops, n_ops, val, xf, tol);
-    std::vector<double> acc((size_t)w * h, 0.0);
-    if (S.P.status != FT_ERR_CAP) {
-        std::vector<adj::D2> pos = adj::positions(S.P, ops, S.bernstein ? S.val.data() : nullptr, S.m);
-        for (int k = 0; k < (int)pos.size(); k++) {
-            adj::D2 p0 = pos[k], p1 = pos[adj::next_vertex(S.P, k)];
-            double dir = p1.y > p0.y ? 1.0 : -1.0;
-            adj::edge_pieces(p0, p1, (int)w, (int)h, [&](int r, int c, double hh, double xm, double, double) {
-                double* row = &acc[(size_t)r * w];
-                if (c < 0) {
-                    row[0] += dir * hh;
-                } else if (c < (int)w) {
-                    row[c] += dir * hh * (c + 1 - xm);
-                    if (c + 1 < (int)w) row[c + 1] += dir * hh * (xm - c);
-                }
-            });
-        }
-    }
-    const double sg = S.P.sign;
-    for (uint32_t r = 0; r < h; r++) {
-        double s = 0.0;
-        for (uint32_t c = 0; c < w; c++) {
-            s += sg * acc[(size_t)r * w + c];
-            if (area) area[(size_t)r * w + c] = s;
-            cov[(size_t)r * w + c] = adj::coverage(rule, s);
-        }
-    }
+    std::vector<adj::D2> pos;
+    if (S.P.status != FT_ERR_CAP) pos = adj::positions(S.P, ops, S.bernstein ? S.val.data() : nullptr, S.m);
+    for (adj::D2& q : pos) q = adj::fx_range(q);
+    adj::cover(S.P, pos, rule, w, h, cov, area);
     return S.P.status;
 }
 
@@ -403,33 +891,10 @@ __attribute__((visibility("default"))) int orc_adj_backward(int32_t rule, const 
                                                             const double* grad_cov, double* grad_val) {
     adj::Setup S = adj::setup(ops, n_ops, val, xf, tol);
     if (S.P.status == FT_ERR_CAP) return S.P.status;
-    std::vector<double> gs((size_t)w * h);
-    for (size_t i = 0; i < gs.size(); i++) gs[i] = S.P.sign * grad_cov[i] * adj::coverage_d(rule, area[i]);
-    std::vector<adj::D2> pos = adj::positions(S.P, ops, S.bernstein ? S.val.data() : nullptr, S.m);
-    std::vector<adj::D2> gp(pos.size(), adj::D2{0.0, 0.0});
-    for (int k = 0; k < (int)pos.size(); k++) {
-        int nk = adj::next_vertex(S.P, k);
-        adj::D2 p0 = pos[k], p1 = pos[nk];
-        bool down = p1.y > p0.y;  // P0 is the top end: s = u
-        double ga = 0.0, gb = 0.0;
-        adj::edge_pieces(p0, p1, (int)w, (int)h, [&](int r, int c, double, double, double u0, double u1) {
-            if (c < 0 || c >= (int)w) return;
-            double g = gs[(size_t)r * w + c];
-            double i1 = u1 - u0, iu = 0.5 * (u1 * u1 - u0 * u0);
-            if (down) {
-                ga += g * (i1 - iu);
-                gb += g * iu;
-            } else {
-                ga += g * iu;
-                gb += g * (i1 - iu);
-            }
-        });
-        double px = -(p1.y - p0.y), py = p1.x - p0.x;
-        gp[k].x += px * ga;
-        gp[k].y += py * ga;
-        gp[nk].x += px * gb;
-        gp[nk].y += py * gb;
-    }
+    std::vector<adj::D2> raw = adj::positions(S.P, ops, S.bernstein ? S.val.data() : nullptr, S.m), pos = raw;
+    for (adj::D2& q : pos) q = adj::fx_range(q);
+    std::vector<adj::D2> gp = adj::vertex_grads(S.P, pos, rule, w, h, area, grad_cov);
+    for (size_t k = 0; k < gp.size(); k++) gp[k] = adj::fx_pass(raw[k], gp[k]);
     for (size_t k = 0; k < pos.size(); k++) {
         const adj::Vert& v = S.P.v[k];
         // back through the transform's linear part
@@ -457,6 +922,113 @@ __attribute__((visibility("default"))) int orc_adj_backward(int32_t rule, const 
         }
     }
     return S.P.status;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// Stroke forward: coverage of Plotter::stroke's outline (the same as orc_adj_forward
+// for fills).  `sw0` is the pen width at the call's start.  `val` (6 per op, may be
+// NULL): Bernstein stroke points and linear widths of the held tree, the PenWidth
+// widths taken from val[6 * op].
+__attribute__((visibility("default"))) int orc_adj_stroke_forward(const ft_op* ops, uint32_t n_ops, const double* val,
+                                                                  double sw0, uint32_t w, uint32_t h, float tol,
+                                                                  const float* xf, int32_t join, float ml,
+                                                                  double* cov, double* area) {
+    const float t = std::max(tol, 0.01f);
+    adj::StrokeFig S = adj::build_stroke(ops, n_ops, xf, t * t, join, ml, (float)sw0);
+    double m[6];
+    for (int k = 0; k < 6; k++) m[k] = xf[k];
+    std::vector<adj::D2> pos;
+    if (S.status != FT_ERR_CAP) pos = adj::evaluate(S, ops, val, sw0, m).V;
+    for (adj::D2& q : pos) q = adj::fx_range(q);
+    adj::cover(S.fig, pos, FT_NONZERO, w, h, cov, area);
+    return S.status;
+}
+
+// Stroke backward: d(sum(grad_cov * cov)) / d(op floats) into grad_val (6 per op;
+// PenWidth ops in slot 0) and / d(sw0) into *grad_sw0.
+__attribute__((visibility("default"))) int orc_adj_stroke_backward(const ft_op* ops, uint32_t n_ops, const double* val,
+                                                                   double sw0, uint32_t w, uint32_t h, float tol,
+                                                                   const float* xf, int32_t join, float ml,
+                                                                   const double* area, const double* grad_cov,
+                                                                   double* grad_val, double* grad_sw0) {
+    const float t = std::max(tol, 0.01f);
+    adj::StrokeFig S = adj::build_stroke(ops, n_ops, xf, t * t, join, ml, (float)sw0);
+    if (S.status == FT_ERR_CAP) return S.status;
+    double m[6];
+    for (int k = 0; k < 6; k++) m[k] = xf[k];
+    adj::StrokeEval E = adj::evaluate(S, ops, val, sw0, m);
+    std::vector<adj::D2> pos = E.V;
+    for (adj::D2& q : pos) q = adj::fx_range(q);
+    std::vector<adj::D2> gV = adj::vertex_grads(S.fig, pos, FT_NONZERO, w, h, area, grad_cov);
+    for (size_t j = 0; j < gV.size(); j++) gV[j] = adj::fx_pass(E.V[j], gV[j]);
+    std::vector<adj::D2> gP;
+    std::vector<double> gW;
+    adj::backprop_nodes(S, E, gV, m, gP, gW);
+    auto gw = [&](int src, double g) {
+        if (src < 0) {
+            if (grad_sw0) *grad_sw0 += g;
+        } else {
+            grad_val[6 * src] += g;
+        }
+    };
+    for (size_t k = 0; k < gP.size(); k++) {
+        const adj::Vert& v = S.cl.v[k];
+        double gx = m[0] * gP[k].x + m[3] * gP[k].y, gy = m[1] * gP[k].x + m[4] * gP[k].y;
+        auto add = [&](int j, int slot, double wgt) {
+            grad_val[6 * j + 2 * slot] += wgt * gx;
+            grad_val[6 * j + 2 * slot + 1] += wgt * gy;
+        };
+        int kind = ops[v.op].kind;
+        if (v.form == adj::V_POINT) {
+            add(v.op, adj::end_slot(kind), 1.0);
+            gw(S.wsrc1[k], gW[k]);
+            continue;
+        }
+        double tt = v.t, u = 1.0 - tt;
+        int ps = S.cl.pen_src[v.op];
+        if (v.form == adj::V_QUAD) {
+            if (ps >= 0) add(ps, adj::end_slot(ops[ps].kind), u * u);
+            add(v.op, 0, 2 * tt * u);
+            add(v.op, 1, tt * tt);
+        } else {
+            if (ps >= 0) add(ps, adj::end_slot(ops[ps].kind), u * u * u);
+            add(v.op, 0, 3 * tt * u * u);
+            add(v.op, 1, 3 * tt * tt * u);
+            add(v.op, 2, tt * tt * tt);
+        }
+        gw(S.wsrc0[k], u * gW[k]);
+        gw(S.wsrc1[k], tt * gW[k]);
+    }
+    return S.status;
+}
+
+// The f32 outline of the stroke (Line / Close ops as footile's Stroke::path_ops emits
+// them, before the second transform), for checking the node pass against the
+// stroker.  Returns the op count (may exceed cap).
+__attribute__((visibility("default"))) uint32_t orc_adj_stroke_outline(const ft_op* ops, uint32_t n_ops, float tol,
+                                                                       const float* xf, int32_t join, float ml,
+                                                                       float sw0, ft_op* out, uint32_t cap) {
+    const float t = std::max(tol, 0.01f);
+    adj::StrokeFig S = adj::build_stroke(ops, n_ops, xf, t * t, join, ml, sw0);
+    uint32_t k = 0;
+    for (int v : S.verts) {
+        if (k < cap) {
+            ft_op o{};
+            if (v < 0) {
+                o.kind = FT_OP_CLOSE;
+            } else {
+                o.kind = FT_OP_LINE;
+                o.v[0] = S.nodes[v].f.x;
+                o.v[1] = S.nodes[v].f.y;
+            }
+            out[k] = o;
+        }
+        k++;
+    }
+    return k;
 }
 
 }  // extern "C"

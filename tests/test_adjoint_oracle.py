@@ -130,3 +130,67 @@ def test_oracle_vertex_cap_status():
     ops["kind"][-1] = _abi.OP_CLOSE
     cov, _, st = oracle.adj_forward(_abi.NONZERO, ops, 64, 64)
     assert st == _abi.ERR_CAP and not cov.any()
+
+
+# ----------------------------------------------------------------------- strokes
+STROKE = (Path2D().absolute().pen_width(6.0).move_to(20.3, 30.1).cubic_to(60, 5, 90, 90, 110.2, 40.7)
+          .line_to(70.5, 100.25).quad_to(40, 120, 25.5, 80.5).finish())
+JOINS = [(_abi.JOIN_MITER, 4.0), (_abi.JOIN_BEVEL, 0.0), (_abi.JOIN_ROUND, 0.0), (_abi.JOIN_MITER, 1.5)]
+
+
+def test_stroke_outline_nodes_match_the_stroker():
+    # the f32 node pass of the stroke adjoint emits exactly the outline footile's
+    # stroker emits (the integer oracle's Stroke::path_ops)
+    from footile_gb300.path import PathOp, ops_array
+    rng = np.random.default_rng(7)
+    for i in range(200):
+        side = int(rng.integers(16, 200))
+        o = workloads.random_path(rng, side, int(rng.integers(1, 25)), n_sub=int(rng.integers(1, 3)),
+                                  close=bool(i % 2))
+        o = np.concatenate([ops_array([PathOp.PenWidth(float(rng.uniform(0.5, 12)))]), o])
+        join = JOINS[i % 4]
+        tol = [0.1, 0.3, 1.0][i % 3]
+        a = oracle.stroke_outline(o, s_width=1.0, join=join[0], miter_limit=join[1], tolerance=tol)
+        b = oracle.adj_stroke_outline(o, s_width=1.0, join=join[0], miter_limit=join[1], tolerance=tol)
+        assert len(a) == len(b) and (a["kind"] == b["kind"]).all(), i
+        assert np.array_equal(a["v"].view(np.uint32), b["v"].view(np.uint32)), i
+
+
+@pytest.mark.parametrize("join", JOINS[:3])
+def test_stroke_gradient_matches_central_differences(join):
+    w = h = 128
+    target = np.random.default_rng(5).random((h, w))
+    base = values(STROKE)
+    kw = dict(join=join[0], miter_limit=join[1])
+    cov, area, st = oracle.adj_stroke_forward(STROKE, w, h, val=base, **kw)
+    assert st == 0
+    g, gsw = oracle.adj_stroke_backward(STROKE, w, h, area, 2 * (cov - target), val=base, **kw)
+
+    def loss(val, sw0=1.0):
+        return ((oracle.adj_stroke_forward(STROKE, w, h, val=val, s_width=sw0, **kw)[0] - target) ** 2).sum()
+    fd = np.zeros_like(base)
+    step = 1e-5
+    for i in range(len(STROKE)):
+        for k in range(6):
+            vp, vm = base.copy(), base.copy()
+            vp[i, k] += step
+            vm[i, k] -= step
+            fd[i, k] = (loss(vp) - loss(vm)) / (2 * step)
+    assert np.abs(g - fd).max() / np.abs(fd).max() < 2e-4
+    assert g[0, 0] != 0.0  # the PenWidth op receives the width gradient
+    # the starting pen width matters only when no PenWidth op precedes the points
+    o2 = STROKE[1:]
+    b2 = values(o2)
+    c2, a2, _ = oracle.adj_stroke_forward(o2, w, h, val=b2, s_width=5.0, **kw)
+    _, gsw2 = oracle.adj_stroke_backward(o2, w, h, a2, 2 * (c2 - target), val=b2, s_width=5.0, **kw)
+    l = lambda s: ((oracle.adj_stroke_forward(o2, w, h, val=b2, s_width=s, **kw)[0] - target) ** 2).sum()
+    fd_sw = (l(5.0 + 1e-5) - l(5.0 - 1e-5)) / 2e-5
+    assert abs(gsw2 - fd_sw) <= 2e-4 * max(abs(fd_sw), 1.0)
+
+
+def test_stroke_coverage_tracks_footile_masks():
+    for join in JOINS[:3]:
+        cov, _, _ = oracle.adj_stroke_forward(STROKE, 128, 128, join=join[0], miter_limit=join[1])
+        m = np.zeros((128, 128), np.uint8)
+        oracle.stroke(STROKE, m, _abi.MATTE8, clr=(255,) * 4, join=join[0], miter_limit=join[1])
+        assert np.abs(cov * 255 - m).mean() < 1.5
