@@ -49,7 +49,7 @@ def parse_args():
     ap.add_argument("--no-extras", action="store_true", help="skip the secondary workloads")
     ap.add_argument("--no-tune", action="store_true", help="use the built-in plan instead of the autotuner")
     ap.add_argument("--tune-cache", default=None, help="autotuner cache file (looked up, then appended)")
-    ap.add_argument("--only", choices=["single", "scene", "strokes", "adjoint"],
+    ap.add_argument("--only", choices=["single", "scene", "strokes", "adjoint", "adjoint_strokes"],
                     help="run one secondary workload alone (for profiling) and print its line")
     return ap.parse_args()
 
@@ -413,6 +413,77 @@ def extra_adjoint(ctx, stream, dev, cpu=True, reps=10, check_paths=32, fd_paths=
     return out
 
 
+def extra_adjoint_strokes(ctx, stream, dev, cpu=True, reps=5, n_paths=1024, side=256, check_paths=8):
+    """Stroke coverage adjoint on 1,024 open strokes shaped like the ordered-composite
+    workload (8..64 cubics, PenWidth 1..12, Miter(4)), each on its own 256x256 f32
+    coverage plane: forward / backward device time and the error of the op-float and
+    pen-width gradients against the FP64 oracle (and central differences, h = 1e-2)."""
+    import torch
+    from footile_gb300 import _abi, workloads
+    from footile_gb300.adjoint import Adjoint, pack_coverage
+    paths_ops, _, _, _ = workloads.strokes_16384(n_paths=n_paths, side=side)
+    ops, paths, cov_bytes = pack_coverage(paths_ops, [side] * n_paths)
+    target = np.random.default_rng(5).random(cov_bytes // 4, dtype=np.float32)
+    ops_d = torch.from_numpy(ops.view(np.uint8).copy()).to(dev)
+    tgt_d = torch.from_numpy(target).to(dev)
+    cov_d = torch.empty(cov_bytes // 4, dtype=torch.float32, device=dev)
+    gops_d = torch.empty((len(ops), 6), dtype=torch.float32, device=dev)
+    gw_d = torch.empty(n_paths, dtype=torch.float32, device=dev)
+    ctx.set_join(_abi.JOIN_MITER, 4.0)
+    adj = Adjoint(ctx)
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    fwd, bwd = [], []
+    for it in range(reps + 2):
+        e[0].record(stream)
+        adj.forward(_abi.NONZERO, ops_d, paths, cov_d, stroke=True)
+        e[1].record(stream)
+        g_cov = 2.0 * (cov_d - tgt_d)
+        e[2].record(stream)
+        adj.backward(g_cov, gops_d, gw_d)
+        e[3].record(stream)
+        torch.cuda.synchronize()
+        if it >= 2:
+            fwd.append(e[0].elapsed_time(e[1]))
+            bwd.append(e[2].elapsed_time(e[3]))
+    st = adj.status()
+    out = {"workload": "strokes adjoint (1,024 open strokes, 8..64 cubics, width 1..12, Miter(4), 256x256 f32 each)",
+           "fwd_ms": float(np.median(fwd)), "bwd_ms": float(np.median(bwd)),
+           "bwd_over_fwd": float(np.median(bwd) / np.median(fwd)), "paths_status_ok": int((st == 0).sum())}
+    if cpu:
+        import oracle
+        cov = cov_d.cpu().numpy()
+        g = gops_d.cpu().numpy().astype(np.float64)
+        gw = gw_d.cpu().numpy().astype(np.float64)
+        gc = (2.0 * (cov.astype(np.float64) - target)).astype(np.float32).astype(np.float64)
+        num, den = 0.0, 0.0
+        for i, p in enumerate(paths[:check_paths]):
+            b, n = int(p["op_begin"]), int(p["n_ops"])
+            o = ops[b:b + n]
+            c64, area, _ = oracle.adj_stroke_forward(o, side, side)
+            off = int(p["raster_offset"]) // 4
+            r, rw = oracle.adj_stroke_backward(o, side, side, area, gc[off:off + side * side].reshape(side, side))
+            num = max(num, float(np.abs(g[b:b + n] - r).max()), abs(gw[i] - rw))
+            den = max(den, float(np.abs(r).max()), abs(rw))
+        out["max_rel_err_vs_fp64"] = num / den
+        out["paths_checked"] = check_paths
+        # central differences (h = 1e-2) of the FP64 loss for the PenWidth op of path 0
+        p = paths[0]
+        b, n = int(p["op_begin"]), int(p["n_ops"])
+        o = ops[b:b + n]
+        off = int(p["raster_offset"]) // 4
+        tg = target[off:off + side * side].reshape(side, side).astype(np.float64)
+        base = np.array([x["v"] for x in o], dtype=np.float64)
+        lo = lambda v: ((oracle.adj_stroke_forward(o, side, side, val=v)[0] - tg) ** 2).sum()
+        vp, vm = base.copy(), base.copy()
+        vp[0, 0] += 1e-2
+        vm[0, 0] -= 1e-2
+        fd_w = (lo(vp) - lo(vm)) / 2e-2
+        out["pen_width_grad_path0"] = float(g[b, 0])
+        out["pen_width_central_fd_h1e-2_path0"] = float(fd_w)
+    adj.close()
+    return out
+
+
 def run_only(args):
     import torch
     from footile_gb300._lib import Context
@@ -421,7 +492,8 @@ def run_only(args):
     torch.cuda.set_stream(stream)
     ctx = Context(0)
     ctx.set_stream(stream.cuda_stream)
-    fn = {"single": extra_single, "scene": extra_scene, "strokes": extra_strokes, "adjoint": extra_adjoint}[args.only]
+    fn = {"single": extra_single, "scene": extra_scene, "strokes": extra_strokes, "adjoint": extra_adjoint,
+          "adjoint_strokes": extra_adjoint_strokes}[args.only]
     print(json.dumps(fn(ctx, stream, dev, cpu=not args.no_cpu)), flush=True)
 
 
@@ -562,7 +634,8 @@ def run_ours(args):
     if rank == 0 and not args.no_extras:
         extras = {}
         for name, fn in (("single_path_256", extra_single), ("scene_4096", extra_scene),
-                         ("strokes_16384", extra_strokes), ("adjoint_cubics_1024", extra_adjoint)):
+                         ("strokes_16384", extra_strokes), ("adjoint_cubics_1024", extra_adjoint),
+                         ("adjoint_strokes_1024", extra_adjoint_strokes)):
             try:
                 extras[name] = fn(ctx, stream, dev, cpu=(world == 1 and not args.no_cpu))
             except Exception as e:  # report, never hide, a failing secondary workload

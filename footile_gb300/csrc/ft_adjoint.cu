@@ -725,22 +725,27 @@ __device__ int build_stroke_dev(const AParams& p, const ft_op* ops, int n, float
     int cur_pw = -1, pen = -1, pen_wsrc = -1;
     P2 penp = p2(0.0f, 0.0f);
     float penw = sw0;
-    int ns = 0, nsub = 1;
-    S.subs[0] = SSub{0, 0, 0, 0};
+    int ns = 0, nsub = 0;
+    SSub cur{0, 0, 0, 0};  // the sub-stroke being built (stored when the next one starts)
+    P2 last = p2(0.0f, 0.0f);
     auto close = [&](int joined) {
         if (ns > 0) {
-            S.subs[nsub - 1].joined = joined;
-            S.subs[nsub - 1].done = 1;
+            cur.joined = joined;
+            cur.done = 1;
         }
     };
     auto add = [&](P2 q, float w, int op, int form, float t, int pn, int w0, int w1) {
         if (ns >= VCAP) return;  // the stroke keeps 65,535 points (stroker.rs:204-216)
-        const int done = S.subs[nsub - 1].done;
-        if (done) S.subs[nsub++] = SSub{ns, 0, 0, 0};
-        const bool coincident = ns > 0 && S.sp[ns - 1].x == q.x && S.sp[ns - 1].y == q.y;
+        const int done = cur.done;
+        if (done) {
+            S.subs[nsub++] = cur;
+            cur = SSub{ns, 0, 0, 0};
+        }
+        const bool coincident = ns > 0 && last.x == q.x && last.y == q.y;
         if (done || !coincident) {
             S.sp[ns++] = SPt{q.x, q.y, w, t, op, form, pn, w0, w1, 0};
-            S.subs[nsub - 1].n++;
+            last = q;
+            cur.n++;
         }
     };
     for (int i = 0; i < n; i++) {
@@ -806,67 +811,74 @@ __device__ int build_stroke_dev(const AParams& p, const ft_op* ops, int n, float
                 break;
         }
     }
+    S.subs[nsub++] = cur;
     *n_sp = ns;
-    // ---- outline (stroker.rs:239-416), filled as Line ops transformed again
+    // ---- outline (stroker.rs:239-416), filled as Line ops transformed again.  Node
+    // values travel with their ids: nothing written here is read back.
+    struct NV {
+        int id;
+        P2 v;
+    };
+    struct SV {
+        P2 p;
+        float w;
+    };
     int nn = 0, nv = 0, sub_start = 0;
     bool fresh = true;
-    auto P = [&](int k) { return p2(S.sp[k].x, S.sp[k].y); };
-    auto N = [&](int i) { return i < NODE_CAP ? p2(S.nd[i].x, S.nd[i].y) : p2(0.0f, 0.0f); };
+    auto SPv = [&](int k) {
+        const SPt q = S.sp[k];
+        return SV{p2(q.x, q.y), q.w};
+    };
     auto node = [&](int kind, int a, int b, int c, int d, P2 v) {
         if (nn < NODE_CAP) S.nd[nn] = SNd{kind, a, b, c, d, v.x, v.y, 0};
-        return nn++;
+        return NV{nn++, v};
     };
-    auto emit = [&](int nd) {
+    auto emit = [&](NV nd) {
         if (nv < VCAP) {
             if (fresh) sub_start = nv;
-            const P2 q = xform(m, N(nd));
+            const P2 q = xform(m, nd.v);
             vpos[nv] = make_float2(fx_range(q.x), fx_range(q.y));
             vsub[nv] = sub_start;
-            S.vnode[nv] = nd;
+            S.vnode[nv] = nd.id;
         }
         fresh = false;
         nv++;
     };
-    auto off = [&](int k0, int k1, int which) {
-        const P2 vr = ftk::pnormalize(ftk::pright(ftk::psub(P(k1), P(k0))));
-        const int ks = which ? k1 : k0;
-        return node(N_OFF, k0, k1, which, 0, ftk::padd(P(ks), ftk::pscale(vr, __fmul_rn(S.sp[ks].w, 0.5f))));
-    };
     const float tol_sq = p.tol_sq;
-    auto arc = [&](int k, int na0, int nb0) {
+    auto arc = [&](int k, SV c0, NV na0, NV nb0) {
         struct Fr {
-            int na, nb, dep;
+            NV na, nb;
+            int dep;
         };
         Fr st[FT_MAX_DEPTH + 3];
         int sp = 0;
         st[sp++] = Fr{na0, nb0, 0};
+        const float hw = __fmul_rn(c0.w, 0.5f);
         while (sp > 0) {
             const Fr f = st[--sp];
-            const P2 a = N(f.na), b = N(f.nb);
-            const P2 vr = ftk::pnormalize(ftk::pright(ftk::psub(b, a)));
-            const P2 c = ftk::padd(P(k), ftk::pscale(vr, __fmul_rn(S.sp[k].w, 0.5f)));
-            if (!pfinite(c) || pdist_sq(c, pmid(a, b)) <= tol_sq) {
+            const P2 vr = ftk::pnormalize(ftk::pright(ftk::psub(f.nb.v, f.na.v)));
+            const P2 c = ftk::padd(c0.p, ftk::pscale(vr, hw));
+            if (!pfinite(c) || pdist_sq(c, pmid(f.na.v, f.nb.v)) <= tol_sq) {
                 emit(f.nb);
             } else if (f.dep >= FT_MAX_DEPTH) {
                 *status = max(*status, (int)FT_ERR_DEPTH);
                 emit(f.nb);
             } else {
-                const int nc = node(N_ARC, k, f.na, f.nb, 0, c);
+                const NV nc = node(N_ARC, k, f.na.id, f.nb.id, 0, c);
                 st[sp++] = Fr{nc, f.nb, f.dep + 1};  // right half after the left
                 st[sp++] = Fr{f.na, nc, f.dep + 1};
             }
         }
     };
-    auto join = [&](int k, int a0, int a1, int b0, int b1) {
-        const P2 A0 = N(a0), A1 = N(a1), B0 = N(b0), B1 = N(b1);
+    auto join = [&](int k, SV pk, NV a0, NV a1, NV b0, NV b1) {
         if (p.join == FT_JOIN_MITER) {
             if (p.miter_limit > 0.0f) {
                 const float sm_min = __fdiv_rn(1.0f, p.miter_limit);
-                const float th = ftk::pangle_rel(ftk::psub(A1, A0), ftk::psub(B0, B1));
+                const float th = ftk::pangle_rel(ftk::psub(a1.v, a0.v), ftk::psub(b0.v, b1.v));
                 const float sm = fabsf(ft_sinf(__fdiv_rn(th, 2.0f)));
                 P2 xp;
-                if (sm >= sm_min && sm < 1.0f && ftk::pline_x(A0, A1, B0, B1, &xp)) {
-                    emit(node(N_MITER, a0, a1, b0, b1, xp));
+                if (sm >= sm_min && sm < 1.0f && ftk::pline_x(a0.v, a1.v, b0.v, b1.v, &xp)) {
+                    emit(node(N_MITER, a0.id, a1.id, b0.id, b1.id, xp));
                     return;
                 }
             }
@@ -876,12 +888,12 @@ __device__ int build_stroke_dev(const AParams& p, const ft_op* ops, int n, float
             emit(a1);
             emit(b0);
         } else {
-            const float th = ftk::pangle_rel(ftk::psub(A1, A0), ftk::psub(B0, B1));
+            const float th = ftk::pangle_rel(ftk::psub(a1.v, a0.v), ftk::psub(b0.v, b1.v));
             emit(a1);
             if (th <= 0.0f)
                 emit(b0);
             else
-                arc(k, a1, b0);
+                arc(k, pk, a1, b0);
         }
     };
     for (int si = 0; si < nsub && nn <= NODE_CAP && nv <= VCAP; si++) {
@@ -896,19 +908,26 @@ __device__ int build_stroke_dev(const AParams& p, const ft_op* ops, int n, float
             const bool fwd = side == 0;
             int v0 = fwd ? sb.start : nextv(sb.start, false);
             int v1 = nextv(v0, fwd);
+            SV q0 = SPv(v0), q1 = SPv(v1);
             bool have = false;
-            int x0 = 0, x1 = 0;
+            NV x0{0, p2(0.0f, 0.0f)}, x1 = x0;
             for (int k = 0; k < len; k++) {
-                const int o0 = off(v0, v1, 0), o1 = off(v0, v1, 1);
+                const int v2 = nextv(v1, fwd);
+                const SV q2 = SPv(v2);  // the next segment's end, loaded ahead
+                const P2 vr = ftk::pnormalize(ftk::pright(ftk::psub(q1.p, q0.p)));
+                const NV o0 = node(N_OFF, v0, v1, 0, 0, ftk::padd(q0.p, ftk::pscale(vr, __fmul_rn(q0.w, 0.5f))));
+                const NV o1 = node(N_OFF, v0, v1, 1, 0, ftk::padd(q1.p, ftk::pscale(vr, __fmul_rn(q1.w, 0.5f))));
                 if (have)
-                    join(v0, x0, x1, o0, o1);
+                    join(v0, q0, x0, x1, o0, o1);
                 else if (!sb.joined)
                     emit(o0);
                 have = true;
                 x0 = o0;
                 x1 = o1;
                 v0 = v1;
-                v1 = nextv(v1, fwd);
+                v1 = v2;
+                q0 = q1;
+                q1 = q2;
             }
             if (!sb.joined && have) emit(x1);
             if (fwd && sb.joined) fresh = true;  // Close between the two sides
@@ -920,95 +939,112 @@ __device__ int build_stroke_dev(const AParams& p, const ft_op* ops, int n, float
     return nv;
 }
 
-// Thread 0, backward: outline vertex gradients (vgrad, in fill space) -> nodes ->
-// stroke points -> op floats and widths.
-__device__ void stroke_backward_dev(const AParams& p, const ft_op* ops, float* gops, float* gwidth, int V, int nn,
-                                    int ns, const StrokeScr& S, const float2* vgrad) {
+// Backward of a stroke, all threads: outline vertex gradients (vgrad, fill space) ->
+// nodes -> stroke points -> op floats and widths.  Children are always older nodes:
+// arcs (reverse creation order, one thread: an arc may feed another), then miter
+// intersections and offset points in parallel, then stroke points.
+__device__ void stroke_backward_block(const AParams& p, const ft_op* ops, float* gops, float* gwidth, int V, int nn,
+                                      int ns, const StrokeScr& S, const float2* vgrad) {
+    const int tid = threadIdx.x;
     const float* m = p.xf;
-    for (int i = 0; i < nn; i++) S.ng[i] = make_float2(0.0f, 0.0f);
-    for (int k = 0; k < ns; k++) S.spg[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    for (int j = 0; j < V; j++) {
+    for (int i = tid; i < nn; i += ABLOCK) S.ng[i] = make_float2(0.0f, 0.0f);
+    for (int k = tid; k < ns; k += ABLOCK) S.spg[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    __syncthreads();
+    for (int j = tid; j < V; j += ABLOCK) {
         const int nd = S.vnode[j];
         const float2 g = fx_pass(xform(m, p2(S.nd[nd].x, S.nd[nd].y)), __ldcg(&vgrad[j]));
-        float2& t = S.ng[nd];
-        t.x += m[0] * g.x + m[3] * g.y;
-        t.y += m[1] * g.x + m[4] * g.y;
+        atomicAdd(&S.ng[nd].x, m[0] * g.x + m[3] * g.y);
+        atomicAdd(&S.ng[nd].y, m[1] * g.x + m[4] * g.y);
     }
-    for (int i = nn - 1; i >= 0; i--) {
-        const SNd nd = S.nd[i];
-        const float2 g = S.ng[i];
-        if (g.x == 0.0f && g.y == 0.0f) continue;
-        if (nd.kind == N_OFF || nd.kind == N_ARC) {
-            float fx, fy, tx, ty;
-            if (nd.kind == N_OFF) {
-                fx = S.sp[nd.a].x, fy = S.sp[nd.a].y, tx = S.sp[nd.b].x, ty = S.sp[nd.b].y;
-            } else {
-                fx = S.nd[nd.b].x, fy = S.nd[nd.b].y, tx = S.nd[nd.c].x, ty = S.nd[nd.c].y;
-            }
-            const float ux = ty - fy, uy = -(tx - fx);
-            const float len = sqrtf(ux * ux + uy * uy);
-            const float vx = ux / len, vy = uy / len;
-            const int ks = nd.kind == N_OFF ? (nd.c ? nd.b : nd.a) : nd.a;
-            const float w = S.sp[ks].w;
-            float4& gs = S.spg[ks];
-            gs.x += g.x;
-            gs.y += g.y;
-            gs.z += 0.5f * (vx * g.x + vy * g.y);
-            const float gvx = g.x * w * 0.5f, gvy = g.y * w * 0.5f;
-            const float dv = vx * gvx + vy * gvy;
-            const float gux = (gvx - vx * dv) / len, guy = (gvy - vy * dv) / len;
-            const float gdx = -guy, gdy = gux;  // u = (d.y, -d.x)
-            if (nd.kind == N_OFF) {
-                S.spg[nd.b].x += gdx;
-                S.spg[nd.b].y += gdy;
-                S.spg[nd.a].x -= gdx;
-                S.spg[nd.a].y -= gdy;
-            } else {
-                S.ng[nd.c].x += gdx;
-                S.ng[nd.c].y += gdy;
-                S.ng[nd.b].x -= gdx;
-                S.ng[nd.b].y -= gdy;
-            }
-        } else {
-            // intersection of lines a0-a1 and b0-b1 in coordinates relative to a1 (well
-            // conditioned in float): x = a1 + (B / D) * (a1 - a0), u = a0 - a1,
-            // v3 = b0 - a1, v4 = b1 - a1, D = u x (v3 - v4), B = v3 x v4
-            const float ax = S.nd[nd.b].x, ay = S.nd[nd.b].y;
-            const float ux = S.nd[nd.a].x - ax, uy = S.nd[nd.a].y - ay;
-            const float v3x = S.nd[nd.c].x - ax, v3y = S.nd[nd.c].y - ay;
-            const float v4x = S.nd[nd.d].x - ax, v4y = S.nd[nd.d].y - ay;
-            const float den = ux * (v3y - v4y) - uy * (v3x - v4x);
-            const float bb = v3x * v4y - v3y * v4x;
-            const float q = bb / den;
-            float gux = -q * g.x, guy = -q * g.y;
-            const float gq = -(ux * g.x + uy * g.y);
-            const float gb = gq / den, gden = -gq * q / den;
-            float g3x = gb * v4y, g3y = -gb * v4x, g4x = -gb * v3y, g4y = gb * v3x;
-            gux += gden * (v3y - v4y);
-            guy -= gden * (v3x - v4x);
-            g3y += gden * ux;
-            g4y -= gden * ux;
-            g3x -= gden * uy;
-            g4x += gden * uy;
-            S.ng[nd.a].x += gux;
-            S.ng[nd.a].y += guy;
-            S.ng[nd.c].x += g3x;
-            S.ng[nd.c].y += g3y;
-            S.ng[nd.d].x += g4x;
-            S.ng[nd.d].y += g4y;
-            S.ng[nd.b].x += g.x - gux - g3x - g4x;
-            S.ng[nd.b].y += g.y - guy - g3y - g4y;
+    __syncthreads();
+    // offset of stroke point ks along normalize(right(to - from)) * w / 2: gradients of
+    // ks's position and width and of the direction's two ends
+    auto offset_back = [&](float2 g, float fx, float fy, float tx, float ty, int ks, float2* gfrom, float2* gto) {
+        const float ux = ty - fy, uy = -(tx - fx);
+        const float len = sqrtf(ux * ux + uy * uy);
+        const float vx = ux / len, vy = uy / len;
+        const float w = S.sp[ks].w;
+        atomicAdd(&S.spg[ks].x, g.x);
+        atomicAdd(&S.spg[ks].y, g.y);
+        atomicAdd(&S.spg[ks].z, 0.5f * (vx * g.x + vy * g.y));
+        const float gvx = g.x * w * 0.5f, gvy = g.y * w * 0.5f;
+        const float dv = vx * gvx + vy * gvy;
+        const float gux = (gvx - vx * dv) / len, guy = (gvy - vy * dv) / len;
+        *gto = make_float2(-guy, gux);  // u = (d.y, -d.x), d = to - from
+        *gfrom = make_float2(guy, -gux);
+    };
+    if (tid == 0) {
+        for (int i = nn - 1; i >= 0; i--) {
+            const SNd nd = S.nd[i];
+            if (nd.kind != N_ARC) continue;
+            const float2 g = __ldcg(&S.ng[i]);
+            if (g.x == 0.0f && g.y == 0.0f) continue;
+            float2 gf, gt;
+            offset_back(g, S.nd[nd.b].x, S.nd[nd.b].y, S.nd[nd.c].x, S.nd[nd.c].y, nd.a, &gf, &gt);
+            atomicAdd(&S.ng[nd.b].x, gf.x);
+            atomicAdd(&S.ng[nd.b].y, gf.y);
+            atomicAdd(&S.ng[nd.c].x, gt.x);
+            atomicAdd(&S.ng[nd.c].y, gt.y);
         }
     }
+    __syncthreads();
+    for (int i = tid; i < nn; i += ABLOCK) {
+        const SNd nd = S.nd[i];
+        if (nd.kind != N_MITER) continue;
+        const float2 g = __ldcg(&S.ng[i]);
+        if (g.x == 0.0f && g.y == 0.0f) continue;
+        // intersection of lines a0-a1 and b0-b1 in coordinates relative to a1 (well
+        // conditioned in float): x = a1 + (B / D) * (a1 - a0), u = a0 - a1,
+        // v3 = b0 - a1, v4 = b1 - a1, D = u x (v3 - v4), B = v3 x v4
+        const float ax = S.nd[nd.b].x, ay = S.nd[nd.b].y;
+        const float ux = S.nd[nd.a].x - ax, uy = S.nd[nd.a].y - ay;
+        const float v3x = S.nd[nd.c].x - ax, v3y = S.nd[nd.c].y - ay;
+        const float v4x = S.nd[nd.d].x - ax, v4y = S.nd[nd.d].y - ay;
+        const float den = ux * (v3y - v4y) - uy * (v3x - v4x);
+        const float bb = v3x * v4y - v3y * v4x;
+        const float q = bb / den;
+        float gux = -q * g.x, guy = -q * g.y;
+        const float gq = -(ux * g.x + uy * g.y);
+        const float gb = gq / den, gden = -gq * q / den;
+        float g3x = gb * v4y, g3y = -gb * v4x, g4x = -gb * v3y, g4y = gb * v3x;
+        gux += gden * (v3y - v4y);
+        guy -= gden * (v3x - v4x);
+        g3y += gden * ux;
+        g4y -= gden * ux;
+        g3x -= gden * uy;
+        g4x += gden * uy;
+        atomicAdd(&S.ng[nd.a].x, gux);
+        atomicAdd(&S.ng[nd.a].y, guy);
+        atomicAdd(&S.ng[nd.c].x, g3x);
+        atomicAdd(&S.ng[nd.c].y, g3y);
+        atomicAdd(&S.ng[nd.d].x, g4x);
+        atomicAdd(&S.ng[nd.d].y, g4y);
+        atomicAdd(&S.ng[nd.b].x, g.x - gux - g3x - g4x);
+        atomicAdd(&S.ng[nd.b].y, g.y - guy - g3y - g4y);
+    }
+    __syncthreads();
+    for (int i = tid; i < nn; i += ABLOCK) {
+        const SNd nd = S.nd[i];
+        if (nd.kind != N_OFF) continue;
+        const float2 g = __ldcg(&S.ng[i]);
+        if (g.x == 0.0f && g.y == 0.0f) continue;
+        float2 gf, gt;
+        offset_back(g, S.sp[nd.a].x, S.sp[nd.a].y, S.sp[nd.b].x, S.sp[nd.b].y, nd.c ? nd.b : nd.a, &gf, &gt);
+        atomicAdd(&S.spg[nd.a].x, gf.x);
+        atomicAdd(&S.spg[nd.a].y, gf.y);
+        atomicAdd(&S.spg[nd.b].x, gt.x);
+        atomicAdd(&S.spg[nd.b].y, gt.y);
+    }
+    __syncthreads();
     auto gw = [&](int src, float v) {
         if (src < 0)
             atomicAdd(gwidth, v);
         else
             atomicAdd(gops + (size_t)src * 6, v);
     };
-    for (int k = 0; k < ns; k++) {
+    for (int k = tid; k < ns; k += ABLOCK) {
         const SPt q = S.sp[k];
-        const float4 g = S.spg[k];
+        const float4 g = __ldcg(&S.spg[k]);
         const float gx = m[0] * g.x + m[3] * g.y, gy = m[1] * g.x + m[4] * g.y;
         const int kind = load_op(ops, q.op).kind;
         auto add = [&](int j, int slot, float wgt) {
@@ -1134,9 +1170,8 @@ __global__ void __launch_bounds__(ABLOCK) k_adjoint(AParams p) {
         if (BWD && !cap) {
             if (p.stroke) {
                 __syncthreads();
-                if (tid == 0)
-                    stroke_backward_dev(p, ops, p.grad_ops + (size_t)d.op_begin * 6, p.grad_width + path, V,
-                                        s_counts[1], s_counts[2], S, vgrad);
+                stroke_backward_block(p, ops, p.grad_ops + (size_t)d.op_begin * 6, p.grad_width + path, V,
+                                      s_counts[1], s_counts[2], S, vgrad);
             } else {
                 path_walk<WALK_GRAD>(p, sm, ops, (int)d.n_ops, vpos, vsub, vgrad, false,
                                      p.grad_ops + (size_t)d.op_begin * 6);
