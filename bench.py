@@ -131,6 +131,26 @@ def extra_scene(ctx, stream, dev, cpu=True):
     ctx.set_join(_abi.JOIN_MITER, 4.0)
     # composite bytes: every Rgba8p pixel from the top row down is read and written
     out["rgba8p_composite_GBps"] = (w * h * 8) / (out["nonzero_rgba8p_ms"] * 1e-3) / 1e9
+    # pix's Rgba8p -> SRgba8 step of footile's examples, on the device (HBM-bound):
+    # the 4096x4096 raster, and an 8192x8192 one whose 512 MB of traffic is far above L2
+    s_d = torch.empty_like(r_d)
+    peak, _ = measured_peak_hbm()
+
+    def kernel_ms(a, b, reps=10):  # device time of the conversion kernel (library events)
+        ctx.convert(a, b)
+        t = []
+        for _ in range(reps):
+            ctx.convert(a, b)
+            t.append(ctx.last_ms())
+        return float(np.median(t))
+    out["srgba8_convert_4096_ms"] = kernel_ms(r_d, s_d)
+    big = torch.randint(0, 256, (8192, 8192, 4), dtype=torch.uint8, device=dev)
+    big_out = torch.empty_like(big)
+    ms_conv = kernel_ms(big, big_out)
+    out["srgba8_convert_8192_ms"] = ms_conv
+    out["srgba8_convert_GBps"] = (8192 * 8192 * 8) / (ms_conv * 1e-3) / 1e9
+    out["srgba8_convert_frac_of_measured_hbm"] = out["srgba8_convert_GBps"] / peak
+    del big, big_out
     if cpu:
         import oracle
         m = np.zeros((h, w), np.uint8)

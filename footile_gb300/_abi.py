@@ -44,6 +44,10 @@ BYTES_PER_PIXEL = {MATTE8: 1, RGBA8P: 4}
 HOST = 0
 DEVICE = 1
 
+# output formats of ft_convert (pix SRgba8 / SGray8)
+SRGBA8 = 2
+SGRAY8 = 3
+
 # struct ft_op (32 bytes)
 OP_DTYPE = np.dtype([("kind", "<i4"), ("v", "<f4", (6,)), ("reserved", "<i4")], align=True)
 assert OP_DTYPE.itemsize == 32

@@ -14,7 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libfootile_gpu.so")
 
-SOURCES = ["ft_kernels.cu", "ft_adjoint.cu", "ft_capi.cu"]
+SOURCES = ["ft_kernels.cu", "ft_adjoint.cu", "ft_convert.cu", "ft_capi.cu"]
 HEADERS = ["ft_device.cuh", "ft_kernels.cuh", "ft_adjoint.cuh"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Bit-exact float stages: no FMA contraction, IEEE division and square root.

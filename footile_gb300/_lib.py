@@ -61,6 +61,7 @@ def load(auto_build=True):
             "ft_adjoint_status": ([P, P, P, u32], ctypes.c_int),
             "ft_adjoint_destroy": ([P], None),
             "ft_set_tuning": ([P, P], ctypes.c_int),
+            "ft_convert": ([P, i32, P, u32, i32, P, u32, u32, u32, i32], ctypes.c_int),
             "ft_get_tuning": ([P, P], ctypes.c_int),
             "ft_autotune_batch": ([P, i32, i32, P, u32, P, u32, i32, P, u64, ctypes.c_char_p, P,
                                    ctypes.POINTER(f32)], ctypes.c_int),
@@ -81,7 +82,8 @@ def exported_symbols():
         "ft_batch_status", "ft_sync", "ft_last_error", "ft_last_timings", "ft_launch_count",
         "ft_batch_create", "ft_batch_launch", "ft_batch_launch_status", "ft_batch_destroy",
         "ft_composite_batch", "ft_fill_noalloc", "ft_adjoint_forward", "ft_adjoint_backward", "ft_adjoint_status",
-        "ft_adjoint_destroy", "ft_set_tuning", "ft_get_tuning", "ft_autotune_batch")]
+        "ft_adjoint_destroy", "ft_set_tuning", "ft_get_tuning", "ft_autotune_batch",
+        "ft_convert")]
 
 
 class Tuning(ctypes.Structure):
@@ -194,6 +196,26 @@ class Context:
                                             ctypes.c_void_p(rasters_dev.data_ptr()), nbytes, cp, ctypes.byref(t),
                                             ctypes.byref(ms)))
         return t.as_dict(), ms.value
+
+    def convert(self, src, dst):
+        """Rgba8p (h, w, 4) -> SRgba8, or Matte8 (h, w) -> SGray8 (`ft_convert`): numpy
+        arrays (host) or CUDA tensors (device); `dst` may be `src`.  Returns `dst`."""
+        dev = hasattr(src, "data_ptr")
+        rgba = (src.dim() if dev else src.ndim) == 3
+        h, w = int(src.shape[0]), int(src.shape[1])
+        if dev:
+            wait = self.torch_fence()
+            sp, ss = src.data_ptr(), int(src.stride(0)) * src.element_size()
+            dp, ds = dst.data_ptr(), int(dst.stride(0)) * dst.element_size()
+        else:
+            sp, ss = src.ctypes.data, int(src.strides[0])
+            dp, ds = dst.ctypes.data, int(dst.strides[0])
+        self.check(self.L.ft_convert(self.h, _abi.RGBA8P if rgba else _abi.MATTE8, ctypes.c_void_p(sp), ss,
+                                     _abi.SRGBA8 if rgba else _abi.SGRAY8, ctypes.c_void_p(dp), ds, w, h,
+                                     _abi.DEVICE if dev else _abi.HOST))
+        if dev and wait:
+            self.sync()
+        return dst
 
     def batch_status(self, n):
         import numpy as np

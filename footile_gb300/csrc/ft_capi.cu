@@ -54,6 +54,7 @@ struct ft_ctx {
     // device buffers
     DevBuf ops, paths, items, items_w, overflow, status, sw_out, rasters, queue, scratch, sw_chain;
     DevBuf pool, pool_used, bandoff, crec;  // ordered composite
+    DevBuf srgb_lut, conv_src, conv_dst;    // ft_convert
     std::vector<ftk::WorkItem> h_items, h_items_w;
     uint32_t last_n_paths = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -590,7 +591,8 @@ FT_API void ft_ctx_destroy(ft_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     DevBuf* bufs[] = {&c->ops,     &c->paths,   &c->items,   &c->items_w, &c->overflow,
                       &c->status,  &c->sw_out,  &c->rasters, &c->queue,   &c->scratch,
-                      &c->sw_chain, &c->pool,   &c->pool_used, &c->bandoff, &c->crec};
+                      &c->sw_chain, &c->pool,   &c->pool_used, &c->bandoff, &c->crec,
+                      &c->srgb_lut, &c->conv_src, &c->conv_dst};
     for (DevBuf* b : bufs) b->release();
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
@@ -829,6 +831,25 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
         return FT_OK;
     }
     return fail(c, FT_ERR_NOMEM, "edge pool did not converge");
+}
+
+// ---------------------------------------------------------------- conversion
+namespace ftc {
+cudaError_t launch_convert(int src_fmt, const uint8_t* src, uint32_t src_stride, uint8_t* dst, uint32_t dst_stride,
+                           uint32_t w, uint32_t h, const uint8_t* lut, int grid, cudaStream_t s);
+int convert_blocks_per_sm();
+}
+
+// lut[a * 256 + c]: the straight channel c / a (clamped to 1; 0 when a = 0) through
+// the sRGB transfer function (IEC 61966-2-1), rounded to the nearest byte.
+static void srgb_table(std::vector<uint8_t>& lut) {
+    lut.assign(256 * 256, 0);
+    for (int a = 1; a < 256; a++)
+        for (int ch = 0; ch < 256; ch++) {
+            const double v = std::min(1.0, (double)ch / (double)a);
+            const double e = v <= 0.0031308 ? 12.92 * v : 1.055 * std::pow(v, 1.0 / 2.4) - 0.055;
+            lut[a * 256 + ch] = (uint8_t)std::min(255.0, std::floor(e * 255.0 + 0.5));
+        }
 }
 
 // ------------------------------------------------------------------ autotuner
@@ -1080,6 +1101,51 @@ FT_API void ft_adjoint_destroy(ft_adjoint* a) {
     DevBuf* bufs[] = {&a->ops, &a->paths, &a->area, &a->status, &a->scratch, &a->cov, &a->gcov, &a->gops, &a->gwidth};
     for (DevBuf* b : bufs) b->release();
     delete a;
+}
+
+FT_API int ft_convert(ft_ctx* c, int32_t src_fmt, const uint8_t* src, uint32_t src_stride, int32_t dst_fmt,
+                      uint8_t* dst, uint32_t dst_stride, uint32_t w, uint32_t h, int32_t where) {
+    if (!c) return FT_ERR_ARG;
+    if (!((src_fmt == FT_RGBA8P && dst_fmt == FT_SRGBA8) || (src_fmt == FT_MATTE8 && dst_fmt == FT_SGRAY8)) ||
+        (where != FT_HOST && where != FT_DEVICE))
+        return fail(c, FT_ERR_ARG, "conversions: Rgba8p -> SRgba8, Matte8 -> SGray8");
+    const uint64_t row = (uint64_t)w * (src_fmt == FT_RGBA8P ? 4 : 1);
+    if (w == 0 || h == 0) return FT_OK;
+    if (!src || !dst || src_stride < row || dst_stride < row) return fail(c, FT_ERR_ARG, "bad buffer or stride");
+    FT_CU(cudaSetDevice(c->device), "set device");
+    if (!c->srgb_lut.p) {
+        std::vector<uint8_t> lut;
+        srgb_table(lut);
+        FT_CU(c->srgb_lut.ensure(lut.size()), "alloc sRGB table");
+        FT_CU(cudaMemcpyAsync(c->srgb_lut.p, lut.data(), lut.size(), cudaMemcpyHostToDevice, c->stream),
+              "upload sRGB table");
+        FT_CU(cudaStreamSynchronize(c->stream), "synchronize");  // the host table goes out of scope
+    }
+    const uint64_t src_bytes = (uint64_t)src_stride * (h - 1) + row, dst_bytes = (uint64_t)dst_stride * (h - 1) + row;
+    const uint8_t* s_d = src;
+    uint8_t* d_d = dst;
+    if (where == FT_HOST) {
+        FT_CU(c->conv_src.ensure(src_bytes), "alloc conversion source");
+        FT_CU(c->conv_dst.ensure(dst_bytes), "alloc conversion output");
+        FT_CU(cudaMemcpyAsync(c->conv_src.p, src, src_bytes, cudaMemcpyHostToDevice, c->stream), "upload raster");
+        s_d = static_cast<const uint8_t*>(c->conv_src.p);
+        d_d = static_cast<uint8_t*>(c->conv_dst.p);
+    }
+    const uint64_t work = (row / 16 + row % 16) * h;
+    const int grid = (int)std::max<uint64_t>(
+        1, std::min<uint64_t>((work + 255) / 256, (uint64_t)c->sm_count * ftc::convert_blocks_per_sm()));
+    FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
+    FT_CU(ftc::launch_convert(src_fmt, s_d, src_stride, d_d, dst_stride, w, h,
+                              static_cast<const uint8_t*>(c->srgb_lut.p), grid, c->stream),
+          "launch conversion");
+    FT_CU(cudaEventRecord(c->ev1, c->stream), "event");
+    c->timed = true;
+    c->launches++;
+    if (where == FT_HOST) {
+        FT_CU(cudaMemcpyAsync(dst, d_d, dst_bytes, cudaMemcpyDeviceToHost, c->stream), "download raster");
+        FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
+    }
+    return FT_OK;
 }
 
 FT_API int ft_autotune_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* ops, uint32_t n_ops_total,

@@ -76,6 +76,8 @@ enum {
     FT_RGBA8P = 1   /* pix Rgba8p: 4 bytes / pixel premultiplied; SrcOver (src/fig.rs:637-643) */
 };
 enum { FT_HOST = 0, FT_DEVICE = 1 };  /* where the ops / raster pointers live */
+/* Output formats of ft_convert (pix SRgba8 / SGray8: straight alpha, sRGB gamma). */
+enum { FT_SRGBA8 = 2, FT_SGRAY8 = 3 };
 
 /* One path of a batch.  Each path is an independent Plotter call onto its own
  * raster (or region of one).  40 bytes. */
@@ -265,6 +267,17 @@ FT_API int ft_adjoint_backward(ft_ctx* ctx, ft_adjoint* saved, const float* grad
                                float* grad_width, int32_t where);
 FT_API int ft_adjoint_status(ft_ctx* ctx, ft_adjoint* saved, int32_t* status, uint32_t n);
 FT_API void ft_adjoint_destroy(ft_adjoint* saved);
+
+/* Pixel conversion after plotting, as footile's examples do with pix
+ * (`Raster::<SRgba8>::with_raster`, examples/fishy.rs:33; `Raster::<SGray8>`,
+ * examples/drop.rs:22): FT_RGBA8P -> FT_SRGBA8 (straight alpha: channel / alpha, then
+ * the sRGB transfer function of IEC 61966-2-1, correctly rounded; alpha kept; alpha 0
+ * gives 0) and FT_MATTE8 -> FT_SGRAY8 (the mask byte as linear gray, sRGB-encoded).
+ * `src` and `dst` may be the same buffer when the strides are equal.  With FT_HOST the
+ * call copies in and out; with FT_DEVICE it is asynchronous on the context stream. */
+FT_API int ft_convert(ft_ctx* ctx, int32_t src_fmt, const uint8_t* src, uint32_t src_stride,
+                      int32_t dst_fmt, uint8_t* dst, uint32_t dst_stride, uint32_t w, uint32_t h,
+                      int32_t where);
 
 /* Per-path status codes of the last batch (synchronises the context stream). */
 FT_API int ft_batch_status(ft_ctx* ctx, int32_t* status, uint32_t n);

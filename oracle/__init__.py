@@ -299,3 +299,30 @@ def adj_stroke_outline(ops, s_width=1.0, tolerance=0.3, transform=_abi.IDENTITY,
         if n <= cap:
             return out[:n]
         cap = n
+
+
+# ------------------------------------------------------------- pixel conversion
+def srgb_table():
+    """lut[a, c]: straight channel c / a (clamped to 1, 0 at a = 0) through the sRGB
+    transfer function (IEC 61966-2-1), rounded to the nearest byte (pix's
+    Rgba8p -> SRgba8 step, restated: the pix crate is not vendored)."""
+    a = np.arange(256, dtype=np.float64)[:, None]
+    c = np.arange(256, dtype=np.float64)[None, :]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        v = np.minimum(1.0, np.where(a > 0, c / np.maximum(a, 1), 0.0))
+    e = np.where(v <= 0.0031308, 12.92 * v, 1.055 * np.power(v, 1.0 / 2.4) - 0.055)
+    lut = np.minimum(255.0, np.floor(e * 255.0 + 0.5)).astype(np.uint8)
+    lut[0, :] = 0
+    return lut
+
+
+def convert(src):
+    """Rgba8p (h, w, 4) -> SRgba8, or Matte8 (h, w) -> SGray8."""
+    lut = srgb_table()
+    if src.ndim == 3:
+        out = src.copy()
+        a = src[..., 3]
+        for ch in range(3):
+            out[..., ch] = lut[a, src[..., ch]]
+        return out
+    return lut[255, src]
