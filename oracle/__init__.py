@@ -2,7 +2,7 @@
 
 The oracle is a sequential C++ restatement of footile's fill/stroke path.  Only
 tests/, __graft_entry__.smoke() and bench.py (cpu_baseline leg and the
-`--impl reference` arm) use it, as the checker / CPU baseline.  The shipped
+`--impl reference` arm) use it, as the test oracle and CPU baseline.  The shipped
 library (footile_gb300) never imports it.
 """
 import ctypes

@@ -1,8 +1,8 @@
-// footile_oracle.cpp — TEST INFRASTRUCTURE ONLY (the oracle / checker).
+// footile_oracle.cpp — TEST INFRASTRUCTURE ONLY (the test oracle).
 //
 // A sequential CPU restatement of footile's fill/stroke path.  Only tests/,
 // __graft_entry__.smoke() and bench.py's cpu_baseline / reference arm load it, as
-// the checker the CUDA path is compared against.  The shipped library never calls
+// the oracle the CUDA path is compared against.  The shipped library never calls
 // it, and nothing in it runs on the GPU.
 //
 // It follows the reference structure line by line (file:line of footile 0.7):
