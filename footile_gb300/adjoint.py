@@ -141,3 +141,62 @@ def make_coverage_fn():
             return g, None, None, None, None, None
 
     return CoverageFn
+
+
+# ------------------------------------------------------- ordered SrcOver adjoint
+def srcover_forward(ctx, cov, n_layers, plane, clr, out, init=None):
+    """C_N of the ordered SrcOver of `n_layers` coverage planes (`ft_srcover_forward`).
+    CUDA tensors: cov (n_layers * plane floats), clr (n_layers x 4 premultiplied
+    float), out / init (n_px x 4 float).  Returns `out`."""
+    wait = ctx.torch_fence()
+    ctx.check(ctx.L.ft_srcover_forward(ctx.h, _ptr(cov), n_layers, plane, _ptr(clr), _ptr(init), _ptr(out),
+                                       out.shape[0]))
+    if wait:
+        ctx.sync()
+    return out
+
+
+def srcover_backward(ctx, cov, n_layers, plane, clr, grad_out, grad_cov, init=None, grad_init=None):
+    """dLoss/dcov of every layer (and dLoss/dC_0) from dLoss/dC_N (`ft_srcover_backward`)."""
+    wait = ctx.torch_fence()
+    ctx.check(ctx.L.ft_srcover_backward(ctx.h, _ptr(cov), n_layers, plane, _ptr(clr), _ptr(init), _ptr(grad_out),
+                                        _ptr(grad_cov), _ptr(grad_init), grad_out.shape[0]))
+    if wait:
+        ctx.sync()
+    return grad_cov
+
+
+def stroke_composite_grads(ctx, ops_dev, paths, clr_dev, width, height, target_dev, adj=None):
+    """Forward and backward of the differentiable ordered composite of strokes on one
+    canvas: coverage of every stroke over the canvas (`ft_adjoint_forward`, stroke = 1),
+    SrcOver in order, loss sum((C_N - target)^2), then the gradients of the op floats
+    (PenWidth ops in column 0) and of the starting pen widths.  `paths` describe one
+    width x height f32 plane per stroke, back to back (pack_coverage).  Returns
+    (loss, C_N, grad_ops, grad_width, timings in ms)."""
+    import torch
+    n = len(paths)
+    plane = width * height
+    dev = ops_dev.device
+    adj = adj or Adjoint(ctx)
+    cov = torch.empty(n * plane, dtype=torch.float32, device=dev)
+    out = torch.empty((plane, 4), dtype=torch.float32, device=dev)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+    stream = torch.cuda.current_stream(dev)
+    ev[0].record(stream)
+    adj.forward(0, ops_dev, paths, cov, stroke=True)
+    ev[1].record(stream)
+    srcover_forward(ctx, cov, n, plane, clr_dev, out)
+    ev[2].record(stream)
+    g_out = 2.0 * (out - target_dev)
+    loss = ((out - target_dev) ** 2).sum()
+    g_cov = torch.empty_like(cov)
+    ev[3].record(stream)
+    srcover_backward(ctx, cov, n, plane, clr_dev, g_out, g_cov)
+    g_ops = torch.empty((ops_dev.numel() * ops_dev.element_size() // 32, 6), dtype=torch.float32, device=dev)
+    g_w = torch.empty(n, dtype=torch.float32, device=dev)
+    adj.backward(g_cov, g_ops, g_w)
+    ev[4].record(stream)
+    torch.cuda.synchronize()
+    ms = {"coverage_fwd_ms": ev[0].elapsed_time(ev[1]), "srcover_fwd_ms": ev[1].elapsed_time(ev[2]),
+          "bwd_ms": ev[3].elapsed_time(ev[4])}
+    return loss, out, g_ops, g_w, ms

@@ -988,39 +988,57 @@ __device__ void stroke_backward_block(const AParams& p, const ft_op* ops, float*
         }
     }
     __syncthreads();
+    // Miter intersections.  Their four offset points are recomputed from the stroke
+    // points in double: between very short segments the float offsets' rounding is a
+    // large part of the offset lines' directions, and the intersection's Jacobian
+    // amplifies it.
+    auto off64 = [&](int id, double& x, double& y) {
+        const SNd o = S.nd[id];  // an offset node: stroke points a -> b
+        const double fx = S.sp[o.a].x, fy = S.sp[o.a].y, tx = S.sp[o.b].x, ty = S.sp[o.b].y;
+        const double ux = ty - fy, uy = -(tx - fx), len = sqrt(ux * ux + uy * uy);
+        const int ks = o.c ? o.b : o.a;
+        const double hw = 0.5 * (double)S.sp[ks].w;
+        x = (double)S.sp[ks].x + ux / len * hw;
+        y = (double)S.sp[ks].y + uy / len * hw;
+    };
     for (int i = tid; i < nn; i += ABLOCK) {
         const SNd nd = S.nd[i];
         if (nd.kind != N_MITER) continue;
-        const float2 g = __ldcg(&S.ng[i]);
-        if (g.x == 0.0f && g.y == 0.0f) continue;
-        // intersection of lines a0-a1 and b0-b1 in coordinates relative to a1 (well
-        // conditioned in float): x = a1 + (B / D) * (a1 - a0), u = a0 - a1,
-        // v3 = b0 - a1, v4 = b1 - a1, D = u x (v3 - v4), B = v3 x v4
-        const float ax = S.nd[nd.b].x, ay = S.nd[nd.b].y;
-        const float ux = S.nd[nd.a].x - ax, uy = S.nd[nd.a].y - ay;
-        const float v3x = S.nd[nd.c].x - ax, v3y = S.nd[nd.c].y - ay;
-        const float v4x = S.nd[nd.d].x - ax, v4y = S.nd[nd.d].y - ay;
-        const float den = ux * (v3y - v4y) - uy * (v3x - v4x);
-        const float bb = v3x * v4y - v3y * v4x;
-        const float q = bb / den;
-        float gux = -q * g.x, guy = -q * g.y;
-        const float gq = -(ux * g.x + uy * g.y);
-        const float gb = gq / den, gden = -gq * q / den;
-        float g3x = gb * v4y, g3y = -gb * v4x, g4x = -gb * v3y, g4y = gb * v3x;
+        const float2 gf = __ldcg(&S.ng[i]);
+        if (gf.x == 0.0f && gf.y == 0.0f) continue;
+        // intersection of lines a0-a1 and b0-b1 in coordinates relative to a1:
+        // x = a1 + (B / D) * (a1 - a0), u = a0 - a1, v3 = b0 - a1, v4 = b1 - a1,
+        // D = u x (v3 - v4), B = v3 x v4
+        double a0x, a0y, ax, ay, b0x, b0y, b1x, b1y;
+        off64(nd.a, a0x, a0y);
+        off64(nd.b, ax, ay);
+        off64(nd.c, b0x, b0y);
+        off64(nd.d, b1x, b1y);
+        const double gx = gf.x, gy = gf.y;
+        const double ux = a0x - ax, uy = a0y - ay;
+        const double v3x = b0x - ax, v3y = b0y - ay;
+        const double v4x = b1x - ax, v4y = b1y - ay;
+        const double den = ux * (v3y - v4y) - uy * (v3x - v4x);
+        const double bb = v3x * v4y - v3y * v4x;
+        const double q = bb / den;
+        double gux = -q * gx, guy = -q * gy;
+        const double gq = -(ux * gx + uy * gy);
+        const double gb = gq / den, gden = -gq * q / den;
+        double g3x = gb * v4y, g3y = -gb * v4x, g4x = -gb * v3y, g4y = gb * v3x;
         gux += gden * (v3y - v4y);
         guy -= gden * (v3x - v4x);
         g3y += gden * ux;
         g4y -= gden * ux;
         g3x -= gden * uy;
         g4x += gden * uy;
-        atomicAdd(&S.ng[nd.a].x, gux);
-        atomicAdd(&S.ng[nd.a].y, guy);
-        atomicAdd(&S.ng[nd.c].x, g3x);
-        atomicAdd(&S.ng[nd.c].y, g3y);
-        atomicAdd(&S.ng[nd.d].x, g4x);
-        atomicAdd(&S.ng[nd.d].y, g4y);
-        atomicAdd(&S.ng[nd.b].x, g.x - gux - g3x - g4x);
-        atomicAdd(&S.ng[nd.b].y, g.y - guy - g3y - g4y);
+        atomicAdd(&S.ng[nd.a].x, (float)gux);
+        atomicAdd(&S.ng[nd.a].y, (float)guy);
+        atomicAdd(&S.ng[nd.c].x, (float)g3x);
+        atomicAdd(&S.ng[nd.c].y, (float)g3y);
+        atomicAdd(&S.ng[nd.d].x, (float)g4x);
+        atomicAdd(&S.ng[nd.d].y, (float)g4y);
+        atomicAdd(&S.ng[nd.b].x, (float)(gx - gux - g3x - g4x));
+        atomicAdd(&S.ng[nd.b].y, (float)(gy - guy - g3y - g4y));
     }
     __syncthreads();
     for (int i = tid; i < nn; i += ABLOCK) {

@@ -838,6 +838,9 @@ namespace ftc {
 cudaError_t launch_convert(int src_fmt, const uint8_t* src, uint32_t src_stride, uint8_t* dst, uint32_t dst_stride,
                            uint32_t w, uint32_t h, const uint8_t* lut, int grid, cudaStream_t s);
 int convert_blocks_per_sm();
+cudaError_t launch_srcover(bool backward, const float* cov, uint32_t n_layers, uint64_t plane, const float4* clr,
+                           const float4* init, float4* out, const float4* grad_out, float* grad_cov,
+                           float4* grad_init, uint32_t n_px, int grid, cudaStream_t s);
 }
 
 // lut[a * 256 + c]: the straight channel c / a (clamped to 1; 0 when a = 0) through
@@ -1146,6 +1149,44 @@ FT_API int ft_convert(ft_ctx* c, int32_t src_fmt, const uint8_t* src, uint32_t s
         FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
     }
     return FT_OK;
+}
+
+static int srcover_call(ft_ctx* c, bool backward, const float* cov, uint32_t n_layers, uint64_t plane,
+                        const float* clr, const float* init, float* out, const float* grad_out, float* grad_cov,
+                        float* grad_init, uint32_t n_px) {
+    if (!c) return FT_ERR_ARG;
+    if (n_px == 0) return FT_OK;
+    if ((n_layers && (!cov || !clr)) || (!backward && !out) || (backward && (!grad_out || (n_layers && !grad_cov))) ||
+        (n_layers > 1 && plane < n_px))
+        return fail(c, FT_ERR_ARG, "bad SrcOver arguments");
+    const uintptr_t v4 = reinterpret_cast<uintptr_t>(clr) | reinterpret_cast<uintptr_t>(init) |
+                         reinterpret_cast<uintptr_t>(out) | reinterpret_cast<uintptr_t>(grad_out) |
+                         reinterpret_cast<uintptr_t>(grad_init);
+    if (v4 & 15) return fail(c, FT_ERR_ARG, "colour and canvas buffers need 16-byte alignment");
+    FT_CU(cudaSetDevice(c->device), "set device");
+    const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((n_px + 255) / 256, (uint64_t)c->sm_count * 16));
+    FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
+    FT_CU(ftc::launch_srcover(backward, cov, n_layers, plane, reinterpret_cast<const float4*>(clr),
+                              reinterpret_cast<const float4*>(init), reinterpret_cast<float4*>(out),
+                              reinterpret_cast<const float4*>(grad_out), grad_cov, reinterpret_cast<float4*>(grad_init),
+                              n_px, grid, c->stream),
+          "launch SrcOver");
+    FT_CU(cudaEventRecord(c->ev1, c->stream), "event");
+    c->timed = true;
+    c->launches++;
+    return FT_OK;
+}
+
+FT_API int ft_srcover_forward(ft_ctx* c, const float* cov, uint32_t n_layers, uint64_t plane_floats, const float* clr,
+                              const float* init, float* out, uint32_t n_px) {
+    return srcover_call(c, false, cov, n_layers, plane_floats, clr, init, out, nullptr, nullptr, nullptr, n_px);
+}
+
+FT_API int ft_srcover_backward(ft_ctx* c, const float* cov, uint32_t n_layers, uint64_t plane_floats,
+                               const float* clr, const float* init, const float* grad_out, float* grad_cov,
+                               float* grad_init, uint32_t n_px) {
+    return srcover_call(c, true, cov, n_layers, plane_floats, clr, init, nullptr, grad_out, grad_cov, grad_init,
+                        n_px);
 }
 
 FT_API int ft_autotune_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* ops, uint32_t n_ops_total,

@@ -1,4 +1,5 @@
-// ft_convert.cu — Rgba8p -> SRgba8 and Matte8 -> SGray8 on the device.
+// ft_convert.cu — Rgba8p -> SRgba8 and Matte8 -> SGray8 on the device, and the float
+// ordered SrcOver of coverage layers with its adjoint.
 //
 // footile plots in linear premultiplied Rgba8p / Matte8; its examples then convert with
 // pix (`Raster::<SRgba8>::with_raster`, examples/fishy.rs:33; `Raster::<SGray8>`,
@@ -97,6 +98,73 @@ int convert_blocks_per_sm() {
 cudaError_t launch_convert(int src_fmt, const uint8_t* src, uint32_t src_stride, uint8_t* dst, uint32_t dst_stride,
                            uint32_t w, uint32_t h, const uint8_t* lut, int grid, cudaStream_t s) {
     k_convert<<<grid, CBLOCK, 0, s>>>(src_fmt, src, src_stride, dst, dst_stride, w, h, lut);
+    return cudaGetLastError();
+}
+
+
+// ------------------------------------------------------ ordered SrcOver adjoint
+// The composite of an ordered batch in float: layer n (coverage cov_n, premultiplied
+// colour c_n with alpha a_n, as footile's pix SrcOver, fig.rs:637-643) gives
+//   C_n = c_n * cov_n + C_{n-1} * (1 - a_n * cov_n).
+// With G = dLoss/dC_N, the factor (1 - a_n cov_n) is one scalar for all four channels,
+// so dLoss/dcov_n = P_n * (G . c_n - a_n * E_{n-1}) with P_n the product of the later
+// factors and E_n = G . C_n following the same recurrence as C (scalar).  Backward:
+// one pass forward for E (recomputed, nothing kept from the forward call), written
+// into the gradient planes, then one pass backward for P.  No division, so opaque
+// layers (factor 0) are exact.  One thread per pixel; planes are n_layers x n_px floats.
+__global__ void k_srcover_fwd(const float* __restrict__ cov, uint32_t n_layers, uint64_t plane,
+                              const float4* __restrict__ clr, const float4* __restrict__ init,
+                              float4* __restrict__ out, uint32_t n_px) {
+    for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n_px;
+         p += (uint64_t)gridDim.x * blockDim.x) {
+        float4 c = init ? init[p] : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (uint32_t n = 0; n < n_layers; n++) {
+            const float v = cov[(uint64_t)n * plane + p];
+            if (v == 0.0f) continue;
+            const float4 k = clr[n];
+            const float f = 1.0f - k.w * v;
+            c = make_float4(k.x * v + c.x * f, k.y * v + c.y * f, k.z * v + c.z * f, k.w * v + c.w * f);
+        }
+        out[p] = c;
+    }
+}
+
+__global__ void k_srcover_bwd(const float* __restrict__ cov, uint32_t n_layers, uint64_t plane,
+                              const float4* __restrict__ clr, const float4* __restrict__ init,
+                              const float4* __restrict__ grad_out, float* __restrict__ grad_cov,
+                              float4* __restrict__ grad_init, uint32_t n_px) {
+    for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n_px;
+         p += (uint64_t)gridDim.x * blockDim.x) {
+        const float4 g = grad_out[p];
+        const float4 c0 = init ? init[p] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float e = g.x * c0.x + g.y * c0.y + g.z * c0.z + g.w * c0.w;
+        for (uint32_t n = 0; n < n_layers; n++) {  // E_{n-1} into the gradient plane
+            const uint64_t i = (uint64_t)n * plane + p;
+            const float v = cov[i];
+            grad_cov[i] = e;
+            if (v == 0.0f) continue;
+            const float4 k = clr[n];
+            e = (g.x * k.x + g.y * k.y + g.z * k.z + g.w * k.w) * v + e * (1.0f - k.w * v);
+        }
+        float P = 1.0f;
+        for (uint32_t n = n_layers; n-- > 0;) {
+            const uint64_t i = (uint64_t)n * plane + p;
+            const float v = cov[i];
+            const float4 k = clr[n];
+            grad_cov[i] = P * ((g.x * k.x + g.y * k.y + g.z * k.z + g.w * k.w) - k.w * grad_cov[i]);
+            P *= 1.0f - k.w * v;
+        }
+        if (grad_init) grad_init[p] = make_float4(g.x * P, g.y * P, g.z * P, g.w * P);
+    }
+}
+
+cudaError_t launch_srcover(bool backward, const float* cov, uint32_t n_layers, uint64_t plane, const float4* clr,
+                           const float4* init, float4* out, const float4* grad_out, float* grad_cov,
+                           float4* grad_init, uint32_t n_px, int grid, cudaStream_t s) {
+    if (backward)
+        k_srcover_bwd<<<grid, 256, 0, s>>>(cov, n_layers, plane, clr, init, grad_out, grad_cov, grad_init, n_px);
+    else
+        k_srcover_fwd<<<grid, 256, 0, s>>>(cov, n_layers, plane, clr, init, out, n_px);
     return cudaGetLastError();
 }
 

@@ -279,6 +279,23 @@ FT_API int ft_convert(ft_ctx* ctx, int32_t src_fmt, const uint8_t* src, uint32_t
                       int32_t dst_fmt, uint8_t* dst, uint32_t dst_stride, uint32_t w, uint32_t h,
                       int32_t where);
 
+/* Ordered SrcOver of float coverage layers, and its adjoint — the differentiable
+ * counterpart of ft_composite_batch, for an ordered batch of fills or strokes whose
+ * coverages come from ft_adjoint_forward (one plane per path over the shared canvas).
+ * Layer n (coverage plane cov + n * plane_floats, premultiplied colour clr[4n..4n+3] in
+ * [0, 1]) composites as pix's SrcOver does (fig.rs:637-643):
+ *   C_n = clr_n * cov_n + C_{n-1} * (1 - alpha_n * cov_n),   C_0 = init (or 0).
+ * ft_srcover_forward writes C_N (n_px float4).  ft_srcover_backward takes dLoss/dC_N
+ * and writes dLoss/dcov for every layer (the layout of cov) and dLoss/dC_0 (may be
+ * NULL); it recomputes the canvas terms it needs (nothing is kept from the forward)
+ * and divides by nothing, so opaque layers are exact.  Device pointers; asynchronous on
+ * the context stream. */
+FT_API int ft_srcover_forward(ft_ctx* ctx, const float* cov, uint32_t n_layers, uint64_t plane_floats,
+                              const float* clr, const float* init, float* out, uint32_t n_px);
+FT_API int ft_srcover_backward(ft_ctx* ctx, const float* cov, uint32_t n_layers, uint64_t plane_floats,
+                               const float* clr, const float* init, const float* grad_out,
+                               float* grad_cov, float* grad_init, uint32_t n_px);
+
 /* Per-path status codes of the last batch (synchronises the context stream). */
 FT_API int ft_batch_status(ft_ctx* ctx, int32_t* status, uint32_t n);
 

@@ -326,3 +326,50 @@ def convert(src):
             out[..., ch] = lut[a, src[..., ch]]
         return out
     return lut[255, src]
+
+
+# ------------------------------------------- ordered SrcOver of strokes (FP64 chain)
+def adj_stroke_composite(ops, paths, clr, w, h, target, val=None, join=_abi.JOIN_MITER, miter_limit=4.0,
+                         tolerance=0.3, transform=_abi.IDENTITY, grads=True):
+    """FP64 loss sum((C_N - target)^2) of strokes SrcOver'd in order on one w x h canvas
+    (C_n = clr_n cov_n + C_{n-1} (1 - a_n cov_n), float premultiplied colours), and with
+    `grads` its gradient w.r.t. the op floats (n_ops, 6) and the starting pen widths.
+    `val` (n_ops x 6) moves the vertices continuously on held decisions (for finite
+    differences)."""
+    ops = np.ascontiguousarray(ops, dtype=_abi.OP_DTYPE)
+    n = len(paths)
+    kw = dict(join=join, miter_limit=miter_limit, tolerance=tolerance, transform=transform)
+    covs, areas = [], []
+    for p in paths:
+        b, k = int(p["op_begin"]), int(p["n_ops"])
+        v = None if val is None else val[b:b + k]
+        c, a, _ = adj_stroke_forward(ops[b:b + k], w, h, val=v, s_width=float(p["s_width"]), **kw)
+        covs.append(c.ravel())
+        areas.append(a)
+    C = np.zeros((w * h, 4))
+    for i in range(n):
+        C = clr[i][None, :] * covs[i][:, None] + C * (1.0 - clr[i][3] * covs[i])[:, None]
+    loss = float(((C - target) ** 2).sum())
+    if not grads:
+        return loss
+    G = 2.0 * (C - target)
+    # E_{n-1} = G . C_{n-1} forward, then the suffix products backward
+    E = np.zeros(w * h)
+    Es = []
+    for i in range(n):
+        Es.append(E.copy())
+        E = (G @ clr[i]) * covs[i] + E * (1.0 - clr[i][3] * covs[i])
+    P = np.ones(w * h)
+    g_ops = np.zeros((len(ops), 6))
+    g_w = np.zeros(n)
+    for i in reversed(range(n)):
+        gc = P * ((G @ clr[i]) - clr[i][3] * Es[i])
+        P = P * (1.0 - clr[i][3] * covs[i])
+        p = paths[i]
+        b, k = int(p["op_begin"]), int(p["n_ops"])
+        v = None if val is None else val[b:b + k]
+        gg, gw = adj_stroke_backward(ops[b:b + k], w, h, areas[i], gc.reshape(h, w), val=v,
+                                     s_width=float(p["s_width"]), **kw)
+        g_ops[b:b + k] += gg
+        g_w[i] = gw
+    return loss, C, g_ops, g_w

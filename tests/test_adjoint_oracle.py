@@ -194,3 +194,24 @@ def test_stroke_coverage_tracks_footile_masks():
         m = np.zeros((128, 128), np.uint8)
         oracle.stroke(STROKE, m, _abi.MATTE8, clr=(255,) * 4, join=join[0], miter_limit=join[1])
         assert np.abs(cov * 255 - m).mean() < 1.5
+
+
+def test_stroke_composite_gradient_matches_central_differences():
+    # the FP64 chain: strokes SrcOver'd in order, L2 loss against an RGBA target
+    from footile_gb300.adjoint import pack_coverage
+    paths_ops, widths, clrs, side = workloads.strokes_16384(n_paths=4, side=48, min_seg=2, max_seg=4)
+    ops, paths, _ = pack_coverage(paths_ops, [side] * 4)
+    clr = clrs.astype(np.float64) / 255.0
+    target = np.random.default_rng(8).random((side * side, 4))
+    base = values(ops)
+    loss, C, g, gw = oracle.adj_stroke_composite(ops, paths, clr, side, side, target, val=base)
+    step = 1e-5
+    rng = np.random.default_rng(2)
+    entries = [(i, k) for i in range(len(ops)) for k in range(6) if g[i, k] != 0.0]
+    for i, k in [entries[j] for j in rng.choice(len(entries), 12, replace=False)]:
+        vp, vm = base.copy(), base.copy()
+        vp[i, k] += step
+        vm[i, k] -= step
+        fd = (oracle.adj_stroke_composite(ops, paths, clr, side, side, target, val=vp, grads=False) -
+              oracle.adj_stroke_composite(ops, paths, clr, side, side, target, val=vm, grads=False)) / (2 * step)
+        assert abs(g[i, k] - fd) <= 2e-4 * np.abs(g).max(), (i, k, g[i, k], fd)
