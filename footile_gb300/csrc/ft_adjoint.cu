@@ -701,6 +701,8 @@ struct StrokeScr {
     float2* ng;
     float4* spg;
     int* vnode;
+    int* soff;  // per sub-stroke: first outline segment (both sides)
+    int2* gst;  // per sub-stroke: first outline vertex of the forward / reverse side
 };
 
 __device__ __forceinline__ StrokeScr stroke_scr(unsigned char* scr) {
@@ -711,14 +713,16 @@ __device__ __forceinline__ StrokeScr stroke_scr(unsigned char* scr) {
     S.ng = reinterpret_cast<float2*>(scr + AS_NG);
     S.spg = reinterpret_cast<float4*>(scr + AS_SPG);
     S.vnode = reinterpret_cast<int*>(scr + AS_VNODE);
+    S.soff = reinterpret_cast<int*>(scr + AS_SOFF);
+    S.gst = reinterpret_cast<int2*>(scr + AS_GST);
     return S;
 }
 
-// Thread 0: stroke points, outline nodes and the outline polygon (vpos, vsub, vnode).
-// Returns the outline vertex count (may exceed VCAP: nothing beyond VCAP is written);
-// *n_nodes / *n_sp get the node and stroke point counts, *status the path status.
-__device__ int build_stroke_dev(const AParams& p, const ft_op* ops, int n, float sw0, const StrokeScr& S,
-                                float2* vpos, int* vsub, int* n_nodes, int* n_sp, int* status) {
+// Thread 0: the stroke points and sub-strokes of the path (Plotter's pen walk into
+// Stroke::add_point / close).  Returns the stroke point count; *n_sub gets the
+// sub-stroke count, *status the path status.
+__device__ int stroke_points_dev(const AParams& p, const ft_op* ops, int n, float sw0, const StrokeScr& S,
+                                 int* n_sub, int* status) {
     const float* m = p.xf;
     // ---- stroke points (plotter.rs:175-332 into Stroke::add_point / close)
     float sw = sw0;
@@ -812,139 +816,215 @@ __device__ int build_stroke_dev(const AParams& p, const ft_op* ops, int n, float
         }
     }
     S.subs[nsub++] = cur;
-    *n_sp = ns;
-    // ---- outline (stroker.rs:239-416), filled as Line ops transformed again.  Node
-    // values travel with their ids: nothing written here is read back.
-    struct NV {
-        int id;
-        P2 v;
-    };
-    struct SV {
-        P2 p;
-        float w;
-    };
-    int nn = 0, nv = 0, sub_start = 0;
-    bool fresh = true;
-    auto SPv = [&](int k) {
-        const SPt q = S.sp[k];
-        return SV{p2(q.x, q.y), q.w};
-    };
-    auto node = [&](int kind, int a, int b, int c, int d, P2 v) {
-        if (nn < NODE_CAP) S.nd[nn] = SNd{kind, a, b, c, d, v.x, v.y, 0};
-        return NV{nn++, v};
-    };
-    auto emit = [&](NV nd) {
-        if (nv < VCAP) {
-            if (fresh) sub_start = nv;
-            const P2 q = xform(m, nd.v);
-            vpos[nv] = make_float2(fx_range(q.x), fx_range(q.y));
-            vsub[nv] = sub_start;
-            S.vnode[nv] = nd.id;
-        }
-        fresh = false;
-        nv++;
-    };
+    *n_sub = nsub;
+    return ns;
+}
+
+// All threads: the outline of every sub-stroke (stroker.rs:239-416) and the polygon
+// Plotter::stroke fills (the outline's Line points transformed again, sub-figures
+// between its Closes).  Segments (sub-stroke, side, k) are independent: their offset
+// points are nodes 2s and 2s + 1; the join at segment k (k >= 1) needs only segments
+// k - 1 and k.  A pass counts each segment's vertices and extra nodes (a miter
+// intersection, or the arc points of a round join), block scans place them, and each
+// segment emits its vertices in footile's order: the open side's first offset point,
+// the join, the open side's last offset point.  Arc points are numbered in the
+// recursion's creation order within their segment, so a node's inputs are older nodes.
+// Returns the vertex count (beyond VCAP nothing is written) and the node count.
+__device__ void outline_block(const AParams& p, const StrokeScr& S, int nsub, ASmem& sm, float2* vpos, int* vsub,
+                              int* out_v, int* out_n) {
+    const int tid = threadIdx.x;
+    const float* m = p.xf;
     const float tol_sq = p.tol_sq;
-    auto arc = [&](int k, SV c0, NV na0, NV nb0) {
-        struct Fr {
-            NV na, nb;
-            int dep;
-        };
+    if (tid == 0) {
+        int t = 0;
+        for (int si = 0; si < nsub; si++) {
+            const SSub sb = S.subs[si];
+            const int len = (sb.joined ? sb.n + 1 : (sb.n > 0 ? sb.n - 1 : 0)) & 0xFFFF;  // SubStroke::len (u16)
+            S.soff[si] = t;
+            t += 2 * len;
+        }
+        S.soff[nsub] = t;
+        sm.total = t;
+    }
+    __syncthreads();
+    const int T = sm.total;
+    if (2LL * T > NODE_CAP) {
+        if (tid == 0) atomicMax(&sm.status, (int)FT_ERR_CAP);
+        *out_v = VCAP + 1;
+        *out_n = 0;
+        return;
+    }
+    struct Seg {
+        int si, k, len, v0, v1;
+        bool fwd, joined;
+    };
+    auto seg = [&](int s) {
+        int lo = 0, hi = nsub - 1;  // the sub-stroke owning segment s
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (S.soff[mid] <= s)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        const SSub sb = S.subs[lo];
+        Seg g;
+        g.si = lo;
+        g.joined = sb.joined != 0;
+        g.len = (S.soff[lo + 1] - S.soff[lo]) >> 1;
+        const int u = s - S.soff[lo];
+        g.fwd = u < g.len;
+        g.k = g.fwd ? u : u - g.len;
+        const int n = sb.n;
+        if (g.fwd) {
+            g.v0 = sb.start + g.k % n;
+            g.v1 = sb.start + (g.k + 1) % n;
+        } else {  // from the last point backwards (stroker.rs:244-246)
+            g.v0 = sb.start + ((n - 1 - g.k) % n + n) % n;
+            g.v1 = sb.start + ((n - 2 - g.k) % n + n) % n;
+        }
+        return g;
+    };
+    auto P = [&](int k) { return p2(S.sp[k].x, S.sp[k].y); };
+    auto N = [&](int i) { return p2(S.nd[i].x, S.nd[i].y); };
+    // offset points
+    for (int s = tid; s < T; s += ABLOCK) {
+        const Seg g = seg(s);
+        const P2 vr = ftk::pnormalize(ftk::pright(ftk::psub(P(g.v1), P(g.v0))));
+        const P2 a = ftk::padd(P(g.v0), ftk::pscale(vr, __fmul_rn(S.sp[g.v0].w, 0.5f)));
+        const P2 b = ftk::padd(P(g.v1), ftk::pscale(vr, __fmul_rn(S.sp[g.v1].w, 0.5f)));
+        S.nd[2 * s] = SNd{N_OFF, g.v0, g.v1, 0, 0, a.x, a.y, 0};
+        S.nd[2 * s + 1] = SNd{N_OFF, g.v0, g.v1, 1, 0, b.x, b.y, 0};
+    }
+    __syncthreads();
+    // arc recursion of a round join (stroker.rs:399-416); emit(node, value) per leaf,
+    // node(c) creates an arc point
+    struct Fr {
+        int na, nb;
+        P2 a, b;
+        int dep;
+    };
+    auto arc_walk = [&](int k, int na0, int nb0, int* depth_hit, auto leaf, auto make) {
         Fr st[FT_MAX_DEPTH + 3];
         int sp = 0;
-        st[sp++] = Fr{na0, nb0, 0};
-        const float hw = __fmul_rn(c0.w, 0.5f);
+        st[sp++] = Fr{na0, nb0, N(na0), N(nb0), 0};
+        const P2 pk = P(k);
+        const float hw = __fmul_rn(S.sp[k].w, 0.5f);
         while (sp > 0) {
             const Fr f = st[--sp];
-            const P2 vr = ftk::pnormalize(ftk::pright(ftk::psub(f.nb.v, f.na.v)));
-            const P2 c = ftk::padd(c0.p, ftk::pscale(vr, hw));
-            if (!pfinite(c) || pdist_sq(c, pmid(f.na.v, f.nb.v)) <= tol_sq) {
-                emit(f.nb);
+            const P2 vr = ftk::pnormalize(ftk::pright(ftk::psub(f.b, f.a)));
+            const P2 c = ftk::padd(pk, ftk::pscale(vr, hw));
+            if (!pfinite(c) || pdist_sq(c, pmid(f.a, f.b)) <= tol_sq) {
+                leaf(f.nb, f.b);
             } else if (f.dep >= FT_MAX_DEPTH) {
-                *status = max(*status, (int)FT_ERR_DEPTH);
-                emit(f.nb);
+                *depth_hit = 1;
+                leaf(f.nb, f.b);
             } else {
-                const NV nc = node(N_ARC, k, f.na.id, f.nb.id, 0, c);
-                st[sp++] = Fr{nc, f.nb, f.dep + 1};  // right half after the left
-                st[sp++] = Fr{f.na, nc, f.dep + 1};
+                const int nc = make(k, f.na, f.nb, c);
+                st[sp++] = Fr{nc, f.nb, c, f.b, f.dep + 1};  // right half after the left
+                st[sp++] = Fr{f.na, nc, f.a, c, f.dep + 1};
             }
         }
     };
-    auto join = [&](int k, SV pk, NV a0, NV a1, NV b0, NV b1) {
-        if (p.join == FT_JOIN_MITER) {
-            if (p.miter_limit > 0.0f) {
-                const float sm_min = __fdiv_rn(1.0f, p.miter_limit);
-                const float th = ftk::pangle_rel(ftk::psub(a1.v, a0.v), ftk::psub(b0.v, b1.v));
-                const float sm = fabsf(ft_sinf(__fdiv_rn(th, 2.0f)));
-                P2 xp;
-                if (sm >= sm_min && sm < 1.0f && ftk::pline_x(a0.v, a1.v, b0.v, b1.v, &xp)) {
-                    emit(node(N_MITER, a0.id, a1.id, b0.id, b1.id, xp));
-                    return;
+    enum { J_NONE = 0, J_MITER = 1, J_BEVEL = 2, J_ARC = 3 };
+    int carry_v = 0, carry_n = 2 * T;
+    for (int c0 = 0; c0 < T; c0 += ABLOCK) {
+        const int s = c0 + tid;
+        const bool valid = s < T;
+        Seg g{};
+        int jt = J_NONE, cnt_v = 0, cnt_n = 0, dh = 0;
+        P2 xp = p2(0.0f, 0.0f);
+        if (valid) {
+            g = seg(s);
+            if (g.k == 0 && !g.joined) cnt_v++;
+            if (g.k >= 1) {
+                const P2 A0 = N(2 * s - 2), A1 = N(2 * s - 1), B0 = N(2 * s), B1 = N(2 * s + 1);
+                if (p.join == FT_JOIN_MITER) {
+                    jt = J_BEVEL;
+                    if (p.miter_limit > 0.0f) {
+                        const float sm_min = __fdiv_rn(1.0f, p.miter_limit);
+                        const float th = ftk::pangle_rel(ftk::psub(A1, A0), ftk::psub(B0, B1));
+                        const float smv = fabsf(ft_sinf(__fdiv_rn(th, 2.0f)));
+                        if (smv >= sm_min && smv < 1.0f && ftk::pline_x(A0, A1, B0, B1, &xp)) jt = J_MITER;
+                    }
+                } else if (p.join == FT_JOIN_BEVEL) {
+                    jt = J_BEVEL;
+                } else {
+                    const float th = ftk::pangle_rel(ftk::psub(A1, A0), ftk::psub(B0, B1));
+                    jt = th <= 0.0f ? J_BEVEL : J_ARC;
+                }
+                if (jt == J_MITER) {
+                    cnt_v += 1;
+                    cnt_n += 1;
+                } else if (jt == J_BEVEL) {
+                    cnt_v += 2;
+                } else {
+                    int leaves = 0, inner = 0;
+                    arc_walk(g.v0, 2 * s - 1, 2 * s, &dh, [&](int, P2) { leaves++; },
+                             [&](int, int, int, P2) { return -1 - (inner++); });
+                    cnt_v += 1 + leaves;
+                    cnt_n += inner;
                 }
             }
-            emit(a1);
-            emit(b0);
-        } else if (p.join == FT_JOIN_BEVEL) {
-            emit(a1);
-            emit(b0);
-        } else {
-            const float th = ftk::pangle_rel(ftk::psub(a1.v, a0.v), ftk::psub(b0.v, b1.v));
-            emit(a1);
-            if (th <= 0.0f)
-                emit(b0);
+            if (g.k == g.len - 1 && !g.joined) cnt_v++;
+            if (dh) atomicMax(&sm.status, (int)FT_ERR_DEPTH);
+        }
+        int tot_v, tot_n;
+        const int ov = carry_v + block_excl_sum(cnt_v, sm.wsum, tot_v);
+        const int on = carry_n + block_excl_sum(cnt_n, sm.wsum, tot_n);
+        if (valid && g.k == 0) {
+            if (g.fwd)
+                S.gst[g.si].x = ov;
             else
-                arc(k, pk, a1, b0);
+                S.gst[g.si].y = ov;
         }
-    };
-    for (int si = 0; si < nsub && nn <= NODE_CAP && nv <= VCAP; si++) {
-        const SSub sb = S.subs[si];
-        const int len = (sb.joined ? sb.n + 1 : (sb.n > 0 ? sb.n - 1 : 0)) & 0xFFFF;  // SubStroke::len (u16)
-        if (len == 0) continue;
-        auto nextv = [&](int v, bool fwd) {
-            if (fwd) return v + 1 < sb.start + sb.n ? v + 1 : sb.start;
-            return v > sb.start ? v - 1 : sb.start + sb.n - 1;
-        };
-        for (int side = 0; side < 2; side++) {
-            const bool fwd = side == 0;
-            int v0 = fwd ? sb.start : nextv(sb.start, false);
-            int v1 = nextv(v0, fwd);
-            SV q0 = SPv(v0), q1 = SPv(v1);
-            bool have = false;
-            NV x0{0, p2(0.0f, 0.0f)}, x1 = x0;
-            for (int k = 0; k < len; k++) {
-                const int v2 = nextv(v1, fwd);
-                const SV q2 = SPv(v2);  // the next segment's end, loaded ahead
-                const P2 vr = ftk::pnormalize(ftk::pright(ftk::psub(q1.p, q0.p)));
-                const NV o0 = node(N_OFF, v0, v1, 0, 0, ftk::padd(q0.p, ftk::pscale(vr, __fmul_rn(q0.w, 0.5f))));
-                const NV o1 = node(N_OFF, v0, v1, 1, 0, ftk::padd(q1.p, ftk::pscale(vr, __fmul_rn(q1.w, 0.5f))));
-                if (have)
-                    join(v0, q0, x0, x1, o0, o1);
-                else if (!sb.joined)
-                    emit(o0);
-                have = true;
-                x0 = o0;
-                x1 = o1;
-                v0 = v1;
-                v1 = v2;
-                q0 = q1;
-                q1 = q2;
+        __syncthreads();
+        if (valid) {
+            const int sub_start = (g.fwd || !g.joined) ? S.gst[g.si].x : S.gst[g.si].y;
+            int w = ov, nid = on;
+            auto put = [&](int nd, P2 v) {
+                if (w < VCAP) {
+                    const P2 q = xform(m, v);
+                    vpos[w] = make_float2(fx_range(q.x), fx_range(q.y));
+                    vsub[w] = sub_start;
+                    S.vnode[w] = nd;
+                }
+                w++;
+            };
+            auto make = [&](int kind, int a, int b, int c, int d, P2 v) {
+                if (nid < NODE_CAP) S.nd[nid] = SNd{kind, a, b, c, d, v.x, v.y, 0};
+                return nid++;
+            };
+            if (g.k == 0 && !g.joined) put(2 * s, N(2 * s));
+            if (jt == J_MITER) {
+                put(make(N_MITER, 2 * s - 2, 2 * s - 1, 2 * s, 2 * s + 1, xp), xp);
+            } else if (jt == J_BEVEL) {
+                put(2 * s - 1, N(2 * s - 1));
+                put(2 * s, N(2 * s));
+            } else if (jt == J_ARC) {
+                put(2 * s - 1, N(2 * s - 1));
+                int d2 = 0;
+                arc_walk(g.v0, 2 * s - 1, 2 * s, &d2, [&](int nb, P2 b) { put(nb, b); },
+                         [&](int k, int na, int nb, P2 c) { return make(N_ARC, k, na, nb, 0, c); });
             }
-            if (!sb.joined && have) emit(x1);
-            if (fwd && sb.joined) fresh = true;  // Close between the two sides
+            if (g.k == g.len - 1 && !g.joined) put(2 * s + 1, N(2 * s + 1));
         }
-        fresh = true;  // Close
+        carry_v += tot_v;
+        carry_n += tot_n;
+        __syncthreads();
     }
-    if (nn > NODE_CAP || nv > VCAP) *status = max(*status, (int)FT_ERR_CAP);
-    *n_nodes = min(nn, NODE_CAP);
-    return nv;
+    if (tid == 0 && (carry_v > VCAP || carry_n > NODE_CAP)) atomicMax(&sm.status, (int)FT_ERR_CAP);
+    *out_v = carry_v;
+    *out_n = min(carry_n, NODE_CAP);
 }
 
 // Backward of a stroke, all threads: outline vertex gradients (vgrad, fill space) ->
-// nodes -> stroke points -> op floats and widths.  Children are always older nodes:
-// arcs (reverse creation order, one thread: an arc may feed another), then miter
-// intersections and offset points in parallel, then stroke points.
+// nodes -> stroke points -> op floats and widths.  Offset nodes are [0, n_off), the
+// others after them; a node's inputs are always older nodes: arcs (reverse creation
+// order, one thread: an arc may feed another), then miter intersections and offset
+// points in parallel, then stroke points.
 __device__ void stroke_backward_block(const AParams& p, const ft_op* ops, float* gops, float* gwidth, int V, int nn,
-                                      int ns, const StrokeScr& S, const float2* vgrad) {
+                                      int ns, int n_off, const StrokeScr& S, const float2* vgrad) {
     const int tid = threadIdx.x;
     const float* m = p.xf;
     for (int i = tid; i < nn; i += ABLOCK) S.ng[i] = make_float2(0.0f, 0.0f);
@@ -973,8 +1053,9 @@ __device__ void stroke_backward_block(const AParams& p, const ft_op* ops, float*
         *gto = make_float2(-guy, gux);  // u = (d.y, -d.x), d = to - from
         *gfrom = make_float2(guy, -gux);
     };
-    if (tid == 0) {
-        for (int i = nn - 1; i >= 0; i--) {
+    // arc points exist only with round joins, after the offset nodes [0, n_off)
+    if (tid == 0 && p.join == FT_JOIN_ROUND) {
+        for (int i = nn - 1; i >= n_off; i--) {
             const SNd nd = S.nd[i];
             if (nd.kind != N_ARC) continue;
             const float2 g = __ldcg(&S.ng[i]);
@@ -1001,7 +1082,7 @@ __device__ void stroke_backward_block(const AParams& p, const ft_op* ops, float*
         x = (double)S.sp[ks].x + ux / len * hw;
         y = (double)S.sp[ks].y + uy / len * hw;
     };
-    for (int i = tid; i < nn; i += ABLOCK) {
+    for (int i = n_off + tid; i < nn; i += ABLOCK) {
         const SNd nd = S.nd[i];
         if (nd.kind != N_MITER) continue;
         const float2 gf = __ldcg(&S.ng[i]);
@@ -1041,7 +1122,7 @@ __device__ void stroke_backward_block(const AParams& p, const ft_op* ops, float*
         atomicAdd(&S.ng[nd.b].y, (float)(gy - guy - g3y - g4y));
     }
     __syncthreads();
-    for (int i = tid; i < nn; i += ABLOCK) {
+    for (int i = tid; i < min(nn, n_off); i += ABLOCK) {
         const SNd nd = S.nd[i];
         if (nd.kind != N_OFF) continue;
         const float2 g = __ldcg(&S.ng[i]);
@@ -1111,7 +1192,7 @@ __global__ void __launch_bounds__(ABLOCK) k_adjoint(AParams p) {
     __shared__ ASmem sm;
     unsigned char* scr = p.scratch + (size_t)blockIdx.x * (p.stroke ? A_SCRATCH_STROKE : A_SCRATCH_PER_CTA);
     const StrokeScr S = stroke_scr(scr);
-    __shared__ int s_counts[3];
+    __shared__ int s_counts[4];
     float2* vpos = reinterpret_cast<float2*>(scr + AS_POS);
     int* vsub = reinterpret_cast<int*>(scr + AS_SUB);
     float2* vgrad = reinterpret_cast<float2*>(scr + AS_GRAD);
@@ -1126,11 +1207,19 @@ __global__ void __launch_bounds__(ABLOCK) k_adjoint(AParams p) {
         int V;
         if (p.stroke) {
             if (tid == 0) {
-                int st = FT_OK, nn = 0, ns = 0;
-                s_counts[0] = build_stroke_dev(p, ops, (int)d.n_ops, d.s_width, S, vpos, vsub, &nn, &ns, &st);
-                s_counts[1] = nn;
-                s_counts[2] = ns;
+                int st = FT_OK, nsub = 0;
+                s_counts[2] = stroke_points_dev(p, ops, (int)d.n_ops, d.s_width, S, &nsub, &st);
+                s_counts[0] = nsub;
                 atomicMax(&sm.status, st);
+            }
+            __syncthreads();
+            int nv = 0, nn = 0;
+            outline_block(p, S, s_counts[0], sm, vpos, vsub, &nv, &nn);
+            __syncthreads();
+            if (tid == 0) {
+                s_counts[0] = nv;
+                s_counts[1] = nn;
+                s_counts[3] = 2 * sm.total;  // offset nodes come first
             }
             __syncthreads();
             V = s_counts[0];
@@ -1189,7 +1278,7 @@ __global__ void __launch_bounds__(ABLOCK) k_adjoint(AParams p) {
             if (p.stroke) {
                 __syncthreads();
                 stroke_backward_block(p, ops, p.grad_ops + (size_t)d.op_begin * 6, p.grad_width + path, V,
-                                      s_counts[1], s_counts[2], S, vgrad);
+                                      s_counts[1], s_counts[2], s_counts[3], S, vgrad);
             } else {
                 path_walk<WALK_GRAD>(p, sm, ops, (int)d.n_ops, vpos, vsub, vgrad, false,
                                      p.grad_ops + (size_t)d.op_begin * 6);

@@ -34,7 +34,9 @@ constexpr size_t AS_SSUB = a_align(AS_SPT + (size_t)VCAP * SPT_BYTES);          
 constexpr size_t AS_SND = a_align(AS_SSUB + (size_t)(VCAP + 1) * SSUB_BYTES);    // nodes
 constexpr size_t AS_NG = a_align(AS_SND + (size_t)NODE_CAP * SND_BYTES);         // float2 node gradients
 constexpr size_t AS_SPG = a_align(AS_NG + (size_t)NODE_CAP * 8);                 // float4 stroke point gradients
-constexpr size_t A_SCRATCH_STROKE = a_align(AS_SPG + (size_t)VCAP * 16);
+constexpr size_t AS_SOFF = a_align(AS_SPG + (size_t)VCAP * 16);                  // int[VCAP + 2] segment offsets
+constexpr size_t AS_GST = a_align(AS_SOFF + (size_t)(VCAP + 2) * 4);             // int2[VCAP + 1] side starts
+constexpr size_t A_SCRATCH_STROKE = a_align(AS_GST + (size_t)(VCAP + 1) * 8);
 
 struct AParams {
     const ft_op* ops;
