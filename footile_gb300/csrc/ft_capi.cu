@@ -56,8 +56,13 @@ struct ft_ctx {
     DevBuf pool, pool_used, bandoff, crec;  // ordered composite
     DevBuf srgb_lut, conv_src, conv_dst;    // ft_convert
     std::vector<ftk::WorkItem> h_items, h_items_w;
+    // the plan behind h_items / items on the device, reused while the same batch comes back
+    std::vector<ft_path_desc> plan_paths;
+    int plan_smem = -1, plan_stroke = -1, plan_wside = -1;
+    uint64_t plan_split = 0;
     uint32_t last_n_paths = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
     bool timed = false;
     uint64_t launches = 0;
     int sm_count = 0;
@@ -244,11 +249,21 @@ int run(ft_ctx* c, int stroke, int rule, const ft_op* ops_d, const ft_path_desc*
     uint32_t max_w = 1;
     for (uint32_t i = 0; i < n_paths; i++) max_w = std::max(max_w, paths[i].width);
     const int smem = choose_smem(c, max_w);
-    plan_items(c, paths, n_paths, smem, c->h_items, c->h_items_w, stroke != 0);
+    // a batch that comes back unchanged (same descriptors and plan knobs) keeps its
+    // planned and uploaded work items
+    const bool same_plan = c->plan_smem == smem && c->plan_stroke == stroke && c->plan_wside == warp_max_side(c) &&
+                           c->plan_split == split_px(c) && c->plan_paths.size() == n_paths &&
+                           (n_paths == 0 || memcmp(c->plan_paths.data(), paths, sizeof(ft_path_desc) * n_paths) == 0);
+    if (!same_plan) {
+        c->plan_smem = -1;  // invalid until the new items are on the device
+        plan_items(c, paths, n_paths, smem, c->h_items, c->h_items_w, stroke != 0);
+    }
     const uint32_t n_items = (uint32_t)c->h_items.size(), n_items_w = (uint32_t)c->h_items_w.size();
     FT_CU(c->paths.ensure(sizeof(ft_path_desc) * std::max(n_paths, 1u)), "alloc paths");
-    FT_CU(c->items.ensure(sizeof(ftk::WorkItem) * std::max(n_items, 1u)), "alloc items");
-    FT_CU(c->items_w.ensure(sizeof(ftk::WorkItem) * std::max(n_items_w, 1u)), "alloc items");
+    if (!same_plan) {
+        FT_CU(c->items.ensure(sizeof(ftk::WorkItem) * std::max(n_items, 1u)), "alloc items");
+        FT_CU(c->items_w.ensure(sizeof(ftk::WorkItem) * std::max(n_items_w, 1u)), "alloc items");
+    }
     FT_CU(c->overflow.ensure(sizeof(uint32_t) * std::max(n_items_w, 1u)), "alloc overflow list");
     FT_CU(c->status.ensure(sizeof(int32_t) * std::max(n_paths, 1u)), "alloc status");
     FT_CU(c->queue.ensure(256), "alloc queue");
@@ -258,14 +273,21 @@ int run(ft_ctx* c, int stroke, int rule, const ft_op* ops_d, const ft_path_desc*
     FT_CU(c->scratch.ensure(ftk::SCRATCH_BYTES_PER_CTA * (size_t)std::max(grid, grid_w)), "alloc scratch");
     FT_CU(cudaMemcpyAsync(c->paths.p, paths, sizeof(ft_path_desc) * n_paths, cudaMemcpyHostToDevice, c->stream),
           "upload paths");
-    if (n_items)
-        FT_CU(cudaMemcpyAsync(c->items.p, c->h_items.data(), sizeof(ftk::WorkItem) * n_items, cudaMemcpyHostToDevice,
-                              c->stream),
-              "upload items");
-    if (n_items_w)
-        FT_CU(cudaMemcpyAsync(c->items_w.p, c->h_items_w.data(), sizeof(ftk::WorkItem) * n_items_w,
-                              cudaMemcpyHostToDevice, c->stream),
-              "upload items");
+    if (!same_plan) {
+        if (n_items)
+            FT_CU(cudaMemcpyAsync(c->items.p, c->h_items.data(), sizeof(ftk::WorkItem) * n_items,
+                                  cudaMemcpyHostToDevice, c->stream),
+                  "upload items");
+        if (n_items_w)
+            FT_CU(cudaMemcpyAsync(c->items_w.p, c->h_items_w.data(), sizeof(ftk::WorkItem) * n_items_w,
+                                  cudaMemcpyHostToDevice, c->stream),
+                  "upload items");
+        c->plan_paths.assign(paths, paths + n_paths);
+        c->plan_smem = smem;
+        c->plan_stroke = stroke;
+        c->plan_wside = warp_max_side(c);
+        c->plan_split = split_px(c);
+    }
     FT_CU(cudaMemsetAsync(c->queue.p, 0, 256, c->stream), "reset queue");
     FT_CU(cudaMemsetAsync(c->status.p, 0, sizeof(int32_t) * std::max(n_paths, 1u), c->stream), "reset status");
     c->last_n_paths = n_paths;
@@ -673,8 +695,7 @@ FT_API int ft_fill_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* o
     }
     const ft_op* ops_d = ops;
     uint8_t* ras_d = rasters;
-    if (where == FT_HOST) {
-        if (!valid_ops_host(ops, n_ops_total)) return fail(c, FT_ERR_ARG, "unknown path op kind");
+    if (where == FT_HOST) {  // unknown op kinds are reported per path (FT_ERR_ARG), as for device ops
         FT_CU(c->ops.ensure(sizeof(ft_op) * std::max<uint64_t>(n_ops_total, 1)), "alloc ops");
         FT_CU(c->rasters.ensure(std::max<uint64_t>(raster_bytes, 1)), "alloc rasters");
         if (n_ops_total)

@@ -72,3 +72,29 @@ def test_batch_rgba_regions(ctx):
     got = init.copy()
     fill_batch(ctx, ops, paths, _abi.RGBA8P, got)
     assert_same(got, want, "rgba batch")
+
+
+def test_plan_reuse_and_invalidation(ctx):
+    # the same batch twice reuses its plan; a changed descriptor, a different batch
+    # and a single call in between must all replan
+    from footile_gb300.plotter import Plotter
+    a_ops, a_paths, a_bytes = workloads.glyphs(n_paths=300, seed=31, max_side=200)
+    b_ops, b_paths, b_bytes = workloads.glyphs(n_paths=300, seed=32, max_side=200)
+
+    def run(ops, paths, nbytes):
+        want = np.zeros(nbytes, np.uint8)
+        oracle.fill_batch(0, _abi.NONZERO, ops, paths, _abi.MATTE8, want, n_threads=8)
+        got = np.zeros(nbytes, np.uint8)
+        assert (fill_batch(ctx, ops, paths, _abi.MATTE8, got) == 0).all()
+        assert np.array_equal(got, want)
+    run(a_ops, a_paths, a_bytes)
+    run(a_ops, a_paths, a_bytes)
+    run(b_ops, b_paths, b_bytes)
+    run(a_ops, a_paths, a_bytes)
+    c_paths = a_paths.copy()
+    c_paths[0]["height"] = max(1, int(c_paths[0]["height"]) // 2)  # same length, one descriptor changed
+    run(a_ops, c_paths, a_bytes)
+    single = np.zeros((64, 64), np.uint8)
+    Plotter(single, context=ctx).fill(_abi.NONZERO, workloads.random_path(np.random.default_rng(3), 64, 10))
+    run(a_ops, a_paths, a_bytes)
+
