@@ -505,15 +505,16 @@ def extra_adjoint_strokes(ctx, stream, dev, cpu=True, reps=5, n_paths=1024, side
     return out
 
 
-def extra_adjoint_composite(ctx, stream, dev, cpu=True, n_paths=1024, side=512, reps=3):
-    """Differentiable ordered composite, the stroke workload at reduced size: 1,024
-    strokes shaped like the 16,384-stroke composite (8..64 cubics, width 1..12, Miter(4),
-    colours with alpha 64..255) SrcOver'd in order on one 512x512 canvas, L2 loss against
-    a seeded RGBA target; gradients of the control points and pen widths.  (The full
-    16,384 x 2048^2 size needs one dense f32 coverage plane per stroke: 275 GB.)"""
+def extra_adjoint_composite(ctx, stream, dev, cpu=True, n_paths=16384, side=2048, reps=2):
+    """Differentiable ordered composite at full size: 16,384 open strokes of 8..64 cubics,
+    width 1..12, Miter(4), colours with alpha 64..255, SrcOver'd in order on one 2048x2048
+    canvas, L2 loss against a seeded RGBA target; gradients of the control points and pen
+    widths (ft_stroke_composite_forward / _backward: coverage in chunks sized to the
+    free memory, recomputed chunk by chunk in the backward).  The FP64 chain checks the
+    first 24 strokes on the same canvas."""
     import torch
     from footile_gb300 import _abi, workloads
-    from footile_gb300.adjoint import Adjoint, pack_coverage, stroke_composite_grads
+    from footile_gb300.adjoint import StrokeComposite, pack_coverage, stroke_composite_grads
     paths_ops, _, clrs, _ = workloads.strokes_16384(n_paths=n_paths, side=side)
     ops, paths, _ = pack_coverage(paths_ops, [side] * n_paths)
     clr = clrs.astype(np.float32) / 255.0
@@ -522,29 +523,31 @@ def extra_adjoint_composite(ctx, stream, dev, cpu=True, n_paths=1024, side=512, 
     clr_d = torch.from_numpy(clr).to(dev)
     tgt_d = torch.from_numpy(target).to(dev)
     ctx.set_join(_abi.JOIN_MITER, 4.0)
-    adj = Adjoint(ctx)
-    stroke_composite_grads(ctx, ops_d, paths, clr_d, side, side, tgt_d, adj)  # warm-up (allocations)
+    comp = StrokeComposite(ctx)
+    stroke_composite_grads(ctx, ops_d, paths, clr_d, side, side, tgt_d, comp)  # warm-up (allocations)
     runs = []
     t0 = time.perf_counter()
     for _ in range(reps):
-        loss, out, g_ops, g_w, ms = stroke_composite_grads(ctx, ops_d, paths, clr_d, side, side, tgt_d, adj)
+        loss, out, g_ops, g_w, ms = stroke_composite_grads(ctx, ops_d, paths, clr_d, side, side, tgt_d, comp)
         runs.append(ms)
     wall = (time.perf_counter() - t0) / reps * 1e3
-    res = {"workload": "strokes composite adjoint (1,024 strokes, 8..64 cubics, width 1..12, Miter(4), "
-                       "ordered SrcOver on one 512x512 canvas, L2 loss vs RGBA target)",
-           "coverage_fwd_ms": float(np.median([r["coverage_fwd_ms"] for r in runs])),
-           "srcover_fwd_ms": float(np.median([r["srcover_fwd_ms"] for r in runs])),
+    st = comp.status()
+    res = {"workload": f"strokes composite adjoint ({n_paths:,} strokes, 8..64 cubics, width 1..12, Miter(4), "
+                       f"ordered SrcOver on one {side}x{side} canvas, L2 loss vs RGBA target)",
+           "fwd_ms": float(np.median([r["fwd_ms"] for r in runs])),
            "bwd_ms": float(np.median([r["bwd_ms"] for r in runs])), "wall_ms_per_fwd_bwd": wall,
-           "loss": float(loss)}
-    res["bwd_over_fwd"] = res["bwd_ms"] / (res["coverage_fwd_ms"] + res["srcover_fwd_ms"])
+           "chunk": runs[-1]["chunk"], "n_chunks": -(-n_paths // runs[-1]["chunk"]),
+           "paths_status_ok": int((st == _abi.OK).sum()), "loss": float(loss),
+           "grad_finite": bool(torch.isfinite(g_ops).all().item() and torch.isfinite(g_w).all().item())}
+    res["bwd_over_fwd"] = res["bwd_ms"] / res["fwd_ms"]
+    comp.close()
     if cpu:
-        # FP64 chain on the first 24 strokes (its own small composite)
+        # FP64 chain on the first 24 strokes (their own composite on the same canvas)
         import oracle
-        from footile_gb300.adjoint import pack_coverage as pc
         k = 24
-        o2, p2, _ = pc(paths_ops[:k], [side] * k)
+        o2, p2, _ = pack_coverage(paths_ops[:k], [side] * k)
         o2_d = torch.from_numpy(o2.view(np.uint8).copy()).to(dev)
-        l2, out2, g2, gw2, _ = stroke_composite_grads(ctx, o2_d, p2, clr_d[:k].contiguous(), side, side, tgt_d, adj)
+        l2, out2, g2, gw2, _ = stroke_composite_grads(ctx, o2_d, p2, clr_d[:k].contiguous(), side, side, tgt_d)
         t1 = time.perf_counter()
         l64, C64, g64, gw64 = oracle.adj_stroke_composite(o2, p2, clr[:k].astype(np.float64), side, side,
                                                           target.astype(np.float64))
@@ -552,7 +555,7 @@ def extra_adjoint_composite(ctx, stream, dev, cpu=True, n_paths=1024, side=512, 
         scale = max(np.abs(g64).max(), np.abs(gw64).max())
         res["max_rel_err_vs_fp64_24_strokes"] = float(max(np.abs(g2.cpu().numpy() - g64).max(),
                                                           np.abs(gw2.cpu().numpy() - gw64).max()) / scale)
-    adj.close()
+        res["max_abs_canvas_err_24_strokes"] = float(np.abs(out2.cpu().numpy() - C64).max())
     return res
 
 
@@ -708,7 +711,7 @@ def run_ours(args):
         for name, fn in (("single_path_256", extra_single), ("scene_4096", extra_scene),
                          ("strokes_16384", extra_strokes), ("adjoint_cubics_1024", extra_adjoint),
                          ("adjoint_strokes_1024", extra_adjoint_strokes),
-                         ("adjoint_composite_1024", extra_adjoint_composite)):
+                         ("adjoint_composite_16384", extra_adjoint_composite)):
             try:
                 extras[name] = fn(ctx, stream, dev, cpu=(world == 1 and not args.no_cpu))
             except Exception as e:  # report, never hide, a failing secondary workload

@@ -64,6 +64,12 @@ def load(auto_build=True):
             "ft_convert": ([P, i32, P, u32, i32, P, u32, u32, u32, i32], ctypes.c_int),
             "ft_srcover_forward": ([P, P, u32, u64, P, P, P, u32], ctypes.c_int),
             "ft_srcover_backward": ([P, P, u32, u64, P, P, P, P, P, u32], ctypes.c_int),
+            "ft_stroke_composite_forward": ([P, P, u32, P, u32, P, u32, u32, P, P, u32, i32, ctypes.POINTER(P)],
+                                            ctypes.c_int),
+            "ft_stroke_composite_backward": ([P, P, P, P, P, P, i32], ctypes.c_int),
+            "ft_stroke_composite_status": ([P, P, P, u32], ctypes.c_int),
+            "ft_stroke_composite_chunk": ([P], u32),
+            "ft_stroke_composite_destroy": ([P], None),
             "ft_get_tuning": ([P, P], ctypes.c_int),
             "ft_autotune_batch": ([P, i32, i32, P, u32, P, u32, i32, P, u64, ctypes.c_char_p, P,
                                    ctypes.POINTER(f32)], ctypes.c_int),
@@ -85,7 +91,9 @@ def exported_symbols():
         "ft_batch_create", "ft_batch_launch", "ft_batch_launch_status", "ft_batch_destroy",
         "ft_composite_batch", "ft_fill_noalloc", "ft_adjoint_forward", "ft_adjoint_backward", "ft_adjoint_status",
         "ft_adjoint_destroy", "ft_set_tuning", "ft_get_tuning", "ft_autotune_batch",
-        "ft_convert", "ft_srcover_forward", "ft_srcover_backward")]
+        "ft_convert", "ft_srcover_forward", "ft_srcover_backward", "ft_stroke_composite_forward",
+        "ft_stroke_composite_backward", "ft_stroke_composite_status", "ft_stroke_composite_chunk",
+        "ft_stroke_composite_destroy")]
 
 
 class Tuning(ctypes.Structure):

@@ -166,37 +166,93 @@ def srcover_backward(ctx, cov, n_layers, plane, clr, grad_out, grad_cov, init=No
     return grad_cov
 
 
-def stroke_composite_grads(ctx, ops_dev, paths, clr_dev, width, height, target_dev, adj=None):
+class StrokeComposite:
+    """Saved state of the differentiable ordered composite of strokes on one canvas
+    (`ft_stroke_composite_forward` / `ft_stroke_composite_backward`): the strokes are
+    covered in chunks, only the canvas before each chunk is kept, and the backward
+    recomputes coverage chunk by chunk.  Numpy arrays or CUDA tensors (all alike)."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        self.h = ctypes.c_void_p()
+        self.n_paths = 0
+
+    def forward(self, ops, paths, clr, width, height, out, init=None, chunk=0):
+        """C_N of the strokes `paths` (op ranges and starting pen widths) SrcOver'd in
+        order with premultiplied colours `clr` ((n, 4) f32) on a width x height canvas
+        starting at `init` ((w*h, 4) f32, None: 0), into `out` ((w*h, 4) f32)."""
+        paths = np.ascontiguousarray(paths, dtype=_abi.PATH_DTYPE)
+        dev = hasattr(out, "data_ptr")
+        if dev:
+            n_ops = ops.numel() * ops.element_size() // 32
+        else:
+            ops = np.ascontiguousarray(ops, dtype=_abi.OP_DTYPE)
+            clr = np.ascontiguousarray(clr, dtype=np.float32)
+            init = None if init is None else np.ascontiguousarray(init, dtype=np.float32)
+            n_ops = len(ops)
+        wait = self.ctx.torch_fence() if dev else False
+        self.ctx.check(self.ctx.L.ft_stroke_composite_forward(
+            self.ctx.h, _ptr(ops), n_ops, _ptr(paths), len(paths), _ptr(clr), int(width), int(height), _ptr(init),
+            _ptr(out), int(chunk), _abi.DEVICE if dev else _abi.HOST, ctypes.byref(self.h)))
+        self.n_paths = len(paths)
+        if wait:
+            self.ctx.sync()
+        return out
+
+    def backward(self, grad_out, grad_ops, grad_width=None, grad_init=None):
+        """dLoss/d(op floats) into `grad_ops` ((n_ops, 6) f32), dLoss/d(starting pen
+        width) into `grad_width` and dLoss/dC_0 into `grad_init`, given dLoss/dC_N."""
+        dev = hasattr(grad_out, "data_ptr")
+        wait = self.ctx.torch_fence() if dev else False
+        self.ctx.check(self.ctx.L.ft_stroke_composite_backward(
+            self.ctx.h, self.h, _ptr(grad_out), _ptr(grad_ops), _ptr(grad_width), _ptr(grad_init),
+            _abi.DEVICE if dev else _abi.HOST))
+        if wait:
+            self.ctx.sync()
+        return grad_ops
+
+    @property
+    def chunk(self):
+        return int(self.ctx.L.ft_stroke_composite_chunk(self.h))
+
+    def status(self):
+        st = np.zeros(self.n_paths, dtype=np.int32)
+        self.ctx.check(self.ctx.L.ft_stroke_composite_status(self.ctx.h, self.h, _ptr(st), self.n_paths))
+        return st
+
+    def close(self):
+        if self.h:
+            load().ft_stroke_composite_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def stroke_composite_grads(ctx, ops_dev, paths, clr_dev, width, height, target_dev, comp=None, chunk=0):
     """Forward and backward of the differentiable ordered composite of strokes on one
-    canvas: coverage of every stroke over the canvas (`ft_adjoint_forward`, stroke = 1),
-    SrcOver in order, loss sum((C_N - target)^2), then the gradients of the op floats
-    (PenWidth ops in column 0) and of the starting pen widths.  `paths` describe one
-    width x height f32 plane per stroke, back to back (pack_coverage).  Returns
+    canvas (StrokeComposite), loss sum((C_N - target)^2): the gradients of the op floats
+    (PenWidth ops in column 0) and of the starting pen widths.  Device tensors.  Returns
     (loss, C_N, grad_ops, grad_width, timings in ms)."""
     import torch
-    n = len(paths)
-    plane = width * height
     dev = ops_dev.device
-    adj = adj or Adjoint(ctx)
-    cov = torch.empty(n * plane, dtype=torch.float32, device=dev)
-    out = torch.empty((plane, 4), dtype=torch.float32, device=dev)
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+    comp = comp or StrokeComposite(ctx)
+    out = torch.empty((width * height, 4), dtype=torch.float32, device=dev)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
     stream = torch.cuda.current_stream(dev)
     ev[0].record(stream)
-    adj.forward(0, ops_dev, paths, cov, stroke=True)
+    comp.forward(ops_dev, paths, clr_dev, width, height, out, chunk=chunk)
     ev[1].record(stream)
-    srcover_forward(ctx, cov, n, plane, clr_dev, out)
-    ev[2].record(stream)
     g_out = 2.0 * (out - target_dev)
     loss = ((out - target_dev) ** 2).sum()
-    g_cov = torch.empty_like(cov)
-    ev[3].record(stream)
-    srcover_backward(ctx, cov, n, plane, clr_dev, g_out, g_cov)
     g_ops = torch.empty((ops_dev.numel() * ops_dev.element_size() // 32, 6), dtype=torch.float32, device=dev)
-    g_w = torch.empty(n, dtype=torch.float32, device=dev)
-    adj.backward(g_cov, g_ops, g_w)
-    ev[4].record(stream)
+    g_w = torch.empty(len(paths), dtype=torch.float32, device=dev)
+    ev[2].record(stream)
+    comp.backward(g_out, g_ops, g_w)
+    ev[3].record(stream)
     torch.cuda.synchronize()
-    ms = {"coverage_fwd_ms": ev[0].elapsed_time(ev[1]), "srcover_fwd_ms": ev[1].elapsed_time(ev[2]),
-          "bwd_ms": ev[3].elapsed_time(ev[4])}
+    ms = {"fwd_ms": ev[0].elapsed_time(ev[1]), "bwd_ms": ev[2].elapsed_time(ev[3]), "chunk": comp.chunk}
     return loss, out, g_ops, g_w, ms

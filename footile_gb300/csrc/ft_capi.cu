@@ -926,6 +926,7 @@ static bool tune_lookup(const char* path, const std::string& key, ft_tuning* t) 
 struct ft_adjoint {
     ft_ctx* ctx = nullptr;
     DevBuf ops, paths, area, status, scratch, cov, gcov, gops, gwidth;
+    const ft_op* ops_d = nullptr;  // device ops the kernels read (`ops` or a caller's copy)
     std::vector<ft_path_desc> h_paths;
     uint32_t n_ops = 0, n_paths = 0;
     uint64_t cov_bytes = 0;
@@ -946,6 +947,108 @@ static int adjoint_check_path(ft_ctx* c, const ft_path_desc& d, uint64_t cov_byt
     if ((uint64_t)d.stride < 4ull * d.width) return fail(c, FT_ERR_ARG, "coverage stride below 4 * width");
     const uint64_t end = d.raster_offset + (uint64_t)d.stride * (d.height - 1) + 4ull * d.width;
     if (end > cov_bytes) return fail(c, FT_ERR_ARG, "coverage outside the buffer");
+    return FT_OK;
+}
+
+// Plotter settings a coverage pass runs with (the context's at the caller's forward).
+struct AdjSettings {
+    int join = FT_JOIN_MITER;
+    float miter_limit = 4.0f;
+    float xf[6] = {1, 0, 0, 0, 1, 0};
+    float tol_sq = 0.09f;
+};
+
+static AdjSettings ctx_settings(const ft_ctx* c) {
+    AdjSettings s;
+    s.join = c->join;
+    s.miter_limit = c->miter_limit;
+    for (int k = 0; k < 6; k++) s.xf[k] = c->xf[k];
+    const float t = std::max(c->tolerance, 0.01f);
+    s.tol_sq = t * t;
+    return s;
+}
+
+static fta::AParams adjoint_params(const ft_adjoint* a) {
+    fta::AParams p{};
+    p.ops = a->ops_d;
+    p.paths = static_cast<const ft_path_desc*>(a->paths.p);
+    p.n_paths = a->n_paths;
+    p.area = static_cast<float*>(a->area.p);
+    p.status = static_cast<int*>(a->status.p);
+    p.scratch = static_cast<unsigned char*>(a->scratch.p);
+    for (int k = 0; k < 6; k++) p.xf[k] = a->xf[k];
+    p.tol_sq = a->tol_sq;
+    p.rule = a->rule;
+    p.stroke = a->stroke;
+    p.join = a->join;
+    p.miter_limit = a->miter_limit;
+    return p;
+}
+
+// Coverage forward of checked paths (host descriptors) over device ops `ops_d` into
+// device coverage `cov_d`: sizes the saved state, uploads the descriptors, resets the
+// status and launches; `events` brackets the launch with the context's timing events.
+static int adjoint_forward_dev(ft_ctx* c, ft_adjoint* a, int stroke, int rule, const ft_op* ops_d,
+                               uint32_t n_ops_total, const ft_path_desc* paths, uint32_t n_paths, float* cov_d,
+                               uint64_t cov_bytes, const AdjSettings& set, bool events) {
+    a->ready = false;
+    a->rule = rule;
+    a->stroke = stroke ? 1 : 0;
+    a->join = set.join;
+    a->miter_limit = set.miter_limit;
+    a->n_ops = n_ops_total;
+    a->n_paths = n_paths;
+    a->cov_bytes = cov_bytes;
+    a->ops_d = ops_d;
+    a->h_paths.assign(paths, paths + n_paths);
+    for (int k = 0; k < 6; k++) a->xf[k] = set.xf[k];
+    a->tol_sq = set.tol_sq;
+    FT_CU(a->paths.ensure(sizeof(ft_path_desc) * std::max(n_paths, 1u)), "alloc paths");
+    FT_CU(a->status.ensure(sizeof(int32_t) * std::max(n_paths, 1u)), "alloc status");
+    FT_CU(a->area.ensure(std::max<uint64_t>(cov_bytes, 4)), "alloc winding area");
+    // strokes: the stroker runs on one thread per CTA over a 14 MB scratch, two CTAs per SM
+    const int bps_f = a->stroke ? 2 : fta::adjoint_blocks_per_sm(false);
+    const int bps_b = a->stroke ? 2 : fta::adjoint_blocks_per_sm(true);
+    a->grid_f = (int)std::max(1u, std::min<uint32_t>(n_paths, (uint32_t)(bps_f * c->sm_count)));
+    a->grid_b = (int)std::max(1u, std::min<uint32_t>(n_paths, (uint32_t)(bps_b * c->sm_count)));
+    const size_t per_cta = a->stroke ? fta::A_SCRATCH_STROKE : fta::A_SCRATCH_PER_CTA;
+    FT_CU(a->scratch.ensure(per_cta * (size_t)std::max(a->grid_f, a->grid_b)), "alloc scratch");
+    if (n_paths)
+        FT_CU(cudaMemcpyAsync(a->paths.p, paths, sizeof(ft_path_desc) * n_paths, cudaMemcpyHostToDevice, c->stream),
+              "upload paths");
+    FT_CU(cudaMemsetAsync(a->status.p, 0, sizeof(int32_t) * std::max(n_paths, 1u), c->stream), "reset status");
+    fta::AParams p = adjoint_params(a);
+    p.cov = cov_d;
+    if (events) FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
+    if (n_paths) {
+        FT_CU(fta::launch_adjoint(false, p, a->grid_f, c->stream), "launch adjoint forward");
+        c->launches++;
+    }
+    if (events) {
+        FT_CU(cudaEventRecord(c->ev1, c->stream), "event");
+        c->timed = true;
+    }
+    a->ready = true;
+    return FT_OK;
+}
+
+// Coverage backward into device gradients; grad_ops and grad_width accumulate (the
+// caller zeroes them).
+static int adjoint_backward_dev(ft_ctx* c, ft_adjoint* a, const float* gcov_d, float* gops_d, float* gw_d,
+                                bool events) {
+    fta::AParams p = adjoint_params(a);
+    p.grad_cov = gcov_d;
+    p.grad_ops = gops_d;
+    p.grad_width = gw_d;
+    if (events) FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
+    if (a->n_paths) {
+        FT_CU(fta::launch_adjoint(true, p, a->grid_b, c->stream), "launch adjoint backward");
+        c->launches++;
+    }
+    if (events) {
+        FT_CU(cudaEventRecord(c->ev1, c->stream), "event");
+        c->timed = true;
+    }
     return FT_OK;
 }
 
@@ -975,67 +1078,23 @@ FT_API int ft_adjoint_forward(ft_ctx* c, int32_t stroke, int32_t rule, const ft_
         *saved = a;
     }
     a->ready = false;
-    a->rule = rule;
-    a->stroke = stroke ? 1 : 0;
-    a->join = c->join;
-    a->miter_limit = c->miter_limit;
-    a->n_ops = n_ops_total;
-    a->n_paths = n_paths;
-    a->cov_bytes = cov_bytes;
-    a->h_paths.assign(paths, paths + n_paths);
-    for (int k = 0; k < 6; k++) a->xf[k] = c->xf[k];
-    const float t = std::max(c->tolerance, 0.01f);
-    a->tol_sq = t * t;
     FT_CU(a->ops.ensure(sizeof(ft_op) * std::max(n_ops_total, 1u)), "alloc ops");
-    FT_CU(a->paths.ensure(sizeof(ft_path_desc) * std::max(n_paths, 1u)), "alloc paths");
-    FT_CU(a->status.ensure(sizeof(int32_t) * std::max(n_paths, 1u)), "alloc status");
-    FT_CU(a->area.ensure(std::max<uint64_t>(cov_bytes, 4)), "alloc winding area");
-    // strokes: the stroker runs on one thread per CTA over a 14 MB scratch, two CTAs per SM
-    const int bps_f = a->stroke ? 2 : fta::adjoint_blocks_per_sm(false);
-    const int bps_b = a->stroke ? 2 : fta::adjoint_blocks_per_sm(true);
-    a->grid_f = (int)std::max(1u, std::min<uint32_t>(n_paths, (uint32_t)(bps_f * c->sm_count)));
-    a->grid_b = (int)std::max(1u, std::min<uint32_t>(n_paths, (uint32_t)(bps_b * c->sm_count)));
-    const size_t per_cta = a->stroke ? fta::A_SCRATCH_STROKE : fta::A_SCRATCH_PER_CTA;
-    FT_CU(a->scratch.ensure(per_cta * (size_t)std::max(a->grid_f, a->grid_b)), "alloc scratch");
     if (n_ops_total)
         FT_CU(cudaMemcpyAsync(a->ops.p, ops, sizeof(ft_op) * n_ops_total,
                               where == FT_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, c->stream),
               "copy ops");
-    if (n_paths)
-        FT_CU(cudaMemcpyAsync(a->paths.p, paths, sizeof(ft_path_desc) * n_paths, cudaMemcpyHostToDevice, c->stream),
-              "upload paths");
-    FT_CU(cudaMemsetAsync(a->status.p, 0, sizeof(int32_t) * std::max(n_paths, 1u), c->stream), "reset status");
     float* cov_d = cov;
     if (where == FT_HOST) {
         FT_CU(a->cov.ensure(std::max<uint64_t>(cov_bytes, 4)), "alloc coverage");
         cov_d = static_cast<float*>(a->cov.p);
     }
-    fta::AParams p{};
-    p.ops = static_cast<const ft_op*>(a->ops.p);
-    p.paths = static_cast<const ft_path_desc*>(a->paths.p);
-    p.n_paths = n_paths;
-    p.cov = cov_d;
-    p.area = static_cast<float*>(a->area.p);
-    p.status = static_cast<int*>(a->status.p);
-    p.scratch = static_cast<unsigned char*>(a->scratch.p);
-    for (int k = 0; k < 6; k++) p.xf[k] = a->xf[k];
-    p.tol_sq = a->tol_sq;
-    p.rule = rule;
-    p.stroke = a->stroke;
-    p.join = a->join;
-    p.miter_limit = a->miter_limit;
-    FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
-    if (n_paths) {
-        FT_CU(fta::launch_adjoint(false, p, a->grid_f, c->stream), "launch adjoint forward");
-        c->launches++;
-    }
-    FT_CU(cudaEventRecord(c->ev1, c->stream), "event");
-    c->timed = true;
+    int st = adjoint_forward_dev(c, a, stroke, rule, static_cast<const ft_op*>(a->ops.p), n_ops_total, paths,
+                                 n_paths, cov_d, cov_bytes, ctx_settings(c), true);
+    if (st != FT_OK) return st;
     if (where == FT_HOST) {
         if (cov_bytes) FT_CU(cudaMemcpyAsync(cov, cov_d, cov_bytes, cudaMemcpyDeviceToHost, c->stream), "download coverage");
         FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
     }
-    a->ready = true;
     return FT_OK;
 }
 
@@ -1072,29 +1131,8 @@ FT_API int ft_adjoint_backward(ft_ctx* c, ft_adjoint* a, const float* grad_cov, 
         }
         FT_CU(cudaMemsetAsync(gw_d, 0, sizeof(float) * a->n_paths, c->stream), "reset width gradient");
     }
-    fta::AParams p{};
-    p.ops = static_cast<const ft_op*>(a->ops.p);
-    p.paths = static_cast<const ft_path_desc*>(a->paths.p);
-    p.n_paths = a->n_paths;
-    p.area = static_cast<float*>(a->area.p);
-    p.grad_cov = gcov_d;
-    p.grad_ops = gops_d;
-    p.status = static_cast<int*>(a->status.p);
-    p.scratch = static_cast<unsigned char*>(a->scratch.p);
-    for (int k = 0; k < 6; k++) p.xf[k] = a->xf[k];
-    p.tol_sq = a->tol_sq;
-    p.rule = a->rule;
-    p.stroke = a->stroke;
-    p.join = a->join;
-    p.miter_limit = a->miter_limit;
-    p.grad_width = gw_d;
-    FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
-    if (a->n_paths) {
-        FT_CU(fta::launch_adjoint(true, p, a->grid_b, c->stream), "launch adjoint backward");
-        c->launches++;
-    }
-    FT_CU(cudaEventRecord(c->ev1, c->stream), "event");
-    c->timed = true;
+    int st = adjoint_backward_dev(c, a, gcov_d, gops_d, gw_d, true);
+    if (st != FT_OK) return st;
     if (where == FT_HOST) {
         if (grad_width && a->n_paths)
             FT_CU(cudaMemcpyAsync(grad_width, gw_d, sizeof(float) * a->n_paths, cudaMemcpyDeviceToHost, c->stream),
@@ -1208,6 +1246,229 @@ FT_API int ft_srcover_backward(ft_ctx* c, const float* cov, uint32_t n_layers, u
                                float* grad_init, uint32_t n_px) {
     return srcover_call(c, true, cov, n_layers, plane_floats, clr, init, nullptr, grad_out, grad_cov, grad_init,
                         n_px);
+}
+
+// ------------------------------------------------ differentiable ordered composite
+}  // extern "C"
+
+// Saved state between ft_stroke_composite_forward and ft_stroke_composite_backward:
+// copies of the ops and colours, the canvas before each chunk of strokes, and the
+// coverage of the chunk last covered.
+struct ft_composite_adjoint {
+    ft_ctx* ctx = nullptr;
+    ft_adjoint* adj = nullptr;  // winding area and scratch of the chunk in `cov`
+    DevBuf ops, clr, prefix, cov, gcov, gbuf, status, gops, gwidth;
+    std::vector<ft_path_desc> h_paths, descs;
+    AdjSettings set;
+    uint32_t n_ops = 0, n_paths = 0, width = 0, height = 0, chunk = 1, n_chunks = 0;
+    int fresh = -1;  // chunk whose coverage `cov` and `adj` hold
+    bool ready = false;
+    uint64_t plane_bytes() const { return 4ull * width * height; }
+    uint32_t chunk_begin(uint32_t ch) const { return ch * chunk; }
+    uint32_t chunk_size(uint32_t ch) const { return std::min(chunk, n_paths - ch * chunk); }
+    float4* prefix_at(uint32_t ch) const {
+        return static_cast<float4*>(prefix.p) + (size_t)ch * width * height;
+    }
+};
+
+// Coverage of chunk `ch` into `cov` (and the winding area into the inner saved state).
+static int composite_cover(ft_ctx* c, ft_composite_adjoint* s, uint32_t ch) {
+    const uint32_t b = s->chunk_begin(ch), k = s->chunk_size(ch);
+    s->descs.resize(k);
+    for (uint32_t j = 0; j < k; j++) {
+        ft_path_desc d = s->h_paths[b + j];
+        d.width = s->width;
+        d.height = s->height;
+        d.raster_offset = (uint64_t)j * s->plane_bytes();
+        d.stride = 4 * s->width;
+        s->descs[j] = d;
+    }
+    s->fresh = -1;
+    int st = adjoint_forward_dev(c, s->adj, 1, FT_NONZERO, static_cast<const ft_op*>(s->ops.p), s->n_ops,
+                                 s->descs.data(), k, static_cast<float*>(s->cov.p), (uint64_t)k * s->plane_bytes(),
+                                 s->set, false);
+    if (st == FT_OK) s->fresh = (int)ch;
+    return st;
+}
+
+extern "C" {
+
+FT_API int ft_stroke_composite_forward(ft_ctx* c, const ft_op* ops, uint32_t n_ops_total, const ft_path_desc* paths,
+                                       uint32_t n_paths, const float* clr, uint32_t width, uint32_t height,
+                                       const float* init, float* out, uint32_t chunk, int32_t where,
+                                       ft_composite_adjoint** saved) {
+    if (!c || !saved) return FT_ERR_ARG;
+    if (where != FT_HOST && where != FT_DEVICE) return fail(c, FT_ERR_ARG, "bad location");
+    if (width == 0 || height == 0) return fail(c, FT_ERR_ARG, "empty canvas");
+    if (width > FT_MAX_WIDTH) return fail(c, FT_ERR_CAP, "canvas wider than FT_MAX_WIDTH");
+    const uint64_t n_px = (uint64_t)width * height;
+    if (n_px > 0xFFFFFFFFull) return fail(c, FT_ERR_CAP, "canvas of more than 2^32 pixels");
+    if ((n_paths && (!paths || !clr)) || (n_ops_total && !ops) || !out) return fail(c, FT_ERR_ARG, "null pointer");
+    for (uint32_t i = 0; i < n_paths; i++)
+        if ((uint64_t)paths[i].op_begin + paths[i].n_ops > n_ops_total)
+            return fail(c, FT_ERR_ARG, "path ops out of range");
+    if (where == FT_DEVICE) {
+        const uintptr_t a16 = reinterpret_cast<uintptr_t>(ops) | reinterpret_cast<uintptr_t>(clr) |
+                              reinterpret_cast<uintptr_t>(init) | reinterpret_cast<uintptr_t>(out);
+        if (a16 & 15) return fail(c, FT_ERR_ARG, "device ops, colours and canvases need 16-byte alignment");
+    } else if (!valid_ops_host(ops, n_ops_total)) {
+        return fail(c, FT_ERR_ARG, "unknown path op kind");
+    }
+    FT_CU(cudaSetDevice(c->device), "set device");
+    ft_composite_adjoint* s = *saved;
+    if (!s) {
+        s = new ft_composite_adjoint();
+        s->ctx = c;
+        *saved = s;
+    }
+    if (s->ctx != c) return fail(c, FT_ERR_ARG, "saved state belongs to another context");
+    s->ready = false;
+    s->fresh = -1;
+    s->set = ctx_settings(c);
+    s->n_ops = n_ops_total;
+    s->n_paths = n_paths;
+    s->width = width;
+    s->height = height;
+    s->h_paths.assign(paths, paths + n_paths);
+    const uint64_t plane = s->plane_bytes();
+    if (chunk == 0) {
+        // coverage, winding area and coverage gradient of a chunk in at most 40 % of the
+        // free memory (96 GB at most), equal chunks
+        size_t free_b = 0, total_b = 0;
+        FT_CU(cudaMemGetInfo(&free_b, &total_b), "memory info");
+        const uint64_t budget = std::min<uint64_t>(free_b / 5 * 2, 96ull << 30);
+        const uint64_t kmax = std::max<uint64_t>(1, budget / (3 * plane));
+        const uint64_t nch = (std::max(n_paths, 1u) + kmax - 1) / kmax;
+        chunk = (uint32_t)((std::max(n_paths, 1u) + nch - 1) / nch);
+    }
+    s->chunk = std::max(1u, std::min(chunk, std::max(n_paths, 1u)));
+    s->n_chunks = (n_paths + s->chunk - 1) / s->chunk;
+    if (!s->adj) {
+        s->adj = new ft_adjoint();
+        s->adj->ctx = c;
+    }
+    FT_CU(s->ops.ensure(sizeof(ft_op) * std::max(n_ops_total, 1u)), "alloc ops");
+    FT_CU(s->clr.ensure(16ull * std::max(n_paths, 1u)), "alloc colours");
+    FT_CU(s->status.ensure(4ull * std::max(n_paths, 1u)), "alloc status");
+    FT_CU(s->prefix.ensure(16ull * n_px * (s->n_chunks + 1)), "alloc canvas before each chunk");
+    FT_CU(s->cov.ensure(std::max<uint64_t>(plane * s->chunk, 4)), "alloc chunk coverage");
+    const cudaMemcpyKind in = where == FT_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    if (n_ops_total) FT_CU(cudaMemcpyAsync(s->ops.p, ops, sizeof(ft_op) * n_ops_total, in, c->stream), "copy ops");
+    if (n_paths) FT_CU(cudaMemcpyAsync(s->clr.p, clr, 16ull * n_paths, in, c->stream), "copy colours");
+    if (init)
+        FT_CU(cudaMemcpyAsync(s->prefix.p, init, 16ull * n_px, in, c->stream), "copy initial canvas");
+    else
+        FT_CU(cudaMemsetAsync(s->prefix.p, 0, 16ull * n_px, c->stream), "clear initial canvas");
+    const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((n_px + 255) / 256, (uint64_t)c->sm_count * 16));
+    FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
+    for (uint32_t ch = 0; ch < s->n_chunks; ch++) {
+        int st = composite_cover(c, s, ch);
+        if (st != FT_OK) return st;
+        const uint32_t b = s->chunk_begin(ch), k = s->chunk_size(ch);
+        FT_CU(cudaMemcpyAsync(static_cast<int32_t*>(s->status.p) + b, s->adj->status.p, 4ull * k,
+                              cudaMemcpyDeviceToDevice, c->stream),
+              "copy status");
+        FT_CU(ftc::launch_srcover(false, static_cast<const float*>(s->cov.p), k, plane / 4,
+                                  static_cast<const float4*>(s->clr.p) + b, s->prefix_at(ch), s->prefix_at(ch + 1),
+                                  nullptr, nullptr, nullptr, (uint32_t)n_px, grid, c->stream),
+              "launch SrcOver");
+        c->launches++;
+    }
+    FT_CU(cudaEventRecord(c->ev1, c->stream), "event");
+    c->timed = true;
+    FT_CU(cudaMemcpyAsync(out, s->prefix_at(s->n_chunks), 16ull * n_px,
+                          where == FT_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, c->stream),
+          "copy canvas");
+    if (where == FT_HOST) FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
+    s->ready = true;
+    return FT_OK;
+}
+
+FT_API int ft_stroke_composite_backward(ft_ctx* c, ft_composite_adjoint* s, const float* grad_out, float* grad_ops,
+                                        float* grad_width, float* grad_init, int32_t where) {
+    if (!c || !s) return FT_ERR_ARG;
+    if (!s->ready) return fail(c, FT_ERR_ARG, "backward without a forward");
+    if (s->ctx != c) return fail(c, FT_ERR_ARG, "saved state belongs to another context");
+    if (where != FT_HOST && where != FT_DEVICE) return fail(c, FT_ERR_ARG, "bad location");
+    if (!grad_out || (s->n_ops && !grad_ops)) return fail(c, FT_ERR_ARG, "null pointer");
+    if (where == FT_DEVICE) {
+        const uintptr_t a16 = reinterpret_cast<uintptr_t>(grad_out) | reinterpret_cast<uintptr_t>(grad_init);
+        if ((a16 & 15) || (reinterpret_cast<uintptr_t>(grad_ops) & 3) || (reinterpret_cast<uintptr_t>(grad_width) & 3))
+            return fail(c, FT_ERR_ARG, "device canvases need 16-byte alignment, gradients 4-byte alignment");
+    }
+    FT_CU(cudaSetDevice(c->device), "set device");
+    const uint64_t n_px = (uint64_t)s->width * s->height, plane = s->plane_bytes();
+    const size_t gops_bytes = 24ull * s->n_ops;
+    FT_CU(s->gcov.ensure(std::max<uint64_t>(plane * s->chunk, 4)), "alloc chunk coverage gradient");
+    FT_CU(s->gbuf.ensure(32ull * n_px), "alloc canvas gradients");
+    float* gops_d = grad_ops;
+    float* gw_d = grad_width;
+    if (where == FT_HOST || !grad_ops) {
+        FT_CU(s->gops.ensure(std::max<size_t>(gops_bytes, 4)), "alloc op gradient");
+        gops_d = static_cast<float*>(s->gops.p);
+    }
+    if (where == FT_HOST || !grad_width) {
+        FT_CU(s->gwidth.ensure(4ull * std::max(s->n_paths, 1u)), "alloc width gradient");
+        gw_d = static_cast<float*>(s->gwidth.p);
+    }
+    float4* g_cur = static_cast<float4*>(s->gbuf.p);
+    float4* g_next = g_cur + n_px;
+    FT_CU(cudaMemcpyAsync(g_cur, grad_out, 16ull * n_px,
+                          where == FT_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, c->stream),
+          "copy canvas gradient");
+    if (gops_bytes) FT_CU(cudaMemsetAsync(gops_d, 0, gops_bytes, c->stream), "reset op gradient");
+    if (s->n_paths) FT_CU(cudaMemsetAsync(gw_d, 0, 4ull * s->n_paths, c->stream), "reset width gradient");
+    const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((n_px + 255) / 256, (uint64_t)c->sm_count * 16));
+    FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
+    for (uint32_t ch = s->n_chunks; ch-- > 0;) {
+        if (s->fresh != (int)ch) {  // recompute this chunk's coverage
+            int st = composite_cover(c, s, ch);
+            if (st != FT_OK) return st;
+        }
+        const uint32_t b = s->chunk_begin(ch), k = s->chunk_size(ch);
+        FT_CU(ftc::launch_srcover(true, static_cast<const float*>(s->cov.p), k, plane / 4,
+                                  static_cast<const float4*>(s->clr.p) + b, s->prefix_at(ch), nullptr, g_cur,
+                                  static_cast<float*>(s->gcov.p), g_next, (uint32_t)n_px, grid, c->stream),
+              "launch SrcOver adjoint");
+        c->launches++;
+        int st = adjoint_backward_dev(c, s->adj, static_cast<const float*>(s->gcov.p), gops_d, gw_d + b, false);
+        if (st != FT_OK) return st;
+        std::swap(g_cur, g_next);
+    }
+    FT_CU(cudaEventRecord(c->ev1, c->stream), "event");
+    c->timed = true;
+    const cudaMemcpyKind outk = where == FT_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    if (grad_init) FT_CU(cudaMemcpyAsync(grad_init, g_cur, 16ull * n_px, outk, c->stream), "copy initial gradient");
+    if (where == FT_HOST) {
+        if (gops_bytes) FT_CU(cudaMemcpyAsync(grad_ops, gops_d, gops_bytes, outk, c->stream), "download op gradient");
+        if (grad_width && s->n_paths)
+            FT_CU(cudaMemcpyAsync(grad_width, gw_d, 4ull * s->n_paths, outk, c->stream), "download width gradient");
+        FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
+    }
+    return FT_OK;
+}
+
+FT_API int ft_stroke_composite_status(ft_ctx* c, ft_composite_adjoint* s, int32_t* status, uint32_t n) {
+    if (!c || !s || (n && !status)) return FT_ERR_ARG;
+    FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
+    const uint32_t k = std::min(n, s->ready ? s->n_paths : 0u);
+    if (k) FT_CU(cudaMemcpy(status, s->status.p, sizeof(int32_t) * k, cudaMemcpyDeviceToHost), "status");
+    for (uint32_t i = k; i < n; i++) status[i] = FT_OK;
+    return FT_OK;
+}
+
+FT_API uint32_t ft_stroke_composite_chunk(ft_composite_adjoint* s) { return s ? s->chunk : 0; }
+
+FT_API void ft_stroke_composite_destroy(ft_composite_adjoint* s) {
+    if (!s) return;
+    if (s->ctx) {
+        cudaSetDevice(s->ctx->device);
+        if (s->ctx->stream) cudaStreamSynchronize(s->ctx->stream);
+    }
+    ft_adjoint_destroy(s->adj);
+    DevBuf* bufs[] = {&s->ops, &s->clr, &s->prefix, &s->cov, &s->gcov, &s->gbuf, &s->status, &s->gops, &s->gwidth};
+    for (DevBuf* b : bufs) b->release();
+    delete s;
 }
 
 FT_API int ft_autotune_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* ops, uint32_t n_ops_total,

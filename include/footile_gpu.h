@@ -296,6 +296,37 @@ FT_API int ft_srcover_backward(ft_ctx* ctx, const float* cov, uint32_t n_layers,
                                const float* clr, const float* init, const float* grad_out,
                                float* grad_cov, float* grad_init, uint32_t n_px);
 
+/* Differentiable ordered composite of strokes on one canvas, at any canvas size and
+ * stroke count: the float counterpart of ft_composite_batch with stroke = 1
+ * (Plotter::stroke of each path in order onto one Rgba8p raster, plotter.rs:356-365,
+ * fig.rs:637-643).  C_n = clr_n * cov_n + C_{n-1} * (1 - alpha_n * cov_n) with cov_n
+ * the stroke coverage of ft_adjoint_forward (stroke = 1) over the width x height
+ * canvas, C_0 = init (n_px float4, or NULL for 0); `out` receives C_N (n_px float4).
+ * paths[i] gives stroke i's op range and starting pen width (op_begin, n_ops,
+ * s_width; the raster fields are ignored); clr holds n_paths premultiplied float4
+ * colours.  The strokes are covered in chunks of `chunk` planes (0: sized to the free
+ * device memory); only the canvas before each chunk is kept, and
+ * ft_stroke_composite_backward recomputes the coverage chunk by chunk, last chunk
+ * first (SrcOver is affine in the canvas with a scalar factor, so the gradient reaching
+ * a chunk's input is the gradient at its output scaled per pixel).  Given dLoss/dC_N it
+ * writes dLoss/d(op floats) (overwritten; the layout of ft_adjoint_backward),
+ * dLoss/d(starting pen width) per stroke and dLoss/dC_0 (each may be NULL except
+ * grad_ops).  The join, miter limit, tolerance and transform are the context's at the
+ * forward call.  `where` is FT_HOST or FT_DEVICE for ops, clr, init, out and the
+ * gradients; path descriptors are host memory.  The saved state holds copies of its
+ * inputs.  Per-stroke status via ft_stroke_composite_status; the chunk size in use via
+ * ft_stroke_composite_chunk. */
+typedef struct ft_composite_adjoint ft_composite_adjoint;
+FT_API int ft_stroke_composite_forward(ft_ctx* ctx, const ft_op* ops, uint32_t n_ops_total,
+                                       const ft_path_desc* paths, uint32_t n_paths, const float* clr,
+                                       uint32_t width, uint32_t height, const float* init, float* out,
+                                       uint32_t chunk, int32_t where, ft_composite_adjoint** saved);
+FT_API int ft_stroke_composite_backward(ft_ctx* ctx, ft_composite_adjoint* saved, const float* grad_out,
+                                        float* grad_ops, float* grad_width, float* grad_init, int32_t where);
+FT_API int ft_stroke_composite_status(ft_ctx* ctx, ft_composite_adjoint* saved, int32_t* status, uint32_t n);
+FT_API uint32_t ft_stroke_composite_chunk(ft_composite_adjoint* saved);
+FT_API void ft_stroke_composite_destroy(ft_composite_adjoint* saved);
+
 /* Per-path status codes of the last batch (synchronises the context stream). */
 FT_API int ft_batch_status(ft_ctx* ctx, int32_t* status, uint32_t n);
 

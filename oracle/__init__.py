@@ -330,11 +330,12 @@ def convert(src):
 
 # ------------------------------------------- ordered SrcOver of strokes (FP64 chain)
 def adj_stroke_composite(ops, paths, clr, w, h, target, val=None, join=_abi.JOIN_MITER, miter_limit=4.0,
-                         tolerance=0.3, transform=_abi.IDENTITY, grads=True):
+                         tolerance=0.3, transform=_abi.IDENTITY, grads=True, init=None):
     """FP64 loss sum((C_N - target)^2) of strokes SrcOver'd in order on one w x h canvas
-    (C_n = clr_n cov_n + C_{n-1} (1 - a_n cov_n), float premultiplied colours), and with
-    `grads` its gradient w.r.t. the op floats (n_ops, 6) and the starting pen widths.
-    `val` (n_ops x 6) moves the vertices continuously on held decisions (for finite
+    (C_n = clr_n cov_n + C_{n-1} (1 - a_n cov_n), float premultiplied colours, C_0 =
+    `init` or 0), and with `grads` its gradient w.r.t. the op floats (n_ops, 6) and the
+    starting pen widths (and, with `init`, w.r.t. C_0 as a fifth result).  `val`
+    (n_ops x 6) moves the vertices continuously on held decisions (for finite
     differences)."""
     ops = np.ascontiguousarray(ops, dtype=_abi.OP_DTYPE)
     n = len(paths)
@@ -346,7 +347,8 @@ def adj_stroke_composite(ops, paths, clr, w, h, target, val=None, join=_abi.JOIN
         c, a, _ = adj_stroke_forward(ops[b:b + k], w, h, val=v, s_width=float(p["s_width"]), **kw)
         covs.append(c.ravel())
         areas.append(a)
-    C = np.zeros((w * h, 4))
+    C = np.zeros((w * h, 4)) if init is None else np.array(init, dtype=np.float64).reshape(w * h, 4)
+    C0 = C.copy()
     for i in range(n):
         C = clr[i][None, :] * covs[i][:, None] + C * (1.0 - clr[i][3] * covs[i])[:, None]
     loss = float(((C - target) ** 2).sum())
@@ -354,7 +356,7 @@ def adj_stroke_composite(ops, paths, clr, w, h, target, val=None, join=_abi.JOIN
         return loss
     G = 2.0 * (C - target)
     # E_{n-1} = G . C_{n-1} forward, then the suffix products backward
-    E = np.zeros(w * h)
+    E = (G * C0).sum(axis=1)
     Es = []
     for i in range(n):
         Es.append(E.copy())
@@ -372,4 +374,6 @@ def adj_stroke_composite(ops, paths, clr, w, h, target, val=None, join=_abi.JOIN
                                      s_width=float(p["s_width"]), **kw)
         g_ops[b:b + k] += gg
         g_w[i] = gw
+    if init is not None:
+        return loss, C, g_ops, g_w, G * P[:, None]
     return loss, C, g_ops, g_w

@@ -215,3 +215,25 @@ def test_stroke_composite_gradient_matches_central_differences():
         fd = (oracle.adj_stroke_composite(ops, paths, clr, side, side, target, val=vp, grads=False) -
               oracle.adj_stroke_composite(ops, paths, clr, side, side, target, val=vm, grads=False)) / (2 * step)
         assert abs(g[i, k] - fd) <= 2e-4 * np.abs(g).max(), (i, k, g[i, k], fd)
+
+
+def test_stroke_composite_initial_canvas_gradient():
+    # C_0 enters the chain linearly: its gradient matches central differences exactly
+    from footile_gb300.adjoint import pack_coverage
+    paths_ops, widths, clrs, side = workloads.strokes_16384(n_paths=3, side=32, min_seg=2, max_seg=3)
+    ops, paths, _ = pack_coverage(paths_ops, [side] * 3)
+    clr = clrs.astype(np.float64) / 255.0
+    rng = np.random.default_rng(12)
+    target = rng.random((side * side, 4))
+    init = rng.random((side * side, 4)) * 0.5
+    loss, C, g, gw, g0 = oracle.adj_stroke_composite(ops, paths, clr, side, side, target, init=init)
+    _, C_zero, g_zero, _ = oracle.adj_stroke_composite(ops, paths, clr, side, side, target)
+    assert not np.allclose(C, C_zero)
+    step = 1e-4
+    for px, ch in [(int(p), int(q)) for p, q in zip(rng.integers(0, side * side, 10), rng.integers(0, 4, 10))]:
+        ip, im = init.copy(), init.copy()
+        ip[px, ch] += step
+        im[px, ch] -= step
+        fd = (oracle.adj_stroke_composite(ops, paths, clr, side, side, target, grads=False, init=ip) -
+              oracle.adj_stroke_composite(ops, paths, clr, side, side, target, grads=False, init=im)) / (2 * step)
+        assert abs(g0[px, ch] - fd) <= 1e-6 * max(1.0, abs(fd)), (px, ch, g0[px, ch], fd)
