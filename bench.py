@@ -49,6 +49,10 @@ def parse_args():
     ap.add_argument("--no-extras", action="store_true", help="skip the secondary workloads")
     ap.add_argument("--no-tune", action="store_true", help="use the built-in plan instead of the autotuner")
     ap.add_argument("--tune-cache", default=None, help="autotuner cache file (looked up, then appended)")
+    ap.add_argument("--composite-strokes", type=int, default=16384,
+                    help="--only adjoint_composite: strokes on the 2048x2048 canvas")
+    ap.add_argument("--composite-chunk", type=int, default=0,
+                    help="--only adjoint_composite: strokes covered per chunk (0: sized to free memory)")
     ap.add_argument("--only", choices=["single", "scene", "strokes", "adjoint", "adjoint_strokes",
                                        "adjoint_composite"],
                     help="run one secondary workload alone (for profiling) and print its line")
@@ -505,7 +509,7 @@ def extra_adjoint_strokes(ctx, stream, dev, cpu=True, reps=5, n_paths=1024, side
     return out
 
 
-def extra_adjoint_composite(ctx, stream, dev, cpu=True, n_paths=16384, side=2048, reps=2):
+def extra_adjoint_composite(ctx, stream, dev, cpu=True, n_paths=16384, side=2048, reps=2, chunk=0):
     """Differentiable ordered composite at full size: 16,384 open strokes of 8..64 cubics,
     width 1..12, Miter(4), colours with alpha 64..255, SrcOver'd in order on one 2048x2048
     canvas, L2 loss against a seeded RGBA target; gradients of the control points and pen
@@ -524,11 +528,11 @@ def extra_adjoint_composite(ctx, stream, dev, cpu=True, n_paths=16384, side=2048
     tgt_d = torch.from_numpy(target).to(dev)
     ctx.set_join(_abi.JOIN_MITER, 4.0)
     comp = StrokeComposite(ctx)
-    stroke_composite_grads(ctx, ops_d, paths, clr_d, side, side, tgt_d, comp)  # warm-up (allocations)
+    stroke_composite_grads(ctx, ops_d, paths, clr_d, side, side, tgt_d, comp, chunk)  # warm-up (allocations)
     runs = []
     t0 = time.perf_counter()
     for _ in range(reps):
-        loss, out, g_ops, g_w, ms = stroke_composite_grads(ctx, ops_d, paths, clr_d, side, side, tgt_d, comp)
+        loss, out, g_ops, g_w, ms = stroke_composite_grads(ctx, ops_d, paths, clr_d, side, side, tgt_d, comp, chunk)
         runs.append(ms)
     wall = (time.perf_counter() - t0) / reps * 1e3
     st = comp.status()
@@ -569,7 +573,10 @@ def run_only(args):
     ctx.set_stream(stream.cuda_stream)
     fn = {"single": extra_single, "scene": extra_scene, "strokes": extra_strokes, "adjoint": extra_adjoint,
           "adjoint_strokes": extra_adjoint_strokes, "adjoint_composite": extra_adjoint_composite}[args.only]
-    print(json.dumps(fn(ctx, stream, dev, cpu=not args.no_cpu)), flush=True)
+    kw = {}
+    if args.only == "adjoint_composite":
+        kw = {"n_paths": args.composite_strokes, "chunk": args.composite_chunk}
+    print(json.dumps(fn(ctx, stream, dev, cpu=not args.no_cpu, **kw)), flush=True)
 
 
 def run_ours(args):

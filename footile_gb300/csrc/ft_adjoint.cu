@@ -508,20 +508,60 @@ __device__ __forceinline__ void row_pieces(const EdgeG& E, int r, int W, CB cb) 
     }
 }
 
+// Forward pieces of the edge in raster row r: cb(cell, h, xmid) as row_pieces gives
+// them, with one division per row (the height per unit of x) instead of two per piece.
+template <class CB>
+__device__ __forceinline__ void row_cells(const EdgeG& E, int r, int W, CB cb) {
+    const float yt = fmaxf(E.a.y, (float)r), yb = fminf(E.b.y, (float)(r + 1));
+    if (!(yb > yt)) return;
+    const float xt = yt == E.a.y ? E.a.x
+                                 : fminf(fmaxf(__fadd_rn(E.a.x, __fmul_rn(__fsub_rn(yt, E.a.y), E.dxdy)), E.xlo), E.xhi);
+    const float xb = yb == E.b.y ? E.b.x
+                                 : fminf(fmaxf(__fadd_rn(E.a.x, __fmul_rn(__fsub_rn(yb, E.a.y), E.dxdy)), E.xlo), E.xhi);
+    const float h = __fsub_rn(yb, yt);
+    const float xl = fminf(xt, xb), xr = fmaxf(xt, xb);
+    const float cl = floorf(xl), cr = floorf(xr);
+    if (cl == cr || xr == xl) {
+        if (cl < (float)W) cb(cl < 0.0f ? -1 : (int)cl, h, __fmul_rn(__fadd_rn(xl, xr), 0.5f));
+        return;
+    }
+    const float hs = __fdiv_rn(h, __fsub_rn(xr, xl));
+    auto piece = [&](float x0, float x1, int c) {
+        cb(c, __fmul_rn(__fsub_rn(x1, x0), hs), __fmul_rn(__fadd_rn(x0, x1), 0.5f));
+    };
+    float c = cl;
+    if (c < 0.0f) {
+        const float x1 = fminf(xr, 0.0f);
+        if (x1 > xl) piece(xl, x1, -1);
+        c = 0.0f;
+    }
+    const float cend = fminf(cr, (float)(W - 1));
+    for (; c <= cend; c = __fadd_rn(c, 1.0f)) {
+        const float x0 = fmaxf(xl, c), x1 = fminf(xr, __fadd_rn(c, 1.0f));
+        if (x1 > x0) piece(x0, x1, (int)c);
+    }
+}
+
 // All (edge, row) items of rows [b0, b0 + nb) of the path: forward adds cell areas to
-// the band, backward accumulates the edge integrals against the band's g values.
-template <bool BWD>
+// the band, backward accumulates the edge integrals against g = gv(row, cell) (the
+// loss gradient times dcov/dS at that cell).  The edges visited are elist[0 .. n_e)
+// (the band's binned edges), or 0 .. n_e - 1 when elist is null.
+struct NoG {
+    __device__ float operator()(int, int) const { return 0.0f; }
+};
+template <bool BWD, class GV = NoG>
 __device__ void band_edges(ASmem& sm, float* band, int W, int b0, int nb, int V, const float2* vpos,
-                           const int* vsub, float2* vgrad) {
+                           const int* vsub, float2* vgrad, const int* elist, int n_e, GV gv = GV()) {
     const int tid = threadIdx.x;
     const int b1 = b0 + nb - 1;
-    for (int e0 = 0; e0 < V; e0 += ECHUNK) {
+    auto edge_at = [&](int i) { return elist ? elist[i] : i; };
+    for (int e0 = 0; e0 < n_e; e0 += ECHUNK) {
         int cnt[EPT], sum = 0;
 #pragma unroll
         for (int q = 0; q < EPT; q++) {
-            const int e = e0 + tid * EPT + q;
+            const int i = e0 + tid * EPT + q;
             int r0;
-            cnt[q] = e < V ? edge_rows(make_edge(vpos, vsub, V, e), b0, b1, &r0) : 0;
+            cnt[q] = i < n_e ? edge_rows(make_edge(vpos, vsub, V, edge_at(i)), b0, b1, &r0) : 0;
             sum += cnt[q];
         }
         int total;
@@ -546,7 +586,7 @@ __device__ void band_edges(ASmem& sm, float* band, int W, int b0, int nb, int V,
                     hi = mid - 1;
             }
             int slot = lo;
-            EdgeG E = make_edge(vpos, vsub, V, e0 + slot);
+            EdgeG E = make_edge(vpos, vsub, V, edge_at(e0 + slot));
             int r0 = 0;
             edge_rows(E, b0, b1, &r0);
             float ga = 0.0f, gb = 0.0f;
@@ -562,13 +602,13 @@ __device__ void band_edges(ASmem& sm, float* band, int W, int b0, int nb, int V,
                     do {
                         slot++;
                     } while (sm.off[slot + 1] <= it);
-                    E = make_edge(vpos, vsub, V, e0 + slot);
+                    E = make_edge(vpos, vsub, V, edge_at(e0 + slot));
                     edge_rows(E, b0, b1, &r0);
                 }
                 const int r = r0 + (it - sm.off[slot]);
-                float* row = band + (size_t)(r - b0) * W;
                 if (!BWD) {
-                    row_pieces(E, r, W, [&](int c, float h, float xm, float, float) {
+                    float* row = band + (size_t)(r - b0) * W;
+                    row_cells(E, r, W, [&](int c, float h, float xm) {
                         const float dh = __fmul_rn(E.dir, h);
                         if (c < 0) {
                             atomicAdd(row, dh);
@@ -581,7 +621,7 @@ __device__ void band_edges(ASmem& sm, float* band, int W, int b0, int nb, int V,
                     const bool down = E.dir > 0.0f;
                     row_pieces(E, r, W, [&](int c, float, float, float u0, float u1) {
                         if (c < 0) return;
-                        const float g = row[c];
+                        const float g = gv(r, c);
                         const float i1 = __fsub_rn(u1, u0);
                         const float iu = __fmul_rn(__fmul_rn(0.5f, i1), __fadd_rn(u1, u0));
                         const float i0 = __fsub_rn(i1, iu);
@@ -601,6 +641,47 @@ __device__ void band_edges(ASmem& sm, float* band, int W, int b0, int nb, int V,
     }
 }
 
+// Bin the path's edges by row band (band k = rows [k * rpb, (k + 1) * rpb)) into the
+// CSR list boff / blist: a count pass into the shared histogram `hist` (the band buffer,
+// free before the band loop), a block scan, a fill pass.  The order of a band's edges is
+// that of the atomics; every edge is visited once per band it reaches, as in the scan of
+// all edges.  Returns false, uniformly, when the pairs exceed PAIR_CAP.
+__device__ bool bin_edges(ASmem& sm, int* hist, int* boff, int* blist, int V, int H, int rpb, int nbands,
+                          const float2* vpos, const int* vsub) {
+    const int tid = threadIdx.x;
+    for (int i = tid; i <= nbands; i += ABLOCK) hist[i] = 0;
+    __syncthreads();
+    for (int e = tid; e < V; e += ABLOCK) {
+        int r0 = 0;
+        const int n = edge_rows(make_edge(vpos, vsub, V, e), 0, H - 1, &r0);
+        if (n > 0)
+            for (int b = r0 / rpb, b1 = (r0 + n - 1) / rpb; b <= b1; b++) atomicAdd(&hist[b], 1);
+    }
+    __syncthreads();
+    const int per = (nbands + ABLOCK - 1) / ABLOCK;
+    const int lo = min(nbands, tid * per), hi = min(nbands, lo + per);
+    int cnt = 0;
+    for (int i = lo; i < hi; i++) cnt += hist[i];
+    int total;
+    int pre = block_excl_sum(cnt, sm.wsum, total);
+    if (total > PAIR_CAP) return false;
+    for (int i = lo; i < hi; i++) {
+        const int c = hist[i];
+        boff[i] = pre;
+        hist[i] = pre;
+        pre += c;
+    }
+    if (tid == 0) boff[nbands] = total;
+    __syncthreads();
+    for (int e = tid; e < V; e += ABLOCK) {
+        int r0 = 0;
+        const int n = edge_rows(make_edge(vpos, vsub, V, e), 0, H - 1, &r0);
+        if (n > 0)
+            for (int b = r0 / rpb, b1 = (r0 + n - 1) / rpb; b <= b1; b++) blist[atomicAdd(&hist[b], 1)] = e;
+    }
+    __syncthreads();
+    return true;
+}
 
 // ------------------------------------------------------------------- strokes
 // Plotter::stroke (plotter.rs:356-365): stroke points with widths from the pen walk
@@ -1187,7 +1268,7 @@ __device__ __forceinline__ float* px_at(float* base, const ft_path_desc& d, int 
 }
 
 template <bool BWD>
-__global__ void __launch_bounds__(ABLOCK) k_adjoint(AParams p) {
+__global__ void __launch_bounds__(ABLOCK, 3) k_adjoint(AParams p) {
     extern __shared__ float band[];
     __shared__ ASmem sm;
     unsigned char* scr = p.scratch + (size_t)blockIdx.x * (p.stroke ? A_SCRATCH_STROKE : A_SCRATCH_PER_CTA);
@@ -1233,41 +1314,95 @@ __global__ void __launch_bounds__(ABLOCK) k_adjoint(AParams p) {
         if (cap && tid == 0) atomicMax(&sm.status, (int)FT_ERR_CAP);
         const float sign = cap ? 1.0f : fig_sign(sm, V, vpos, vsub, vflag);
         const int rows_per_band = W > 0 ? max(1, BAND_FLOATS / W) : 1;
-        for (int b0 = 0; b0 < H && W > 0; b0 += rows_per_band) {
-            const int nb = min(rows_per_band, H - b0);
-            const int nc = nb * W;
-            if (!BWD) {
-                for (int i = tid; i < nc; i += ABLOCK) band[i] = 0.0f;
-            } else {
-                for (int i = tid; i < nc; i += ABLOCK) {
-                    const int r = b0 + i / W, c = i - (i / W) * W;
-                    const float g = px_at(const_cast<float*>(p.grad_cov), d, r)[c];
-                    band[i] = cap ? 0.0f : __fmul_rn(__fmul_rn(sign, g), cov_d(p.rule, px_at(p.area, d, r)[c]));
-                }
+        const int nbands = W > 0 ? (H + rows_per_band - 1) / rows_per_band : 0;
+        int* boff = reinterpret_cast<int*>(scr + AS_BOFF);
+        const int* blist = reinterpret_cast<const int*>(scr + AS_BLIST);
+        if (BWD) {
+            // every (edge, row) item of the path in one pass, g read at its own cell
+            if (!cap && W > 0 && H > 0) {
+                const float* gc = p.grad_cov;
+                const float* cvp = p.cov;
+                const float* arp = p.area;
+                const int rule = p.rule;
+                if (p.no_area)
+                    band_edges<true>(sm, nullptr, W, 0, H, V, vpos, vsub, vgrad, nullptr, V, [&](int r, int c) {
+                        const size_t o = d.raster_offset + (size_t)r * d.stride + 4 * (size_t)c;
+                        const float cv = *reinterpret_cast<const float*>(reinterpret_cast<const char*>(cvp) + o);
+                        const float g = *reinterpret_cast<const float*>(reinterpret_cast<const char*>(gc) + o);
+                        return cv > 0.0f && cv < 1.0f ? __fmul_rn(sign, g) : 0.0f;
+                    });
+                else
+                    band_edges<true>(sm, nullptr, W, 0, H, V, vpos, vsub, vgrad, nullptr, V, [&](int r, int c) {
+                        const size_t o = d.raster_offset + (size_t)r * d.stride + 4 * (size_t)c;
+                        const float a = *reinterpret_cast<const float*>(reinterpret_cast<const char*>(arp) + o);
+                        const float g = *reinterpret_cast<const float*>(reinterpret_cast<const char*>(gc) + o);
+                        return __fmul_rn(__fmul_rn(sign, g), cov_d(rule, a));
+                    });
             }
             __syncthreads();
-            if (!cap) band_edges<BWD>(sm, band, W, b0, nb, V, vpos, vsub, vgrad);
-            if (!BWD) {
+        }
+        bool binned = false;
+        if (!BWD && !cap && nbands > 2 && nbands <= NB_CAP)
+            binned = bin_edges(sm, reinterpret_cast<int*>(band), boff, reinterpret_cast<int*>(scr + AS_BLIST), V, H,
+                               rows_per_band, nbands, vpos, vsub);
+        __syncthreads();
+        // forward: bands of rows accumulated in shared memory, resolved row by row
+        for (int b0 = 0; b0 < H && W > 0 && !BWD; b0 += rows_per_band) {
+            const int nb = min(rows_per_band, H - b0);
+            const int nc = nb * W;
+            int e_lo = 0, n_e = V;
+            if (binned) {
+                e_lo = boff[b0 / rows_per_band];
+                n_e = boff[b0 / rows_per_band + 1] - e_lo;
+            }
+            if (binned && n_e == 0) {  // no edge reaches these rows: coverage and area 0
+                for (int rr = warp; rr < nb; rr += NW) {
+                    float* ar = px_at(p.area, d, b0 + rr);
+                    float* cv = px_at(p.cov, d, b0 + rr);
+                    for (int c = lane; c < W; c += 32) {
+                        if (!p.no_area) ar[c] = 0.0f;
+                        cv[c] = 0.0f;
+                    }
+                }
+                continue;
+            }
+            for (int i = tid; i < nc; i += ABLOCK) band[i] = 0.0f;
+            __syncthreads();
+            if (!cap) band_edges<false>(sm, band, W, b0, nb, V, vpos, vsub, vgrad, binned ? blist + e_lo : nullptr, n_e);
+            {
                 __syncthreads();
+                // row prefix sums, four 32-cell chunks scanned side by side; the float
+                // additions are those of one chunk after the other
                 for (int rr = warp; rr < nb; rr += NW) {
                     float* ar = px_at(p.area, d, b0 + rr);
                     float* cv = px_at(p.cov, d, b0 + rr);
                     const float* src = band + (size_t)rr * W;
                     float carry = 0.0f;
-                    for (int c0 = 0; c0 < W; c0 += 32) {
-                        const int c = c0 + lane;
-                        float v = c < W ? src[c] : 0.0f;
+                    for (int c0 = 0; c0 < W; c0 += 128) {
+                        float v[4];
+#pragma unroll
+                        for (int u = 0; u < 4; u++) {
+                            const int c = c0 + 32 * u + lane;
+                            v[u] = c < W ? src[c] : 0.0f;
+                        }
 #pragma unroll
                         for (int o = 1; o < 32; o <<= 1) {
-                            const float t = __shfl_up_sync(FULL, v, o);
-                            if (lane >= o) v = __fadd_rn(v, t);
+#pragma unroll
+                            for (int u = 0; u < 4; u++) {
+                                const float t = __shfl_up_sync(FULL, v[u], o);
+                                if (lane >= o) v[u] = __fadd_rn(v[u], t);
+                            }
                         }
-                        v = __fadd_rn(v, carry);
-                        carry = __shfl_sync(FULL, v, 31);
-                        if (c < W) {
-                            const float sv = __fmul_rn(sign, v);
-                            ar[c] = sv;
-                            cv[c] = cov_of(p.rule, sv);
+#pragma unroll
+                        for (int u = 0; u < 4; u++) {
+                            const int c = c0 + 32 * u + lane;
+                            v[u] = __fadd_rn(v[u], carry);
+                            carry = __shfl_sync(FULL, v[u], 31);
+                            if (c < W) {
+                                const float sv = __fmul_rn(sign, v[u]);
+                                if (!p.no_area) ar[c] = sv;
+                                cv[c] = cov_of(p.rule, sv);
+                            }
                         }
                     }
                 }
@@ -1291,12 +1426,12 @@ __global__ void __launch_bounds__(ABLOCK) k_adjoint(AParams p) {
 
 }  // namespace
 
+// The backward reads g at each piece's own cell and needs no shared band.
 int adjoint_blocks_per_sm(bool backward) {
     const int smem = BAND_FLOATS * (int)sizeof(float);
     int n = 0;
     if (backward) {
-        cudaFuncSetAttribute(k_adjoint<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_adjoint<true>, ABLOCK, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_adjoint<true>, ABLOCK, 0);
     } else {
         cudaFuncSetAttribute(k_adjoint<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_adjoint<false>, ABLOCK, smem);
@@ -1307,8 +1442,7 @@ int adjoint_blocks_per_sm(bool backward) {
 cudaError_t launch_adjoint(bool backward, const AParams& p, int grid, cudaStream_t s) {
     const int smem = BAND_FLOATS * (int)sizeof(float);
     if (backward) {
-        cudaFuncSetAttribute(k_adjoint<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        k_adjoint<true><<<grid, ABLOCK, smem, s>>>(p);
+        k_adjoint<true><<<grid, ABLOCK, 0, s>>>(p);
     } else {
         cudaFuncSetAttribute(k_adjoint<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         k_adjoint<false><<<grid, ABLOCK, smem, s>>>(p);

@@ -21,7 +21,14 @@ constexpr size_t AS_POS = 0;                                              // flo
 constexpr size_t AS_SUB = a_align(AS_POS + (size_t)VCAP * 8);             // int[VCAP]
 constexpr size_t AS_GRAD = a_align(AS_SUB + (size_t)VCAP * 4);            // float2[VCAP]
 constexpr size_t AS_FLAG = a_align(AS_GRAD + (size_t)VCAP * 8);           // int[VCAP]
-constexpr size_t A_SCRATCH_PER_CTA = a_align(AS_FLAG + (size_t)VCAP * 4);
+// Edges binned by row band, built once per path: band k's edges are
+// blist[boff[k] .. boff[k + 1]).  Paths with more bands or (edge, band) pairs scan
+// every edge for every band instead.
+constexpr int NB_CAP = BAND_FLOATS - 1;     // bands (the shared band buffer is the histogram)
+constexpr int PAIR_CAP = 1 << 18;           // (edge, band) pairs
+constexpr size_t AS_BOFF = a_align(AS_FLAG + (size_t)VCAP * 4);          // int[NB_CAP + 1]
+constexpr size_t AS_BLIST = a_align(AS_BOFF + (size_t)(NB_CAP + 1) * 4);  // int[PAIR_CAP]
+constexpr size_t A_SCRATCH_PER_CTA = a_align(AS_BLIST + (size_t)PAIR_CAP * 4);
 
 // Strokes add, after the fill arrays: the node of each outline vertex, stroke points,
 // sub-strokes, outline nodes (offset points, miter intersections, arc points) and
@@ -55,6 +62,8 @@ struct AParams {
     int stroke;             // Plotter::stroke: the outline of each path is filled NonZero
     int join;
     float miter_limit;
+    int no_area;            // NonZero only: keep no winding area; the backward takes dcov/dS from cov
+                            // (0 < cov < 1 exactly where 0 < S < 1) and reads grad_cov only there
 };
 
 cudaError_t launch_adjoint(bool backward, const AParams& p, int grid, cudaStream_t s);

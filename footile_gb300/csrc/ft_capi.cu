@@ -861,7 +861,7 @@ cudaError_t launch_convert(int src_fmt, const uint8_t* src, uint32_t src_stride,
 int convert_blocks_per_sm();
 cudaError_t launch_srcover(bool backward, const float* cov, uint32_t n_layers, uint64_t plane, const float4* clr,
                            const float4* init, float4* out, const float4* grad_out, float* grad_cov,
-                           float4* grad_init, uint32_t n_px, int grid, cudaStream_t s);
+                           float4* grad_init, uint32_t n_px, int grid, cudaStream_t s, bool partial = false);
 }
 
 // lut[a * 256 + c]: the straight channel c / a (clamped to 1; 0 when a = 0) through
@@ -927,6 +927,8 @@ struct ft_adjoint {
     ft_ctx* ctx = nullptr;
     DevBuf ops, paths, area, status, scratch, cov, gcov, gops, gwidth;
     const ft_op* ops_d = nullptr;  // device ops the kernels read (`ops` or a caller's copy)
+    float* cov_d = nullptr;        // device coverage of the last forward
+    int no_area = 0;               // no winding area kept: the backward reads cov_d (NonZero)
     std::vector<ft_path_desc> h_paths;
     uint32_t n_ops = 0, n_paths = 0;
     uint64_t cov_bytes = 0;
@@ -982,6 +984,8 @@ static fta::AParams adjoint_params(const ft_adjoint* a) {
     p.stroke = a->stroke;
     p.join = a->join;
     p.miter_limit = a->miter_limit;
+    p.cov = a->cov_d;
+    p.no_area = a->no_area;
     return p;
 }
 
@@ -990,8 +994,10 @@ static fta::AParams adjoint_params(const ft_adjoint* a) {
 // status and launches; `events` brackets the launch with the context's timing events.
 static int adjoint_forward_dev(ft_ctx* c, ft_adjoint* a, int stroke, int rule, const ft_op* ops_d,
                                uint32_t n_ops_total, const ft_path_desc* paths, uint32_t n_paths, float* cov_d,
-                               uint64_t cov_bytes, const AdjSettings& set, bool events) {
+                               uint64_t cov_bytes, const AdjSettings& set, bool events, bool no_area = false) {
     a->ready = false;
+    a->cov_d = cov_d;
+    a->no_area = no_area && rule == FT_NONZERO ? 1 : 0;
     a->rule = rule;
     a->stroke = stroke ? 1 : 0;
     a->join = set.join;
@@ -1005,10 +1011,10 @@ static int adjoint_forward_dev(ft_ctx* c, ft_adjoint* a, int stroke, int rule, c
     a->tol_sq = set.tol_sq;
     FT_CU(a->paths.ensure(sizeof(ft_path_desc) * std::max(n_paths, 1u)), "alloc paths");
     FT_CU(a->status.ensure(sizeof(int32_t) * std::max(n_paths, 1u)), "alloc status");
-    FT_CU(a->area.ensure(std::max<uint64_t>(cov_bytes, 4)), "alloc winding area");
-    // strokes: the stroker runs on one thread per CTA over a 14 MB scratch, two CTAs per SM
-    const int bps_f = a->stroke ? 2 : fta::adjoint_blocks_per_sm(false);
-    const int bps_b = a->stroke ? 2 : fta::adjoint_blocks_per_sm(true);
+    FT_CU(a->area.ensure(a->no_area ? 4 : std::max<uint64_t>(cov_bytes, 4)), "alloc winding area");
+    // as many CTAs per SM as fit (strokes: at most 3, each with a 16 MB scratch)
+    const int bps_f = std::min(a->stroke ? 3 : 64, fta::adjoint_blocks_per_sm(false));
+    const int bps_b = std::min(a->stroke ? 3 : 64, fta::adjoint_blocks_per_sm(true));
     a->grid_f = (int)std::max(1u, std::min<uint32_t>(n_paths, (uint32_t)(bps_f * c->sm_count)));
     a->grid_b = (int)std::max(1u, std::min<uint32_t>(n_paths, (uint32_t)(bps_b * c->sm_count)));
     const size_t per_cta = a->stroke ? fta::A_SCRATCH_STROKE : fta::A_SCRATCH_PER_CTA;
@@ -1018,7 +1024,6 @@ static int adjoint_forward_dev(ft_ctx* c, ft_adjoint* a, int stroke, int rule, c
               "upload paths");
     FT_CU(cudaMemsetAsync(a->status.p, 0, sizeof(int32_t) * std::max(n_paths, 1u), c->stream), "reset status");
     fta::AParams p = adjoint_params(a);
-    p.cov = cov_d;
     if (events) FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
     if (n_paths) {
         FT_CU(fta::launch_adjoint(false, p, a->grid_f, c->stream), "launch adjoint forward");
@@ -1286,7 +1291,7 @@ static int composite_cover(ft_ctx* c, ft_composite_adjoint* s, uint32_t ch) {
     s->fresh = -1;
     int st = adjoint_forward_dev(c, s->adj, 1, FT_NONZERO, static_cast<const ft_op*>(s->ops.p), s->n_ops,
                                  s->descs.data(), k, static_cast<float*>(s->cov.p), (uint64_t)k * s->plane_bytes(),
-                                 s->set, false);
+                                 s->set, false, true);
     if (st == FT_OK) s->fresh = (int)ch;
     return st;
 }
@@ -1332,12 +1337,12 @@ FT_API int ft_stroke_composite_forward(ft_ctx* c, const ft_op* ops, uint32_t n_o
     s->h_paths.assign(paths, paths + n_paths);
     const uint64_t plane = s->plane_bytes();
     if (chunk == 0) {
-        // coverage, winding area and coverage gradient of a chunk in at most 40 % of the
-        // free memory (96 GB at most), equal chunks
+        // coverage and coverage gradient of a chunk in at most 40 % of the free memory
+        // (96 GB at most), equal chunks
         size_t free_b = 0, total_b = 0;
         FT_CU(cudaMemGetInfo(&free_b, &total_b), "memory info");
         const uint64_t budget = std::min<uint64_t>(free_b / 5 * 2, 96ull << 30);
-        const uint64_t kmax = std::max<uint64_t>(1, budget / (3 * plane));
+        const uint64_t kmax = std::max<uint64_t>(1, budget / (2 * plane));
         const uint64_t nch = (std::max(n_paths, 1u) + kmax - 1) / kmax;
         chunk = (uint32_t)((std::max(n_paths, 1u) + nch - 1) / nch);
     }
@@ -1428,7 +1433,7 @@ FT_API int ft_stroke_composite_backward(ft_ctx* c, ft_composite_adjoint* s, cons
         const uint32_t b = s->chunk_begin(ch), k = s->chunk_size(ch);
         FT_CU(ftc::launch_srcover(true, static_cast<const float*>(s->cov.p), k, plane / 4,
                                   static_cast<const float4*>(s->clr.p) + b, s->prefix_at(ch), nullptr, g_cur,
-                                  static_cast<float*>(s->gcov.p), g_next, (uint32_t)n_px, grid, c->stream),
+                                  static_cast<float*>(s->gcov.p), g_next, (uint32_t)n_px, grid, c->stream, true),
               "launch SrcOver adjoint");
         c->launches++;
         int st = adjoint_backward_dev(c, s->adj, static_cast<const float*>(s->gcov.p), gops_d, gw_d + b, false);

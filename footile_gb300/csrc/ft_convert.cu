@@ -112,23 +112,38 @@ cudaError_t launch_convert(int src_fmt, const uint8_t* src, uint32_t src_stride,
 // one pass forward for E (recomputed, nothing kept from the forward call), written
 // into the gradient planes, then one pass backward for P.  No division, so opaque
 // layers (factor 0) are exact.  One thread per pixel; planes are n_layers x n_px floats.
+// Layers are read SB at a time (independent streaming loads, then the recurrence), so
+// that each thread keeps SB coverage loads in flight.
+constexpr int SB = 8;
+
 __global__ void k_srcover_fwd(const float* __restrict__ cov, uint32_t n_layers, uint64_t plane,
                               const float4* __restrict__ clr, const float4* __restrict__ init,
                               float4* __restrict__ out, uint32_t n_px) {
     for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n_px;
          p += (uint64_t)gridDim.x * blockDim.x) {
         float4 c = init ? init[p] : make_float4(0.f, 0.f, 0.f, 0.f);
-        for (uint32_t n = 0; n < n_layers; n++) {
-            const float v = cov[(uint64_t)n * plane + p];
-            if (v == 0.0f) continue;
+        auto layer = [&](uint32_t n, float v) {
+            if (v == 0.0f) return;
             const float4 k = clr[n];
             const float f = 1.0f - k.w * v;
             c = make_float4(k.x * v + c.x * f, k.y * v + c.y * f, k.z * v + c.z * f, k.w * v + c.w * f);
+        };
+        uint32_t n = 0;
+        for (; n + SB <= n_layers; n += SB) {
+            float v[SB];
+#pragma unroll
+            for (int u = 0; u < SB; u++) v[u] = __ldcs(cov + (uint64_t)(n + u) * plane + p);
+#pragma unroll
+            for (int u = 0; u < SB; u++) layer(n + u, v[u]);
         }
+        for (; n < n_layers; n++) layer(n, __ldcs(cov + (uint64_t)n * plane + p));
         out[p] = c;
     }
 }
 
+// PARTIAL: dLoss/dcov only where 0 < cov < 1 (elsewhere the plane is neither read nor
+// written) — all a NonZero coverage adjoint needs, since dcov/dS is 0 at cov 0 and 1.
+template <bool PARTIAL>
 __global__ void k_srcover_bwd(const float* __restrict__ cov, uint32_t n_layers, uint64_t plane,
                               const float4* __restrict__ clr, const float4* __restrict__ init,
                               const float4* __restrict__ grad_out, float* __restrict__ grad_cov,
@@ -138,21 +153,43 @@ __global__ void k_srcover_bwd(const float* __restrict__ cov, uint32_t n_layers, 
         const float4 g = grad_out[p];
         const float4 c0 = init ? init[p] : make_float4(0.f, 0.f, 0.f, 0.f);
         float e = g.x * c0.x + g.y * c0.y + g.z * c0.z + g.w * c0.w;
-        for (uint32_t n = 0; n < n_layers; n++) {  // E_{n-1} into the gradient plane
-            const uint64_t i = (uint64_t)n * plane + p;
-            const float v = cov[i];
-            grad_cov[i] = e;
-            if (v == 0.0f) continue;
+        auto keep = [](float v) { return !PARTIAL || (v > 0.0f && v < 1.0f); };
+        // E_{n-1} = g . C_{n-1} into the gradient plane
+        auto up = [&](uint32_t n, float v) {
+            if (keep(v)) grad_cov[(uint64_t)n * plane + p] = e;
+            if (v == 0.0f) return;
             const float4 k = clr[n];
             e = (g.x * k.x + g.y * k.y + g.z * k.z + g.w * k.w) * v + e * (1.0f - k.w * v);
+        };
+        uint32_t n = 0;
+        for (; n + SB <= n_layers; n += SB) {
+            float v[SB];
+#pragma unroll
+            for (int u = 0; u < SB; u++) v[u] = __ldcs(cov + (uint64_t)(n + u) * plane + p);
+#pragma unroll
+            for (int u = 0; u < SB; u++) up(n + u, v[u]);
         }
+        for (; n < n_layers; n++) up(n, __ldcs(cov + (uint64_t)n * plane + p));
+        // then the suffix products P, last layer first
         float P = 1.0f;
-        for (uint32_t n = n_layers; n-- > 0;) {
-            const uint64_t i = (uint64_t)n * plane + p;
-            const float v = cov[i];
+        auto down = [&](uint32_t n, float v, float en) {
             const float4 k = clr[n];
-            grad_cov[i] = P * ((g.x * k.x + g.y * k.y + g.z * k.z + g.w * k.w) - k.w * grad_cov[i]);
+            if (keep(v)) grad_cov[(uint64_t)n * plane + p] = P * ((g.x * k.x + g.y * k.y + g.z * k.z + g.w * k.w) - k.w * en);
             P *= 1.0f - k.w * v;
+        };
+        uint32_t m = n_layers;
+        for (; m >= SB; m -= SB) {
+            float v[SB], en[SB];
+#pragma unroll
+            for (int u = 0; u < SB; u++) v[u] = __ldcs(cov + (uint64_t)(m - 1 - u) * plane + p);
+#pragma unroll
+            for (int u = 0; u < SB; u++) en[u] = keep(v[u]) ? grad_cov[(uint64_t)(m - 1 - u) * plane + p] : 0.0f;
+#pragma unroll
+            for (int u = 0; u < SB; u++) down(m - 1 - u, v[u], en[u]);
+        }
+        for (; m > 0; m--) {
+            const float v = __ldcs(cov + (uint64_t)(m - 1) * plane + p);
+            down(m - 1, v, keep(v) ? grad_cov[(uint64_t)(m - 1) * plane + p] : 0.0f);
         }
         if (grad_init) grad_init[p] = make_float4(g.x * P, g.y * P, g.z * P, g.w * P);
     }
@@ -160,9 +197,11 @@ __global__ void k_srcover_bwd(const float* __restrict__ cov, uint32_t n_layers, 
 
 cudaError_t launch_srcover(bool backward, const float* cov, uint32_t n_layers, uint64_t plane, const float4* clr,
                            const float4* init, float4* out, const float4* grad_out, float* grad_cov,
-                           float4* grad_init, uint32_t n_px, int grid, cudaStream_t s) {
-    if (backward)
-        k_srcover_bwd<<<grid, 256, 0, s>>>(cov, n_layers, plane, clr, init, grad_out, grad_cov, grad_init, n_px);
+                           float4* grad_init, uint32_t n_px, int grid, cudaStream_t s, bool partial) {
+    if (backward && partial)
+        k_srcover_bwd<true><<<grid, 256, 0, s>>>(cov, n_layers, plane, clr, init, grad_out, grad_cov, grad_init, n_px);
+    else if (backward)
+        k_srcover_bwd<false><<<grid, 256, 0, s>>>(cov, n_layers, plane, clr, init, grad_out, grad_cov, grad_init, n_px);
     else
         k_srcover_fwd<<<grid, 256, 0, s>>>(cov, n_layers, plane, clr, init, out, n_px);
     return cudaGetLastError();

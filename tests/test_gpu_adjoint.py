@@ -6,8 +6,10 @@ respect to every op float, edges recomputed) go through the C ABI
 oracle on the same paths: coverage within 1e-4 absolute, gradients within 1e-4 of
 the oracle's largest gradient entry (max |g - g64| / max |g64|) for NonZero.  Both
 cover the same polygon (footile's f32 flattened vertices).  EvenOdd has a kink at
-every integer winding area; an edge pixel whose area lies within float rounding of
-one can take the other side of it in float, so its bound is 5e-4."""
+every integer winding area, NonZero at the clamp's 0 and 1; an edge pixel whose net
+area lies within float rounding of a kink can take the other side of it in float
+(in the self-intersecting mixed paths below one pixel has a net area of 2e-7 in
+FP64 and clamps to 0 in float), so EvenOdd and the mixed paths are held to 5e-4."""
 import numpy as np
 import pytest
 
@@ -21,6 +23,7 @@ pytestmark = pytest.mark.gpu
 
 COV_TOL = 1e-4
 GRAD_TOL = {_abi.NONZERO: 1e-4, _abi.EVENODD: 5e-4}
+KINK_TOL = 5e-4  # self-intersecting paths with pixels at a kink to float rounding
 
 
 def run_gpu(ctx, rule, ops, paths, cov_bytes, target):
@@ -49,7 +52,7 @@ def run_oracle(rule, ops, paths, g_cov, transform=_abi.IDENTITY, tolerance=0.3):
     return np.concatenate(covs) if covs else np.zeros(0), grads, np.array(sts)
 
 
-def check(ctx, rule, ops, paths, cov_bytes, seed=5, transform=_abi.IDENTITY, tolerance=0.3):
+def check(ctx, rule, ops, paths, cov_bytes, seed=5, transform=_abi.IDENTITY, tolerance=0.3, grad_tol=None):
     target = np.random.default_rng(seed).random(cov_bytes // 4)
     cov, g_cov, g_ops, st = run_gpu(ctx, rule, ops, paths, cov_bytes, target)
     want_cov, want_g, want_st = run_oracle(rule, ops, paths, g_cov, transform, tolerance)
@@ -58,7 +61,7 @@ def check(ctx, rule, ops, paths, cov_bytes, seed=5, transform=_abi.IDENTITY, tol
     scale = np.abs(want_g).max()
     if scale > 0:
         err = np.abs(g_ops - want_g).max() / scale
-        assert err < GRAD_TOL[rule], err
+        assert err < (grad_tol or GRAD_TOL[rule]), err
     else:
         assert not g_ops.any()
     return cov, g_ops
@@ -88,7 +91,7 @@ def mixed_paths(seed, n):
 @pytest.mark.parametrize("rule", [_abi.NONZERO, _abi.EVENODD])
 def test_mixed_paths_match_fp64_oracle(ctx, rule):
     ops, paths, cov_bytes = mixed_paths(21 + rule, 40)
-    check(ctx, rule, ops, paths, cov_bytes)
+    check(ctx, rule, ops, paths, cov_bytes, grad_tol=KINK_TOL)
 
 
 def test_transform_and_tolerance(ctx):
