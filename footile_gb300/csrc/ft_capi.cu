@@ -229,7 +229,8 @@ int grid_for_warp(ft_ctx* c, uint32_t n_items_w) {
 
 // Enqueue the two rasterisers for prepared parameters: warps for small paths,
 // then CTAs for large paths and for small ones a warp could not hold.
-cudaError_t enqueue(const ftk::KParams& p, int grid_b, int grid_w, int smem, cudaStream_t st, uint64_t* launches) {
+cudaError_t enqueue(const ftk::KParams& p, int grid_b, int grid_w, int smem, cudaStream_t st, uint64_t* launches,
+                    int sm_count) {
     cudaError_t e = cudaSuccess;
     if (p.n_items_w) {
         e = ftk::launch_raster_warp(p, grid_w, st);
@@ -237,7 +238,7 @@ cudaError_t enqueue(const ftk::KParams& p, int grid_b, int grid_w, int smem, cud
         (*launches)++;
     }
     if (p.n_items || p.n_items_w) {
-        e = ftk::launch_raster(p, grid_b, smem, st);
+        e = ftk::launch_raster(p, grid_b, smem, st, grid_b <= sm_count);
         if (e == cudaSuccess) (*launches)++;
     }
     return e;
@@ -308,7 +309,7 @@ int run(ft_ctx* c, int stroke, int rule, const ft_op* ops_d, const ft_path_desc*
     p.sw_chain = sw_chain;
     p.scratch = static_cast<unsigned char*>(c->scratch.p);
     FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
-    FT_CU(enqueue(p, grid, grid_w, smem, c->stream, &c->launches), "launch rasteriser");
+    FT_CU(enqueue(p, grid, grid_w, smem, c->stream, &c->launches, c->sm_count), "launch rasteriser");
     FT_CU(cudaEventRecord(c->ev1, c->stream), "event");
     c->timed = true;
     return FT_OK;
@@ -510,7 +511,8 @@ FT_API int ft_batch_launch(ft_ctx* c, ft_batch* b, const ft_op* ops, uint32_t n_
         FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
         FT_CU(cudaMemsetAsync(b->queue.p, 0, 256, c->stream), "reset queue");
         FT_CU(cudaMemsetAsync(b->status.p, 0, sizeof(int32_t) * std::max(b->n_paths, 1u), c->stream), "reset status");
-        FT_CU(enqueue(b->params, b->grid, b->grid_w, b->smem, c->stream, &c->launches), "launch rasteriser");
+        FT_CU(enqueue(b->params, b->grid, b->grid_w, b->smem, c->stream, &c->launches, c->sm_count),
+              "launch rasteriser");
         FT_CU(cudaEventRecord(c->ev1, c->stream), "event");
         c->timed = true;
         return FT_OK;
@@ -523,7 +525,7 @@ FT_API int ft_batch_launch(ft_ctx* c, ft_batch* b, const ft_op* ops, uint32_t n_
         cudaError_t e1 = cudaMemsetAsync(b->queue.p, 0, 256, c->stream);
         cudaError_t e2 = cudaMemsetAsync(b->status.p, 0, sizeof(int32_t) * std::max(b->n_paths, 1u), c->stream);
         uint64_t nl = 0;
-        cudaError_t e3 = enqueue(b->params, b->grid, b->grid_w, b->smem, c->stream, &nl);
+        cudaError_t e3 = enqueue(b->params, b->grid, b->grid_w, b->smem, c->stream, &nl, c->sm_count);
         cudaError_t e4 = cudaStreamEndCapture(c->stream, &g);
         if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess || e4 != cudaSuccess) {
             if (g) cudaGraphDestroy(g);
@@ -826,7 +828,8 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
         p.sw_out = sw_out;
         FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
         if (n_paths) {
-            FT_CU(ftk::launch_composite_build(p, grid, smem_a, c->stream), "launch composite build");
+            FT_CU(ftk::launch_composite_build(p, grid, smem_a, c->stream, grid <= c->sm_count),
+                  "launch composite build");
             c->launches++;
         }
         unsigned long long used = 0;

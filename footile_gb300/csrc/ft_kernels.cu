@@ -857,10 +857,27 @@ __device__ void build_outline(const KParams& P, CState& S, const float4* spts, c
 // `limit` is the vertex capacity of pts/ss (a warp stops with S.overflow set beyond it).
 // STROKE (Plotter::stroke, plotter.rs:356-365, first half): collects the stroke points
 // with their widths in spts[0..S.s_count) and the sub-strokes in subs[0..S.s_nsubs).
+// Global raw store of a CTA figure build (SCR_RAWG ...); null: windows of raw
+// vertices in shared memory, each emitted by re-walking the ops that reach it.
+struct RawStore {
+    float4* p4 = nullptr;
+    unsigned char* rs = nullptr;
+    unsigned char* jp = nullptr;
+    int* opi = nullptr;
+};
+__device__ __forceinline__ RawStore raw_store(unsigned char* scr) {
+    RawStore r;
+    r.p4 = reinterpret_cast<float4*>(scr + SCR_RAWG);
+    r.rs = scr + SCR_RSG;
+    r.jp = scr + SCR_JPG;
+    r.opi = reinterpret_cast<int*>(scr + SCR_OPIG);
+    return r;
+}
+
 template <class G, bool STROKE = false>
 __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, BuildSmemT<G::N, G::RAW>& B,
                            CompactSmem* Cs, CState& S, int2* pts, int* ss, int limit, float4* spts = nullptr,
-                           SubRec* subs = nullptr, int* opi = nullptr) {
+                           SubRec* subs = nullptr, int* opi = nullptr, RawStore rg = RawStore()) {
     constexpr int N = G::N;
     const int tid = G::rank();
     if (tid == 0) {
@@ -1019,71 +1036,139 @@ __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, B
                 S.last_pc_kind = B.kind[last_pc];
             }
         }
-        // ---- emit and compact window by window
-        for (int w0 = 0; w0 < total; w0 += WIN) {
-            const int w1 = min(w0 + WIN, total);
-            if (n > 0 && off < w1 && off + n > w0) {
-                const int lo = max(w0, off) - off, hi = min(w1, off + n) - off;
-                if (STROKE) {
-                    // stroke points keep f32 coordinates and their width (stroker.rs:204-225)
-                    float4* raw4 = reinterpret_cast<float4*>(B.raw);
-                    auto emit = [&](int k, P2 q, float w) {
-                        const int idx = off + k - w0;
-                        raw4[idx] = make_float4(q.x, q.y, w, 0.f);
-                        B.rs[idx] = (k == 0) ? (unsigned char)rs : (unsigned char)0;
-                        // a Move closes the previous sub-stroke open, a Close joined (F7)
-                        B.rs[SRAW + idx] = (unsigned char)(kind != FT_OP_MOVE);
-                        opi[idx] = i;
-                    };
-                    if (kind == FT_OP_MOVE || kind == FT_OP_LINE) {
-                        emit(0, A, sw_i);
-                    } else if (nonfinite) {
-                        emit(0, kind == FT_OP_QUAD ? C : D, kind == FT_OP_QUAD ? wc : wd);
-                    } else if (kind == FT_OP_QUAD) {
-                        int dh = 0;
-                        quad_walk<true>(A, Bq, C, wa, wb, wc, tol_sq, lo, hi, &dh, emit);
-                    } else {
-                        int dh = 0;
-                        cubic_walk<true>(A, Bq, C, D, wa, wb, wc, wd, tol_sq, lo, hi, &dh, emit);
-                    }
-                } else {
-                    auto emit = [&](int k, P2 q, float) {
-                        int idx = off + k - w0;
-                        B.raw[idx] = make_int2(f2fx(q.x), f2fx(q.y));
-                        B.rs[idx] = (k == 0) ? (unsigned char)rs : (unsigned char)0;
-                    };
-                    if (kind == FT_OP_MOVE || kind == FT_OP_LINE) {
-                        emit(0, A, 0.f);
-                    } else if (nonfinite) {
-                        emit(0, kind == FT_OP_QUAD ? C : D, 0.f);
-                    } else if (n <= LEAF_CACHE) {
-                        for (int k = lo; k < hi; k++) {
-                            const int idx = off + k - w0;
-                            B.raw[idx] = cache[k];
-                            B.rs[idx] = (k == 0) ? (unsigned char)rs : (unsigned char)0;
+        if (G::N != 32 && rg.p4 && total > WIN) {
+            // ---- a chunk of several windows: emit every op's vertices once into the raw
+            //      store (super-windows of RAWG when the chunk has more), then compact the
+            //      store window by window
+            for (int g0 = 0; g0 < total; g0 += RAWG) {
+                const int g1 = min(g0 + RAWG, total);
+                if (n > 0 && off < g1 && off + n > g0) {
+                    const int lo = max(g0, off) - off, hi = min(g1, off + n) - off;
+                    if (STROKE) {
+                        auto emit = [&](int k, P2 q, float w) {
+                            const int idx = off + k - g0;
+                            rg.p4[idx] = make_float4(q.x, q.y, w, 0.f);
+                            rg.rs[idx] = (k == 0) ? (unsigned char)rs : (unsigned char)0;
+                            rg.jp[idx] = (unsigned char)(kind != FT_OP_MOVE);
+                            rg.opi[idx] = i;
+                        };
+                        if (kind == FT_OP_MOVE || kind == FT_OP_LINE) {
+                            emit(0, A, sw_i);
+                        } else if (nonfinite) {
+                            emit(0, kind == FT_OP_QUAD ? C : D, kind == FT_OP_QUAD ? wc : wd);
+                        } else if (kind == FT_OP_QUAD) {
+                            int dh = 0;
+                            quad_walk<true>(A, Bq, C, wa, wb, wc, tol_sq, lo, hi, &dh, emit);
+                        } else {
+                            int dh = 0;
+                            cubic_walk<true>(A, Bq, C, D, wa, wb, wc, wd, tol_sq, lo, hi, &dh, emit);
                         }
-                    } else if (kind == FT_OP_QUAD) {
-                        int dh = 0;
-                        quad_walk<false>(A, Bq, C, 0.f, 0.f, 0.f, tol_sq, lo, hi, &dh, emit);
                     } else {
-                        int dh = 0;
-                        cubic_walk<false>(A, Bq, C, D, 0.f, 0.f, 0.f, 0.f, tol_sq, lo, hi, &dh, emit);
+                        int2* raw2 = reinterpret_cast<int2*>(rg.p4);
+                        auto emit = [&](int k, P2 q, float) {
+                            const int idx = off + k - g0;
+                            raw2[idx] = make_int2(f2fx(q.x), f2fx(q.y));
+                            rg.rs[idx] = (k == 0) ? (unsigned char)rs : (unsigned char)0;
+                        };
+                        if (kind == FT_OP_MOVE || kind == FT_OP_LINE) {
+                            emit(0, A, 0.f);
+                        } else if (nonfinite) {
+                            emit(0, kind == FT_OP_QUAD ? C : D, 0.f);
+                        } else if (n <= LEAF_CACHE) {
+                            for (int k = lo; k < hi; k++) {
+                                const int idx = off + k - g0;
+                                raw2[idx] = cache[k];
+                                rg.rs[idx] = (k == 0) ? (unsigned char)rs : (unsigned char)0;
+                            }
+                        } else if (kind == FT_OP_QUAD) {
+                            int dh = 0;
+                            quad_walk<false>(A, Bq, C, 0.f, 0.f, 0.f, tol_sq, lo, hi, &dh, emit);
+                        } else {
+                            int dh = 0;
+                            cubic_walk<false>(A, Bq, C, D, 0.f, 0.f, 0.f, 0.f, tol_sq, lo, hi, &dh, emit);
+                        }
                     }
                 }
+                G::sync();
+                for (int w0 = g0; w0 < g1; w0 += WIN) {
+                    const int w1 = min(w0 + WIN, g1), o = w0 - g0;
+                    if (STROKE)
+                        compact_stroke_block(S, rg.p4 + o, rg.rs + o, rg.jp + o, rg.opi + o, w1 - w0, spts, subs, *Cs);
+                    else
+                        compact_window_block(S, reinterpret_cast<const int2*>(rg.p4) + o, rg.rs + o, w1 - w0, pts, ss,
+                                             *Cs);
+                    G::sync();
+                    if (S.capped || S.overflow || S.s_capped) break;
+                }
+                if (S.capped || S.overflow || S.s_capped) break;
             }
-            G::sync();
-            if (STROKE) {
-                compact_stroke_block(S, reinterpret_cast<const float4*>(B.raw), B.rs, B.rs + SRAW, opi, w1 - w0,
-                                     spts, subs, *Cs);
-            } else if (N == 32) {
-                compact_window(S, B.raw, B.rs, w1 - w0, pts, ss, limit);
-            } else if (BLOCK_COMPACT) {
-                compact_window_block(S, B.raw, B.rs, w1 - w0, pts, ss, *Cs);
-            } else if (tid < 32) {
-                compact_window(S, B.raw, B.rs, w1 - w0, pts, ss, limit);
+        } else {
+            // ---- emit and compact window by window
+            for (int w0 = 0; w0 < total; w0 += WIN) {
+                const int w1 = min(w0 + WIN, total);
+                if (n > 0 && off < w1 && off + n > w0) {
+                    const int lo = max(w0, off) - off, hi = min(w1, off + n) - off;
+                    if (STROKE) {
+                        // stroke points keep f32 coordinates and their width (stroker.rs:204-225)
+                        float4* raw4 = reinterpret_cast<float4*>(B.raw);
+                        auto emit = [&](int k, P2 q, float w) {
+                            const int idx = off + k - w0;
+                            raw4[idx] = make_float4(q.x, q.y, w, 0.f);
+                            B.rs[idx] = (k == 0) ? (unsigned char)rs : (unsigned char)0;
+                            // a Move closes the previous sub-stroke open, a Close joined (F7)
+                            B.rs[SRAW + idx] = (unsigned char)(kind != FT_OP_MOVE);
+                            opi[idx] = i;
+                        };
+                        if (kind == FT_OP_MOVE || kind == FT_OP_LINE) {
+                            emit(0, A, sw_i);
+                        } else if (nonfinite) {
+                            emit(0, kind == FT_OP_QUAD ? C : D, kind == FT_OP_QUAD ? wc : wd);
+                        } else if (kind == FT_OP_QUAD) {
+                            int dh = 0;
+                            quad_walk<true>(A, Bq, C, wa, wb, wc, tol_sq, lo, hi, &dh, emit);
+                        } else {
+                            int dh = 0;
+                            cubic_walk<true>(A, Bq, C, D, wa, wb, wc, wd, tol_sq, lo, hi, &dh, emit);
+                        }
+                    } else {
+                        auto emit = [&](int k, P2 q, float) {
+                            int idx = off + k - w0;
+                            B.raw[idx] = make_int2(f2fx(q.x), f2fx(q.y));
+                            B.rs[idx] = (k == 0) ? (unsigned char)rs : (unsigned char)0;
+                        };
+                        if (kind == FT_OP_MOVE || kind == FT_OP_LINE) {
+                            emit(0, A, 0.f);
+                        } else if (nonfinite) {
+                            emit(0, kind == FT_OP_QUAD ? C : D, 0.f);
+                        } else if (n <= LEAF_CACHE) {
+                            for (int k = lo; k < hi; k++) {
+                                const int idx = off + k - w0;
+                                B.raw[idx] = cache[k];
+                                B.rs[idx] = (k == 0) ? (unsigned char)rs : (unsigned char)0;
+                            }
+                        } else if (kind == FT_OP_QUAD) {
+                            int dh = 0;
+                            quad_walk<false>(A, Bq, C, 0.f, 0.f, 0.f, tol_sq, lo, hi, &dh, emit);
+                        } else {
+                            int dh = 0;
+                            cubic_walk<false>(A, Bq, C, D, 0.f, 0.f, 0.f, 0.f, tol_sq, lo, hi, &dh, emit);
+                        }
+                    }
+                }
+                G::sync();
+                if (STROKE) {
+                    compact_stroke_block(S, reinterpret_cast<const float4*>(B.raw), B.rs, B.rs + SRAW, opi, w1 - w0,
+                                         spts, subs, *Cs);
+                } else if (N == 32) {
+                    compact_window(S, B.raw, B.rs, w1 - w0, pts, ss, limit);
+                } else if (BLOCK_COMPACT) {
+                    compact_window_block(S, B.raw, B.rs, w1 - w0, pts, ss, *Cs);
+                } else if (tid < 32) {
+                    compact_window(S, B.raw, B.rs, w1 - w0, pts, ss, limit);
+                }
+                G::sync();
+                if (S.capped || S.overflow || S.s_capped) break;
             }
-            G::sync();
-            if (S.capped || S.overflow || S.s_capped) break;
         }
         G::sync();
         if (S.capped || S.overflow || S.s_capped) break;
@@ -1538,11 +1623,11 @@ __global__ void __launch_bounds__(BLOCK) k_raster(KParams P) {
         if (STROKE) {
             // Plotter::stroke: stroke points, sub-strokes, outline, then the NonZero fill
             int* opi = reinterpret_cast<int*>(smem + cs_off + ((sizeof(CompactSmem) + 15) & ~(size_t)15));
-            build_fill<BlockG, true>(P, d, sw0, B, Cs, S, pts, ss, PT_CAP, spts, subs, opi);
+            build_fill<BlockG, true>(P, d, sw0, B, Cs, S, pts, ss, PT_CAP, spts, subs, opi, raw_store(scr));
             finish_subs(P, d, S, subs, B.scan);
             build_outline(P, S, spts, subs, B, *Cs, pts, ss);
         } else {
-            build_fill<BlockG>(P, d, sw0, B, Cs, S, pts, ss, PT_CAP);
+            build_fill<BlockG>(P, d, sw0, B, Cs, S, pts, ss, PT_CAP, nullptr, nullptr, nullptr, raw_store(scr));
         }
         if (S.count > 0) {
             top_and_dir<BlockG>(S, pts, ss, s_tmp3);
@@ -1566,8 +1651,14 @@ __global__ void __launch_bounds__(BLOCK) k_raster(KParams P) {
     }
 }
 
-cudaError_t launch_raster(const KParams& p, int grid, int smem_bytes, cudaStream_t s) {
+// Shared-memory carve-out (percent of the SM's unified L1) when a launch has at most
+// one CTA per SM: the rest stays L1 for the curve walks' local-memory stacks.
+constexpr int FEW_CTAS_CARVEOUT = 25;
+
+cudaError_t launch_raster(const KParams& p, int grid, int smem_bytes, cudaStream_t s, bool few_ctas) {
     auto kern = p.stroke ? k_raster<true> : k_raster<false>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         few_ctas ? FEW_CTAS_CARVEOUT : (int)cudaSharedmemCarveoutDefault);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
     if (e != cudaSuccess) return e;
     kern<<<grid, BLOCK, smem_bytes, s>>>(p);
@@ -1701,11 +1792,11 @@ __global__ void __launch_bounds__(BLOCK) k_cbuild(KParams P) {
         const ft_path_desc d = P.paths[it];
         if (STROKE) {
             int* opi = reinterpret_cast<int*>(smem + cs_off + ((sizeof(CompactSmem) + 15) & ~(size_t)15));
-            build_fill<BlockG, true>(P, d, d.s_width, B, Cs, S, pts, ss, PT_CAP, spts, subs, opi);
+            build_fill<BlockG, true>(P, d, d.s_width, B, Cs, S, pts, ss, PT_CAP, spts, subs, opi, raw_store(scr));
             finish_subs(P, d, S, subs, B.scan);
             build_outline(P, S, spts, subs, B, *Cs, pts, ss);
         } else {
-            build_fill<BlockG>(P, d, d.s_width, B, Cs, S, pts, ss, PT_CAP);
+            build_fill<BlockG>(P, d, d.s_width, B, Cs, S, pts, ss, PT_CAP, nullptr, nullptr, nullptr, raw_store(scr));
         }
         if (S.count > 0) {
             top_and_dir<BlockG>(S, pts, ss, s_tmp3);
@@ -1889,8 +1980,10 @@ __global__ void __launch_bounds__(BLOCK) k_cbands(KParams P) {
 
 int composite_bands_smem(int band_rows, int width) { return FTAB_BYTES + band_rows * row_smem_bytes(width); }
 
-cudaError_t launch_composite_build(const KParams& p, int grid, int smem_bytes, cudaStream_t s) {
+cudaError_t launch_composite_build(const KParams& p, int grid, int smem_bytes, cudaStream_t s, bool few_ctas) {
     auto kern = p.stroke ? k_cbuild<true> : k_cbuild<false>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         few_ctas ? FEW_CTAS_CARVEOUT : (int)cudaSharedmemCarveoutDefault);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
     if (e != cudaSuccess) return e;
     kern<<<grid, BLOCK, smem_bytes, s>>>(p);

@@ -51,7 +51,15 @@ constexpr size_t SCR_EDGES = align256(SCR_SS + (size_t)PT_CAP * sizeof(int));   
 constexpr size_t SCR_SPTS = align256(SCR_EDGES + (size_t)PT_CAP * sizeof(EdgeRec));  // float4[PT_CAP] stroke points
 constexpr size_t SCR_SUBS = align256(SCR_SPTS + (size_t)PT_CAP * sizeof(float4));    // SubRec[PT_CAP] sub-strokes
 constexpr size_t SCR_SOFF = align256(SCR_SUBS + (size_t)PT_CAP * sizeof(SubRec));    // int[2*PT_CAP+8] offsets
-constexpr size_t SCRATCH_BYTES_PER_CTA = align256(SCR_SOFF + (size_t)(2 * PT_CAP + 8) * sizeof(int));
+// Raw (pre-dedupe) vertices of one chunk of ops, emitted once by all threads and
+// compacted window by window (CTA figure builds): positions as int2 (fills) or float4
+// with the width (strokes), sub-figure start flags, stroke join flags, source ops.
+constexpr int RAWG = 32768;
+constexpr size_t SCR_RAWG = align256(SCR_SOFF + (size_t)(2 * PT_CAP + 8) * sizeof(int));  // float4[RAWG]
+constexpr size_t SCR_RSG = align256(SCR_RAWG + (size_t)RAWG * 16);                         // u8[RAWG]
+constexpr size_t SCR_JPG = align256(SCR_RSG + (size_t)RAWG);                               // u8[RAWG]
+constexpr size_t SCR_OPIG = align256(SCR_JPG + (size_t)RAWG);                              // int[RAWG]
+constexpr size_t SCRATCH_BYTES_PER_CTA = align256(SCR_OPIG + (size_t)RAWG * sizeof(int));
 
 // Warp rasteriser (one warp per small path): per-warp share of the CTA scratch.
 constexpr int WARP_CAP = 8191;        // vertices a warp holds; larger figures go to a CTA
@@ -98,7 +106,9 @@ struct KParams {
 };
 
 // Ordered composite: per-path figure build and edge binning, then one CTA per band.
-cudaError_t launch_composite_build(const KParams& p, int grid, int smem_bytes, cudaStream_t s);
+// `few_ctas`: at most one CTA per SM — prefer L1 over shared memory (the curve walks'
+// stacks are in local memory).
+cudaError_t launch_composite_build(const KParams& p, int grid, int smem_bytes, cudaStream_t s, bool few_ctas);
 cudaError_t launch_composite_bands(const KParams& p, int smem_bytes, cudaStream_t s);
 int composite_bands_smem(int band_rows, int width);
 int composite_build_blocks_per_sm(int smem_bytes, bool stroke);
@@ -107,7 +117,7 @@ int composite_build_blocks_per_sm(int smem_bytes, bool stroke);
 constexpr int RASTER_FIXED_SMEM = BLOCK * (int)sizeof(EdgeRec) + 3 * BLOCK * 4 + 256 + 4096;
 
 // Launch the persistent rasteriser.  Returns the CUDA error of the launch.
-cudaError_t launch_raster(const KParams& p, int grid, int smem_bytes, cudaStream_t s);
+cudaError_t launch_raster(const KParams& p, int grid, int smem_bytes, cudaStream_t s, bool few_ctas);
 // Launch the warp rasteriser (small paths).  Its dynamic shared memory is fixed.
 cudaError_t launch_raster_warp(const KParams& p, int grid, cudaStream_t s);
 int raster_warp_smem();
