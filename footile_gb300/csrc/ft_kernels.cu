@@ -1729,11 +1729,29 @@ __device__ void bin_edges(const KParams& P, uint32_t path, const CState& S, cons
     const int rb = count > 0 ? max(S.top_row, 0) : H;  // first raster row footile writes
     for (int b = tid; b < nb; b += BLOCK) hist[b] = 0;
     __syncthreads();
-    for (int e = tid; e < count; e += BLOCK) {
-        const EdgeRec E = edges[e];
-        if (!E.ed) continue;
-        const int lo = max(E.start_row - tmin, rb), hi = min(E.end_row - tmin, H - 1);
-        for (int b = lo / R; lo <= hi && b <= hi / R; b++) atomicAdd(&hist[b], 1);
+    // several edges per thread per step, loaded before they are used (one CTA may bin
+    // a whole figure alone: keep several L2 loads in flight); the count pass reads only
+    // the half of each record with its rows (step_pix, ed, start_row, end_row)
+    auto rows_of = [&](const int4& q, int& lo, int& hi) {
+        lo = max(q.z - tmin, rb);
+        hi = min(q.w - tmin, H - 1);
+        return q.y != 0 && lo <= hi;
+    };
+    const int4* erec = reinterpret_cast<const int4*>(edges);
+    constexpr int EU = 4;
+    for (int e0 = 0; e0 < count; e0 += BLOCK * EU) {
+        int4 q[EU];
+#pragma unroll
+        for (int u = 0; u < EU; u++) {
+            const int e = e0 + u * BLOCK + tid;
+            q[u] = e < count ? erec[2 * e + 1] : make_int4(0, 0, 0, 0);
+        }
+#pragma unroll
+        for (int u = 0; u < EU; u++) {
+            int lo, hi;
+            if (rows_of(q[u], lo, hi))
+                for (int b = lo / R; b <= hi / R; b++) atomicAdd(&hist[b], 1);
+        }
     }
     __syncthreads();
     int carry = 0;
@@ -1757,11 +1775,25 @@ __device__ void bin_edges(const KParams& P, uint32_t path, const CState& S, cons
     }
     __syncthreads();
     if (fits) {
-        for (int e = tid; e < count; e += BLOCK) {
-            const EdgeRec E = edges[e];
-            if (!E.ed) continue;
-            const int lo = max(E.start_row - tmin, rb), hi = min(E.end_row - tmin, H - 1);
-            for (int b = lo / R; lo <= hi && b <= hi / R; b++) P.pool[base + (unsigned)atomicAdd(&hist[b], 1)] = E;
+        constexpr int FU = 2;
+        for (int e0 = 0; e0 < count; e0 += BLOCK * FU) {
+            int4 q0[FU], q1[FU];
+#pragma unroll
+            for (int u = 0; u < FU; u++) {
+                const int e = e0 + u * BLOCK + tid;
+                q0[u] = e < count ? erec[2 * e] : make_int4(0, 0, 0, 0);
+                q1[u] = e < count ? erec[2 * e + 1] : make_int4(0, 0, 0, 0);
+            }
+#pragma unroll
+            for (int u = 0; u < FU; u++) {
+                int lo, hi;
+                if (!rows_of(q1[u], lo, hi)) continue;
+                for (int b = lo / R; b <= hi / R; b++) {
+                    int4* dst = reinterpret_cast<int4*>(P.pool + base + (unsigned)atomicAdd(&hist[b], 1));
+                    dst[0] = q0[u];
+                    dst[1] = q1[u];
+                }
+            }
         }
     }
     __syncthreads();
