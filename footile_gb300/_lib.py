@@ -43,6 +43,8 @@ def load(auto_build=True):
             "ft_set_join": ([P, i32, f32], ctypes.c_int),
             "ft_set_pen_width": ([P, f32], ctypes.c_int),
             "ft_get_pen_width": ([P, ctypes.POINTER(f32)], ctypes.c_int),
+            "ft_set_figure_cap": ([P, u32], ctypes.c_int),
+            "ft_get_figure_cap": ([P, ctypes.POINTER(u32)], ctypes.c_int),
             "ft_fill": ([P, i32, P, u32, i32, P, P, u32, u32, u32, i32], ctypes.c_int),
             "ft_stroke": ([P, P, u32, i32, P, P, u32, u32, u32, i32], ctypes.c_int),
             "ft_fill_batch": ([P, i32, i32, P, u32, P, u32, i32, P, u64, i32], ctypes.c_int),
@@ -93,7 +95,7 @@ def exported_symbols():
         "ft_adjoint_destroy", "ft_set_tuning", "ft_get_tuning", "ft_autotune_batch",
         "ft_convert", "ft_srcover_forward", "ft_srcover_backward", "ft_stroke_composite_forward",
         "ft_stroke_composite_backward", "ft_stroke_composite_status", "ft_stroke_composite_chunk",
-        "ft_stroke_composite_destroy")]
+        "ft_stroke_composite_destroy", "ft_set_figure_cap", "ft_get_figure_cap")]
 
 
 class Tuning(ctypes.Structure):
@@ -145,6 +147,16 @@ class Context:
 
     def set_pen_width(self, w):
         self.check(self.L.ft_set_pen_width(self.h, w))
+
+    def set_figure_cap(self, max_points):
+        """Un-capped figures (a documented extension): fills keep up to `max_points`
+        vertices per figure; 0 restores footile's 65,535 (`ft_set_figure_cap`)."""
+        self.check(self.L.ft_set_figure_cap(self.h, int(max_points)))
+
+    def figure_cap(self):
+        v = ctypes.c_uint32()
+        self.check(self.L.ft_get_figure_cap(self.h, ctypes.byref(v)))
+        return v.value
 
     def pen_width(self):
         v = ctypes.c_float()

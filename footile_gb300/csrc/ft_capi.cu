@@ -67,6 +67,7 @@ struct ft_ctx {
     uint64_t launches = 0;
     int sm_count = 0;
     int max_smem = 0;
+    uint32_t fig_cap = 0;  // vertices per figure of a fill above footile's 65,535 (0: footile's cap)
     ft_tuning tune{0, 0, 0, 0};
     bool tuned = false;  // `tune` replaces the built-in plan defaults
     std::string err;
@@ -213,6 +214,8 @@ void fill_params(ft_ctx* c, ftk::KParams& p, int stroke, int rule, int fmt, int 
     p.fmt = fmt;
     p.stroke = stroke;
     p.smem_bytes = smem;
+    p.pt_cap = ftk::PT_CAP;
+    p.L = ftk::scr_layout(ftk::PT_CAP);
 }
 
 int grid_for(ft_ctx* c, int smem, uint32_t n_items, bool stroke) {
@@ -367,9 +370,10 @@ int single(ft_ctx* c, int stroke, int32_t rule, const ft_op* ops, uint32_t n_ops
     } else if ((reinterpret_cast<uintptr_t>(ops) & 15) || (fmt == FT_RGBA8P && (reinterpret_cast<uintptr_t>(raster) & 3))) {
         return fail(c, FT_ERR_ARG, "device ops need 16-byte alignment, Rgba8p rasters 4-byte alignment");
     }
-    if ((uint64_t)w * h >= split_px(c) && ftk::composite_bands_smem(1, (int)w) <= c->max_smem) {
-        // a large canvas: build the figure once and bin its edges, then one CTA per
-        // band of rows (the ordered compositor with a single call)
+    const bool uncapped = !stroke && c->fig_cap > (uint32_t)ftk::PT_CAP;
+    if ((uncapped || (uint64_t)w * h >= split_px(c)) && ftk::composite_bands_smem(1, (int)w) <= c->max_smem) {
+        // a large canvas, or an un-capped fill: build the figure once and bin its edges,
+        // then one CTA per band of rows (the ordered compositor with a single call)
         float sw0 = c->s_width;
         FT_CU(cudaMemcpyAsync(&sw0, swd, sizeof(float), cudaMemcpyDeviceToHost, c->stream), "pen width");
         FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
@@ -661,6 +665,19 @@ FT_API int ft_set_pen_width(ft_ctx* c, float w) {
     return FT_OK;
 }
 
+FT_API int ft_set_figure_cap(ft_ctx* c, uint32_t max_points) {
+    if (!c) return FT_ERR_ARG;
+    if (max_points > ftk::FIG_CAP_MAX) return fail(c, FT_ERR_ARG, "figure cap above FT_FIG_CAP_MAX");
+    c->fig_cap = max_points <= (uint32_t)ftk::PT_CAP ? 0u : max_points;
+    return FT_OK;
+}
+
+FT_API int ft_get_figure_cap(ft_ctx* c, uint32_t* max_points) {
+    if (!c || !max_points) return FT_ERR_ARG;
+    *max_points = c->fig_cap ? c->fig_cap : (uint32_t)ftk::PT_CAP;
+    return FT_OK;
+}
+
 FT_API int ft_get_pen_width(ft_ctx* c, float* w) {
     if (!c || !w) return FT_ERR_ARG;
     if (c->sw_on_device && c->sw_chain.p) {
@@ -789,9 +806,13 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
     FT_CU(c->crec.ensure(sizeof(int4) * std::max(n_paths, 1u)), "alloc path records");
     FT_CU(c->bandoff.ensure(sizeof(int) * (size_t)std::max(n_paths, 1u) * (n_bands + 1)), "alloc band offsets");
     FT_CU(c->pool_used.ensure(sizeof(unsigned long long)), "alloc pool counter");
-    const int grid = std::max(1, std::min((int)std::max(n_paths, 1u),
-                                          c->sm_count * ftk::composite_build_blocks_per_sm(smem_a, stroke != 0)));
-    FT_CU(c->scratch.ensure(ftk::SCRATCH_BYTES_PER_CTA * (size_t)grid), "alloc scratch");
+    // un-capped fills: every CTA's scratch holds a figure of fig_cap vertices (8 GB in all at most)
+    const bool uncapped = !stroke && c->fig_cap > (uint32_t)ftk::PT_CAP;
+    const ftk::ScrLayout L = ftk::scr_layout(uncapped ? c->fig_cap : ftk::PT_CAP);
+    int grid = std::max(1, std::min((int)std::max(n_paths, 1u),
+                                    c->sm_count * ftk::composite_build_blocks_per_sm(smem_a, stroke != 0)));
+    if (uncapped) grid = (int)std::max<size_t>(1, std::min<size_t>((size_t)grid, (8ull << 30) / L.bytes));
+    FT_CU(c->scratch.ensure(L.bytes * (size_t)grid), "alloc scratch");
     if (n_paths)
         FT_CU(cudaMemcpyAsync(c->paths.p, paths, sizeof(ft_path_desc) * n_paths, cudaMemcpyHostToDevice, c->stream),
               "upload paths");
@@ -826,6 +847,8 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
         p.bandoff = static_cast<int*>(c->bandoff.p);
         p.crec = static_cast<int4*>(c->crec.p);
         p.sw_out = sw_out;
+        p.pt_cap = uncapped ? (int)c->fig_cap : ftk::PT_CAP;
+        p.L = L;
         FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
         if (n_paths) {
             FT_CU(ftk::launch_composite_build(p, grid, smem_a, c->stream, grid <= c->sm_count),

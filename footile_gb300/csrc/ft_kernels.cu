@@ -342,7 +342,8 @@ static_assert(offsetof(WarpBuildSmem, raw) % 8 == 0, "warp build smem alignment"
 // ------------------------------------------------------------ figure builder
 // Sequential restatement of Fig::add_point / Fig::close (fig.rs:373-461) for one
 // group of raw vertices; used for the group in which the 65,535 cap is reached.
-__device__ void seq_group(CState& S, const int2* raw, const unsigned char* rsf, int n, int2* pts, int* ss) {
+__device__ void seq_group(CState& S, const int2* raw, const unsigned char* rsf, int n, int2* pts, int* ss,
+                          int cap = PT_CAP) {
     int count = S.count, has_prev = S.has_prev;
     int px = S.prev_x, py = S.prev_y, rfx = S.rf_x, rfy = S.rf_y, rf_pos = S.rf_pos;
     for (int l = 0; l < n; l++) {
@@ -351,7 +352,7 @@ __device__ void seq_group(CState& S, const int2* raw, const unsigned char* rsf, 
         // a close event precedes a vertex that starts a sub-figure: pop when the
         // last vertex equals the sub-figure start (fig.rs:373-383)
         if (rs && has_prev && rfx == px && rfy == py) count -= 1;
-        if (count >= PT_CAP) {
+        if (count >= cap) {
             // add_point is ignored from here on (fig.rs:430).  The next close —
             // an explicit one or the one Plotter::fill ends with — pops the last
             // vertex if it equals the open sub-figure's start.
@@ -504,7 +505,7 @@ __device__ __forceinline__ int mask_prev(const unsigned* m, int i) {
 }
 
 __device__ void compact_window_block(CState& S, const int2* raw, const unsigned char* rsf, int m, int2* pts,
-                                     int* ss, CompactSmem& C) {
+                                     int* ss, CompactSmem& C, int cap = PT_CAP) {
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     for (int base = 0; base < m; base += BLOCK) {
         const int k = base + tid;
@@ -544,9 +545,9 @@ __device__ void compact_window_block(CState& S, const int2* raw, const unsigned 
         const int ex = block_excl_sum((keep ? 1 : 0) - (pop ? 1 : 0), C.scan, tot);
         const int pos = count_b + ex;
         C.posv[tid] = pos;
-        const int capped = __syncthreads_or(keep && pos >= PT_CAP);
+        const int capped = __syncthreads_or(keep && pos >= cap);
         if (capped) {
-            if (tid == 0) seq_group(S, raw + base, rsf + base, nb, pts, ss);
+            if (tid == 0) seq_group(S, raw + base, rsf + base, nb, pts, ss, cap);
             __syncthreads();
             return;
         }
@@ -865,12 +866,12 @@ struct RawStore {
     unsigned char* jp = nullptr;
     int* opi = nullptr;
 };
-__device__ __forceinline__ RawStore raw_store(unsigned char* scr) {
+__device__ __forceinline__ RawStore raw_store(unsigned char* scr, const ScrLayout& L = scr_layout(PT_CAP)) {
     RawStore r;
-    r.p4 = reinterpret_cast<float4*>(scr + SCR_RAWG);
-    r.rs = scr + SCR_RSG;
-    r.jp = scr + SCR_JPG;
-    r.opi = reinterpret_cast<int*>(scr + SCR_OPIG);
+    r.p4 = reinterpret_cast<float4*>(scr + L.rawg);
+    r.rs = scr + L.rsg;
+    r.jp = scr + L.jpg;
+    r.opi = reinterpret_cast<int*>(scr + L.opig);
     return r;
 }
 
@@ -1096,7 +1097,7 @@ __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, B
                         compact_stroke_block(S, rg.p4 + o, rg.rs + o, rg.jp + o, rg.opi + o, w1 - w0, spts, subs, *Cs);
                     else
                         compact_window_block(S, reinterpret_cast<const int2*>(rg.p4) + o, rg.rs + o, w1 - w0, pts, ss,
-                                             *Cs);
+                                             *Cs, limit);
                     G::sync();
                     if (S.capped || S.overflow || S.s_capped) break;
                 }
@@ -1162,7 +1163,7 @@ __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, B
                 } else if (N == 32) {
                     compact_window(S, B.raw, B.rs, w1 - w0, pts, ss, limit);
                 } else if (BLOCK_COMPACT) {
-                    compact_window_block(S, B.raw, B.rs, w1 - w0, pts, ss, *Cs);
+                    compact_window_block(S, B.raw, B.rs, w1 - w0, pts, ss, *Cs, limit);
                 } else if (tid < 32) {
                     compact_window(S, B.raw, B.rs, w1 - w0, pts, ss, limit);
                 }
@@ -1806,12 +1807,13 @@ __global__ void __launch_bounds__(BLOCK) k_cbuild(KParams P) {
     __shared__ int s_item;
     __shared__ int s_tmp3[3 * NWARP];
     const int tid = threadIdx.x;
-    unsigned char* scr = P.scratch + (size_t)blockIdx.x * SCRATCH_BYTES_PER_CTA;
-    int2* pts = reinterpret_cast<int2*>(scr + SCR_PTS);
-    int* ss = reinterpret_cast<int*>(scr + SCR_SS);
-    EdgeRec* edges = reinterpret_cast<EdgeRec*>(scr + SCR_EDGES);
-    float4* spts = reinterpret_cast<float4*>(scr + SCR_SPTS);
-    SubRec* subs = reinterpret_cast<SubRec*>(scr + SCR_SUBS);
+    const ScrLayout L = P.L;
+    unsigned char* scr = P.scratch + (size_t)blockIdx.x * L.bytes;
+    int2* pts = reinterpret_cast<int2*>(scr + L.pts);
+    int* ss = reinterpret_cast<int*>(scr + L.ss);
+    EdgeRec* edges = reinterpret_cast<EdgeRec*>(scr + L.edges);
+    float4* spts = reinterpret_cast<float4*>(scr + L.spts);
+    SubRec* subs = reinterpret_cast<SubRec*>(scr + L.subs);
     BuildSmem& B = *reinterpret_cast<BuildSmem*>(smem);
     const size_t cs_off = (sizeof(BuildSmem) + 15) & ~(size_t)15;
     CompactSmem* Cs = reinterpret_cast<CompactSmem*>(smem + cs_off);
@@ -1824,11 +1826,12 @@ __global__ void __launch_bounds__(BLOCK) k_cbuild(KParams P) {
         const ft_path_desc d = P.paths[it];
         if (STROKE) {
             int* opi = reinterpret_cast<int*>(smem + cs_off + ((sizeof(CompactSmem) + 15) & ~(size_t)15));
-            build_fill<BlockG, true>(P, d, d.s_width, B, Cs, S, pts, ss, PT_CAP, spts, subs, opi, raw_store(scr));
+            build_fill<BlockG, true>(P, d, d.s_width, B, Cs, S, pts, ss, PT_CAP, spts, subs, opi, raw_store(scr, L));
             finish_subs(P, d, S, subs, B.scan);
             build_outline(P, S, spts, subs, B, *Cs, pts, ss);
         } else {
-            build_fill<BlockG>(P, d, d.s_width, B, Cs, S, pts, ss, PT_CAP, nullptr, nullptr, nullptr, raw_store(scr));
+            build_fill<BlockG>(P, d, d.s_width, B, Cs, S, pts, ss, P.pt_cap, nullptr, nullptr, nullptr,
+                               raw_store(scr, L));
         }
         if (S.count > 0) {
             top_and_dir<BlockG>(S, pts, ss, s_tmp3);

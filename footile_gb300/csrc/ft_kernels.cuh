@@ -61,6 +61,32 @@ constexpr size_t SCR_JPG = align256(SCR_RSG + (size_t)RAWG);                    
 constexpr size_t SCR_OPIG = align256(SCR_JPG + (size_t)RAWG);                              // int[RAWG]
 constexpr size_t SCRATCH_BYTES_PER_CTA = align256(SCR_OPIG + (size_t)RAWG * sizeof(int));
 
+// Scratch layout of one CTA figure build for figures of up to `cap` vertices: the
+// SCR_* layout above for footile's cap, larger for the un-capped extension (fills).
+struct ScrLayout {
+    size_t pts, ss, edges, spts, subs, soff, rawg, rsg, jpg, opig, bytes;
+};
+constexpr ScrLayout scr_layout(size_t cap) {
+    ScrLayout L{};
+    L.pts = 0;
+    L.ss = align256(L.pts + cap * sizeof(int2));
+    L.edges = align256(L.ss + cap * sizeof(int));
+    L.spts = align256(L.edges + cap * sizeof(EdgeRec));
+    L.subs = align256(L.spts + (size_t)PT_CAP * sizeof(float4));
+    L.soff = align256(L.subs + (size_t)PT_CAP * sizeof(SubRec));
+    L.rawg = align256(L.soff + (size_t)(2 * PT_CAP + 8) * sizeof(int));
+    L.rsg = align256(L.rawg + (size_t)RAWG * 16);
+    L.jpg = align256(L.rsg + (size_t)RAWG);
+    L.opig = align256(L.jpg + (size_t)RAWG);
+    L.bytes = align256(L.opig + (size_t)RAWG * sizeof(int));
+    return L;
+}
+static_assert(scr_layout(PT_CAP).bytes == SCRATCH_BYTES_PER_CTA && scr_layout(PT_CAP).rawg == SCR_RAWG &&
+                  scr_layout(PT_CAP).edges == SCR_EDGES && scr_layout(PT_CAP).subs == SCR_SUBS,
+              "scratch layouts agree");
+// Largest figure of the un-capped extension (ft_set_figure_cap).
+constexpr uint32_t FIG_CAP_MAX = 1u << 26;
+
 // Warp rasteriser (one warp per small path): per-warp share of the CTA scratch.
 constexpr int WARP_CAP = 8191;        // vertices a warp holds; larger figures go to a CTA
 constexpr int WARP_MAX_SIDE = 512;    // canvases up to this width and height use the warp rasteriser
@@ -103,6 +129,9 @@ struct KParams {
     unsigned long long pool_cap;    // edges
     int* bandoff;                // per path: n_bands + 1 offsets into its pool run
     int4* crec;                  // per path: rowbegin, tmin, pool offset lo, pool offset hi
+    // figure builds of the ordered compositor (k_cbuild): vertex cap and scratch layout
+    int pt_cap;                  // PT_CAP, or more for un-capped fills
+    ScrLayout L;                 // scr_layout(pt_cap); gridDim.x * L.bytes of scratch
 };
 
 // Ordered composite: per-path figure build and edge binning, then one CTA per band.

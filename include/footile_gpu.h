@@ -115,6 +115,17 @@ FT_API int ft_set_join(ft_ctx* ctx, int32_t join, float miter_limit);
 FT_API int ft_set_pen_width(ft_ctx* ctx, float w);
 FT_API int ft_get_pen_width(ft_ctx* ctx, float* w);
 
+/* Un-capped figures — a documented extension, not footile's behaviour.  footile keeps at
+ * most FT_MAX_POINTS vertices per figure (Vid is u16; Fig::add_point ignores the rest,
+ * fig.rs:428-442, vid.rs:9-70).  With a cap above that, fills (ft_fill and the fill calls
+ * of ft_composite_batch) keep up to `max_points` vertices per figure, with 32-bit vertex
+ * ids and otherwise footile's algorithm; vertices past the cap are still dropped.  0 (or
+ * any value up to FT_MAX_POINTS) restores footile's cap.  Strokes and ft_fill_batch keep
+ * footile's caps.  Each figure build holds about 45 bytes of device scratch per vertex. */
+#define FT_FIG_CAP_MAX (1u << 26)
+FT_API int ft_set_figure_cap(ft_ctx* ctx, uint32_t max_points);
+FT_API int ft_get_figure_cap(ft_ctx* ctx, uint32_t* max_points);
+
 /* ---- single-path calls ------------------------------------------------ */
 
 /* Plotter::fill (src/plotter.rs:339-350).  `raster` is `h` rows of `stride` bytes in

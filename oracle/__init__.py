@@ -27,16 +27,19 @@ def build():
 
 class Params(ctypes.Structure):
     _fields_ = [("tolerance", ctypes.c_float), ("transform", ctypes.c_float * 6),
-                ("join", ctypes.c_int32), ("miter_limit", ctypes.c_float)]
+                ("join", ctypes.c_int32), ("miter_limit", ctypes.c_float), ("fig_cap", ctypes.c_uint32)]
 
 
-def make_params(tolerance=0.3, transform=_abi.IDENTITY, join=_abi.JOIN_MITER, miter_limit=4.0):
+def make_params(tolerance=0.3, transform=_abi.IDENTITY, join=_abi.JOIN_MITER, miter_limit=4.0, fig_cap=0):
+    """`fig_cap` above 65,535: fills keep that many vertices per figure (u32 vertex ids),
+    the un-capped extension; 0 is footile's 65,535-vertex Fig."""
     p = Params()
     p.tolerance = tolerance
     for i in range(6):
         p.transform[i] = transform[i]
     p.join = join
     p.miter_limit = miter_limit
+    p.fig_cap = fig_cap
     return p
 
 

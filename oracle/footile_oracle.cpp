@@ -181,23 +181,26 @@ static inline i32 row_of(i32 y) { return fx_to_int(y); }  // fig.rs:167-169
 // fig.rs:677-682
 static inline i16 pixel_cov(i32 fcov) { return (i16)fx_to_int(fx_round(fx_shl(fcov, 8))); }
 
-struct SubFig {
-    u16 start;
+// Vertex ids are V: footile's u16 (vid.rs:9-70), or u32 for the un-capped extension.
+template <class V>
+struct SubFigT {
+    V start;
     size_t n_points;
     bool done;
-    u16 next(u16 vid, FigDir dir) const {  // fig.rs:143-163
+    V next(V vid, FigDir dir) const {  // fig.rs:143-163
         if (dir == Forward) {
-            u16 v = (u16)(vid + 1);
-            return v < (u16)(start + n_points) ? v : start;
+            V v = (V)(vid + 1);
+            return v < (V)(start + n_points) ? v : start;
         }
-        if (vid > start) return (u16)(vid - 1);
-        if (n_points > 0) return (u16)(start + n_points - 1);
+        if (vid > start) return (V)(vid - 1);
+        if (n_points > 0) return (V)(start + n_points - 1);
         return start;
     }
 };
 
-struct Edge {  // fig.rs:47-66
-    u16 v1;
+template <class V>
+struct EdgeT {  // fig.rs:47-66
+    V v1;
     i32 y_upper, y_lower;
     FigDir dir;
     i32 step_pix, inv_slope, x_bot, min_x, max_x;
@@ -206,9 +209,9 @@ struct Edge {  // fig.rs:47-66
         if (dx != 0) return std::min(fx_abs(fx_div(dy, dx)), FX_ONE);
         return 0;
     }
-    static Edge make(u16 v0, u16 v1, FxPt p0, FxPt p1, FigDir dir) {  // fig.rs:179-201
+    static EdgeT make(V v0, V v1, FxPt p0, FxPt p1, FigDir dir) {  // fig.rs:179-201
         (void)v0;
-        Edge e;
+        EdgeT e;
         i32 dx = wsub(p1.x, p0.x);
         i32 dy = wsub(p1.y, p0.y);
         e.step_pix = calculate_step(dx, dy);
@@ -308,15 +311,20 @@ struct PlotDest {
     virtual ~PlotDest() {}
 };
 
-struct Fig : PlotDest {
+// `cap`: footile's 65,535 vertices (Fig::add_point, fig.rs:430); larger only for the
+// un-capped extension (u32 ids).
+template <class V>
+struct FigT : PlotDest {
+    using SubFig = SubFigT<V>;
     std::vector<FxPt> points;
     std::vector<SubFig> subs;
-    Fig() {
+    size_t cap = 65535;
+    FigT() {
         points.reserve(1024);
         subs.push_back(SubFig{0, 0, false});
     }
     SubFig& sub_current() { return subs.back(); }
-    void sub_add() { subs.push_back(SubFig{(u16)points.size(), 0, false}); }
+    void sub_add() { subs.push_back(SubFig{(V)points.size(), 0, false}); }
     bool is_coincident(FxPt p) const { return !points.empty() && points.back() == p; }
     void sub_set_done() {  // fig.rs:373-383
         SubFig& sub = sub_current();
@@ -329,13 +337,13 @@ struct Fig : PlotDest {
             sub.done = true;
         }
     }
-    const SubFig& sub_at(u16 vid) const {  // fig.rs:386-394
+    const SubFig& sub_at(V vid) const {  // fig.rs:386-394
         for (const SubFig& s : subs)
-            if (vid < (u16)(s.start + s.n_points)) return s;
+            if (vid < (V)(s.start + s.n_points)) return s;
         abort();  // unreachable!() in footile
     }
-    u16 next(u16 vid, FigDir dir) const { return sub_at(vid).next(vid, dir); }
-    FigDir get_dir(u16 vid) const {  // fig.rs:402-411
+    V next(V vid, FigDir dir) const { return sub_at(vid).next(vid, dir); }
+    FigDir get_dir(V vid) const {  // fig.rs:402-411
         FxPt p = points[vid];
         FxPt p0 = points[next(vid, Forward)];
         FxPt p1 = points[next(vid, Reverse)];
@@ -343,7 +351,7 @@ struct Fig : PlotDest {
     }
     void add_point_pt(Pt pt) {  // fig.rs:428-442
         size_t n = points.size();
-        if (n < 65535) {
+        if (n < cap) {
             bool done = sub_current().done;
             if (done) sub_add();
             FxPt p{fx_from_f32(pt.x), fx_from_f32(pt.y)};
@@ -361,7 +369,10 @@ struct Fig : PlotDest {
 };
 
 // fig.rs:505-666  Scanner
-struct Scanner {
+template <class V>
+struct ScannerT {
+    using Fig = FigT<V>;
+    using Edge = EdgeT<V>;
     const Fig& fig;
     int rule;
     FigDir dir;
@@ -371,16 +382,16 @@ struct Scanner {
     std::vector<i16>& sgn_area;
     std::vector<Edge> edges;
 
-    Scanner(const Fig& f, int rule_, FigDir d, Raster& r_, u32 rb, const uint8_t* c, std::vector<i16>& sa)
+    ScannerT(const Fig& f, int rule_, FigDir d, Raster& r_, u32 rb, const uint8_t* c, std::vector<i16>& sa)
         : fig(f), rule(rule_), dir(d), r(r_), row_begin(rb), clr(c), sgn_area(sa) {}
 
-    void scan_vertices(const std::vector<u16>& vids, i32 top_row) {
+    void scan_vertices(const std::vector<V>& vids, i32 top_row) {
         size_t vi = 0;
         i32 y_row = top_row;
         for (u32 row = row_begin; row < r.h; row++) {
             scan_continuing_edges(y_row);
             while (vi < vids.size()) {
-                u16 vid = vids[vi];
+                V vid = vids[vi];
                 if (row_of(fig.points[vid].y) > y_row) break;
                 vi++;
                 update_edges(vid, Forward);
@@ -403,8 +414,8 @@ struct Scanner {
     void advance_edges() {
         for (Edge& e : edges) e.x_bot = wadd(e.x_bot, e.inv_slope);
     }
-    void update_edges(u16 vid, FigDir d) {
-        u16 v = fig.next(vid, d);
+    void update_edges(V vid, FigDir d) {
+        V v = fig.next(vid, d);
         if (v != vid) {
             i32 y = fig.points[vid].y;
             i32 yv = fig.points[v].y;
@@ -414,7 +425,7 @@ struct Scanner {
                 remove_edge(vid, opposite(d));
         }
     }
-    void add_edge(u16 v0, u16 v1, FigDir d) {
+    void add_edge(V v0, V v1, FigDir d) {
         Edge e = Edge::make(v0, v1, fig.points[v0], fig.points[v1], d);
         i16 cov = e.starting_cov();
         if (cov > 0) {
@@ -423,7 +434,7 @@ struct Scanner {
         }
         edges.push_back(e);
     }
-    void remove_edge(u16 v1, FigDir d) {
+    void remove_edge(V v1, FigDir d) {
         for (size_t i = 0; i < edges.size(); i++) {
             if (edges[i].v1 == v1 && edges[i].dir == d) {
                 edges[i] = edges.back();  // swap_remove
@@ -458,13 +469,19 @@ struct Scanner {
     }
 };
 
+using SubFig = SubFigT<u16>;
+using Edge = EdgeT<u16>;
+using Fig = FigT<u16>;
+using Scanner = ScannerT<u16>;
+
 // fig.rs:480-502
-static void fig_fill(const Fig& fig, int rule, Raster& r, const uint8_t* clr, std::vector<i16>& sgn_area) {
+template <class V>
+static void fig_fill(const FigT<V>& fig, int rule, Raster& r, const uint8_t* clr, std::vector<i16>& sgn_area) {
     size_t n = fig.points.size();
     if (n == 0) return;
-    std::vector<u16> vids(n);
-    for (size_t i = 0; i < n; i++) vids[i] = (u16)i;
-    std::stable_sort(vids.begin(), vids.end(), [&](u16 a, u16 b) {
+    std::vector<V> vids(n);
+    for (size_t i = 0; i < n; i++) vids[i] = (V)i;
+    std::stable_sort(vids.begin(), vids.end(), [&](V a, V b) {
         const FxPt& p0 = fig.points[a];
         const FxPt& p1 = fig.points[b];
         if (p0.y != p1.y) return p0.y < p1.y;
@@ -474,7 +491,7 @@ static void fig_fill(const Fig& fig, int rule, Raster& r, const uint8_t* clr, st
     i32 top_row = row_of(fig.points[vids[0]].y);
     u32 row_begin = (u32)std::max(top_row, 0);
     if (row_begin >= r.h) return;
-    Scanner s(fig, rule, dir, r, row_begin, clr, sgn_area);
+    ScannerT<V> s(fig, rule, dir, r, row_begin, clr, sgn_area);
     s.scan_vertices(vids, top_row);
 }
 
@@ -660,6 +677,7 @@ struct Plotter {
     int join;
     float miter_limit;
     int status;
+    size_t fig_cap = 0;  // vertices per figure above footile's 65,535: the un-capped extension
 
     Plotter(Raster rr, float tol, const float* m, int j, float ml, float sw)
         : r(rr), sgn_area(rr.w, 0), xf(), join(j), miter_limit(ml), status(0) {
@@ -763,6 +781,14 @@ struct Plotter {
     }
     // plotter.rs:339-350
     void fill(int rule, const ft_op* ops, size_t n, const uint8_t* clr) {
+        if (fig_cap > 65535) {  // un-capped extension: u32 vertex ids, `fig_cap` vertices
+            FigT<u32> fig;
+            fig.cap = fig_cap;
+            add_ops(ops, n, fig);
+            fig.close_fig();
+            fig_fill(fig, rule, r, clr, sgn_area);
+            return;
+        }
         Fig fig;
         add_ops(ops, n, fig);
         fig.close_fig();
@@ -788,6 +814,7 @@ typedef struct orc_params {
     float transform[6];
     int32_t join;
     float miter_limit;
+    uint32_t fig_cap;  // 0: footile's 65,535-vertex figures; larger: the un-capped extension (fills)
 } orc_params;
 
 static const float ORC_IDENTITY[6] = {1, 0, 0, 0, 1, 0};
@@ -803,6 +830,7 @@ static int orc_run(int stroke, int32_t rule, const ft_op* ops, uint32_t n_ops, i
     float sw = s_width_inout ? *s_width_inout : 1.0f;
     static const uint8_t zero_clr[4] = {0, 0, 0, 0};
     orc::Plotter p(r, tol, m, join, ml, sw);
+    if (prm && !stroke) p.fig_cap = prm->fig_cap;
     if (stroke)
         p.stroke(ops, n_ops, clr ? clr : zero_clr);
     else
