@@ -134,6 +134,12 @@ def extra_scene(ctx, stream, dev, cpu=True):
     stroke()
     out["stroke_w8_round_matte8_ms"] = _events_ms(stream, stroke, 3)
     ctx.set_join(_abi.JOIN_MITER, 4.0)
+    # the un-capped extension: every sub-path kept (about 6 M vertices in one figure)
+    ctx.set_figure_cap(8 << 20)
+    fill(_abi.NONZERO, _abi.MATTE8, m_d, w)
+    out["uncapped_nonzero_matte8_ms"] = _events_ms(stream, lambda: fill(_abi.NONZERO, _abi.MATTE8, m_d, w), 3)
+    out["uncapped_coverage_fraction"] = float((m_d != 0).float().mean().item())
+    ctx.set_figure_cap(0)
     # composite bytes: every Rgba8p pixel from the top row down is read and written
     out["rgba8p_composite_GBps"] = (w * h * 8) / (out["nonzero_rgba8p_ms"] * 1e-3) / 1e9
     # pix's Rgba8p -> SRgba8 step of footile's examples, on the device (HBM-bound):
