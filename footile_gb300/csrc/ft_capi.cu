@@ -54,6 +54,7 @@ struct ft_ctx {
     // device buffers
     DevBuf ops, paths, items, items_w, overflow, status, sw_out, rasters, queue, scratch, sw_chain;
     DevBuf pool, pool_used, bandoff, crec;  // ordered composite
+    DevBuf figbins;                         // one path's figure state and band counts (split binning)
     DevBuf srgb_lut, conv_src, conv_dst;    // ft_convert
     std::vector<ftk::WorkItem> h_items, h_items_w;
     // the plan behind h_items / items on the device, reused while the same batch comes back
@@ -620,7 +621,7 @@ FT_API void ft_ctx_destroy(ft_ctx* c) {
     DevBuf* bufs[] = {&c->ops,     &c->paths,   &c->items,   &c->items_w, &c->overflow,
                       &c->status,  &c->sw_out,  &c->rasters, &c->queue,   &c->scratch,
                       &c->sw_chain, &c->pool,   &c->pool_used, &c->bandoff, &c->crec,
-                      &c->srgb_lut, &c->conv_src, &c->conv_dst};
+                      &c->srgb_lut, &c->conv_src, &c->conv_dst, &c->figbins};
     for (DevBuf* b : bufs) b->release();
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
@@ -827,6 +828,12 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
         FT_CU(cudaMemsetAsync(c->queue.p, 0, 256, c->stream), "reset queue");
         FT_CU(cudaMemsetAsync(c->status.p, 0, sizeof(int32_t) * std::max(n_paths, 1u), c->stream), "reset status");
         FT_CU(cudaMemsetAsync(c->pool_used.p, 0, sizeof(unsigned long long), c->stream), "reset pool");
+        // one path: its edges are built and binned over the whole GPU after the figure
+        const bool split = n_paths == 1;
+        if (split) {
+            FT_CU(c->figbins.ensure(16 + sizeof(int) * 2 * (size_t)std::max(n_bands, 1)), "alloc figure bins");
+            FT_CU(cudaMemsetAsync(c->figbins.p, 0, 16 + sizeof(int) * (size_t)n_bands, c->stream), "reset bins");
+        }
         ftk::KParams p;
         fill_params(c, p, stroke, rule, fmt, smem_a);
         p.ops = ops_d;
@@ -849,11 +856,20 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
         p.sw_out = sw_out;
         p.pt_cap = uncapped ? (int)c->fig_cap : ftk::PT_CAP;
         p.L = L;
+        if (split) {
+            p.split_bin = 1;
+            p.fig_state = static_cast<int4*>(c->figbins.p);
+            p.bin_hist = reinterpret_cast<int*>(static_cast<char*>(c->figbins.p) + 16);
+        }
         FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
         if (n_paths) {
             FT_CU(ftk::launch_composite_build(p, grid, smem_a, c->stream, grid <= c->sm_count),
                   "launch composite build");
             c->launches++;
+            if (split) {
+                FT_CU(ftk::launch_figure_bins(p, 4 * c->sm_count, c->stream), "launch figure bins");
+                c->launches += 3;
+            }
         }
         unsigned long long used = 0;
         FT_CU(cudaMemcpyAsync(&used, c->pool_used.p, sizeof(used), cudaMemcpyDeviceToHost, c->stream), "pool size");

@@ -1253,45 +1253,50 @@ __device__ void top_and_dir(CState& S, const int2* pts, const int* ss, int* tmp3
 }
 
 // One edge per non-horizontal segment (fig.rs:179-201, 576-600).
+// Edge from vertex i to the next vertex of its sub-figure (fig.rs:179-210, 402-411): its
+// rows, slope and direction relative to the figure's; horizontal and degenerate edges
+// have ed == 0.
+__device__ __forceinline__ EdgeRec edge_rec(int i, int count, int figdir, const int2* pts, const int* ss) {
+    const int s = ss[i];
+    const int nx = (i + 1 < count && ss[i + 1] == s) ? i + 1 : s;
+    EdgeRec e;
+    e.ed = 0;
+    e.y_upper = e.y_lower = e.x_bot0 = e.inv_slope = e.step_pix = e.start_row = e.end_row = 0;
+    if (nx != i) {
+        int2 a = pts[i], b = pts[nx];
+        if (a.y != b.y) {
+            int2 up, lo;
+            int edir;
+            if (b.y > a.y) {
+                up = a;
+                lo = b;
+                edir = 0;
+            } else {
+                up = b;
+                lo = a;
+                edir = 1;
+            }
+            const int dx = wsub(lo.x, up.x), dy = wsub(lo.y, up.y);
+            const int step = dx != 0 ? min(fxabs(fxdiv(dy, dx)), FX_ONE) : 0;
+            const int inv = fxdiv(dx, dy);
+            const int ybot = wsub(fxfloor(wadd(up.y, FX_ONE)), up.y);
+            e.y_upper = up.y;
+            e.y_lower = lo.y;
+            e.x_bot0 = wadd(up.x, fxmul(inv, ybot));
+            e.inv_slope = inv;
+            e.step_pix = step;
+            e.ed = (edir == figdir) ? 1 : -1;
+            e.start_row = up.y >> 16;
+            e.end_row = lo.y >> 16;
+        }
+    }
+    return e;
+}
+
 template <class G>
 __device__ void build_edges(const CState& S, const int2* pts, const int* ss, EdgeRec* edges) {
     const int count = S.count, figdir = S.dir;
-    for (int i = G::rank(); i < count; i += G::N) {
-        const int s = ss[i];
-        const int nx = (i + 1 < count && ss[i + 1] == s) ? i + 1 : s;
-        EdgeRec e;
-        e.ed = 0;
-        e.y_upper = e.y_lower = e.x_bot0 = e.inv_slope = e.step_pix = e.start_row = e.end_row = 0;
-        if (nx != i) {
-            int2 a = pts[i], b = pts[nx];
-            if (a.y != b.y) {
-                int2 up, lo;
-                int edir;
-                if (b.y > a.y) {
-                    up = a;
-                    lo = b;
-                    edir = 0;
-                } else {
-                    up = b;
-                    lo = a;
-                    edir = 1;
-                }
-                const int dx = wsub(lo.x, up.x), dy = wsub(lo.y, up.y);
-                const int step = dx != 0 ? min(fxabs(fxdiv(dy, dx)), FX_ONE) : 0;
-                const int inv = fxdiv(dx, dy);
-                const int ybot = wsub(fxfloor(wadd(up.y, FX_ONE)), up.y);
-                e.y_upper = up.y;
-                e.y_lower = lo.y;
-                e.x_bot0 = wadd(up.x, fxmul(inv, ybot));
-                e.inv_slope = inv;
-                e.step_pix = step;
-                e.ed = (edir == figdir) ? 1 : -1;
-                e.start_row = up.y >> 16;
-                e.end_row = lo.y >> 16;
-            }
-        }
-        edges[i] = e;
-    }
+    for (int i = G::rank(); i < count; i += G::N) edges[i] = edge_rec(i, count, figdir, pts, ss);
 }
 
 // Signed cell areas of one edge on one scan row (fig.rs:238-321), added into
@@ -1833,12 +1838,19 @@ __global__ void __launch_bounds__(BLOCK) k_cbuild(KParams P) {
             build_fill<BlockG>(P, d, d.s_width, B, Cs, S, pts, ss, P.pt_cap, nullptr, nullptr, nullptr,
                                raw_store(scr, L));
         }
-        if (S.count > 0) {
-            top_and_dir<BlockG>(S, pts, ss, s_tmp3);
-            build_edges<BlockG>(S, pts, ss, edges);
+        if (P.split_bin) {
+            // the figure's edges are built and binned by launch_figure_bins
+            if (S.count > 0) top_and_dir<BlockG>(S, pts, ss, s_tmp3);
+            __syncthreads();
+            if (tid == 0) P.fig_state[it] = make_int4(S.count, S.dir, S.top_row, 0);
+        } else {
+            if (S.count > 0) {
+                top_and_dir<BlockG>(S, pts, ss, s_tmp3);
+                build_edges<BlockG>(S, pts, ss, edges);
+            }
+            __syncthreads();
+            bin_edges(P, (uint32_t)it, S, edges, reinterpret_cast<int*>(smem), s_tmp3);
         }
-        __syncthreads();
-        bin_edges(P, (uint32_t)it, S, edges, reinterpret_cast<int*>(smem), s_tmp3);
         if (P.sw_out) {  // pen width after the call: the last PenWidth op of the path
             int lp = -1;
             for (int i = tid; i < (int)d.n_ops; i += BLOCK)
@@ -2014,6 +2026,95 @@ __global__ void __launch_bounds__(BLOCK) k_cbands(KParams P) {
 }
 
 int composite_bands_smem(int band_rows, int width) { return FTAB_BYTES + band_rows * row_smem_bytes(width); }
+
+// ---- edges and band bins of one path's figure over the whole GPU (split_bin); the
+//      figure was built by CTA 0 of k_cbuild.  Band rows follow bin_edges.
+struct FigBins {
+    int count, figdir, H, R, nb, tmin, rb;
+};
+__device__ __forceinline__ FigBins fig_bins(const KParams& P) {
+    const int4 fs = P.fig_state[0];
+    FigBins f;
+    f.count = fs.x;
+    f.figdir = fs.y;
+    f.H = (int)P.canvas_h;
+    f.R = P.band_rows;
+    f.nb = P.n_bands;
+    f.tmin = min(fs.z, 0);
+    f.rb = f.count > 0 ? max(fs.z, 0) : f.H;
+    return f;
+}
+
+__global__ void __launch_bounds__(BLOCK) k_fig_edges(KParams P) {
+    const FigBins f = fig_bins(P);
+    const unsigned char* scr = P.scratch;
+    const int2* pts = reinterpret_cast<const int2*>(scr + P.L.pts);
+    const int* ss = reinterpret_cast<const int*>(scr + P.L.ss);
+    EdgeRec* edges = reinterpret_cast<EdgeRec*>(P.scratch + P.L.edges);
+    for (int e = blockIdx.x * BLOCK + threadIdx.x; e < f.count; e += gridDim.x * BLOCK) {
+        const EdgeRec E = edge_rec(e, f.count, f.figdir, pts, ss);
+        edges[e] = E;
+        if (!E.ed) continue;
+        const int lo = max(E.start_row - f.tmin, f.rb), hi = min(E.end_row - f.tmin, f.H - 1);
+        for (int b = lo / f.R; lo <= hi && b <= hi / f.R; b++) atomicAdd(&P.bin_hist[b], 1);
+    }
+}
+
+__global__ void __launch_bounds__(BLOCK) k_fig_bin_scan(KParams P) {
+    __shared__ int tmp[2 * NWARP + 2];
+    __shared__ unsigned long long s_base;
+    const FigBins f = fig_bins(P);
+    const int tid = threadIdx.x;
+    int carry = 0;
+    for (int b0 = 0; b0 < f.nb; b0 += BLOCK) {
+        const int b = b0 + tid;
+        int tot;
+        const int off = block_excl_sum(b < f.nb ? P.bin_hist[b] : 0, tmp, tot);
+        if (b < f.nb) P.bin_hist[f.nb + b] = carry + off;  // fill cursors
+        carry += tot;
+    }
+    if (tid == 0) s_base = atomicAdd(P.pool_used, (unsigned long long)carry);
+    __syncthreads();
+    const unsigned long long base = s_base;
+    const bool fits = base + (unsigned long long)carry <= P.pool_cap;
+    for (int b = tid; b <= f.nb; b += BLOCK) P.bandoff[b] = fits ? (b < f.nb ? P.bin_hist[f.nb + b] : carry) : 0;
+    if (tid == 0) {
+        P.crec[0] = make_int4(f.rb, f.tmin, (int)(unsigned)(base & 0xFFFFFFFFull), (int)(unsigned)(base >> 32));
+        P.fig_state[0].w = fits ? 1 : 0;
+        if (!fits) atomicMax(&P.status[0], FT_ERR_CAP);  // the host grows the pool and runs again
+    }
+}
+
+__global__ void __launch_bounds__(BLOCK) k_fig_bin_fill(KParams P) {
+    const FigBins f = fig_bins(P);
+    if (!P.fig_state[0].w) return;
+    const int4 cr = P.crec[0];
+    const unsigned long long base = (unsigned long long)(unsigned)cr.z | ((unsigned long long)(unsigned)cr.w << 32);
+    const int4* erec = reinterpret_cast<const int4*>(P.scratch + P.L.edges);
+    int* cursor = P.bin_hist + f.nb;
+    for (int e = blockIdx.x * BLOCK + threadIdx.x; e < f.count; e += gridDim.x * BLOCK) {
+        const int4 q1 = erec[2 * e + 1];  // step_pix, ed, start_row, end_row
+        if (!q1.y) continue;
+        const int4 q0 = erec[2 * e];
+        const int lo = max(q1.z - f.tmin, f.rb), hi = min(q1.w - f.tmin, f.H - 1);
+        for (int b = lo / f.R; lo <= hi && b <= hi / f.R; b++) {
+            int4* dst = reinterpret_cast<int4*>(P.pool + base + (unsigned)atomicAdd(&cursor[b], 1));
+            dst[0] = q0;
+            dst[1] = q1;
+        }
+    }
+}
+
+cudaError_t launch_figure_bins(const KParams& p, int grid, cudaStream_t s) {
+    k_fig_edges<<<grid, BLOCK, 0, s>>>(p);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_fig_bin_scan<<<1, BLOCK, 0, s>>>(p);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_fig_bin_fill<<<grid, BLOCK, 0, s>>>(p);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_composite_build(const KParams& p, int grid, int smem_bytes, cudaStream_t s, bool few_ctas) {
     auto kern = p.stroke ? k_cbuild<true> : k_cbuild<false>;

@@ -132,6 +132,11 @@ struct KParams {
     // figure builds of the ordered compositor (k_cbuild): vertex cap and scratch layout
     int pt_cap;                  // PT_CAP, or more for un-capped fills
     ScrLayout L;                 // scr_layout(pt_cap); gridDim.x * L.bytes of scratch
+    // one path (split_bin): k_cbuild stops after the figure and its direction, the
+    // grid-wide kernels below build and bin its edges
+    int split_bin;
+    int4* fig_state;             // count, direction, top row, edges fit the pool
+    int* bin_hist;               // n_bands counts, then n_bands fill cursors
 };
 
 // Ordered composite: per-path figure build and edge binning, then one CTA per band.
@@ -139,6 +144,9 @@ struct KParams {
 // stacks are in local memory).
 cudaError_t launch_composite_build(const KParams& p, int grid, int smem_bytes, cudaStream_t s, bool few_ctas);
 cudaError_t launch_composite_bands(const KParams& p, int smem_bytes, cudaStream_t s);
+// Edges and band bins of a single path's figure (after k_cbuild with split_bin), over
+// the whole GPU: edge records and band counts, a scan and pool allocation, the fill.
+cudaError_t launch_figure_bins(const KParams& p, int grid, cudaStream_t s);
 int composite_bands_smem(int band_rows, int width);
 int composite_build_blocks_per_sm(int smem_bytes, bool stroke);
 
