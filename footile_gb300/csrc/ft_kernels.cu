@@ -40,10 +40,9 @@
 namespace ftk {
 
 constexpr unsigned FULL = 0xFFFFFFFFu;
-// Curve leaves kept from the count pass for the emit pass (local memory): a warp's 32
-// ops keep 16 each, a CTA's 256 ops 64 each (fewer ops re-walked in the emit).
-template <int N>
-constexpr int leaf_cache() { return N == 32 ? 16 : 64; }
+// Curve leaves of an op kept (in local memory) from the count pass for the emit pass;
+// ops with more leaves are walked again.
+constexpr int LEAF_CACHE = 64;
 constexpr bool BLOCK_COMPACT = true;  // figure building by the whole CTA (false: warp 0)
 constexpr int SRAW = 1024;            // stroke points per window (float4 in the raw window's bytes)
 
@@ -989,7 +988,6 @@ __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, B
         int n = 0;
         int depth_hit = 0;
         bool nonfinite = false;
-        constexpr int LEAF_CACHE = leaf_cache<N>();
         int2 cache[LEAF_CACHE];  // leaves of the count pass, reused by the emit pass
         auto keep_leaf = [&](int k, P2 q, float) {
             if (k < LEAF_CACHE) cache[k] = make_int2(f2fx(q.x), f2fx(q.y));
