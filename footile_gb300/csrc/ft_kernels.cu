@@ -1475,8 +1475,10 @@ struct WarpSmem {
 };
 static_assert(offsetof(WarpSmem, row) % 16 == 0 && sizeof(WarpSmem) % 16 == 0, "warp smem alignment");
 
+// The active edge list holds the records themselves (one load per edge and row from a
+// list that stays small and hot, instead of an index and a record of the figure's edges).
 __device__ void raster_sweep_warp(const KParams& P, const ft_path_desc& d, const CState& S, const EdgeRec* edges,
-                                  int* sorted, int* active, int* hist, int* row) {
+                                  int* sorted, EdgeRec* active, int* hist, int* row) {
     const int lane = threadIdx.x & 31;
     const int count = S.count, H = (int)d.height, W = (int)d.width, Wp = (W + 3) & ~3;
     const int top_row = S.top_row, row_begin = max(top_row, 0);
@@ -1518,24 +1520,24 @@ __device__ void raster_sweep_warp(const KParams& P, const ft_path_desc& d, const
     for (int s = 0; s < nrows; s++) {
         const int y = top_row + s;
         const int bs = s == 0 ? 0 : hist[s - 1], be = hist[s];
-        for (int k = lane; k < be - bs; k += 32) active[n_act + k] = sorted[bs + k];
+        for (int k = lane; k < be - bs; k += 32) active[n_act + k] = edges[sorted[bs + k]];
         n_act += be - bs;
         __syncwarp();
         int nn = 0;
         for (int a0 = 0; a0 < n_act; a0 += 32) {
             const int idx = a0 + lane;
             const bool v = idx < n_act;
-            int e = 0, end_row = INT_MIN;
+            EdgeRec E;
+            int end_row = INT_MIN;
             if (v) {
-                e = active[idx];
-                const EdgeRec E = edges[e];
+                E = active[idx];
                 end_row = E.end_row;
                 scan_item(E, y, row, W);
             }
             // an edge leaves the active list after its last row (fig.rs:582, 603-617)
             const bool keep = v && end_row > y;
             const unsigned km = __ballot_sync(FULL, keep);
-            if (keep) active[nn + __popc(km & ((1u << lane) - 1u))] = e;
+            if (keep) active[nn + __popc(km & ((1u << lane) - 1u))] = E;
             nn += __popc(km);
         }
         n_act = nn;
@@ -1545,7 +1547,7 @@ __device__ void raster_sweep_warp(const KParams& P, const ft_path_desc& d, const
     }
 }
 
-__global__ void __launch_bounds__(BLOCK) k_raster_warp(KParams P) {
+__global__ void __launch_bounds__(BLOCK, 4) k_raster_warp(KParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     WarpSmem& M = reinterpret_cast<WarpSmem*>(smem)[warp];
@@ -1554,7 +1556,7 @@ __global__ void __launch_bounds__(BLOCK) k_raster_warp(KParams P) {
     int* ss = reinterpret_cast<int*>(scr + WS_SS);
     EdgeRec* edges = reinterpret_cast<EdgeRec*>(scr + WS_EDGES);
     int* sorted = reinterpret_cast<int*>(scr + WS_SORT);
-    int* active = reinterpret_cast<int*>(scr + WS_ACT);
+    EdgeRec* active = reinterpret_cast<EdgeRec*>(scr + WS_ACT);
     for (;;) {
         int it = 0;
         if (lane == 0) it = (int)atomicAdd(&P.queue[1], 1u);
