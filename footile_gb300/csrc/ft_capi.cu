@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -40,6 +41,22 @@ struct DevBuf {
 
 struct ft_batch;
 
+namespace {
+// A planned batch: the descriptors it was planned for, its work items on the host and the
+// device, and the plan knobs; kept while the same batch comes back.
+struct PlanSlot {
+    std::vector<ft_path_desc> paths;
+    std::vector<ftk::WorkItem> h_items, h_items_w;
+    DevBuf items, items_w;
+    int smem = -1, stroke = -1, wside = -1;
+    uint64_t split = 0;
+    void release() {
+        items.release();
+        items_w.release();
+    }
+};
+}  // namespace
+
 struct ft_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -52,15 +69,14 @@ struct ft_ctx {
     float s_width = 1.0f;   // host copy, valid unless sw_on_device
     bool sw_on_device = false;
     // device buffers
-    DevBuf ops, paths, items, items_w, overflow, status, sw_out, rasters, queue, scratch, sw_chain;
+    DevBuf ops, paths, overflow, status, sw_out, rasters, queue, scratch, sw_chain;
     DevBuf pool, pool_used, bandoff, crec;  // ordered composite
     DevBuf figbins;                         // one path's figure state and band counts (split binning)
     DevBuf srgb_lut, conv_src, conv_dst;    // ft_convert
-    std::vector<ftk::WorkItem> h_items, h_items_w;
-    // the plan behind h_items / items on the device, reused while the same batch comes back
-    std::vector<ft_path_desc> plan_paths;
-    int plan_smem = -1, plan_stroke = -1, plan_wside = -1;
-    uint64_t plan_split = 0;
+    PlanSlot plan;                                   // the last batch's plan
+    std::vector<std::unique_ptr<PlanSlot>> chunk_plans;  // host batches in pipelined chunks
+    cudaStream_t s_in = nullptr, s_out = nullptr;    // their copy streams
+    std::vector<cudaEvent_t> ev_chunk;               // copied in / drawn, per chunk
     uint32_t last_n_paths = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
@@ -249,28 +265,30 @@ cudaError_t enqueue(const ftk::KParams& p, int grid_b, int grid_w, int smem, cud
 }
 
 // Queue, statuses, launch.  `ops_d` / `rasters_d` are device pointers.
-int run(ft_ctx* c, int stroke, int rule, const ft_op* ops_d, const ft_path_desc* paths, uint32_t n_paths, int fmt,
-        uint8_t* rasters_d, const float* sw_chain, float* sw_out) {
+// Plan (or reuse the plan of `slot`), upload and launch one batch on the context stream;
+// per-path statuses go to status_d.
+int run_plan(ft_ctx* c, PlanSlot& slot, int stroke, int rule, const ft_op* ops_d, const ft_path_desc* paths,
+             uint32_t n_paths, int fmt, uint8_t* rasters_d, const float* sw_chain, float* sw_out, int32_t* status_d,
+             bool events = true) {
     uint32_t max_w = 1;
     for (uint32_t i = 0; i < n_paths; i++) max_w = std::max(max_w, paths[i].width);
     const int smem = choose_smem(c, max_w);
     // a batch that comes back unchanged (same descriptors and plan knobs) keeps its
     // planned and uploaded work items
-    const bool same_plan = c->plan_smem == smem && c->plan_stroke == stroke && c->plan_wside == warp_max_side(c) &&
-                           c->plan_split == split_px(c) && c->plan_paths.size() == n_paths &&
-                           (n_paths == 0 || memcmp(c->plan_paths.data(), paths, sizeof(ft_path_desc) * n_paths) == 0);
+    const bool same_plan = slot.smem == smem && slot.stroke == stroke && slot.wside == warp_max_side(c) &&
+                           slot.split == split_px(c) && slot.paths.size() == n_paths &&
+                           (n_paths == 0 || memcmp(slot.paths.data(), paths, sizeof(ft_path_desc) * n_paths) == 0);
     if (!same_plan) {
-        c->plan_smem = -1;  // invalid until the new items are on the device
-        plan_items(c, paths, n_paths, smem, c->h_items, c->h_items_w, stroke != 0);
+        slot.smem = -1;  // invalid until the new items are on the device
+        plan_items(c, paths, n_paths, smem, slot.h_items, slot.h_items_w, stroke != 0);
     }
-    const uint32_t n_items = (uint32_t)c->h_items.size(), n_items_w = (uint32_t)c->h_items_w.size();
+    const uint32_t n_items = (uint32_t)slot.h_items.size(), n_items_w = (uint32_t)slot.h_items_w.size();
     FT_CU(c->paths.ensure(sizeof(ft_path_desc) * std::max(n_paths, 1u)), "alloc paths");
     if (!same_plan) {
-        FT_CU(c->items.ensure(sizeof(ftk::WorkItem) * std::max(n_items, 1u)), "alloc items");
-        FT_CU(c->items_w.ensure(sizeof(ftk::WorkItem) * std::max(n_items_w, 1u)), "alloc items");
+        FT_CU(slot.items.ensure(sizeof(ftk::WorkItem) * std::max(n_items, 1u)), "alloc items");
+        FT_CU(slot.items_w.ensure(sizeof(ftk::WorkItem) * std::max(n_items_w, 1u)), "alloc items");
     }
     FT_CU(c->overflow.ensure(sizeof(uint32_t) * std::max(n_items_w, 1u)), "alloc overflow list");
-    FT_CU(c->status.ensure(sizeof(int32_t) * std::max(n_paths, 1u)), "alloc status");
     FT_CU(c->queue.ensure(256), "alloc queue");
     const int grid = n_items_w ? std::max(grid_for(c, smem, n_items, stroke), c->sm_count)
                                : grid_for(c, smem, n_items, stroke);
@@ -280,43 +298,52 @@ int run(ft_ctx* c, int stroke, int rule, const ft_op* ops_d, const ft_path_desc*
           "upload paths");
     if (!same_plan) {
         if (n_items)
-            FT_CU(cudaMemcpyAsync(c->items.p, c->h_items.data(), sizeof(ftk::WorkItem) * n_items,
+            FT_CU(cudaMemcpyAsync(slot.items.p, slot.h_items.data(), sizeof(ftk::WorkItem) * n_items,
                                   cudaMemcpyHostToDevice, c->stream),
                   "upload items");
         if (n_items_w)
-            FT_CU(cudaMemcpyAsync(c->items_w.p, c->h_items_w.data(), sizeof(ftk::WorkItem) * n_items_w,
+            FT_CU(cudaMemcpyAsync(slot.items_w.p, slot.h_items_w.data(), sizeof(ftk::WorkItem) * n_items_w,
                                   cudaMemcpyHostToDevice, c->stream),
                   "upload items");
-        c->plan_paths.assign(paths, paths + n_paths);
-        c->plan_smem = smem;
-        c->plan_stroke = stroke;
-        c->plan_wside = warp_max_side(c);
-        c->plan_split = split_px(c);
+        slot.paths.assign(paths, paths + n_paths);
+        slot.smem = smem;
+        slot.stroke = stroke;
+        slot.wside = warp_max_side(c);
+        slot.split = split_px(c);
     }
     FT_CU(cudaMemsetAsync(c->queue.p, 0, 256, c->stream), "reset queue");
-    FT_CU(cudaMemsetAsync(c->status.p, 0, sizeof(int32_t) * std::max(n_paths, 1u), c->stream), "reset status");
+    if (n_paths) FT_CU(cudaMemsetAsync(status_d, 0, sizeof(int32_t) * n_paths, c->stream), "reset status");
     c->last_n_paths = n_paths;
     if (n_items == 0 && n_items_w == 0) return FT_OK;
     ftk::KParams p;
     fill_params(c, p, stroke, rule, fmt, smem);
     p.ops = ops_d;
     p.paths = static_cast<const ft_path_desc*>(c->paths.p);
-    p.items = static_cast<const ftk::WorkItem*>(c->items.p);
+    p.items = static_cast<const ftk::WorkItem*>(slot.items.p);
     p.n_items = n_items;
-    p.items_w = static_cast<const ftk::WorkItem*>(c->items_w.p);
+    p.items_w = static_cast<const ftk::WorkItem*>(slot.items_w.p);
     p.n_items_w = n_items_w;
     p.overflow = static_cast<uint32_t*>(c->overflow.p);
     p.queue = static_cast<uint32_t*>(c->queue.p);
     p.rasters = rasters_d;
-    p.status = static_cast<int32_t*>(c->status.p);
+    p.status = status_d;
     p.sw_out = sw_out;
     p.sw_chain = sw_chain;
     p.scratch = static_cast<unsigned char*>(c->scratch.p);
-    FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
+    if (events) FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
     FT_CU(enqueue(p, grid, grid_w, smem, c->stream, &c->launches, c->sm_count), "launch rasteriser");
-    FT_CU(cudaEventRecord(c->ev1, c->stream), "event");
-    c->timed = true;
+    if (events) {
+        FT_CU(cudaEventRecord(c->ev1, c->stream), "event");
+        c->timed = true;
+    }
     return FT_OK;
+}
+
+int run(ft_ctx* c, int stroke, int rule, const ft_op* ops_d, const ft_path_desc* paths, uint32_t n_paths, int fmt,
+        uint8_t* rasters_d, const float* sw_chain, float* sw_out) {
+    FT_CU(c->status.ensure(sizeof(int32_t) * std::max(n_paths, 1u)), "alloc status");
+    return run_plan(c, c->plan, stroke, rule, ops_d, paths, n_paths, fmt, rasters_d, sw_chain, sw_out,
+                    static_cast<int32_t*>(c->status.p));
 }
 
 bool valid_ops_host(const ft_op* ops, uint64_t n) {
@@ -618,7 +645,12 @@ FT_API void ft_ctx_destroy(ft_ctx* c) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
-    DevBuf* bufs[] = {&c->ops,     &c->paths,   &c->items,   &c->items_w, &c->overflow,
+    c->plan.release();
+    for (auto& sl : c->chunk_plans) sl->release();
+    for (cudaEvent_t e : c->ev_chunk) cudaEventDestroy(e);
+    if (c->s_in) cudaStreamDestroy(c->s_in);
+    if (c->s_out) cudaStreamDestroy(c->s_out);
+    DevBuf* bufs[] = {&c->ops,     &c->paths,   &c->overflow,
                       &c->status,  &c->sw_out,  &c->rasters, &c->queue,   &c->scratch,
                       &c->sw_chain, &c->pool,   &c->pool_used, &c->bandoff, &c->crec,
                       &c->srgb_lut, &c->conv_src, &c->conv_dst, &c->figbins};
@@ -699,6 +731,104 @@ FT_API int ft_stroke(ft_ctx* c, const ft_op* ops, uint32_t n_ops, int32_t fmt, c
     return single(c, 1, FT_NONZERO, ops, n_ops, fmt, clr, raster, w, h, stride, where);
 }
 
+// Host batches in chunks of paths whose ops and rasters are ascending, disjoint ranges of
+// the host buffers: chunk k + 1 is copied in and chunk k - 1 copied out while chunk k is
+// drawn (one copy stream each way, events between the stages, each chunk's plan kept).
+// Returns -1 (nothing done) when the layout does not allow it.
+static int run_pipelined(ft_ctx* c, int stroke, int rule, const ft_op* ops, uint32_t n_ops_total,
+                         const ft_path_desc* paths, uint32_t n_paths, int fmt, uint8_t* rasters, uint64_t raster_bytes,
+                         int n_chunks) {
+    const uint32_t bpp = fmt == FT_RGBA8P ? 4 : 1;
+    auto rend = [&](const ft_path_desc& d) {
+        return d.height ? d.raster_offset + (uint64_t)(d.height - 1) * d.stride + (uint64_t)d.width * bpp
+                        : d.raster_offset;
+    };
+    // chunks of about equal raster bytes, by the paths' raster offsets
+    std::vector<uint32_t> pb(n_chunks + 1, n_paths);
+    pb[0] = 0;
+    for (int k = 1, i = 0; k < n_chunks; k++) {
+        const uint64_t cut = raster_bytes / n_chunks * k;
+        while (i < (int)n_paths && paths[i].raster_offset < cut) i++;
+        pb[k] = (uint32_t)i;
+    }
+    struct Range {
+        uint64_t o0, o1, r0, r1;
+    };
+    std::vector<Range> rg(n_chunks);
+    for (int k = 0; k < n_chunks; k++) {
+        if (pb[k + 1] <= pb[k]) return -1;
+        Range r{UINT64_MAX, 0, UINT64_MAX, 0};
+        for (uint32_t i = pb[k]; i < pb[k + 1]; i++) {
+            const ft_path_desc& d = paths[i];
+            r.o0 = std::min<uint64_t>(r.o0, d.op_begin);
+            r.o1 = std::max<uint64_t>(r.o1, (uint64_t)d.op_begin + d.n_ops);
+            r.r0 = std::min<uint64_t>(r.r0, d.raster_offset);
+            r.r1 = std::max<uint64_t>(r.r1, rend(d));
+        }
+        if (k && (r.o0 < rg[k - 1].o1 || r.r0 < rg[k - 1].r1)) return -1;
+        rg[k] = r;
+    }
+    if (!c->s_in) FT_CU(cudaStreamCreateWithFlags(&c->s_in, cudaStreamNonBlocking), "copy stream");
+    if (!c->s_out) FT_CU(cudaStreamCreateWithFlags(&c->s_out, cudaStreamNonBlocking), "copy stream");
+    while ((int)c->ev_chunk.size() < 2 * n_chunks + 2) {
+        cudaEvent_t e;
+        FT_CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+        c->ev_chunk.push_back(e);
+    }
+    while ((int)c->chunk_plans.size() < n_chunks) c->chunk_plans.emplace_back(new PlanSlot());
+    FT_CU(c->ops.ensure(sizeof(ft_op) * std::max<uint64_t>(n_ops_total, 1)), "alloc ops");
+    FT_CU(c->rasters.ensure(std::max<uint64_t>(raster_bytes, 1)), "alloc rasters");
+    FT_CU(c->status.ensure(sizeof(int32_t) * std::max(n_paths, 1u)), "alloc status");
+    cudaEvent_t* ev = c->ev_chunk.data();  // [0]: start, [1 + k]: copied in, [1 + K + k]: drawn, [1 + 2K]: out
+    auto* ops_d = static_cast<ft_op*>(c->ops.p);
+    auto* ras_d = static_cast<uint8_t*>(c->rasters.p);
+    auto* st_d = static_cast<int32_t*>(c->status.p);
+    FT_CU(cudaEventRecord(ev[0], c->stream), "event");  // after the context's earlier work
+    FT_CU(cudaStreamWaitEvent(c->s_in, ev[0], 0), "wait");
+    FT_CU(cudaStreamWaitEvent(c->s_out, ev[0], 0), "wait");
+    for (int k = 0; k < n_chunks; k++) {
+        const Range& r = rg[k];
+        if (r.o1 > r.o0)
+            FT_CU(cudaMemcpyAsync(ops_d + r.o0, ops + r.o0, sizeof(ft_op) * (r.o1 - r.o0), cudaMemcpyHostToDevice,
+                                  c->s_in),
+                  "upload ops");
+        if (r.r1 > r.r0)
+            FT_CU(cudaMemcpyAsync(ras_d + r.r0, rasters + r.r0, r.r1 - r.r0, cudaMemcpyHostToDevice, c->s_in),
+                  "upload rasters");
+        FT_CU(cudaEventRecord(ev[1 + k], c->s_in), "event");
+    }
+    for (int k = 0; k < n_chunks; k++) {
+        FT_CU(cudaStreamWaitEvent(c->stream, ev[1 + k], 0), "wait");
+        if (k == 0) FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
+        int st = run_plan(c, *c->chunk_plans[k], stroke, rule, ops_d, paths + pb[k], pb[k + 1] - pb[k], fmt, ras_d,
+                          nullptr, nullptr, st_d + pb[k], false);
+        if (st != FT_OK) return st;
+        FT_CU(cudaEventRecord(ev[1 + n_chunks + k], c->stream), "event");
+        FT_CU(cudaStreamWaitEvent(c->s_out, ev[1 + n_chunks + k], 0), "wait");
+        const Range& r = rg[k];
+        if (r.r1 > r.r0)
+            FT_CU(cudaMemcpyAsync(rasters + r.r0, ras_d + r.r0, r.r1 - r.r0, cudaMemcpyDeviceToHost, c->s_out),
+                  "download rasters");
+    }
+    FT_CU(cudaEventRecord(c->ev1, c->stream), "event");
+    c->timed = true;
+    c->last_n_paths = n_paths;
+    FT_CU(cudaEventRecord(ev[1 + 2 * n_chunks], c->s_out), "event");
+    FT_CU(cudaStreamWaitEvent(c->stream, ev[1 + 2 * n_chunks], 0), "wait");
+    FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
+    return FT_OK;
+}
+
+// Chunks of a host batch: FT_HOST_CHUNKS, else 2 from 64 MB of rasters.  More chunks
+// lose: every chunk's persistent launch ends on its slowest paths (65,536 glyphs in
+// 1 / 2 / 4 chunks: 16.3 / 15.7 / 21.6 ms end to end).
+static int host_chunks(uint64_t raster_bytes, uint32_t n_paths) {
+    const char* env = getenv("FT_HOST_CHUNKS");
+    int k = env ? atoi(env) : (raster_bytes >= (64ull << 20) ? 2 : 1);
+    k = std::max(1, std::min(k, 16));
+    return n_paths >= 4u * (uint32_t)k ? k : 1;
+}
+
 FT_API int ft_fill_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* ops, uint32_t n_ops_total,
                          const ft_path_desc* paths, uint32_t n_paths, int32_t fmt, uint8_t* rasters,
                          uint64_t raster_bytes, int32_t where) {
@@ -712,6 +842,13 @@ FT_API int ft_fill_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* o
     for (uint32_t i = 0; i < n_paths; i++) {
         int st = check_path(c, paths[i], fmt, raster_bytes, n_ops_total);
         if (st != FT_OK) return st;
+    }
+    if (where == FT_HOST) {
+        const int k = host_chunks(raster_bytes, n_paths);
+        if (k > 1) {
+            const int st = run_pipelined(c, stroke, rule, ops, n_ops_total, paths, n_paths, fmt, rasters, raster_bytes, k);
+            if (st != -1) return st;
+        }
     }
     const ft_op* ops_d = ops;
     uint8_t* ras_d = rasters;
