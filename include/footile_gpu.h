@@ -149,7 +149,10 @@ FT_API int ft_stroke(ft_ctx* ctx, const ft_op* ops, uint32_t n_ops, int32_t fmt,
  * raster region.  `ops` holds all ops (n_ops_total), `rasters` all rasters
  * (raster_bytes).  `paths` is always a host array; `ops` / `rasters` live where
  * `where` says.  The per-path status of the last batch is read with
- * ft_batch_status.  The raster regions of the paths must not overlap. */
+ * ft_batch_status.  The raster regions of the paths must not overlap.  With
+ * FT_HOST and 64 MB of rasters or more, paths whose ops and rasters lie in ascending
+ * order in the host buffers are drawn in two chunks, the copies of one overlapping
+ * the drawing of the other (FT_HOST_CHUNKS in the environment sets the count). */
 FT_API int ft_fill_batch(ft_ctx* ctx, int32_t stroke, int32_t rule, const ft_op* ops,
                          uint32_t n_ops_total, const ft_path_desc* paths,
                          uint32_t n_paths, int32_t fmt, uint8_t* rasters,
