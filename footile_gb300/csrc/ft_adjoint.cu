@@ -548,6 +548,7 @@ __device__ __forceinline__ void row_cells(const EdgeG& E, int r, int W, CB cb) {
 // (the band's binned edges), or 0 .. n_e - 1 when elist is null.
 struct NoG {
     __device__ float operator()(int, int) const { return 0.0f; }
+    __device__ void prefetch(int, int) const {}
 };
 template <bool BWD, class GV = NoG>
 __device__ void band_edges(ASmem& sm, float* band, int W, int b0, int nb, int V, const float2* vpos,
@@ -618,6 +619,18 @@ __device__ void band_edges(ASmem& sm, float* band, int W, int b0, int nb, int V,
                         }
                     });
                 } else {
+                    // the next item is usually this edge one row down: ask L1 for its cells now
+                    if (r + 1 <= b1 && (float)(r + 1) < E.b.y) {
+                        const float y0 = (float)(r + 1), y1 = fminf(E.b.y, (float)(r + 2));
+                        const float xa = fminf(fmaxf(__fadd_rn(E.a.x, __fmul_rn(__fsub_rn(y0, E.a.y), E.dxdy)), E.xlo), E.xhi);
+                        const float xb = fminf(fmaxf(__fadd_rn(E.a.x, __fmul_rn(__fsub_rn(y1, E.a.y), E.dxdy)), E.xlo), E.xhi);
+                        const float lo = fminf(xa, xb), hi = fmaxf(xa, xb);
+                        if (hi >= 0.0f && lo < (float)W) {
+                            const int c0 = max((int)floorf(lo), 0), c1 = min((int)floorf(hi), W - 1);
+                            gv.prefetch(r + 1, c0);
+                            if ((c1 >> 5) != (c0 >> 5)) gv.prefetch(r + 1, c1);
+                        }
+                    }
                     const bool down = E.dir > 0.0f;
                     row_pieces(E, r, W, [&](int c, float, float, float u0, float u1) {
                         if (c < 0) return;
@@ -1263,8 +1276,38 @@ __device__ __forceinline__ float cov_d(int rule, float s) {
     return m < 1.0f ? 1.0f : -1.0f;
 }
 
+// g = sign * dLoss/dcov * dcov/dS at (row, cell) of one path's planes; dcov/dS from the
+// winding area, or (no_area, NonZero) from the coverage: 1 exactly where 0 < cov < 1.
+struct GradAt {
+    const char* g;
+    const char* cv;
+    const char* ar;
+    size_t off;
+    uint32_t stride;
+    float sign;
+    int rule;
+    bool no_area;
+    __device__ size_t at(int r, int c) const { return off + (size_t)r * stride + 4 * (size_t)c; }
+    __device__ float operator()(int r, int c) const;
+    __device__ void prefetch(int r, int c) const {
+        const size_t o = at(r, c);
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(g + o));
+        asm volatile("prefetch.global.L1 [%0];" ::"l"((no_area ? cv : ar) + o));
+    }
+};
+
 __device__ __forceinline__ float* px_at(float* base, const ft_path_desc& d, int r) {
     return reinterpret_cast<float*>(reinterpret_cast<char*>(base) + d.raster_offset + (size_t)r * d.stride);
+}
+
+__device__ __forceinline__ float GradAt::operator()(int r, int c) const {
+    const size_t o = at(r, c);
+    const float gg = *reinterpret_cast<const float*>(g + o);
+    if (no_area) {
+        const float v = *reinterpret_cast<const float*>(cv + o);
+        return v > 0.0f && v < 1.0f ? __fmul_rn(sign, gg) : 0.0f;
+    }
+    return __fmul_rn(__fmul_rn(sign, gg), cov_d(rule, *reinterpret_cast<const float*>(ar + o)));
 }
 
 template <bool BWD>
@@ -1320,24 +1363,10 @@ __global__ void __launch_bounds__(ABLOCK, 3) k_adjoint(AParams p) {
         if (BWD) {
             // every (edge, row) item of the path in one pass, g read at its own cell
             if (!cap && W > 0 && H > 0) {
-                const float* gc = p.grad_cov;
-                const float* cvp = p.cov;
-                const float* arp = p.area;
-                const int rule = p.rule;
-                if (p.no_area)
-                    band_edges<true>(sm, nullptr, W, 0, H, V, vpos, vsub, vgrad, nullptr, V, [&](int r, int c) {
-                        const size_t o = d.raster_offset + (size_t)r * d.stride + 4 * (size_t)c;
-                        const float cv = *reinterpret_cast<const float*>(reinterpret_cast<const char*>(cvp) + o);
-                        const float g = *reinterpret_cast<const float*>(reinterpret_cast<const char*>(gc) + o);
-                        return cv > 0.0f && cv < 1.0f ? __fmul_rn(sign, g) : 0.0f;
-                    });
-                else
-                    band_edges<true>(sm, nullptr, W, 0, H, V, vpos, vsub, vgrad, nullptr, V, [&](int r, int c) {
-                        const size_t o = d.raster_offset + (size_t)r * d.stride + 4 * (size_t)c;
-                        const float a = *reinterpret_cast<const float*>(reinterpret_cast<const char*>(arp) + o);
-                        const float g = *reinterpret_cast<const float*>(reinterpret_cast<const char*>(gc) + o);
-                        return __fmul_rn(__fmul_rn(sign, g), cov_d(rule, a));
-                    });
+                GradAt gv{reinterpret_cast<const char*>(p.grad_cov), reinterpret_cast<const char*>(p.cov),
+                          reinterpret_cast<const char*>(p.area), d.raster_offset, d.stride, sign, p.rule,
+                          p.no_area != 0};
+                band_edges<true>(sm, nullptr, W, 0, H, V, vpos, vsub, vgrad, nullptr, V, gv);
             }
             __syncthreads();
         }
