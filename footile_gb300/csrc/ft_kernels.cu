@@ -1898,6 +1898,9 @@ __device__ __forceinline__ void composite_row(int* row, unsigned short* last, un
                                               uint8_t* drow, int rule, bool rgba, unsigned clr, int G,
                                               const unsigned char* ftab, bool skip_spans) {
     const int lane = threadIdx.x & 31;
+    // Rgba8p rows on a 16-byte boundary: a lane's four pixels are read and written as
+    // one 16-byte access (one load latency per span instead of four)
+    const bool vec = rgba && (reinterpret_cast<uintptr_t>(drow) & 15) == 0;
     unsigned carry = 0;
     for (int x0 = 0; x0 < W; x0 += 128) {
         const int sp = x0 >> 7;
@@ -1915,6 +1918,23 @@ __device__ __forceinline__ void composite_row(int* row, unsigned short* last, un
         carry += __shfl_sync(FULL, inc, 31);
         const unsigned av[4] = {resolve_cov(s0 + ex, rule), resolve_cov(s1 + ex, rule), resolve_cov(s2 + ex, rule),
                                 resolve_cov(s3 + ex, rule)};
+        if (vec && x + 3 < W) {
+            if (av[0] | av[1] | av[2] | av[3]) {
+                uint4* dp4 = reinterpret_cast<uint4*>(reinterpret_cast<unsigned*>(drow) + x);
+                const uint4 d = *dp4;
+                unsigned dv[4] = {d.x, d.y, d.z, d.w};
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    if (!av[c]) continue;  // this pixel keeps its bytes
+                    const int kk = min(G - (int)last[x + c], 15);
+                    if (kk) dv[c] = ftab4(ftab, dv[c], kk);
+                    dv[c] = srcover_rgba(dv[c], clr, av[c]);
+                    last[x + c] = (unsigned short)(G + 1);
+                }
+                *dp4 = make_uint4(dv[0], dv[1], dv[2], dv[3]);
+            }
+            continue;
+        }
 #pragma unroll
         for (int c = 0; c < 4; c++) {
             const int xc = x + c;
