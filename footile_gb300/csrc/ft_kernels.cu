@@ -1478,7 +1478,7 @@ static_assert(offsetof(WarpSmem, row) % 16 == 0 && sizeof(WarpSmem) % 16 == 0, "
 // The active edge list holds the records themselves (one load per edge and row from a
 // list that stays small and hot, instead of an index and a record of the figure's edges).
 __device__ void raster_sweep_warp(const KParams& P, const ft_path_desc& d, const CState& S, const EdgeRec* edges,
-                                  int* sorted, EdgeRec* active, int* hist, int* row) {
+                                  EdgeRec* sorted, EdgeRec* active, int* hist, int* row) {
     const int lane = threadIdx.x & 31;
     const int count = S.count, H = (int)d.height, W = (int)d.width, Wp = (W + 3) & ~3;
     const int top_row = S.top_row, row_begin = max(top_row, 0);
@@ -1506,11 +1506,11 @@ __device__ void raster_sweep_warp(const KParams& P, const ft_path_desc& d, const
         carry += __shfl_sync(FULL, inc, 31);
     }
     __syncwarp();
-    for (int e = lane; e < count; e += 32) {
-        const EdgeRec& E = edges[e];
+    for (int e = lane; e < count; e += 32) {  // the records themselves, in bucket order
+        const EdgeRec E = edges[e];
         if (E.ed) {
             const long long b = (long long)E.start_row - top_row;
-            if (b < nrows) sorted[atomicAdd(&hist[b], 1)] = e;
+            if (b < nrows) sorted[atomicAdd(&hist[b], 1)] = E;
         }
     }
     for (int x = lane; x < Wp; x += 32) row[x] = 0;
@@ -1520,7 +1520,7 @@ __device__ void raster_sweep_warp(const KParams& P, const ft_path_desc& d, const
     for (int s = 0; s < nrows; s++) {
         const int y = top_row + s;
         const int bs = s == 0 ? 0 : hist[s - 1], be = hist[s];
-        for (int k = lane; k < be - bs; k += 32) active[n_act + k] = edges[sorted[bs + k]];
+        for (int k = lane; k < be - bs; k += 32) active[n_act + k] = sorted[bs + k];
         n_act += be - bs;
         __syncwarp();
         int nn = 0;
@@ -1555,7 +1555,7 @@ __global__ void __launch_bounds__(BLOCK, 4) k_raster_warp(KParams P) {
     int2* pts = reinterpret_cast<int2*>(scr + WS_PTS);
     int* ss = reinterpret_cast<int*>(scr + WS_SS);
     EdgeRec* edges = reinterpret_cast<EdgeRec*>(scr + WS_EDGES);
-    int* sorted = reinterpret_cast<int*>(scr + WS_SORT);
+    EdgeRec* sorted = reinterpret_cast<EdgeRec*>(scr + WS_SORT);
     EdgeRec* active = reinterpret_cast<EdgeRec*>(scr + WS_ACT);
     for (;;) {
         int it = 0;
