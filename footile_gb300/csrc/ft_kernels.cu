@@ -1301,6 +1301,21 @@ __device__ void build_edges(const CState& S, const int2* pts, const int* ss, Edg
     for (int i = G::rank(); i < count; i += G::N) edges[i] = edge_rec(i, count, figdir, pts, ss);
 }
 
+// build_edges for one warp's figure, also counting the edges by first scan row into
+// hist[0 .. nrows) (zeroed by the caller) for raster_sweep_warp's buckets.
+__device__ void build_edges_warp(const CState& S, const int2* pts, const int* ss, EdgeRec* edges, int* hist,
+                                 int nrows) {
+    const int count = S.count, figdir = S.dir, top_row = S.top_row;
+    for (int i = threadIdx.x & 31; i < count; i += 32) {
+        const EdgeRec E = edge_rec(i, count, figdir, pts, ss);
+        edges[i] = E;
+        if (E.ed) {
+            const long long b = (long long)E.start_row - top_row;
+            if (b < nrows) atomicAdd(&hist[b], 1);
+        }
+    }
+}
+
 // Signed cell areas of one edge on one scan row (fig.rs:238-321), added into
 // `area` (the band row of width W).
 // With `spans`, the 128-pixel spans holding the touched cells are marked too.
@@ -1477,8 +1492,9 @@ static_assert(offsetof(WarpSmem, row) % 16 == 0 && sizeof(WarpSmem) % 16 == 0, "
 
 // The active edge list holds the records themselves (one load per edge and row from a
 // list that stays small and hot, instead of an index and a record of the figure's edges).
+// `counted`: hist already holds every start row's edge count (build_edges_warp).
 __device__ void raster_sweep_warp(const KParams& P, const ft_path_desc& d, const CState& S, const EdgeRec* edges,
-                                  EdgeRec* sorted, EdgeRec* active, int* hist, int* row) {
+                                  EdgeRec* sorted, EdgeRec* active, int* hist, int* row, bool counted = false) {
     const int lane = threadIdx.x & 31;
     const int count = S.count, H = (int)d.height, W = (int)d.width, Wp = (W + 3) & ~3;
     const int top_row = S.top_row, row_begin = max(top_row, 0);
@@ -1487,16 +1503,18 @@ __device__ void raster_sweep_warp(const KParams& P, const ft_path_desc& d, const
                          ((unsigned)d.clr[3] << 24);
     uint8_t* base = P.rasters + d.raster_offset;
     // bucket the edges by their first scan row (edges below the last row never start)
-    for (int b = lane; b < nrows; b += 32) hist[b] = 0;
-    __syncwarp();
-    for (int e = lane; e < count; e += 32) {
-        const EdgeRec& E = edges[e];
-        if (E.ed) {
-            const long long b = (long long)E.start_row - top_row;
-            if (b < nrows) atomicAdd(&hist[b], 1);
+    if (!counted) {
+        for (int b = lane; b < nrows; b += 32) hist[b] = 0;
+        __syncwarp();
+        for (int e = lane; e < count; e += 32) {
+            const EdgeRec& E = edges[e];
+            if (E.ed) {
+                const long long b = (long long)E.start_row - top_row;
+                if (b < nrows) atomicAdd(&hist[b], 1);
+            }
         }
+        __syncwarp();
     }
-    __syncwarp();
     int carry = 0;
     for (int b0 = 0; b0 < nrows; b0 += 32) {
         const int b = b0 + lane;
@@ -1574,10 +1592,15 @@ __global__ void __launch_bounds__(BLOCK, 4) k_raster_warp(KParams P) {
         }
         if (M.S.count > 0) {
             top_and_dir<WarpG>(M.S, pts, ss, M.tmp3);
-            build_edges<WarpG>(M.S, pts, ss, edges);
             __syncwarp();
-            if (max(M.S.top_row, 0) < (int)d.height && d.width > 0)
-                raster_sweep_warp(P, d, M.S, edges, sorted, active, M.u.hist, M.row);
+            const int nrows = (int)d.height - max(M.S.top_row, 0);
+            if (nrows > 0 && d.width > 0) {
+                for (int b = lane; b < nrows; b += 32) M.u.hist[b] = 0;  // the build's shared area is free
+                __syncwarp();
+                build_edges_warp(M.S, pts, ss, edges, M.u.hist, nrows);
+                __syncwarp();
+                raster_sweep_warp(P, d, M.S, edges, sorted, active, M.u.hist, M.row, true);
+            }
         }
         if (P.sw_out) {
             int lp = -1;
