@@ -286,16 +286,32 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """DRAM bytes per launch of the rasteriser from the committed ncu summary."""
+def profiled(key):
+    """A per-launch figure of the rasteriser from the committed ncu summary."""
     p = os.path.join(ROOT, "profiles", "k_raster_warp_glyphs_65536.txt")
     try:
         for line in open(p):
-            if line.startswith("traffic_bytes_per_launch:"):
+            if line.startswith(key + ":"):
                 return float(line.split(":")[1])
     except OSError:
         pass
     return None
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of the rasteriser (dram__bytes_read.sum + write.sum)."""
+    return profiled("traffic_bytes_per_launch")
+
+
+def accumulation(kernel_ms):
+    wf = profiled("shared_atomic_wavefronts_per_launch")
+    if wf is None:
+        return None
+    return {"bound": "shared-memory atomics", "wavefronts_per_launch": wf,
+            "warp_instructions_per_launch": profiled("shared_atomic_warp_insts_per_launch"),
+            "achieved": wf / (kernel_ms * 1e-3) / 1e9, "unit": "G atomic wavefronts/s",
+            "utilisation_pct_of_peak": profiled("shared_atomic_pipe_pct_of_peak"),
+            "source": "profiles/k_raster_warp_glyphs_65536.txt"}
 
 
 def cpu_baseline(ops, paths, nbytes, seconds, threads):
@@ -753,6 +769,10 @@ def run_ours(args):
                      "traffic": profiled_traffic(), "peak_kind": peak_kind,
                      "kernel": "ftk::k_raster_warp + ftk::k_raster (graph: 2 memsets, warp rasteriser, CTA rasteriser)", "kernel_ms": kmean,
                      "algorithmic_bytes_per_launch": int(alg_bytes)},
+        # the cell accumulation's bound: shared-memory atomics (data-path wavefronts of one
+        # launch from the ncu summary, over this run's kernel time; the atomic data path's
+        # utilisation as ncu measured it)
+        "accumulation": accumulation(kmean),
         "cpu_baseline": cpu,
         "modes": {"batched_paths_per_s": len(paths) / (ms_max * 1e-3), "per_path_launch": per_path,
                   "batched_over_per_path": (len(paths) / (ms_max * 1e-3) / per_path["paths_per_s"]) if per_path else None},
