@@ -118,14 +118,37 @@ __device__ __forceinline__ float2 fx_pass(P2 raw, float2 g) {
 
 __device__ __forceinline__ float pow2neg(int d) { return __int_as_float((127 - d) << 23); }  // 2^-d, d <= 126
 
+// Stack frames of the walks below: the right half of a subdivided curve without its
+// start point, which is the end point of the left half's last leaf (the same value,
+// carried down unchanged).  W: with pen widths.
+template <bool CUBIC, bool W>
+struct WalkFr {
+    P2 b, c, d;
+    float wb, wc, wd;
+    int dep;
+};
+template <>
+struct WalkFr<true, false> {
+    P2 b, c, d;
+    int dep;
+};
+template <>
+struct WalkFr<false, true> {
+    P2 b, c;
+    float wb, wc;
+    int dep;
+};
+template <>
+struct WalkFr<false, false> {
+    P2 b, c;
+    int dep;
+};
+
 // De Casteljau walk of one quad (plotter.rs:248-265) or cubic (plotter.rs:311-332) in
 // depth-first order; leaf(index, end point, end parameter t).  Returns the leaf count.
 template <bool CUBIC, class Leaf>
 __device__ int curve_walk(P2 a, P2 b, P2 c, P2 d, float tol_sq, int* depth_hit, Leaf leaf) {
-    struct Fr {
-        P2 a, b, c, d;
-        int dep;
-    };
+    using Fr = WalkFr<CUBIC, false>;
     Fr st[FT_MAX_DEPTH + 1];
     int sp = 0, n = 0, dep = 0;
     float t = 0.0f;
@@ -157,19 +180,19 @@ __device__ int curve_walk(P2 a, P2 b, P2 c, P2 d, float tol_sq, int* depth_hit, 
             n++;
             if (sp == 0) break;
             --sp;
-            a = st[sp].a;
+            a = CUBIC ? d : c;
             b = st[sp].b;
             c = st[sp].c;
-            d = st[sp].d;
+            if constexpr (CUBIC) d = st[sp].d;
             dep = st[sp].dep;
         } else {
-            if (CUBIC) {
-                st[sp] = Fr{m, r1, r2, d, dep + 1};
+            if constexpr (CUBIC) {
+                st[sp] = Fr{r1, r2, d, dep + 1};
                 b = l1;
                 c = l2;
                 d = m;
             } else {
-                st[sp] = Fr{m, r1, r2, r2, dep + 1};
+                st[sp] = Fr{r1, r2, dep + 1};
                 b = l1;
                 c = l2;
             }
@@ -727,11 +750,7 @@ enum { F_POINT = 0, F_QUAD = 1, F_CUBIC = 2 };
 template <bool CUBIC, class Leaf>
 __device__ int curve_walk_w(P2 a, P2 b, P2 c, P2 d, float wa, float wb, float wc, float wd, float tol_sq,
                             int* depth_hit, Leaf leaf) {
-    struct Fr {
-        P2 a, b, c, d;
-        float wa, wb, wc, wd;
-        int dep;
-    };
+    using Fr = WalkFr<CUBIC, true>;
     Fr st[FT_MAX_DEPTH + 1];
     int sp = 0, n = 0, dep = 0;
     float t = 0.0f;
@@ -768,16 +787,17 @@ __device__ int curve_walk_w(P2 a, P2 b, P2 c, P2 d, float wa, float wb, float wc
             n++;
             if (sp == 0) break;
             --sp;
-            a = st[sp].a, b = st[sp].b, c = st[sp].c, d = st[sp].d;
-            wa = st[sp].wa, wb = st[sp].wb, wc = st[sp].wc, wd = st[sp].wd;
+            a = CUBIC ? d : c, wa = CUBIC ? wd : wc;
+            b = st[sp].b, c = st[sp].c, wb = st[sp].wb, wc = st[sp].wc;
+            if constexpr (CUBIC) d = st[sp].d, wd = st[sp].wd;
             dep = st[sp].dep;
         } else {
-            if (CUBIC) {
-                st[sp] = Fr{m, r1, r2, d, wm, wr1, wr2, wd, dep + 1};
+            if constexpr (CUBIC) {
+                st[sp] = Fr{r1, r2, d, wr1, wr2, wd, dep + 1};
                 b = l1, c = l2, d = m;
                 wb = wl1, wc = wl2, wd = wm;
             } else {
-                st[sp] = Fr{m, r1, r2, r2, wm, wr1, wr2, wr2, dep + 1};
+                st[sp] = Fr{r1, r2, wr1, wr2, dep + 1};
                 b = l1, c = l2;
                 wb = wl1, wc = wl2;
             }

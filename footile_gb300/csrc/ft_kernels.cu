@@ -162,17 +162,39 @@ struct WarpG {
 };
 
 // ------------------------------------------------- De Casteljau flattening
+// Stack frames of the walks: the right half of a subdivided curve.  A frame keeps no
+// start point: the right half starts where the last leaf of the left half ends (that
+// leaf's end point is the same value, carried down unchanged).  Fills carry no widths.
+template <bool W>
+struct QuadFr {
+    P2 b, c;
+    float wb, wc;
+    int d;
+};
+template <>
+struct QuadFr<false> {
+    P2 b, c;
+    int d;
+};
+template <bool W>
+struct CubicFr {
+    P2 b, c, e;
+    float wb, wc, we;
+    int d;
+};
+template <>
+struct CubicFr<false> {
+    P2 b, c, e;
+    int d;
+};
+
 // Walk the subdivision of a quad (plotter.rs:248-265) in depth-first order.
 // Leaves with index in [lo, hi) go to emit(index, point, width).  Returns the
 // number of leaves walked (the total when hi == INT_MAX).
 template <bool W, class Emit>
 __device__ int quad_walk(P2 a, P2 b, P2 c, float wa, float wb, float wc, float tol_sq, int lo, int hi,
                          int* depth_hit, Emit emit) {
-    struct Fr {
-        P2 a, b, c;
-        float wa, wb, wc;
-        int d;
-    };
+    using Fr = QuadFr<W>;
     Fr st[FT_MAX_DEPTH + 1];
     int sp = 0, leaf = 0, d = 0;
     for (;;) {
@@ -184,27 +206,25 @@ __device__ int quad_walk(P2 a, P2 b, P2 c, float wa, float wb, float wc, float t
             leaf++;
             if (leaf >= hi || sp == 0) break;
             --sp;
-            a = st[sp].a;
+            a = c;
             b = st[sp].b;
             c = st[sp].c;
-            if (W) {
-                wa = st[sp].wa;
+            if constexpr (W) {
+                wa = wc;
                 wb = st[sp].wb;
                 wc = st[sp].wc;
             }
             d = st[sp].d;
         } else {
             float wab = 0, wbc = 0, wabbc = 0;
-            if (W) {
+            if constexpr (W) {
                 wab = fmid(wa, wb);
                 wbc = fmid(wb, wc);
                 wabbc = fmid(wab, wbc);
             }
-            st[sp].a = abbc;
             st[sp].b = bc;
             st[sp].c = c;
-            if (W) {
-                st[sp].wa = wabbc;
+            if constexpr (W) {
                 st[sp].wb = wbc;
                 st[sp].wc = wc;
             }
@@ -212,7 +232,7 @@ __device__ int quad_walk(P2 a, P2 b, P2 c, float wa, float wb, float wc, float t
             sp++;
             b = ab;
             c = abbc;
-            if (W) {
+            if constexpr (W) {
                 wb = wab;
                 wc = wabbc;
             }
@@ -226,11 +246,7 @@ __device__ int quad_walk(P2 a, P2 b, P2 c, float wa, float wb, float wc, float t
 template <bool W, class Emit>
 __device__ int cubic_walk(P2 a, P2 b, P2 c, P2 e, float wa, float wb, float wc, float we, float tol_sq, int lo,
                           int hi, int* depth_hit, Emit emit) {
-    struct Fr {
-        P2 a, b, c, e;
-        float wa, wb, wc, we;
-        int d;
-    };
+    using Fr = CubicFr<W>;
     Fr st[FT_MAX_DEPTH + 1];
     int sp = 0, leaf = 0, d = 0;
     for (;;) {
@@ -245,12 +261,12 @@ __device__ int cubic_walk(P2 a, P2 b, P2 c, P2 e, float wa, float wb, float wc, 
             leaf++;
             if (leaf >= hi || sp == 0) break;
             --sp;
-            a = st[sp].a;
+            a = e;
             b = st[sp].b;
             c = st[sp].c;
             e = st[sp].e;
-            if (W) {
-                wa = st[sp].wa;
+            if constexpr (W) {
+                wa = we;
                 wb = st[sp].wb;
                 wc = st[sp].wc;
                 we = st[sp].we;
@@ -258,7 +274,7 @@ __device__ int cubic_walk(P2 a, P2 b, P2 c, P2 e, float wa, float wb, float wc, 
             d = st[sp].d;
         } else {
             float wab = 0, wbc = 0, wcd = 0, wabbc = 0, wbccd = 0, wpe = 0;
-            if (W) {
+            if constexpr (W) {
                 wab = fmid(wa, wb);
                 wbc = fmid(wb, wc);
                 wcd = fmid(wc, we);
@@ -266,12 +282,10 @@ __device__ int cubic_walk(P2 a, P2 b, P2 c, P2 e, float wa, float wb, float wc, 
                 wbccd = fmid(wbc, wcd);
                 wpe = fmid(wabbc, wbccd);
             }
-            st[sp].a = pe;
             st[sp].b = bccd;
             st[sp].c = cd;
             st[sp].e = e;
-            if (W) {
-                st[sp].wa = wpe;
+            if constexpr (W) {
                 st[sp].wb = wbccd;
                 st[sp].wc = wcd;
                 st[sp].we = we;
@@ -281,7 +295,7 @@ __device__ int cubic_walk(P2 a, P2 b, P2 c, P2 e, float wa, float wb, float wc, 
             b = ab;
             c = abbc;
             e = pe;
-            if (W) {
+            if constexpr (W) {
                 wb = wab;
                 wc = wabbc;
                 we = wpe;
@@ -1301,18 +1315,19 @@ __device__ void build_edges(const CState& S, const int2* pts, const int* ss, Edg
     for (int i = G::rank(); i < count; i += G::N) edges[i] = edge_rec(i, count, figdir, pts, ss);
 }
 
-// build_edges for one warp's figure, also counting the edges by first scan row into
-// hist[0 .. nrows) (zeroed by the caller) for raster_sweep_warp's buckets.
-__device__ void build_edges_warp(const CState& S, const int2* pts, const int* ss, EdgeRec* edges, int* hist,
-                                 int nrows) {
-    const int count = S.count, figdir = S.dir, top_row = S.top_row;
+// Count one warp's edges by first scan row into hist[0 .. nrows) (zeroed by the
+// caller) for raster_sweep_warp's buckets: the rows of edge_rec's non-horizontal
+// edges, from the vertices alone (the records are built once, into their buckets).
+__device__ void count_edges_warp(const CState& S, const int2* pts, const int* ss, int* hist, int nrows) {
+    const int count = S.count, top_row = S.top_row;
     for (int i = threadIdx.x & 31; i < count; i += 32) {
-        const EdgeRec E = edge_rec(i, count, figdir, pts, ss);
-        edges[i] = E;
-        if (E.ed) {
-            const long long b = (long long)E.start_row - top_row;
-            if (b < nrows) atomicAdd(&hist[b], 1);
-        }
+        const int s = ss[i];
+        const int nx = (i + 1 < count && ss[i + 1] == s) ? i + 1 : s;
+        if (nx == i) continue;
+        const int ay = pts[i].y, by = pts[nx].y;
+        if (ay == by) continue;
+        const long long b = (long long)(min(ay, by) >> 16) - top_row;
+        if (b < nrows) atomicAdd(&hist[b], 1);
     }
 }
 
@@ -1490,11 +1505,12 @@ struct WarpSmem {
 };
 static_assert(offsetof(WarpSmem, row) % 16 == 0 && sizeof(WarpSmem) % 16 == 0, "warp smem alignment");
 
-// The active edge list holds the records themselves (one load per edge and row from a
-// list that stays small and hot, instead of an index and a record of the figure's edges).
-// `counted`: hist already holds every start row's edge count (build_edges_warp).
-__device__ void raster_sweep_warp(const KParams& P, const ft_path_desc& d, const CState& S, const EdgeRec* edges,
-                                  EdgeRec* sorted, EdgeRec* active, int* hist, int* row, bool counted = false) {
+// The edge records are built straight into their buckets (`sorted`); the active edge
+// list holds the records themselves (one load per edge and row from a list that stays
+// small and hot, instead of an index and a record of the figure's edges).  hist holds
+// every start row's edge count (count_edges_warp).
+__device__ void raster_sweep_warp(const KParams& P, const ft_path_desc& d, const CState& S, const int2* pts,
+                                  const int* ss, EdgeRec* sorted, EdgeRec* active, int* hist, int* row) {
     const int lane = threadIdx.x & 31;
     const int count = S.count, H = (int)d.height, W = (int)d.width, Wp = (W + 3) & ~3;
     const int top_row = S.top_row, row_begin = max(top_row, 0);
@@ -1503,18 +1519,6 @@ __device__ void raster_sweep_warp(const KParams& P, const ft_path_desc& d, const
                          ((unsigned)d.clr[3] << 24);
     uint8_t* base = P.rasters + d.raster_offset;
     // bucket the edges by their first scan row (edges below the last row never start)
-    if (!counted) {
-        for (int b = lane; b < nrows; b += 32) hist[b] = 0;
-        __syncwarp();
-        for (int e = lane; e < count; e += 32) {
-            const EdgeRec& E = edges[e];
-            if (E.ed) {
-                const long long b = (long long)E.start_row - top_row;
-                if (b < nrows) atomicAdd(&hist[b], 1);
-            }
-        }
-        __syncwarp();
-    }
     int carry = 0;
     for (int b0 = 0; b0 < nrows; b0 += 32) {
         const int b = b0 + lane;
@@ -1525,7 +1529,7 @@ __device__ void raster_sweep_warp(const KParams& P, const ft_path_desc& d, const
     }
     __syncwarp();
     for (int e = lane; e < count; e += 32) {  // the records themselves, in bucket order
-        const EdgeRec E = edges[e];
+        const EdgeRec E = edge_rec(e, count, S.dir, pts, ss);
         if (E.ed) {
             const long long b = (long long)E.start_row - top_row;
             if (b < nrows) sorted[atomicAdd(&hist[b], 1)] = E;
@@ -1572,7 +1576,6 @@ __global__ void __launch_bounds__(BLOCK, 4) k_raster_warp(KParams P) {
     unsigned char* scr = P.scratch + (size_t)blockIdx.x * SCRATCH_BYTES_PER_CTA + (size_t)warp * WS_BYTES;
     int2* pts = reinterpret_cast<int2*>(scr + WS_PTS);
     int* ss = reinterpret_cast<int*>(scr + WS_SS);
-    EdgeRec* edges = reinterpret_cast<EdgeRec*>(scr + WS_EDGES);
     EdgeRec* sorted = reinterpret_cast<EdgeRec*>(scr + WS_SORT);
     EdgeRec* active = reinterpret_cast<EdgeRec*>(scr + WS_ACT);
     for (;;) {
@@ -1597,9 +1600,9 @@ __global__ void __launch_bounds__(BLOCK, 4) k_raster_warp(KParams P) {
             if (nrows > 0 && d.width > 0) {
                 for (int b = lane; b < nrows; b += 32) M.u.hist[b] = 0;  // the build's shared area is free
                 __syncwarp();
-                build_edges_warp(M.S, pts, ss, edges, M.u.hist, nrows);
+                count_edges_warp(M.S, pts, ss, M.u.hist, nrows);
                 __syncwarp();
-                raster_sweep_warp(P, d, M.S, edges, sorted, active, M.u.hist, M.row, true);
+                raster_sweep_warp(P, d, M.S, pts, ss, sorted, active, M.u.hist, M.row);
             }
         }
         if (P.sw_out) {

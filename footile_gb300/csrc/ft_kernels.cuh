@@ -92,9 +92,8 @@ constexpr int WARP_CAP = 8191;        // vertices a warp holds; larger figures g
 constexpr int WARP_MAX_SIDE = 512;    // canvases up to this width and height use the warp rasteriser
 constexpr size_t WS_PTS = 0;
 constexpr size_t WS_SS = align256(WS_PTS + (size_t)WARP_CAP * sizeof(int2));
-constexpr size_t WS_EDGES = align256(WS_SS + (size_t)WARP_CAP * sizeof(int));
-constexpr size_t WS_SORT = align256(WS_EDGES + (size_t)WARP_CAP * sizeof(EdgeRec));
-constexpr size_t WS_ACT = align256(WS_SORT + (size_t)WARP_CAP * sizeof(EdgeRec));  // after the edge records by start row
+constexpr size_t WS_SORT = align256(WS_SS + (size_t)WARP_CAP * sizeof(int));       // edge records by start row
+constexpr size_t WS_ACT = align256(WS_SORT + (size_t)WARP_CAP * sizeof(EdgeRec));
 constexpr size_t WS_BYTES = align256(WS_ACT + (size_t)WARP_CAP * sizeof(EdgeRec));  // active edge records
 static_assert(NWARP * WS_BYTES <= SCRATCH_BYTES_PER_CTA, "warp scratch layout");
 
