@@ -1332,26 +1332,25 @@ __device__ void count_edges_warp(const CState& S, const int2* pts, const int* ss
 }
 
 // Signed cell areas of one edge on one scan row (fig.rs:238-321), added into
-// `area` (the band row of width W).
+// `area` (the band row of width W).  The edge on this row: x_bot where it leaves the
+// row, its inverse slope, whether the row is its first (st) or last (en), the 16.16
+// fractions of its upper and lower y, the cell step (1 .. ONE) and its direction ed.
 // With `spans`, the 128-pixel spans holding the touched cells are marked too.
-__device__ __forceinline__ void scan_item(const EdgeRec& E, int y, int* area, int W, unsigned* spans = nullptr) {
-    const int k = y - E.start_row;
-    const int x_bot = wadd(E.x_bot0, wmul(k, E.inv_slope));
-    const bool st = (y == E.start_row), en = (y == E.end_row);
-    const int ccov = en ? pixel_cov(fxfract(E.y_lower)) : 256;
-    const int cov = st ? ccov - pixel_cov(fxfract(E.y_upper)) : ccov;
+__device__ __forceinline__ void scan_row(int x_bot, int inv, bool st, bool en, int fu, int fl, int step, int ed,
+                                         int* area, int W, unsigned* spans) {
+    const int ccov = en ? pixel_cov(fl) : 256;
+    const int cov = st ? ccov - pixel_cov(fu) : ccov;
     if (cov <= 0) return;
-    const int x0 = st ? wsub(x_bot, fxmul(E.inv_slope, wsub(FX_ONE, fxfract(E.y_upper)))) : wsub(x_bot, E.inv_slope);
-    const int x1 = en ? wsub(x_bot, fxmul(E.inv_slope, wsub(fxceil(E.y_lower), E.y_lower))) : x_bot;
+    const int x0 = st ? wsub(x_bot, fxmul(inv, wsub(FX_ONE, fu))) : wsub(x_bot, inv);
+    // fxceil(y_lower) - y_lower, from the fraction alone
+    const int x1 = en ? wsub(x_bot, fxmul(inv, fl ? FX_ONE - fl : 0)) : x_bot;
     const int mnx = min(x0, x1), mxx = max(x0, x1);
     const int minp = mnx >> 16, maxp = mxx >> 16;
     if (minp >= W) return;
     const int full = cov << 8;
     const int r = (minp == maxp) ? fxmul(wsub(FX_ONE, fxfract(fxavg(mxx, mnx))), full)
                                  : fxmul(wsub(FX_ONE, fxfract(mnx)), FX_HALF);
-    const int first = E.step_pix > 0 ? fxmul(r, E.step_pix) : r;
-    const int step = E.step_pix > 0 ? E.step_pix : FX_ONE;
-    const int ed = E.ed;
+    const int first = fxmul(r, step);  // fxmul(r, ONE) == r
     // fig.rs:292-301: x_cov runs first, first + step, ... capped at ONE; each cell
     // gets the growth of min(pixel_cov(x_cov), cov) until it reaches cov
     const int jmax = W - 1 - minp;  // the loop also stops at the raster's last cell
@@ -1385,6 +1384,36 @@ __device__ __forceinline__ void scan_item(const EdgeRec& E, int y, int* area, in
     }
     if (spans)
         for (int sp = cell0 >> 7; sp <= (cell1 >> 7); sp++) atomicOr(&spans[sp >> 5], 1u << (sp & 31));
+}
+
+// The cell step of an edge, step_cov(ONE) (fig.rs:315-321): step_pix when positive,
+// else ONE; first_cov's r * step equals step_cov(r) for both.
+__device__ __forceinline__ int cell_step(const EdgeRec& E) { return E.step_pix > 0 ? E.step_pix : FX_ONE; }
+
+__device__ __forceinline__ void scan_item(const EdgeRec& E, int y, int* area, int W, unsigned* spans = nullptr) {
+    const int x_bot = wadd(E.x_bot0, wmul(y - E.start_row, E.inv_slope));
+    scan_row(x_bot, E.inv_slope, y == E.start_row, y == E.end_row, fxfract(E.y_upper), fxfract(E.y_lower),
+             cell_step(E), E.ed, area, W, spans);
+}
+
+// Edge record of the warp sweep, 16 bytes, relative to the figure's top row t (rows
+// t .. t + 511 at most): x where the edge would leave row t (wrapping, like the row
+// steps), the inverse slope, the two y fractions, and the cell step with the end row
+// and the direction.  The first row is the bucket the record sits in.
+__device__ __forceinline__ int4 sweep_rec(const EdgeRec& E, int t) {
+    int4 R;
+    R.x = wsub(E.x_bot0, wmul(E.start_row - t, E.inv_slope));
+    R.y = E.inv_slope;
+    R.z = fxfract(E.y_upper) | (fxfract(E.y_lower) << 16);
+    R.w = (cell_step(E) - 1) | (min(E.end_row - t, SWEEP_END_FAR) << 16) | ((E.ed < 0) << 26);
+    return R;
+}
+__device__ __forceinline__ int sweep_end(int4 R) { return (R.w >> 16) & 1023; }
+
+// scan_item for a sweep record on row t + s; st: s is its first row.
+__device__ __forceinline__ void scan_sweep(int4 R, int s, bool st, int* row, int W) {
+    scan_row(wadd(R.x, wmul(s, R.y)), R.y, st, s == sweep_end(R), R.z & FX_MASK, (int)((unsigned)R.z >> 16),
+             (R.w & FX_MASK) + 1, (R.w >> 26) & 1 ? -1 : 1, row, W, nullptr);
 }
 
 // Resolve one band row and write it (fig.rs:621-665, imgbuf.rs:38-199).
@@ -1505,12 +1534,12 @@ struct WarpSmem {
 };
 static_assert(offsetof(WarpSmem, row) % 16 == 0 && sizeof(WarpSmem) % 16 == 0, "warp smem alignment");
 
-// The edge records are built straight into their buckets (`sorted`); the active edge
-// list holds the records themselves (one load per edge and row from a list that stays
-// small and hot, instead of an index and a record of the figure's edges).  hist holds
-// every start row's edge count (count_edges_warp).
+// The edge records (sweep_rec) are built straight into their buckets (`sorted`); the
+// active edge list holds the records themselves (one load per edge and row from a list
+// that stays small and hot, instead of an index and a record of the figure's edges).
+// hist holds every start row's edge count (count_edges_warp).
 __device__ void raster_sweep_warp(const KParams& P, const ft_path_desc& d, const CState& S, const int2* pts,
-                                  const int* ss, EdgeRec* sorted, EdgeRec* active, int* hist, int* row) {
+                                  const int* ss, int4* sorted, int4* active, int* hist, int* row) {
     const int lane = threadIdx.x & 31;
     const int count = S.count, H = (int)d.height, W = (int)d.width, Wp = (W + 3) & ~3;
     const int top_row = S.top_row, row_begin = max(top_row, 0);
@@ -1532,7 +1561,7 @@ __device__ void raster_sweep_warp(const KParams& P, const ft_path_desc& d, const
         const EdgeRec E = edge_rec(e, count, S.dir, pts, ss);
         if (E.ed) {
             const long long b = (long long)E.start_row - top_row;
-            if (b < nrows) sorted[atomicAdd(&hist[b], 1)] = E;
+            if (b < nrows) sorted[atomicAdd(&hist[b], 1)] = sweep_rec(E, top_row);
         }
     }
     for (int x = lane; x < Wp; x += 32) row[x] = 0;
@@ -1540,26 +1569,28 @@ __device__ void raster_sweep_warp(const KParams& P, const ft_path_desc& d, const
     // hist[b] now ends bucket b
     int n_act = 0;
     for (int s = 0; s < nrows; s++) {
-        const int y = top_row + s;
         const int bs = s == 0 ? 0 : hist[s - 1], be = hist[s];
         for (int k = lane; k < be - bs; k += 32) active[n_act + k] = sorted[bs + k];
+        const int n_old = n_act;  // records from n_old on start on this row
         n_act += be - bs;
         __syncwarp();
         int nn = 0;
         for (int a0 = 0; a0 < n_act; a0 += 32) {
             const int idx = a0 + lane;
             const bool v = idx < n_act;
-            EdgeRec E;
-            int end_row = INT_MIN;
+            int4 R;
+            int end = -1;
             if (v) {
-                E = active[idx];
-                end_row = E.end_row;
-                scan_item(E, y, row, W);
+                R = active[idx];
+                end = sweep_end(R);
+                scan_sweep(R, s, idx >= n_old, row, W);
             }
-            // an edge leaves the active list after its last row (fig.rs:582, 603-617)
-            const bool keep = v && end_row > y;
+            // an edge leaves the active list after its last row (fig.rs:582, 603-617);
+            // records that keep their place are not rewritten
+            const bool keep = v && end > s;
             const unsigned km = __ballot_sync(FULL, keep);
-            if (keep) active[nn + __popc(km & ((1u << lane) - 1u))] = E;
+            const int dst = nn + __popc(km & ((1u << lane) - 1u));
+            if (keep && dst != idx) active[dst] = R;
             nn += __popc(km);
         }
         n_act = nn;
@@ -1576,8 +1607,8 @@ __global__ void __launch_bounds__(BLOCK, 4) k_raster_warp(KParams P) {
     unsigned char* scr = P.scratch + (size_t)blockIdx.x * SCRATCH_BYTES_PER_CTA + (size_t)warp * WS_BYTES;
     int2* pts = reinterpret_cast<int2*>(scr + WS_PTS);
     int* ss = reinterpret_cast<int*>(scr + WS_SS);
-    EdgeRec* sorted = reinterpret_cast<EdgeRec*>(scr + WS_SORT);
-    EdgeRec* active = reinterpret_cast<EdgeRec*>(scr + WS_ACT);
+    int4* sorted = reinterpret_cast<int4*>(scr + WS_SORT);
+    int4* active = reinterpret_cast<int4*>(scr + WS_ACT);
     for (;;) {
         int it = 0;
         if (lane == 0) it = (int)atomicAdd(&P.queue[1], 1u);

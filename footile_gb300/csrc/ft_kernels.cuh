@@ -90,11 +90,13 @@ constexpr uint32_t FIG_CAP_MAX = 1u << 26;
 // Warp rasteriser (one warp per small path): per-warp share of the CTA scratch.
 constexpr int WARP_CAP = 8191;        // vertices a warp holds; larger figures go to a CTA
 constexpr int WARP_MAX_SIDE = 512;    // canvases up to this width and height use the warp rasteriser
+static_assert(WARP_MAX_SIDE <= 1023, "sweep records hold rows below 1023");
 constexpr size_t WS_PTS = 0;
 constexpr size_t WS_SS = align256(WS_PTS + (size_t)WARP_CAP * sizeof(int2));
-constexpr size_t WS_SORT = align256(WS_SS + (size_t)WARP_CAP * sizeof(int));       // edge records by start row
-constexpr size_t WS_ACT = align256(WS_SORT + (size_t)WARP_CAP * sizeof(EdgeRec));
-constexpr size_t WS_BYTES = align256(WS_ACT + (size_t)WARP_CAP * sizeof(EdgeRec));  // active edge records
+constexpr size_t WS_SORT = align256(WS_SS + (size_t)WARP_CAP * sizeof(int));     // sweep records by start row
+constexpr size_t WS_ACT = align256(WS_SORT + (size_t)WARP_CAP * sizeof(int4));
+constexpr size_t WS_BYTES = align256(WS_ACT + (size_t)WARP_CAP * sizeof(int4));  // active sweep records
+constexpr int SWEEP_END_FAR = 1023;  // sweep record end row: beyond the warp's last row
 static_assert(NWARP * WS_BYTES <= SCRATCH_BYTES_PER_CTA, "warp scratch layout");
 
 struct KParams {
