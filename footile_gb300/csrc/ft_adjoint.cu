@@ -42,12 +42,27 @@ constexpr int NW = ABLOCK / 32;
 constexpr int EPT = 4;                 // edges per thread per edge chunk
 constexpr int ECHUNK = ABLOCK * EPT;
 
+// The block's stroke point walk, carried from one chunk of ops (or window of points) to
+// the next (stroke_points_block).
+struct SPCarry {
+    int pw;           // last PenWidth op so far, -1
+    int pc, pc_pw;    // last Close/Move/Line/Quad/Cubic op so far and the PenWidth op before it
+    int ce;           // last close event so far: 2 * op + (op is a Close), -1
+    int kept;         // points kept so far (uncapped)
+    int nsub;         // sub-strokes started after the first
+    int have_prev;    // a point has been walked: its position and op follow
+    float px, py;
+    int pop;
+    int last_op;      // op of the last stored point, -1
+};
+
 struct ASmem {
     int wsum[NW];
     int wmax[NW];
     int wmax2[NW];
     int wmax3[NW];
     int off[ECHUNK + 1];
+    SPCarry spc;
     int carry_pen, carry_close, carry_base, carry_sub;
     int status;
     int total;
@@ -722,9 +737,9 @@ __device__ bool bin_edges(ASmem& sm, int* hist, int* boff, int* blist, int V, in
 // ------------------------------------------------------------------- strokes
 // Plotter::stroke (plotter.rs:356-365): stroke points with widths from the pen walk
 // (stroker.rs:204-236), the outline of every sub-stroke (stroker.rs:239-416) as
-// footile emits it, then the fill of the outline transformed a second time.  Thread 0
-// runs the stroker sequentially and records every outline point as a node over the
-// stroke points: an offset point, a miter intersection or an arc point.  The backward
+// footile emits it, then the fill of the outline transformed a second time.  Every
+// outline point is recorded as a node over the stroke points: an offset point, a miter
+// intersection or an arc point.  The backward
 // reverses the nodes with their Jacobians (decisions held) and chains stroke points to
 // the op floats (Bernstein weights of the transformed curve) and widths to the
 // PenWidth ops (linear in t between the pen's width and the op's).
@@ -832,104 +847,205 @@ __device__ __forceinline__ StrokeScr stroke_scr(unsigned char* scr) {
     return S;
 }
 
-// Thread 0: the stroke points and sub-strokes of the path (Plotter's pen walk into
-// Stroke::add_point / close).  Returns the stroke point count; *n_sub gets the
-// sub-stroke count, *status the path status.
-__device__ int stroke_points_dev(const AParams& p, const ft_op* ops, int n, float sw0, const StrokeScr& S,
-                                 int* n_sub, int* status) {
+// The stroke points and sub-strokes of the path (Plotter's pen walk into
+// Stroke::add_point / close, plotter.rs:175-332, stroker.rs:204-236) with the whole
+// block, the same as a walk of the ops one by one.  Ops go in chunks of ABLOCK: max scans give every op the PenWidth in effect and the pen before it (the last
+// Close/Move/Line/Quad/Cubic before it, its end point and width), each op's points (curve
+// leaves) are placed by a block scan into a raw window (the node area, unused until the
+// outline), and the window is compacted in order.  The one-thread walk's rules, per raw
+// point k after the first: a close event (a Close, or the Move's own close before its
+// point) between the ops of points k - 1 and k ends the sub-stroke and keeps point k,
+// the last such event giving the ended sub-stroke's `joined`; else k is dropped when it
+// repeats point k - 1's position (the last kept point then has that position too).  The
+// first VCAP kept points are stored; close events after the last stored point mark the
+// last sub-stroke.  Returns the stored point count; *n_sub gets the sub-stroke count.
+// Every thread must call.
+constexpr int SP_RAW = 65536;  // raw points per window
+static_assert((size_t)SP_RAW * SPT_BYTES <= (size_t)NODE_CAP * SND_BYTES, "raw window fits the node area");
+__device__ int stroke_points_block(const AParams& p, ASmem& sm, const ft_op* ops, int n, float sw0,
+                                   const StrokeScr& S, int* n_sub) {
+    const int tid = threadIdx.x;
     const float* m = p.xf;
-    // ---- stroke points (plotter.rs:175-332 into Stroke::add_point / close)
-    float sw = sw0;
-    int cur_pw = -1, pen = -1, pen_wsrc = -1;
-    P2 penp = p2(0.0f, 0.0f);
-    float penw = sw0;
-    int ns = 0, nsub = 0;
-    SSub cur{0, 0, 0, 0};  // the sub-stroke being built (stored when the next one starts)
-    P2 last = p2(0.0f, 0.0f);
-    auto close = [&](int joined) {
-        if (ns > 0) {
-            cur.joined = joined;
-            cur.done = 1;
-        }
-    };
-    auto add = [&](P2 q, float w, int op, int form, float t, int pn, int w0, int w1) {
-        if (ns >= VCAP) return;  // the stroke keeps 65,535 points (stroker.rs:204-216)
-        const int done = cur.done;
-        if (done) {
-            S.subs[nsub++] = cur;
-            cur = SSub{ns, 0, 0, 0};
-        }
-        const bool coincident = ns > 0 && last.x == q.x && last.y == q.y;
-        if (done || !coincident) {
-            S.sp[ns++] = SPt{q.x, q.y, w, t, op, form, pn, w0, w1, 0};
-            last = q;
-            cur.n++;
-        }
-    };
-    for (int i = 0; i < n; i++) {
-        const ft_op o = load_op(ops, i);
-        switch (o.kind) {
-            case FT_OP_CLOSE:
-                close(1);
-                pen = -1;
-                pen_wsrc = cur_pw;
-                penp = p2(0.0f, 0.0f);
-                penw = sw;
-                break;
-            case FT_OP_MOVE:
-            case FT_OP_LINE: {
-                const P2 q = op_pt(o, 0);
-                if (o.kind == FT_OP_MOVE) close(0);
-                add(xform(m, q), sw, i, F_POINT, 1.0f, -1, cur_pw, cur_pw);
-                pen = i;
-                pen_wsrc = cur_pw;
-                penp = q;
-                penw = sw;
-                break;
+    SPCarry& C = sm.spc;
+    SPt* raw = reinterpret_cast<SPt*>(S.nd);
+    int* lpw_of = sm.off;  // per op of the chunk: the last PenWidth op before it
+    if (tid == 0) {
+        C.pw = C.pc = C.pc_pw = C.ce = -1;
+        C.kept = C.nsub = C.have_prev = 0;
+        C.px = C.py = 0.0f;
+        C.pop = C.last_op = -1;
+        S.subs[0].start = 0;
+    }
+    __syncthreads();
+    auto sw_at = [&](int pw) { return pw >= 0 ? ops[pw].v[0] : sw0; };
+    for (int c0 = 0; c0 < n; c0 += ABLOCK) {
+        const int i = c0 + tid;
+        ft_op o;
+        o.kind = -1;
+        if (i < n) o = load_op(ops, i);
+        const int kind = o.kind;
+        const bool pc = kind >= FT_OP_CLOSE && kind <= FT_OP_CUBIC;
+        int inc, exc;
+        block_max_scan(kind == FT_OP_PEN_WIDTH ? i : -1, sm.wmax, inc, exc);
+        const int lpw = max(exc, C.pw);
+        const int pw_last = max(inc, C.pw);
+        lpw_of[tid] = lpw;
+        int pc_inc, pc_exc;
+        block_max_scan(pc ? i : -1, sm.wmax2, pc_inc, pc_exc);
+        int ce_inc, ce_exc;
+        block_max_scan(kind == FT_OP_CLOSE || kind == FT_OP_MOVE ? 2 * i + (kind == FT_OP_CLOSE) : -1, sm.wmax3,
+                       ce_inc, ce_exc);
+        const int ce = max(ce_inc, C.ce);  // close events up to and with this op
+        // the pen before this op (plotter.rs:175-224; Close resets it to the origin)
+        const int j = max(pc_exc, C.pc);
+        const int j_pw = j < 0 ? -1 : (j >= c0 ? lpw_of[j - c0] : C.pc_pw);
+        int pen = -1, pen_wsrc = -1;
+        P2 penp = p2(0.0f, 0.0f);
+        float penw = sw0;
+        if (j >= 0) {
+            const ft_op q = load_op(ops, j);
+            pen_wsrc = j_pw;
+            penw = sw_at(j_pw);
+            if (q.kind != FT_OP_CLOSE) {
+                pen = j;
+                penp = op_pt(q, end_slot(q.kind));
             }
-            case FT_OP_QUAD:
-            case FT_OP_CUBIC: {
-                const bool cubic = o.kind == FT_OP_CUBIC;
-                const P2 A = xform(m, penp), B = xform(m, op_pt(o, 0)), C = xform(m, op_pt(o, 1));
-                const P2 D = cubic ? xform(m, op_pt(o, 2)) : C;
-                float wb, wc, wd;
-                if (cubic) {  // float_lerp (geom.rs:14-16)
-                    wb = __fadd_rn(sw, __fmul_rn(__fsub_rn(penw, sw), 1.0f / 3.0f));
-                    wc = __fadd_rn(sw, __fmul_rn(__fsub_rn(penw, sw), 2.0f / 3.0f));
-                    wd = sw;
-                } else {
-                    wb = ftk::fmid(penw, sw);
-                    wc = sw;
-                    wd = sw;
-                }
-                if (!pfinite(A) || !pfinite(B) || !pfinite(C) || !pfinite(D)) {
-                    *status = max(*status, (int)FT_ERR_ARG);
-                    add(D, sw, i, F_POINT, 1.0f, -1, cur_pw, cur_pw);
+        }
+        const float sw = sw_at(lpw);
+        const int cur_pw = lpw;
+        // this op's points
+        const bool cubic = kind == FT_OP_CUBIC;
+        P2 A = p2(0.0f, 0.0f), B = A, Cc = A, D = A;
+        float wb = 0.0f, wc = 0.0f, wd = 0.0f;
+        bool curve = false;
+        int cnt = 0;
+        if (kind == FT_OP_MOVE || kind == FT_OP_LINE) {
+            cnt = 1;
+        } else if (kind == FT_OP_QUAD || cubic) {
+            A = xform(m, penp);
+            B = xform(m, op_pt(o, 0));
+            Cc = xform(m, op_pt(o, 1));
+            D = cubic ? xform(m, op_pt(o, 2)) : Cc;
+            if (cubic) {  // float_lerp (geom.rs:14-16)
+                wb = __fadd_rn(sw, __fmul_rn(__fsub_rn(penw, sw), 1.0f / 3.0f));
+                wc = __fadd_rn(sw, __fmul_rn(__fsub_rn(penw, sw), 2.0f / 3.0f));
+                wd = sw;
+            } else {
+                wb = ftk::fmid(penw, sw);
+                wc = sw;
+                wd = sw;
+            }
+            cnt = 1;
+            if (!pfinite(A) || !pfinite(B) || !pfinite(Cc) || !pfinite(D)) {
+                atomicMax(&sm.status, (int)FT_ERR_ARG);
+            } else {
+                curve = true;
+                int dh = 0;
+                auto none = [](int, P2, float, float) {};
+                cnt = cubic ? curve_walk_w<true>(A, B, Cc, D, penw, wb, wc, wd, p.tol_sq, &dh, none)
+                            : curve_walk_w<false>(A, B, Cc, D, penw, wb, wc, wd, p.tol_sq, &dh, none);
+                if (dh) atomicMax(&sm.status, (int)FT_ERR_DEPTH);
+            }
+        }
+        int total;
+        const int base = block_excl_sum(cnt, sm.wsum, total);
+        for (int w0 = 0; w0 < total; w0 += SP_RAW) {
+            const int w1 = min(w0 + SP_RAW, total);
+            // ---- this window's raw points; `pad` holds the op's close events
+            if (cnt > 0 && base < w1 && base + cnt > w0) {
+                auto put = [&](int k, P2 q, float w, float t, int form, int pn, int ws0) {
+                    const int r = base + k;
+                    if (r >= w0 && r < w1) raw[r - w0] = SPt{q.x, q.y, w, t, i, form, pn, ws0, cur_pw, ce};
+                };
+                if (!curve) {
+                    put(0, kind == FT_OP_MOVE || kind == FT_OP_LINE ? xform(m, op_pt(o, 0)) : D, sw, 1.0f, F_POINT,
+                        -1, cur_pw);
                 } else {
                     int dh = 0;
-                    const int pn = pen, w0 = pen_wsrc, w1 = cur_pw;
-                    auto leaf = [&](int, P2 q, float w, float t) { add(q, w, i, cubic ? F_CUBIC : F_QUAD, t, pn, w0, w1); };
+                    auto leaf = [&](int k, P2 q, float w, float t) {
+                        put(k, q, w, t, cubic ? F_CUBIC : F_QUAD, pen, pen_wsrc);
+                    };
                     if (cubic)
-                        curve_walk_w<true>(A, B, C, D, penw, wb, wc, wd, p.tol_sq, &dh, leaf);
+                        curve_walk_w<true>(A, B, Cc, D, penw, wb, wc, wd, p.tol_sq, &dh, leaf);
                     else
-                        curve_walk_w<false>(A, B, C, D, penw, wb, wc, wd, p.tol_sq, &dh, leaf);
-                    if (dh) *status = max(*status, (int)FT_ERR_DEPTH);
+                        curve_walk_w<false>(A, B, Cc, D, penw, wb, wc, wd, p.tol_sq, &dh, leaf);
                 }
-                pen = i;
-                pen_wsrc = cur_pw;
-                penp = cubic ? op_pt(o, 2) : op_pt(o, 1);
-                penw = sw;
-                break;
             }
-            case FT_OP_PEN_WIDTH:
-                sw = o.v[0];
-                cur_pw = i;
-                break;
-            default:
-                break;
+            __syncthreads();
+            // ---- compact the window in order
+            for (int r0 = 0; r0 < w1 - w0; r0 += ABLOCK) {
+                const int r = r0 + tid;
+                const bool valid = r < w1 - w0;
+                SPt q{};
+                bool have_prev = false, close_between = false, keep = false;
+                if (valid) {
+                    q = raw[r];
+                    float px = C.px, py = C.py;
+                    int pop = C.pop;
+                    have_prev = C.have_prev != 0;
+                    if (r > 0) {
+                        const SPt pv = raw[r - 1];
+                        px = pv.x;
+                        py = pv.y;
+                        pop = pv.op;
+                        have_prev = true;
+                    }
+                    close_between = have_prev && (q.pad >> 1) > pop;
+                    keep = !have_prev || close_between || !(q.x == px && q.y == py);
+                }
+                int ktot;
+                const int K = C.kept + block_excl_sum(keep ? 1 : 0, sm.wsum, ktot);
+                const bool stored = keep && K < VCAP;
+                const bool starts = stored && close_between;
+                int stot;
+                const int J = C.nsub + 1 + block_excl_sum(starts ? 1 : 0, sm.wsum, stot);
+                if (stored) {
+                    const int joined = q.pad & 1;
+                    q.pad = 0;
+                    S.sp[K] = q;
+                    if (starts) {
+                        S.subs[J].start = K;
+                        S.subs[J - 1].joined = joined;
+                        S.subs[J - 1].done = 1;
+                    }
+                    atomicMax(&C.last_op, q.op);  // stored points come in op order
+                }
+                __syncthreads();
+                if (valid && (r == w1 - w0 - 1 || tid == ABLOCK - 1)) {
+                    C.have_prev = 1;
+                    C.px = q.x;
+                    C.py = q.y;
+                    C.pop = q.op;
+                }
+                if (tid == 0) {
+                    C.kept += ktot;
+                    C.nsub += stot;
+                }
+                __syncthreads();
+            }
+        }
+        if (tid == ABLOCK - 1) {
+            C.pw = pw_last;
+            const int pc_last = max(pc_inc, C.pc);
+            if (pc_last >= c0) C.pc_pw = lpw_of[pc_last - c0];
+            C.pc = pc_last;
+            C.ce = ce;
+        }
+        __syncthreads();
+    }
+    const int ns = min(C.kept, VCAP), nsub = C.nsub + 1;
+    for (int jj = tid; jj < nsub; jj += ABLOCK) {
+        const int st = ns > 0 ? S.subs[jj].start : 0;
+        S.subs[jj].n = (jj + 1 < nsub ? S.subs[jj + 1].start : ns) - st;
+        if (jj == nsub - 1) {
+            // close events after the last stored point end the last sub-stroke
+            const bool closed = ns > 0 && (C.ce >> 1) > C.last_op;
+            S.subs[jj].start = st;
+            S.subs[jj].joined = closed ? (C.ce & 1) : 0;
+            S.subs[jj].done = closed ? 1 : 0;
         }
     }
-    S.subs[nsub++] = cur;
+    __syncthreads();
     *n_sub = nsub;
     return ns;
 }
@@ -1350,11 +1466,11 @@ __global__ void __launch_bounds__(ABLOCK, 3) k_adjoint(AParams p) {
         __syncthreads();
         int V;
         if (p.stroke) {
+            int nsub = 0;
+            const int ns = stroke_points_block(p, sm, ops, (int)d.n_ops, d.s_width, S, &nsub);
             if (tid == 0) {
-                int st = FT_OK, nsub = 0;
-                s_counts[2] = stroke_points_dev(p, ops, (int)d.n_ops, d.s_width, S, &nsub, &st);
+                s_counts[2] = ns;
                 s_counts[0] = nsub;
-                atomicMax(&sm.status, st);
             }
             __syncthreads();
             int nv = 0, nn = 0;
