@@ -704,6 +704,25 @@ def run_ours(args):
     e2e_val = job_px / e2e_s / 1e6
     # masks of the e2e path must equal the device path's
     same = bool(np.array_equal(ras_np, ras_d.cpu().numpy()))
+    # The pinned Matte8 rasters above are written in place by the kernels over the host
+    # link; the copy pipeline (rasters copied in, drawn, copied out in two overlapped
+    # chunks) is timed beside it with the mapping switched off.
+    mapped = os.environ.get("FT_HOST_MAPPED", "1") != "0"
+    old_env = os.environ.get("FT_HOST_MAPPED")
+    os.environ["FT_HOST_MAPPED"] = "0"
+    try:
+        fill_batch(ctx2, ops_np, paths, _abi.MATTE8, ras_np)
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            fill_batch(ctx2, ops_np, paths, _abi.MATTE8, ras_np)
+        e2e_copy_s = replicas.reduce_max((time.perf_counter() - t0) / e2e_steps, dev)
+    finally:
+        if old_env is None:
+            os.environ.pop("FT_HOST_MAPPED", None)
+        else:
+            os.environ["FT_HOST_MAPPED"] = old_env
+    same = same and bool(np.array_equal(ras_np, ras_d.cpu().numpy()))
 
     # ---- one launch per path (ft_fill, device mode), on a sample
     per_path = None
@@ -763,11 +782,18 @@ def run_ours(args):
         "vs_baseline": None, "dtype": "int32 (16.16 fixed) + f32", "data": "synthetic",
         "config": config(args, world),
         "paths_per_s": len(paths) * world / (ms_max * 1e-3),
-        "e2e": {"value": e2e_val, "unit": METRIC, "h2d_bytes_per_step": int(32 * n_ops + nbytes + 40 * len(paths)),
-                "d2h_bytes_per_step": int(nbytes), "ms_per_step": e2e_s * 1e3, "masks_equal_device_path": same},
+        "e2e": {"value": e2e_val, "unit": METRIC,
+                "h2d_bytes_per_step": int(32 * n_ops + 40 * len(paths) + (0 if mapped else nbytes)),
+                "d2h_bytes_per_step": int(nbytes), "ms_per_step": e2e_s * 1e3, "masks_equal_device_path": same,
+                "rasters": ("pinned host memory written in place by the kernels over the host link (every "
+                            "raster row a figure reaches; the rest keep the host's bytes)") if mapped else
+                           "copied in, drawn and copied out in two overlapped chunks",
+                "copy_pipeline": {"value": job_px / e2e_copy_s / 1e6, "ms_per_step": e2e_copy_s * 1e3,
+                                  "h2d_bytes_per_step": int(32 * n_ops + nbytes + 40 * len(paths)),
+                                  "d2h_bytes_per_step": int(nbytes)}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": profiled_traffic(), "peak_kind": peak_kind,
-                     "kernel": "ftk::k_raster_warp + ftk::k_raster (graph: 2 memsets, warp rasteriser, CTA rasteriser)", "kernel_ms": kmean,
+                     "kernel": "ftk::k_raster_warp<false> + ftk::k_raster<false> (graph: 2 memsets, warp rasteriser, CTA rasteriser)", "kernel_ms": kmean,
                      "algorithmic_bytes_per_launch": int(alg_bytes)},
         # the cell accumulation's bound: shared-memory atomics (data-path wavefronts of one
         # launch from the ncu summary, over this run's kernel time; the atomic data path's

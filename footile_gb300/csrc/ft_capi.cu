@@ -269,7 +269,7 @@ cudaError_t enqueue(const ftk::KParams& p, int grid_b, int grid_w, int smem, cud
 // per-path statuses go to status_d.
 int run_plan(ft_ctx* c, PlanSlot& slot, int stroke, int rule, const ft_op* ops_d, const ft_path_desc* paths,
              uint32_t n_paths, int fmt, uint8_t* rasters_d, const float* sw_chain, float* sw_out, int32_t* status_d,
-             bool events = true) {
+             bool events = true, bool host_rasters = false) {
     uint32_t max_w = 1;
     for (uint32_t i = 0; i < n_paths; i++) max_w = std::max(max_w, paths[i].width);
     const int smem = choose_smem(c, max_w);
@@ -326,6 +326,7 @@ int run_plan(ft_ctx* c, PlanSlot& slot, int stroke, int rule, const ft_op* ops_d
     p.overflow = static_cast<uint32_t*>(c->overflow.p);
     p.queue = static_cast<uint32_t*>(c->queue.p);
     p.rasters = rasters_d;
+    p.host_rasters = host_rasters ? 1 : 0;
     p.status = status_d;
     p.sw_out = sw_out;
     p.sw_chain = sw_chain;
@@ -340,10 +341,10 @@ int run_plan(ft_ctx* c, PlanSlot& slot, int stroke, int rule, const ft_op* ops_d
 }
 
 int run(ft_ctx* c, int stroke, int rule, const ft_op* ops_d, const ft_path_desc* paths, uint32_t n_paths, int fmt,
-        uint8_t* rasters_d, const float* sw_chain, float* sw_out) {
+        uint8_t* rasters_d, const float* sw_chain, float* sw_out, bool host_rasters = false) {
     FT_CU(c->status.ensure(sizeof(int32_t) * std::max(n_paths, 1u)), "alloc status");
     return run_plan(c, c->plan, stroke, rule, ops_d, paths, n_paths, fmt, rasters_d, sw_chain, sw_out,
-                    static_cast<int32_t*>(c->status.p));
+                    static_cast<int32_t*>(c->status.p), true, host_rasters);
 }
 
 bool valid_ops_host(const ft_op* ops, uint64_t n) {
@@ -829,6 +830,29 @@ static int host_chunks(uint64_t raster_bytes, uint32_t n_paths) {
     return n_paths >= 4u * (uint32_t)k ? k : 1;
 }
 
+// Device address of a host raster buffer that the kernels can write in place: page-locked
+// memory mapped into this device's address space (cudaHostAlloc, torch's pinned memory,
+// cudaHostRegister), checked at both ends of the range; nullptr otherwise or when
+// FT_HOST_MAPPED=0.
+static uint8_t* mapped_host(ft_ctx* c, const void* host, uint64_t n, const char* switch_env = "FT_HOST_MAPPED") {
+    const char* env = getenv(switch_env);
+    uint8_t* p = static_cast<uint8_t*>(const_cast<void*>(host));
+    if ((env && atoi(env) == 0) || !p || n == 0) return nullptr;
+    cudaPointerAttributes a{}, b{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess || cudaPointerGetAttributes(&b, p + (n - 1)) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || b.type != cudaMemoryTypeHost || !a.devicePointer || !b.devicePointer ||
+        a.device != c->device || b.device != c->device)
+        return nullptr;
+    uint8_t* d = static_cast<uint8_t*>(a.devicePointer);
+    return static_cast<uint8_t*>(b.devicePointer) == d + (n - 1) ? d : nullptr;
+}
+
+// The kernels load ops as 16-byte words: ops read in place must be 16-byte aligned.
+static bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
 FT_API int ft_fill_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* ops, uint32_t n_ops_total,
                          const ft_path_desc* paths, uint32_t n_paths, int32_t fmt, uint8_t* rasters,
                          uint64_t raster_bytes, int32_t where) {
@@ -842,6 +866,31 @@ FT_API int ft_fill_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* o
     for (uint32_t i = 0; i < n_paths; i++) {
         int st = check_path(c, paths[i], fmt, raster_bytes, n_ops_total);
         if (st != FT_OK) return st;
+    }
+    if (where == FT_HOST && fmt == FT_MATTE8) {
+        // Matte8 rasters are only written (whole rows from the figure's first row down),
+        // so a mapped host buffer takes the kernels' stores directly over the host link:
+        // no raster copy in or out, the writes overlap the drawing
+        uint8_t* mapped = mapped_host(c, rasters, raster_bytes);
+        if (mapped) {
+            // page-locked ops are read in place too (FT_HOST_MAPPED_OPS=0: uploaded first)
+            const ft_op* ops_d = reinterpret_cast<const ft_op*>(
+                aligned16(ops) ? mapped_host(c, ops, sizeof(ft_op) * (uint64_t)n_ops_total,
+                                                         "FT_HOST_MAPPED_OPS")
+                                           : nullptr);
+            if (!ops_d) {
+                FT_CU(c->ops.ensure(sizeof(ft_op) * std::max<uint64_t>(n_ops_total, 1)), "alloc ops");
+                if (n_ops_total)
+                    FT_CU(cudaMemcpyAsync(c->ops.p, ops, sizeof(ft_op) * n_ops_total, cudaMemcpyHostToDevice,
+                                          c->stream),
+                          "upload ops");
+                ops_d = static_cast<const ft_op*>(c->ops.p);
+            }
+            const int st = run(c, stroke, rule, ops_d, paths, n_paths, fmt, mapped, nullptr, nullptr, true);
+            if (st != FT_OK) return st;
+            FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
+            return FT_OK;
+        }
     }
     if (where == FT_HOST) {
         const int k = host_chunks(raster_bytes, n_paths);

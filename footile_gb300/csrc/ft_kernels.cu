@@ -1416,13 +1416,22 @@ __device__ __forceinline__ void scan_sweep(int4 R, int s, bool st, int* row, int
              (R.w & FX_MASK) + 1, (R.w >> 26) & 1 ? -1 : 1, row, W, nullptr);
 }
 
-// Resolve one band row and write it (fig.rs:621-665, imgbuf.rs:38-199).
-template <bool ZERO = false>
+// Resolve one band row and write it (fig.rs:621-665, imgbuf.rs:38-199).  With WORDS
+// (rasters in mapped host memory), Matte8 rows are written as aligned 4-byte words
+// whatever the row's alignment: lane L of a step stores the word at row position x - a
+// (a = the row's misalignment), made of the last a bytes of the previous lane's four
+// pixels and the first 4 - a of its own; the words at the row's ends are written byte by
+// byte inside the row — no partial words cross the host link.  In device memory the byte
+// stores of a misaligned row cost less than the shuffles.
+template <bool ZERO, bool WORDS>
 __device__ __forceinline__ void resolve_row(int* arow, int W, int Wp, uint8_t* drow, int rule, int fmt,
                                             unsigned clr) {
     const int lane = threadIdx.x & 31;
     unsigned carry = 0;
-    for (int x0 = 0; x0 < W; x0 += 128) {
+    const int mis = WORDS ? (int)(reinterpret_cast<uintptr_t>(drow) & 3) : 0;
+    const int xend = (WORDS && fmt == FT_MATTE8) ? W + mis : W;
+    unsigned pcarry = 0;  // Matte8: the previous step's last four pixels
+    for (int x0 = 0; x0 < xend; x0 += 128) {
         const int x = x0 + lane * 4;
         int4 a = make_int4(0, 0, 0, 0);
         if (x < Wp) {
@@ -1438,8 +1447,8 @@ __device__ __forceinline__ void resolve_row(int* arow, int W, int Wp, uint8_t* d
         carry += __shfl_sync(FULL, inc, 31);
         const unsigned v0 = resolve_cov(s0 + ex, rule), v1 = resolve_cov(s1 + ex, rule);
         const unsigned v2 = resolve_cov(s2 + ex, rule), v3 = resolve_cov(s3 + ex, rule);
-        if (x >= W) continue;
-        if (fmt == FT_MATTE8) {
+        if (fmt == FT_MATTE8 && !WORDS) {
+            if (x >= W) continue;
             uint8_t* dp = drow + x;
             if (x + 3 < W && ((reinterpret_cast<uintptr_t>(dp) & 3) == 0)) {
                 *reinterpret_cast<unsigned*>(dp) = v0 | (v1 << 8) | (v2 << 16) | (v3 << 24);
@@ -1449,7 +1458,27 @@ __device__ __forceinline__ void resolve_row(int* arow, int W, int Wp, uint8_t* d
                 if (x + 2 < W) dp[2] = (uint8_t)v2;
                 if (x + 3 < W) dp[3] = (uint8_t)v3;
             }
-        } else {
+            continue;
+        }
+        if (WORDS && fmt == FT_MATTE8) {
+            const unsigned px4 = v0 | (v1 << 8) | (v2 << 16) | (v3 << 24);  // pixels x .. x + 3
+            unsigned prev = __shfl_up_sync(FULL, px4, 1);
+            if (lane == 0) prev = pcarry;
+            pcarry = __shfl_sync(FULL, px4, 31);
+            const unsigned word = mis ? (px4 << (8 * mis)) | (prev >> (32 - 8 * mis)) : px4;
+            const int lo = x - mis;  // row position of the word's first byte (4-byte aligned address)
+            uint8_t* wp = drow + lo;
+            if (lo >= 0 && lo + 3 < W) {
+                *reinterpret_cast<unsigned*>(wp) = word;
+            } else {
+#pragma unroll
+                for (int b = 0; b < 4; b++)
+                    if (lo + b >= 0 && lo + b < W) wp[b] = (uint8_t)(word >> (8 * b));
+            }
+            continue;
+        }
+        if (x >= W) continue;
+        {
             unsigned* dp = reinterpret_cast<unsigned*>(drow) + x;
             const unsigned vv[4] = {v0, v1, v2, v3};
 #pragma unroll
@@ -1513,7 +1542,8 @@ __device__ void raster_rows(const KParams& P, const ft_path_desc& d, const CStat
             }
         }
         for (int rr = r0 + warp; rr < r1; rr += NWARP)
-            resolve_row(area + (size_t)(rr - r0) * Wp, W, Wp, base + (size_t)rr * d.stride, P.rule, P.fmt, clr);
+            resolve_row<false, false>(area + (size_t)(rr - r0) * Wp, W, Wp, base + (size_t)rr * d.stride, P.rule,
+                                      P.fmt, clr);
         __syncthreads();
     }
 }
@@ -1538,6 +1568,7 @@ static_assert(offsetof(WarpSmem, row) % 16 == 0 && sizeof(WarpSmem) % 16 == 0, "
 // active edge list holds the records themselves (one load per edge and row from a list
 // that stays small and hot, instead of an index and a record of the figure's edges).
 // hist holds every start row's edge count (count_edges_warp).
+template <bool WORDS>
 __device__ void raster_sweep_warp(const KParams& P, const ft_path_desc& d, const CState& S, const int2* pts,
                                   const int* ss, int4* sorted, int4* active, int* hist, int* row) {
     const int lane = threadIdx.x & 31;
@@ -1595,11 +1626,13 @@ __device__ void raster_sweep_warp(const KParams& P, const ft_path_desc& d, const
         }
         n_act = nn;
         __syncwarp();
-        resolve_row<true>(row, W, Wp, base + (size_t)(row_begin + s) * d.stride, P.rule, P.fmt, clr);
+        resolve_row<true, WORDS>(row, W, Wp, base + (size_t)(row_begin + s) * d.stride, P.rule, P.fmt, clr);
         __syncwarp();
     }
 }
 
+// WORDS: the rasters are mapped host memory (Matte8 rows go out as aligned words).
+template <bool WORDS>
 __global__ void __launch_bounds__(BLOCK, 4) k_raster_warp(KParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1633,7 +1666,7 @@ __global__ void __launch_bounds__(BLOCK, 4) k_raster_warp(KParams P) {
                 __syncwarp();
                 count_edges_warp(M.S, pts, ss, M.u.hist, nrows);
                 __syncwarp();
-                raster_sweep_warp(P, d, M.S, pts, ss, sorted, active, M.u.hist, M.row);
+                raster_sweep_warp<WORDS>(P, d, M.S, pts, ss, sorted, active, M.u.hist, M.row);
             }
         }
         if (P.sw_out) {
@@ -1742,9 +1775,13 @@ int raster_blocks_per_sm(int smem_bytes, bool stroke) {
 
 cudaError_t launch_raster_warp(const KParams& p, int grid, cudaStream_t s) {
     const int smem = raster_warp_smem();
-    cudaError_t e = cudaFuncSetAttribute(k_raster_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaError_t e = cudaFuncSetAttribute(p.host_rasters ? k_raster_warp<true> : k_raster_warp<false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
-    k_raster_warp<<<grid, BLOCK, smem, s>>>(p);
+    if (p.host_rasters)
+        k_raster_warp<true><<<grid, BLOCK, smem, s>>>(p);
+    else
+        k_raster_warp<false><<<grid, BLOCK, smem, s>>>(p);
     return cudaGetLastError();
 }
 
@@ -1752,9 +1789,10 @@ int raster_warp_smem() { return (int)(NWARP * sizeof(WarpSmem)); }
 
 int raster_warp_blocks_per_sm() {
     const int smem = raster_warp_smem();
-    cudaFuncSetAttribute(k_raster_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_raster_warp<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_raster_warp<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_raster_warp, BLOCK, smem) != cudaSuccess) return 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_raster_warp<false>, BLOCK, smem) != cudaSuccess) return 1;
     return n > 0 ? n : 1;
 }
 

@@ -111,6 +111,7 @@ struct KParams {
     uint8_t* rasters;
     int32_t* status;         // per path, atomicMax of FT_ERR_* codes
     float* sw_out;           // per path pen width after the call (nullable)
+    int host_rasters;        // rasters are mapped host memory: Matte8 rows go out as aligned words
     const float* sw_chain;   // nullable: initial pen width of every path
     unsigned char* scratch;  // gridDim.x * SCRATCH_BYTES_PER_CTA bytes
     float xf[6];

@@ -169,8 +169,10 @@ def pack_batch(paths_ops, sizes, fmt=_abi.MATTE8, clrs=None, s_width=1.0):
 def fill_batch(ctx, ops, paths, fmt, rasters, rule=FillRule.NonZero, stroke=False):
     """One persistent launch over many independent Plotter calls (`ft_fill_batch`).
 
-    `ops` / `rasters` are host numpy arrays (copied in and out) or CUDA tensors
-    (device-resident, asynchronous).  `paths` is a host `ft_path_desc` array.
+    `ops` / `rasters` are host numpy arrays (copied in and out; Matte8 rasters in
+    page-locked memory, e.g. a pinned torch tensor's `.numpy()`, are written in place by
+    the kernels) or CUDA tensors (device-resident, asynchronous).  `paths` is a host
+    `ft_path_desc` array.
     Returns the per-path status array.
     """
     paths = np.ascontiguousarray(paths, dtype=_abi.PATH_DTYPE)

@@ -150,9 +150,14 @@ FT_API int ft_stroke(ft_ctx* ctx, const ft_op* ops, uint32_t n_ops, int32_t fmt,
  * (raster_bytes).  `paths` is always a host array; `ops` / `rasters` live where
  * `where` says.  The per-path status of the last batch is read with
  * ft_batch_status.  The raster regions of the paths must not overlap.  With
- * FT_HOST and 64 MB of rasters or more, paths whose ops and rasters lie in ascending
- * order in the host buffers are drawn in two chunks, the copies of one overlapping
- * the drawing of the other (FT_HOST_CHUNKS in the environment sets the count). */
+ * FT_HOST, Matte8 rasters in page-locked host memory mapped into the device's address
+ * space (cudaHostAlloc, cudaHostRegister, a pinned torch tensor) are written in place
+ * by the kernels — a Matte8 fill or stroke only writes, so nothing is copied in or out
+ * — and page-locked, 16-byte aligned ops are read in place (FT_HOST_MAPPED=0 /
+ * FT_HOST_MAPPED_OPS=0 in the environment switch either off).  Otherwise, with 64 MB of
+ * rasters or more, paths whose ops and rasters lie in ascending order in the host
+ * buffers are drawn in two chunks, the copies of one overlapping the drawing of the
+ * other (FT_HOST_CHUNKS sets the count). */
 FT_API int ft_fill_batch(ft_ctx* ctx, int32_t stroke, int32_t rule, const ft_op* ops,
                          uint32_t n_ops_total, const ft_path_desc* paths,
                          uint32_t n_paths, int32_t fmt, uint8_t* rasters,

@@ -1,6 +1,8 @@
 """Host batches in pipelined chunks (`ft_fill_batch` with host buffers: chunks copied in,
 drawn and copied out on overlapping streams) give the same masks and statuses as the
-device path and the oracle, and fall back to one pass when the layout does not allow it."""
+device path and the oracle, and fall back to one pass when the layout does not allow it.
+Matte8 rasters in page-locked host memory are written in place by the kernels; the rows
+a figure does not reach keep the caller's bytes."""
 import os
 
 import numpy as np
@@ -21,6 +23,41 @@ def chunks():
         os.environ.pop("FT_HOST_CHUNKS", None)
     else:
         os.environ["FT_HOST_CHUNKS"] = old
+
+
+@pytest.fixture
+def mapped_env():
+    old = os.environ.get("FT_HOST_MAPPED")
+    yield lambda v: os.environ.__setitem__("FT_HOST_MAPPED", str(v))
+    if old is None:
+        os.environ.pop("FT_HOST_MAPPED", None)
+    else:
+        os.environ["FT_HOST_MAPPED"] = old
+
+
+@pytest.mark.parametrize("stroke", [False, True])
+def test_mapped_host_rasters(ctx, mapped_env, stroke):
+    torch = pytest.importorskip("torch")
+    ops, paths, nbytes = workloads.glyphs(n_paths=400, seed=41 + stroke, max_side=200)
+    ops["kind"][int(paths["op_begin"][11]) + 1] = 9  # an unknown op kind in path 11
+    init = np.random.default_rng(2).integers(0, 256, nbytes).astype(np.uint8)
+    want = init.copy()
+    oracle.fill_batch(int(stroke), _abi.NONZERO, ops, paths, _abi.MATTE8, want)
+    pinned = torch.from_numpy(init.copy()).pin_memory()
+    got = pinned.numpy()
+    st = fill_batch(ctx, ops, paths, _abi.MATTE8, got, stroke=stroke)
+    assert st[11] == _abi.ERR_ARG and (np.delete(st, 11) == 0).all()
+    ok = np.ones(nbytes, bool)
+    p = paths[11]
+    ok[int(p["raster_offset"]):int(p["raster_offset"]) + int(p["height"]) * int(p["stride"])] = False
+    assert np.array_equal(got[ok], want[ok])
+    # the copy path (mapping off) writes the same bytes
+    mapped_env(0)
+    pinned2 = torch.from_numpy(init.copy()).pin_memory()
+    got2 = pinned2.numpy()
+    st2 = fill_batch(ctx, ops, paths, _abi.MATTE8, got2, stroke=stroke)
+    assert np.array_equal(st2, st)
+    assert np.array_equal(got2, got)
 
 
 @pytest.mark.parametrize("k", [2, 3, 5])
