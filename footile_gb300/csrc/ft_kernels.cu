@@ -1564,13 +1564,52 @@ struct WarpSmem {
 };
 static_assert(offsetof(WarpSmem, row) % 16 == 0 && sizeof(WarpSmem) % 16 == 0, "warp smem alignment");
 
+// Rows of a mapped host raster staged in shared memory so that whole 128-byte lines cross
+// the host link: a raster whose rows are contiguous (stride == width) is one byte range
+// [lo, end); rows are resolved into `stg` (which holds the bytes from the line address L0
+// on), then every complete line is stored with one aligned word per lane, and the partial
+// line left over moves to the front of the buffer.  Bytes outside [lo, end) are never
+// stored (the rows above the figure and other rasters keep theirs).
+constexpr int STAGE_BYTES = 768;  // a partial line (< 128 B) and one row (<= WARP_MAX_SIDE B)
+static_assert(127 + WARP_MAX_SIDE < STAGE_BYTES && STAGE_BYTES % 128 == 0, "staging holds a line and a row");
+static_assert(sizeof(int) * WARP_MAX_SIDE + STAGE_BYTES <= sizeof(WarpBuildSmem), "row staging fits the build window");
+
+__device__ __forceinline__ void stage_flush(unsigned char* stg, uint8_t*& L0, const uint8_t* lo, const uint8_t* end,
+                                            bool final) {
+    const int lane = threadIdx.x & 31;
+    const int fill = (int)(end - L0);
+    const int nfull = final ? (fill + 127) >> 7 : fill >> 7;
+    for (int li = 0; li < nfull; li++) {
+        const int o = (li << 7) + 4 * lane;
+        uint8_t* a = L0 + o;
+        const unsigned wv = *reinterpret_cast<const unsigned*>(stg + o);
+        if (a >= lo && a + 4 <= end) {
+            *reinterpret_cast<unsigned*>(a) = wv;
+        } else {
+#pragma unroll
+            for (int b = 0; b < 4; b++)
+                if (a + b >= lo && a + b < end) a[b] = (uint8_t)(wv >> (8 * b));
+        }
+    }
+    if (final) return;
+    const int rest = fill - (nfull << 7);  // < 128: the partial line moves to the front
+    if (nfull > 0) {
+        const unsigned v = *reinterpret_cast<const unsigned*>(stg + (nfull << 7) + 4 * lane);
+        __syncwarp();
+        if (4 * lane < rest) *reinterpret_cast<unsigned*>(stg + 4 * lane) = v;
+        __syncwarp();
+        L0 += nfull << 7;
+    }
+}
+
 // The edge records (sweep_rec) are built straight into their buckets (`sorted`); the
 // active edge list holds the records themselves (one load per edge and row from a list
 // that stays small and hot, instead of an index and a record of the figure's edges).
 // hist holds every start row's edge count (count_edges_warp).
 template <bool WORDS>
 __device__ void raster_sweep_warp(const KParams& P, const ft_path_desc& d, const CState& S, const int2* pts,
-                                  const int* ss, int4* sorted, int4* active, int* hist, int* row) {
+                                  const int* ss, int4* sorted, int4* active, int* hist, int* row,
+                                  unsigned char* stg) {
     const int lane = threadIdx.x & 31;
     const int count = S.count, H = (int)d.height, W = (int)d.width, Wp = (W + 3) & ~3;
     const int top_row = S.top_row, row_begin = max(top_row, 0);
@@ -1597,6 +1636,10 @@ __device__ void raster_sweep_warp(const KParams& P, const ft_path_desc& d, const
     }
     for (int x = lane; x < Wp; x += 32) row[x] = 0;
     __syncwarp();
+    // mapped host rasters with contiguous rows go out in whole lines (stage_flush)
+    const bool staged = WORDS && d.stride == d.width;
+    uint8_t* const lo = base + (size_t)row_begin * d.stride;
+    uint8_t* L0 = reinterpret_cast<uint8_t*>(reinterpret_cast<uintptr_t>(lo) & ~(uintptr_t)127);
     // hist[b] now ends bucket b
     int n_act = 0;
     for (int s = 0; s < nrows; s++) {
@@ -1626,9 +1669,17 @@ __device__ void raster_sweep_warp(const KParams& P, const ft_path_desc& d, const
         }
         n_act = nn;
         __syncwarp();
-        resolve_row<true, WORDS>(row, W, Wp, base + (size_t)(row_begin + s) * d.stride, P.rule, P.fmt, clr);
+        uint8_t* drow = base + (size_t)(row_begin + s) * d.stride;
+        if (staged) {
+            resolve_row<true, false>(row, W, Wp, stg + (drow - L0), P.rule, P.fmt, clr);
+            __syncwarp();
+            stage_flush(stg, L0, lo, drow + W, false);
+        } else {
+            resolve_row<true, WORDS>(row, W, Wp, drow, P.rule, P.fmt, clr);
+        }
         __syncwarp();
     }
+    if (staged) stage_flush(stg, L0, lo, base + (size_t)H * d.stride, true);
 }
 
 // WORDS: the rasters are mapped host memory (Matte8 rows go out as aligned words).
@@ -1666,7 +1717,10 @@ __global__ void __launch_bounds__(BLOCK, 4) k_raster_warp(KParams P) {
                 __syncwarp();
                 count_edges_warp(M.S, pts, ss, M.u.hist, nrows);
                 __syncwarp();
-                raster_sweep_warp<WORDS>(P, d, M.S, pts, ss, sorted, active, M.u.hist, M.row);
+                // the build's window is free during the sweep: its bytes after the
+                // histogram stage the rows of a mapped host raster
+                raster_sweep_warp<WORDS>(P, d, M.S, pts, ss, sorted, active, M.u.hist, M.row,
+                                         reinterpret_cast<unsigned char*>(&M.u) + sizeof(M.u.hist));
             }
         }
         if (P.sw_out) {
