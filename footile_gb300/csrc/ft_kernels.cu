@@ -2106,8 +2106,8 @@ __device__ __forceinline__ void composite_row(int* row, unsigned short* last, un
     __syncwarp();
 }
 
-// One CTA per band of P.band_rows rows, one warp per row.  Each warp walks the calls
-// in order with warp-level steps only (no block barriers after set-up).
+// One CTA per band of P.band_rows rows (32 threads per row), one warp per row.  Each warp
+// walks the calls in order with warp-level steps only (no block barriers after set-up).
 __global__ void __launch_bounds__(BLOCK) k_cbands(KParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -2115,7 +2115,7 @@ __global__ void __launch_bounds__(BLOCK) k_cbands(KParams P) {
     const int R = P.band_rows, nb = P.n_bands, b = blockIdx.x;
     const int r = b * R + warp;  // this warp's raster row
     unsigned char* ftab = smem;
-    for (int i = threadIdx.x; i < FTAB_BYTES; i += BLOCK) {
+    for (int i = threadIdx.x; i < FTAB_BYTES; i += blockDim.x) {
         unsigned v = (unsigned)(i & 255);
         for (int k = 0; k < (i >> 8); k++) v = ch8_mul(v, 255u);
         ftab[i] = (unsigned char)v;
@@ -2310,7 +2310,7 @@ int composite_build_blocks_per_sm(int smem_bytes, bool stroke) {
 cudaError_t launch_composite_bands(const KParams& p, int smem_bytes, cudaStream_t s) {
     cudaError_t e = cudaFuncSetAttribute(k_cbands, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
     if (e != cudaSuccess) return e;
-    k_cbands<<<p.n_bands, BLOCK, smem_bytes, s>>>(p);
+    k_cbands<<<p.n_bands, 32 * p.band_rows, smem_bytes, s>>>(p);
     return cudaGetLastError();
 }
 
