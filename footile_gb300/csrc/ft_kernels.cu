@@ -41,8 +41,10 @@ namespace ftk {
 
 constexpr unsigned FULL = 0xFFFFFFFFu;
 // Curve leaves of an op kept (in local memory) from the count pass for the emit pass;
-// ops with more leaves are walked again.
+// ops with more leaves are walked again.  Warp builds (small glyphs) keep 64; CTA builds
+// (large figures, few CTAs, L1 to spare) keep more.
 constexpr int LEAF_CACHE = 64;
+constexpr int LEAF_CACHE_CTA = 256;
 constexpr bool BLOCK_COMPACT = true;  // figure building by the whole CTA (false: warp 0)
 constexpr int SRAW = 1024;            // stroke points per window (float4 in the raw window's bytes)
 
@@ -1002,9 +1004,10 @@ __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, B
         int n = 0;
         int depth_hit = 0;
         bool nonfinite = false;
-        int2 cache[LEAF_CACHE];  // leaves of the count pass, reused by the emit pass
+        constexpr int LC = G::N == 32 ? LEAF_CACHE : LEAF_CACHE_CTA;
+        int2 cache[LC];  // leaves of the count pass, reused by the emit pass
         auto keep_leaf = [&](int k, P2 q, float) {
-            if (k < LEAF_CACHE) cache[k] = make_int2(f2fx(q.x), f2fx(q.y));
+            if (k < LC) cache[k] = make_int2(f2fx(q.x), f2fx(q.y));
         };
         P2 A = p2(0, 0), Bq = p2(0, 0), C = p2(0, 0), D = p2(0, 0);
         if (kind == FT_OP_MOVE || kind == FT_OP_LINE) {
@@ -1091,7 +1094,7 @@ __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, B
                             emit(0, A, 0.f);
                         } else if (nonfinite) {
                             emit(0, kind == FT_OP_QUAD ? C : D, 0.f);
-                        } else if (n <= LEAF_CACHE) {
+                        } else if (n <= LC) {
                             for (int k = lo; k < hi; k++) {
                                 const int idx = off + k - g0;
                                 raw2[idx] = cache[k];
@@ -1157,7 +1160,7 @@ __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, B
                             emit(0, A, 0.f);
                         } else if (nonfinite) {
                             emit(0, kind == FT_OP_QUAD ? C : D, 0.f);
-                        } else if (n <= LEAF_CACHE) {
+                        } else if (n <= LC) {
                             for (int k = lo; k < hi; k++) {
                                 const int idx = off + k - w0;
                                 B.raw[idx] = cache[k];
