@@ -17,6 +17,8 @@ crate and cannot be built here; its restatement is the timed CPU code).
 
 Multi-GPU (torchrun): every rank renders its own 65,536-path batch (weak
 scaling, no collective on the data path); value = all ranks' pixels / max time.
+`--gpus N` (N > 1) outside torchrun starts the N ranks itself under
+torch.distributed.run, so such a call never measures one GPU in their place.
 """
 import argparse
 import json
@@ -211,6 +213,18 @@ def extra_strokes(ctx, stream, dev, cpu=True, reps=2):
     return out
 
 
+def launch_ranks(args):
+    """`--gpus N` with N > 1 outside torchrun: run this script as N ranks (one process
+    per GPU) under torch.distributed.run on this node and return their exit status."""
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__)] + sys.argv[1:]
+    return subprocess.call(cmd)
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -317,8 +331,11 @@ def accumulation(kernel_ms):
             "source": "profiles/k_raster_warp_glyphs_65536.txt"}
 
 
-def cpu_baseline(ops, paths, nbytes, seconds, threads):
-    """Time the oracle on a bounded sample of the workload (all host threads)."""
+def cpu_baseline(ops, paths, nbytes, seconds, threads, gpu_masks=None):
+    """Time the oracle on a bounded sample of the workload (all host threads).  With
+    `gpu_masks` (the timed batch's rasters, copied to the host), the oracle's masks of
+    every path (the timed sample, then the rest outside the timing) are compared with
+    them byte for byte: returns (baseline, parity)."""
     import oracle
     from footile_gb300 import _abi
     px = paths["width"].astype(np.int64) * paths["height"]
@@ -332,9 +349,19 @@ def cpu_baseline(ops, paths, nbytes, seconds, threads):
     t0 = time.perf_counter()
     oracle.fill_batch(0, _abi.NONZERO, ops, paths[:n], _abi.MATTE8, r, n_threads=threads)
     dt = time.perf_counter() - t0
-    return {"value": float(px[:n].sum() / dt / 1e6), "unit": METRIC, "cores": threads, "kind": "port",
+    base = {"value": float(px[:n].sum() / dt / 1e6), "unit": METRIC, "cores": threads, "kind": "port",
             "sample": f"first {n} of {len(paths)} paths ({int(px[:n].sum())} px), one Plotter per path",
             "paths_per_s": n / dt, "seconds": dt}
+    if gpu_masks is None:
+        return base, None
+    if n < len(paths):
+        oracle.fill_batch(0, _abi.NONZERO, ops, paths[n:], _abi.MATTE8, r, n_threads=threads)
+    bad = np.flatnonzero(r != gpu_masks)
+    bad_paths = np.unique(np.searchsorted(paths["raster_offset"].astype(np.int64), bad, side="right") - 1)
+    parity = {"paths_checked": int(len(paths)), "mismatching_paths": int(len(bad_paths)),
+              "bytes_compared": int(nbytes), "mismatching_bytes": int(len(bad)), "bit_exact": len(bad) == 0,
+              "against": "oracle masks of every path of the timed batch (initial rasters zero on both sides)"}
+    return base, parity
 
 
 def run_reference(args):
@@ -607,6 +634,8 @@ def run_only(args):
 def run_ours(args):
     import torch
     rank, world, local = dist_env()
+    if world != args.gpus:
+        raise SystemExit(f"--gpus {args.gpus} but {world} rank(s) were started")
     torch.cuda.set_device(local)
     if world > 1:
         import torch.distributed as dist
@@ -676,6 +705,8 @@ def run_ours(args):
     barrier()
     launches = ctx.launch_count() - launches0
     ms = e0.elapsed_time(e1) / max(args.steps, 1)
+    # the timed graph's masks, for the parity check against the oracle
+    gpu_masks = ras_d.cpu().numpy() if (rank == 0 and world == 1 and not args.no_cpu) else None
     # per-launch device time of the graph (memsets + rasteriser), library events
     kms = []
     for _ in range(args.steps):
@@ -710,21 +741,14 @@ def run_ours(args):
     # The pinned Matte8 rasters above are written in place by the kernels over the host
     # link; the copy pipeline (rasters copied in, drawn, copied out in two overlapped
     # chunks) is timed beside it with the mapping switched off.
-    mapped = os.environ.get("FT_HOST_MAPPED", "1") != "0"
-    old_env = os.environ.get("FT_HOST_MAPPED")
-    os.environ["FT_HOST_MAPPED"] = "0"
-    try:
+    mapped = ctx2.tuning()["host_mapped"] == 0
+    ctx2.tune(host_mapped=1)  # ops and rasters copied in, rasters copied out
+    fill_batch(ctx2, ops_np, paths, _abi.MATTE8, ras_np)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
         fill_batch(ctx2, ops_np, paths, _abi.MATTE8, ras_np)
-        barrier()
-        t0 = time.perf_counter()
-        for _ in range(e2e_steps):
-            fill_batch(ctx2, ops_np, paths, _abi.MATTE8, ras_np)
-        e2e_copy_s = replicas.reduce_max((time.perf_counter() - t0) / e2e_steps, dev)
-    finally:
-        if old_env is None:
-            os.environ.pop("FT_HOST_MAPPED", None)
-        else:
-            os.environ["FT_HOST_MAPPED"] = old_env
+    e2e_copy_s = replicas.reduce_max((time.perf_counter() - t0) / e2e_steps, dev)
     same = same and bool(np.array_equal(ras_np, ras_d.cpu().numpy()))
 
     # ---- one launch per path (ft_fill, device mode), on a sample
@@ -769,9 +793,9 @@ def run_ours(args):
                 extras[name] = {"error": repr(e)}
 
     # ---- CPU baseline (rank 0, N=1 only)
-    cpu = None
+    cpu, parity = None, None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline(ops, paths, nbytes, args.cpu_seconds, os.cpu_count() or 1)
+        cpu, parity = cpu_baseline(ops, paths, nbytes, args.cpu_seconds, os.cpu_count() or 1, gpu_masks)
 
     if rank != 0:
         return
@@ -803,6 +827,7 @@ def run_ours(args):
         # utilisation as ncu measured it)
         "accumulation": accumulation(kmean),
         "cpu_baseline": cpu,
+        "parity": parity,
         "modes": {"batched_paths_per_s": len(paths) / (ms_max * 1e-3), "per_path_launch": per_path,
                   "batched_over_per_path": (len(paths) / (ms_max * 1e-3) / per_path["paths_per_s"]) if per_path else None},
         "clocks": clk,
@@ -815,6 +840,8 @@ def run_ours(args):
 
 def main():
     args = parse_args()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(launch_ranks(args))
     if args.impl == "reference":
         run_reference(args)
     elif args.only:

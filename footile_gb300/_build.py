@@ -1,8 +1,11 @@
-"""Compile the CUDA library (libfootile_gpu.so) for sm_103a with nvcc, in-tree.
+"""Compile the CUDA library for sm_103a with nvcc, in-tree.
 
-Each translation unit compiles in parallel; the shared library lands in
-footile_gb300/_build/.  No torch extension machinery is involved: the library is
-a plain C ABI shared object.
+Each translation unit compiles in parallel into footile_gb300/_build/, which then
+holds the C-ABI shared library (libfootile_gpu.so, loaded by the Python mirror) and
+the same objects as a static library (libfootile_gpu.a, for a host program or a Rust
+crate that links the path in: link it with the CUDA runtime, e.g. `-lcudart_static
+-ldl -lpthread -lrt`, and the C++ standard library).  No torch extension machinery is
+involved.
 """
 import concurrent.futures as cf
 import os
@@ -13,13 +16,15 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libfootile_gpu.so")
+STATIC_LIB = os.path.join(OUT, "libfootile_gpu.a")
 
 SOURCES = ["ft_kernels.cu", "ft_adjoint.cu", "ft_convert.cu", "ft_capi.cu"]
 HEADERS = ["ft_device.cuh", "ft_kernels.cuh", "ft_adjoint.cuh"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Bit-exact float stages: no FMA contraction, IEEE division and square root.
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-prec-div=true", "-prec-sqrt=true",
-           "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden", "--expt-relaxed-constexpr"]
+           "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden", "-Xcompiler", "-ffp-contract=off",
+           "--expt-relaxed-constexpr"]
 
 
 def nvcc():
@@ -37,9 +42,9 @@ def _inputs():
 
 
 def up_to_date():
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(STATIC_LIB):
         return False
-    t = os.path.getmtime(LIB)
+    t = min(os.path.getmtime(LIB), os.path.getmtime(STATIC_LIB))
     return all(os.path.getmtime(p) <= t for p in _inputs())
 
 
@@ -69,6 +74,14 @@ def build(force=False, verbose=False):
     if r.returncode != 0:
         raise RuntimeError("nvcc link failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
     os.replace(tmp, LIB)
+    # the static library: the same objects (whole-program device code, no device link)
+    tmp_a = STATIC_LIB + ".tmp"
+    if os.path.exists(tmp_a):
+        os.remove(tmp_a)
+    r = subprocess.run(["ar", "rcs", tmp_a] + objs, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("ar failed:\n" + r.stdout + r.stderr)
+    os.replace(tmp_a, STATIC_LIB)
     return LIB
 
 

@@ -101,7 +101,8 @@ def exported_symbols():
 class Tuning(ctypes.Structure):
     """`ft_tuning`: the knobs of a batch plan (see include/footile_gpu.h)."""
     _fields_ = [("warp_max_side", ctypes.c_int32), ("cta_smem_bytes", ctypes.c_int32),
-                ("split_px", ctypes.c_int32), ("grid_per_sm", ctypes.c_int32)]
+                ("split_px", ctypes.c_int32), ("grid_per_sm", ctypes.c_int32), ("band_rows", ctypes.c_int32),
+                ("pool_edges", ctypes.c_int32), ("host_chunks", ctypes.c_int32), ("host_mapped", ctypes.c_int32)]
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}
@@ -202,6 +203,12 @@ class Context:
         t = Tuning()
         self.check(self.L.ft_get_tuning(self.h, ctypes.byref(t)))
         return t.as_dict()
+
+    def tune(self, **knobs):
+        """Change some plan knobs, keeping the others as they are in effect."""
+        t = self.tuning()
+        t.update(knobs)
+        self.set_tuning(t)
 
     def autotune(self, ops_dev, paths, fmt, rasters_dev, rule=0, stroke=False, cache_path=None):
         """Time candidate plans of a batch on device buffers (CUDA tensors) and keep the

@@ -1171,17 +1171,14 @@ __device__ void outline_block(const AParams& p, const StrokeScr& S, int nsub, AS
                 const P2 A0 = N(2 * s - 2), A1 = N(2 * s - 1), B0 = N(2 * s), B1 = N(2 * s + 1);
                 if (p.join == FT_JOIN_MITER) {
                     jt = J_BEVEL;
-                    if (p.miter_limit > 0.0f) {
-                        const float sm_min = __fdiv_rn(1.0f, p.miter_limit);
-                        const float th = ftk::pangle_rel(ftk::psub(A1, A0), ftk::psub(B0, B1));
-                        const float smv = fabsf(ft_sinf(__fdiv_rn(th, 2.0f)));
-                        if (smv >= sm_min && smv < 1.0f && ftk::pline_x(A0, A1, B0, B1, &xp)) jt = J_MITER;
-                    }
+                    const ftk::P2 u = ftk::psub(A1, A0), v = ftk::psub(B0, B1);
+                    if (ft_miter_join(u.x, u.y, v.x, v.y, p.miter_g) && ftk::pline_x(A0, A1, B0, B1, &xp))
+                        jt = J_MITER;
                 } else if (p.join == FT_JOIN_BEVEL) {
                     jt = J_BEVEL;
                 } else {
-                    const float th = ftk::pangle_rel(ftk::psub(A1, A0), ftk::psub(B0, B1));
-                    jt = th <= 0.0f ? J_BEVEL : J_ARC;
+                    const ftk::P2 u = ftk::psub(A1, A0), v = ftk::psub(B0, B1);
+                    jt = ft_round_join_arc(u.x, u.y, v.x, v.y) ? J_ARC : J_BEVEL;
                 }
                 if (jt == J_MITER) {
                     cnt_v += 1;

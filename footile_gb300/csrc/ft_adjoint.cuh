@@ -62,6 +62,7 @@ struct AParams {
     int stroke;             // Plotter::stroke: the outline of each path is filled NonZero
     int join;
     float miter_limit;
+    float miter_g;  // ft_miter_angle(miter_limit)
     int no_area;            // NonZero only: keep no winding area; the backward takes dcov/dS from cov
                             // (0 < cov < 1 exactly where 0 < S < 1) and reads grad_cov only there
 };

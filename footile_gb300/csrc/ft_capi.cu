@@ -9,6 +9,7 @@
 #include <string>
 #include <vector>
 
+#include "../../include/ft_fmath.h"
 #include "ft_adjoint.cuh"
 #include "ft_kernels.cuh"
 
@@ -85,7 +86,7 @@ struct ft_ctx {
     int sm_count = 0;
     int max_smem = 0;
     uint32_t fig_cap = 0;  // vertices per figure of a fill above footile's 65,535 (0: footile's cap)
-    ft_tuning tune{0, 0, 0, 0};
+    ft_tuning tune{0, 0, 0, 0, 0, 0, 0, 0};
     bool tuned = false;  // `tune` replaces the built-in plan defaults
     std::string err;
 };
@@ -112,16 +113,13 @@ int cuda_fail(ft_ctx* c, cudaError_t e, const char* what) {
         if (_e != cudaSuccess) return cuda_fail(c, _e, what); \
     } while (0)
 
-// Plan knobs: an environment variable overrides the context's tuning (ft_set_tuning /
-// ft_autotune_batch), which overrides the built-in default.
+// Plan knobs: the context's tuning (ft_set_tuning / ft_autotune_batch) overrides the
+// built-in default.
 // Dynamic shared memory for a batch whose widest raster row is `max_w` pixels.
 int choose_smem(const ft_ctx* c, uint32_t max_w) {
     const int wp = (int)((max_w + 3) & ~3u);
-    const char* env = getenv("FT_SMEM_BYTES");
     int smem;
-    if (env) {
-        smem = atoi(env);
-    } else if (c->tuned && c->tune.cta_smem_bytes > 0) {
+    if (c->tuned && c->tune.cta_smem_bytes > 0) {
         smem = c->tune.cta_smem_bytes;
     } else if (wp <= 512) {
         smem = 48 * 1024;  // four CTAs per SM
@@ -134,25 +132,20 @@ int choose_smem(const ft_ctx* c, uint32_t max_w) {
     return smem;
 }
 
-// Largest canvas side the warp rasteriser takes (FT_WARP_MAX_SIDE, 0 disables it).
+// Largest canvas side the warp rasteriser takes (0 disables it).
 int warp_max_side(const ft_ctx* c) {
-    const char* env = getenv("FT_WARP_MAX_SIDE");
-    int v = env ? atoi(env) : (c->tuned ? c->tune.warp_max_side : ftk::WARP_MAX_SIDE);
+    const int v = c->tuned ? c->tune.warp_max_side : ftk::WARP_MAX_SIDE;
     return std::max(0, std::min(v, ftk::WARP_MAX_SIDE));
 }
 
-// Paths of at least this many pixels are split into row ranges (FT_SPLIT_PX).
+// Paths of at least this many pixels are split into row ranges.
 uint64_t split_px(const ft_ctx* c) {
-    const char* env = getenv("FT_SPLIT_PX");
-    if (env) return strtoull(env, nullptr, 10);
     if (c->tuned && c->tune.split_px > 0) return (uint64_t)c->tune.split_px;
     return (uint64_t)(1u << 20);
 }
 
-// Resident CTAs per SM of the persistent rasterisers (FT_GRID sets the whole grid).
+// Resident CTAs per SM of the persistent rasterisers.
 int grid_cap(const ft_ctx* c, int per_sm) {
-    const char* genv = getenv("FT_GRID");
-    if (genv) return atoi(genv);
     if (c->tuned && c->tune.grid_per_sm > 0) per_sm = std::min(per_sm, (int)c->tune.grid_per_sm);
     return c->sm_count * per_sm;
 }
@@ -227,6 +220,7 @@ void fill_params(ft_ctx* c, ftk::KParams& p, int stroke, int rule, int fmt, int 
     p.tol_sq = t * t;
     p.join = c->join;
     p.miter_limit = c->miter_limit;
+    p.miter_g = ft_miter_angle(c->miter_limit);
     p.rule = rule;
     p.fmt = fmt;
     p.stroke = stroke;
@@ -599,13 +593,14 @@ FT_API void ft_batch_destroy(ft_batch* b) {
 FT_API int ft_set_tuning(ft_ctx* c, const ft_tuning* t) {
     if (!c) return FT_ERR_ARG;
     if (!t) {
-        c->tune = ft_tuning{0, 0, 0, 0};
+        c->tune = ft_tuning{0, 0, 0, 0, 0, 0, 0, 0};
         c->tuned = false;
         return FT_OK;
     }
     if (t->warp_max_side < 0 || t->warp_max_side > ftk::WARP_MAX_SIDE || t->cta_smem_bytes < 0 ||
         (t->cta_smem_bytes && t->cta_smem_bytes < 40 * 1024) || t->cta_smem_bytes > c->max_smem ||
-        t->split_px < 0 || t->grid_per_sm < 0)
+        t->split_px < 0 || t->grid_per_sm < 0 || t->band_rows < 0 || t->band_rows > ftk::NWARP ||
+        t->pool_edges < 0 || t->host_chunks < 0 || t->host_chunks > 16 || t->host_mapped < 0 || t->host_mapped > 2)
         return fail(c, FT_ERR_ARG, "tuning out of range");
     c->tune = *t;
     c->tuned = true;
@@ -617,7 +612,7 @@ FT_API int ft_get_tuning(ft_ctx* c, ft_tuning* t) {
     if (c->tuned) {
         *t = c->tune;
     } else {
-        *t = ft_tuning{ftk::WARP_MAX_SIDE, 0, 1 << 20, 0};
+        *t = ft_tuning{ftk::WARP_MAX_SIDE, 0, 1 << 20, 0, 0, 0, 0, 0};
     }
     return FT_OK;
 }
@@ -820,24 +815,24 @@ static int run_pipelined(ft_ctx* c, int stroke, int rule, const ft_op* ops, uint
     return FT_OK;
 }
 
-// Chunks of a host batch: FT_HOST_CHUNKS, else 2 from 64 MB of rasters.  More chunks
-// lose: every chunk's persistent launch ends on its slowest paths (65,536 glyphs in
-// 1 / 2 / 4 chunks: 16.3 / 15.7 / 21.6 ms end to end).
-static int host_chunks(uint64_t raster_bytes, uint32_t n_paths) {
-    const char* env = getenv("FT_HOST_CHUNKS");
-    int k = env ? atoi(env) : (raster_bytes >= (64ull << 20) ? 2 : 1);
+// Chunks of a host batch: the tuning's host_chunks, else 2 from 64 MB of rasters.  More
+// chunks lose: every chunk's persistent launch ends on its slowest paths (65,536 glyphs
+// in 1 / 2 / 4 chunks: 16.3 / 15.7 / 21.6 ms end to end).
+static int host_chunks(const ft_ctx* c, uint64_t raster_bytes, uint32_t n_paths) {
+    int k = (c->tuned && c->tune.host_chunks > 0) ? c->tune.host_chunks : (raster_bytes >= (64ull << 20) ? 2 : 1);
     k = std::max(1, std::min(k, 16));
     return n_paths >= 4u * (uint32_t)k ? k : 1;
 }
 
 // Device address of a host raster buffer that the kernels can write in place: page-locked
 // memory mapped into this device's address space (cudaHostAlloc, torch's pinned memory,
-// cudaHostRegister), checked at both ends of the range; nullptr otherwise or when
-// FT_HOST_MAPPED=0.
-static uint8_t* mapped_host(ft_ctx* c, const void* host, uint64_t n, const char* switch_env = "FT_HOST_MAPPED") {
-    const char* env = getenv(switch_env);
+// cudaHostRegister), checked at both ends of the range; nullptr otherwise or when the
+// tuning's host_mapped switches the mapping off for this buffer (1: rasters and ops are
+// copied, 2: ops are copied).
+static uint8_t* mapped_host(ft_ctx* c, const void* host, uint64_t n, bool ops) {
     uint8_t* p = static_cast<uint8_t*>(const_cast<void*>(host));
-    if ((env && atoi(env) == 0) || !p || n == 0) return nullptr;
+    const int mode = c->tuned ? c->tune.host_mapped : 0;
+    if (mode == 1 || (ops && mode == 2) || !p || n == 0) return nullptr;
     cudaPointerAttributes a{}, b{};
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess || cudaPointerGetAttributes(&b, p + (n - 1)) != cudaSuccess) {
         cudaGetLastError();
@@ -871,13 +866,11 @@ FT_API int ft_fill_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* o
         // Matte8 rasters are only written (whole rows from the figure's first row down),
         // so a mapped host buffer takes the kernels' stores directly over the host link:
         // no raster copy in or out, the writes overlap the drawing
-        uint8_t* mapped = mapped_host(c, rasters, raster_bytes);
+        uint8_t* mapped = mapped_host(c, rasters, raster_bytes, false);
         if (mapped) {
-            // page-locked ops are read in place too (FT_HOST_MAPPED_OPS=0: uploaded first)
+            // page-locked ops are read in place too (host_mapped 2: uploaded first)
             const ft_op* ops_d = reinterpret_cast<const ft_op*>(
-                aligned16(ops) ? mapped_host(c, ops, sizeof(ft_op) * (uint64_t)n_ops_total,
-                                                         "FT_HOST_MAPPED_OPS")
-                                           : nullptr);
+                aligned16(ops) ? mapped_host(c, ops, sizeof(ft_op) * (uint64_t)n_ops_total, true) : nullptr);
             if (!ops_d) {
                 FT_CU(c->ops.ensure(sizeof(ft_op) * std::max<uint64_t>(n_ops_total, 1)), "alloc ops");
                 if (n_ops_total)
@@ -893,7 +886,7 @@ FT_API int ft_fill_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* o
         }
     }
     if (where == FT_HOST) {
-        const int k = host_chunks(raster_bytes, n_paths);
+        const int k = host_chunks(c, raster_bytes, n_paths);
         if (k > 1) {
             const int st = run_pipelined(c, stroke, rule, ops, n_ops_total, paths, n_paths, fmt, rasters, raster_bytes, k);
             if (st != -1) return st;
@@ -930,8 +923,7 @@ FT_API int ft_fill_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* o
 // as many as the shared memory holds, at most eight.
 static int composite_band_rows(ft_ctx* c, uint32_t w, uint32_t h) {
     (void)h;
-    const char* env = getenv("FT_BAND_ROWS");
-    int R = env ? std::max(1, std::min(atoi(env), ftk::NWARP)) : ftk::NWARP;
+    int R = (c->tuned && c->tune.band_rows > 0) ? std::min((int)c->tune.band_rows, ftk::NWARP) : ftk::NWARP;
     while (R > 1 && ftk::composite_bands_smem(R, (int)w) > c->max_smem) R--;
     return R;
 }
@@ -1004,9 +996,9 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
         FT_CU(cudaMemcpyAsync(c->paths.p, paths, sizeof(ft_path_desc) * n_paths, cudaMemcpyHostToDevice, c->stream),
               "upload paths");
     // edge pool: grows until every path's binned edges fit
-    const char* penv = getenv("FT_POOL_EDGES");  // first pool size in edges (it grows on demand)
-    uint64_t want = penv ? std::max<uint64_t>(strtoull(penv, nullptr, 10), 1)
-                         : std::max<uint64_t>((uint64_t)n_ops_total * 64, 1u << 20);
+    // first pool size in edges (it grows on demand)
+    const bool penv = c->tuned && c->tune.pool_edges > 0;
+    uint64_t want = penv ? (uint64_t)c->tune.pool_edges : std::max<uint64_t>((uint64_t)n_ops_total * 64, 1u << 20);
     for (int attempt = 0; attempt < 4; attempt++) {
         if (!penv || attempt > 0) want = std::max<uint64_t>(want, c->pool.cap / sizeof(ftk::EdgeRec));
         if (penv && attempt == 0 && c->pool.cap > want * sizeof(ftk::EdgeRec)) c->pool.release();
@@ -1138,8 +1130,9 @@ static bool tune_lookup(const char* path, const std::string& key, ft_tuning* t) 
         char k[600];
         ft_tuning v;
         float ms;
-        if (sscanf(line, "%599s %d %d %d %d %f", k, &v.warp_max_side, &v.cta_smem_bytes, &v.split_px,
-                   &v.grid_per_sm, &ms) == 6 &&
+        v = ft_tuning{0, 0, 0, 0, 0, 0, 0, 0};
+        if (sscanf(line, "%599s %d %d %d %d %d %d %d %d %f", k, &v.warp_max_side, &v.cta_smem_bytes, &v.split_px,
+                   &v.grid_per_sm, &v.band_rows, &v.pool_edges, &v.host_chunks, &v.host_mapped, &ms) == 10 &&
             key == k) {
             *t = v;  // the last entry for a key wins
             found = true;
@@ -1212,6 +1205,7 @@ static fta::AParams adjoint_params(const ft_adjoint* a) {
     p.stroke = a->stroke;
     p.join = a->join;
     p.miter_limit = a->miter_limit;
+    p.miter_g = ft_miter_angle(a->miter_limit);
     p.cov = a->cov_d;
     p.no_area = a->no_area;
     return p;
@@ -1715,7 +1709,7 @@ FT_API int ft_autotune_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_o
     }
     if (ms_out) *ms_out = 0.0f;
     const std::string key = tune_key(c, stroke, rule, fmt, paths, n_paths);
-    ft_tuning best{0, 0, 0, 0};
+    ft_tuning best{0, 0, 0, 0, 0, 0, 0, 0};
     if (tune_lookup(cache_path, key, &best) && ft_set_tuning(c, &best) == FT_OK) {
         if (chosen) *chosen = best;
         return FT_OK;
@@ -1736,7 +1730,9 @@ FT_API int ft_autotune_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_o
         for (int sm : smems)
             for (int gp : grids) {
                 if (sm > c->max_smem) continue;
-                c->tune = ft_tuning{ws, sm, 1 << 20, gp};
+                // the batch plan's knobs; the composite and host-transfer knobs stay as set
+                c->tune = ft_tuning{ws, sm, 1 << 20, gp, saved.band_rows, saved.pool_edges, saved.host_chunks,
+                                    saved.host_mapped};
                 c->tuned = true;
                 ft_batch* b = nullptr;
                 if (ft_batch_create(c, stroke, rule, paths, n_paths, fmt, &b) != FT_OK) continue;
@@ -1770,8 +1766,9 @@ FT_API int ft_autotune_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_o
     if (cache_path) {
         FILE* f = fopen(cache_path, "a");
         if (f) {
-            fprintf(f, "%s %d %d %d %d %.4f\n", key.c_str(), best.warp_max_side, best.cta_smem_bytes, best.split_px,
-                    best.grid_per_sm, best_ms);
+            fprintf(f, "%s %d %d %d %d %d %d %d %d %.4f\n", key.c_str(), best.warp_max_side, best.cta_smem_bytes,
+                    best.split_px, best.grid_per_sm, best.band_rows, best.pool_edges, best.host_chunks,
+                    best.host_mapped, best_ms);
             fclose(f);
         }
     }

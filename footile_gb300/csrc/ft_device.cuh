@@ -1,7 +1,7 @@
 // ft_device.cuh — device primitives of the GB300 fill/stroke path.
 //
-// Fixed 16.16 arithmetic with release-mode wrapping (footile src/fixed.rs:65-199),
-// the f32 -> Fixed conversion of `Fixed::from(f32)` (fixed.rs:129-134, Rust `as`
+// Fixed 16.16 arithmetic with release-mode wrapping (footile src/fixed.rs:24-158),
+// the f32 -> Fixed conversion of `Fixed::from(f32)` (fixed.rs:88-93, Rust `as`
 // saturation), pointy 0.7 point operations as footile uses them (geom.rs:31-35,
 // plotter.rs:170,275, stroker.rs:305-309,354-360) with every float operation
 // rounded individually (no FMA contraction), and pix 0.14 Ch8 / SrcOver
@@ -24,11 +24,11 @@ constexpr int FX_MASK = FX_ONE - 1;
 __device__ __forceinline__ int wadd(int a, int b) { return (int)((unsigned)a + (unsigned)b); }
 __device__ __forceinline__ int wsub(int a, int b) { return (int)((unsigned)a - (unsigned)b); }
 __device__ __forceinline__ int wmul(int a, int b) { return (int)((unsigned)a * (unsigned)b); }
-// (a as i64 * b as i64) >> 16, as i32          fixed.rs:81-88
+// (a as i64 * b as i64) >> 16, as i32          fixed.rs:40-47
 __device__ __forceinline__ int fxmul(int a, int b) {
     return (int)(unsigned)(((long long)a * (long long)b) >> 16);
 }
-// ((a as i64) << 16) / b as i64, as i32          fixed.rs:90-97
+// ((a as i64) << 16) / b as i64, as i32          fixed.rs:49-56
 __device__ __forceinline__ int fxdiv(int a, int b) {
     return (int)(unsigned)(((long long)a * 65536LL) / (long long)b);
 }

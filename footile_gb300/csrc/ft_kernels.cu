@@ -771,21 +771,16 @@ __device__ int outline_item(const KParams& P, const float4* spts, const SubRec& 
     P2 a0, a1, b0, b1;
     seg(j - 1, &a0, &a1);
     seg(j, &b0, &b1);
-    if (P.join == FT_JOIN_MITER) {  // stroker.rs:340-367
-        const float ml = P.miter_limit;
-        if (ml > 0.0f) {
-            const float sm_min = __fdiv_rn(1.0f, ml);
-            const float th = pangle_rel(psub(a1, a0), psub(b0, b1));
-            const float sm = fabsf(ft_sinf(__fmul_rn(th, 0.5f)));
-            P2 xp;
-            if (sm >= sm_min && sm < 1.0f && pline_x(a0, a1, b0, b1, &xp)) {
-                if (lo <= 0 && 0 < hi) emit(0, xp);
-                return 1;
-            }
+    if (P.join == FT_JOIN_MITER) {  // stroker.rs:340-367 (the decision as ft_fmath.h takes it)
+        const P2 u = psub(a1, a0), v = psub(b0, b1);
+        P2 xp;
+        if (ft_miter_join(u.x, u.y, v.x, v.y, P.miter_g) && pline_x(a0, a1, b0, b1, &xp)) {
+            if (lo <= 0 && 0 < hi) emit(0, xp);
+            return 1;
         }
     } else if (P.join == FT_JOIN_ROUND) {  // stroker.rs:380-396
-        const float th = pangle_rel(psub(a1, a0), psub(b0, b1));
-        if (th > 0.0f) {
+        const P2 u = psub(a1, a0), v = psub(b0, b1);
+        if (ft_round_join_arc(u.x, u.y, v.x, v.y)) {
             if (lo <= 0 && 0 < hi) emit(0, a1);
             const int na = arc_walk(spts[v0(j)], a1, b0, P.tol_sq, max(lo - 1, 0), hi - 1, depth_hit,
                                     [&](int k, P2 q) { emit(k + 1, q); });
@@ -2322,11 +2317,13 @@ cudaError_t launch_composite_bands(const KParams& p, int smem_bytes, cudaStream_
 // ===========================================================================
 // Allocation-free single-path fill (ft_fill_noalloc).
 //
-// For callers that cannot allocate device memory: code running inside a stream
-// capture, under a fixed memory budget, or in a process whose allocator belongs to
-// another runtime.  The figure scratch of one CTA lives in a file-scope device
-// array that every GPU loading this library holds until the process exits; the
-// caller passes only inputs and outputs.  One CTA rasterises the whole path.
+// For callers that may not allocate device memory themselves or through this
+// library: a host whose device memory belongs to another runtime's allocator (a game
+// engine's or a language runtime's pool that must see every allocation), or a
+// process held to a fixed device-memory budget.  The figure scratch of one CTA lives
+// in a file-scope device array that every GPU loading this library holds until the
+// process exits; the caller passes only inputs and outputs.  One CTA rasterises the
+// whole path.
 namespace ftk {
 
 // vertices, sub-figure starts and edges of one figure of up to FT_MAX_POINTS vertices
@@ -2359,13 +2356,74 @@ __global__ void __launch_bounds__(BLOCK) k_fill_noalloc(KParams P, ft_path_desc 
 
 }  // namespace ftk
 
+#include <cuda.h>
 #include <mutex>
 
 namespace {
-// device address of g_noalloc_scratch, looked up once per device
+// Set-up of ft_fill_noalloc per device: the device address of g_noalloc_scratch and the
+// kernel's dynamic shared-memory limit, both belonging to the device's current context.
+// A device reset (cudaDeviceReset) destroys that context and unloads the module, so the
+// set-up is keyed by the context's unique id and done again in a new context.
 constexpr int NOALLOC_MAX_DEVICES = 64;
-void* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {nullptr};
+struct NoallocDev {
+    unsigned long long ctx_id = 0;  // 0: not set up
+    void* scratch = nullptr;
+    int smem_max = 0;
+};
+NoallocDev g_noalloc[NOALLOC_MAX_DEVICES];
 std::mutex g_noalloc_mu;
+
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+
+// Unique id of the calling thread's current context (0 when none is current yet),
+// through the runtime's driver entry points (no link against the driver library).
+unsigned long long current_ctx_id() {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<CtxGetIdFn>(f);
+    });
+    CUcontext cu = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&cu) != CUDA_SUCCESS || !cu || get_id(cu, &id) != CUDA_SUCCESS)
+        return 0;
+    return id;
+}
+
+// The set-up of `dev` (current) for its current context; false when a CUDA call fails.
+bool noalloc_setup(int dev, NoallocDev& out) {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    NoallocDev& D = g_noalloc[dev];
+    unsigned long long id = current_ctx_id();
+    if (id == 0 || id != D.ctx_id) {
+        void* p = nullptr;
+        // also makes the device's primary context current when none was
+        if (cudaGetSymbolAddress(&p, ftk::g_noalloc_scratch) != cudaSuccess || !p) return false;
+        int optin = 0;
+        if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return false;
+        const int smem_max = optin - 1024;
+        if (cudaFuncSetAttribute(ftk::k_fill_noalloc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max) !=
+            cudaSuccess)
+            return false;
+        id = current_ctx_id();
+        if (id == 0) return false;
+        D.ctx_id = id;
+        D.scratch = p;
+        D.smem_max = smem_max;
+    }
+    out = D;
+    return true;
+}
 }  // namespace
 
 extern "C" FT_API int ft_fill_noalloc(int32_t rule, const ft_op* ops, uint32_t n_ops, int32_t fmt,
@@ -2382,17 +2440,8 @@ extern "C" FT_API int ft_fill_noalloc(int32_t rule, const ft_op* ops, uint32_t n
         return FT_ERR_ARG;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES) return FT_ERR_CUDA;
-    void* scratch = nullptr;
-    {
-        // first call on this device: find the array's device address (before any stream capture)
-        std::lock_guard<std::mutex> lk(g_noalloc_mu);
-        if (!g_noalloc_ptr[dev]) {
-            void* p = nullptr;
-            if (cudaGetSymbolAddress(&p, ftk::g_noalloc_scratch) != cudaSuccess || !p) return FT_ERR_CUDA;
-            g_noalloc_ptr[dev] = p;
-        }
-        scratch = g_noalloc_ptr[dev];
-    }
+    NoallocDev D;
+    if (!noalloc_setup(dev, D)) return FT_ERR_CUDA;
     ft_path_desc d;
     memset(&d, 0, sizeof(d));
     d.n_ops = n_ops;
@@ -2411,15 +2460,15 @@ extern "C" FT_API int ft_fill_noalloc(int32_t rule, const ft_op* ops, uint32_t n
     for (int i = 0; i < 6; i++) p.xf[i] = transform ? transform[i] : ident[i];
     const float t = tolerance > 0.01f ? tolerance : 0.01f;
     p.tol_sq = t * t;
-    int optin = 0;
-    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return FT_ERR_CUDA;
     const int wp = (int)((w + 3) & ~3u);
     int smem = std::max(ftk::RASTER_FIXED_SMEM + 16 * wp * 4, 40 * 1024);
-    smem = std::min(smem, optin - 1024);
+    smem = std::min(smem, D.smem_max);
     p.smem_bytes = smem;
-    if (cudaFuncSetAttribute(ftk::k_fill_noalloc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
-        return FT_ERR_CUDA;
-    ftk::k_fill_noalloc<<<1, ftk::BLOCK, smem, static_cast<cudaStream_t>(stream)>>>(p, d, static_cast<unsigned char*>(scratch),
-                                                                                 status);
-    return cudaGetLastError() == cudaSuccess ? FT_OK : FT_ERR_CUDA;
+    unsigned char* scratch = static_cast<unsigned char*>(D.scratch);
+    // the launch's own status: an error some earlier, unrelated call left in the runtime
+    // is neither consumed nor reported here
+    void* args[] = {&p, &d, &scratch, &status};
+    const cudaError_t e = cudaLaunchKernel(reinterpret_cast<const void*>(ftk::k_fill_noalloc), dim3(1),
+                                           dim3(ftk::BLOCK), args, (size_t)smem, static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? FT_OK : FT_ERR_CUDA;
 }

@@ -118,6 +118,7 @@ struct KParams {
     float tol_sq;
     int join;
     float miter_limit;
+    float miter_g;           // ft_miter_angle(miter_limit): the miter decision's threshold on |th/2|
     int rule;
     int fmt;
     int stroke;

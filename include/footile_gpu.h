@@ -153,11 +153,11 @@ FT_API int ft_stroke(ft_ctx* ctx, const ft_op* ops, uint32_t n_ops, int32_t fmt,
  * FT_HOST, Matte8 rasters in page-locked host memory mapped into the device's address
  * space (cudaHostAlloc, cudaHostRegister, a pinned torch tensor) are written in place
  * by the kernels — a Matte8 fill or stroke only writes, so nothing is copied in or out
- * — and page-locked, 16-byte aligned ops are read in place (FT_HOST_MAPPED=0 /
- * FT_HOST_MAPPED_OPS=0 in the environment switch either off).  Otherwise, with 64 MB of
- * rasters or more, paths whose ops and rasters lie in ascending order in the host
- * buffers are drawn in two chunks, the copies of one overlapping the drawing of the
- * other (FT_HOST_CHUNKS sets the count). */
+ * — and page-locked, 16-byte aligned ops are read in place (ft_tuning.host_mapped
+ * switches either off).  Otherwise, with 64 MB of rasters or more, paths whose ops and
+ * rasters lie in ascending order in the host buffers are drawn in two chunks, the
+ * copies of one overlapping the drawing of the other (ft_tuning.host_chunks sets the
+ * count). */
 FT_API int ft_fill_batch(ft_ctx* ctx, int32_t stroke, int32_t rule, const ft_op* ops,
                          uint32_t n_ops_total, const ft_path_desc* paths,
                          uint32_t n_paths, int32_t fmt, uint8_t* rasters,
@@ -197,15 +197,24 @@ FT_API void ft_batch_destroy(ft_batch* batch);
  * CTA rasteriser's shared memory, which sets its tile: bands of as many full-width rows
  * as fit (0 = built-in choice); `split_px`, paths of at least this many pixels are
  * split into row ranges, the queue grain of large paths (0 = 1 Mpx); `grid_per_sm`,
- * resident CTAs per SM of the persistent kernels (0 = occupancy maximum).  Results do
- * not depend on the tuning.  ft_set_tuning(ctx, NULL) restores the defaults.
- * Environment variables FT_WARP_MAX_SIDE, FT_SMEM_BYTES, FT_SPLIT_PX and FT_GRID
- * override both. */
+ * resident CTAs per SM of the persistent kernels (0 = occupancy maximum).
+ * Ordered composites (ft_composite_batch): `band_rows`, rows per band of the band
+ * compositor (1..8, 0 = built-in); `pool_edges`, the first size of the binned-edge pool
+ * in edges (it grows on demand; 0 = built-in).  Host batches (ft_fill_batch with
+ * FT_HOST): `host_chunks`, chunks of the copy pipeline (1..16, 0 = built-in: 2 from
+ * 64 MB of rasters); `host_mapped`, 0 = page-locked Matte8 rasters are written and
+ * page-locked ops read in place (built-in), 1 = rasters and ops are copied, 2 = rasters
+ * in place, ops copied.  Results do not depend on the tuning.  ft_set_tuning(ctx, NULL) restores the
+ * defaults; ft_get_tuning gives the values in effect (the defaults when none were set). */
 typedef struct ft_tuning {
     int32_t warp_max_side;
     int32_t cta_smem_bytes;
     int32_t split_px;
     int32_t grid_per_sm;
+    int32_t band_rows;
+    int32_t pool_edges;
+    int32_t host_chunks;
+    int32_t host_mapped;
 } ft_tuning;
 FT_API int ft_set_tuning(ft_ctx* ctx, const ft_tuning* tuning);
 FT_API int ft_get_tuning(ft_ctx* ctx, ft_tuning* tuning);
@@ -224,20 +233,31 @@ FT_API int ft_autotune_batch(ft_ctx* ctx, int32_t stroke, int32_t rule, const ft
                              const char* cache_path, ft_tuning* chosen, float* ms);
 
 /* Allocation-free fill of one path — this entry point has no counterpart in footile.
- * For callers that cannot allocate device memory: work recorded into a CUDA graph
- * while a stream is being captured, processes under a fixed device-memory budget,
- * or hosts whose device allocator belongs to another runtime.  It needs no
- * context and calls no allocator: the figure scratch (vertices, sub-figure starts
- * and edges of one figure, about 2.9 MB) is a file-scope device array that every
- * GPU which loads this library holds until the process exits.  All pointers are
- * device pointers; `ops` must be 16-byte aligned, Rgba8p rows 4-byte aligned.
- * `transform` may be NULL (identity); `status` (device int, may be NULL) receives
- * FT_OK, FT_ERR_DEPTH or FT_ERR_ARG.  The call is asynchronous on `stream`.  The
- * first call on each device looks up the array's device address; make that first
- * call before any stream capture.  Every call shares the one array, so calls that
- * overlap on the GPU race: serialise them on one stream.  Widths above
- * FT_MAX_WIDTH return FT_ERR_CAP; figures are capped at FT_MAX_POINTS vertices as
- * in footile, so every path fits the array. */
+ * It is for callers that may not allocate device memory, themselves or through this
+ * library: a host whose device memory belongs to another runtime's allocator (a game
+ * engine's or a language runtime's pool that has to account for every allocation),
+ * or a process held to a fixed device-memory budget.  It needs no context and calls
+ * no allocator: the figure scratch of the call (vertices, sub-figure starts and edges
+ * of one figure, about 2.9 MB) is a file-scope device array that every GPU which loads
+ * this library holds until the process exits.  The caller passes the inputs and the
+ * output; all pointers are device pointers; `ops` must be 16-byte aligned, Rgba8p rows
+ * 4-byte aligned.  `transform` may be NULL (identity); `status` (device int, may be
+ * NULL) receives FT_OK, FT_ERR_DEPTH or FT_ERR_ARG.  The call is asynchronous on
+ * `stream`; its return value is the launch's own status (an error that an earlier,
+ * unrelated CUDA call left behind is neither reported nor cleared).
+ *
+ * `pen_width` is the pen width at the start of the call (footile's Plotter state,
+ * plotter.rs:151-153).  Unlike ft_fill, which keeps the width a PenWidth op leaves for
+ * the next call in its context, this call has no context: a PenWidth op affects this
+ * call only, and the caller carries the width to its next call itself.
+ *
+ * The first call on each device (and the first after a device reset) looks up the
+ * array's device address and sets the kernel's shared-memory limit in the device's
+ * current context; make that first call before any stream capture.  Every call shares
+ * the one array, and each call leaves its figure there for the next call to overwrite:
+ * calls whose kernels overlap on the GPU race on it, so serialise them (one stream, or
+ * events between streams).  Widths above FT_MAX_WIDTH return FT_ERR_CAP; figures are
+ * capped at FT_MAX_POINTS vertices as in footile, so every path fits the array. */
 FT_API int ft_fill_noalloc(int32_t rule, const ft_op* ops, uint32_t n_ops, int32_t fmt,
                            const uint8_t clr[4], uint8_t* raster, uint32_t w, uint32_t h,
                            uint32_t stride, const float transform[6], float tolerance,

@@ -61,6 +61,8 @@ def lib():
             L.orc_stroke.restype = ctypes.c_int
             L.orc_stroke_outline.argtypes = [P, u32, ctypes.POINTER(Params), ctypes.c_float, P, u32]
             L.orc_stroke_outline.restype = u32
+            L.orc_join_decisions.argtypes = [P, u32, ctypes.POINTER(Params), ctypes.c_float, i32, P, P, u32]
+            L.orc_join_decisions.restype = u32
             L.orc_fig_points.argtypes = [P, u32, ctypes.POINTER(Params), P, u32]
             L.orc_fig_points.restype = u32
             L.orc_accumulate.argtypes = [i32, P, P, u32]
@@ -148,6 +150,23 @@ def stroke_outline(ops, s_width=1.0, **params):
                                      _ptr(out), cap)
         if n <= cap:
             return out[:n]
+        cap = n
+
+
+def join_decisions(ops, s_width=1.0, libm=False, with_uv=False, **params):
+    """The stroke outline's join decisions in order (0 bevel, 1 miter, 2 round arc), taken
+    by ft_fmath.h as a correctly rounded f32 libm takes them (libm=False, the CUDA path's
+    decisions) or with the C library's atan2f / sinf (libm=True).  with_uv: also the
+    joins' vectors u = a1 - a0, v = b0 - b1 as an (n, 4) f32 array."""
+    ops = np.ascontiguousarray(ops, dtype=_abi.OP_DTYPE)
+    cap = 1 << 16
+    while True:
+        out = np.zeros(cap, dtype=np.int8)
+        uv = np.zeros((cap, 4), dtype=np.float32) if with_uv else None
+        n = lib().orc_join_decisions(_ptr(ops), len(ops), ctypes.byref(make_params(**params)), s_width,
+                                     int(bool(libm)), _ptr(out), _ptr(uv) if with_uv else None, cap)
+        if n <= cap:
+            return (out[:n], uv[:n]) if with_uv else out[:n]
         cap = n
 
 

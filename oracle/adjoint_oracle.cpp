@@ -441,13 +441,6 @@ static inline F2 f2norm(F2 v) {
     float m = sqrtf(v.x * v.x + v.y * v.y);
     return F2{v.x / m, v.y / m};
 }
-static inline float f2angle_rel(F2 a, F2 b) {
-    float th = ft_atan2f(a.y, a.x) - ft_atan2f(b.y, b.x);
-    const float PI = 3.14159265358979323846f;
-    if (th < -PI) return th + 2.0f * PI;
-    if (th > PI) return th - 2.0f * PI;
-    return th;
-}
 static inline bool f2line_x(F2 a0, F2 a1, F2 b0, F2 b1, F2* out) {
     float x1 = a0.x, y1 = a0.y, x2 = a1.x, y2 = a1.y, x3 = b0.x, y3 = b0.y, x4 = b1.x, y4 = b1.y;
     float den = (x1 - x2) * (y3 - y4) - (y1 - y2) * (x3 - x4);
@@ -647,12 +640,11 @@ static StrokeFig build_stroke(const ft_op* ops, uint32_t n, const float* m, floa
     auto do_join = [&](int k, int a0, int a1, int b0, int b1) {
         F2 A0 = S.nodes[a0].f, A1 = S.nodes[a1].f, B0 = S.nodes[b0].f, B1 = S.nodes[b1].f;
         if (join == FT_JOIN_MITER) {
-            if (ml > 0.0f) {
-                float sm_min = 1.0f / ml;
-                float th = f2angle_rel(f2sub(A1, A0), f2sub(B0, B1));
-                float sm = fabsf(ft_sinf(th / 2.0f));
+            // footile's decision as a correctly rounded f32 libm takes it (ft_fmath.h)
+            const F2 u = f2sub(A1, A0), v = f2sub(B0, B1);
+            {
                 F2 xp;
-                if (sm >= sm_min && sm < 1.0f && f2line_x(A0, A1, B0, B1, &xp)) {
+                if (ft_miter_join(u.x, u.y, v.x, v.y, ft_miter_angle(ml)) && f2line_x(A0, A1, B0, B1, &xp)) {
                     S.nodes.push_back(SNode{N_MITER, a0, a1, b0, b1, xp});
                     emit((int)S.nodes.size() - 1);
                     return;
@@ -664,8 +656,8 @@ static StrokeFig build_stroke(const ft_op* ops, uint32_t n, const float* m, floa
             emit(a1);
             emit(b0);
         } else {
-            float th = f2angle_rel(f2sub(A1, A0), f2sub(B0, B1));
-            if (th <= 0.0f) {
+            const F2 u = f2sub(A1, A0), v = f2sub(B0, B1);
+            if (!ft_round_join_arc(u.x, u.y, v.x, v.y)) {
                 emit(a1);
                 emit(b0);
             } else {

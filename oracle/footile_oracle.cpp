@@ -6,7 +6,7 @@
 // it, and nothing in it runs on the GPU.
 //
 // It follows the reference structure line by line (file:line of footile 0.7):
-//   fixed.rs:65-199   Fixed 16.16 arithmetic, release-mode wrapping
+//   fixed.rs:24-158   Fixed 16.16 arithmetic, release-mode wrapping
 //   vid.rs:9-70       Vid(u16) vertex ids and the 65,535-vertex cap
 //   geom.rs:8-35      WidePt, float_lerp, midpoint
 //   plotter.rs:96-365 Plotter state, add_ops/add_op, quad/cubic De Casteljau
@@ -52,20 +52,20 @@ static const i32 FX_EPS = 1;
 
 static inline i32 wadd(i32 a, i32 b) { return (i32)((u32)a + (u32)b); }
 static inline i32 wsub(i32 a, i32 b) { return (i32)((u32)a - (u32)b); }
-// fixed.rs:81-88  (a as i64 * b as i64) >> 16, as i32
+// fixed.rs:40-47  (a as i64 * b as i64) >> 16, as i32
 static inline i32 fx_mul(i32 a, i32 b) { return (i32)(u32)(((i64)a * (i64)b) >> FRACT_BITS); }
-// fixed.rs:90-97  ((a as i64) << 16) / b as i64, as i32
+// fixed.rs:49-56  ((a as i64) << 16) / b as i64, as i32
 static inline i32 fx_div(i32 a, i32 b) { return (i32)(u32)(((i64)a * 65536) / (i64)b); }
 static inline i32 fx_shl(i32 a, u32 s) { return (i32)((u32)a << s); }
-static inline i32 fx_floor(i32 v) { return v & ~FRACT_MASK; }                 // fixed.rs:167-170
-static inline i32 fx_ceil(i32 v) { return fx_floor(wsub(wadd(v, FX_ONE), FX_EPS)); }  // :172-175
-static inline i32 fx_round(i32 v) { return fx_floor(wadd(v, FX_HALF)); }      // :177-180
-static inline i32 fx_trunc(i32 v) { return v >= 0 ? fx_floor(v) : fx_ceil(v); }  // :182-189
-static inline i32 fx_fract(i32 v) { return v & FRACT_MASK; }                  // :191-194
-static inline i32 fx_avg(i32 a, i32 b) { return wadd(a, b) >> 1; }           // :196-199
-static inline i32 fx_abs(i32 v) { return v == INT32_MIN ? INT32_MIN : (v < 0 ? -v : v); }  // :162-165 (wraps)
-static inline i32 fx_to_int(i32 v) { return v >> FRACT_BITS; }                // :122-127
-static inline i32 fx_from_int(i32 i) { return fx_shl(i, FRACT_BITS); }        // :115-120
+static inline i32 fx_floor(i32 v) { return v & ~FRACT_MASK; }                 // fixed.rs:126-129
+static inline i32 fx_ceil(i32 v) { return fx_floor(wsub(wadd(v, FX_ONE), FX_EPS)); }  // :131-134
+static inline i32 fx_round(i32 v) { return fx_floor(wadd(v, FX_HALF)); }      // :136-139
+static inline i32 fx_trunc(i32 v) { return v >= 0 ? fx_floor(v) : fx_ceil(v); }  // :141-148
+static inline i32 fx_fract(i32 v) { return v & FRACT_MASK; }                  // :150-153
+static inline i32 fx_avg(i32 a, i32 b) { return wadd(a, b) >> 1; }           // :155-158
+static inline i32 fx_abs(i32 v) { return v == INT32_MIN ? INT32_MIN : (v < 0 ? -v : v); }  // :121-124 (wraps)
+static inline i32 fx_to_int(i32 v) { return v >> FRACT_BITS; }                // :81-86
+static inline i32 fx_from_int(i32 i) { return fx_shl(i, FRACT_BITS); }        // :74-79
 // Rust `f32 as i32`: truncate toward zero, saturate, NaN -> 0.
 static inline i32 rust_f32_as_i32(float f) {
     if (f != f) return 0;
@@ -73,7 +73,7 @@ static inline i32 rust_f32_as_i32(float f) {
     if (f <= -2147483648.0f) return INT32_MIN;
     return (i32)f;
 }
-// fixed.rs:129-134  Fixed((f * 65536.0) as i32)
+// fixed.rs:88-93  Fixed((f * 65536.0) as i32)
 static inline i32 fx_from_f32(float f) {
     volatile float m = f * 65536.0f;
     return rust_f32_as_i32(m);
@@ -98,8 +98,22 @@ static inline Pt pnormalize(Pt v) {
     float m = sqrtf(v.x * v.x + v.y * v.y);
     return pt(v.x / m, v.y / m);
 }
+// Trig of the join decisions: 0 = the shared ft_fmath.h functions (the ones the CUDA path
+// uses), 1 = the C library's atan2f / sinf, for the test that counts the decisions the
+// two would take differently (orc_join_decisions).  Recorded decisions go to the log.
+static thread_local int g_trig_libm = 0;
+static thread_local std::vector<int8_t>* g_join_log = nullptr;
+static thread_local std::vector<float>* g_join_uv = nullptr;  // the vectors u = a1 - a0, v = b0 - b1 of each join
+static inline float trig_atan2f(float y, float x) { return g_trig_libm ? atan2f(y, x) : ft_atan2f(y, x); }
+static inline float trig_sinf(float x) { return g_trig_libm ? sinf(x) : ft_sinf(x); }
+static inline void log_join(int d) {
+    if (g_join_log) g_join_log->push_back((int8_t)d);
+}
+static inline void log_join_uv(float ux, float uy, float vx, float vy) {
+    if (g_join_uv) g_join_uv->insert(g_join_uv->end(), {ux, uy, vx, vy});
+}
 static inline float pangle_rel(Pt a, Pt b) {
-    float th = ft_atan2f(a.y, a.x) - ft_atan2f(b.y, b.x);
+    float th = trig_atan2f(a.y, a.x) - trig_atan2f(b.y, b.x);
     const float PI = 3.14159265358979323846f;
     if (th < -PI) return th + 2.0f * PI;
     if (th > PI) return th - 2.0f * PI;
@@ -519,12 +533,14 @@ struct SubStroke {  // stroker.rs:31-97
 struct Stroke : PlotDest {
     int join;
     float miter_limit;
+    float miter_g;  // ft_miter_angle(miter_limit)
     float tol_sq;
     std::vector<WidePt> points;
     std::vector<SubStroke> subs;
     int* status;
 
-    Stroke(int j, float ml, float tsq, int* st) : join(j), miter_limit(ml), tol_sq(tsq), status(st) {
+    Stroke(int j, float ml, float tsq, int* st)
+        : join(j), miter_limit(ml), miter_g(ft_miter_angle(ml)), tol_sq(tsq), status(st) {
         points.reserve(1024);
         subs.push_back(SubStroke{0, 0, false, false});
     }
@@ -619,20 +635,28 @@ struct Stroke : PlotDest {
         else
             stroke_round(ops, p, a0, a1, b0, b1);
     }
-    // stroker.rs:340-367
+    // stroker.rs:340-367.  The decision sm >= 1/ml && sm < 1 is taken as a correctly
+    // rounded f32 libm takes it (ft_fmath.h: the CUDA path's function); the test mode
+    // g_trig_libm takes it with the C library's atan2f / sinf instead.
+    bool miter_decision(Pt u, Pt v, float ml) const {
+        if (!g_trig_libm) return ft_miter_join(u.x, u.y, v.x, v.y, miter_g);
+        if (!(ml > 0.0f)) return false;
+        float sm_min = 1.0f / ml;
+        float th = pangle_rel(u, v);
+        float sm = fabsf(trig_sinf(th / 2.0f));
+        return sm >= sm_min && sm < 1.0f;
+    }
     void stroke_miter(std::vector<ft_op>& ops, Pt a0, Pt a1, Pt b0, Pt b1, float ml) const {
-        if (ml > 0.0f) {
-            float sm_min = 1.0f / ml;
-            float th = pangle_rel(psub(a1, a0), psub(b0, b1));
-            float sm = fabsf(ft_sinf(th / 2.0f));
-            if (sm >= sm_min && sm < 1.0f) {
-                Pt xp;
-                if (pline_intersection(a0, a1, b0, b1, &xp)) {
-                    stroke_point(ops, xp);
-                    return;
-                }
+        log_join_uv(a1.x - a0.x, a1.y - a0.y, b0.x - b1.x, b0.y - b1.y);
+        if (miter_decision(psub(a1, a0), psub(b0, b1), ml)) {
+            Pt xp;
+            if (pline_intersection(a0, a1, b0, b1, &xp)) {
+                log_join(1);
+                stroke_point(ops, xp);
+                return;
             }
         }
+        log_join(0);
         stroke_bevel(ops, a1, b0);
     }
     static void stroke_bevel(std::vector<ft_op>& ops, Pt a1, Pt b0) {
@@ -641,8 +665,11 @@ struct Stroke : PlotDest {
     }
     // stroker.rs:380-396
     void stroke_round(std::vector<ft_op>& ops, WidePt p, Pt a0, Pt a1, Pt b0, Pt b1) const {
-        float th = pangle_rel(psub(a1, a0), psub(b0, b1));
-        if (th <= 0.0f) {
+        const Pt u = psub(a1, a0), v = psub(b0, b1);
+        log_join_uv(u.x, u.y, v.x, v.y);
+        const bool arc = g_trig_libm ? !(pangle_rel(u, v) <= 0.0f) : ft_round_join_arc(u.x, u.y, v.x, v.y);
+        log_join(arc ? 2 : 0);
+        if (!arc) {
             stroke_bevel(ops, a1, b0);
         } else {
             stroke_point(ops, a1);
@@ -867,6 +894,41 @@ __attribute__((visibility("default"))) uint32_t orc_stroke_outline(const ft_op* 
     st.path_ops(outline);
     for (uint32_t i = 0; i < outline.size() && i < cap; i++) out[i] = outline[i];
     return (uint32_t)outline.size();
+}
+
+// The join decisions of the stroke outline of `ops` (stroker.rs:340-396), one byte per
+// join in outline order: 0 bevel, 1 miter, 2 round arc.  `libm` 0 takes the angle and
+// the miter sine from ft_fmath.h (as the CUDA path does), 1 from the C library's
+// atan2f / sinf — the functions Rust's f32::atan2 / f32::sin call — so a test can count
+// the joins whose decision depends on which is used.  Returns the number of joins (may
+// exceed `cap`).  With `uv` (4 floats per join, may be NULL), the join's vectors
+// u = a1 - a0 and v = b0 - b1 (th = angle_rel(u, v)).
+__attribute__((visibility("default"))) uint32_t orc_join_decisions(const ft_op* ops, uint32_t n_ops,
+                                                                   const orc_params* prm, float s_width, int32_t libm,
+                                                                   int8_t* out, float* uv, uint32_t cap) {
+    uint8_t dummy = 0;
+    orc::Raster r{&dummy, 1, 1, 1, FT_MATTE8};
+    float tol = prm ? prm->tolerance : 0.3f;
+    const float* m = prm ? prm->transform : ORC_IDENTITY;
+    orc::Plotter p(r, tol, m, prm ? prm->join : FT_JOIN_MITER, prm ? prm->miter_limit : 4.0f, s_width);
+    orc::Stroke st(p.join, p.miter_limit, p.tol_sq, &p.status);
+    p.add_ops(ops, n_ops, st);
+    std::vector<ft_op> outline;
+    std::vector<int8_t> log;
+    std::vector<float> uvs;
+    orc::g_trig_libm = libm ? 1 : 0;
+    orc::g_join_log = &log;
+    orc::g_join_uv = uv ? &uvs : nullptr;
+    st.path_ops(outline);
+    orc::g_join_log = nullptr;
+    orc::g_join_uv = nullptr;
+    orc::g_trig_libm = 0;
+    for (uint32_t i = 0; i < log.size() && i < cap; i++) {
+        out[i] = log[i];
+        if (uv)
+            for (int k = 0; k < 4; k++) uv[4 * i + k] = uvs[4 * i + k];
+    }
+    return (uint32_t)log.size();
 }
 
 // Fixed vertices of the figure footile fills for `ops` (after Fig::close): for tests

@@ -12,6 +12,8 @@ def fig_ops(points):
 
 
 def new_raster(w, h, fmt, fill=0):
+    if isinstance(fill, np.ndarray):
+        return fill.copy()
     if fmt == _abi.MATTE8:
         return np.full((h, w), fill, np.uint8)
     return np.full((h, w, 4), fill, np.uint8)
@@ -32,7 +34,8 @@ def assert_same(got, want, what=""):
 
 def gpu_vs_oracle(ctx, ops, w, h, fmt=_abi.MATTE8, rule=_abi.NONZERO, clr=(0, 0, 0, 0), init=0, stroke=False,
                   tolerance=0.3, transform=_abi.IDENTITY, join=_abi.JOIN_MITER, miter_limit=4.0, s_width=1.0):
-    """Draw `ops` with the oracle and with the GPU (host-mode C ABI call)."""
+    """Draw `ops` with the oracle and with the GPU (host-mode C ABI call).  `init` is
+    the initial byte of every raster byte, or a whole initial raster (copied)."""
     from footile_gb300.plotter import Plotter
     want = new_raster(w, h, fmt, init)
     params = dict(tolerance=tolerance, transform=transform, join=join, miter_limit=miter_limit)

@@ -23,8 +23,8 @@ def _compare_paths(got, want, paths, which):
 
 @pytest.mark.parametrize("warp", ["512", "0"])
 @pytest.mark.parametrize("rule", [_abi.NONZERO, _abi.EVENODD])
-def test_glyph_batch_host(ctx, rule, warp, monkeypatch):
-    monkeypatch.setenv("FT_WARP_MAX_SIDE", warp)
+def test_glyph_batch_host(ctx, rule, warp):
+    ctx.tune(warp_max_side=int(warp))
     ops, paths, nbytes = workloads.glyphs(3000, seed=31)
     want = np.zeros(nbytes, np.uint8)
     st_o = oracle.fill_batch(0, rule, ops, paths, _abi.MATTE8, want, n_threads=8)
@@ -35,11 +35,20 @@ def test_glyph_batch_host(ctx, rule, warp, monkeypatch):
         _compare_paths(got, want, paths, range(len(paths)))
 
 
+def _mismatching_paths(got, want, paths):
+    """Indices of the paths whose raster bytes differ (rasters back to back)."""
+    bad = np.flatnonzero(got != want)
+    if len(bad) == 0:
+        return np.zeros(0, np.int64)
+    return np.unique(np.searchsorted(paths["raster_offset"].astype(np.int64), bad, side="right") - 1)
+
+
 def test_glyph_batch_device_full_size(ctx):
-    """The full 65,536-path glyph workload on the device; 1,500 random paths checked
-    bit-exact, and every path checked for the property that rows above its top
-    vertex keep their initial value."""
+    """The full 65,536-path glyph workload of the benchmark, on the device: every path's
+    mask bit-exact against the oracle (rows above a path's top vertex keep the initial
+    byte on both sides)."""
     torch = pytest.importorskip("torch")
+    import os
     ops, paths, nbytes = workloads.glyphs_65536()
     init = 0x5A
     ops_d = torch.from_numpy(ops.view(np.uint8)).cuda()
@@ -47,12 +56,34 @@ def test_glyph_batch_device_full_size(ctx):
     st = fill_batch(ctx, ops_d, paths, _abi.MATTE8, ras_d)
     assert (st == 0).all()
     got = ras_d.cpu().numpy()
-    rng = np.random.default_rng(5)
-    which = np.sort(rng.choice(len(paths), 1500, replace=False))
     want = np.full(nbytes, init, np.uint8)
-    sub = paths[which].copy()
-    oracle.fill_batch(0, _abi.NONZERO, ops, sub, _abi.MATTE8, want, n_threads=8)
-    _compare_paths(got, want, paths, which)
+    st_o = oracle.fill_batch(0, _abi.NONZERO, ops, paths, _abi.MATTE8, want, n_threads=os.cpu_count() or 8)
+    assert (st_o == 0).all()
+    bad = _mismatching_paths(got, want, paths)
+    if len(bad):
+        _compare_paths(got, want, paths, bad[:1])
+    assert len(bad) == 0, f"{len(bad)} of {len(paths)} paths differ"
+
+
+def test_glyph_batch_prepared_full_size(ctx):
+    """The benchmark's timed object: a prepared batch (CUDA graph replay) of the
+    65,536 glyphs, launched twice onto the same rasters; every mask bit-exact."""
+    torch = pytest.importorskip("torch")
+    import os
+    from footile_gb300.plotter import PreparedBatch
+    ops, paths, nbytes = workloads.glyphs_65536()
+    ops_d = torch.from_numpy(ops.view(np.uint8)).cuda()
+    ras_d = torch.zeros(nbytes, dtype=torch.uint8, device="cuda")
+    b = PreparedBatch(ctx, paths, _abi.MATTE8)
+    b.launch(ops_d, ras_d)
+    b.launch(ops_d, ras_d)
+    assert (b.status() == 0).all()
+    b.close()
+    got = ras_d.cpu().numpy()
+    want = np.zeros(nbytes, np.uint8)
+    oracle.fill_batch(0, _abi.NONZERO, ops, paths, _abi.MATTE8, want, n_threads=os.cpu_count() or 8)
+    bad = _mismatching_paths(got, want, paths)
+    assert len(bad) == 0, f"{len(bad)} of {len(paths)} paths differ"
 
 
 def test_batch_rgba_regions(ctx):

@@ -48,8 +48,8 @@ def test_composite_rgba(ctx, stroke, seed):
 
 
 @pytest.mark.parametrize("band_rows", ["1", "3", "8"])
-def test_composite_band_heights(ctx, band_rows, monkeypatch):
-    monkeypatch.setenv("FT_BAND_ROWS", band_rows)
+def test_composite_band_heights(ctx, band_rows):
+    ctx.tune(band_rows=int(band_rows))
     ops, paths, init = _scene(7, 30, 97, 61, True)
     want = init.copy()
     oracle.composite(1, _abi.NONZERO, ops, paths, _abi.RGBA8P, want)
@@ -69,9 +69,9 @@ def test_composite_matte8_evenodd(ctx):
     assert_same(got, want, "matte8 even-odd")
 
 
-def test_composite_pool_grows(ctx, monkeypatch):
+def test_composite_pool_grows(ctx):
     # a tiny first edge pool forces the build to overflow and run again
-    monkeypatch.setenv("FT_POOL_EDGES", "500")
+    ctx.tune(pool_edges=500)
     ops, paths, init = _scene(11, 24, 150, 110, True)
     want = init.copy()
     oracle.composite(1, _abi.NONZERO, ops, paths, _abi.RGBA8P, want)
@@ -93,3 +93,32 @@ def test_composite_device_buffers(ctx):
     ras_d = torch.from_numpy(init).cuda()
     composite_batch(ctx, ops_d, paths, _abi.RGBA8P, ras_d, stroke=True)
     assert_same(ras_d.cpu().numpy(), want, "device composite")
+
+
+@pytest.mark.parametrize("init_kind", ["zero", "random"])
+def test_strokes_16384_prefix_full_canvas(ctx, init_kind):
+    """The benchmark's ordered stroke composite at full canvas size: the first 1,024 of
+    the 16,384 strokes (8..64 cubics, width 1..12, Miter(4), alpha 64..255) drawn in
+    order onto the 2048x2048 Rgba8p canvas, against the oracle's Plotter::stroke calls
+    one after another (the oracle composites every pixel from each call's top row down:
+    about 24 s on one core).  A random initial canvas also exercises the alpha-0
+    composites of every call."""
+    torch = pytest.importorskip("torch")
+    from footile_gb300.plotter import pen_width_chain
+    k = 1024
+    paths_ops, _, clrs, side = workloads.strokes_16384()
+    ops, paths, _ = pack_batch(paths_ops[:k], [side] * k, _abi.RGBA8P, clrs[:k])
+    paths["s_width"], _ = pen_width_chain(ops, paths, 1.0)
+    if init_kind == "zero":
+        init = np.zeros((side, side, 4), np.uint8)
+    else:
+        init = np.random.default_rng(6).integers(0, 256, (side, side, 4)).astype(np.uint8)
+    want = init.copy()
+    st_o, _ = oracle.composite(1, _abi.NONZERO, ops, paths, _abi.RGBA8P, want, s_width=1.0,
+                               join=_abi.JOIN_MITER, miter_limit=4.0)
+    ctx.set_join(_abi.JOIN_MITER, 4.0)
+    ops_d = torch.from_numpy(ops.view(np.uint8)).cuda()
+    ras_d = torch.from_numpy(init).cuda()
+    st = composite_batch(ctx, ops_d, paths, _abi.RGBA8P, ras_d, stroke=True)
+    assert (st == st_o).all()
+    assert_same(ras_d.cpu().numpy(), want, f"{k} strokes on {side}x{side} ({init_kind} canvas)")

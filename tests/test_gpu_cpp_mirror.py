@@ -15,12 +15,22 @@ pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def test_cpp_mirror_fishy(cuda_ok, gpu_lib, tmp_path):
+def _cuda_lib_dir():
+    nvcc = _build.nvcc()
+    return os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc))), "lib64")
+
+
+@pytest.mark.parametrize("link", ["shared", "static"])
+def test_cpp_mirror_fishy(cuda_ok, gpu_lib, tmp_path, link):
     exe = tmp_path / "fishy_demo"
     lib_dir = os.path.dirname(_build.LIB)
-    subprocess.check_call(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
-                           os.path.join(ROOT, "tests", "cpp", "fishy_demo.cpp"), "-o", str(exe),
-                           "-L", lib_dir, "-lfootile_gpu", f"-Wl,-rpath,{lib_dir}"])
+    src = [os.path.join(ROOT, "tests", "cpp", "fishy_demo.cpp")]
+    if link == "shared":
+        libs = ["-L", lib_dir, "-lfootile_gpu", f"-Wl,-rpath,{lib_dir}"]
+    else:  # the static library, as a Rust crate's build.rs would link it
+        libs = [_build.STATIC_LIB, "-L", _cuda_lib_dir(), "-lcudart_static", "-ldl", "-lpthread", "-lrt"]
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include")] + src +
+                          ["-o", str(exe)] + libs)
     out = subprocess.run([str(exe), str(tmp_path / "rgba.bin"), str(tmp_path / "matte.bin")],
                          capture_output=True, text=True)
     assert out.returncode == 0, out.stderr

@@ -4,7 +4,7 @@ Known answers from footile's tests (src/fig.rs:691-794), seeded random paths, an
 the quirks of the reference: the 65,535-vertex cap (fig.rs:428-442), the shift
 of figures whose top row is negative (fig.rs:496-499), the Matte8 overwrite of
 every row from the top row down (fig.rs:629-636), wrapping Fixed arithmetic
-(fixed.rs:81-97, fig.rs:116-119) and the close-pop of a vertex equal to the
+(fixed.rs:40-56, fig.rs:116-119) and the close-pop of a vertex equal to the
 sub-figure start (fig.rs:373-383).
 """
 import numpy as np
@@ -22,11 +22,12 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.fixture(params=["warp", "cta"])
-def rasteriser(request, monkeypatch):
-    """Small canvases go to the warp rasteriser by default; FT_WARP_MAX_SIDE=0
-    sends every path to the CTA rasteriser, so both kernels are checked."""
+def rasteriser(request, ctx):
+    """Small canvases go to the warp rasteriser by default; a tuning with
+    warp_max_side 0 sends every path to the CTA rasteriser, so both kernels are
+    checked."""
     if request.param == "cta":
-        monkeypatch.setenv("FT_WARP_MAX_SIDE", "0")
+        ctx.tune(warp_max_side=0)
     return request.param
 
 
@@ -236,3 +237,24 @@ def test_warp_overflow_hands_path_to_cta(ctx):
     st = fill_batch(ctx, ops, paths, _abi.MATTE8, got)
     assert (st == 0).all()
     assert_same(got, want, "overflow batch")
+
+
+@pytest.mark.parametrize("init_kind", ["zero", "random"])
+@pytest.mark.parametrize("stroke", [False, True])
+def test_scene_4096_rgba8p(ctx, stroke, init_kind):
+    """The benchmark's 4096x4096 scene composited onto Rgba8p: the NonZero fill, and the
+    stroke at width 8 with round joins, each bit-exact against the oracle; on the
+    benchmark's zeroed canvas and on random bytes (where every call's alpha-0 SrcOver
+    from its top row down changes the destination)."""
+    from footile_gb300.path import PathOp, ops_array
+    ops, w, h, clr = workloads.scene_4096()
+    init = 0 if init_kind == "zero" else np.random.default_rng(2).integers(0, 256, (h, w, 4)).astype(np.uint8)
+    if stroke:
+        ops = np.concatenate([ops_array([PathOp.PenWidth(8.0)]), ops])
+        got, want, st_o, _, err = gpu_vs_oracle(ctx, ops, w, h, fmt=_abi.RGBA8P, clr=tuple(int(c) for c in clr),
+                                                init=init, stroke=True, join=_abi.JOIN_ROUND, miter_limit=0.0)
+    else:
+        got, want, st_o, _, err = gpu_vs_oracle(ctx, ops, w, h, fmt=_abi.RGBA8P, clr=tuple(int(c) for c in clr),
+                                                init=init)
+    assert err is None and st_o == 0
+    assert_same(got, want, f"scene Rgba8p stroke={stroke} ({init_kind} canvas)")

@@ -3,8 +3,6 @@ drawn and copied out on overlapping streams) give the same masks and statuses as
 device path and the oracle, and fall back to one pass when the layout does not allow it.
 Matte8 rasters in page-locked host memory are written in place by the kernels; the rows
 a figure does not reach keep the caller's bytes."""
-import os
-
 import numpy as np
 import pytest
 
@@ -16,23 +14,16 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.fixture
-def chunks():
-    old = os.environ.get("FT_HOST_CHUNKS")
-    yield lambda k: os.environ.__setitem__("FT_HOST_CHUNKS", str(k))
-    if old is None:
-        os.environ.pop("FT_HOST_CHUNKS", None)
-    else:
-        os.environ["FT_HOST_CHUNKS"] = old
+def chunks(ctx):
+    """Force the copy pipeline's chunk count (ft_tuning.host_chunks)."""
+    return lambda k: ctx.tune(host_chunks=int(k))
 
 
 @pytest.fixture
-def mapped_env():
-    old = os.environ.get("FT_HOST_MAPPED")
-    yield lambda v: os.environ.__setitem__("FT_HOST_MAPPED", str(v))
-    if old is None:
-        os.environ.pop("FT_HOST_MAPPED", None)
-    else:
-        os.environ["FT_HOST_MAPPED"] = old
+def mapped_env(ctx):
+    """0: page-locked host buffers used in place; 1: rasters copied; 2: ops copied too
+    (ft_tuning.host_mapped)."""
+    return lambda v: ctx.tune(host_mapped=int(v))
 
 
 @pytest.mark.parametrize("stroke", [False, True])
@@ -52,7 +43,7 @@ def test_mapped_host_rasters(ctx, mapped_env, stroke):
     ok[int(p["raster_offset"]):int(p["raster_offset"]) + int(p["height"]) * int(p["stride"])] = False
     assert np.array_equal(got[ok], want[ok])
     # the copy path (mapping off) writes the same bytes
-    mapped_env(0)
+    mapped_env(1)
     pinned2 = torch.from_numpy(init.copy()).pin_memory()
     got2 = pinned2.numpy()
     st2 = fill_batch(ctx, ops, paths, _abi.MATTE8, got2, stroke=stroke)

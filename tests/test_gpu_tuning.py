@@ -44,8 +44,6 @@ def test_bad_tuning_rejected(ctx):
 
 def test_autotune_and_cache(ctx, tmp_path):
     torch = pytest.importorskip("torch")
-    if any(k in os.environ for k in ("FT_WARP_MAX_SIDE", "FT_SMEM_BYTES", "FT_SPLIT_PX", "FT_GRID")):
-        pytest.skip("plan knobs overridden by the environment")
     ops, paths, nbytes = small_glyphs(2000)
     ops_d = torch.from_numpy(ops.view(np.uint8)).cuda()
     ras_d = torch.zeros(nbytes, dtype=torch.uint8, device="cuda")
@@ -54,7 +52,7 @@ def test_autotune_and_cache(ctx, tmp_path):
     t, ms = ctx.autotune(ops_d, paths, _abi.MATTE8, ras_d, cache_path=cache)
     assert ms > 0 and ctx.tuning() == t
     line = open(cache).read().split()
-    assert len(line) == 6 and [int(v) for v in line[1:5]] == list(t.values())
+    assert len(line) == 10 and [int(v) for v in line[1:9]] == list(t.values())
     # the tuned plan draws the same bytes
     b = PreparedBatch(ctx, paths, _abi.MATTE8)
     ras_d.zero_()

@@ -1,8 +1,8 @@
 """The oracle against every known-answer test footile holds for this path.
 
-footile's own tests (Rust #[test]s) pin Fixed arithmetic (src/fixed.rs:207-354),
+footile's own tests (Rust #[test]s) pin Fixed arithmetic (src/fixed.rs:166-313),
 the figure rasteriser from fixed vertices to Matte8 / Rgba8p bytes
-(src/fig.rs:691-794) and the row resolve (src/imgbuf.rs:622-649).  Each is
+(src/fig.rs:691-794) and the row resolve (src/imgbuf.rs:205-232).  Each is
 restated here with the same inputs and expected values.  CPU only.
 """
 import math
@@ -22,8 +22,8 @@ def op(o, a, b=0):
     return oracle.fx_op(o, F(a) if not isinstance(a, np.int32) else a, F(b) if not isinstance(b, int) else b)
 
 
-# ---------------------------------------------------------------- fixed.rs:207-354
-def test_fixed_add():  # fixed.rs:207-215
+# ---------------------------------------------------------------- fixed.rs:166-313
+def test_fixed_add():  # fixed.rs:166-174
     assert oracle.fx_op(ADD, F(1), F(1)) == F(2)
     assert oracle.fx_op(ADD, F(2), F(2)) == F(4)
     assert oracle.fx_op(ADD, F(2), F(-2)) == F(0)
@@ -32,7 +32,7 @@ def test_fixed_add():  # fixed.rs:207-215
     assert oracle.fx_op(ADD, F(3.5), F(-1.25)) == F(2.25)
 
 
-def test_fixed_sub():  # fixed.rs:217-225
+def test_fixed_sub():  # fixed.rs:176-184
     assert oracle.fx_op(SUB, F(1), F(1)) == F(0)
     assert oracle.fx_op(SUB, F(3), F(2)) == F(1)
     assert oracle.fx_op(SUB, F(2), F(-2)) == F(4)
@@ -41,7 +41,7 @@ def test_fixed_sub():  # fixed.rs:217-225
     assert oracle.fx_op(SUB, F(3.5), F(1.25)) == F(2.25)
 
 
-def test_fixed_mul():  # fixed.rs:227-235
+def test_fixed_mul():  # fixed.rs:186-194
     assert oracle.fx_op(MUL, F(2), F(2)) == F(4)
     assert oracle.fx_op(MUL, F(3), F(-2)) == F(-6)
     assert oracle.fx_op(MUL, F(4), F(0.5)) == F(2)
@@ -50,7 +50,7 @@ def test_fixed_mul():  # fixed.rs:227-235
     assert oracle.fx_op(MUL, F(128), F(128)) == F(16384)
 
 
-def test_fixed_div():  # fixed.rs:237-246
+def test_fixed_div():  # fixed.rs:196-205
     assert oracle.fx_op(DIV, F(4), F(2)) == F(2)
     assert oracle.fx_op(DIV, F(-6), F(2)) == F(-3)
     assert oracle.fx_op(DIV, F(2), F(0.5)) == F(4)
@@ -60,7 +60,7 @@ def test_fixed_div():  # fixed.rs:237-246
     assert oracle.fx_op(DIV, F(16384), F(128)) == F(128)
 
 
-def test_fixed_shl():  # fixed.rs:248-255
+def test_fixed_shl():  # fixed.rs:207-214
     assert oracle.fx_op(SHL, F(0), 2) == F(0)
     assert oracle.fx_op(SHL, F(1), 1) == F(2)
     assert oracle.fx_op(SHL, F(0.5), 1) == F(1)
@@ -68,7 +68,7 @@ def test_fixed_shl():  # fixed.rs:248-255
     assert oracle.fx_op(SHL, F(0.125), 3) == F(1)
 
 
-def test_fixed_shr():  # fixed.rs:257-264
+def test_fixed_shr():  # fixed.rs:216-223
     assert oracle.fx_op(SHR, F(0), 2) == F(0)
     assert oracle.fx_op(SHR, F(1), 1) == F(0.5)
     assert oracle.fx_op(SHR, F(2), 1) == F(1)
@@ -77,38 +77,38 @@ def test_fixed_shr():  # fixed.rs:257-264
 
 
 @pytest.mark.parametrize("a,want", [(1, 1), (500, 500), (-500, 500), (-1.5, 1.5), (-2.5, 2.5)])
-def test_fixed_abs(a, want):  # fixed.rs:266-273
+def test_fixed_abs(a, want):  # fixed.rs:225-232
     assert oracle.fx_op(ABS, F(a)) == F(want)
 
 
 @pytest.mark.parametrize("a,want", [(1, 1), (500, 500), (1.5, 1), (1.99999, 1), (-0.0001, -1), (-2.5, -3)])
-def test_fixed_floor(a, want):  # fixed.rs:275-283
+def test_fixed_floor(a, want):  # fixed.rs:234-242
     assert oracle.fx_op(FLOOR, F(a)) == F(want)
 
 
 @pytest.mark.parametrize("a,want", [(1, 1), (500, 500), (1.5, 2), (1.99999, 2), (-0.0001, 0), (-2.5, -2)])
-def test_fixed_ceil(a, want):  # fixed.rs:285-293
+def test_fixed_ceil(a, want):  # fixed.rs:244-252
     assert oracle.fx_op(CEIL, F(a)) == F(want)
 
 
 @pytest.mark.parametrize("a,want", [(1, 1), (500, 500), (1.5, 2), (1.49999, 1), (1.99999, 2), (-0.0001, 0),
                                     (-2.5, -2), (-2.9, -3)])
-def test_fixed_round(a, want):  # fixed.rs:295-305
+def test_fixed_round(a, want):  # fixed.rs:254-264
     assert oracle.fx_op(ROUND, F(a)) == F(want)
 
 
 @pytest.mark.parametrize("a,want", [(1, 1), (500, 500), (1.5, 1), (1.49999, 1), (1.99999, 1), (-0.0001, 0),
                                     (-2.5, -2), (-2.9, -2)])
-def test_fixed_trunc(a, want):  # fixed.rs:307-317
+def test_fixed_trunc(a, want):  # fixed.rs:266-276
     assert oracle.fx_op(TRUNC, F(a)) == F(want)
 
 
 @pytest.mark.parametrize("a,want", [(0, 0), (0.1, 0.1), (0.9, 0.9), (1.5, 0.5), (-2.5, 0.5)])
-def test_fixed_fract(a, want):  # fixed.rs:319-326
+def test_fixed_fract(a, want):  # fixed.rs:278-285
     assert oracle.fx_op(FRACT, F(a)) == F(want)
 
 
-def test_fixed_avg():  # fixed.rs:328-335
+def test_fixed_avg():  # fixed.rs:287-294
     assert oracle.fx_op(AVG, F(1), F(2)) == F(1.5)
     assert oracle.fx_op(AVG, F(1), F(1)) == F(1)
     assert oracle.fx_op(AVG, F(5), F(-5)) == F(0)
@@ -116,13 +116,13 @@ def test_fixed_avg():  # fixed.rs:328-335
     assert oracle.fx_op(AVG, F(3), F(1.5)) == F(2.25)
 
 
-def test_fixed_into():  # fixed.rs:337-345
+def test_fixed_into():  # fixed.rs:296-304
     assert oracle.fx_to_int(F(37)) == 37
     assert oracle.fx_to_f32(F(2.5)) == 2.5
     assert oracle.fx_to_int(F(2.5)) == 2
 
 
-def test_fixed_cmp():  # fixed.rs:347-354
+def test_fixed_cmp():  # fixed.rs:306-313
     assert F(37) > F(3)
     assert F(3) < F(37)
     assert F(-4) < F(4)
@@ -183,14 +183,14 @@ def test_fig_3x3_rgba8p():  # fig.rs:702-721
 
 
 # ------------------------------------------------------------------- imgbuf.rs
-def test_imgbuf_non_zero():  # imgbuf.rs:622-638
+def test_imgbuf_non_zero():  # imgbuf.rs:205-221
     d, s = oracle.accumulate(_abi.NONZERO, [200] + [0] * 2999)
     assert (d == 200).all() and (s == 0).all()
     d, s = oracle.accumulate(_abi.NONZERO, [300] + [0] * 4999)
     assert (d == 255).all()
 
 
-def test_imgbuf_even_odd():  # imgbuf.rs:640-649
+def test_imgbuf_even_odd():  # imgbuf.rs:223-232
     d, _ = oracle.accumulate(_abi.EVENODD, [300] + [0] * 2999)
     assert (d == 212).all()
 
