@@ -52,6 +52,7 @@ def load(auto_build=True):
             "ft_sync": ([P], ctypes.c_int),
             "ft_last_error": ([P], ctypes.c_char_p),
             "ft_last_timings": ([P, ctypes.POINTER(f32)], ctypes.c_int),
+            "ft_last_composite_ms": ([P, ctypes.POINTER(f32)], ctypes.c_int),
             "ft_launch_count": ([P], u64),
             "ft_batch_create": ([P, i32, i32, P, u32, i32, ctypes.POINTER(P)], ctypes.c_int),
             "ft_batch_launch": ([P, P, P, u32, P, u64], ctypes.c_int),
@@ -89,7 +90,7 @@ def exported_symbols():
     return [n for n in (
         "ft_ctx_create", "ft_ctx_destroy", "ft_set_stream", "ft_set_tolerance", "ft_set_transform",
         "ft_set_join", "ft_set_pen_width", "ft_get_pen_width", "ft_fill", "ft_stroke", "ft_fill_batch",
-        "ft_batch_status", "ft_sync", "ft_last_error", "ft_last_timings", "ft_launch_count",
+        "ft_batch_status", "ft_sync", "ft_last_error", "ft_last_timings", "ft_last_composite_ms", "ft_launch_count",
         "ft_batch_create", "ft_batch_launch", "ft_batch_launch_status", "ft_batch_destroy",
         "ft_composite_batch", "ft_fill_noalloc", "ft_adjoint_forward", "ft_adjoint_backward", "ft_adjoint_status",
         "ft_adjoint_destroy", "ft_set_tuning", "ft_get_tuning", "ft_autotune_batch",
@@ -102,7 +103,8 @@ class Tuning(ctypes.Structure):
     """`ft_tuning`: the knobs of a batch plan (see include/footile_gpu.h)."""
     _fields_ = [("warp_max_side", ctypes.c_int32), ("cta_smem_bytes", ctypes.c_int32),
                 ("split_px", ctypes.c_int32), ("grid_per_sm", ctypes.c_int32), ("band_rows", ctypes.c_int32),
-                ("pool_edges", ctypes.c_int32), ("host_chunks", ctypes.c_int32), ("host_mapped", ctypes.c_int32)]
+                ("pool_edges", ctypes.c_int32), ("host_chunks", ctypes.c_int32), ("host_mapped", ctypes.c_int32),
+                ("tile_w", ctypes.c_int32)]
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}
@@ -186,6 +188,12 @@ class Context:
     def last_ms(self):
         v = ctypes.c_float()
         self.check(self.L.ft_last_timings(self.h, ctypes.byref(v)))
+        return v.value
+
+    def last_composite_ms(self):
+        """Device time of the last call's Rgba8p tile compositor alone (0 if it did not run)."""
+        v = ctypes.c_float()
+        self.check(self.L.ft_last_composite_ms(self.h, ctypes.byref(v)))
         return v.value
 
     def launch_count(self):

@@ -6,6 +6,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -80,13 +81,15 @@ struct ft_ctx {
     std::vector<cudaEvent_t> ev_chunk;               // copied in / drawn, per chunk
     uint32_t last_n_paths = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev_comp = nullptr;  // before the tile compositor of the last call
+    bool comp_timed = false;        // the last call ran the tile compositor (ev_comp .. ev1)
 
     bool timed = false;
     uint64_t launches = 0;
     int sm_count = 0;
     int max_smem = 0;
     uint32_t fig_cap = 0;  // vertices per figure of a fill above footile's 65,535 (0: footile's cap)
-    ft_tuning tune{0, 0, 0, 0, 0, 0, 0, 0};
+    ft_tuning tune{0, 0, 0, 0, 0, 0, 0, 0, 0};
     bool tuned = false;  // `tune` replaces the built-in plan defaults
     std::string err;
 };
@@ -325,6 +328,7 @@ int run_plan(ft_ctx* c, PlanSlot& slot, int stroke, int rule, const ft_op* ops_d
     p.sw_out = sw_out;
     p.sw_chain = sw_chain;
     p.scratch = static_cast<unsigned char*>(c->scratch.p);
+    c->comp_timed = false;
     if (events) FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
     FT_CU(enqueue(p, grid, grid_w, smem, c->stream, &c->launches, c->sm_count), "launch rasteriser");
     if (events) {
@@ -535,6 +539,7 @@ FT_API int ft_batch_launch(ft_ctx* c, ft_batch* b, const ft_op* ops, uint32_t n_
     b->params.rasters = rasters;
     if (c->stream == nullptr || c->stream == cudaStreamLegacy || c->stream == cudaStreamPerThread) {
         // the legacy and per-thread default streams cannot be captured: launch directly
+        c->comp_timed = false;
         FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
         FT_CU(cudaMemsetAsync(b->queue.p, 0, 256, c->stream), "reset queue");
         FT_CU(cudaMemsetAsync(b->status.p, 0, sizeof(int32_t) * std::max(b->n_paths, 1u), c->stream), "reset status");
@@ -566,6 +571,7 @@ FT_API int ft_batch_launch(ft_ctx* c, ft_batch* b, const ft_op* ops, uint32_t n_
         b->g_ras = rasters;
         b->g_stream = c->stream;
     }
+    c->comp_timed = false;
     FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
     FT_CU(cudaGraphLaunch(b->exec, c->stream), "launch batch graph");
     FT_CU(cudaEventRecord(c->ev1, c->stream), "event");
@@ -593,14 +599,15 @@ FT_API void ft_batch_destroy(ft_batch* b) {
 FT_API int ft_set_tuning(ft_ctx* c, const ft_tuning* t) {
     if (!c) return FT_ERR_ARG;
     if (!t) {
-        c->tune = ft_tuning{0, 0, 0, 0, 0, 0, 0, 0};
+        c->tune = ft_tuning{0, 0, 0, 0, 0, 0, 0, 0, 0};
         c->tuned = false;
         return FT_OK;
     }
     if (t->warp_max_side < 0 || t->warp_max_side > ftk::WARP_MAX_SIDE || t->cta_smem_bytes < 0 ||
         (t->cta_smem_bytes && t->cta_smem_bytes < 40 * 1024) || t->cta_smem_bytes > c->max_smem ||
         t->split_px < 0 || t->grid_per_sm < 0 || t->band_rows < 0 || t->band_rows > ftk::NWARP ||
-        t->pool_edges < 0 || t->host_chunks < 0 || t->host_chunks > 16 || t->host_mapped < 0 || t->host_mapped > 2)
+        t->pool_edges < 0 || t->host_chunks < 0 || t->host_chunks > 16 || t->host_mapped < 0 || t->host_mapped > 2 ||
+        (t->tile_w != 0 && t->tile_w != 128 && t->tile_w != 256 && t->tile_w != 512 && t->tile_w != 1024))
         return fail(c, FT_ERR_ARG, "tuning out of range");
     c->tune = *t;
     c->tuned = true;
@@ -612,7 +619,7 @@ FT_API int ft_get_tuning(ft_ctx* c, ft_tuning* t) {
     if (c->tuned) {
         *t = c->tune;
     } else {
-        *t = ft_tuning{ftk::WARP_MAX_SIDE, 0, 1 << 20, 0, 0, 0, 0, 0};
+        *t = ft_tuning{ftk::WARP_MAX_SIDE, 0, 1 << 20, 0, 0, 0, 0, 0, 0};
     }
     return FT_OK;
 }
@@ -626,6 +633,7 @@ FT_API int ft_ctx_create(int device, ft_ctx** out) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev_comp);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
     if (e != cudaSuccess) {
         delete c;
@@ -652,6 +660,7 @@ FT_API void ft_ctx_destroy(ft_ctx* c) {
                       &c->srgb_lut, &c->conv_src, &c->conv_dst, &c->figbins};
     for (DevBuf* b : bufs) b->release();
     if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev_comp) cudaEventDestroy(c->ev_comp);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -795,6 +804,7 @@ static int run_pipelined(ft_ctx* c, int stroke, int rule, const ft_op* ops, uint
     }
     for (int k = 0; k < n_chunks; k++) {
         FT_CU(cudaStreamWaitEvent(c->stream, ev[1 + k], 0), "wait");
+        c->comp_timed = false;
         if (k == 0) FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
         int st = run_plan(c, *c->chunk_plans[k], stroke, rule, ops_d, paths + pb[k], pb[k + 1] - pb[k], fmt, ras_d,
                           nullptr, nullptr, st_d + pb[k], false);
@@ -920,12 +930,47 @@ FT_API int ft_fill_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* o
 }
 
 // Rows per band of the ordered composite = warps of a compositor CTA (one row each):
-// as many as the shared memory holds, at most eight.
-static int composite_band_rows(ft_ctx* c, uint32_t w, uint32_t h) {
-    (void)h;
+// at most eight; the Matte8 compositor keeps whole rows, so as many as its shared memory
+// holds.
+static int composite_band_rows(ft_ctx* c, uint32_t w, int fmt) {
     int R = (c->tuned && c->tune.band_rows > 0) ? std::min((int)c->tune.band_rows, ftk::NWARP) : ftk::NWARP;
-    while (R > 1 && ftk::composite_bands_smem(R, (int)w) > c->max_smem) R--;
+    if (fmt == FT_MATTE8)
+        while (R > 1 && ftk::composite_bands_smem(R, (int)w) > c->max_smem) R--;
     return R;
+}
+
+// Width of an Rgba8p compositor tile (pixels).
+static int composite_tile_w(const ft_ctx* c) { return (c->tuned && c->tune.tile_w > 0) ? c->tune.tile_w : 512; }
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// A 2-D tensor map of an Rgba8p canvas (u32 pixels, rows `stride` bytes apart) with boxes
+// of box_w x box_h pixels, through the runtime's driver entry point; false when the
+// canvas does not allow one (TMA wants a 16-byte aligned base and row stride).
+static bool canvas_tensor_map(CUtensorMap* tm, void* base, uint32_t w, uint32_t h, uint32_t stride, int box_w,
+                              int box_h) {
+    static EncodeTiledFn encode = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            encode = reinterpret_cast<EncodeTiledFn>(f);
+    });
+    if (!encode || !base || !w || !h || (reinterpret_cast<uintptr_t>(base) & 15) || (stride & 15) ||
+        (uint64_t)stride >= (1ull << 40))
+        return false;
+    const cuuint64_t dims[2] = {w, h};
+    const cuuint64_t strides[1] = {stride};
+    const cuuint32_t box[2] = {(cuuint32_t)box_w, (cuuint32_t)box_h};
+    const cuuint32_t elem[2] = {1, 1};
+    return encode(tm, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, base, dims, strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 FT_API int ft_composite_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* ops, uint32_t n_ops_total,
@@ -972,9 +1017,10 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
     } else if ((reinterpret_cast<uintptr_t>(ops) & 15) || (fmt == FT_RGBA8P && (reinterpret_cast<uintptr_t>(raster) & 3))) {
         return fail(c, FT_ERR_ARG, "device ops need 16-byte alignment, Rgba8p rasters 4-byte alignment");
     }
-    const int R = composite_band_rows(c, w, h);
+    const int R = composite_band_rows(c, w, fmt);
     const int n_bands = (int)((h + R - 1) / R);
-    const int smem_b = ftk::composite_bands_smem(R, (int)w);
+    const int tile_w = composite_tile_w(c);
+    const int smem_b = fmt == FT_MATTE8 ? ftk::composite_bands_smem(R, (int)w) : ftk::composite_tile_smem(R, tile_w);
     if (smem_b > c->max_smem) return fail(c, FT_ERR_CAP, "raster too wide for the band compositor");
     const int smem_a = choose_smem(c, 1);
     if ((size_t)(n_bands + 1) * sizeof(int) > (size_t)smem_a)
@@ -1039,6 +1085,7 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
             p.fig_state = static_cast<int4*>(c->figbins.p);
             p.bin_hist = reinterpret_cast<int*>(static_cast<char*>(c->figbins.p) + 16);
         }
+        c->comp_timed = false;
         FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
         if (n_paths) {
             FT_CU(ftk::launch_composite_build(p, grid, smem_a, c->stream, grid <= c->sm_count),
@@ -1057,7 +1104,17 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
             continue;
         }
         if (n_paths && n_bands) {
-            FT_CU(ftk::launch_composite_bands(p, smem_b, c->stream), "launch band compositor");
+            if (fmt == FT_MATTE8) {
+                FT_CU(ftk::launch_composite_bands(p, smem_b, c->stream), "launch band compositor");
+            } else {
+                CUtensorMap tm;
+                memset(&tm, 0, sizeof(tm));
+                p.seg_w = tile_w;
+                p.use_tma = canvas_tensor_map(&tm, ras_d, w, h, stride, std::min(tile_w, 256), R) ? 1 : 0;
+                FT_CU(cudaEventRecord(c->ev_comp, c->stream), "event");
+                FT_CU(ftk::launch_composite_tiles(p, tm, c->stream), "launch tile compositor");
+                c->comp_timed = true;
+            }
             c->launches++;
         }
         FT_CU(cudaEventRecord(c->ev1, c->stream), "event");
@@ -1130,9 +1187,9 @@ static bool tune_lookup(const char* path, const std::string& key, ft_tuning* t) 
         char k[600];
         ft_tuning v;
         float ms;
-        v = ft_tuning{0, 0, 0, 0, 0, 0, 0, 0};
-        if (sscanf(line, "%599s %d %d %d %d %d %d %d %d %f", k, &v.warp_max_side, &v.cta_smem_bytes, &v.split_px,
-                   &v.grid_per_sm, &v.band_rows, &v.pool_edges, &v.host_chunks, &v.host_mapped, &ms) == 10 &&
+        v = ft_tuning{0, 0, 0, 0, 0, 0, 0, 0, 0};
+        if (sscanf(line, "%599s %d %d %d %d %d %d %d %d %d %f", k, &v.warp_max_side, &v.cta_smem_bytes, &v.split_px,
+                   &v.grid_per_sm, &v.band_rows, &v.pool_edges, &v.host_chunks, &v.host_mapped, &v.tile_w, &ms) == 11 &&
             key == k) {
             *t = v;  // the last entry for a key wins
             found = true;
@@ -1246,6 +1303,7 @@ static int adjoint_forward_dev(ft_ctx* c, ft_adjoint* a, int stroke, int rule, c
               "upload paths");
     FT_CU(cudaMemsetAsync(a->status.p, 0, sizeof(int32_t) * std::max(n_paths, 1u), c->stream), "reset status");
     fta::AParams p = adjoint_params(a);
+    c->comp_timed = false;
     if (events) FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
     if (n_paths) {
         FT_CU(fta::launch_adjoint(false, p, a->grid_f, c->stream), "launch adjoint forward");
@@ -1267,6 +1325,7 @@ static int adjoint_backward_dev(ft_ctx* c, ft_adjoint* a, const float* gcov_d, f
     p.grad_cov = gcov_d;
     p.grad_ops = gops_d;
     p.grad_width = gw_d;
+    c->comp_timed = false;
     if (events) FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
     if (a->n_paths) {
         FT_CU(fta::launch_adjoint(true, p, a->grid_b, c->stream), "launch adjoint backward");
@@ -1423,6 +1482,7 @@ FT_API int ft_convert(ft_ctx* c, int32_t src_fmt, const uint8_t* src, uint32_t s
     const uint64_t work = (row / 16 + row % 16) * h;
     const int grid = (int)std::max<uint64_t>(
         1, std::min<uint64_t>((work + 255) / 256, (uint64_t)c->sm_count * ftc::convert_blocks_per_sm()));
+    c->comp_timed = false;
     FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
     FT_CU(ftc::launch_convert(src_fmt, s_d, src_stride, d_d, dst_stride, w, h,
                               static_cast<const uint8_t*>(c->srgb_lut.p), grid, c->stream),
@@ -1451,6 +1511,7 @@ static int srcover_call(ft_ctx* c, bool backward, const float* cov, uint32_t n_l
     if (v4 & 15) return fail(c, FT_ERR_ARG, "colour and canvas buffers need 16-byte alignment");
     FT_CU(cudaSetDevice(c->device), "set device");
     const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((n_px + 255) / 256, (uint64_t)c->sm_count * 16));
+    c->comp_timed = false;
     FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
     FT_CU(ftc::launch_srcover(backward, cov, n_layers, plane, reinterpret_cast<const float4*>(clr),
                               reinterpret_cast<const float4*>(init), reinterpret_cast<float4*>(out),
@@ -1587,6 +1648,7 @@ FT_API int ft_stroke_composite_forward(ft_ctx* c, const ft_op* ops, uint32_t n_o
     else
         FT_CU(cudaMemsetAsync(s->prefix.p, 0, 16ull * n_px, c->stream), "clear initial canvas");
     const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((n_px + 255) / 256, (uint64_t)c->sm_count * 16));
+    c->comp_timed = false;
     FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
     for (uint32_t ch = 0; ch < s->n_chunks; ch++) {
         int st = composite_cover(c, s, ch);
@@ -1646,6 +1708,7 @@ FT_API int ft_stroke_composite_backward(ft_ctx* c, ft_composite_adjoint* s, cons
     if (gops_bytes) FT_CU(cudaMemsetAsync(gops_d, 0, gops_bytes, c->stream), "reset op gradient");
     if (s->n_paths) FT_CU(cudaMemsetAsync(gw_d, 0, 4ull * s->n_paths, c->stream), "reset width gradient");
     const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((n_px + 255) / 256, (uint64_t)c->sm_count * 16));
+    c->comp_timed = false;
     FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
     for (uint32_t ch = s->n_chunks; ch-- > 0;) {
         if (s->fresh != (int)ch) {  // recompute this chunk's coverage
@@ -1709,7 +1772,7 @@ FT_API int ft_autotune_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_o
     }
     if (ms_out) *ms_out = 0.0f;
     const std::string key = tune_key(c, stroke, rule, fmt, paths, n_paths);
-    ft_tuning best{0, 0, 0, 0, 0, 0, 0, 0};
+    ft_tuning best{0, 0, 0, 0, 0, 0, 0, 0, 0};
     if (tune_lookup(cache_path, key, &best) && ft_set_tuning(c, &best) == FT_OK) {
         if (chosen) *chosen = best;
         return FT_OK;
@@ -1732,7 +1795,7 @@ FT_API int ft_autotune_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_o
                 if (sm > c->max_smem) continue;
                 // the batch plan's knobs; the composite and host-transfer knobs stay as set
                 c->tune = ft_tuning{ws, sm, 1 << 20, gp, saved.band_rows, saved.pool_edges, saved.host_chunks,
-                                    saved.host_mapped};
+                                    saved.host_mapped, saved.tile_w};
                 c->tuned = true;
                 ft_batch* b = nullptr;
                 if (ft_batch_create(c, stroke, rule, paths, n_paths, fmt, &b) != FT_OK) continue;
@@ -1766,9 +1829,9 @@ FT_API int ft_autotune_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_o
     if (cache_path) {
         FILE* f = fopen(cache_path, "a");
         if (f) {
-            fprintf(f, "%s %d %d %d %d %d %d %d %d %.4f\n", key.c_str(), best.warp_max_side, best.cta_smem_bytes,
+            fprintf(f, "%s %d %d %d %d %d %d %d %d %d %.4f\n", key.c_str(), best.warp_max_side, best.cta_smem_bytes,
                     best.split_px, best.grid_per_sm, best.band_rows, best.pool_edges, best.host_chunks,
-                    best.host_mapped, best_ms);
+                    best.host_mapped, best.tile_w, best_ms);
             fclose(f);
         }
     }
@@ -1803,6 +1866,15 @@ FT_API int ft_last_timings(ft_ctx* c, float* kernel_ms) {
     if (!c->timed) return FT_OK;
     FT_CU(cudaEventSynchronize(c->ev1), "event sync");
     FT_CU(cudaEventElapsedTime(kernel_ms, c->ev0, c->ev1), "event time");
+    return FT_OK;
+}
+
+FT_API int ft_last_composite_ms(ft_ctx* c, float* ms) {
+    if (!c || !ms) return FT_ERR_ARG;
+    *ms = 0.f;
+    if (!c->timed || !c->comp_timed) return FT_OK;
+    FT_CU(cudaEventSynchronize(c->ev1), "event sync");
+    FT_CU(cudaEventElapsedTime(ms, c->ev_comp, c->ev1), "event time");
     return FT_OK;
 }
 

@@ -34,6 +34,8 @@
 #include <cstdio>
 #include <cstring>
 
+#include <cuda.h>
+
 #include "ft_device.cuh"
 #include "ft_kernels.cuh"
 
@@ -2022,9 +2024,10 @@ __device__ __forceinline__ unsigned ftab4(const unsigned char* ftab, unsigned d,
 
 constexpr int FTAB_BYTES = 16 * 256;  // ftab[k][d]: d after k alpha-0 SrcOver composites
 
-// Per-warp shared memory of the band compositor for rows of `width` pixels.
+// Per-warp shared memory of the Matte8 band compositor for rows of `width` pixels: the
+// row's i32 cell areas and its touched-span marks.
 __host__ __device__ constexpr int row_smem_bytes(int width) {
-    return (int)align256((size_t)((width + 3) & ~3) * (4 + 2) + (size_t)(((width + 127) / 128 + 31) / 32) * 4);
+    return (int)align256((size_t)((width + 3) & ~3) * 4 + (size_t)(((width + 127) / 128 + 31) / 32) * 4);
 }
 
 // Accumulate the cells of the `ne` band edges that cross scan row y into `row`
@@ -2037,25 +2040,15 @@ __device__ __forceinline__ void row_items(const EdgeRec* edges, int ne, int y, i
     }
 }
 
-// Resolve one row and write it: Matte8 overwrites every pixel; Rgba8p composites
-// the covered pixels after their pending alpha-0 maps (see above).  Spans that no
-// cell touched keep the running sum, so when that sum resolves to alpha 0 the
-// whole span is skipped.  Clears the row buffer and the span marks.
-__device__ __forceinline__ void composite_row(int* row, unsigned short* last, unsigned* spans, int W, int Wp,
-                                              uint8_t* drow, int rule, bool rgba, unsigned clr, int G,
-                                              const unsigned char* ftab, bool skip_spans) {
+// Resolve one Matte8 row (imgbuf.rs:38-199) and overwrite every pixel of it
+// (fig.rs:629-636).  Clears the row buffer and the span marks.
+__device__ __forceinline__ void matte_row(int* row, unsigned* spans, int W, int Wp, uint8_t* drow, int rule) {
     const int lane = threadIdx.x & 31;
-    // Rgba8p rows on a 16-byte boundary: a lane's four pixels are read and written as
-    // one 16-byte access (one load latency per span instead of four)
-    const bool vec = rgba && (reinterpret_cast<uintptr_t>(drow) & 15) == 0;
     unsigned carry = 0;
     for (int x0 = 0; x0 < W; x0 += 128) {
-        const int sp = x0 >> 7;
-        const bool touched = (spans[sp >> 5] >> (sp & 31)) & 1u;
-        if (skip_spans && !touched && resolve_cov(carry, rule) == 0) continue;
         const int x = x0 + lane * 4;
         int4 a = make_int4(0, 0, 0, 0);
-        if (touched && x < Wp) {
+        if (x < Wp) {
             a = *reinterpret_cast<const int4*>(row + x);
             *reinterpret_cast<int4*>(row + x) = make_int4(0, 0, 0, 0);
         }
@@ -2065,38 +2058,9 @@ __device__ __forceinline__ void composite_row(int* row, unsigned short* last, un
         carry += __shfl_sync(FULL, inc, 31);
         const unsigned av[4] = {resolve_cov(s0 + ex, rule), resolve_cov(s1 + ex, rule), resolve_cov(s2 + ex, rule),
                                 resolve_cov(s3 + ex, rule)};
-        if (vec && x + 3 < W) {
-            if (av[0] | av[1] | av[2] | av[3]) {
-                uint4* dp4 = reinterpret_cast<uint4*>(reinterpret_cast<unsigned*>(drow) + x);
-                const uint4 d = *dp4;
-                unsigned dv[4] = {d.x, d.y, d.z, d.w};
 #pragma unroll
-                for (int c = 0; c < 4; c++) {
-                    if (!av[c]) continue;  // this pixel keeps its bytes
-                    const int kk = min(G - (int)last[x + c], 15);
-                    if (kk) dv[c] = ftab4(ftab, dv[c], kk);
-                    dv[c] = srcover_rgba(dv[c], clr, av[c]);
-                    last[x + c] = (unsigned short)(G + 1);
-                }
-                *dp4 = make_uint4(dv[0], dv[1], dv[2], dv[3]);
-            }
-            continue;
-        }
-#pragma unroll
-        for (int c = 0; c < 4; c++) {
-            const int xc = x + c;
-            if (xc >= W) break;
-            if (!rgba) {
-                drow[xc] = (uint8_t)av[c];  // Matte8 rows are overwritten (fig.rs:629-636)
-            } else if (av[c]) {
-                unsigned* dp = reinterpret_cast<unsigned*>(drow) + xc;
-                unsigned dv = *dp;
-                const int kk = min(G - (int)last[xc], 15);
-                if (kk) dv = ftab4(ftab, dv, kk);
-                *dp = srcover_rgba(dv, clr, av[c]);
-                last[xc] = (unsigned short)(G + 1);
-            }
-        }
+        for (int c = 0; c < 4; c++)
+            if (x + c < W) drow[x + c] = (uint8_t)av[c];
     }
     __syncwarp();
     const int n_words = ((W + 127) / 128 + 31) / 32;
@@ -2104,99 +2068,363 @@ __device__ __forceinline__ void composite_row(int* row, unsigned short* last, un
     __syncwarp();
 }
 
-// One CTA per band of P.band_rows rows (32 threads per row), one warp per row.  Each warp
-// walks the calls in order with warp-level steps only (no block barriers after set-up).
+// Matte8 ordered composite: every call overwrites its rows from its top row down
+// (fig.rs:629-636), so a raster row shows only the last call that reaches it.  One CTA per
+// band of P.band_rows rows, one warp per row: the warp finds that call and draws it.
 __global__ void __launch_bounds__(BLOCK) k_cbands(KParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int W = (int)P.canvas_w, H = (int)P.canvas_h, Wp = (W + 3) & ~3;
     const int R = P.band_rows, nb = P.n_bands, b = blockIdx.x;
     const int r = b * R + warp;  // this warp's raster row
+    if (warp >= R || r >= H) return;
+    unsigned char* mine = smem + (size_t)warp * row_smem_bytes(W);
+    int* row = reinterpret_cast<int*>(mine);
+    unsigned* spans = reinterpret_cast<unsigned*>(row + Wp);
+    const int n_words = ((W + 127) / 128 + 31) / 32;
+    for (int x = lane * 4; x < Wp; x += 128) *reinterpret_cast<int4*>(row + x) = make_int4(0, 0, 0, 0);
+    for (int k = lane; k < n_words; k += 32) spans[k] = 0;
+    __syncwarp();
+    uint8_t* drow = P.rasters + (size_t)r * P.canvas_stride;
+    const int n = (int)P.n_items;
+    int found = -1;
+    for (int c1 = n; c1 > 0 && found < 0; c1 -= 32) {
+        const int i = c1 - 32 + lane;
+        const bool hit = i >= 0 && P.crec[i].x <= r;
+        const unsigned m = __ballot_sync(FULL, hit);
+        if (m) found = c1 - 32 + 31 - __clz(m);
+    }
+    if (found < 0) return;
+    const int4 cr = P.crec[found];
+    const int* boff = P.bandoff + (size_t)found * (nb + 1);
+    const int o0 = boff[b], o1 = boff[b + 1];
+    const unsigned long long first = ((unsigned long long)(unsigned)cr.z | ((unsigned long long)(unsigned)cr.w << 32)) + o0;
+    row_items(P.pool + first, o1 - o0, r + cr.y, row, W, spans);
+    __syncwarp();
+    matte_row(row, spans, W, Wp, drow, P.rule);
+}
+
+// ===========================================================================
+// Rgba8p ordered composite on tiles (ft_composite_batch, and single large calls).
+//
+// One CTA per tile of R band rows x `seg_w` pixels; one warp per tile row.  The tile's
+// canvas pixels are staged in shared memory for the whole call sequence: loaded by TMA
+// (cp.async.bulk.tensor.2d, boxes of at most 256 pixels x R rows, completion on an
+// mbarrier) when the canvas allows a tensor map, stored back by TMA at the end.  Each
+// warp walks the calls in order.  For a call, every band edge crossing the row gives its
+// cells inside the segment (into a shared i32 segment row, atomics) and, from the closed
+// form of the cell walk, the running sum it leaves to the left of the segment (the carry
+// into the segment: the cumulative cell sum through column c of an (edge, row) item is
+// min(pixel_cov(min(first + (c - minp) * step, ONE)), cov), fig.rs:285-321).  The warp then resolves the touched spans, compacts the covered pixels
+// (alpha > 0) into a queue and composites them 32 at a time, one pixel per lane; the
+// alpha-0 SrcOver footile applies to every other pixel from the call's top row down is
+// applied lazily, as a pending count per pixel and a table of powers of the alpha-0 map
+// (the map changes only channel values 1..15 and settles after 15 applications).
+
+constexpr int CT_QN = 160;  // queued covered pixels per warp (one span of 128 + a partial round)
+
+struct CTileLayout {
+    int tile, mbar, area, last, queue, bytes;
+};
+__host__ __device__ inline CTileLayout ctile_layout(int R, int sw) {
+    CTileLayout L;
+    int o = FTAB_BYTES;
+    o = (o + 127) & ~127;
+    L.tile = o;  // R x sw canvas pixels, [box][row][box width]
+    o += R * sw * 4;
+    L.mbar = o;
+    o += 16;
+    L.area = o;  // per warp: sw i32 cell areas
+    o += R * sw * 4;
+    L.last = o;  // per warp: sw u16, calls so far at each pixel's last cover
+    o += R * sw * 2;
+    o = (o + 15) & ~15;
+    L.queue = o;  // per warp: CT_QN covered pixels (x << 8 | alpha)
+    o += R * CT_QN * 4;
+    L.bytes = o;
+    return L;
+}
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+
+// Bounded wait on an mbarrier phase; false when it did not complete.
+__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, unsigned parity) {
+    const unsigned a = smem_u32(mbar);
+    for (int it = 0; it < (1 << 24); it++) {
+        unsigned done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// Cells of one (edge, row) item inside the segment [s0, s0 + sw) of a raster row of W
+// pixels (fig.rs:238-321 restricted to the segment): the cells' growths go into `area`
+// (segment-relative), the cumulative sum the item leaves left of s0 into `carry`, and
+// the touched 128-pixel spans into `tmask`.  The arguments are scan_row's.
+__device__ __forceinline__ void seg_row(int x_bot, int inv, bool st, bool en, int fu, int fl, int step, int ed,
+                                        int* area, int s0, int sw, int W, unsigned& carry, unsigned& tmask) {
+    const int ccov = en ? pixel_cov(fl) : 256;
+    const int cov = st ? ccov - pixel_cov(fu) : ccov;
+    if (cov <= 0) return;
+    const int x0 = st ? wsub(x_bot, fxmul(inv, wsub(FX_ONE, fu))) : wsub(x_bot, inv);
+    const int x1 = en ? wsub(x_bot, fxmul(inv, fl ? FX_ONE - fl : 0)) : x_bot;
+    const int mnx = min(x0, x1), mxx = max(x0, x1);
+    const int minp = mnx >> 16, maxp = mxx >> 16;
+    if (minp >= W) return;
+    const int s1 = min(s0 + sw, W);
+    if (minp >= s1) return;  // right of the segment: nothing here, nothing carried in
+    const int full = cov << 8;
+    const int r = (minp == maxp) ? fxmul(wsub(FX_ONE, fxfract(fxavg(mxx, mnx))), full)
+                                 : fxmul(wsub(FX_ONE, fxfract(mnx)), FX_HALF);
+    const int first = fxmul(r, step);
+    // cumulative sum through cell minp + j: min(pixel_cov(min(first + j * step, ONE)), cov)
+    auto cum = [&](int j) {
+        const long long v = (long long)first + (long long)j * step;
+        return min(pixel_cov(v > FX_ONE ? FX_ONE : (int)v), cov);
+    };
+    int c = max(max(s0, minp), 0);
+    int prev = 0;
+    if (s0 > 0 && minp < s0) {
+        prev = cum(s0 - 1 - minp);
+        carry += (unsigned)(ed * prev);
+    }
+    if (prev >= cov) return;
+    long long xv = (long long)first + (long long)(c - minp) * step;
+    int x_cov = xv > FX_ONE ? FX_ONE : (int)xv;
+    for (; c < s1; c++) {
+        const int v = min(pixel_cov(x_cov), cov);
+        if (v != prev) {
+            atomicAdd(&area[c - s0], ed * (v - prev));
+            tmask |= 1u << ((c - s0) >> 7);
+        }
+        prev = v;
+        if (v >= cov) break;
+        x_cov = min(x_cov + step, FX_ONE);
+    }
+}
+
+__device__ __forceinline__ unsigned warp_sum_u(unsigned v) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+    return v;
+}
+
+__global__ void __launch_bounds__(BLOCK) k_ctile(KParams P, const __grid_constant__ CUtensorMap tmap) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int W = (int)P.canvas_w, H = (int)P.canvas_h, R = P.band_rows, nb = P.n_bands, sw = P.seg_w;
+    const int nseg = (W + sw - 1) / sw;
+    const int b = (int)blockIdx.x / nseg, x0 = ((int)blockIdx.x % nseg) * sw;
+    const int r = b * R + warp;
+    const CTileLayout L = ctile_layout(R, sw);
+    const int BW = sw < 256 ? sw : 256;  // TMA box width (pixels)
+    const int bw_shift = BW == 256 ? 8 : 7;
     unsigned char* ftab = smem;
+    unsigned* tile = reinterpret_cast<unsigned*>(smem + L.tile);
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + L.mbar);
+    int* area = reinterpret_cast<int*>(smem + L.area) + warp * sw;
+    unsigned short* last = reinterpret_cast<unsigned short*>(smem + L.last) + warp * sw;
+    unsigned* q = reinterpret_cast<unsigned*>(smem + L.queue) + warp * CT_QN;
+    // the tile pixel of this warp's row at segment position x
+    auto px = [&](int x) -> unsigned* {
+        return tile + (((x >> bw_shift) * R + warp) << bw_shift) + (x & (BW - 1));
+    };
+    const bool tma = P.use_tma != 0;
+    if (tma && threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (tma && threadIdx.x == 0) {
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)),
+                     "r"(R * sw * 4)
+                     : "memory");
+        for (int bx = 0; bx < sw / BW; bx++)
+            asm volatile(
+                "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, "
+                "%3}], [%4];" ::"r"(smem_u32(tile + bx * R * BW)),
+                "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(x0 + bx * BW), "r"(b * R), "r"(smem_u32(mbar))
+                : "memory");
+    }
     for (int i = threadIdx.x; i < FTAB_BYTES; i += blockDim.x) {
         unsigned v = (unsigned)(i & 255);
         for (int k = 0; k < (i >> 8); k++) v = ch8_mul(v, 255u);
         ftab[i] = (unsigned char)v;
     }
+    for (int x = lane * 4; x < sw; x += 128) *reinterpret_cast<int4*>(area + x) = make_int4(0, 0, 0, 0);
+    for (int x = lane; x < sw; x += 32) last[x] = 0;
+    unsigned* crow = reinterpret_cast<unsigned*>(P.rasters + (size_t)r * P.canvas_stride);
+    if (!tma && r < H)
+        for (int x = lane; x < sw && x0 + x < W; x += 32) *px(x) = crow[x0 + x];
+    bool ok = true;
+    if (tma) {
+        ok = mbar_wait(mbar, 0);
+        if (!ok && threadIdx.x == 0) atomicMax(&P.status[0], FT_ERR_TIMEOUT);
+    }
     __syncthreads();
-    if (warp >= R || r >= H) return;
-    unsigned char* mine = smem + FTAB_BYTES + (size_t)warp * row_smem_bytes(W);
-    int* row = reinterpret_cast<int*>(mine);
-    unsigned short* last = reinterpret_cast<unsigned short*>(row + Wp);
-    unsigned* spans = reinterpret_cast<unsigned*>(last + Wp);
-    const int n_words = ((W + 127) / 128 + 31) / 32;
-    for (int x = lane * 4; x < Wp; x += 128) *reinterpret_cast<int4*>(row + x) = make_int4(0, 0, 0, 0);
-    for (int x = lane; x < Wp; x += 32) last[x] = 0;
-    for (int k = lane; k < n_words; k += 32) spans[k] = 0;
-    __syncwarp();
-    uint8_t* drow = P.rasters + (size_t)r * P.canvas_stride;
-    const bool rgba = P.fmt == FT_RGBA8P;
-    const int n = (int)P.n_items;
-    // a call's record: band edge range, scan-row offset and colour
-    struct Call {
-        unsigned long long first;  // pool index of the call's first edge in this band
-        int ne, tmin;
-        unsigned clr;
-    };
-    auto fetch = [&](int i) {
-        Call c;
-        const int4 cr = P.crec[i];
-        const int* boff = P.bandoff + (size_t)i * (nb + 1);
-        const int o0 = boff[b], o1 = boff[b + 1];
-        c.first = ((unsigned long long)(unsigned)cr.z | ((unsigned long long)(unsigned)cr.w << 32)) + o0;
-        c.ne = o1 - o0;
-        c.tmin = cr.y;
-        const ft_path_desc& d = P.paths[i];
-        c.clr = (unsigned)d.clr[0] | ((unsigned)d.clr[1] << 8) | ((unsigned)d.clr[2] << 16) |
-                ((unsigned)d.clr[3] << 24);
-        return c;
-    };
-    auto draw = [&](const Call& c, int G, bool skip) {
-        row_items(P.pool + c.first, c.ne, r + c.tmin, row, W, spans);
+    if (ok && r < H) {
+        const int n = (int)P.n_items, rule = P.rule;
+        const unsigned below = (1u << lane) - 1u;
+        int G = 0;  // calls so far that reach this row
+        for (int c0 = 0; c0 < n; c0 += 32) {
+            // 32 calls' records at once, one per lane
+            const int i = c0 + lane;
+            const int4 cr = i < n ? P.crec[i] : make_int4(INT_MAX, 0, 0, 0);
+            const bool reach = cr.x <= r;
+            int o0 = 0, o1 = 0;
+            if (reach) {
+                const int* boff = P.bandoff + (size_t)i * (nb + 1);
+                o0 = boff[b];
+                o1 = boff[b + 1];
+            }
+            const unsigned rmask = __ballot_sync(FULL, reach);
+            unsigned dmask = __ballot_sync(FULL, reach && o1 > o0);
+            const unsigned long long my_first =
+                ((unsigned long long)(unsigned)cr.z | ((unsigned long long)(unsigned)cr.w << 32)) + (unsigned)o0;
+            unsigned my_clr = 0;
+            if (reach && o1 > o0) {
+                const ft_path_desc& d = P.paths[i];
+                my_clr = (unsigned)d.clr[0] | ((unsigned)d.clr[1] << 8) | ((unsigned)d.clr[2] << 16) |
+                         ((unsigned)d.clr[3] << 24);
+            }
+            while (dmask) {
+                const int j = __ffs(dmask) - 1;
+                dmask &= dmask - 1;
+                const int Gj = G + __popc(rmask & ((1u << j) - 1u));
+                const unsigned long long first = __shfl_sync(FULL, my_first, j);
+                const int ne = __shfl_sync(FULL, o1 - o0, j);
+                const int y = r + __shfl_sync(FULL, cr.y, j);
+                const unsigned clr = __shfl_sync(FULL, my_clr, j);
+                // cells of the band edges crossing scan row y, inside the segment
+                unsigned carry = 0, tmask = 0;
+                const int4* E = reinterpret_cast<const int4*>(P.pool + first);
+                for (int e = lane; e < ne; e += 32) {
+                    const int4 hb = E[2 * e + 1];  // step_pix, ed, start_row, end_row
+                    if (y < hb.z || y > hb.w) continue;
+                    const int4 ha = E[2 * e];  // y_upper, y_lower, x_bot0, inv_slope
+                    const int x_bot = wadd(ha.z, wmul(y - hb.z, ha.w));
+                    seg_row(x_bot, ha.w, y == hb.z, y == hb.w, fxfract(ha.x), fxfract(ha.y), hb.x > 0 ? hb.x : FX_ONE,
+                            hb.y, area, x0, sw, W, carry, tmask);
+                }
+                carry = warp_sum_u(carry);
+                tmask = __reduce_or_sync(FULL, tmask);
+                __syncwarp();
+                if (!tmask && resolve_cov(carry, rule) == 0) continue;  // nothing covered in this segment
+                // resolve the spans, queue the covered pixels, composite them 32 at a time
+                unsigned run = carry;
+                int qn = 0;
+                auto flush = [&](int cnt) {
+                    __syncwarp();
+                    for (int k = lane; k < cnt; k += 32) {
+                        const unsigned e = q[k];
+                        const int x = (int)(e >> 8);
+                        unsigned* p = px(x);
+                        unsigned dv = *p;
+                        const int kk = min(Gj - (int)last[x], 15);
+                        if (kk) dv = ftab4(ftab, dv, kk);
+                        *p = srcover_rgba(dv, clr, e & 255u);
+                        last[x] = (unsigned short)(Gj + 1);
+                    }
+                    __syncwarp();
+                };
+                for (int sp = 0; sp < (sw >> 7); sp++) {
+                    const bool t = (tmask >> sp) & 1u;
+                    if (!t && resolve_cov(run, rule) == 0) continue;
+                    const int x = (sp << 7) + lane * 4;
+                    int4 a = make_int4(0, 0, 0, 0);
+                    if (t) {
+                        a = *reinterpret_cast<const int4*>(area + x);
+                        *reinterpret_cast<int4*>(area + x) = make_int4(0, 0, 0, 0);
+                    }
+                    const unsigned s0v = (unsigned)a.x, s1v = s0v + (unsigned)a.y, s2v = s1v + (unsigned)a.z,
+                                   s3v = s2v + (unsigned)a.w;
+                    const unsigned inc = warp_incl_sum_u(s3v);
+                    const unsigned ex = inc - s3v + run;
+                    run += __shfl_sync(FULL, inc, 31);
+                    unsigned av[4] = {resolve_cov(s0v + ex, rule), resolve_cov(s1v + ex, rule),
+                                      resolve_cov(s2v + ex, rule), resolve_cov(s3v + ex, rule)};
+                    int cnt = 0;
+#pragma unroll
+                    for (int k = 0; k < 4; k++) {
+                        if (x0 + x + k >= W) av[k] = 0;
+                        cnt += av[k] != 0;
+                    }
+                    const unsigned cinc = warp_incl_sum_u((unsigned)cnt);
+                    const int tot = (int)__shfl_sync(FULL, cinc, 31);
+                    if (!tot) continue;
+                    int pos = qn + (int)(cinc - (unsigned)cnt);
+#pragma unroll
+                    for (int k = 0; k < 4; k++)
+                        if (av[k]) q[pos++] = ((unsigned)(x + k) << 8) | av[k];
+                    qn += tot;
+                    if (qn >= 32) {
+                        const int done = qn & ~31, rest = qn & 31;
+                        flush(done);
+                        const unsigned mv = lane < rest ? q[done + lane] : 0u;
+                        __syncwarp();
+                        if (lane < rest) q[lane] = mv;
+                        qn = rest;
+                    }
+                }
+                if (qn) flush(qn);
+            }
+            G += __popc(rmask);
+            (void)below;
+            if (G >= 0xC000) {  // keep the u16 call counts in range: pending counts saturate at 15
+                __syncwarp();
+                for (int x = lane; x < sw; x += 32) last[x] = last[x] > 0x8000 ? (unsigned short)(last[x] - 0x8000) : 0;
+                G -= 0x8000;
+                __syncwarp();
+            }
+        }
+        // the alpha-0 composites still pending since each pixel's last cover
         __syncwarp();
-        composite_row(row, last, spans, W, Wp, drow, P.rule, rgba, c.clr, G, ftab, skip);
-    };
-    if (!rgba) {
-        // Matte8: every call overwrites its rows, so only the last call reaching this row shows
-        int found = -1;
-        for (int c1 = n; c1 > 0 && found < 0; c1 -= 32) {
-            const int i = c1 - 32 + lane;
-            const bool hit = i >= 0 && P.crec[i].x <= r;
-            const unsigned m = __ballot_sync(FULL, hit);
-            if (m) found = c1 - 32 + 31 - __clz(m);
-        }
-        if (found >= 0) draw(fetch(found), 0, false);
-        return;
-    }
-    int G = 0;  // calls so far that reach this row
-    for (int c0 = 0; c0 < n; c0 += 32) {
-        // 32 calls' records at once, one per lane, then handed out by shuffles
-        const int i = c0 + lane;
-        const int rb = i < n ? P.crec[i].x : INT_MAX;
-        unsigned reach = __ballot_sync(FULL, rb <= r);
-        Call mine_c{0ull, 0, 0, 0u};
-        if (rb <= r) mine_c = fetch(i);
-        while (reach) {
-            const int j = __ffs(reach) - 1;
-            reach &= reach - 1;
-            Call c;
-            c.first = __shfl_sync(FULL, mine_c.first, j);
-            c.ne = __shfl_sync(FULL, mine_c.ne, j);
-            c.tmin = __shfl_sync(FULL, mine_c.tmin, j);
-            c.clr = __shfl_sync(FULL, mine_c.clr, j);
-            draw(c, G, true);
-            G++;
+        for (int x = lane; x < sw; x += 32) {
+            const int kk = min(G - (int)last[x], 15);
+            if (kk) {
+                unsigned* p = px(x);
+                *p = ftab4(ftab, *p, kk);
+            }
         }
     }
-    // the alpha-0 composites still pending since each pixel's last cover
-    unsigned* dp = reinterpret_cast<unsigned*>(drow);
-    for (int x = lane; x < W; x += 32) {
-        const int kk = min(G - (int)last[x], 15);
-        if (kk) dp[x] = ftab4(ftab, dp[x], kk);
+    if (tma) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (ok && threadIdx.x == 0) {
+            for (int bx = 0; bx < sw / BW; bx++)
+                asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                                 reinterpret_cast<uint64_t>(&tmap)),
+                             "r"(x0 + bx * BW), "r"(b * R), "r"(smem_u32(tile + bx * R * BW))
+                             : "memory");
+            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+            asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+        }
+    } else {
+        __syncwarp();
+        if (r < H)
+            for (int x = lane; x < sw && x0 + x < W; x += 32) crow[x0 + x] = *px(x);
     }
 }
 
-int composite_bands_smem(int band_rows, int width) { return FTAB_BYTES + band_rows * row_smem_bytes(width); }
+int composite_tile_smem(int band_rows, int seg_w) { return ctile_layout(band_rows, seg_w).bytes; }
+
+cudaError_t launch_composite_tiles(const KParams& p, const CUtensorMap& tmap, cudaStream_t s) {
+    const int smem = composite_tile_smem(p.band_rows, p.seg_w);
+    cudaError_t e = cudaFuncSetAttribute(k_ctile, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    const int nseg = ((int)p.canvas_w + p.seg_w - 1) / p.seg_w;
+    k_ctile<<<p.n_bands * nseg, 32 * p.band_rows, smem, s>>>(p, tmap);
+    return cudaGetLastError();
+}
+
+int composite_bands_smem(int band_rows, int width) { return band_rows * row_smem_bytes(width); }
 
 // ---- edges and band bins of one path's figure over the whole GPU (split_bin); the
 //      figure was built by CTA 0 of k_cbuild.  Band rows follow bin_edges.

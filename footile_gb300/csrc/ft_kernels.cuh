@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "../../include/footile_gpu.h"
@@ -140,6 +141,10 @@ struct KParams {
     int split_bin;
     int4* fig_state;             // count, direction, top row, edges fit the pool
     int* bin_hist;               // n_bands counts, then n_bands fill cursors
+    // Rgba8p tile compositor (k_ctile): tile width in pixels (128, 256, 512 or 1024) and
+    // whether the canvas is staged by TMA through the tensor map passed beside these
+    int seg_w;
+    int use_tma;
 };
 
 // Ordered composite: per-path figure build and edge binning, then one CTA per band.
@@ -147,6 +152,9 @@ struct KParams {
 // stacks are in local memory).
 cudaError_t launch_composite_build(const KParams& p, int grid, int smem_bytes, cudaStream_t s, bool few_ctas);
 cudaError_t launch_composite_bands(const KParams& p, int smem_bytes, cudaStream_t s);
+// Rgba8p: tiles of band_rows x seg_w pixels, canvas staged through `tmap` when use_tma.
+cudaError_t launch_composite_tiles(const KParams& p, const CUtensorMap& tmap, cudaStream_t s);
+int composite_tile_smem(int band_rows, int seg_w);
 // Edges and band bins of a single path's figure (after k_cbuild with split_bin), over
 // the whole GPU: edge records and band counts, a scan and pool allocation, the fill.
 cudaError_t launch_figure_bins(const KParams& p, int grid, cudaStream_t s);

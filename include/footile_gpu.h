@@ -198,9 +198,11 @@ FT_API void ft_batch_destroy(ft_batch* batch);
  * as fit (0 = built-in choice); `split_px`, paths of at least this many pixels are
  * split into row ranges, the queue grain of large paths (0 = 1 Mpx); `grid_per_sm`,
  * resident CTAs per SM of the persistent kernels (0 = occupancy maximum).
- * Ordered composites (ft_composite_batch): `band_rows`, rows per band of the band
- * compositor (1..8, 0 = built-in); `pool_edges`, the first size of the binned-edge pool
- * in edges (it grows on demand; 0 = built-in).  Host batches (ft_fill_batch with
+ * Ordered composites (ft_composite_batch, and single calls of at least split_px pixels):
+ * `band_rows`, rows per band (1..8, 0 = built-in 8) — the height of a compositor tile;
+ * `tile_w`, the width of an Rgba8p compositor tile in pixels (128, 256, 512 or 1024,
+ * 0 = built-in 512); `pool_edges`, the first size of the binned-edge pool in edges (it
+ * grows on demand; 0 = built-in).  Host batches (ft_fill_batch with
  * FT_HOST): `host_chunks`, chunks of the copy pipeline (1..16, 0 = built-in: 2 from
  * 64 MB of rasters); `host_mapped`, 0 = page-locked Matte8 rasters are written and
  * page-locked ops read in place (built-in), 1 = rasters and ops are copied, 2 = rasters
@@ -215,6 +217,7 @@ typedef struct ft_tuning {
     int32_t pool_edges;
     int32_t host_chunks;
     int32_t host_mapped;
+    int32_t tile_w;
 } ft_tuning;
 FT_API int ft_set_tuning(ft_ctx* ctx, const ft_tuning* tuning);
 FT_API int ft_get_tuning(ft_ctx* ctx, ft_tuning* tuning);
@@ -377,6 +380,12 @@ FT_API const char* ft_last_error(ft_ctx* ctx);
 
 /* Device time in milliseconds of the last call's kernels (CUDA events). */
 FT_API int ft_last_timings(ft_ctx* ctx, float* kernel_ms);
+
+/* Device time in milliseconds of the Rgba8p tile compositor alone in the last call (the
+ * ordered SrcOver after the figures are built and binned; ft_composite_batch, and ft_fill /
+ * ft_stroke of at least split_px pixels); 0 when the last call did not run it.  No
+ * counterpart in footile: for measuring the compositing step against the HBM roofline. */
+FT_API int ft_last_composite_ms(ft_ctx* ctx, float* ms);
 
 /* Number of kernel launches the library has issued since the context was created. */
 FT_API uint64_t ft_launch_count(ft_ctx* ctx);

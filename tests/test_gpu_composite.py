@@ -59,6 +59,35 @@ def test_composite_band_heights(ctx, band_rows):
     assert_same(got, want, f"band rows {band_rows}")
 
 
+@pytest.mark.parametrize("tile_w", [128, 256, 512, 1024])
+@pytest.mark.parametrize("band_rows", [1, 3, 8])
+def test_composite_tile_shapes(ctx, tile_w, band_rows):
+    """Every compositor tile shape (band rows x tile width) gives the same bytes; the
+    300-pixel canvas spans several tiles of 128 and 256 pixels and part of one of 512
+    or 1024, so the carries between tiles and the canvas edge are exercised."""
+    ctx.tune(band_rows=band_rows, tile_w=tile_w)
+    ops, paths, init = _scene(17, 40, 300, 77, True)
+    want = init.copy()
+    oracle.composite(1, _abi.NONZERO, ops, paths, _abi.RGBA8P, want)
+    got = init.copy()
+    ctx.set_pen_width(1.0)
+    composite_batch(ctx, ops, paths, _abi.RGBA8P, got, stroke=True)
+    assert_same(got, want, f"tile {band_rows}x{tile_w}")
+
+
+@pytest.mark.parametrize("w", [101, 300])
+def test_composite_canvas_staging(ctx, w):
+    """Rows 404 bytes apart (not a multiple of 16) cannot be described by a TMA tensor
+    map: the compositor stages the canvas with plain loads and stores; 1,200-byte rows
+    go through TMA.  Both give the oracle's bytes."""
+    ops, paths, init = _scene(23, 36, w, 90, False)
+    want = init.copy()
+    oracle.composite(0, _abi.EVENODD, ops, paths, _abi.RGBA8P, want)
+    got = init.copy()
+    composite_batch(ctx, ops, paths, _abi.RGBA8P, got, rule=_abi.EVENODD)
+    assert_same(got, want, f"width {w}")
+
+
 def test_composite_matte8_evenodd(ctx):
     ops, paths, _ = _scene(3, 40, 120, 90, False)
     init = np.random.default_rng(1).integers(0, 256, (90, 120)).astype(np.uint8)

@@ -16,7 +16,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def test_stroke_points_block_matches_one_thread(cuda_ok, tmp_path):
     exe = tmp_path / "stroke_points_check"
-    flags = [f for f in _build.NVFLAGS if f not in ("-Xcompiler", "-fPIC", "-fvisibility=hidden")]
+    flags = [f for f in _build.NVFLAGS if f not in ("-Xcompiler", "-fPIC", "-fvisibility=hidden", "-ffp-contract=off")]
+    flags += ["-Xcompiler", "-ffp-contract=off"]
     subprocess.check_call([_build.nvcc(), *flags, *_build.GENCODE, "-I",
                            os.path.join(ROOT, "footile_gb300", "csrc"),
                            os.path.join(ROOT, "tests", "cpp", "stroke_points_check.cu"), "-o", str(exe)])
