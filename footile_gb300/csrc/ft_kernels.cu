@@ -1926,8 +1926,10 @@ __device__ void bin_edges(const KParams& P, uint32_t path, const CState& S, cons
     __syncthreads();
     const unsigned long long base = s_base;
     const bool fits = base + (unsigned long long)carry <= P.pool_cap;
-    int* boff = P.bandoff + (size_t)path * (nb + 1);
-    for (int b = tid; b <= nb; b += BLOCK) boff[b] = fits ? (b < nb ? hist[b] : carry) : 0;
+    // band offsets band-major (bandoff[b * n_items + path]): the compositors read 32 calls'
+    // offsets of one band as one coalesced load
+    for (int b = tid; b <= nb; b += BLOCK)
+        P.bandoff[(size_t)b * P.n_items + path] = fits ? (b < nb ? hist[b] : carry) : 0;
     if (tid == 0) {
         P.crec[path] = make_int4(rb, tmin, (int)(unsigned)(base & 0xFFFFFFFFull), (int)(unsigned)(base >> 32));
         if (!fits) atomicMax(&P.status[path], FT_ERR_CAP);  // the host grows the pool and runs again
@@ -2096,8 +2098,7 @@ __global__ void __launch_bounds__(BLOCK) k_cbands(KParams P) {
     }
     if (found < 0) return;
     const int4 cr = P.crec[found];
-    const int* boff = P.bandoff + (size_t)found * (nb + 1);
-    const int o0 = boff[b], o1 = boff[b + 1];
+    const int o0 = P.bandoff[(size_t)b * n + found], o1 = P.bandoff[(size_t)(b + 1) * n + found];
     const unsigned long long first = ((unsigned long long)(unsigned)cr.z | ((unsigned long long)(unsigned)cr.w << 32)) + o0;
     row_items(P.pool + first, o1 - o0, r + cr.y, row, W, spans);
     __syncwarp();
@@ -2121,10 +2122,8 @@ __global__ void __launch_bounds__(BLOCK) k_cbands(KParams P) {
 // applied lazily, as a pending count per pixel and a table of powers of the alpha-0 map
 // (the map changes only channel values 1..15 and settles after 15 applications).
 
-constexpr int CT_QN = 160;  // queued covered pixels per warp (one span of 128 + a partial round)
-
 struct CTileLayout {
-    int tile, mbar, area, last, queue, bytes;
+    int tile, mbar, area, last, bytes;
 };
 __host__ __device__ inline CTileLayout ctile_layout(int R, int sw) {
     CTileLayout L;
@@ -2138,9 +2137,6 @@ __host__ __device__ inline CTileLayout ctile_layout(int R, int sw) {
     o += R * sw * 4;
     L.last = o;  // per warp: sw u16, calls so far at each pixel's last cover
     o += R * sw * 2;
-    o = (o + 15) & ~15;
-    L.queue = o;  // per warp: CT_QN covered pixels (x << 8 | alpha)
-    o += R * CT_QN * 4;
     L.bytes = o;
     return L;
 }
@@ -2164,12 +2160,23 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, unsigned parity) {
     return false;
 }
 
+// Position of segment cell c in a warp's area row: lane l owns cells [l * 4k, (l + 1) * 4k)
+// (k = 1 << k_shift int4 per lane), stored as its k int4 with the int4 index XORed by the
+// lane's low bits, so that the 32 lanes reading their j-th int4 hit distinct bank groups.
+__device__ __forceinline__ int swz_cell(int c, int k_shift) {
+    const int i = c >> 2, km = (1 << k_shift) - 1;
+    const int l = i >> k_shift;
+    return (((l << k_shift) | ((i & km) ^ (l & km))) << 2) | (c & 3);
+}
+
 // Cells of one (edge, row) item inside the segment [s0, s0 + sw) of a raster row of W
 // pixels (fig.rs:238-321 restricted to the segment): the cells' growths go into `area`
-// (segment-relative), the cumulative sum the item leaves left of s0 into `carry`, and
-// the touched 128-pixel spans into `tmask`.  The arguments are scan_row's.
+// (segment cells, swz_cell layout), the cumulative sum the item leaves left of s0 into
+// `carry`, and the touched lane chunks (4 << k_shift cells each) into `tmask`.  The
+// other arguments are scan_row's.
 __device__ __forceinline__ void seg_row(int x_bot, int inv, bool st, bool en, int fu, int fl, int step, int ed,
-                                        int* area, int s0, int sw, int W, unsigned& carry, unsigned& tmask) {
+                                        int* area, int s0, int sw, int W, int k_shift, unsigned& carry,
+                                        unsigned& tmask) {
     const int ccov = en ? pixel_cov(fl) : 256;
     const int cov = st ? ccov - pixel_cov(fu) : ccov;
     if (cov <= 0) return;
@@ -2201,8 +2208,8 @@ __device__ __forceinline__ void seg_row(int x_bot, int inv, bool st, bool en, in
     for (; c < s1; c++) {
         const int v = min(pixel_cov(x_cov), cov);
         if (v != prev) {
-            atomicAdd(&area[c - s0], ed * (v - prev));
-            tmask |= 1u << ((c - s0) >> 7);
+            atomicAdd(&area[swz_cell(c - s0, k_shift)], ed * (v - prev));
+            tmask |= 1u << ((c - s0) >> (k_shift + 2));
         }
         prev = v;
         if (v >= cov) break;
@@ -2216,7 +2223,7 @@ __device__ __forceinline__ unsigned warp_sum_u(unsigned v) {
     return v;
 }
 
-__global__ void __launch_bounds__(BLOCK) k_ctile(KParams P, const __grid_constant__ CUtensorMap tmap) {
+__global__ void __launch_bounds__(BLOCK, 4) k_ctile(KParams P, const __grid_constant__ CUtensorMap tmap) {
     extern __shared__ __align__(128) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int W = (int)P.canvas_w, H = (int)P.canvas_h, R = P.band_rows, nb = P.n_bands, sw = P.seg_w;
@@ -2231,7 +2238,11 @@ __global__ void __launch_bounds__(BLOCK) k_ctile(KParams P, const __grid_constan
     uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + L.mbar);
     int* area = reinterpret_cast<int*>(smem + L.area) + warp * sw;
     unsigned short* last = reinterpret_cast<unsigned short*>(smem + L.last) + warp * sw;
-    unsigned* q = reinterpret_cast<unsigned*>(smem + L.queue) + warp * CT_QN;
+    // the covered pixels of a call (x << 8 | alpha) are queued in the area row, which the
+    // resolve leaves zero; the queue's words are zeroed again after the composite
+    unsigned* q = reinterpret_cast<unsigned*>(area);
+    const int ks = sw == 1024 ? 3 : sw == 512 ? 2 : sw == 256 ? 1 : 0;  // log2(int4 per lane)
+    const int PL = 4 << ks;                                              // pixels per lane
     // the tile pixel of this warp's row at segment position x
     auto px = [&](int x) -> unsigned* {
         return tile + (((x >> bw_shift) * R + warp) << bw_shift) + (x & (BW - 1));
@@ -2271,7 +2282,6 @@ __global__ void __launch_bounds__(BLOCK) k_ctile(KParams P, const __grid_constan
     __syncthreads();
     if (ok && r < H) {
         const int n = (int)P.n_items, rule = P.rule;
-        const unsigned below = (1u << lane) - 1u;
         int G = 0;  // calls so far that reach this row
         for (int c0 = 0; c0 < n; c0 += 32) {
             // 32 calls' records at once, one per lane
@@ -2279,10 +2289,9 @@ __global__ void __launch_bounds__(BLOCK) k_ctile(KParams P, const __grid_constan
             const int4 cr = i < n ? P.crec[i] : make_int4(INT_MAX, 0, 0, 0);
             const bool reach = cr.x <= r;
             int o0 = 0, o1 = 0;
-            if (reach) {
-                const int* boff = P.bandoff + (size_t)i * (nb + 1);
-                o0 = boff[b];
-                o1 = boff[b + 1];
+            if (i < n) {
+                o0 = P.bandoff[(size_t)b * n + i];
+                o1 = P.bandoff[(size_t)(b + 1) * n + i];
             }
             const unsigned rmask = __ballot_sync(FULL, reach);
             unsigned dmask = __ballot_sync(FULL, reach && o1 > o0);
@@ -2311,72 +2320,93 @@ __global__ void __launch_bounds__(BLOCK) k_ctile(KParams P, const __grid_constan
                     const int4 ha = E[2 * e];  // y_upper, y_lower, x_bot0, inv_slope
                     const int x_bot = wadd(ha.z, wmul(y - hb.z, ha.w));
                     seg_row(x_bot, ha.w, y == hb.z, y == hb.w, fxfract(ha.x), fxfract(ha.y), hb.x > 0 ? hb.x : FX_ONE,
-                            hb.y, area, x0, sw, W, carry, tmask);
+                            hb.y, area, x0, sw, W, ks, carry, tmask);
                 }
                 carry = warp_sum_u(carry);
                 tmask = __reduce_or_sync(FULL, tmask);
                 __syncwarp();
                 if (!tmask && resolve_cov(carry, rule) == 0) continue;  // nothing covered in this segment
-                // resolve the spans, queue the covered pixels, composite them 32 at a time
-                unsigned run = carry;
-                int qn = 0;
-                auto flush = [&](int cnt) {
-                    __syncwarp();
-                    for (int k = lane; k < cnt; k += 32) {
-                        const unsigned e = q[k];
-                        const int x = (int)(e >> 8);
-                        unsigned* p = px(x);
-                        unsigned dv = *p;
-                        const int kk = min(Gj - (int)last[x], 15);
-                        if (kk) dv = ftab4(ftab, dv, kk);
-                        *p = srcover_rgba(dv, clr, e & 255u);
-                        last[x] = (unsigned short)(Gj + 1);
+                // resolve: each lane sums its chunk, one warp scan gives every chunk its running
+                // sum, each lane resolves its chunk; the covered pixels are queued (one warp
+                // scan of the counts) and composited 32 at a time, one pixel per lane
+                const bool tch = (tmask >> lane) & 1u;
+                int4* a4 = reinterpret_cast<int4*>(area);
+                const int km = (1 << ks) - 1;
+                unsigned csum = 0;
+                if (tch)
+                    for (int j = 0; j <= km; j++) {
+                        const int4 a = a4[(lane << ks) | (j ^ (lane & km))];
+                        csum += (unsigned)a.x + (unsigned)a.y + (unsigned)a.z + (unsigned)a.w;
                     }
-                    __syncwarp();
-                };
-                for (int sp = 0; sp < (sw >> 7); sp++) {
-                    const bool t = (tmask >> sp) & 1u;
-                    if (!t && resolve_cov(run, rule) == 0) continue;
-                    const int x = (sp << 7) + lane * 4;
-                    int4 a = make_int4(0, 0, 0, 0);
-                    if (t) {
-                        a = *reinterpret_cast<const int4*>(area + x);
-                        *reinterpret_cast<int4*>(area + x) = make_int4(0, 0, 0, 0);
+                const unsigned inc = warp_incl_sum_u(csum);
+                unsigned run = inc - csum + carry;
+                unsigned avw[8];
+                int cnt = 0;
+                if (tch) {
+#pragma unroll
+                    for (int j = 0; j < 8; j++) {
+                        if (j > km) break;
+                        int4* ap = a4 + ((lane << ks) | (j ^ (lane & km)));
+                        const int4 a = *ap;
+                        *ap = make_int4(0, 0, 0, 0);
+                        unsigned w = 0;
+                        run += (unsigned)a.x;
+                        w |= resolve_cov(run, rule);
+                        run += (unsigned)a.y;
+                        w |= resolve_cov(run, rule) << 8;
+                        run += (unsigned)a.z;
+                        w |= resolve_cov(run, rule) << 16;
+                        run += (unsigned)a.w;
+                        w |= resolve_cov(run, rule) << 24;
+                        avw[j] = w;
                     }
-                    const unsigned s0v = (unsigned)a.x, s1v = s0v + (unsigned)a.y, s2v = s1v + (unsigned)a.z,
-                                   s3v = s2v + (unsigned)a.w;
-                    const unsigned inc = warp_incl_sum_u(s3v);
-                    const unsigned ex = inc - s3v + run;
-                    run += __shfl_sync(FULL, inc, 31);
-                    unsigned av[4] = {resolve_cov(s0v + ex, rule), resolve_cov(s1v + ex, rule),
-                                      resolve_cov(s2v + ex, rule), resolve_cov(s3v + ex, rule)};
-                    int cnt = 0;
+                } else {
+                    const unsigned v = resolve_cov(run, rule) * 0x01010101u;
+#pragma unroll
+                    for (int j = 0; j < 8; j++) avw[j] = v;
+                }
+                const int xl = lane * PL;  // this lane's first pixel in the segment
+                const int past = x0 + xl + PL - W;  // pixels of the chunk right of the canvas
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    if (j > km) break;
+                    if (past > 0)
+#pragma unroll
+                        for (int k = 0; k < 4; k++)
+                            if (4 * j + k >= PL - past) avw[j] &= ~(0xFFu << (8 * k));
+                    const unsigned w = avw[j];
+                    cnt += ((w & 0xFFu) != 0) + ((w & 0xFF00u) != 0) + ((w & 0xFF0000u) != 0) + ((w >> 24) != 0);
+                }
+                const unsigned cinc = warp_incl_sum_u((unsigned)cnt);
+                const int tot = (int)__shfl_sync(FULL, cinc, 31);
+                if (!tot) continue;
+                int pos = (int)(cinc - (unsigned)cnt);
+                __syncwarp();  // every lane has read and cleared its chunk
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    if (j > km) break;
+                    const unsigned w = avw[j];
 #pragma unroll
                     for (int k = 0; k < 4; k++) {
-                        if (x0 + x + k >= W) av[k] = 0;
-                        cnt += av[k] != 0;
-                    }
-                    const unsigned cinc = warp_incl_sum_u((unsigned)cnt);
-                    const int tot = (int)__shfl_sync(FULL, cinc, 31);
-                    if (!tot) continue;
-                    int pos = qn + (int)(cinc - (unsigned)cnt);
-#pragma unroll
-                    for (int k = 0; k < 4; k++)
-                        if (av[k]) q[pos++] = ((unsigned)(x + k) << 8) | av[k];
-                    qn += tot;
-                    if (qn >= 32) {
-                        const int done = qn & ~31, rest = qn & 31;
-                        flush(done);
-                        const unsigned mv = lane < rest ? q[done + lane] : 0u;
-                        __syncwarp();
-                        if (lane < rest) q[lane] = mv;
-                        qn = rest;
+                        const unsigned av = (w >> (8 * k)) & 0xFFu;
+                        if (av) q[pos++] = ((unsigned)(xl + 4 * j + k) << 8) | av;
                     }
                 }
-                if (qn) flush(qn);
+                __syncwarp();
+                for (int k = lane; k < tot; k += 32) {
+                    const unsigned e = q[k];
+                    const int x = (int)(e >> 8);
+                    unsigned* p = px(x);
+                    unsigned dv = *p;
+                    const int kk = min(Gj - (int)last[x], 15);
+                    if (kk) dv = ftab4(ftab, dv, kk);
+                    *p = srcover_rgba(dv, clr, e & 255u);
+                    last[x] = (unsigned short)(Gj + 1);
+                    q[k] = 0u;
+                }
+                __syncwarp();
             }
             G += __popc(rmask);
-            (void)below;
             if (G >= 0xC000) {  // keep the u16 call counts in range: pending counts saturate at 15
                 __syncwarp();
                 for (int x = lane; x < sw; x += 32) last[x] = last[x] > 0x8000 ? (unsigned short)(last[x] - 0x8000) : 0;
