@@ -52,7 +52,7 @@ def parse_args():
     ap.add_argument("--no-tune", action="store_true", help="use the built-in plan instead of the autotuner")
     ap.add_argument("--tune-cache", default=None, help="autotuner cache file (looked up, then appended)")
     ap.add_argument("--composite-strokes", type=int, default=16384,
-                    help="--only adjoint_composite: strokes on the 2048x2048 canvas")
+                    help="--only strokes / adjoint_composite: strokes on the 2048x2048 canvas")
     ap.add_argument("--composite-chunk", type=int, default=0,
                     help="--only adjoint_composite: strokes covered per chunk (0: sized to free memory)")
     ap.add_argument("--only", choices=["single", "scene", "strokes", "adjoint", "adjoint_strokes",
@@ -176,13 +176,13 @@ def extra_scene(ctx, stream, dev, cpu=True):
     return out
 
 
-def extra_strokes(ctx, stream, dev, cpu=True, reps=2):
+def extra_strokes(ctx, stream, dev, cpu=True, reps=2, n_paths=16384):
     """16,384 open cubic strokes (pen width 1..12, Miter(4)) composited in order onto
     one 2048x2048 Rgba8p canvas (ft_composite_batch)."""
     import torch
     from footile_gb300 import _abi, workloads
     from footile_gb300.plotter import composite_batch, pack_batch, pen_width_chain
-    paths_ops, widths, clrs, side = workloads.strokes_16384()
+    paths_ops, widths, clrs, side = workloads.strokes_16384(n_paths=n_paths)
     ops, paths, _ = pack_batch(paths_ops, [side] * len(paths_ops), _abi.RGBA8P, clrs)
     paths["s_width"], _ = pen_width_chain(ops, paths, 1.0)
     ops_d = torch.from_numpy(ops.view(np.uint8)).to(dev)
@@ -193,13 +193,33 @@ def extra_strokes(ctx, stream, dev, cpu=True, reps=2):
         composite_batch(ctx, ops_d, paths, _abi.RGBA8P, ras_d, stroke=True)
     run()
     t0 = time.perf_counter()
+    dev_ms, comp_ms = [], []
     for _ in range(reps):
         run()
+        dev_ms.append(ctx.last_ms())
+        comp_ms.append(ctx.last_composite_ms())
     torch.cuda.synchronize()
     ms = (time.perf_counter() - t0) / reps * 1e3
-    out = {"workload": "strokes_16384 (8..64 cubics each, width 1..12, ordered SrcOver on 2048x2048 Rgba8p)",
+    # per-bbox algorithmic bytes of the ordered composite: every call reads and writes its
+    # bounding box of RGBA (8 B/px) and its mask (1 B/px); the minimum is one canvas read
+    # and write
+    bbox_px = 0
+    for o in paths_ops:
+        pts = o["v"][1:, :6].reshape(-1, 2)
+        lo = np.floor(pts.min(axis=0) - 6.0).clip(0, side)
+        hi = np.ceil(pts.max(axis=0) + 6.0).clip(0, side)
+        bbox_px += int(np.prod(hi - lo))
+    peak, peak_kind = measured_peak_hbm()
+    cms = float(np.median(comp_ms))
+    out = {"workload": f"strokes_{n_paths} (8..64 cubics each, width 1..12, ordered SrcOver on 2048x2048 Rgba8p)",
            "ms_per_composite": ms, "paths_per_s": len(paths) / (ms * 1e-3),
-           "canvas_Mpx_per_s": side * side / (ms * 1e-3) / 1e6}
+           "canvas_Mpx_per_s": side * side / (ms * 1e-3) / 1e6,
+           "device_ms": float(np.median(dev_ms)), "tile_compositor_ms": cms,
+           "figure_build_and_bin_ms": float(np.median(dev_ms)) - cms,
+           "compositor_roofline": {"bound": "hbm", "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                                   "bbox_bytes": 9 * bbox_px, "canvas_bytes": 2 * side * side * 4,
+                                   "achieved_bbox": 9 * bbox_px / (cms * 1e-3) / 1e9 if cms else None,
+                                   "frac_bbox": 9 * bbox_px / (cms * 1e-3) / 1e9 / peak if cms else None}}
     if cpu:
         # the reference composites every pixel from each call's top row down: time a few calls
         import oracle
@@ -628,6 +648,8 @@ def run_only(args):
     kw = {}
     if args.only == "adjoint_composite":
         kw = {"n_paths": args.composite_strokes, "chunk": args.composite_chunk}
+    elif args.only == "strokes":
+        kw = {"n_paths": args.composite_strokes}
     print(json.dumps(fn(ctx, stream, dev, cpu=not args.no_cpu, **kw)), flush=True)
 
 

@@ -2116,14 +2116,20 @@ __global__ void __launch_bounds__(BLOCK) k_cbands(KParams P) {
 // cells inside the segment (into a shared i32 segment row, atomics) and, from the closed
 // form of the cell walk, the running sum it leaves to the left of the segment (the carry
 // into the segment: the cumulative cell sum through column c of an (edge, row) item is
-// min(pixel_cov(min(first + (c - minp) * step, ONE)), cov), fig.rs:285-321).  The warp then resolves the touched spans, compacts the covered pixels
-// (alpha > 0) into a queue and composites them 32 at a time, one pixel per lane; the
-// alpha-0 SrcOver footile applies to every other pixel from the call's top row down is
-// applied lazily, as a pending count per pixel and a table of powers of the alpha-0 map
-// (the map changes only channel values 1..15 and settles after 15 applications).
+// min(pixel_cov(min(first + (c - minp) * step, ONE)), cov), fig.rs:285-321).  The row is
+// then resolved sparsely: only the 8-pixel chunks that received cells are summed and
+// resolved (32 at a time, one per lane, a warp scan placing them), and the untouched gap
+// after each chunk holds that chunk's final running sum, so it is one run of a single
+// alpha.  The covered pixels (alpha > 0) of the chunks and of the runs are composited
+// with all lanes busy; the alpha-0 SrcOver footile applies to every other pixel from the
+// call's top row down is applied lazily, as a pending count per pixel and a table of
+// powers of the alpha-0 map (the map changes only channel values 1..15 and settles after
+// 15 applications).
+
+constexpr int CT_QN = 256 + 40;  // queued covered pixels of one round (32 chunks of 8) and its runs
 
 struct CTileLayout {
-    int tile, mbar, area, last, bytes;
+    int tile, mbar, area, last, queue, bmap, bytes;
 };
 __host__ __device__ inline CTileLayout ctile_layout(int R, int sw) {
     CTileLayout L;
@@ -2135,6 +2141,11 @@ __host__ __device__ inline CTileLayout ctile_layout(int R, int sw) {
     o += 16;
     L.area = o;  // per warp: sw i32 cell areas
     o += R * sw * 4;
+    L.queue = o;  // per warp: CT_QN queued pixels (x << 8 | alpha) and runs
+    o += R * CT_QN * 4;
+    L.bmap = o;  // per warp: touched 8-pixel chunks, sw / 256 words, then the chunk list (sw / 8 bytes)
+    o += R * (sw / 256 * 4 + sw / 8);
+    o = (o + 15) & ~15;
     L.last = o;  // per warp: sw u16, calls so far at each pixel's last cover
     o += R * sw * 2;
     L.bytes = o;
@@ -2160,23 +2171,12 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, unsigned parity) {
     return false;
 }
 
-// Position of segment cell c in a warp's area row: lane l owns cells [l * 4k, (l + 1) * 4k)
-// (k = 1 << k_shift int4 per lane), stored as its k int4 with the int4 index XORed by the
-// lane's low bits, so that the 32 lanes reading their j-th int4 hit distinct bank groups.
-__device__ __forceinline__ int swz_cell(int c, int k_shift) {
-    const int i = c >> 2, km = (1 << k_shift) - 1;
-    const int l = i >> k_shift;
-    return (((l << k_shift) | ((i & km) ^ (l & km))) << 2) | (c & 3);
-}
-
 // Cells of one (edge, row) item inside the segment [s0, s0 + sw) of a raster row of W
 // pixels (fig.rs:238-321 restricted to the segment): the cells' growths go into `area`
-// (segment cells, swz_cell layout), the cumulative sum the item leaves left of s0 into
-// `carry`, and the touched lane chunks (4 << k_shift cells each) into `tmask`.  The
-// other arguments are scan_row's.
+// (segment cells), the cumulative sum the item leaves left of s0 into `carry`, and the
+// 8-pixel chunks it touched into the bitmap `bmap`.  The other arguments are scan_row's.
 __device__ __forceinline__ void seg_row(int x_bot, int inv, bool st, bool en, int fu, int fl, int step, int ed,
-                                        int* area, int s0, int sw, int W, int k_shift, unsigned& carry,
-                                        unsigned& tmask) {
+                                        int* area, int s0, int sw, int W, unsigned& carry, unsigned* bmap) {
     const int ccov = en ? pixel_cov(fl) : 256;
     const int cov = st ? ccov - pixel_cov(fu) : ccov;
     if (cov <= 0) return;
@@ -2191,29 +2191,36 @@ __device__ __forceinline__ void seg_row(int x_bot, int inv, bool st, bool en, in
     const int r = (minp == maxp) ? fxmul(wsub(FX_ONE, fxfract(fxavg(mxx, mnx))), full)
                                  : fxmul(wsub(FX_ONE, fxfract(mnx)), FX_HALF);
     const int first = fxmul(r, step);
-    // cumulative sum through cell minp + j: min(pixel_cov(min(first + j * step, ONE)), cov)
-    auto cum = [&](int j) {
-        const long long v = (long long)first + (long long)j * step;
-        return min(pixel_cov(v > FX_ONE ? FX_ONE : (int)v), cov);
-    };
     int c = max(max(s0, minp), 0);
     int prev = 0;
     if (s0 > 0 && minp < s0) {
-        prev = cum(s0 - 1 - minp);
+        // cumulative sum through cell s0 - 1: min(pixel_cov(min(first + j * step, ONE)), cov)
+        const long long v = (long long)first + (long long)(s0 - 1 - minp) * step;
+        prev = min(pixel_cov(v > FX_ONE ? FX_ONE : (int)v), cov);
         carry += (unsigned)(ed * prev);
     }
     if (prev >= cov) return;
-    long long xv = (long long)first + (long long)(c - minp) * step;
+    const long long xv = (long long)first + (long long)(c - minp) * step;
     int x_cov = xv > FX_ONE ? FX_ONE : (int)xv;
+    int c_lo = -1, c_hi = -1;
     for (; c < s1; c++) {
         const int v = min(pixel_cov(x_cov), cov);
         if (v != prev) {
-            atomicAdd(&area[swz_cell(c - s0, k_shift)], ed * (v - prev));
-            tmask |= 1u << ((c - s0) >> (k_shift + 2));
+            atomicAdd(&area[c - s0], ed * (v - prev));
+            if (c_lo < 0) c_lo = c - s0;
+            c_hi = c - s0;
         }
         prev = v;
         if (v >= cov) break;
         x_cov = min(x_cov + step, FX_ONE);
+    }
+    if (c_lo >= 0) {  // the touched chunks c_lo / 8 .. c_hi / 8
+        const int k0 = c_lo >> 3, k1 = c_hi >> 3;
+        for (int w = k0 >> 5; w <= (k1 >> 5); w++) {
+            const int lo = max(k0 - 32 * w, 0), hi = min(k1 - 32 * w, 31);
+            const unsigned m = (hi == 31 ? 0xFFFFFFFFu : ((1u << (hi + 1)) - 1u)) & ~((1u << lo) - 1u);
+            atomicOr(&bmap[w], m);
+        }
     }
 }
 
@@ -2233,16 +2240,16 @@ __global__ void __launch_bounds__(BLOCK, 4) k_ctile(KParams P, const __grid_cons
     const CTileLayout L = ctile_layout(R, sw);
     const int BW = sw < 256 ? sw : 256;  // TMA box width (pixels)
     const int bw_shift = BW == 256 ? 8 : 7;
+    const int nwords = sw >> 8;          // bitmap words (32 chunks of 8 pixels each)
+    const int nchunks = sw >> 3;
     unsigned char* ftab = smem;
     unsigned* tile = reinterpret_cast<unsigned*>(smem + L.tile);
     uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + L.mbar);
     int* area = reinterpret_cast<int*>(smem + L.area) + warp * sw;
+    unsigned* q = reinterpret_cast<unsigned*>(smem + L.queue) + warp * CT_QN;
+    unsigned* bmap = reinterpret_cast<unsigned*>(smem + L.bmap + warp * (nwords * 4 + nchunks));
+    unsigned char* clist = reinterpret_cast<unsigned char*>(bmap + nwords);
     unsigned short* last = reinterpret_cast<unsigned short*>(smem + L.last) + warp * sw;
-    // the covered pixels of a call (x << 8 | alpha) are queued in the area row, which the
-    // resolve leaves zero; the queue's words are zeroed again after the composite
-    unsigned* q = reinterpret_cast<unsigned*>(area);
-    const int ks = sw == 1024 ? 3 : sw == 512 ? 2 : sw == 256 ? 1 : 0;  // log2(int4 per lane)
-    const int PL = 4 << ks;                                              // pixels per lane
     // the tile pixel of this warp's row at segment position x
     auto px = [&](int x) -> unsigned* {
         return tile + (((x >> bw_shift) * R + warp) << bw_shift) + (x & (BW - 1));
@@ -2271,6 +2278,7 @@ __global__ void __launch_bounds__(BLOCK, 4) k_ctile(KParams P, const __grid_cons
     }
     for (int x = lane * 4; x < sw; x += 128) *reinterpret_cast<int4*>(area + x) = make_int4(0, 0, 0, 0);
     for (int x = lane; x < sw; x += 32) last[x] = 0;
+    if (lane < nwords) bmap[lane] = 0u;
     unsigned* crow = reinterpret_cast<unsigned*>(P.rasters + (size_t)r * P.canvas_stride);
     if (!tma && r < H)
         for (int x = lane; x < sw && x0 + x < W; x += 32) *px(x) = crow[x0 + x];
@@ -2282,6 +2290,8 @@ __global__ void __launch_bounds__(BLOCK, 4) k_ctile(KParams P, const __grid_cons
     __syncthreads();
     if (ok && r < H) {
         const int n = (int)P.n_items, rule = P.rule;
+        const unsigned lt = (1u << lane) - 1u;
+        const int xend = min(sw, W - x0);  // segment pixels on the canvas
         int G = 0;  // calls so far that reach this row
         for (int c0 = 0; c0 < n; c0 += 32) {
             // 32 calls' records at once, one per lane
@@ -2312,7 +2322,7 @@ __global__ void __launch_bounds__(BLOCK, 4) k_ctile(KParams P, const __grid_cons
                 const int y = r + __shfl_sync(FULL, cr.y, j);
                 const unsigned clr = __shfl_sync(FULL, my_clr, j);
                 // cells of the band edges crossing scan row y, inside the segment
-                unsigned carry = 0, tmask = 0;
+                unsigned carry = 0;
                 const int4* E = reinterpret_cast<const int4*>(P.pool + first);
                 for (int e = lane; e < ne; e += 32) {
                     const int4 hb = E[2 * e + 1];  // step_pix, ed, start_row, end_row
@@ -2320,91 +2330,94 @@ __global__ void __launch_bounds__(BLOCK, 4) k_ctile(KParams P, const __grid_cons
                     const int4 ha = E[2 * e];  // y_upper, y_lower, x_bot0, inv_slope
                     const int x_bot = wadd(ha.z, wmul(y - hb.z, ha.w));
                     seg_row(x_bot, ha.w, y == hb.z, y == hb.w, fxfract(ha.x), fxfract(ha.y), hb.x > 0 ? hb.x : FX_ONE,
-                            hb.y, area, x0, sw, W, ks, carry, tmask);
+                            hb.y, area, x0, sw, W, carry, bmap);
                 }
                 carry = warp_sum_u(carry);
-                tmask = __reduce_or_sync(FULL, tmask);
                 __syncwarp();
-                if (!tmask && resolve_cov(carry, rule) == 0) continue;  // nothing covered in this segment
-                // resolve: each lane sums its chunk, one warp scan gives every chunk its running
-                // sum, each lane resolves its chunk; the covered pixels are queued (one warp
-                // scan of the counts) and composited 32 at a time, one pixel per lane
-                const bool tch = (tmask >> lane) & 1u;
-                int4* a4 = reinterpret_cast<int4*>(area);
-                const int km = (1 << ks) - 1;
-                unsigned csum = 0;
-                if (tch)
-                    for (int j = 0; j <= km; j++) {
-                        const int4 a = a4[(lane << ks) | (j ^ (lane & km))];
-                        csum += (unsigned)a.x + (unsigned)a.y + (unsigned)a.z + (unsigned)a.w;
-                    }
-                const unsigned inc = warp_incl_sum_u(csum);
-                unsigned run = inc - csum + carry;
-                unsigned avw[8];
-                int cnt = 0;
-                if (tch) {
-#pragma unroll
-                    for (int j = 0; j < 8; j++) {
-                        if (j > km) break;
-                        int4* ap = a4 + ((lane << ks) | (j ^ (lane & km)));
-                        const int4 a = *ap;
-                        *ap = make_int4(0, 0, 0, 0);
-                        unsigned w = 0;
-                        run += (unsigned)a.x;
-                        w |= resolve_cov(run, rule);
-                        run += (unsigned)a.y;
-                        w |= resolve_cov(run, rule) << 8;
-                        run += (unsigned)a.z;
-                        w |= resolve_cov(run, rule) << 16;
-                        run += (unsigned)a.w;
-                        w |= resolve_cov(run, rule) << 24;
-                        avw[j] = w;
-                    }
-                } else {
-                    const unsigned v = resolve_cov(run, rule) * 0x01010101u;
-#pragma unroll
-                    for (int j = 0; j < 8; j++) avw[j] = v;
-                }
-                const int xl = lane * PL;  // this lane's first pixel in the segment
-                const int past = x0 + xl + PL - W;  // pixels of the chunk right of the canvas
-#pragma unroll
-                for (int j = 0; j < 8; j++) {
-                    if (j > km) break;
-                    if (past > 0)
-#pragma unroll
-                        for (int k = 0; k < 4; k++)
-                            if (4 * j + k >= PL - past) avw[j] &= ~(0xFFu << (8 * k));
-                    const unsigned w = avw[j];
-                    cnt += ((w & 0xFFu) != 0) + ((w & 0xFF00u) != 0) + ((w & 0xFF0000u) != 0) + ((w >> 24) != 0);
-                }
-                const unsigned cinc = warp_incl_sum_u((unsigned)cnt);
-                const int tot = (int)__shfl_sync(FULL, cinc, 31);
-                if (!tot) continue;
-                int pos = (int)(cinc - (unsigned)cnt);
-                __syncwarp();  // every lane has read and cleared its chunk
-#pragma unroll
-                for (int j = 0; j < 8; j++) {
-                    if (j > km) break;
-                    const unsigned w = avw[j];
-#pragma unroll
-                    for (int k = 0; k < 4; k++) {
-                        const unsigned av = (w >> (8 * k)) & 0xFFu;
-                        if (av) q[pos++] = ((unsigned)(xl + 4 * j + k) << 8) | av;
-                    }
+                // the touched chunks, in order
+                int T = 0;
+                for (int w = 0; w < nwords; w++) {
+                    const unsigned bw = bmap[w];
+                    if ((bw >> lane) & 1u) clist[T + __popc(bw & lt)] = (unsigned char)(32 * w + lane);
+                    T += __popc(bw);
                 }
                 __syncwarp();
-                for (int k = lane; k < tot; k += 32) {
-                    const unsigned e = q[k];
-                    const int x = (int)(e >> 8);
+                if (lane < nwords) bmap[lane] = 0u;
+                auto compose = [&](int x, unsigned av) {
                     unsigned* p = px(x);
                     unsigned dv = *p;
                     const int kk = min(Gj - (int)last[x], 15);
                     if (kk) dv = ftab4(ftab, dv, kk);
-                    *p = srcover_rgba(dv, clr, e & 255u);
+                    *p = srcover_rgba(dv, clr, av);
                     last[x] = (unsigned short)(Gj + 1);
-                    q[k] = 0u;
+                };
+                // the run before the first touched chunk holds the carry
+                {
+                    const unsigned av0 = resolve_cov(carry, rule);
+                    if (av0) {
+                        const int end = min(T ? (int)clist[0] * 8 : sw, xend);
+                        for (int x = lane; x < end; x += 32) compose(x, av0);
+                    }
                 }
-                __syncwarp();
+                unsigned base = carry;
+                for (int t0 = 0; t0 < T; t0 += 32) {
+                    const int t = t0 + lane;
+                    const bool valid = t < T;
+                    const int ch = valid ? clist[t] : 0;
+                    int4 a0 = make_int4(0, 0, 0, 0), a1 = a0;
+                    if (valid) {
+                        int4* ap = reinterpret_cast<int4*>(area + ch * 8);
+                        a0 = ap[0];
+                        a1 = ap[1];
+                        ap[0] = make_int4(0, 0, 0, 0);
+                        ap[1] = make_int4(0, 0, 0, 0);
+                    }
+                    const unsigned csum = (unsigned)a0.x + (unsigned)a0.y + (unsigned)a0.z + (unsigned)a0.w +
+                                          (unsigned)a1.x + (unsigned)a1.y + (unsigned)a1.z + (unsigned)a1.w;
+                    const unsigned inc = warp_incl_sum_u(csum);
+                    unsigned run = base + inc - csum;
+                    base += __shfl_sync(FULL, inc, 31);
+                    const int av_v[8] = {(int)a0.x, (int)a0.y, (int)a0.z, (int)a0.w,
+                                         (int)a1.x, (int)a1.y, (int)a1.z, (int)a1.w};
+                    unsigned w0 = 0, w1 = 0;
+#pragma unroll
+                    for (int k = 0; k < 8; k++) {
+                        run += (unsigned)av_v[k];
+                        const unsigned v = (valid && ch * 8 + k < xend) ? resolve_cov(run, rule) : 0u;
+                        if (k < 4)
+                            w0 |= v << (8 * k);
+                        else
+                            w1 |= v << (8 * (k - 4));
+                    }
+                    // the gap after this chunk up to the next touched one holds `run`
+                    const int nxt = t + 1 < T ? (int)clist[t + 1] : nchunks;
+                    const unsigned gav = valid ? resolve_cov(run, rule) : 0u;
+                    const int g0 = ch * 8 + 8, g1 = min(nxt * 8, xend);
+                    const bool has_gap = gav && g0 < g1;
+                    auto nzb = [](unsigned w) { return (((w & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | w) & 0x80808080u; };
+                    const int cnt = __popc(nzb(w0)) + __popc(nzb(w1));
+                    const unsigned cinc = warp_incl_sum_u((unsigned)cnt);
+                    const int tot = (int)__shfl_sync(FULL, cinc, 31);
+                    const unsigned gm = __ballot_sync(FULL, has_gap);
+                    int pos = (int)(cinc - (unsigned)cnt);
+#pragma unroll
+                    for (int k = 0; k < 8; k++) {
+                        const unsigned v = ((k < 4 ? w0 : w1) >> (8 * (k & 3))) & 0xFFu;
+                        if (v) q[pos++] = ((unsigned)(ch * 8 + k) << 8) | v;
+                    }
+                    if (has_gap) q[256 + __popc(gm & lt)] = ((unsigned)g0 << 19) | ((unsigned)(g1 - g0) << 8) | gav;
+                    __syncwarp();
+                    for (int k = lane; k < tot; k += 32) {
+                        const unsigned e = q[k];
+                        compose((int)(e >> 8), e & 255u);
+                    }
+                    for (unsigned m = gm; m; m &= m - 1) {  // the gap runs, all lanes on each
+                        const unsigned e = q[256 + __popc(gm & ((1u << (__ffs(m) - 1)) - 1u))];
+                        const int gs = (int)(e >> 19), gl = (int)((e >> 8) & 0x7FF);
+                        for (int x = gs + lane; x < gs + gl; x += 32) compose(x, e & 255u);
+                    }
+                    __syncwarp();
+                }
             }
             G += __popc(rmask);
             if (G >= 0xC000) {  // keep the u16 call counts in range: pending counts saturate at 15

@@ -199,9 +199,9 @@ FT_API void ft_batch_destroy(ft_batch* batch);
  * split into row ranges, the queue grain of large paths (0 = 1 Mpx); `grid_per_sm`,
  * resident CTAs per SM of the persistent kernels (0 = occupancy maximum).
  * Ordered composites (ft_composite_batch, and single calls of at least split_px pixels):
- * `band_rows`, rows per band (1..8, 0 = built-in 8) — the height of a compositor tile;
- * `tile_w`, the width of an Rgba8p compositor tile in pixels (128, 256, 512 or 1024,
- * 0 = built-in 512); `pool_edges`, the first size of the binned-edge pool in edges (it
+ * `band_rows`, rows per band (1..8, 0 = built-in: 4 for Rgba8p, 8 for Matte8) — the
+ * height of a compositor tile; `tile_w`, the width of an Rgba8p compositor tile in pixels
+ * (128, 256, 512 or 1024, 0 = built-in: 1024, or the narrowest that needs no more tiles); `pool_edges`, the first size of the binned-edge pool in edges (it
  * grows on demand; 0 = built-in).  Host batches (ft_fill_batch with
  * FT_HOST): `host_chunks`, chunks of the copy pipeline (1..16, 0 = built-in: 2 from
  * 64 MB of rasters); `host_mapped`, 0 = page-locked Matte8 rasters are written and
