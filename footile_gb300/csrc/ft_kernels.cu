@@ -2143,8 +2143,8 @@ __host__ __device__ inline CTileLayout ctile_layout(int R, int sw) {
     o += R * sw * 4;
     L.queue = o;  // per warp: CT_QN queued pixels (x << 8 | alpha) and runs
     o += R * CT_QN * 4;
-    L.bmap = o;  // per warp: touched 8-pixel chunks, sw / 256 words, then the chunk list (sw / 8 bytes)
-    o += R * (sw / 256 * 4 + sw / 8);
+    L.bmap = o;  // per warp: touched 8-pixel chunks (one bit each), then the chunk list (a byte each)
+    o += R * (((sw / 8 + 31) / 32) * 4 + sw / 8);
     o = (o + 15) & ~15;
     L.last = o;  // per warp: sw u16, calls so far at each pixel's last cover
     o += R * sw * 2;
@@ -2240,8 +2240,8 @@ __global__ void __launch_bounds__(BLOCK, 4) k_ctile(KParams P, const __grid_cons
     const CTileLayout L = ctile_layout(R, sw);
     const int BW = sw < 256 ? sw : 256;  // TMA box width (pixels)
     const int bw_shift = BW == 256 ? 8 : 7;
-    const int nwords = sw >> 8;          // bitmap words (32 chunks of 8 pixels each)
-    const int nchunks = sw >> 3;
+    const int nchunks = sw >> 3;             // 8-pixel chunks of the segment
+    const int nwords = (nchunks + 31) >> 5;  // bitmap words
     unsigned char* ftab = smem;
     unsigned* tile = reinterpret_cast<unsigned*>(smem + L.tile);
     uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + L.mbar);
