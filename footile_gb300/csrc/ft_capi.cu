@@ -89,7 +89,7 @@ struct ft_ctx {
     int sm_count = 0;
     int max_smem = 0;
     uint32_t fig_cap = 0;  // vertices per figure of a fill above footile's 65,535 (0: footile's cap)
-    ft_tuning tune{0, 0, 0, 0, 0, 0, 0, 0, 0};
+    ft_tuning tune{0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     bool tuned = false;  // `tune` replaces the built-in plan defaults
     std::string err;
 };
@@ -599,7 +599,7 @@ FT_API void ft_batch_destroy(ft_batch* b) {
 FT_API int ft_set_tuning(ft_ctx* c, const ft_tuning* t) {
     if (!c) return FT_ERR_ARG;
     if (!t) {
-        c->tune = ft_tuning{0, 0, 0, 0, 0, 0, 0, 0, 0};
+        c->tune = ft_tuning{0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
         c->tuned = false;
         return FT_OK;
     }
@@ -607,7 +607,8 @@ FT_API int ft_set_tuning(ft_ctx* c, const ft_tuning* t) {
         (t->cta_smem_bytes && t->cta_smem_bytes < 40 * 1024) || t->cta_smem_bytes > c->max_smem ||
         t->split_px < 0 || t->grid_per_sm < 0 || t->band_rows < 0 || t->band_rows > ftk::NWARP ||
         t->pool_edges < 0 || t->host_chunks < 0 || t->host_chunks > 16 || t->host_mapped < 0 || t->host_mapped > 2 ||
-        (t->tile_w != 0 && t->tile_w != 128 && t->tile_w != 256 && t->tile_w != 512 && t->tile_w != 1024))
+        (t->tile_w != 0 && t->tile_w != 128 && t->tile_w != 256 && t->tile_w != 512 && t->tile_w != 1024) ||
+        t->tile_stage < 0 || t->tile_stage > 2)
         return fail(c, FT_ERR_ARG, "tuning out of range");
     c->tune = *t;
     c->tuned = true;
@@ -619,7 +620,7 @@ FT_API int ft_get_tuning(ft_ctx* c, ft_tuning* t) {
     if (c->tuned) {
         *t = c->tune;
     } else {
-        *t = ft_tuning{ftk::WARP_MAX_SIDE, 0, 1 << 20, 0, 0, 0, 0, 0, 0};
+        *t = ft_tuning{ftk::WARP_MAX_SIDE, 0, 1 << 20, 0, 0, 0, 0, 0, 0, 0};
     }
     return FT_OK;
 }
@@ -1028,7 +1029,9 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
     const int R = composite_band_rows(c, w, fmt);
     const int n_bands = (int)((h + R - 1) / R);
     const int tile_w = composite_tile_w(c, w);
-    const int smem_b = fmt == FT_MATTE8 ? ftk::composite_bands_smem(R, (int)w) : ftk::composite_tile_smem(R, tile_w);
+    const int stage = (c->tuned && c->tune.tile_stage > 0) ? c->tune.tile_stage : 1;
+    const int smem_b = fmt == FT_MATTE8 ? ftk::composite_bands_smem(R, (int)w)
+                                        : ftk::composite_tile_smem(R, tile_w, stage == 1);
     if (smem_b > c->max_smem) return fail(c, FT_ERR_CAP, "raster too wide for the band compositor");
     const int smem_a = choose_smem(c, 1);
     if ((size_t)(n_bands + 1) * sizeof(int) > (size_t)smem_a)
@@ -1118,7 +1121,7 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
                 CUtensorMap tm;
                 memset(&tm, 0, sizeof(tm));
                 p.seg_w = tile_w;
-                p.use_tma = canvas_tensor_map(&tm, ras_d, w, h, stride, std::min(tile_w, 256), R) ? 1 : 0;
+                p.use_tma = stage == 1 && canvas_tensor_map(&tm, ras_d, w, h, stride, std::min(tile_w, 256), R) ? 1 : 0;
                 FT_CU(cudaEventRecord(c->ev_comp, c->stream), "event");
                 FT_CU(ftk::launch_composite_tiles(p, tm, c->stream), "launch tile compositor");
                 c->comp_timed = true;
@@ -1195,9 +1198,10 @@ static bool tune_lookup(const char* path, const std::string& key, ft_tuning* t) 
         char k[600];
         ft_tuning v;
         float ms;
-        v = ft_tuning{0, 0, 0, 0, 0, 0, 0, 0, 0};
-        if (sscanf(line, "%599s %d %d %d %d %d %d %d %d %d %f", k, &v.warp_max_side, &v.cta_smem_bytes, &v.split_px,
-                   &v.grid_per_sm, &v.band_rows, &v.pool_edges, &v.host_chunks, &v.host_mapped, &v.tile_w, &ms) == 11 &&
+        v = ft_tuning{0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+        if (sscanf(line, "%599s %d %d %d %d %d %d %d %d %d %d %f", k, &v.warp_max_side, &v.cta_smem_bytes,
+                   &v.split_px, &v.grid_per_sm, &v.band_rows, &v.pool_edges, &v.host_chunks, &v.host_mapped,
+                   &v.tile_w, &v.tile_stage, &ms) == 12 &&
             key == k) {
             *t = v;  // the last entry for a key wins
             found = true;
@@ -1780,7 +1784,7 @@ FT_API int ft_autotune_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_o
     }
     if (ms_out) *ms_out = 0.0f;
     const std::string key = tune_key(c, stroke, rule, fmt, paths, n_paths);
-    ft_tuning best{0, 0, 0, 0, 0, 0, 0, 0, 0};
+    ft_tuning best{0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     if (tune_lookup(cache_path, key, &best) && ft_set_tuning(c, &best) == FT_OK) {
         if (chosen) *chosen = best;
         return FT_OK;
@@ -1803,7 +1807,7 @@ FT_API int ft_autotune_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_o
                 if (sm > c->max_smem) continue;
                 // the batch plan's knobs; the composite and host-transfer knobs stay as set
                 c->tune = ft_tuning{ws, sm, 1 << 20, gp, saved.band_rows, saved.pool_edges, saved.host_chunks,
-                                    saved.host_mapped, saved.tile_w};
+                                    saved.host_mapped, saved.tile_w, saved.tile_stage};
                 c->tuned = true;
                 ft_batch* b = nullptr;
                 if (ft_batch_create(c, stroke, rule, paths, n_paths, fmt, &b) != FT_OK) continue;
@@ -1837,9 +1841,9 @@ FT_API int ft_autotune_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_o
     if (cache_path) {
         FILE* f = fopen(cache_path, "a");
         if (f) {
-            fprintf(f, "%s %d %d %d %d %d %d %d %d %d %.4f\n", key.c_str(), best.warp_max_side, best.cta_smem_bytes,
-                    best.split_px, best.grid_per_sm, best.band_rows, best.pool_edges, best.host_chunks,
-                    best.host_mapped, best.tile_w, best_ms);
+            fprintf(f, "%s %d %d %d %d %d %d %d %d %d %d %.4f\n", key.c_str(), best.warp_max_side,
+                    best.cta_smem_bytes, best.split_px, best.grid_per_sm, best.band_rows, best.pool_edges,
+                    best.host_chunks, best.host_mapped, best.tile_w, best.tile_stage, best_ms);
             fclose(f);
         }
     }

@@ -2018,13 +2018,19 @@ __global__ void __launch_bounds__(BLOCK) k_cbuild(KParams P) {
     }
 }
 
+// The alpha-0 SrcOver of pix maps a premultiplied channel d to ch8_mul(d, 255), which
+// leaves d >= 16 unchanged: ftab[k][d] (d < 16) is d after k such composites.
+constexpr int FTAB_BYTES = 16 * 16;
 __device__ __forceinline__ unsigned ftab4(const unsigned char* ftab, unsigned d, int k) {
-    const unsigned char* t = ftab + (k << 8);
-    return (unsigned)t[d & 0xFF] | ((unsigned)t[(d >> 8) & 0xFF] << 8) | ((unsigned)t[(d >> 16) & 0xFF] << 16) |
-           ((unsigned)t[d >> 24] << 24);
+    const unsigned char* t = ftab + (k << 4);
+    unsigned out = 0;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const unsigned c = (d >> (8 * i)) & 0xFFu;
+        out |= (c < 16u ? (unsigned)t[c] : c) << (8 * i);
+    }
+    return out;
 }
-
-constexpr int FTAB_BYTES = 16 * 256;  // ftab[k][d]: d after k alpha-0 SrcOver composites
 
 // Per-warp shared memory of the Matte8 band compositor for rows of `width` pixels: the
 // row's i32 cell areas and its touched-span marks.
@@ -2131,12 +2137,13 @@ constexpr int CT_QN = 256 + 40;  // queued covered pixels of one round (32 chunk
 struct CTileLayout {
     int tile, mbar, area, last, queue, bmap, bytes;
 };
-__host__ __device__ inline CTileLayout ctile_layout(int R, int sw) {
+// Shared memory of a compositor CTA; `staged`: the canvas tile is held in shared memory.
+__host__ __device__ inline CTileLayout ctile_layout(int R, int sw, bool staged) {
     CTileLayout L;
     int o = FTAB_BYTES;
     o = (o + 127) & ~127;
     L.tile = o;  // R x sw canvas pixels, [box][row][box width]
-    o += R * sw * 4;
+    if (staged) o += R * sw * 4;
     L.mbar = o;
     o += 16;
     L.area = o;  // per warp: sw i32 cell areas
@@ -2146,9 +2153,9 @@ __host__ __device__ inline CTileLayout ctile_layout(int R, int sw) {
     L.bmap = o;  // per warp: touched 8-pixel chunks (one bit each), then the chunk list (a byte each)
     o += R * (((sw / 8 + 31) / 32) * 4 + sw / 8);
     o = (o + 15) & ~15;
-    L.last = o;  // per warp: sw u16, calls so far at each pixel's last cover
-    o += R * sw * 2;
-    L.bytes = o;
+    L.last = o;  // per warp: sw u8, calls so far (mod 256) at each pixel's last cover
+    o += R * sw;
+    L.bytes = (o + 15) & ~15;
     return L;
 }
 
@@ -2230,6 +2237,7 @@ __device__ __forceinline__ unsigned warp_sum_u(unsigned v) {
     return v;
 }
 
+template <bool STAGED>
 __global__ void __launch_bounds__(BLOCK, 4) k_ctile(KParams P, const __grid_constant__ CUtensorMap tmap) {
     extern __shared__ __align__(128) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -2237,7 +2245,7 @@ __global__ void __launch_bounds__(BLOCK, 4) k_ctile(KParams P, const __grid_cons
     const int nseg = (W + sw - 1) / sw;
     const int b = (int)blockIdx.x / nseg, x0 = ((int)blockIdx.x % nseg) * sw;
     const int r = b * R + warp;
-    const CTileLayout L = ctile_layout(R, sw);
+    const CTileLayout L = ctile_layout(R, sw, STAGED);
     const int BW = sw < 256 ? sw : 256;  // TMA box width (pixels)
     const int bw_shift = BW == 256 ? 8 : 7;
     const int nchunks = sw >> 3;             // 8-pixel chunks of the segment
@@ -2249,12 +2257,14 @@ __global__ void __launch_bounds__(BLOCK, 4) k_ctile(KParams P, const __grid_cons
     unsigned* q = reinterpret_cast<unsigned*>(smem + L.queue) + warp * CT_QN;
     unsigned* bmap = reinterpret_cast<unsigned*>(smem + L.bmap + warp * (nwords * 4 + nchunks));
     unsigned char* clist = reinterpret_cast<unsigned char*>(bmap + nwords);
-    unsigned short* last = reinterpret_cast<unsigned short*>(smem + L.last) + warp * sw;
-    // the tile pixel of this warp's row at segment position x
+    unsigned char* last = smem + L.last + warp * sw;
+    unsigned* crow = reinterpret_cast<unsigned*>(P.rasters + (size_t)r * P.canvas_stride) + x0;
+    // the canvas pixel of this warp's row at segment position x: in the shared tile
+    // (staged by TMA), or in place in global memory
     auto px = [&](int x) -> unsigned* {
-        return tile + (((x >> bw_shift) * R + warp) << bw_shift) + (x & (BW - 1));
+        return STAGED ? tile + (((x >> bw_shift) * R + warp) << bw_shift) + (x & (BW - 1)) : crow + x;
     };
-    const bool tma = P.use_tma != 0;
+    const bool tma = STAGED;
     if (tma && threadIdx.x == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -2272,16 +2282,13 @@ __global__ void __launch_bounds__(BLOCK, 4) k_ctile(KParams P, const __grid_cons
                 : "memory");
     }
     for (int i = threadIdx.x; i < FTAB_BYTES; i += blockDim.x) {
-        unsigned v = (unsigned)(i & 255);
-        for (int k = 0; k < (i >> 8); k++) v = ch8_mul(v, 255u);
+        unsigned v = (unsigned)(i & 15);
+        for (int k = 0; k < (i >> 4); k++) v = ch8_mul(v, 255u);
         ftab[i] = (unsigned char)v;
     }
     for (int x = lane * 4; x < sw; x += 128) *reinterpret_cast<int4*>(area + x) = make_int4(0, 0, 0, 0);
     for (int x = lane; x < sw; x += 32) last[x] = 0;
     if (lane < nwords) bmap[lane] = 0u;
-    unsigned* crow = reinterpret_cast<unsigned*>(P.rasters + (size_t)r * P.canvas_stride);
-    if (!tma && r < H)
-        for (int x = lane; x < sw && x0 + x < W; x += 32) *px(x) = crow[x0 + x];
     bool ok = true;
     if (tma) {
         ok = mbar_wait(mbar, 0);
@@ -2346,10 +2353,10 @@ __global__ void __launch_bounds__(BLOCK, 4) k_ctile(KParams P, const __grid_cons
                 auto compose = [&](int x, unsigned av) {
                     unsigned* p = px(x);
                     unsigned dv = *p;
-                    const int kk = min(Gj - (int)last[x], 15);
+                    const int kk = min((Gj - (int)last[x]) & 255, 15);
                     if (kk) dv = ftab4(ftab, dv, kk);
                     *p = srcover_rgba(dv, clr, av);
-                    last[x] = (unsigned short)(Gj + 1);
+                    last[x] = (unsigned char)(Gj + 1);
                 };
                 // the run before the first touched chunk holds the carry
                 {
@@ -2419,18 +2426,21 @@ __global__ void __launch_bounds__(BLOCK, 4) k_ctile(KParams P, const __grid_cons
                     __syncwarp();
                 }
             }
+            const int G0 = G;
             G += __popc(rmask);
-            if (G >= 0xC000) {  // keep the u16 call counts in range: pending counts saturate at 15
+            if ((G0 >> 6) != (G >> 6)) {
+                // every 64 calls: pending counts of 15 or more saturate, so a pixel's stamp
+                // moves up to 15 calls behind; the u8 differences then stay below 256
                 __syncwarp();
-                for (int x = lane; x < sw; x += 32) last[x] = last[x] > 0x8000 ? (unsigned short)(last[x] - 0x8000) : 0;
-                G -= 0x8000;
+                for (int x = lane; x < sw; x += 32)
+                    if (((G - (int)last[x]) & 255) > 15) last[x] = (unsigned char)(G - 15);
                 __syncwarp();
             }
         }
         // the alpha-0 composites still pending since each pixel's last cover
         __syncwarp();
-        for (int x = lane; x < sw; x += 32) {
-            const int kk = min(G - (int)last[x], 15);
+        for (int x = lane; x < xend; x += 32) {
+            const int kk = min((G - (int)last[x]) & 255, 15);
             if (kk) {
                 unsigned* p = px(x);
                 *p = ftab4(ftab, *p, kk);
@@ -2449,21 +2459,19 @@ __global__ void __launch_bounds__(BLOCK, 4) k_ctile(KParams P, const __grid_cons
             asm volatile("cp.async.bulk.commit_group;" ::: "memory");
             asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
         }
-    } else {
-        __syncwarp();
-        if (r < H)
-            for (int x = lane; x < sw && x0 + x < W; x += 32) crow[x0 + x] = *px(x);
     }
 }
 
-int composite_tile_smem(int band_rows, int seg_w) { return ctile_layout(band_rows, seg_w).bytes; }
+int composite_tile_smem(int band_rows, int seg_w, bool staged) { return ctile_layout(band_rows, seg_w, staged).bytes; }
 
 cudaError_t launch_composite_tiles(const KParams& p, const CUtensorMap& tmap, cudaStream_t s) {
-    const int smem = composite_tile_smem(p.band_rows, p.seg_w);
-    cudaError_t e = cudaFuncSetAttribute(k_ctile, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    const bool staged = p.use_tma != 0;
+    const int smem = composite_tile_smem(p.band_rows, p.seg_w, staged);
+    auto kern = staged ? k_ctile<true> : k_ctile<false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     const int nseg = ((int)p.canvas_w + p.seg_w - 1) / p.seg_w;
-    k_ctile<<<p.n_bands * nseg, 32 * p.band_rows, smem, s>>>(p, tmap);
+    kern<<<p.n_bands * nseg, 32 * p.band_rows, smem, s>>>(p, tmap);
     return cudaGetLastError();
 }
 

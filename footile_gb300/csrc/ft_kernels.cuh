@@ -154,7 +154,7 @@ cudaError_t launch_composite_build(const KParams& p, int grid, int smem_bytes, c
 cudaError_t launch_composite_bands(const KParams& p, int smem_bytes, cudaStream_t s);
 // Rgba8p: tiles of band_rows x seg_w pixels, canvas staged through `tmap` when use_tma.
 cudaError_t launch_composite_tiles(const KParams& p, const CUtensorMap& tmap, cudaStream_t s);
-int composite_tile_smem(int band_rows, int seg_w);
+int composite_tile_smem(int band_rows, int seg_w, bool staged);
 // Edges and band bins of a single path's figure (after k_cbuild with split_bin), over
 // the whole GPU: edge records and band counts, a scan and pool allocation, the fill.
 cudaError_t launch_figure_bins(const KParams& p, int grid, cudaStream_t s);

@@ -201,7 +201,10 @@ FT_API void ft_batch_destroy(ft_batch* batch);
  * Ordered composites (ft_composite_batch, and single calls of at least split_px pixels):
  * `band_rows`, rows per band (1..8, 0 = built-in: 4 for Rgba8p, 8 for Matte8) — the
  * height of a compositor tile; `tile_w`, the width of an Rgba8p compositor tile in pixels
- * (128, 256, 512 or 1024, 0 = built-in: 1024, or the narrowest that needs no more tiles); `pool_edges`, the first size of the binned-edge pool in edges (it
+ * (128, 256, 512 or 1024, 0 = built-in: 1024, or the narrowest that needs no more tiles);
+ * `tile_stage`, how an Rgba8p compositor tile reaches the canvas: 1 = staged in shared
+ * memory by TMA (when the canvas base and row stride are 16-byte aligned), 2 = read and
+ * written in place, 0 = built-in; `pool_edges`, the first size of the binned-edge pool in edges (it
  * grows on demand; 0 = built-in).  Host batches (ft_fill_batch with
  * FT_HOST): `host_chunks`, chunks of the copy pipeline (1..16, 0 = built-in: 2 from
  * 64 MB of rasters); `host_mapped`, 0 = page-locked Matte8 rasters are written and
@@ -218,6 +221,7 @@ typedef struct ft_tuning {
     int32_t host_chunks;
     int32_t host_mapped;
     int32_t tile_w;
+    int32_t tile_stage;
 } ft_tuning;
 FT_API int ft_set_tuning(ft_ctx* ctx, const ft_tuning* tuning);
 FT_API int ft_get_tuning(ft_ctx* ctx, ft_tuning* tuning);
