@@ -2187,12 +2187,27 @@ __device__ __forceinline__ void seg_row(int x_bot, int inv, bool st, bool en, in
     const int ccov = en ? pixel_cov(fl) : 256;
     const int cov = st ? ccov - pixel_cov(fu) : ccov;
     if (cov <= 0) return;
+    const int s1 = min(s0 + sw, W);
+    {
+        // quick bounds: the item's x-range lies between x_bot and x_bot - inv (when that
+        // does not wrap, neither do the exact ends below)
+        const long long xa = (long long)x_bot - inv;
+        if (xa == (long long)(int)xa) {
+            const int lo = (int)(min((long long)x_bot, xa) >> 16), hi = (int)(max((long long)x_bot, xa) >> 16);
+            if (lo >= s1) return;  // right of the segment: nothing here, nothing carried in
+            // left of it, its walk complete before s0 (first + j * step >= ONE for every
+            // cell left of the segment from any start <= hi): it leaves its whole coverage
+            if (s0 - 1 - hi > 0 && (long long)(s0 - 1 - hi) * step >= FX_ONE) {
+                carry += (unsigned)(ed * cov);
+                return;
+            }
+        }
+    }
     const int x0 = st ? wsub(x_bot, fxmul(inv, wsub(FX_ONE, fu))) : wsub(x_bot, inv);
     const int x1 = en ? wsub(x_bot, fxmul(inv, fl ? FX_ONE - fl : 0)) : x_bot;
     const int mnx = min(x0, x1), mxx = max(x0, x1);
     const int minp = mnx >> 16, maxp = mxx >> 16;
     if (minp >= W) return;
-    const int s1 = min(s0 + sw, W);
     if (minp >= s1) return;  // right of the segment: nothing here, nothing carried in
     const int full = cov << 8;
     const int r = (minp == maxp) ? fxmul(wsub(FX_ONE, fxfract(fxavg(mxx, mnx))), full)
@@ -2333,8 +2348,8 @@ __global__ void __launch_bounds__(BLOCK, 4) k_ctile(KParams P, const __grid_cons
                 const int4* E = reinterpret_cast<const int4*>(P.pool + first);
                 for (int e = lane; e < ne; e += 32) {
                     const int4 hb = E[2 * e + 1];  // step_pix, ed, start_row, end_row
+                    const int4 ha = E[2 * e];      // y_upper, y_lower, x_bot0, inv_slope
                     if (y < hb.z || y > hb.w) continue;
-                    const int4 ha = E[2 * e];  // y_upper, y_lower, x_bot0, inv_slope
                     const int x_bot = wadd(ha.z, wmul(y - hb.z, ha.w));
                     seg_row(x_bot, ha.w, y == hb.z, y == hb.w, fxfract(ha.x), fxfract(ha.y), hb.x > 0 ? hb.x : FX_ONE,
                             hb.y, area, x0, sw, W, carry, bmap);
