@@ -144,6 +144,25 @@ def extra_scene(ctx, stream, dev, cpu=True):
     ctx.set_figure_cap(0)
     # composite bytes: every Rgba8p pixel from the top row down is read and written
     out["rgba8p_composite_GBps"] = (w * h * 8) / (out["nonzero_rgba8p_ms"] * 1e-3) / 1e9
+    # the tile compositor alone (after the figure build and binning), canvas tiles staged in
+    # shared memory by TMA, and composited in place for comparison; roofline: 8 B per
+    # pixel (RGBA read and write) over the rows the call composites
+    peak, peak_kind = measured_peak_hbm()
+    comp = {}
+    for name, stage in (("tma_staged", 1), ("in_place", 2)):
+        ctx.tune(tile_stage=stage)
+        fill(_abi.NONZERO, _abi.RGBA8P, r_d, 4 * w)
+        t = []
+        for _ in range(10):
+            fill(_abi.NONZERO, _abi.RGBA8P, r_d, 4 * w)
+            t.append(ctx.last_composite_ms())
+        cms = float(np.median(t))
+        comp[name] = {"ms": cms, "GBps": (w * h * 8) / (cms * 1e-3) / 1e9,
+                      "frac_of_hbm": (w * h * 8) / (cms * 1e-3) / 1e9 / peak}
+    ctx.set_tuning(None)
+    out["rgba8p_tile_compositor"] = dict(comp, bytes=w * h * 8, peak=peak, peak_kind=peak_kind,
+                                         tile=f"{ctx.tuning()['band_rows'] or 4} rows x "
+                                              f"{ctx.tuning()['tile_w'] or 1024} px")
     # pix's Rgba8p -> SRgba8 step of footile's examples, on the device (HBM-bound):
     # the 4096x4096 raster, and an 8192x8192 one whose 512 MB of traffic is far above L2
     s_d = torch.empty_like(r_d)
