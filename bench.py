@@ -144,12 +144,14 @@ def extra_scene(ctx, stream, dev, cpu=True):
     ctx.set_figure_cap(0)
     # composite bytes: every Rgba8p pixel from the top row down is read and written
     out["rgba8p_composite_GBps"] = (w * h * 8) / (out["nonzero_rgba8p_ms"] * 1e-3) / 1e9
-    # the tile compositor alone (after the figure build and binning), canvas tiles staged in
-    # shared memory by TMA, and composited in place for comparison; roofline: 8 B per
-    # pixel (RGBA read and write) over the rows the call composites
+    # the compositing step alone (after the figure build and binning): by default the
+    # call's coverage goes to a Matte8 mask and SrcOver streams canvas and mask through
+    # shared memory by TMA; beside it the tile compositor (coverage and SrcOver fused),
+    # TMA-staged and in place.  Roofline: 8 B per pixel (RGBA read and write; the mask
+    # read adds 1 B) over the rows the call composites
     peak, peak_kind = measured_peak_hbm()
     comp = {}
-    for name, stage in (("tma_staged", 1), ("in_place", 2)):
+    for name, stage in (("mask_then_tma_stream", 0), ("tile_tma_staged", 1), ("tile_in_place", 2)):
         ctx.tune(tile_stage=stage)
         fill(_abi.NONZERO, _abi.RGBA8P, r_d, 4 * w)
         t = []

@@ -74,6 +74,7 @@ struct ft_ctx {
     DevBuf ops, paths, overflow, status, sw_out, rasters, queue, scratch, sw_chain;
     DevBuf pool, pool_used, bandoff, crec;  // ordered composite
     DevBuf figbins;                         // one path's figure state and band counts (split binning)
+    DevBuf mask;                            // a single large Rgba8p call's Matte8 coverage
     DevBuf srgb_lut, conv_src, conv_dst;    // ft_convert
     PlanSlot plan;                                   // the last batch's plan
     std::vector<std::unique_ptr<PlanSlot>> chunk_plans;  // host batches in pipelined chunks
@@ -658,7 +659,7 @@ FT_API void ft_ctx_destroy(ft_ctx* c) {
     DevBuf* bufs[] = {&c->ops,     &c->paths,   &c->overflow,
                       &c->status,  &c->sw_out,  &c->rasters, &c->queue,   &c->scratch,
                       &c->sw_chain, &c->pool,   &c->pool_used, &c->bandoff, &c->crec,
-                      &c->srgb_lut, &c->conv_src, &c->conv_dst, &c->figbins};
+                      &c->srgb_lut, &c->conv_src, &c->conv_dst, &c->figbins, &c->mask};
     for (DevBuf* b : bufs) b->release();
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev_comp) cudaEventDestroy(c->ev_comp);
@@ -959,7 +960,7 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
 // of box_w x box_h pixels, through the runtime's driver entry point; false when the
 // canvas does not allow one (TMA wants a 16-byte aligned base and row stride).
 static bool canvas_tensor_map(CUtensorMap* tm, void* base, uint32_t w, uint32_t h, uint32_t stride, int box_w,
-                              int box_h) {
+                              int box_h, bool bytes = false) {
     static EncodeTiledFn encode = nullptr;
     static std::once_flag once;
     std::call_once(once, [] {
@@ -977,7 +978,8 @@ static bool canvas_tensor_map(CUtensorMap* tm, void* base, uint32_t w, uint32_t 
     const cuuint64_t strides[1] = {stride};
     const cuuint32_t box[2] = {(cuuint32_t)box_w, (cuuint32_t)box_h};
     const cuuint32_t elem[2] = {1, 1};
-    return encode(tm, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, base, dims, strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE,
+    return encode(tm, bytes ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, base, dims, strides,
+                  box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE,
                   CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
@@ -1108,14 +1110,45 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
             }
         }
         unsigned long long used = 0;
+        int4 cr0 = make_int4(0, 0, 0, 0);  // a single call's first raster row, binned edges
         FT_CU(cudaMemcpyAsync(&used, c->pool_used.p, sizeof(used), cudaMemcpyDeviceToHost, c->stream), "pool size");
+        if (n_paths == 1)
+            FT_CU(cudaMemcpyAsync(&cr0, c->crec.p, sizeof(int4), cudaMemcpyDeviceToHost, c->stream), "path record");
         FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
         if (used > p.pool_cap) {
             want = used + used / 4;
             continue;
         }
         if (n_paths && n_bands) {
-            if (fmt == FT_MATTE8) {
+            // a single Rgba8p call: its Matte8 coverage into a mask (the band compositor), then
+            // SrcOver from the mask, canvas and mask streamed through shared memory by TMA
+            const uint32_t mstride = (w + 15) & ~15u;
+            const int smem_m = ftk::composite_bands_smem(R, (int)w);
+            bool streamed = false;
+            if (fmt == FT_RGBA8P && n_paths == 1 && !(c->tuned && c->tune.tile_stage > 0) && smem_m <= c->max_smem) {
+                FT_CU(c->mask.ensure((size_t)mstride * h), "alloc mask");
+                CUtensorMap tc, tmk;
+                if (canvas_tensor_map(&tc, ras_d, w, h, stride, 256, 16) &&
+                    canvas_tensor_map(&tmk, c->mask.p, w, h, mstride, 256, 16, true)) {
+                    ftk::KParams pm = p;
+                    pm.rasters = static_cast<uint8_t*>(c->mask.p);
+                    pm.canvas_stride = mstride;
+                    pm.fmt = FT_MATTE8;
+                    FT_CU(ftk::launch_composite_bands(pm, smem_m, c->stream), "launch band compositor");
+                    const uint8_t* k = paths[0].clr;
+                    const unsigned clr = (unsigned)k[0] | ((unsigned)k[1] << 8) | ((unsigned)k[2] << 16) |
+                                         ((unsigned)k[3] << 24);
+                    FT_CU(cudaEventRecord(c->ev_comp, c->stream), "event");
+                    FT_CU(ftk::launch_srcover_mask(tc, tmk, (int)w, (int)h, std::min(cr0.x, (int)h), clr, p.status,
+                                                   c->sm_count, c->stream),
+                          "launch mask compositor");
+                    c->comp_timed = true;
+                    c->launches++;
+                    streamed = true;
+                }
+            }
+            if (streamed) {
+            } else if (fmt == FT_MATTE8) {
                 FT_CU(ftk::launch_composite_bands(p, smem_b, c->stream), "launch band compositor");
             } else {
                 CUtensorMap tm;

@@ -2477,6 +2477,124 @@ __global__ void __launch_bounds__(BLOCK, 4) k_ctile(KParams P, const __grid_cons
     }
 }
 
+// ===========================================================================
+// SrcOver of one call from its coverage mask (single large Rgba8p calls).
+//
+// footile's rasterize_row composites every pixel of the call's rows from its top row down
+// with the row's coverage (fig.rs:637-643; alpha 0 where nothing covers).  With the
+// call's Matte8 coverage already in a mask (the band compositor writes it), this pass
+// streams the canvas and the mask through shared memory by TMA: per tile of 16 rows x
+// 256 pixels, a 2-D tensor load of the canvas (u32 pixels) and of the mask (bytes)
+// completing on the stage's mbarrier, SrcOver in place, a 2-D tensor store; four stages
+// per CTA keep loads, compute and stores in flight together.  A pixel with coverage 0
+// takes the alpha-0 map, which changes only channel values 1..15: the common case of no
+// such channel leaves the pixel as it is.
+
+constexpr int SO_ROWS = 16, SO_COLS = 256, SO_STAGES = 4;
+constexpr int SO_CANVAS_BYTES = SO_ROWS * SO_COLS * 4, SO_MASK_BYTES = SO_ROWS * SO_COLS;
+constexpr int SO_STAGE_BYTES = SO_CANVAS_BYTES + SO_MASK_BYTES;
+constexpr int SO_SMEM = SO_STAGES * SO_STAGE_BYTES + 128;
+
+__global__ void __launch_bounds__(BLOCK, 2) k_srcover_mask(const __grid_constant__ CUtensorMap tm_canvas,
+                                                            const __grid_constant__ CUtensorMap tm_mask, int W, int H,
+                                                            int r0, unsigned clr, int32_t* status) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + SO_STAGES * SO_STAGE_BYTES);
+    const int tx = (W + SO_COLS - 1) / SO_COLS, ty = (H - r0 + SO_ROWS - 1) / SO_ROWS;
+    const int ntiles = tx * ty;
+    const int tid = threadIdx.x;
+    const uint64_t cmap = reinterpret_cast<uint64_t>(&tm_canvas), mmap = reinterpret_cast<uint64_t>(&tm_mask);
+    auto canvas_s = [&](int st) { return reinterpret_cast<unsigned*>(smem + st * SO_STAGE_BYTES); };
+    auto mask_s = [&](int st) { return smem + st * SO_STAGE_BYTES + SO_CANVAS_BYTES; };
+    auto load = [&](int t, int st) {  // thread 0: the tile's canvas and mask into stage st
+        const int x = (t % tx) * SO_COLS, y = r0 + (t / tx) * SO_ROWS;
+        const unsigned mb = smem_u32(full + st);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(SO_STAGE_BYTES)
+                     : "memory");
+        asm volatile(
+            "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+            "[%4];" ::"r"(smem_u32(canvas_s(st))),
+            "l"(cmap), "r"(x), "r"(y), "r"(mb)
+            : "memory");
+        asm volatile(
+            "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+            "[%4];" ::"r"(smem_u32(mask_s(st))),
+            "l"(mmap), "r"(x), "r"(y), "r"(mb)
+            : "memory");
+    };
+    if (tid == 0) {
+        for (int st = 0; st < SO_STAGES; st++)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(full + st)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    // this CTA's tiles: blockIdx.x, blockIdx.x + gridDim.x, ...
+    const int mine = ntiles > (int)blockIdx.x ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    if (tid == 0)
+        for (int k = 0; k < SO_STAGES && k < mine; k++) load((int)blockIdx.x + k * (int)gridDim.x, k);
+    bool ok = true;
+    for (int k = 0; k < mine && ok; k++) {
+        const int st = k % SO_STAGES;
+        const unsigned parity = (unsigned)((k / SO_STAGES) & 1);
+        ok = mbar_wait(full + st, parity);
+        if (!ok) {
+            if (tid == 0) atomicMax(status, FT_ERR_TIMEOUT);
+            break;
+        }
+        unsigned* cv = canvas_s(st);
+        const unsigned* mk = reinterpret_cast<const unsigned*>(mask_s(st));
+        // four pixels per step: one mask word, four canvas words
+        for (int i = tid; i < SO_ROWS * SO_COLS / 4; i += BLOCK) {
+            const unsigned m4 = mk[i];
+            uint4 d = reinterpret_cast<uint4*>(cv)[i];
+            unsigned dv[4] = {d.x, d.y, d.z, d.w};
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const unsigned av = (m4 >> (8 * j)) & 0xFFu;
+                const unsigned v = dv[j];
+                if (av) {
+                    dv[j] = srcover_rgba(v, clr, av);
+                } else {
+                    // channels in 1..15: nonzero bytes whose high nibble is zero
+                    const unsigned nz = (((v & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | v) & 0x80808080u;
+                    const unsigned hi = (((v & 0x70707070u) + 0x70707070u) | v) & 0x80808080u;
+                    if (nz & ~hi) dv[j] = srcover_rgba(v, clr, 0u);
+                }
+            }
+            reinterpret_cast<uint4*>(cv)[i] = make_uint4(dv[0], dv[1], dv[2], dv[3]);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            const int t = (int)blockIdx.x + k * (int)gridDim.x;
+            asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group [%0, {%1, %2}], [%3];" ::"l"(cmap),
+                         "r"((t % tx) * SO_COLS), "r"(r0 + (t / tx) * SO_ROWS), "r"(smem_u32(cv))
+                         : "memory");
+            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+            // the stage of tile k - 1 is free once its store has read it: reload it
+            if (k >= 1 && k - 1 + SO_STAGES < mine) {
+                asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+                load((int)blockIdx.x + (k - 1 + SO_STAGES) * (int)gridDim.x, (k - 1) % SO_STAGES);
+            }
+        }
+    }
+    if (tid == 0) {
+        // the last tile's stage was not reloaded (k - 1 + STAGES >= mine for it)
+        asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+    }
+}
+
+cudaError_t launch_srcover_mask(const CUtensorMap& canvas, const CUtensorMap& mask, int W, int H, int r0,
+                                unsigned clr, int32_t* status, int sm_count, cudaStream_t s) {
+    cudaError_t e = cudaFuncSetAttribute(k_srcover_mask, cudaFuncAttributeMaxDynamicSharedMemorySize, SO_SMEM);
+    if (e != cudaSuccess) return e;
+    const int ntiles = ((W + SO_COLS - 1) / SO_COLS) * ((H - r0 + SO_ROWS - 1) / SO_ROWS);
+    if (ntiles <= 0) return cudaSuccess;
+    const int grid = std::max(1, std::min(ntiles, 2 * sm_count));
+    k_srcover_mask<<<grid, BLOCK, SO_SMEM, s>>>(canvas, mask, W, H, r0, clr, status);
+    return cudaGetLastError();
+}
+
 int composite_tile_smem(int band_rows, int seg_w, bool staged) { return ctile_layout(band_rows, seg_w, staged).bytes; }
 
 cudaError_t launch_composite_tiles(const KParams& p, const CUtensorMap& tmap, cudaStream_t s) {

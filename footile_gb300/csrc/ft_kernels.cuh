@@ -155,6 +155,10 @@ cudaError_t launch_composite_bands(const KParams& p, int smem_bytes, cudaStream_
 // Rgba8p: tiles of band_rows x seg_w pixels, canvas staged through `tmap` when use_tma.
 cudaError_t launch_composite_tiles(const KParams& p, const CUtensorMap& tmap, cudaStream_t s);
 int composite_tile_smem(int band_rows, int seg_w, bool staged);
+// SrcOver of one call's colour onto the canvas rows r0.. from its Matte8 coverage `mask`
+// (both as 2-D tensor maps with boxes of 256 x 16), streamed by TMA.
+cudaError_t launch_srcover_mask(const CUtensorMap& canvas, const CUtensorMap& mask, int W, int H, int r0,
+                                unsigned clr, int32_t* status, int sm_count, cudaStream_t s);
 // Edges and band bins of a single path's figure (after k_cbuild with split_bin), over
 // the whole GPU: edge records and band counts, a scan and pool allocation, the fill.
 cudaError_t launch_figure_bins(const KParams& p, int grid, cudaStream_t s);

@@ -258,3 +258,31 @@ def test_scene_4096_rgba8p(ctx, stroke, init_kind):
                                                 init=init)
     assert err is None and st_o == 0
     assert_same(got, want, f"scene Rgba8p stroke={stroke} ({init_kind} canvas)")
+
+
+@pytest.mark.parametrize("stage", [0, 1, 2])
+def test_large_rgba8p_compositing_paths(ctx, stage):
+    """A single Rgba8p call of at least 1 Mpx is composited from its Matte8 coverage by the
+    TMA streaming pass (stage 0, built-in), or by the tile compositor with its tile staged
+    by TMA (1) or in place (2); all give the oracle's bytes, on random canvas bytes."""
+    ctx.tune(tile_stage=stage)
+    rng = np.random.default_rng(50 + stage)
+    w, h = 1280, 1000
+    ops = workloads.random_path(rng, 1280, 300, n_sub=3)
+    init = rng.integers(0, 256, (h, w, 4)).astype(np.uint8)
+    got, want, st_o, _, err = gpu_vs_oracle(ctx, ops, w, h, fmt=_abi.RGBA8P, clr=(30, 10, 5, 120), init=init,
+                                            rule=_abi.EVENODD)
+    assert err is None
+    assert_same(got, want, f"stage {stage}")
+
+
+def test_large_rgba8p_unaligned_rows(ctx):
+    """Rows 4,004 bytes apart admit no TMA tensor map: the single large call is composited
+    in place by the tile compositor."""
+    rng = np.random.default_rng(61)
+    w, h = 1001, 1100
+    ops = workloads.random_path(rng, 1100, 200, n_sub=2)
+    init = rng.integers(0, 256, (h, w, 4)).astype(np.uint8)
+    got, want, _, _, err = gpu_vs_oracle(ctx, ops, w, h, fmt=_abi.RGBA8P, clr=(9, 200, 14, 230), init=init)
+    assert err is None
+    assert_same(got, want, "unaligned rows")
