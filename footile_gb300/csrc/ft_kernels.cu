@@ -2490,16 +2490,34 @@ __global__ void __launch_bounds__(BLOCK, 4) k_ctile(KParams P, const __grid_cons
 // takes the alpha-0 map, which changes only channel values 1..15: the common case of no
 // such channel leaves the pixel as it is.
 
-constexpr int SO_ROWS = 16, SO_COLS = 256, SO_STAGES = 4;
+constexpr int SO_ROWS = 16, SO_COLS = 256, SO_STAGES = 3;
 constexpr int SO_CANVAS_BYTES = SO_ROWS * SO_COLS * 4, SO_MASK_BYTES = SO_ROWS * SO_COLS;
 constexpr int SO_STAGE_BYTES = SO_CANVAS_BYTES + SO_MASK_BYTES;
-constexpr int SO_SMEM = SO_STAGES * SO_STAGE_BYTES + 128;
+constexpr int SO_SMEM = SO_STAGES * SO_STAGE_BYTES + 128 + 1024;
 
-__global__ void __launch_bounds__(BLOCK, 2) k_srcover_mask(const __grid_constant__ CUtensorMap tm_canvas,
+// ch8_mul(d, b) of the four channels of d, b's 12-bit expansion (b << 4 | b >> 4) given
+__device__ __forceinline__ unsigned ch8_mul4(unsigned d, unsigned bx) {
+    unsigned out = 0;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        const unsigned dc = (d >> (8 * c)) & 0xFFu;
+        out |= ((((dc << 4) | (dc >> 4)) * bx) >> 16) << (8 * c);
+    }
+    return out;
+}
+
+__global__ void __launch_bounds__(BLOCK, 3) k_srcover_mask(const __grid_constant__ CUtensorMap tm_canvas,
                                                             const __grid_constant__ CUtensorMap tm_mask, int W, int H,
                                                             int r0, unsigned clr, int32_t* status) {
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + SO_STAGES * SO_STAGE_BYTES);
+    // src[a]: the colour's four channels times coverage a (pix's ch8_mul), packed; its
+    // alpha byte is the SrcOver's source alpha
+    unsigned* src = reinterpret_cast<unsigned*>(smem + SO_STAGES * SO_STAGE_BYTES + 128);
+    {
+        const unsigned a = threadIdx.x & 255u;
+        src[a] = ch8_mul4(clr, (a << 4) | (a >> 4));
+    }
     const int tx = (W + SO_COLS - 1) / SO_COLS, ty = (H - r0 + SO_ROWS - 1) / SO_ROWS;
     const int ntiles = tx * ty;
     const int tid = threadIdx.x;
@@ -2552,14 +2570,16 @@ __global__ void __launch_bounds__(BLOCK, 2) k_srcover_mask(const __grid_constant
             for (int j = 0; j < 4; j++) {
                 const unsigned av = (m4 >> (8 * j)) & 0xFFu;
                 const unsigned v = dv[j];
-                if (av) {
-                    dv[j] = srcover_rgba(v, clr, av);
-                } else {
-                    // channels in 1..15: nonzero bytes whose high nibble is zero
+                if (!av) {
+                    // alpha 0: only channels in 1..15 change (nonzero bytes, high nibble zero)
                     const unsigned nz = (((v & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | v) & 0x80808080u;
                     const unsigned hi = (((v & 0x70707070u) + 0x70707070u) | v) & 0x80808080u;
-                    if (nz & ~hi) dv[j] = srcover_rgba(v, clr, 0u);
+                    if (!(nz & ~hi)) continue;
                 }
+                // pix SrcOver: clr * a + d * (255 - clr_alpha * a), channel by channel
+                const unsigned s4 = src[av];
+                const unsigned inv = 255u - (s4 >> 24);
+                dv[j] = __vaddus4(s4, ch8_mul4(v, (inv << 4) | (inv >> 4)));
             }
             reinterpret_cast<uint4*>(cv)[i] = make_uint4(dv[0], dv[1], dv[2], dv[3]);
         }
@@ -2590,7 +2610,7 @@ cudaError_t launch_srcover_mask(const CUtensorMap& canvas, const CUtensorMap& ma
     if (e != cudaSuccess) return e;
     const int ntiles = ((W + SO_COLS - 1) / SO_COLS) * ((H - r0 + SO_ROWS - 1) / SO_ROWS);
     if (ntiles <= 0) return cudaSuccess;
-    const int grid = std::max(1, std::min(ntiles, 2 * sm_count));
+    const int grid = std::max(1, std::min(ntiles, 3 * sm_count));
     k_srcover_mask<<<grid, BLOCK, SO_SMEM, s>>>(canvas, mask, W, H, r0, clr, status);
     return cudaGetLastError();
 }
