@@ -1128,8 +1128,8 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
             if (fmt == FT_RGBA8P && n_paths == 1 && !(c->tuned && c->tune.tile_stage > 0) && smem_m <= c->max_smem) {
                 FT_CU(c->mask.ensure((size_t)mstride * h), "alloc mask");
                 CUtensorMap tc, tmk;
-                if (canvas_tensor_map(&tc, ras_d, w, h, stride, 256, 16) &&
-                    canvas_tensor_map(&tmk, c->mask.p, w, h, mstride, 256, 16, true)) {
+                if (canvas_tensor_map(&tc, ras_d, w, h, stride, ftk::SO_COLS, ftk::SO_ROWS) &&
+                    canvas_tensor_map(&tmk, c->mask.p, w, h, mstride, ftk::SO_COLS, ftk::SO_ROWS, true)) {
                     ftk::KParams pm = p;
                     pm.rasters = static_cast<uint8_t*>(c->mask.p);
                     pm.canvas_stride = mstride;

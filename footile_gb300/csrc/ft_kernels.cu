@@ -2163,10 +2163,13 @@ __device__ __forceinline__ unsigned smem_u32(const void* p) {
     return (unsigned)__cvta_generic_to_shared(p);
 }
 
-// Bounded wait on an mbarrier phase; false when it did not complete.
+// Wait on an mbarrier phase for at most about 0.2 s of GPU time (the global timer);
+// false when it did not complete.
 __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, unsigned parity) {
     const unsigned a = smem_u32(mbar);
-    for (int it = 0; it < (1 << 24); it++) {
+    unsigned long long t0;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    for (int it = 0; it < (1 << 22); it++) {
         unsigned done;
         asm volatile(
             "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
@@ -2174,6 +2177,11 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, unsigned parity) {
             : "r"(a), "r"(parity)
             : "memory");
         if (done) return true;
+        if ((it & 255) == 255) {
+            unsigned long long t;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+            if (t - t0 > 200000000ull) break;
+        }
     }
     return false;
 }
@@ -2305,11 +2313,9 @@ __global__ void __launch_bounds__(BLOCK, 4) k_ctile(KParams P, const __grid_cons
     for (int x = lane; x < sw; x += 32) last[x] = 0;
     if (lane < nwords) bmap[lane] = 0u;
     bool ok = true;
-    if (tma) {
-        ok = mbar_wait(mbar, 0);
-        if (!ok && threadIdx.x == 0) atomicMax(&P.status[0], FT_ERR_TIMEOUT);
-    }
-    __syncthreads();
+    if (tma) ok = mbar_wait(mbar, 0);
+    ok = __syncthreads_and(ok) != 0;
+    if (!ok && threadIdx.x == 0) atomicMax(&P.status[0], FT_ERR_TIMEOUT);
     if (ok && r < H) {
         const int n = (int)P.n_items, rule = P.rule;
         const unsigned lt = (1u << lane) - 1u;
@@ -2490,7 +2496,7 @@ __global__ void __launch_bounds__(BLOCK, 4) k_ctile(KParams P, const __grid_cons
 // takes the alpha-0 map, which changes only channel values 1..15: the common case of no
 // such channel leaves the pixel as it is.
 
-constexpr int SO_ROWS = 16, SO_COLS = 256, SO_STAGES = 3;
+constexpr int SO_STAGES = 3;  // SO_ROWS x SO_COLS tiles: ft_kernels.cuh (the host's tensor-map boxes)
 constexpr int SO_CANVAS_BYTES = SO_ROWS * SO_COLS * 4, SO_MASK_BYTES = SO_ROWS * SO_COLS;
 constexpr int SO_STAGE_BYTES = SO_CANVAS_BYTES + SO_MASK_BYTES;
 constexpr int SO_SMEM = SO_STAGES * SO_STAGE_BYTES + 128 + 1024;
@@ -2554,7 +2560,7 @@ __global__ void __launch_bounds__(BLOCK, 3) k_srcover_mask(const __grid_constant
     for (int k = 0; k < mine && ok; k++) {
         const int st = k % SO_STAGES;
         const unsigned parity = (unsigned)((k / SO_STAGES) & 1);
-        ok = mbar_wait(full + st, parity);
+        ok = __syncthreads_and(mbar_wait(full + st, parity)) != 0;  // the CTA leaves together
         if (!ok) {
             if (tid == 0) atomicMax(status, FT_ERR_TIMEOUT);
             break;

@@ -156,7 +156,10 @@ cudaError_t launch_composite_bands(const KParams& p, int smem_bytes, cudaStream_
 cudaError_t launch_composite_tiles(const KParams& p, const CUtensorMap& tmap, cudaStream_t s);
 int composite_tile_smem(int band_rows, int seg_w, bool staged);
 // SrcOver of one call's colour onto the canvas rows r0.. from its Matte8 coverage `mask`
-// (both as 2-D tensor maps with boxes of 256 x 16), streamed by TMA.
+// (both as 2-D tensor maps with boxes of SO_COLS x SO_ROWS elements: the kernel's stage
+// size and its expected transaction bytes derive from the same two constants), streamed
+// by TMA.
+constexpr int SO_ROWS = 16, SO_COLS = 256;
 cudaError_t launch_srcover_mask(const CUtensorMap& canvas, const CUtensorMap& mask, int W, int H, int r0,
                                 unsigned clr, int32_t* status, int sm_count, cudaStream_t s);
 // Edges and band bins of a single path's figure (after k_cbuild with split_bin), over
