@@ -2570,22 +2570,25 @@ __global__ void __launch_bounds__(BLOCK, 3) k_srcover_mask(const __grid_constant
         // four pixels per step: one mask word, four canvas words
         for (int i = tid; i < SO_ROWS * SO_COLS / 4; i += BLOCK) {
             const unsigned m4 = mk[i];
-            uint4 d = reinterpret_cast<uint4*>(cv)[i];
+            const uint4 d = reinterpret_cast<const uint4*>(cv)[i];
             unsigned dv[4] = {d.x, d.y, d.z, d.w};
+            // alpha 0 changes only channels in 1..15 (nonzero bytes whose high nibble is zero)
+            auto low = [](unsigned v) {
+                const unsigned nz = (((v & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | v) & 0x80808080u;
+                const unsigned hi = (((v & 0x70707070u) + 0x70707070u) | v) & 0x80808080u;
+                return nz & ~hi;
+            };
+            if (!m4 && !(low(dv[0]) | low(dv[1]) | low(dv[2]) | low(dv[3]))) continue;  // four pixels unchanged
 #pragma unroll
             for (int j = 0; j < 4; j++) {
                 const unsigned av = (m4 >> (8 * j)) & 0xFFu;
                 const unsigned v = dv[j];
-                if (!av) {
-                    // alpha 0: only channels in 1..15 change (nonzero bytes, high nibble zero)
-                    const unsigned nz = (((v & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | v) & 0x80808080u;
-                    const unsigned hi = (((v & 0x70707070u) + 0x70707070u) | v) & 0x80808080u;
-                    if (!(nz & ~hi)) continue;
-                }
-                // pix SrcOver: clr * a + d * (255 - clr_alpha * a), channel by channel
+                if (!av && !low(v)) continue;
+                // pix SrcOver: clr * a + d * (255 - clr_alpha * a), channel by channel; an opaque
+                // source (inverse alpha 0) replaces the pixel
                 const unsigned s4 = src[av];
                 const unsigned inv = 255u - (s4 >> 24);
-                dv[j] = __vaddus4(s4, ch8_mul4(v, (inv << 4) | (inv >> 4)));
+                dv[j] = inv ? __vaddus4(s4, ch8_mul4(v, (inv << 4) | (inv >> 4))) : s4;
             }
             reinterpret_cast<uint4*>(cv)[i] = make_uint4(dv[0], dv[1], dv[2], dv[3]);
         }
