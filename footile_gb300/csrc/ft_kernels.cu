@@ -1451,7 +1451,13 @@ __device__ __forceinline__ void resolve_row(int* arow, int W, int Wp, uint8_t* d
             if (x >= W) continue;
             uint8_t* dp = drow + x;
             if (x + 3 < W && ((reinterpret_cast<uintptr_t>(dp) & 3) == 0)) {
-                *reinterpret_cast<unsigned*>(dp) = v0 | (v1 << 8) | (v2 << 16) | (v3 << 24);
+                // masks are written once and not read back: stream them past L2 (evict first),
+                // leaving L2 to the rasterisers' figure scratch
+                const unsigned px4 = v0 | (v1 << 8) | (v2 << 16) | (v3 << 24);
+                if (__isGlobal(dp))
+                    __stcs(reinterpret_cast<unsigned*>(dp), px4);
+                else
+                    *reinterpret_cast<unsigned*>(dp) = px4;
             } else {
                 dp[0] = (uint8_t)v0;
                 if (x + 1 < W) dp[1] = (uint8_t)v1;
