@@ -7,6 +7,8 @@
 #include <cstring>
 #include <memory>
 #include <mutex>
+
+#include <nvtx3/nvToolsExt.h>
 #include <string>
 #include <vector>
 
@@ -100,6 +102,15 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
                           uint32_t h, uint32_t stride, int32_t where, float* sw_out);
 
 namespace {
+
+// An NVTX range over one stage of a call (a profiler's timeline shows the path's stages;
+// without a tool attached the calls return at once).
+struct Stage {
+    explicit Stage(const char* name) { nvtxRangePushA(name); }
+    ~Stage() { nvtxRangePop(); }
+    Stage(const Stage&) = delete;
+    Stage& operator=(const Stage&) = delete;
+};
 
 int fail(ft_ctx* c, int code, const std::string& msg) {
     if (c) c->err = msg;
@@ -530,6 +541,7 @@ FT_API int ft_batch_create(ft_ctx* c, int32_t stroke, int32_t rule, const ft_pat
 
 FT_API int ft_batch_launch(ft_ctx* c, ft_batch* b, const ft_op* ops, uint32_t n_ops_total, uint8_t* rasters,
                            uint64_t raster_bytes) {
+    Stage stage_("ft_batch_launch");
     if (!c || !b) return FT_ERR_ARG;
     if (n_ops_total < b->ops_needed || raster_bytes < b->bytes_needed)
         return fail(c, FT_ERR_ARG, "ops or raster buffer smaller than the batch needs");
@@ -730,11 +742,13 @@ FT_API int ft_get_pen_width(ft_ctx* c, float* w) {
 
 FT_API int ft_fill(ft_ctx* c, int32_t rule, const ft_op* ops, uint32_t n_ops, int32_t fmt, const uint8_t clr[4],
                    uint8_t* raster, uint32_t w, uint32_t h, uint32_t stride, int32_t where) {
+    Stage stage_("ft_fill");
     return single(c, 0, rule, ops, n_ops, fmt, clr, raster, w, h, stride, where);
 }
 
 FT_API int ft_stroke(ft_ctx* c, const ft_op* ops, uint32_t n_ops, int32_t fmt, const uint8_t clr[4],
                      uint8_t* raster, uint32_t w, uint32_t h, uint32_t stride, int32_t where) {
+    Stage stage_("ft_stroke");
     return single(c, 1, FT_NONZERO, ops, n_ops, fmt, clr, raster, w, h, stride, where);
 }
 
@@ -863,6 +877,7 @@ static bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 
 FT_API int ft_fill_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* ops, uint32_t n_ops_total,
                          const ft_path_desc* paths, uint32_t n_paths, int32_t fmt, uint8_t* rasters,
                          uint64_t raster_bytes, int32_t where) {
+    Stage stage_("ft_fill_batch");
     if (!c) return FT_ERR_ARG;
     if ((rule != FT_NONZERO && rule != FT_EVENODD) || (fmt != FT_MATTE8 && fmt != FT_RGBA8P) ||
         (where != FT_HOST && where != FT_DEVICE))
@@ -987,6 +1002,7 @@ static bool canvas_tensor_map(CUtensorMap* tm, void* base, uint32_t w, uint32_t 
 FT_API int ft_composite_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* ops, uint32_t n_ops_total,
                               const ft_path_desc* paths, uint32_t n_paths, int32_t fmt, uint8_t* raster, uint32_t w,
                               uint32_t h, uint32_t stride, int32_t where) {
+    Stage stage_("ft_composite_batch");
     return composite_impl(c, stroke, rule, ops, n_ops_total, paths, n_paths, fmt, raster, w, h, stride, where,
                           nullptr);
 }
@@ -1101,6 +1117,7 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
         c->comp_timed = false;
         FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
         if (n_paths) {
+            Stage st_build("figure build and edge binning");
             FT_CU(ftk::launch_composite_build(p, grid, smem_a, c->stream, grid <= c->sm_count),
                   "launch composite build");
             c->launches++;
@@ -1120,6 +1137,7 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
             continue;
         }
         if (n_paths && n_bands) {
+            Stage st_comp("compositing");
             // a single Rgba8p call: its Matte8 coverage into a mask (the band compositor), then
             // SrcOver from the mask, canvas and mask streamed through shared memory by TMA
             const uint32_t mstride = (w + 15) & ~15u;
@@ -1388,6 +1406,7 @@ extern "C" {
 FT_API int ft_adjoint_forward(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* ops, uint32_t n_ops_total,
                               const ft_path_desc* paths, uint32_t n_paths, float* cov, uint64_t cov_bytes,
                               int32_t where, ft_adjoint** saved) {
+    Stage stage_("ft_adjoint_forward");
     if (!c || !saved) return FT_ERR_ARG;
     if (stroke) rule = FT_NONZERO;  // Plotter::stroke fills the outline NonZero (plotter.rs:364)
     if ((rule != FT_NONZERO && rule != FT_EVENODD) || (where != FT_HOST && where != FT_DEVICE))
@@ -1431,6 +1450,7 @@ FT_API int ft_adjoint_forward(ft_ctx* c, int32_t stroke, int32_t rule, const ft_
 
 FT_API int ft_adjoint_backward(ft_ctx* c, ft_adjoint* a, const float* grad_cov, float* grad_ops, float* grad_width,
                                int32_t where) {
+    Stage stage_("ft_adjoint_backward");
     if (!c || !a) return FT_ERR_ARG;
     if (!a->ready) return fail(c, FT_ERR_ARG, "backward without a forward");
     if (a->ctx != c) return fail(c, FT_ERR_ARG, "saved state belongs to another context");
@@ -1498,6 +1518,7 @@ FT_API void ft_adjoint_destroy(ft_adjoint* a) {
 
 FT_API int ft_convert(ft_ctx* c, int32_t src_fmt, const uint8_t* src, uint32_t src_stride, int32_t dst_fmt,
                       uint8_t* dst, uint32_t dst_stride, uint32_t w, uint32_t h, int32_t where) {
+    Stage stage_("ft_convert");
     if (!c) return FT_ERR_ARG;
     if (!((src_fmt == FT_RGBA8P && dst_fmt == FT_SRGBA8) || (src_fmt == FT_MATTE8 && dst_fmt == FT_SGRAY8)) ||
         (where != FT_HOST && where != FT_DEVICE))
@@ -1630,6 +1651,7 @@ FT_API int ft_stroke_composite_forward(ft_ctx* c, const ft_op* ops, uint32_t n_o
                                        uint32_t n_paths, const float* clr, uint32_t width, uint32_t height,
                                        const float* init, float* out, uint32_t chunk, int32_t where,
                                        ft_composite_adjoint** saved) {
+    Stage stage_("ft_stroke_composite_forward");
     if (!c || !saved) return FT_ERR_ARG;
     if (where != FT_HOST && where != FT_DEVICE) return fail(c, FT_ERR_ARG, "bad location");
     if (width == 0 || height == 0) return fail(c, FT_ERR_ARG, "empty canvas");
@@ -1720,6 +1742,7 @@ FT_API int ft_stroke_composite_forward(ft_ctx* c, const ft_op* ops, uint32_t n_o
 
 FT_API int ft_stroke_composite_backward(ft_ctx* c, ft_composite_adjoint* s, const float* grad_out, float* grad_ops,
                                         float* grad_width, float* grad_init, int32_t where) {
+    Stage stage_("ft_stroke_composite_backward");
     if (!c || !s) return FT_ERR_ARG;
     if (!s->ready) return fail(c, FT_ERR_ARG, "backward without a forward");
     if (s->ctx != c) return fail(c, FT_ERR_ARG, "saved state belongs to another context");
@@ -1809,6 +1832,7 @@ FT_API void ft_stroke_composite_destroy(ft_composite_adjoint* s) {
 FT_API int ft_autotune_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* ops, uint32_t n_ops_total,
                              const ft_path_desc* paths, uint32_t n_paths, int32_t fmt, uint8_t* rasters,
                              uint64_t raster_bytes, const char* cache_path, ft_tuning* chosen, float* ms_out) {
+    Stage stage_("ft_autotune_batch");
     if (!c) return FT_ERR_ARG;
     if (n_paths && !paths) return fail(c, FT_ERR_ARG, "null path list");
     for (uint32_t i = 0; i < n_paths; i++) {
