@@ -85,5 +85,28 @@ def build(force=False, verbose=False):
     return LIB
 
 
+def build_variant(out_dir, extra_flags):
+    """Compile the library with extra nvcc flags (the bounds-check build: -DFT_CHECK=1)
+    into out_dir; returns the path of its shared library."""
+    os.makedirs(out_dir, exist_ok=True)
+    cc = nvcc()
+
+    def compile_one(src):
+        obj = os.path.join(out_dir, src.replace(".cu", ".o"))
+        cmd = [cc] + GENCODE + NVFLAGS + list(extra_flags) + ["-c", os.path.join(CSRC, src), "-o", obj]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("nvcc failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+        return obj
+
+    with cf.ThreadPoolExecutor(len(SOURCES)) as ex:
+        objs = list(ex.map(compile_one, SOURCES))
+    lib = os.path.join(out_dir, "libfootile_gpu.so")
+    r = subprocess.run([cc] + GENCODE + ["-shared", "-o", lib] + objs, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("nvcc link failed:\n" + r.stdout + r.stderr)
+    return lib
+
+
 if __name__ == "__main__":
     print(build(force=True, verbose=True))

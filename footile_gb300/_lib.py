@@ -21,17 +21,19 @@ class FootileError(RuntimeError):
         self.code = code
 
 
-def load(auto_build=True):
-    """Load libfootile_gpu.so, compiling it first when it is missing or stale."""
+def load(auto_build=True, path=None):
+    """Load libfootile_gpu.so, compiling it first when it is missing or stale.  `path`
+    loads another build of the library instead (the bounds-check build of the tests);
+    it must come before the first load of the process."""
     global _lib
     with _lock:
         if _lib is not None:
             return _lib
-        if not up_to_date():
+        if path is None and not up_to_date():
             if not auto_build:
                 raise RuntimeError(f"{LIB} is missing; run footile_gb300._build.build()")
             build()
-        L = ctypes.CDLL(LIB)
+        L = ctypes.CDLL(path or LIB)
         P = ctypes.c_void_p
         i32, u32, u64, f32 = ctypes.c_int32, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_float
         sig = {
@@ -53,6 +55,7 @@ def load(auto_build=True):
             "ft_last_error": ([P], ctypes.c_char_p),
             "ft_last_timings": ([P, ctypes.POINTER(f32)], ctypes.c_int),
             "ft_last_composite_ms": ([P, ctypes.POINTER(f32)], ctypes.c_int),
+            "ft_check_failures": ([P, P], ctypes.c_int),
             "ft_launch_count": ([P], u64),
             "ft_batch_create": ([P, i32, i32, P, u32, i32, ctypes.POINTER(P)], ctypes.c_int),
             "ft_batch_launch": ([P, P, P, u32, P, u64], ctypes.c_int),
@@ -91,6 +94,7 @@ def exported_symbols():
         "ft_ctx_create", "ft_ctx_destroy", "ft_set_stream", "ft_set_tolerance", "ft_set_transform",
         "ft_set_join", "ft_set_pen_width", "ft_get_pen_width", "ft_fill", "ft_stroke", "ft_fill_batch",
         "ft_batch_status", "ft_sync", "ft_last_error", "ft_last_timings", "ft_last_composite_ms", "ft_launch_count",
+        "ft_check_failures",
         "ft_batch_create", "ft_batch_launch", "ft_batch_launch_status", "ft_batch_destroy",
         "ft_composite_batch", "ft_fill_noalloc", "ft_adjoint_forward", "ft_adjoint_backward", "ft_adjoint_status",
         "ft_adjoint_destroy", "ft_set_tuning", "ft_get_tuning", "ft_autotune_batch",

@@ -42,6 +42,18 @@
 namespace ftk {
 
 constexpr unsigned FULL = 0xFFFFFFFFu;
+
+// Bounds checks of the check build (nvcc -DFT_CHECK=1, see _build.build_variant): a failed
+// check keeps the first failing site's number in g_check and skips the access; no trap.
+// In the shipped build every check folds to true.
+#ifndef FT_CHECK
+#define FT_CHECK 0
+#endif
+static __device__ int g_check = 0;
+__device__ __forceinline__ bool ck(bool ok, int site) {
+    if (FT_CHECK && !ok) atomicCAS(&g_check, 0, site);
+    return !FT_CHECK || ok;
+}
 // Curve leaves of an op kept (in local memory) from the count pass for the emit pass;
 // ops with more leaves are walked again.  Warp builds (small glyphs) keep 64; CTA builds
 // (large figures, few CTAs, L1 to spare) keep more.
@@ -1363,7 +1375,7 @@ __device__ __forceinline__ void scan_row(int x_bot, int inv, bool st, bool en, i
         long long v = (long long)first + (long long)j * step;
         x_cov = v > FX_ONE ? FX_ONE : (int)v;
         prev = min(pixel_cov(x_cov), cov);
-        if (prev) atomicAdd(&area[0], ed * prev);
+        if (prev && ck(W > 0, 1)) atomicAdd(&area[0], ed * prev);
         j++;
         x_cov = min(x_cov + step, FX_ONE);
     } else {
@@ -1376,7 +1388,7 @@ __device__ __forceinline__ void scan_row(int x_bot, int inv, bool st, bool en, i
             const int v = min(pixel_cov(x_cov), cov);
             const int p = v - prev;
             prev = v;
-            if (p) atomicAdd(&area[minp + j], ed * p);
+            if (p && ck(minp + j >= 0 && minp + j < W, 2)) atomicAdd(&area[minp + j], ed * p);
             cell1 = minp + j;
             if (v >= cov) break;
             x_cov = min(x_cov + step, FX_ONE);
@@ -1637,7 +1649,10 @@ __device__ void raster_sweep_warp(const KParams& P, const ft_path_desc& d, const
         const EdgeRec E = edge_rec(e, count, S.dir, pts, ss);
         if (E.ed) {
             const long long b = (long long)E.start_row - top_row;
-            if (b < nrows) sorted[atomicAdd(&hist[b], 1)] = sweep_rec(E, top_row);
+            if (b < nrows && ck(b >= 0, 3)) {
+                const int k = atomicAdd(&hist[b], 1);
+                if (ck(k >= 0 && k < WARP_CAP, 4)) sorted[k] = sweep_rec(E, top_row);
+            }
         }
     }
     for (int x = lane; x < Wp; x += 32) row[x] = 0;
@@ -1650,7 +1665,8 @@ __device__ void raster_sweep_warp(const KParams& P, const ft_path_desc& d, const
     int n_act = 0;
     for (int s = 0; s < nrows; s++) {
         const int bs = s == 0 ? 0 : hist[s - 1], be = hist[s];
-        for (int k = lane; k < be - bs; k += 32) active[n_act + k] = sorted[bs + k];
+        for (int k = lane; k < be - bs; k += 32)
+            if (ck(n_act + k < WARP_CAP && bs + k < WARP_CAP, 5)) active[n_act + k] = sorted[bs + k];
         const int n_old = n_act;  // records from n_old on start on this row
         n_act += be - bs;
         __syncwarp();
@@ -1956,7 +1972,9 @@ __device__ void bin_edges(const KParams& P, uint32_t path, const CState& S, cons
                 int lo, hi;
                 if (!rows_of(q1[u], lo, hi)) continue;
                 for (int b = lo / R; b <= hi / R; b++) {
-                    int4* dst = reinterpret_cast<int4*>(P.pool + base + (unsigned)atomicAdd(&hist[b], 1));
+                    const unsigned long long k = base + (unsigned)atomicAdd(&hist[b], 1);
+                    if (!ck(k < P.pool_cap, 11)) continue;
+                    int4* dst = reinterpret_cast<int4*>(P.pool + k);
                     dst[0] = q0[u];
                     dst[1] = q1[u];
                 }
@@ -2242,7 +2260,7 @@ __device__ __forceinline__ void seg_row(int x_bot, int inv, bool st, bool en, in
     for (; c < s1; c++) {
         const int v = min(pixel_cov(x_cov), cov);
         if (v != prev) {
-            atomicAdd(&area[c - s0], ed * (v - prev));
+            if (ck(c - s0 >= 0 && c - s0 < sw, 6)) atomicAdd(&area[c - s0], ed * (v - prev));
             if (c_lo < 0) c_lo = c - s0;
             c_hi = c - s0;
         }
@@ -2255,7 +2273,7 @@ __device__ __forceinline__ void seg_row(int x_bot, int inv, bool st, bool en, in
         for (int w = k0 >> 5; w <= (k1 >> 5); w++) {
             const int lo = max(k0 - 32 * w, 0), hi = min(k1 - 32 * w, 31);
             const unsigned m = (hi == 31 ? 0xFFFFFFFFu : ((1u << (hi + 1)) - 1u)) & ~((1u << lo) - 1u);
-            atomicOr(&bmap[w], m);
+            if (ck(w < (sw / 8 + 31) / 32, 7)) atomicOr(&bmap[w], m);
         }
     }
 }
@@ -2372,12 +2390,14 @@ __global__ void __launch_bounds__(BLOCK, 4) k_ctile(KParams P, const __grid_cons
                 int T = 0;
                 for (int w = 0; w < nwords; w++) {
                     const unsigned bw = bmap[w];
-                    if ((bw >> lane) & 1u) clist[T + __popc(bw & lt)] = (unsigned char)(32 * w + lane);
+                    if (((bw >> lane) & 1u) && ck(T + __popc(bw & lt) < nchunks, 8))
+                        clist[T + __popc(bw & lt)] = (unsigned char)(32 * w + lane);
                     T += __popc(bw);
                 }
                 __syncwarp();
                 if (lane < nwords) bmap[lane] = 0u;
                 auto compose = [&](int x, unsigned av) {
+                    if (!ck(x >= 0 && x < xend, 10)) return;
                     unsigned* p = px(x);
                     unsigned dv = *p;
                     const int kk = min((Gj - (int)last[x]) & 255, 15);
@@ -2437,7 +2457,7 @@ __global__ void __launch_bounds__(BLOCK, 4) k_ctile(KParams P, const __grid_cons
 #pragma unroll
                     for (int k = 0; k < 8; k++) {
                         const unsigned v = ((k < 4 ? w0 : w1) >> (8 * (k & 3))) & 0xFFu;
-                        if (v) q[pos++] = ((unsigned)(ch * 8 + k) << 8) | v;
+                        if (v && ck(pos < 256, 9)) q[pos++] = ((unsigned)(ch * 8 + k) << 8) | v;
                     }
                     if (has_gap) q[256 + __popc(gm & lt)] = ((unsigned)g0 << 19) | ((unsigned)(g1 - g0) << 8) | gav;
                     __syncwarp();
@@ -2716,7 +2736,9 @@ __global__ void __launch_bounds__(BLOCK) k_fig_bin_fill(KParams P) {
         const int4 q0 = erec[2 * e];
         const int lo = max(q1.z - f.tmin, f.rb), hi = min(q1.w - f.tmin, f.H - 1);
         for (int b = lo / f.R; lo <= hi && b <= hi / f.R; b++) {
-            int4* dst = reinterpret_cast<int4*>(P.pool + base + (unsigned)atomicAdd(&cursor[b], 1));
+            const unsigned long long k = base + (unsigned)atomicAdd(&cursor[b], 1);
+            if (!ck(k < P.pool_cap, 12)) continue;
+            int4* dst = reinterpret_cast<int4*>(P.pool + k);
             dst[0] = q0;
             dst[1] = q1;
         }
@@ -2918,4 +2940,17 @@ extern "C" FT_API int ft_fill_noalloc(int32_t rule, const ft_op* ops, uint32_t n
     const cudaError_t e = cudaLaunchKernel(reinterpret_cast<const void*>(ftk::k_fill_noalloc), dim3(1),
                                            dim3(ftk::BLOCK), args, (size_t)smem, static_cast<cudaStream_t>(stream));
     return e == cudaSuccess ? FT_OK : FT_ERR_CUDA;
+}
+
+// Check build: the first failing bounds check's site since the last call (0: none), and
+// whether the checks are compiled in.  No counterpart in footile.
+extern "C" FT_API int ft_check_failures(int32_t* site, int32_t* compiled_in) {
+    if (compiled_in) *compiled_in = FT_CHECK;
+    if (!site) return FT_OK;
+    int v = 0;
+    if (cudaMemcpyFromSymbol(&v, ftk::g_check, sizeof(int)) != cudaSuccess) return FT_ERR_CUDA;
+    *site = v;
+    const int zero = 0;
+    if (cudaMemcpyToSymbol(ftk::g_check, &zero, sizeof(int)) != cudaSuccess) return FT_ERR_CUDA;
+    return FT_OK;
 }

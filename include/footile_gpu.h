@@ -391,6 +391,14 @@ FT_API int ft_last_timings(ft_ctx* ctx, float* kernel_ms);
  * counterpart in footile: for measuring the compositing step against the HBM roofline. */
 FT_API int ft_last_composite_ms(ft_ctx* ctx, float* ms);
 
+/* Bounds-check build (the library compiled with -DFT_CHECK=1) — no counterpart in
+ * footile; it stands in for a memory checker.  Device code checks the indices of its
+ * shared-memory cell buffers, warp scratch, edge pool and compositor queues; a failed check
+ * skips the access and keeps the first failing site's number.  `site` (may be NULL)
+ * receives that number since the last call (0: none) and is reset; `compiled_in` (may be
+ * NULL) is 1 in the check build and 0 in the shipped build, whose checks fold away. */
+FT_API int ft_check_failures(int32_t* site, int32_t* compiled_in);
+
 /* Number of kernel launches the library has issued since the context was created. */
 FT_API uint64_t ft_launch_count(ft_ctx* ctx);
 
