@@ -2525,7 +2525,7 @@ __global__ void __launch_bounds__(BLOCK, 4) k_ctile(KParams P, const __grid_cons
 constexpr int SO_STAGES = 3;  // SO_ROWS x SO_COLS tiles: ft_kernels.cuh (the host's tensor-map boxes)
 constexpr int SO_CANVAS_BYTES = SO_ROWS * SO_COLS * 4, SO_MASK_BYTES = SO_ROWS * SO_COLS;
 constexpr int SO_STAGE_BYTES = SO_CANVAS_BYTES + SO_MASK_BYTES;
-constexpr int SO_SMEM = SO_STAGES * SO_STAGE_BYTES + 128 + 1024;
+constexpr int SO_SMEM = SO_STAGES * SO_STAGE_BYTES + 128 + 1024;  // stages, mbarriers, colour table
 
 // ch8_mul(d, b) of the four channels of d, b's 12-bit expansion (b << 4 | b >> 4) given
 __device__ __forceinline__ unsigned ch8_mul4(unsigned d, unsigned bx) {
@@ -2538,63 +2538,92 @@ __device__ __forceinline__ unsigned ch8_mul4(unsigned d, unsigned bx) {
     return out;
 }
 
-__global__ void __launch_bounds__(BLOCK, 3) k_srcover_mask(const __grid_constant__ CUtensorMap tm_canvas,
-                                                            const __grid_constant__ CUtensorMap tm_mask, int W, int H,
-                                                            int r0, unsigned clr, int32_t* status) {
+// Warps 0..7 composite; warp 8 moves the tiles (one lane issues every TMA operation):
+// full[s] completes when stage s holds a loaded tile, done[s] when the eight compositing
+// warps have finished it (each warp fences its shared-memory writes for the async proxy
+// first), so no CTA-wide barrier sits in the loop.
+constexpr int SO_CWARPS = 8;
+constexpr int SO_THREADS = 32 * (SO_CWARPS + 1);
+
+__global__ void __launch_bounds__(SO_THREADS, 3) k_srcover_mask(const __grid_constant__ CUtensorMap tm_canvas,
+                                                                 const __grid_constant__ CUtensorMap tm_mask, int W,
+                                                                 int H, int r0, unsigned clr, int32_t* status) {
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + SO_STAGES * SO_STAGE_BYTES);
+    uint64_t* done = full + SO_STAGES;
     // src[a]: the colour's four channels times coverage a (pix's ch8_mul), packed; its
     // alpha byte is the SrcOver's source alpha
     unsigned* src = reinterpret_cast<unsigned*>(smem + SO_STAGES * SO_STAGE_BYTES + 128);
-    {
-        const unsigned a = threadIdx.x & 255u;
-        src[a] = ch8_mul4(clr, (a << 4) | (a >> 4));
-    }
+    for (int a = threadIdx.x; a < 256; a += SO_THREADS) src[a] = ch8_mul4(clr, ((unsigned)a << 4) | ((unsigned)a >> 4));
     const int tx = (W + SO_COLS - 1) / SO_COLS, ty = (H - r0 + SO_ROWS - 1) / SO_ROWS;
     const int ntiles = tx * ty;
-    const int tid = threadIdx.x;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint64_t cmap = reinterpret_cast<uint64_t>(&tm_canvas), mmap = reinterpret_cast<uint64_t>(&tm_mask);
     auto canvas_s = [&](int st) { return reinterpret_cast<unsigned*>(smem + st * SO_STAGE_BYTES); };
     auto mask_s = [&](int st) { return smem + st * SO_STAGE_BYTES + SO_CANVAS_BYTES; };
-    auto load = [&](int t, int st) {  // thread 0: the tile's canvas and mask into stage st
-        const int x = (t % tx) * SO_COLS, y = r0 + (t / tx) * SO_ROWS;
-        const unsigned mb = smem_u32(full + st);
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(SO_STAGE_BYTES)
-                     : "memory");
-        asm volatile(
-            "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
-            "[%4];" ::"r"(smem_u32(canvas_s(st))),
-            "l"(cmap), "r"(x), "r"(y), "r"(mb)
-            : "memory");
-        asm volatile(
-            "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
-            "[%4];" ::"r"(smem_u32(mask_s(st))),
-            "l"(mmap), "r"(x), "r"(y), "r"(mb)
-            : "memory");
-    };
-    if (tid == 0) {
-        for (int st = 0; st < SO_STAGES; st++)
+    auto tile_x = [&](int t) { return (t % tx) * SO_COLS; };
+    auto tile_y = [&](int t) { return r0 + (t / tx) * SO_ROWS; };
+    if (threadIdx.x == 0) {
+        for (int st = 0; st < SO_STAGES; st++) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(full + st)) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(done + st)), "r"(SO_CWARPS)
+                         : "memory");
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
     // this CTA's tiles: blockIdx.x, blockIdx.x + gridDim.x, ...
     const int mine = ntiles > (int)blockIdx.x ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
-    if (tid == 0)
-        for (int k = 0; k < SO_STAGES && k < mine; k++) load((int)blockIdx.x + k * (int)gridDim.x, k);
-    bool ok = true;
-    for (int k = 0; k < mine && ok; k++) {
+    auto tile_of = [&](int k) { return (int)blockIdx.x + k * (int)gridDim.x; };
+    if (warp == SO_CWARPS) {
+        if (lane != 0) return;
+        auto load = [&](int k, int st) {
+            const int t = tile_of(k);
+            const unsigned mb = smem_u32(full + st);
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(SO_STAGE_BYTES)
+                         : "memory");
+            asm volatile(
+                "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, "
+                "%3}], [%4];" ::"r"(smem_u32(canvas_s(st))),
+                "l"(cmap), "r"(tile_x(t)), "r"(tile_y(t)), "r"(mb)
+                : "memory");
+            asm volatile(
+                "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, "
+                "%3}], [%4];" ::"r"(smem_u32(mask_s(st))),
+                "l"(mmap), "r"(tile_x(t)), "r"(tile_y(t)), "r"(mb)
+                : "memory");
+        };
+        for (int k = 0; k < SO_STAGES && k < mine; k++) load(k, k);
+        for (int k = 0; k < mine; k++) {
+            const int st = k % SO_STAGES;
+            if (!mbar_wait(done + st, (unsigned)((k / SO_STAGES) & 1))) {
+                atomicMax(status, FT_ERR_TIMEOUT);
+                break;
+            }
+            const int t = tile_of(k);
+            asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group [%0, {%1, %2}], [%3];" ::"l"(cmap),
+                         "r"(tile_x(t)), "r"(tile_y(t)), "r"(smem_u32(canvas_s(st)))
+                         : "memory");
+            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+            // the stage of tile k - 1 is free once its store has read it: reload it
+            if (k >= 1 && k - 1 + SO_STAGES < mine) {
+                asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+                load(k - 1 + SO_STAGES, (k - 1) % SO_STAGES);
+            }
+        }
+        asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+        return;
+    }
+    for (int k = 0; k < mine; k++) {
         const int st = k % SO_STAGES;
-        const unsigned parity = (unsigned)((k / SO_STAGES) & 1);
-        ok = __syncthreads_and(mbar_wait(full + st, parity)) != 0;  // the CTA leaves together
-        if (!ok) {
-            if (tid == 0) atomicMax(status, FT_ERR_TIMEOUT);
+        if (!mbar_wait(full + st, (unsigned)((k / SO_STAGES) & 1))) {
+            if (lane == 0) atomicMax(status, FT_ERR_TIMEOUT);
             break;
         }
         unsigned* cv = canvas_s(st);
         const unsigned* mk = reinterpret_cast<const unsigned*>(mask_s(st));
         // four pixels per step: one mask word, four canvas words
-        for (int i = tid; i < SO_ROWS * SO_COLS / 4; i += BLOCK) {
+        for (int i = threadIdx.x; i < SO_ROWS * SO_COLS / 4; i += 32 * SO_CWARPS) {
             const unsigned m4 = mk[i];
             const uint4 d = reinterpret_cast<const uint4*>(cv)[i];
             unsigned dv[4] = {d.x, d.y, d.z, d.w};
@@ -2619,23 +2648,8 @@ __global__ void __launch_bounds__(BLOCK, 3) k_srcover_mask(const __grid_constant
             reinterpret_cast<uint4*>(cv)[i] = make_uint4(dv[0], dv[1], dv[2], dv[3]);
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
-            const int t = (int)blockIdx.x + k * (int)gridDim.x;
-            asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group [%0, {%1, %2}], [%3];" ::"l"(cmap),
-                         "r"((t % tx) * SO_COLS), "r"(r0 + (t / tx) * SO_ROWS), "r"(smem_u32(cv))
-                         : "memory");
-            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-            // the stage of tile k - 1 is free once its store has read it: reload it
-            if (k >= 1 && k - 1 + SO_STAGES < mine) {
-                asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
-                load((int)blockIdx.x + (k - 1 + SO_STAGES) * (int)gridDim.x, (k - 1) % SO_STAGES);
-            }
-        }
-    }
-    if (tid == 0) {
-        // the last tile's stage was not reloaded (k - 1 + STAGES >= mine for it)
-        asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(done + st)) : "memory");
     }
 }
 
@@ -2646,7 +2660,7 @@ cudaError_t launch_srcover_mask(const CUtensorMap& canvas, const CUtensorMap& ma
     const int ntiles = ((W + SO_COLS - 1) / SO_COLS) * ((H - r0 + SO_ROWS - 1) / SO_ROWS);
     if (ntiles <= 0) return cudaSuccess;
     const int grid = std::max(1, std::min(ntiles, 3 * sm_count));
-    k_srcover_mask<<<grid, BLOCK, SO_SMEM, s>>>(canvas, mask, W, H, r0, clr, status);
+    k_srcover_mask<<<grid, SO_THREADS, SO_SMEM, s>>>(canvas, mask, W, H, r0, clr, status);
     return cudaGetLastError();
 }
 
