@@ -2515,10 +2515,11 @@ __global__ void __launch_bounds__(BLOCK, 4) k_ctile(KParams P, const __grid_cons
 // footile's rasterize_row composites every pixel of the call's rows from its top row down
 // with the row's coverage (fig.rs:637-643; alpha 0 where nothing covers).  With the
 // call's Matte8 coverage already in a mask (the band compositor writes it), this pass
-// streams the canvas and the mask through shared memory by TMA: per tile of 16 rows x
+// streams the canvas and the mask through shared memory by TMA: per tile of 8 rows x
 // 256 pixels, a 2-D tensor load of the canvas (u32 pixels) and of the mask (bytes)
-// completing on the stage's mbarrier, SrcOver in place, a 2-D tensor store; four stages
-// per CTA keep loads, compute and stores in flight together.  A pixel with coverage 0
+// completing on the stage's mbarrier, SrcOver in place, a 2-D tensor store; three stages
+// per CTA and six CTAs per SM keep loads, compute and stores in flight together (the
+// fastest of 8 / 16 / 32-row tiles with 2 to 6 stages on the 4096x4096 scene).  A pixel with coverage 0
 // takes the alpha-0 map, which changes only channel values 1..15: the common case of no
 // such channel leaves the pixel as it is.
 
@@ -2545,7 +2546,7 @@ __device__ __forceinline__ unsigned ch8_mul4(unsigned d, unsigned bx) {
 constexpr int SO_CWARPS = 8;
 constexpr int SO_THREADS = 32 * (SO_CWARPS + 1);
 
-__global__ void __launch_bounds__(SO_THREADS, 3) k_srcover_mask(const __grid_constant__ CUtensorMap tm_canvas,
+__global__ void __launch_bounds__(SO_THREADS, 6) k_srcover_mask(const __grid_constant__ CUtensorMap tm_canvas,
                                                                  const __grid_constant__ CUtensorMap tm_mask, int W,
                                                                  int H, int r0, unsigned clr, int32_t* status) {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -2659,7 +2660,7 @@ cudaError_t launch_srcover_mask(const CUtensorMap& canvas, const CUtensorMap& ma
     if (e != cudaSuccess) return e;
     const int ntiles = ((W + SO_COLS - 1) / SO_COLS) * ((H - r0 + SO_ROWS - 1) / SO_ROWS);
     if (ntiles <= 0) return cudaSuccess;
-    const int grid = std::max(1, std::min(ntiles, 3 * sm_count));
+    const int grid = std::max(1, std::min(ntiles, 6 * sm_count));
     k_srcover_mask<<<grid, SO_THREADS, SO_SMEM, s>>>(canvas, mask, W, H, r0, clr, status);
     return cudaGetLastError();
 }

@@ -159,7 +159,7 @@ int composite_tile_smem(int band_rows, int seg_w, bool staged);
 // (both as 2-D tensor maps with boxes of SO_COLS x SO_ROWS elements: the kernel's stage
 // size and its expected transaction bytes derive from the same two constants), streamed
 // by TMA.
-constexpr int SO_ROWS = 16, SO_COLS = 256;
+constexpr int SO_ROWS = 8, SO_COLS = 256;
 cudaError_t launch_srcover_mask(const CUtensorMap& canvas, const CUtensorMap& mask, int W, int H, int r0,
                                 unsigned clr, int32_t* status, int sm_count, cudaStream_t s);
 // Edges and band bins of a single path's figure (after k_cbuild with split_bin), over
