@@ -612,6 +612,7 @@ def extra_adjoint_composite(ctx, stream, dev, cpu=True, n_paths=16384, side=2048
     import torch
     from footile_gb300 import _abi, workloads
     from footile_gb300.adjoint import StrokeComposite, pack_coverage, stroke_composite_grads
+    torch.cuda.empty_cache()  # the chunk size follows the free device memory
     paths_ops, _, clrs, _ = workloads.strokes_16384(n_paths=n_paths, side=side)
     ops, paths, _ = pack_coverage(paths_ops, [side] * n_paths)
     clr = clrs.astype(np.float32) / 255.0

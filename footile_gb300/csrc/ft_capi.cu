@@ -1687,11 +1687,12 @@ FT_API int ft_stroke_composite_forward(ft_ctx* c, const ft_op* ops, uint32_t n_o
     s->h_paths.assign(paths, paths + n_paths);
     const uint64_t plane = s->plane_bytes();
     if (chunk == 0) {
-        // coverage and coverage gradient of a chunk in at most 40 % of the free memory
-        // (96 GB at most), equal chunks
+        // coverage and coverage gradient of a chunk in at most 60 % of the free memory
+        // (160 GB at most), equal chunks.  Fewer chunks recompute less in the backward:
+        // 16,384 strokes on 2048x2048 in 4 / 6 / 8 chunks measured bwd / fwd 1.98 / 2.05 / 2.05
         size_t free_b = 0, total_b = 0;
         FT_CU(cudaMemGetInfo(&free_b, &total_b), "memory info");
-        const uint64_t budget = std::min<uint64_t>(free_b / 5 * 2, 96ull << 30);
+        const uint64_t budget = std::min<uint64_t>(free_b / 5 * 3, 160ull << 30);
         const uint64_t kmax = std::max<uint64_t>(1, budget / (2 * plane));
         const uint64_t nch = (std::max(n_paths, 1u) + kmax - 1) / kmax;
         chunk = (uint32_t)((std::max(n_paths, 1u) + nch - 1) / nch);
