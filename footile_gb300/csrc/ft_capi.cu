@@ -1692,7 +1692,9 @@ FT_API int ft_stroke_composite_forward(ft_ctx* c, const ft_op* ops, uint32_t n_o
         // 16,384 strokes on 2048x2048 in 4 / 6 / 8 chunks measured bwd / fwd 1.98 / 2.05 / 2.05
         size_t free_b = 0, total_b = 0;
         FT_CU(cudaMemGetInfo(&free_b, &total_b), "memory info");
-        const uint64_t budget = std::min<uint64_t>(free_b / 5 * 3, 160ull << 30);
+        // the saved state's own coverage buffers from an earlier call count as free
+        const uint64_t avail = (uint64_t)free_b + s->cov.cap + s->gcov.cap;
+        const uint64_t budget = std::min<uint64_t>(avail / 5 * 3, 160ull << 30);
         const uint64_t kmax = std::max<uint64_t>(1, budget / (2 * plane));
         const uint64_t nch = (std::max(n_paths, 1u) + kmax - 1) / kmax;
         chunk = (uint32_t)((std::max(n_paths, 1u) + nch - 1) / nch);
