@@ -2745,36 +2745,13 @@ __global__ void __launch_bounds__(BLOCK) k_fig_bin_fill(KParams P) {
     const unsigned long long base = (unsigned long long)(unsigned)cr.z | ((unsigned long long)(unsigned)cr.w << 32);
     const int4* erec = reinterpret_cast<const int4*>(P.scratch + P.L.edges);
     int* cursor = P.bin_hist + f.nb;
-    const int lane = threadIdx.x & 31;
-    const unsigned lt = (1u << lane) - 1u;
-    // neighbouring edges of a figure share bands: the lanes of a warp that put an edge
-    // into the same band take their slots with one atomic (order within a band is free:
-    // the i16 cell sums commute)
-    for (int e0 = blockIdx.x * BLOCK; e0 < f.count; e0 += gridDim.x * BLOCK) {
-        const int e = e0 + (int)threadIdx.x;
-        int4 q0 = make_int4(0, 0, 0, 0), q1 = q0;
-        int b0 = 0, nbands = 0;
-        if (e < f.count) {
-            q1 = erec[2 * e + 1];  // step_pix, ed, start_row, end_row
-            if (q1.y) {
-                q0 = erec[2 * e];
-                const int lo = max(q1.z - f.tmin, f.rb), hi = min(q1.w - f.tmin, f.H - 1);
-                if (lo <= hi) {
-                    b0 = lo / f.R;
-                    nbands = hi / f.R - b0 + 1;
-                }
-            }
-        }
-        const int rounds = __reduce_max_sync(FULL, nbands);
-        for (int r = 0; r < rounds; r++) {
-            const int b = r < nbands ? b0 + r : -1;
-            const unsigned m = __match_any_sync(FULL, b);
-            const int leader = __ffs(m) - 1;
-            unsigned old = 0;
-            if (b >= 0 && lane == leader) old = (unsigned)atomicAdd(&cursor[b], __popc(m));
-            old = __shfl_sync(FULL, old, leader);
-            if (b < 0) continue;
-            const unsigned long long k = base + old + (unsigned)__popc(m & lt);
+    for (int e = blockIdx.x * BLOCK + threadIdx.x; e < f.count; e += gridDim.x * BLOCK) {
+        const int4 q1 = erec[2 * e + 1];  // step_pix, ed, start_row, end_row
+        if (!q1.y) continue;
+        const int4 q0 = erec[2 * e];
+        const int lo = max(q1.z - f.tmin, f.rb), hi = min(q1.w - f.tmin, f.H - 1);
+        for (int b = lo / f.R; lo <= hi && b <= hi / f.R; b++) {
+            const unsigned long long k = base + (unsigned)atomicAdd(&cursor[b], 1);
             if (!ck(k < P.pool_cap, 12)) continue;
             int4* dst = reinterpret_cast<int4*>(P.pool + k);
             dst[0] = q0;
