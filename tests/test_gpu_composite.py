@@ -151,3 +151,50 @@ def test_strokes_16384_prefix_full_canvas(ctx, init_kind):
     st = composite_batch(ctx, ops_d, paths, _abi.RGBA8P, ras_d, stroke=True)
     assert (st == st_o).all()
     assert_same(ras_d.cpu().numpy(), want, f"{k} strokes on {side}x{side} ({init_kind} canvas)")
+
+
+@pytest.mark.parametrize("w,h", [(1, 1), (5, 3), (130, 1), (3, 200), (1030, 9)])
+def test_composite_ragged_canvases(ctx, w, h):
+    """Canvases narrower than a tile, one row or one column high, and a width just past a
+    1,024-pixel tile: the tile compositor's edges (partial tiles, rows past the canvas,
+    chunks past its right edge) against the oracle, Rgba8p on random bytes."""
+    rng = np.random.default_rng(w * 1000 + h)
+    paths_ops, clrs = [], []
+    for i in range(12):
+        o = workloads.random_path(rng, max(w, h) + 4, int(rng.integers(1, 8)), close=bool(i % 2))
+        o["v"] -= 2.0  # some coordinates left of and above the canvas
+        paths_ops.append(o)
+        a = int(rng.integers(1, 256))
+        clrs.append([int(v) * a // 255 for v in rng.integers(0, 256, 3)] + [a])
+    ops, paths, _ = pack_batch(paths_ops, [(w, h)] * len(paths_ops), _abi.RGBA8P, clrs)
+    init = rng.integers(0, 256, (h, w, 4)).astype(np.uint8)
+    for stroke in (False, True):
+        want = init.copy()
+        oracle.composite(int(stroke), _abi.NONZERO, ops, paths, _abi.RGBA8P, want, s_width=1.0)
+        got = init.copy()
+        ctx.set_pen_width(1.0)
+        composite_batch(ctx, ops, paths, _abi.RGBA8P, got, stroke=stroke)
+        assert_same(got, want, f"{w}x{h} stroke={stroke}")
+
+
+def test_composite_empty_and_offcanvas_calls(ctx):
+    """Calls with no ops, calls whose figures lie wholly below, right of or above the
+    canvas, and an empty call list: only footile's alpha-0 composites of the calls that
+    reach a row change the canvas."""
+    rng = np.random.default_rng(99)
+    w, h = 300, 120
+    square = lambda x, y: ops_array([PathOp.Move(x, y), PathOp.Line(x + 20, y), PathOp.Line(x + 20, y + 20),
+                                     PathOp.Line(x, y + 20), PathOp.Close()])
+    paths_ops = [ops_array([]), square(10, 500), square(900, 10), square(10, -400), square(40, 30),
+                 ops_array([PathOp.Move(5, 5)]), square(-30, 60)]
+    clrs = [[10, 5, 3, 200]] * len(paths_ops)
+    ops, paths, _ = pack_batch(paths_ops, [(w, h)] * len(paths_ops), _abi.RGBA8P, clrs)
+    init = rng.integers(0, 24, (h, w, 4)).astype(np.uint8)
+    want = init.copy()
+    oracle.composite(0, _abi.NONZERO, ops, paths, _abi.RGBA8P, want)
+    got = init.copy()
+    composite_batch(ctx, ops, paths, _abi.RGBA8P, got)
+    assert_same(got, want, "empty and off-canvas calls")
+    none = init.copy()
+    composite_batch(ctx, ops[:0], paths[:0], _abi.RGBA8P, none)
+    assert_same(none, init, "no calls")
