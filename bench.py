@@ -141,6 +141,18 @@ def extra_scene(ctx, stream, dev, cpu=True):
     fill(_abi.NONZERO, _abi.MATTE8, m_d, w)
     out["uncapped_nonzero_matte8_ms"] = _events_ms(stream, lambda: fill(_abi.NONZERO, _abi.MATTE8, m_d, w), 3)
     out["uncapped_coverage_fraction"] = float((m_d != 0).float().mean().item())
+    # who builds the one large figure: the whole GPU (built-in from FT_GRID_BUILD_OPS ops)
+    # or one CTA, capped and un-capped
+    fb = {}
+    for name, mode in (("grid", 2), ("one_cta", 1)):
+        ctx.tune(fig_build=mode)
+        for cap_name, cap in (("capped", 0), ("uncapped", 8 << 20)):
+            ctx.set_figure_cap(cap)
+            fill(_abi.NONZERO, _abi.MATTE8, m_d, w)
+            fb[f"{name}_{cap_name}_nonzero_matte8_ms"] = _events_ms(
+                stream, lambda: fill(_abi.NONZERO, _abi.MATTE8, m_d, w), 3)
+    ctx.set_tuning(None)
+    out["figure_build"] = fb
     ctx.set_figure_cap(0)
     # composite bytes: every Rgba8p pixel from the top row down is read and written
     out["rgba8p_composite_GBps"] = (w * h * 8) / (out["nonzero_rgba8p_ms"] * 1e-3) / 1e9

@@ -108,7 +108,8 @@ class Tuning(ctypes.Structure):
     _fields_ = [("warp_max_side", ctypes.c_int32), ("cta_smem_bytes", ctypes.c_int32),
                 ("split_px", ctypes.c_int32), ("grid_per_sm", ctypes.c_int32), ("band_rows", ctypes.c_int32),
                 ("pool_edges", ctypes.c_int32), ("host_chunks", ctypes.c_int32), ("host_mapped", ctypes.c_int32),
-                ("tile_w", ctypes.c_int32), ("tile_stage", ctypes.c_int32)]
+                ("tile_w", ctypes.c_int32), ("tile_stage", ctypes.c_int32),
+                ("fig_build", ctypes.c_int32)]
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}

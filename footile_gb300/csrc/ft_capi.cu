@@ -77,6 +77,8 @@ struct ft_ctx {
     DevBuf pool, pool_used, bandoff, crec;  // ordered composite
     DevBuf figbins;                         // one path's figure state and band counts (split binning)
     DevBuf mask;                            // a single large Rgba8p call's Matte8 coverage
+    DevBuf gbuf;                            // one fill path's grid-wide figure build
+    size_t gb_raw_cap = 0;                  // its raw vertex capacity (grows on demand)
     DevBuf srgb_lut, conv_src, conv_dst;    // ft_convert
     PlanSlot plan;                                   // the last batch's plan
     std::vector<std::unique_ptr<PlanSlot>> chunk_plans;  // host batches in pipelined chunks
@@ -92,7 +94,7 @@ struct ft_ctx {
     int sm_count = 0;
     int max_smem = 0;
     uint32_t fig_cap = 0;  // vertices per figure of a fill above footile's 65,535 (0: footile's cap)
-    ft_tuning tune{0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    ft_tuning tune{0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     bool tuned = false;  // `tune` replaces the built-in plan defaults
     std::string err;
 };
@@ -612,7 +614,7 @@ FT_API void ft_batch_destroy(ft_batch* b) {
 FT_API int ft_set_tuning(ft_ctx* c, const ft_tuning* t) {
     if (!c) return FT_ERR_ARG;
     if (!t) {
-        c->tune = ft_tuning{0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+        c->tune = ft_tuning{0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
         c->tuned = false;
         return FT_OK;
     }
@@ -621,7 +623,7 @@ FT_API int ft_set_tuning(ft_ctx* c, const ft_tuning* t) {
         t->split_px < 0 || t->grid_per_sm < 0 || t->band_rows < 0 || t->band_rows > ftk::NWARP ||
         t->pool_edges < 0 || t->host_chunks < 0 || t->host_chunks > 16 || t->host_mapped < 0 || t->host_mapped > 2 ||
         (t->tile_w != 0 && t->tile_w != 128 && t->tile_w != 256 && t->tile_w != 512 && t->tile_w != 1024) ||
-        t->tile_stage < 0 || t->tile_stage > 2)
+        t->tile_stage < 0 || t->tile_stage > 2 || t->fig_build < 0 || t->fig_build > 2)
         return fail(c, FT_ERR_ARG, "tuning out of range");
     c->tune = *t;
     c->tuned = true;
@@ -633,7 +635,7 @@ FT_API int ft_get_tuning(ft_ctx* c, ft_tuning* t) {
     if (c->tuned) {
         *t = c->tune;
     } else {
-        *t = ft_tuning{ftk::WARP_MAX_SIDE, 0, 1 << 20, 0, 0, 0, 0, 0, 0, 0};
+        *t = ft_tuning{ftk::WARP_MAX_SIDE, 0, 1 << 20, 0, 0, 0, 0, 0, 0, 0, 0};
     }
     return FT_OK;
 }
@@ -1070,6 +1072,16 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
     if (n_paths)
         FT_CU(cudaMemcpyAsync(c->paths.p, paths, sizeof(ft_path_desc) * n_paths, cudaMemcpyHostToDevice, c->stream),
               "upload paths");
+    // one fill path: its figure is built over the whole GPU (the grid build, whose raw
+    // vertex arrays grow until the path's raw vertices fit) or by one CTA of k_cbuild
+    const int fig_build = c->tuned ? c->tune.fig_build : 0;
+    bool grid_build = !stroke && n_paths == 1 && paths[0].n_ops > 0 &&
+                      (fig_build == 2 || (fig_build == 0 && paths[0].n_ops >= FT_GRID_BUILD_OPS));
+    if (grid_build && c->gb_raw_cap == 0) {
+        const uint64_t est = std::max<uint64_t>((uint64_t)paths[0].n_ops * 64, 1u << 20);
+        c->gb_raw_cap = (size_t)std::min<uint64_t>((est + ftk::GB_TILE - 1) / ftk::GB_TILE * ftk::GB_TILE,
+                                                   (uint64_t)ftk::GB_RAW_MAX);
+    }
     // edge pool: grows until every path's binned edges fit
     // first pool size in edges (it grows on demand)
     const bool penv = c->tuned && c->tune.pool_edges > 0;
@@ -1114,13 +1126,45 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
             p.fig_state = static_cast<int4*>(c->figbins.p);
             p.bin_hist = reinterpret_cast<int*>(static_cast<char*>(c->figbins.p) + 16);
         }
+        const size_t raw_cap = c->gb_raw_cap;
+        if (grid_build) {
+            const ftk::GbLayout G = ftk::gb_layout(paths[0].n_ops, raw_cap);
+            FT_CU(c->gbuf.ensure(G.bytes), "alloc grid build");
+            unsigned char* gb = static_cast<unsigned char*>(c->gbuf.p);
+            FT_CU(cudaMemsetAsync(gb, 0, 256, c->stream), "reset grid build");
+            FT_CU(cudaMemsetAsync(gb + G.tr, 0xFF, raw_cap / ftk::GB_TILE * sizeof(int), c->stream),
+                  "reset grid build");
+            ftk::GridBuildBufs& g = p.gb;
+            g.ops = ops_d + paths[0].op_begin;
+            g.n_ops = (int)paths[0].n_ops;
+            g.s_width = paths[0].s_width;
+            g.raw_cap = (int)raw_cap;
+            g.done = reinterpret_cast<unsigned*>(gb);
+            g.n_raw = reinterpret_cast<long long*>(gb + 32);
+            g.count = reinterpret_cast<int*>(gb + 40);
+            g.opa = reinterpret_cast<int2*>(gb + G.opa);
+            g.opn = reinterpret_cast<long long*>(gb + G.opn);
+            g.opi = reinterpret_cast<int2*>(gb + G.opi);
+            g.raw = reinterpret_cast<int2*>(gb + G.raw);
+            g.fl = gb + G.fl;
+            g.kp = gb + G.kp;
+            g.rk = reinterpret_cast<int*>(gb + G.rk);
+            g.tr = reinterpret_cast<int*>(gb + G.tr);
+            g.tp = reinterpret_cast<int4*>(gb + G.tp);
+            g.top = reinterpret_cast<int4*>(gb + G.top);
+        }
         c->comp_timed = false;
         FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
         if (n_paths) {
             Stage st_build("figure build and edge binning");
-            FT_CU(ftk::launch_composite_build(p, grid, smem_a, c->stream, grid <= c->sm_count),
-                  "launch composite build");
-            c->launches++;
+            if (grid_build) {
+                FT_CU(ftk::launch_grid_build(p, c->sm_count, c->stream), "launch grid figure build");
+                c->launches += 6;
+            } else {
+                FT_CU(ftk::launch_composite_build(p, grid, smem_a, c->stream, grid <= c->sm_count),
+                      "launch composite build");
+                c->launches++;
+            }
             if (split) {
                 FT_CU(ftk::launch_figure_bins(p, 4 * c->sm_count, c->stream), "launch figure bins");
                 c->launches += 3;
@@ -1131,7 +1175,21 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
         FT_CU(cudaMemcpyAsync(&used, c->pool_used.p, sizeof(used), cudaMemcpyDeviceToHost, c->stream), "pool size");
         if (n_paths == 1)
             FT_CU(cudaMemcpyAsync(&cr0, c->crec.p, sizeof(int4), cudaMemcpyDeviceToHost, c->stream), "path record");
+        long long n_raw = 0;
+        if (grid_build)
+            FT_CU(cudaMemcpyAsync(&n_raw, p.gb.n_raw, sizeof(n_raw), cudaMemcpyDeviceToHost, c->stream), "raw count");
         FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
+        if (grid_build && n_raw > (long long)raw_cap) {
+            // more raw vertices than the arrays hold: grow them, or build on one CTA
+            if (n_raw > ftk::GB_RAW_MAX) {
+                grid_build = false;
+            } else {
+                const long long want_raw = std::min<long long>(n_raw + n_raw / 8, ftk::GB_RAW_MAX);
+                c->gb_raw_cap = (size_t)((want_raw + ftk::GB_TILE - 1) / ftk::GB_TILE * ftk::GB_TILE);
+            }
+            attempt--;  // a raw-vertex retry does not count against the edge pool's
+            continue;
+        }
         if (used > p.pool_cap) {
             want = used + used / 4;
             continue;
@@ -1249,7 +1307,7 @@ static bool tune_lookup(const char* path, const std::string& key, ft_tuning* t) 
         char k[600];
         ft_tuning v;
         float ms;
-        v = ft_tuning{0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+        v = ft_tuning{0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
         if (sscanf(line, "%599s %d %d %d %d %d %d %d %d %d %d %f", k, &v.warp_max_side, &v.cta_smem_bytes,
                    &v.split_px, &v.grid_per_sm, &v.band_rows, &v.pool_edges, &v.host_chunks, &v.host_mapped,
                    &v.tile_w, &v.tile_stage, &ms) == 12 &&
@@ -1844,7 +1902,7 @@ FT_API int ft_autotune_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_o
     }
     if (ms_out) *ms_out = 0.0f;
     const std::string key = tune_key(c, stroke, rule, fmt, paths, n_paths);
-    ft_tuning best{0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    ft_tuning best{0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     if (tune_lookup(cache_path, key, &best) && ft_set_tuning(c, &best) == FT_OK) {
         if (chosen) *chosen = best;
         return FT_OK;
@@ -1867,7 +1925,7 @@ FT_API int ft_autotune_batch(ft_ctx* c, int32_t stroke, int32_t rule, const ft_o
                 if (sm > c->max_smem) continue;
                 // the batch plan's knobs; the composite and host-transfer knobs stay as set
                 c->tune = ft_tuning{ws, sm, 1 << 20, gp, saved.band_rows, saved.pool_edges, saved.host_chunks,
-                                    saved.host_mapped, saved.tile_w, saved.tile_stage};
+                                    saved.host_mapped, saved.tile_w, saved.tile_stage, saved.fig_build};
                 c->tuned = true;
                 ft_batch* b = nullptr;
                 if (ft_batch_create(c, stroke, rule, paths, n_paths, fmt, &b) != FT_OK) continue;

@@ -1212,6 +1212,38 @@ __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, B
     G::sync();
 }
 
+// Direction of a figure from its top vertex `top` (fig.rs:402-411): the vertex after it
+// and the one before it in its sub-figure.
+__device__ int fig_dir(int top, int count, const int2* pts, const int* ss) {
+    const int s = ss[top];
+    const int nf = (top + 1 < count && ss[top + 1] == s) ? top + 1 : s;
+    int nr;
+    if (top > s) {
+        nr = top - 1;
+    } else {
+        // last vertex of the sub-figure: ss[] is non-decreasing
+        int lo = top, hi = count - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (ss[mid] == s)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        nr = lo;
+    }
+    int2 p = pts[top], p0 = pts[nf], p1 = pts[nr];
+    int ax = wsub(p1.x, p.x), ay = wsub(p1.y, p.y);
+    int cx = wsub(p0.x, p.x), cy = wsub(p0.y, p.y);
+    // (p1 - p).widdershins(p0 - p) -> Forward   (fig.rs:116-119)
+    return (fxmul(ax, cy) > fxmul(cx, ay)) ? 0 : 1;
+}
+
+// min (y, x, id)
+__device__ __forceinline__ bool top_less(int ay, int ax, int ai, int by, int bx, int bi) {
+    return ay < by || (ay == by && (ax < bx || (ax == bx && ai < bi)));
+}
+
 // Top vertex (min (y, x, id)) and figure direction (fig.rs:402-411, 493-496).
 template <class G>
 __device__ void top_and_dir(CState& S, const int2* pts, const int* ss, int* tmp3) {
@@ -1252,29 +1284,7 @@ __device__ void top_and_dir(CState& S, const int2* pts, const int* ss, int* tmp3
                 bi = oi;
             }
         }
-        const int top = bi;
-        const int s = ss[top];
-        const int nf = (top + 1 < count && ss[top + 1] == s) ? top + 1 : s;
-        int nr;
-        if (top > s) {
-            nr = top - 1;
-        } else {
-            // last vertex of the sub-figure: ss[] is non-decreasing
-            int lo = top, hi = count - 1;
-            while (lo < hi) {
-                int mid = (lo + hi + 1) >> 1;
-                if (ss[mid] == s)
-                    lo = mid;
-                else
-                    hi = mid - 1;
-            }
-            nr = lo;
-        }
-        int2 p = pts[top], p0 = pts[nf], p1 = pts[nr];
-        int ax = wsub(p1.x, p.x), ay = wsub(p1.y, p.y);
-        int cx = wsub(p0.x, p.x), cy = wsub(p0.y, p.y);
-        // (p1 - p).widdershins(p0 - p) -> Forward   (fig.rs:116-119)
-        S.dir = (fxmul(ax, cy) > fxmul(cx, ay)) ? 0 : 1;
+        S.dir = fig_dir(bi, count, pts, ss);
         S.top_row = by >> 16;
     }
     G::sync();
@@ -2768,6 +2778,505 @@ cudaError_t launch_figure_bins(const KParams& p, int grid, cudaStream_t s) {
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_fig_bin_fill<<<grid, BLOCK, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+// ---- grid-wide figure build of one fill path
+//
+// footile builds the figure sequentially (Fig::add_point / Fig::close, fig.rs:373-461):
+// a raw vertex is kept when it starts a sub-figure or differs from the raw vertex before
+// it, and a close event (a Move or a Close before the next vertex, and the close that
+// Plotter::fill ends with, plotter.rs:347) pops the last vertex when it equals the
+// sub-figure's first.  Each of these decisions is a function of the raw stream alone:
+//   keep(k) = starts(k) or raw(k) != raw(k-1)
+//   pop(k)  = (starts(k+1) or k is the last raw vertex) and raw(k) == raw(R(k)),
+//             R(k) the last sub-figure start at or before k,
+// and the vertex count when raw vertex l is reached (the pops before it applied) is the
+// exclusive prefix sum pos(l) of keep - pop.  A kept vertex goes to position pos(k) with
+// sub-figure start pos(R(k)), unless it is the last kept vertex of a sub-figure that pops
+// (the next sub-figure's first vertex takes its position).  The cap (65,535, or
+// ft_set_figure_cap's) is reached at the first l with pos(l) >= cap: raw vertices from l
+// on are ignored, and the count is the cap less one when l starts no sub-figure and
+// raw(l-1) equals its sub-figure's first vertex (the close after the cap, as seq_group
+// takes it).  Without the cap the count is the sum of keep - pop over all raw vertices.
+//
+// pos(k) and pos(R(k)) come out of one scan under an associative combination of
+// (s: sum of keep - pop, h: has a sub-figure start, r: pos of the last start relative
+// to the range's beginning, mp: largest exclusive prefix in the range); mp finds the
+// first tile that reaches the cap.  Kernels, in stream order (each scan is run by the
+// last CTA of its kernel to finish):
+//   k_gb_ops    per 256 ops: the last Move/Line/Quad/Cubic/Close op and the last PenWidth op
+//   k_gb_count  every op's pen (the end point of the last such op before it) and raw
+//               vertex count (the count walk); scan of the counts
+//   k_gb_emit   every op's raw vertices at its offset (the emit walk); per tile of 1,024
+//               raw vertices its last sub-figure start, scanned
+//   k_gb_keep   keep, pop and R per raw vertex; tile aggregates, scanned
+//   k_gb_write  positions, the cap, the vertex and sub-figure start writes
+//   k_gb_top    the top vertex (min (y, x, id)), the direction, the figure state
+struct PAgg {
+    int s, h, r, mp;
+};
+constexpr int GB_NEG = -(1 << 30);  // mp of the empty range (sums stay within +-2^29)
+static_assert(GB_RAW_MAX <= (1ll << 29), "position sums fit the aggregate");
+__device__ __forceinline__ PAgg pa_id() { return PAgg{0, 0, 0, GB_NEG}; }
+__device__ __forceinline__ PAgg pa_comb(const PAgg& a, const PAgg& b) {
+    return PAgg{a.s + b.s, a.h | b.h, b.h ? a.s + b.r : a.r, max(a.mp, a.s + b.mp)};
+}
+// one raw vertex: keep - pop, and whether it starts a sub-figure
+__device__ __forceinline__ PAgg pa_elem(int v, int starts) { return PAgg{v, starts, 0, 0}; }
+__device__ __forceinline__ PAgg pa_shfl_up(const PAgg& a, int o) {
+    return PAgg{__shfl_up_sync(FULL, a.s, o), __shfl_up_sync(FULL, a.h, o), __shfl_up_sync(FULL, a.r, o),
+                __shfl_up_sync(FULL, a.mp, o)};
+}
+__device__ __forceinline__ PAgg pa_load(const int4* p) {
+    const int4 x = __ldcg(p);
+    return PAgg{x.x, x.y, x.z, x.w};
+}
+// Exclusive block scan under pa_comb; `total` receives the whole block's combination.
+__device__ PAgg block_scan_pa(PAgg v, PAgg* wt, PAgg& total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    PAgg inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const PAgg t = pa_shfl_up(inc, o);
+        if (lane >= o) inc = pa_comb(t, inc);
+    }
+    PAgg ex = pa_shfl_up(inc, 1);
+    if (lane == 0) ex = pa_id();
+    if (lane == 31) wt[w] = inc;
+    __syncthreads();
+    PAgg base = pa_id(), all = pa_id();
+    for (int k = 0; k < NWARP; k++) {
+        if (k == w) base = all;
+        all = pa_comb(all, wt[k]);
+    }
+    total = all;
+    __syncthreads();
+    return pa_comb(base, ex);
+}
+__device__ long long block_excl_sum_ll(long long v, long long* tmp, long long& total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    long long inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long t = __shfl_up_sync(FULL, inc, o);
+        if (lane >= o) inc += t;
+    }
+    if (lane == 31) tmp[w] = inc;
+    __syncthreads();
+    long long base = 0, all = 0;
+    for (int k = 0; k < NWARP; k++) {
+        if (k == w) base = all;
+        all += tmp[k];
+    }
+    total = all;
+    __syncthreads();
+    return base + inc - v;
+}
+
+// True in the last CTA of the grid to get here (after every CTA's global writes).
+__device__ bool gb_last_block(unsigned* ticket) {
+    __shared__ int s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(ticket, 1u) == gridDim.x - 1 ? 1 : 0;
+    __syncthreads();
+    const bool last = s_last != 0;
+    if (last) __threadfence();
+    return last;
+}
+
+__device__ __forceinline__ ft_op gb_op(const ft_op* ops, int i) {
+    const int4* src = reinterpret_cast<const int4*>(ops + i);
+    const int4 q0 = __ldg(src), q1 = __ldg(src + 1);
+    ft_op op;
+    op.kind = q0.x;
+    op.v[0] = __int_as_float(q0.y);
+    op.v[1] = __int_as_float(q0.z);
+    op.v[2] = __int_as_float(q0.w);
+    op.v[3] = __int_as_float(q1.x);
+    op.v[4] = __int_as_float(q1.y);
+    op.v[5] = __int_as_float(q1.z);
+    op.reserved = 0;
+    return op;
+}
+// Pen after op j, a Move/Line/Quad/Cubic/Close (a Close puts it at the origin,
+// plotter.rs:200-203), and j's kind; j < 0: the origin and kind -1.
+__device__ __forceinline__ void gb_pen(const ft_op* ops, int j, float& x, float& y, int& kind) {
+    x = 0.f;
+    y = 0.f;
+    kind = -1;
+    if (j < 0) return;
+    const ft_op op = gb_op(ops, j);
+    kind = op.kind;
+    if (kind == FT_OP_MOVE || kind == FT_OP_LINE) {
+        x = op.v[0];
+        y = op.v[1];
+    } else if (kind == FT_OP_QUAD) {
+        x = op.v[2];
+        y = op.v[3];
+    } else if (kind == FT_OP_CUBIC) {
+        x = op.v[4];
+        y = op.v[5];
+    }
+}
+// Raw vertices of a Move/Line/Quad/Cubic op with the pen at (px, py), as build_fill
+// flattens them for a fill: emit(k, vertex) in order; returns their number.  flags:
+// 1 depth cap reached, 2 non-finite control point.
+template <class Emit>
+__device__ int gb_walk(const KParams& P, const ft_op& op, int kind, float px, float py, int& flags, Emit emit) {
+    if (kind == FT_OP_MOVE || kind == FT_OP_LINE) {
+        const P2 A = xform(P.xf, p2(op.v[0], op.v[1]));
+        emit(0, make_int2(f2fx(A.x), f2fx(A.y)));
+        return 1;
+    }
+    const P2 A = xform(P.xf, p2(px, py)), B = xform(P.xf, p2(op.v[0], op.v[1])),
+             C = xform(P.xf, p2(op.v[2], op.v[3]));
+    auto leaf = [&](int k, P2 q, float) { emit(k, make_int2(f2fx(q.x), f2fx(q.y))); };
+    int dh = 0, n;
+    if (kind == FT_OP_QUAD) {
+        if (!pfinite(A) || !pfinite(B) || !pfinite(C)) {
+            flags |= 2;
+            emit(0, make_int2(f2fx(C.x), f2fx(C.y)));
+            return 1;
+        }
+        n = quad_walk<false>(A, B, C, 0.f, 0.f, 0.f, P.tol_sq, 0, INT_MAX, &dh, leaf);
+    } else {
+        const P2 D = xform(P.xf, p2(op.v[4], op.v[5]));
+        if (!pfinite(A) || !pfinite(B) || !pfinite(C) || !pfinite(D)) {
+            flags |= 2;
+            emit(0, make_int2(f2fx(D.x), f2fx(D.y)));
+            return 1;
+        }
+        n = cubic_walk<false>(A, B, C, D, 0.f, 0.f, 0.f, 0.f, P.tol_sq, 0, INT_MAX, &dh, leaf);
+    }
+    if (dh) flags |= 1;
+    return n;
+}
+
+__global__ void __launch_bounds__(BLOCK) k_gb_ops(KParams P) {
+    __shared__ int tmp[2 * NWARP + 2];
+    __shared__ int s_pc, s_pw;
+    const GridBuildBufs& G = P.gb;
+    const int tid = threadIdx.x, i = blockIdx.x * BLOCK + tid;
+    const int kind = i < G.n_ops ? __ldg(&G.ops[i].kind) : -1;
+    const int mpc = block_incl_max((kind >= FT_OP_CLOSE && kind <= FT_OP_CUBIC) ? i : -1, tmp);
+    const int mpw = block_incl_max(kind == FT_OP_PEN_WIDTH ? i : -1, tmp);
+    if (tid == BLOCK - 1) G.opa[blockIdx.x] = make_int2(mpc, mpw);
+    if (!gb_last_block(&G.done[0])) return;
+    // exclusive max over the blocks, in place
+    const int nb = (int)gridDim.x;
+    int cpc = -1, cpw = -1;
+    for (int b0 = 0; b0 < nb; b0 += BLOCK) {
+        const int b = b0 + tid;
+        const int2 a = b < nb ? __ldcg(&G.opa[b]) : make_int2(-1, -1);
+        int ipc, epc, ipw, epw;
+        block_max_scan(a.x, tmp, ipc, epc);
+        if (tid == BLOCK - 1) s_pc = ipc;
+        block_max_scan(a.y, tmp, ipw, epw);
+        if (tid == BLOCK - 1) s_pw = ipw;
+        __syncthreads();
+        if (b < nb) G.opa[b] = make_int2(max(cpc, epc), max(cpw, epw));
+        cpc = max(cpc, s_pc);
+        cpw = max(cpw, s_pw);
+        __syncthreads();
+    }
+    // pen width after the call: the last PenWidth op of the path
+    if (tid == 0 && P.sw_out) P.sw_out[0] = cpw >= 0 ? G.ops[cpw].v[0] : G.s_width;
+}
+
+__global__ void __launch_bounds__(BLOCK) k_gb_count(KParams P) {
+    __shared__ int tmp[2 * NWARP + 2];
+    __shared__ long long ltmp[NWARP];
+    const GridBuildBufs& G = P.gb;
+    const int tid = threadIdx.x, i = blockIdx.x * BLOCK + tid;
+    ft_op op;
+    int kind = -1;
+    if (i < G.n_ops) {
+        op = gb_op(G.ops, i);
+        kind = op.kind;
+    }
+    int flags = 0;
+    if (kind < -1 || kind > FT_OP_PEN_WIDTH) {
+        flags = 2;
+        kind = -1;
+    }
+    int inc, lpc;
+    block_max_scan((kind >= FT_OP_CLOSE && kind <= FT_OP_CUBIC) ? i : -1, tmp, inc, lpc);
+    lpc = max(lpc, G.opa[blockIdx.x].x);
+    int n = 0;
+    if (kind >= FT_OP_MOVE && kind <= FT_OP_CUBIC) {
+        float px, py;
+        int pk;
+        gb_pen(G.ops, lpc, px, py, pk);
+        n = gb_walk(P, op, kind, px, py, flags, [](int, int2) {});
+    }
+    if (flags) atomicMax(&P.status[0], (flags & 1) ? FT_ERR_DEPTH : FT_ERR_ARG);
+    int tot;
+    const int loc = block_excl_sum(n, tmp, tot);
+    if (i < G.n_ops) G.opi[i] = make_int2(lpc, loc);
+    if (tid == 0) G.opn[blockIdx.x] = tot;
+    if (!gb_last_block(&G.done[1])) return;
+    // exclusive sum over the blocks, in place; the total is the path's raw vertex count
+    const int nb = (int)gridDim.x;
+    long long carry = 0;
+    for (int b0 = 0; b0 < nb; b0 += BLOCK) {
+        const int b = b0 + tid;
+        long long t;
+        const long long ex = block_excl_sum_ll(b < nb ? __ldcg(&G.opn[b]) : 0ll, ltmp, t);
+        if (b < nb) G.opn[b] = carry + ex;
+        carry += t;
+    }
+    if (tid == 0) *G.n_raw = carry;
+}
+
+__global__ void __launch_bounds__(BLOCK) k_gb_emit(KParams P) {
+    __shared__ int tmp[2 * NWARP + 2];
+    __shared__ int s_c;
+    const GridBuildBufs& G = P.gb;
+    const long long n_raw = *G.n_raw;
+    if (n_raw > G.raw_cap) return;  // every CTA: the caller grows the arrays
+    const int tid = threadIdx.x, i = blockIdx.x * BLOCK + tid;
+    if (i < G.n_ops) {
+        const ft_op op = gb_op(G.ops, i);
+        const int kind = op.kind;
+        if (kind >= FT_OP_MOVE && kind <= FT_OP_CUBIC) {
+            const int2 oi = G.opi[i];
+            const int off = (int)(G.opn[blockIdx.x] + oi.y);
+            float px, py;
+            int pk;
+            gb_pen(G.ops, oi.x, px, py, pk);
+            // the first vertex of this op starts a sub-figure after a close event
+            const int rs = kind == FT_OP_MOVE || pk == FT_OP_CLOSE || pk == -1;
+            int flags = 0;
+            int2* raw = G.raw;
+            unsigned char* fl = G.fl;
+            const int cap = G.raw_cap;
+            gb_walk(P, op, kind, px, py, flags, [&](int k, int2 q) {
+                if (ck(off + k < cap, 13) && off + k < cap) {
+                    raw[off + k] = q;
+                    fl[off + k] = k == 0 ? (unsigned char)rs : (unsigned char)0;
+                }
+            });
+            if (rs && ck(off < cap, 13) && off < cap) atomicMax(&G.tr[off / GB_TILE], off);
+        }
+    }
+    if (!gb_last_block(&G.done[2])) return;
+    // exclusive max of the tiles' last sub-figure starts, in place
+    const int nt = (int)((n_raw + GB_TILE - 1) / GB_TILE);
+    int carry = -1;
+    for (int b0 = 0; b0 < nt; b0 += BLOCK) {
+        const int b = b0 + tid;
+        int inc, exc;
+        block_max_scan(b < nt ? __ldcg(&G.tr[b]) : -1, tmp, inc, exc);
+        if (tid == BLOCK - 1) s_c = inc;
+        __syncthreads();
+        if (b < nt) G.tr[b] = max(carry, exc);
+        carry = max(carry, s_c);
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(BLOCK) k_gb_keep(KParams P) {
+    __shared__ int tmp[2 * NWARP + 2];
+    __shared__ PAgg wt[NWARP];
+    const GridBuildBufs& G = P.gb;
+    const long long n_raw = *G.n_raw;
+    if (n_raw > G.raw_cap) return;
+    const int M = (int)n_raw, nt = (M + GB_TILE - 1) / GB_TILE, tid = threadIdx.x;
+    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+        const int k0 = t * GB_TILE + GB_PER * tid;
+        int2 p[GB_PER];
+        int rl[GB_PER];
+        int st = 0, run = -1;
+#pragma unroll
+        for (int j = 0; j < GB_PER; j++) {
+            const int k = k0 + j;
+            p[j] = make_int2(0, 0);
+            if (k < M) {
+                p[j] = G.raw[k];
+                if (G.fl[k] & 1) {
+                    st |= 1 << j;
+                    run = k;
+                }
+            }
+            rl[j] = run;
+        }
+        int inc, exc;
+        block_max_scan(run, tmp, inc, exc);
+        const int carry = max(G.tr[t], exc);
+        int2 q = (k0 > 0 && k0 <= M) ? G.raw[k0 - 1] : make_int2(0, 0);  // raw predecessor
+        PAgg a = pa_id();
+#pragma unroll
+        for (int j = 0; j < GB_PER; j++) {
+            const int k = k0 + j;
+            if (k < M) {
+                const int R = max(0, max(carry, rl[j]));  // raw vertex 0 always starts one
+                const int2 f = G.raw[R];
+                const int s = (st >> j) & 1;
+                const bool keep = s || p[j].x != q.x || p[j].y != q.y;
+                const bool ends = k + 1 >= M || (G.fl[k + 1] & 1);
+                const bool pop = ends && p[j].x == f.x && p[j].y == f.y;
+                G.kp[k] = (unsigned char)((keep ? 1 : 0) | (pop ? 2 : 0));
+                G.rk[k] = R;
+                a = pa_comb(a, pa_elem((keep ? 1 : 0) - (pop ? 1 : 0), s));
+            }
+            q = p[j];
+        }
+        PAgg tot;
+        block_scan_pa(a, wt, tot);
+        if (tid == 0) G.tp[t] = make_int4(tot.s, tot.h, tot.r, tot.mp);
+    }
+    if (!gb_last_block(&G.done[3])) return;
+    // exclusive scan of the tiles, in place, GB_PER tiles a thread; the total is the
+    // vertex count when the cap is not reached
+    PAgg carry = pa_id();
+    for (int b0 = 0; b0 < nt; b0 += GB_TILE) {
+        const int b = b0 + GB_PER * tid;
+        PAgg v[GB_PER], a = pa_id();
+#pragma unroll
+        for (int j = 0; j < GB_PER; j++) {
+            v[j] = b + j < nt ? pa_load(&G.tp[b + j]) : pa_id();
+            a = pa_comb(a, v[j]);
+        }
+        PAgg tot;
+        PAgg ex = pa_comb(carry, block_scan_pa(a, wt, tot));
+#pragma unroll
+        for (int j = 0; j < GB_PER; j++) {
+            if (b + j < nt) G.tp[b + j] = make_int4(ex.s, ex.h, ex.r, ex.mp);
+            ex = pa_comb(ex, v[j]);
+        }
+        carry = pa_comb(carry, tot);
+    }
+    if (tid == 0) *G.count = carry.s;
+}
+
+__global__ void __launch_bounds__(BLOCK) k_gb_write(KParams P) {
+    __shared__ PAgg wt[NWARP];
+    __shared__ int s_l;
+    const GridBuildBufs& G = P.gb;
+    const long long n_raw = *G.n_raw;
+    if (n_raw > G.raw_cap) return;
+    const int M = (int)n_raw, nt = (M + GB_TILE - 1) / GB_TILE, tid = threadIdx.x, cap = P.pt_cap;
+    int2* pts = reinterpret_cast<int2*>(P.scratch + P.L.pts);
+    int* ss = reinterpret_cast<int*>(P.scratch + P.L.ss);
+    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+        const PAgg C = pa_load(&G.tp[t]);
+        if (C.mp >= cap) continue;  // the cap was reached before this tile
+        const int k0 = t * GB_TILE + GB_PER * tid;
+        int kp[GB_PER], st[GB_PER];
+        PAgg a = pa_id();
+#pragma unroll
+        for (int j = 0; j < GB_PER; j++) {
+            const int k = k0 + j;
+            kp[j] = 0;
+            st[j] = 0;
+            if (k < M) {
+                kp[j] = G.kp[k];
+                st[j] = G.fl[k] & 1;
+                a = pa_comb(a, pa_elem((kp[j] & 1) - ((kp[j] >> 1) & 1), st[j]));
+            }
+        }
+        if (tid == 0) s_l = INT_MAX;
+        PAgg tot;
+        PAgg run = pa_comb(C, block_scan_pa(a, wt, tot));
+        int pos[GB_PER], posr[GB_PER], lc = INT_MAX;
+#pragma unroll
+        for (int j = 0; j < GB_PER; j++) {
+            const int k = k0 + j;
+            pos[j] = run.s;
+            if (k < M) {
+                if (run.s >= cap) lc = min(lc, k);
+                run = pa_comb(run, pa_elem((kp[j] & 1) - ((kp[j] >> 1) & 1), st[j]));
+            }
+            posr[j] = run.r;
+        }
+        if (lc != INT_MAX) atomicMin(&s_l, lc);
+        __syncthreads();
+        const int l = s_l;  // first raw vertex at the cap, INT_MAX: not in this tile
+#pragma unroll
+        for (int j = 0; j < GB_PER; j++) {
+            const int k = k0 + j;
+            if (k >= M || k >= l || !(kp[j] & 1)) continue;
+            const int2 v = G.raw[k], f = G.raw[G.rk[k]];
+            bool gone = false;
+            if (v.x == f.x && v.y == f.y) {
+                // the last kept vertex of a sub-figure that pops: the next kept vertex
+                // starts a sub-figure (or there is none)
+                int m = k + 1;
+                while (m < M && !(G.kp[m] & 1)) m++;
+                gone = m >= M || (G.fl[m] & 1);
+            }
+            if (!gone && ck(pos[j] >= 0 && pos[j] < cap, 14) && pos[j] >= 0 && pos[j] < cap) {
+                pts[pos[j]] = v;
+                ss[pos[j]] = posr[j];
+            }
+        }
+        if (l != INT_MAX && l >= k0 && l < k0 + GB_PER) {
+            // the close after the cap pops the last vertex if it equals its sub-figure's first
+            const int2 v = G.raw[l - 1], f = G.raw[G.rk[l - 1]];
+            *G.count = cap - ((!(G.fl[l] & 1) && v.x == f.x && v.y == f.y) ? 1 : 0);
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(BLOCK) k_gb_top(KParams P) {
+    __shared__ int4 wb[NWARP];
+    const GridBuildBufs& G = P.gb;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int count = *G.n_raw > G.raw_cap ? 0 : *G.count;
+    const int2* pts = reinterpret_cast<const int2*>(P.scratch + P.L.pts);
+    const int* ss = reinterpret_cast<const int*>(P.scratch + P.L.ss);
+    int by = INT_MAX, bx = INT_MAX, bi = INT_MAX;
+    for (int i = blockIdx.x * BLOCK + tid; i < count; i += gridDim.x * BLOCK) {
+        const int2 p = pts[i];
+        if (top_less(p.y, p.x, i, by, bx, bi)) {
+            by = p.y;
+            bx = p.x;
+            bi = i;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const int oy = __shfl_down_sync(FULL, by, o), ox = __shfl_down_sync(FULL, bx, o),
+                  oi = __shfl_down_sync(FULL, bi, o);
+        if (top_less(oy, ox, oi, by, bx, bi)) {
+            by = oy;
+            bx = ox;
+            bi = oi;
+        }
+    }
+    if (lane == 0) wb[w] = make_int4(by, bx, bi, 0);
+    __syncthreads();
+    if (tid == 0) {
+        int4 b = wb[0];
+        for (int k = 1; k < NWARP; k++)
+            if (top_less(wb[k].x, wb[k].y, wb[k].z, b.x, b.y, b.z)) b = wb[k];
+        G.top[blockIdx.x] = b;
+    }
+    if (!gb_last_block(&G.done[4])) return;
+    if (tid == 0) {
+        int4 b = make_int4(INT_MAX, INT_MAX, INT_MAX, 0);
+        for (int k = 0; k < (int)gridDim.x; k++) {
+            const int4 o = __ldcg(&G.top[k]);
+            if (top_less(o.x, o.y, o.z, b.x, b.y, b.z)) b = o;
+        }
+        P.fig_state[0] = count > 0 ? make_int4(count, fig_dir(b.z, count, pts, ss), b.x >> 16, 0)
+                                   : make_int4(0, 0, 0, 0);
+    }
+}
+
+cudaError_t launch_grid_build(const KParams& p, int sm_count, cudaStream_t s) {
+    const int nbo = (p.gb.n_ops + BLOCK - 1) / BLOCK;
+    if (nbo <= 0 || p.gb.raw_cap % GB_TILE || p.gb.raw_cap > GB_RAW_MAX) return cudaErrorInvalidValue;
+    const int gt = std::max(1, 4 * sm_count);
+    k_gb_ops<<<nbo, BLOCK, 0, s>>>(p);
+    k_gb_count<<<nbo, BLOCK, 0, s>>>(p);
+    k_gb_emit<<<nbo, BLOCK, 0, s>>>(p);
+    k_gb_keep<<<gt, BLOCK, 0, s>>>(p);
+    k_gb_write<<<gt, BLOCK, 0, s>>>(p);
+    k_gb_top<<<GB_TOP_BLOCKS, BLOCK, 0, s>>>(p);
     return cudaGetLastError();
 }
 

@@ -100,6 +100,52 @@ constexpr size_t WS_BYTES = align256(WS_ACT + (size_t)WARP_CAP * sizeof(int4)); 
 constexpr int SWEEP_END_FAR = 1023;  // sweep record end row: beyond the warp's last row
 static_assert(NWARP * WS_BYTES <= SCRATCH_BYTES_PER_CTA, "warp scratch layout");
 
+// Grid-wide figure build of one fill path (launch_grid_build): per-op and per-raw-vertex
+// arrays in one device buffer laid out by gb_layout.
+constexpr int GB_PER = 4;                      // raw vertices per thread of the tile kernels
+constexpr int GB_TILE = GB_PER * BLOCK;        // raw vertices per tile
+constexpr int GB_TOP_BLOCKS = 512;             // CTAs of the top-vertex search
+constexpr long long GB_RAW_MAX = 1ll << 29;    // raw vertices the grid build takes at most
+struct GridBuildBufs {
+    const ft_op* ops;   // the path's ops
+    int n_ops;
+    float s_width;      // pen width before the path
+    int raw_cap;        // raw vertices the arrays hold (a multiple of GB_TILE)
+    unsigned* done;     // [8] tickets: the last CTA of a kernel to finish runs its scan
+    long long* n_raw;   // raw vertices of the path
+    int* count;         // vertices kept
+    int2* opa;          // per block of 256 ops: last Move/Line/Quad/Cubic/Close op, last PenWidth op
+    long long* opn;     // per block of 256 ops: raw vertices
+    int2* opi;          // per op: last Move/Line/Quad/Cubic/Close op before it, raw offset in its block
+    int2* raw;          // raw vertices, 16.16
+    unsigned char* fl;  // per raw vertex: 1 = starts a sub-figure
+    unsigned char* kp;  // per raw vertex: 1 = kept, 2 = pops its sub-figure's first vertex
+    int* rk;            // per raw vertex: the first raw vertex of its sub-figure
+    int* tr;            // per tile: last sub-figure start
+    int4* tp;           // per tile: position aggregate (kept - popped, runs, max prefix)
+    int4* top;          // per CTA of the top-vertex search: min (y, x, id)
+};
+struct GbLayout {
+    size_t state, opa, opn, opi, raw, fl, kp, rk, tr, tp, top, bytes;
+};
+constexpr GbLayout gb_layout(size_t n_ops, size_t raw_cap) {
+    GbLayout g{};
+    const size_t nbo = (n_ops + BLOCK - 1) / BLOCK, ntiles = raw_cap / GB_TILE;
+    g.state = 0;  // done[8] at 0, n_raw at 32, count at 40
+    g.opa = 256;
+    g.opn = align256(g.opa + nbo * 8);
+    g.opi = align256(g.opn + nbo * 8);
+    g.raw = align256(g.opi + n_ops * 8);
+    g.fl = align256(g.raw + raw_cap * 8);
+    g.kp = align256(g.fl + raw_cap);
+    g.rk = align256(g.kp + raw_cap);
+    g.tr = align256(g.rk + raw_cap * 4);
+    g.tp = align256(g.tr + ntiles * 4);
+    g.top = align256(g.tp + ntiles * 16);
+    g.bytes = align256(g.top + (size_t)GB_TOP_BLOCKS * 16);
+    return g;
+}
+
 struct KParams {
     const ft_op* ops;
     const ft_path_desc* paths;
@@ -145,6 +191,8 @@ struct KParams {
     // whether the canvas is staged by TMA through the tensor map passed beside these
     int seg_w;
     int use_tma;
+    // one fill path built over the whole GPU (launch_grid_build) instead of by k_cbuild
+    GridBuildBufs gb;
 };
 
 // Ordered composite: per-path figure build and edge binning, then one CTA per band.
@@ -165,6 +213,13 @@ cudaError_t launch_srcover_mask(const CUtensorMap& canvas, const CUtensorMap& ma
 // Edges and band bins of a single path's figure (after k_cbuild with split_bin), over
 // the whole GPU: edge records and band counts, a scan and pool allocation, the fill.
 cudaError_t launch_figure_bins(const KParams& p, int grid, cudaStream_t s);
+// The figure of one fill path (p.gb's ops) over the whole GPU, in place of k_cbuild with
+// split_bin: vertices and sub-figure starts into CTA 0's scratch, fig_state[0], the pen
+// width after the path and the path's status.  p.gb's state (done, n_raw, count) must be
+// zero and tr all -1 (bytes 0xFF) before the launch.  When the path has more raw
+// vertices than p.gb.raw_cap, *n_raw says how many and nothing else is written but a
+// figure of no vertices; the caller grows the arrays and builds again.
+cudaError_t launch_grid_build(const KParams& p, int sm_count, cudaStream_t s);
 int composite_bands_smem(int band_rows, int width);
 int composite_build_blocks_per_sm(int smem_bytes, bool stroke);
 

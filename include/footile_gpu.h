@@ -42,6 +42,9 @@ enum {
 /* Maximum De Casteljau / round-join arc recursion depth.  footile recurses without
  * a limit (README.md:32-33); deeper subdivisions are emitted as leaves and flagged. */
 #define FT_MAX_DEPTH 22
+/* Single fill paths of at least this many ops build their figure over the whole GPU
+ * (ft_tuning.fig_build). */
+#define FT_GRID_BUILD_OPS 2048
 
 /* Vertices kept per figure, from `Vid(u16)` (src/vid.rs:9-18, src/fig.rs:428-442). */
 #define FT_MAX_POINTS 65535
@@ -205,7 +208,10 @@ FT_API void ft_batch_destroy(ft_batch* batch);
  * `tile_stage`, how an Rgba8p compositor tile reaches the canvas: 1 = staged in shared
  * memory by TMA (when the canvas base and row stride are 16-byte aligned), 2 = read and
  * written in place, 0 = built-in; `pool_edges`, the first size of the binned-edge pool in edges (it
- * grows on demand; 0 = built-in).  Host batches (ft_fill_batch with
+ * grows on demand; 0 = built-in); `fig_build`, who builds the figure of a single fill
+ * path (ft_fill of at least split_px pixels, or an ft_composite_batch of one path):
+ * 1 = one CTA, 2 = the whole GPU (scans over the path's ops and raw vertices), 0 =
+ * built-in: the whole GPU from FT_GRID_BUILD_OPS ops.  Host batches (ft_fill_batch with
  * FT_HOST): `host_chunks`, chunks of the copy pipeline (1..16, 0 = built-in: 2 from
  * 64 MB of rasters); `host_mapped`, 0 = page-locked Matte8 rasters are written and
  * page-locked ops read in place (built-in), 1 = rasters and ops are copied, 2 = rasters
@@ -222,6 +228,7 @@ typedef struct ft_tuning {
     int32_t host_mapped;
     int32_t tile_w;
     int32_t tile_stage;
+    int32_t fig_build;
 } ft_tuning;
 FT_API int ft_set_tuning(ft_ctx* ctx, const ft_tuning* tuning);
 FT_API int ft_get_tuning(ft_ctx* ctx, ft_tuning* tuning);
@@ -393,7 +400,8 @@ FT_API int ft_last_composite_ms(ft_ctx* ctx, float* ms);
 
 /* Bounds-check build (the library compiled with -DFT_CHECK=1) — no counterpart in
  * footile; it stands in for a memory checker.  Device code checks the indices of its
- * shared-memory cell buffers, warp scratch, edge pool and compositor queues; a failed check
+ * shared-memory cell buffers, warp scratch, edge pool, compositor queues and the grid-wide
+ * figure build's raw vertices and figure writes; a failed check
  * skips the access and keeps the first failing site's number.  `site` (may be NULL)
  * receives that number since the last call (0: none) and is reset; `compiled_in` (may be
  * NULL) is 1 in the check build and 0 in the shipped build, whose checks fold away. */

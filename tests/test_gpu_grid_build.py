@@ -1,0 +1,132 @@
+"""The grid-wide figure build (k_gb_* in footile_gb300/csrc/ft_kernels.cu) against the
+oracle: single fills sent to the one-build compositor (split_px 1) with the figure built
+by the whole GPU (fig_build 2) and, beside it, by one CTA (fig_build 1).  Random line
+paths with coincident points, returns to the start, Moves and Closes in every order;
+random curve paths under a transform; the 65,535-vertex cap crossed at many offsets;
+status words, the pen width after the call, and un-capped figures."""
+import numpy as np
+import pytest
+
+import oracle
+from footile_gb300 import _abi, workloads
+from footile_gb300.path import Path2D, PathOp, ops_array
+from footile_gb300.plotter import Plotter
+
+from helpers import assert_same, gpu_vs_oracle
+from test_grid_build_model import random_lines
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(params=[2, 1], ids=["grid", "cta"])
+def build(request, ctx):
+    ctx.tune(split_px=1, fig_build=request.param)
+    return request.param
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_random_line_paths(ctx, build, seed):
+    rng = np.random.default_rng(100 + seed)
+    ops = random_lines(rng, int(rng.integers(1, 3000)), grid=int(rng.integers(2, 60)))
+    ops["v"][:, :2] *= np.float32(4.0)  # grid points 1 px apart on a 64 px canvas
+    fmt = _abi.MATTE8 if seed % 2 else _abi.RGBA8P
+    rule = _abi.NONZERO if seed % 3 else _abi.EVENODD
+    got, want, *_ = gpu_vs_oracle(ctx, ops, 64, 64, fmt=fmt, rule=rule, clr=(200, 40, 90, 180), init=37)
+    assert_same(got, want, f"lines seed {seed}")
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_random_curve_paths(ctx, build, seed):
+    rng = np.random.default_rng(200 + seed)
+    ops = workloads.random_path(rng, 300, int(rng.integers(20, 400)), n_sub=int(rng.integers(1, 12)),
+                                close=bool(seed % 2))
+    xf = (1.25, 0.125, 5.0, -0.25, 0.75, 9.0) if seed % 3 == 0 else _abi.IDENTITY
+    got, want, *_ = gpu_vs_oracle(ctx, ops, 384, 320, fmt=_abi.RGBA8P, clr=(20, 200, 90, 255), init=3,
+                                  tolerance=(0.05, 0.3, 1.0)[seed % 3], transform=xf)
+    assert_same(got, want, f"curves seed {seed}")
+
+
+@pytest.mark.parametrize("extra", [-2, -1, 0, 1, 3])
+@pytest.mark.parametrize("tail", ["dup", "back", "move", "close"])
+def test_cap_crossing(ctx, build, extra, tail):
+    n = _abi.MAX_POINTS + extra
+    k = np.arange(n)
+    ops = np.zeros(n + 3, dtype=_abi.OP_DTYPE)
+    ops["kind"][0] = _abi.OP_MOVE
+    ops["kind"][1:n] = _abi.OP_LINE
+    ops["v"][:n, 0] = ((k * 7919) % 256).astype(np.float32) * np.float32(0.25)
+    ops["v"][:n, 1] = ((k * 104729) % 240).astype(np.float32) * np.float32(0.25)
+    x, y = float(ops["v"][n - 1, 0]), float(ops["v"][n - 1, 1])
+    x0, y0 = float(ops["v"][0, 0]), float(ops["v"][0, 1])
+    t = ops_array({
+        "dup": [PathOp.Line(x, y), PathOp.Line(33.0, 21.0)],
+        "back": [PathOp.Line(x0, y0), PathOp.Line(x0, y0)],
+        "move": [PathOp.Move(5.0, 5.0), PathOp.Line(40.0, 9.0), PathOp.Line(12.0, 50.0)],
+        "close": [PathOp.Line(x0, y0), PathOp.Close(), PathOp.Line(30.0, 30.0)],
+    }[tail])
+    ops[n:n + len(t)] = t
+    ops = ops[:n + len(t)]
+    got, want, *_ = gpu_vs_oracle(ctx, ops, 64, 60, rule=_abi.EVENODD)
+    assert_same(got, want, f"cap {tail} {extra}")
+
+
+def test_many_short_subfigures_over_the_cap(ctx, build):
+    rng = np.random.default_rng(9)
+    ops = random_lines(rng, 150000, grid=200, p_move=0.2, p_close=0.2, p_back=0.2)
+    ops["v"][:, :2] *= np.float32(1.5)
+    got, want, *_ = gpu_vs_oracle(ctx, ops, 80, 80, fmt=_abi.RGBA8P, clr=(9, 99, 199, 255), init=200)
+    assert_same(got, want, "short sub-figures")
+
+
+def test_status_and_pen_width(ctx, build):
+    nan = float("nan")
+    ops = ops_array([PathOp.PenWidth(3.0), PathOp.Move(1, 1), PathOp.Quad(nan, 5, 9, 9), PathOp.Line(12, 1),
+                     PathOp.PenWidth(6.5), PathOp.Close()])
+    got, want, st, sw, err = gpu_vs_oracle(ctx, ops, 16, 16)
+    assert st == _abi.ERR_ARG and err is not None and err.code == _abi.ERR_ARG
+    assert_same(got, want, "nan quad")
+    r = np.zeros((8, 8), np.uint8)
+    p = Plotter(r, context=ctx)
+    ctx.set_pen_width(1.0)
+    p.fill(_abi.NONZERO, Path2D().pen_width(5.5).move_to(1, 1).line_to(6, 2).pen_width(2.5).line_to(3, 6)
+           .finish())
+    assert p.pen_width() == 2.5
+    p.fill(_abi.NONZERO, ops_array([PathOp.Move(1, 1), PathOp.Line(6, 2), PathOp.Line(3, 6)]))
+    assert p.pen_width() == 2.5
+
+
+def test_empty_and_vertexless_paths(ctx, build):
+    for ops in ([PathOp.Close()], [PathOp.PenWidth(2.0), PathOp.Close(), PathOp.Close()],
+                [PathOp.Move(3, 3)], [PathOp.Move(3, 3), PathOp.Line(3, 3), PathOp.Close()]):
+        got, want, *_ = gpu_vs_oracle(ctx, ops_array(ops), 8, 8, fmt=_abi.RGBA8P, clr=(1, 2, 3, 4), init=77)
+        assert_same(got, want, "empty")
+
+
+@pytest.mark.parametrize("cap", [80000, 4 << 20])
+def test_uncapped(ctx, build, cap):
+    ops = workloads.random_path(np.random.default_rng(17), 512, 100, n_sub=120, close=True)
+    want = np.zeros((512, 512, 4), np.uint8)
+    oracle.fill(_abi.NONZERO, ops, want, _abi.RGBA8P, (30, 120, 200, 255), fig_cap=cap)
+    ctx.set_figure_cap(cap)
+    try:
+        got = np.zeros_like(want)
+        Plotter(got, context=ctx).fill(_abi.NONZERO, ops, (30, 120, 200, 255))
+    finally:
+        ctx.set_figure_cap(0)
+    assert_same(got, want, f"un-capped {cap}")
+
+
+def test_raw_arrays_grow(ctx):
+    """A first path sizes the raw vertex arrays; a path with far more raw vertices per op
+    (long cubics) makes the build grow them and run again."""
+    ctx.tune(split_px=1, fig_build=2)
+    small = ops_array([PathOp.Move(1, 1), PathOp.Line(60, 3), PathOp.Line(30, 60)])
+    got, want, *_ = gpu_vs_oracle(ctx, small, 64, 64)
+    assert_same(got, want, "small")
+    ops = [PathOp.Move(0, 0)]
+    rng = np.random.default_rng(5)
+    for _ in range(200000):
+        ops.append(PathOp.Cubic(*(rng.random(6) * 4000).astype(np.float32).tolist()))
+    ops = ops_array(ops)
+    got, want, *_ = gpu_vs_oracle(ctx, ops, 1000, 900, tolerance=0.05)
+    assert_same(got, want, "long cubics")
