@@ -1145,6 +1145,7 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
             g.opa = reinterpret_cast<int2*>(gb + G.opa);
             g.opn = reinterpret_cast<long long*>(gb + G.opn);
             g.opi = reinterpret_cast<int2*>(gb + G.opi);
+            g.opl = reinterpret_cast<int*>(gb + G.opl);
             g.raw = reinterpret_cast<int2*>(gb + G.raw);
             g.fl = gb + G.fl;
             g.kp = gb + G.kp;

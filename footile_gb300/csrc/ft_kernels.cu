@@ -206,13 +206,14 @@ struct CubicFr<false> {
 
 // Walk the subdivision of a quad (plotter.rs:248-265) in depth-first order.
 // Leaves with index in [lo, hi) go to emit(index, point, width).  Returns the
-// number of leaves walked (the total when hi == INT_MAX).
+// number of leaves walked (the total when hi == INT_MAX).  `d0`: the depth of (a, b, c)
+// in the subdivision of a larger curve (0: the curve itself).
 template <bool W, class Emit>
 __device__ int quad_walk(P2 a, P2 b, P2 c, float wa, float wb, float wc, float tol_sq, int lo, int hi,
-                         int* depth_hit, Emit emit) {
+                         int* depth_hit, Emit emit, int d0 = 0) {
     using Fr = QuadFr<W>;
     Fr st[FT_MAX_DEPTH + 1];
-    int sp = 0, leaf = 0, d = 0;
+    int sp = 0, leaf = 0, d = d0;
     for (;;) {
         P2 ab = pmid(a, b), bc = pmid(b, c), abbc = pmid(ab, bc), ac = pmid(a, c);
         bool within = pdist_sq(abbc, ac) <= tol_sq;
@@ -261,10 +262,10 @@ __device__ int quad_walk(P2 a, P2 b, P2 c, float wa, float wb, float wc, float t
 // The same for a cubic (plotter.rs:311-332).
 template <bool W, class Emit>
 __device__ int cubic_walk(P2 a, P2 b, P2 c, P2 e, float wa, float wb, float wc, float we, float tol_sq, int lo,
-                          int hi, int* depth_hit, Emit emit) {
+                          int hi, int* depth_hit, Emit emit, int d0 = 0) {
     using Fr = CubicFr<W>;
     Fr st[FT_MAX_DEPTH + 1];
-    int sp = 0, leaf = 0, d = 0;
+    int sp = 0, leaf = 0, d = d0;
     for (;;) {
         P2 ab = pmid(a, b), bc = pmid(b, c), cd = pmid(c, e);
         P2 abbc = pmid(ab, bc), bccd = pmid(bc, cd);
@@ -2708,18 +2709,34 @@ __device__ __forceinline__ FigBins fig_bins(const KParams& P) {
     return f;
 }
 
+// Bands counted in shared memory by each CTA of the edge binning (one global atomic per
+// CTA and band instead of one per edge and band); more bands count in global memory.
+constexpr int BIN_SMEM_BANDS = 8192;
+
 __global__ void __launch_bounds__(BLOCK) k_fig_edges(KParams P) {
+    extern __shared__ int sh_bins[];  // n_bands counts (when n_bands <= BIN_SMEM_BANDS)
     const FigBins f = fig_bins(P);
+    const bool local = f.nb <= BIN_SMEM_BANDS;
     const unsigned char* scr = P.scratch;
     const int2* pts = reinterpret_cast<const int2*>(scr + P.L.pts);
     const int* ss = reinterpret_cast<const int*>(scr + P.L.ss);
     EdgeRec* edges = reinterpret_cast<EdgeRec*>(P.scratch + P.L.edges);
+    if (local) {
+        for (int b = threadIdx.x; b < f.nb; b += BLOCK) sh_bins[b] = 0;
+        __syncthreads();
+    }
+    int* hist = local ? sh_bins : P.bin_hist;
     for (int e = blockIdx.x * BLOCK + threadIdx.x; e < f.count; e += gridDim.x * BLOCK) {
         const EdgeRec E = edge_rec(e, f.count, f.figdir, pts, ss);
         edges[e] = E;
         if (!E.ed) continue;
         const int lo = max(E.start_row - f.tmin, f.rb), hi = min(E.end_row - f.tmin, f.H - 1);
-        for (int b = lo / f.R; lo <= hi && b <= hi / f.R; b++) atomicAdd(&P.bin_hist[b], 1);
+        for (int b = lo / f.R; lo <= hi && b <= hi / f.R; b++) atomicAdd(&hist[b], 1);
+    }
+    if (local) {
+        __syncthreads();
+        for (int b = threadIdx.x; b < f.nb; b += BLOCK)
+            if (sh_bins[b]) atomicAdd(&P.bin_hist[b], sh_bins[b]);
     }
 }
 
@@ -2749,12 +2766,30 @@ __global__ void __launch_bounds__(BLOCK) k_fig_bin_scan(KParams P) {
 }
 
 __global__ void __launch_bounds__(BLOCK) k_fig_bin_fill(KParams P) {
+    extern __shared__ int sh_bins[];  // n_bands counts, then n_bands cursors (n_bands <= BIN_SMEM_BANDS)
     const FigBins f = fig_bins(P);
     if (!P.fig_state[0].w) return;
+    const bool local = f.nb <= BIN_SMEM_BANDS;
     const int4 cr = P.crec[0];
     const unsigned long long base = (unsigned long long)(unsigned)cr.z | ((unsigned long long)(unsigned)cr.w << 32);
     const int4* erec = reinterpret_cast<const int4*>(P.scratch + P.L.edges);
     int* cursor = P.bin_hist + f.nb;
+    if (local) {
+        // this CTA's edges per band, then one run of slots per band taken from the cursors
+        for (int b = threadIdx.x; b < f.nb; b += BLOCK) sh_bins[b] = 0;
+        __syncthreads();
+        for (int e = blockIdx.x * BLOCK + threadIdx.x; e < f.count; e += gridDim.x * BLOCK) {
+            const int4 q1 = erec[2 * e + 1];
+            if (!q1.y) continue;
+            const int lo = max(q1.z - f.tmin, f.rb), hi = min(q1.w - f.tmin, f.H - 1);
+            for (int b = lo / f.R; lo <= hi && b <= hi / f.R; b++) atomicAdd(&sh_bins[b], 1);
+        }
+        __syncthreads();
+        for (int b = threadIdx.x; b < f.nb; b += BLOCK)
+            sh_bins[f.nb + b] = sh_bins[b] ? atomicAdd(&cursor[b], sh_bins[b]) : 0;
+        __syncthreads();
+        cursor = sh_bins + f.nb;
+    }
     for (int e = blockIdx.x * BLOCK + threadIdx.x; e < f.count; e += gridDim.x * BLOCK) {
         const int4 q1 = erec[2 * e + 1];  // step_pix, ed, start_row, end_row
         if (!q1.y) continue;
@@ -2771,13 +2806,18 @@ __global__ void __launch_bounds__(BLOCK) k_fig_bin_fill(KParams P) {
 }
 
 cudaError_t launch_figure_bins(const KParams& p, int grid, cudaStream_t s) {
-    k_fig_edges<<<grid, BLOCK, 0, s>>>(p);
-    cudaError_t e = cudaGetLastError();
+    const bool local = p.n_bands <= BIN_SMEM_BANDS;
+    const int sm_e = local ? p.n_bands * (int)sizeof(int) : 0, sm_f = 2 * sm_e;
+    cudaError_t e = cudaFuncSetAttribute(k_fig_bin_fill, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         2 * BIN_SMEM_BANDS * (int)sizeof(int));
+    if (e != cudaSuccess) return e;
+    k_fig_edges<<<grid, BLOCK, sm_e, s>>>(p);
+    e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_fig_bin_scan<<<1, BLOCK, 0, s>>>(p);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_fig_bin_fill<<<grid, BLOCK, 0, s>>>(p);
+    k_fig_bin_fill<<<grid, BLOCK, sm_f, s>>>(p);
     return cudaGetLastError();
 }
 
@@ -2807,7 +2847,7 @@ cudaError_t launch_figure_bins(const KParams& p, int grid, cudaStream_t s) {
 // last CTA of its kernel to finish):
 //   k_gb_ops    per 256 ops: the last Move/Line/Quad/Cubic/Close op and the last PenWidth op
 //   k_gb_count  every op's pen (the end point of the last such op before it) and raw
-//               vertex count (the count walk); scan of the counts
+//               vertex count (the count walk, GB_LANES lanes per op); scan of the counts
 //   k_gb_emit   every op's raw vertices at its offset (the emit walk); per tile of 1,024
 //               raw vertices its last sub-figure start, scanned
 //   k_gb_keep   keep, pop and R per raw vertex; tile aggregates, scanned
@@ -2921,34 +2961,81 @@ __device__ __forceinline__ void gb_pen(const ft_op* ops, int j, float& x, float&
     }
 }
 // Raw vertices of a Move/Line/Quad/Cubic op with the pen at (px, py), as build_fill
-// flattens them for a fill: emit(k, vertex) in order; returns their number.  flags:
-// 1 depth cap reached, 2 non-finite control point.
+// flattens them for a fill, split over GB_LANES lanes: lane s takes the subtree of the
+// curve's subdivision whose path from the root is the GB_D0 bits of s (left half 0, in
+// the depth-first order of the walk); a leaf above that depth goes to the first lane of
+// its range, a Move or Line to lane 0.  Each subtree is the walk's own arithmetic, so the
+// lanes' leaves in lane order are the walk's leaves.  emit(k, vertex) for the lane's k-th
+// leaf; returns the lane's leaf count.  flags: 1 depth cap reached, 2 non-finite control
+// point.
 template <class Emit>
-__device__ int gb_walk(const KParams& P, const ft_op& op, int kind, float px, float py, int& flags, Emit emit) {
+__device__ int gb_walk(const KParams& P, const ft_op& op, int kind, float px, float py, int lane, int& flags,
+                       Emit emit) {
     if (kind == FT_OP_MOVE || kind == FT_OP_LINE) {
+        if (lane) return 0;
         const P2 A = xform(P.xf, p2(op.v[0], op.v[1]));
         emit(0, make_int2(f2fx(A.x), f2fx(A.y)));
         return 1;
     }
-    const P2 A = xform(P.xf, p2(px, py)), B = xform(P.xf, p2(op.v[0], op.v[1])),
-             C = xform(P.xf, p2(op.v[2], op.v[3]));
+    P2 a = xform(P.xf, p2(px, py)), b = xform(P.xf, p2(op.v[0], op.v[1])), c = xform(P.xf, p2(op.v[2], op.v[3]));
     auto leaf = [&](int k, P2 q, float) { emit(k, make_int2(f2fx(q.x), f2fx(q.y))); };
+    const float tol_sq = P.tol_sq;
     int dh = 0, n;
     if (kind == FT_OP_QUAD) {
-        if (!pfinite(A) || !pfinite(B) || !pfinite(C)) {
+        if (!pfinite(a) || !pfinite(b) || !pfinite(c)) {
+            if (lane) return 0;
             flags |= 2;
-            emit(0, make_int2(f2fx(C.x), f2fx(C.y)));
+            emit(0, make_int2(f2fx(c.x), f2fx(c.y)));
             return 1;
         }
-        n = quad_walk<false>(A, B, C, 0.f, 0.f, 0.f, P.tol_sq, 0, INT_MAX, &dh, leaf);
+        for (int d = 0; d < GB_D0; d++) {
+            const P2 ab = pmid(a, b), bc = pmid(b, c), abbc = pmid(ab, bc), ac = pmid(a, c);
+            const bool within = pdist_sq(abbc, ac) <= tol_sq;
+            if (within || d >= FT_MAX_DEPTH) {
+                if (lane & ((1 << (GB_D0 - d)) - 1)) return 0;
+                if (!within) flags |= 1;
+                emit(0, make_int2(f2fx(c.x), f2fx(c.y)));
+                return 1;
+            }
+            if ((lane >> (GB_D0 - 1 - d)) & 1) {
+                a = abbc;
+                b = bc;
+            } else {
+                b = ab;
+                c = abbc;
+            }
+        }
+        n = quad_walk<false>(a, b, c, 0.f, 0.f, 0.f, tol_sq, 0, INT_MAX, &dh, leaf, GB_D0);
     } else {
-        const P2 D = xform(P.xf, p2(op.v[4], op.v[5]));
-        if (!pfinite(A) || !pfinite(B) || !pfinite(C) || !pfinite(D)) {
+        P2 e = xform(P.xf, p2(op.v[4], op.v[5]));
+        if (!pfinite(a) || !pfinite(b) || !pfinite(c) || !pfinite(e)) {
+            if (lane) return 0;
             flags |= 2;
-            emit(0, make_int2(f2fx(D.x), f2fx(D.y)));
+            emit(0, make_int2(f2fx(e.x), f2fx(e.y)));
             return 1;
         }
-        n = cubic_walk<false>(A, B, C, D, 0.f, 0.f, 0.f, 0.f, P.tol_sq, 0, INT_MAX, &dh, leaf);
+        for (int d = 0; d < GB_D0; d++) {
+            const P2 ab = pmid(a, b), bc = pmid(b, c), cd = pmid(c, e);
+            const P2 abbc = pmid(ab, bc), bccd = pmid(bc, cd);
+            const P2 pe = pmid(abbc, bccd), ad = pmid(a, e);
+            const bool within = pdist_sq(pe, ad) <= tol_sq;
+            if (within || d >= FT_MAX_DEPTH) {
+                if (lane & ((1 << (GB_D0 - d)) - 1)) return 0;
+                if (!within) flags |= 1;
+                emit(0, make_int2(f2fx(e.x), f2fx(e.y)));
+                return 1;
+            }
+            if ((lane >> (GB_D0 - 1 - d)) & 1) {
+                a = pe;
+                b = bccd;
+                c = cd;
+            } else {
+                b = ab;
+                c = abbc;
+                e = pe;
+            }
+        }
+        n = cubic_walk<false>(a, b, c, e, 0.f, 0.f, 0.f, 0.f, tol_sq, 0, INT_MAX, &dh, leaf, GB_D0);
     }
     if (dh) flags |= 1;
     return n;
@@ -2960,8 +3047,10 @@ __global__ void __launch_bounds__(BLOCK) k_gb_ops(KParams P) {
     const GridBuildBufs& G = P.gb;
     const int tid = threadIdx.x, i = blockIdx.x * BLOCK + tid;
     const int kind = i < G.n_ops ? __ldg(&G.ops[i].kind) : -1;
-    const int mpc = block_incl_max((kind >= FT_OP_CLOSE && kind <= FT_OP_CUBIC) ? i : -1, tmp);
+    int mpc, lpc;
+    block_max_scan((kind >= FT_OP_CLOSE && kind <= FT_OP_CUBIC) ? i : -1, tmp, mpc, lpc);
     const int mpw = block_incl_max(kind == FT_OP_PEN_WIDTH ? i : -1, tmp);
+    if (i < G.n_ops) G.opi[i].x = lpc;  // the block's part; k_gb_count adds the blocks before
     if (tid == BLOCK - 1) G.opa[blockIdx.x] = make_int2(mpc, mpw);
     if (!gb_last_block(&G.done[0])) return;
     // exclusive max over the blocks, in place
@@ -2985,46 +3074,70 @@ __global__ void __launch_bounds__(BLOCK) k_gb_ops(KParams P) {
     if (tid == 0 && P.sw_out) P.sw_out[0] = cpw >= 0 ? G.ops[cpw].v[0] : G.s_width;
 }
 
+// Op i of a CTA of k_gb_count / k_gb_emit (GB_OPB ops, GB_LANES lanes each) and its pen.
+struct GbOp {
+    int i, lane, kind, lpc, rs;
+    float px, py;
+    ft_op op;
+};
+__device__ __forceinline__ GbOp gb_op_of(const GridBuildBufs& G, int& flags) {
+    GbOp o;
+    o.i = blockIdx.x * GB_OPB + (int)(threadIdx.x / GB_LANES);
+    o.lane = (int)(threadIdx.x % GB_LANES);
+    o.kind = -1;
+    o.lpc = -1;
+    o.rs = 0;
+    o.px = o.py = 0.f;
+    if (o.i >= G.n_ops) return o;
+    o.op = gb_op(G.ops, o.i);
+    o.kind = o.op.kind;
+    if (o.kind < -1 || o.kind > FT_OP_PEN_WIDTH) {
+        if (o.lane == 0) flags |= 2;
+        o.kind = -1;
+    }
+    o.lpc = max(G.opi[o.i].x, G.opa[o.i / BLOCK].x);
+    int pk = -1;
+    if (o.kind >= FT_OP_MOVE && o.kind <= FT_OP_CUBIC) gb_pen(G.ops, o.lpc, o.px, o.py, pk);
+    // the first vertex of this op starts a sub-figure after a close event
+    o.rs = o.kind == FT_OP_MOVE || pk == FT_OP_CLOSE || pk == -1;
+    return o;
+}
+
 __global__ void __launch_bounds__(BLOCK) k_gb_count(KParams P) {
     __shared__ int tmp[2 * NWARP + 2];
     __shared__ long long ltmp[NWARP];
     const GridBuildBufs& G = P.gb;
-    const int tid = threadIdx.x, i = blockIdx.x * BLOCK + tid;
-    ft_op op;
-    int kind = -1;
-    if (i < G.n_ops) {
-        op = gb_op(G.ops, i);
-        kind = op.kind;
-    }
+    const int tid = threadIdx.x;
     int flags = 0;
-    if (kind < -1 || kind > FT_OP_PEN_WIDTH) {
-        flags = 2;
-        kind = -1;
-    }
-    int inc, lpc;
-    block_max_scan((kind >= FT_OP_CLOSE && kind <= FT_OP_CUBIC) ? i : -1, tmp, inc, lpc);
-    lpc = max(lpc, G.opa[blockIdx.x].x);
+    const GbOp o = gb_op_of(G, flags);
     int n = 0;
-    if (kind >= FT_OP_MOVE && kind <= FT_OP_CUBIC) {
-        float px, py;
-        int pk;
-        gb_pen(G.ops, lpc, px, py, pk);
-        n = gb_walk(P, op, kind, px, py, flags, [](int, int2) {});
-    }
+    if (o.kind >= FT_OP_MOVE && o.kind <= FT_OP_CUBIC)
+        n = gb_walk(P, o.op, o.kind, o.px, o.py, o.lane, flags, [](int, int2) {});
     if (flags) atomicMax(&P.status[0], (flags & 1) ? FT_ERR_DEPTH : FT_ERR_ARG);
+    // the lanes' offsets within the op, the ops' offsets within the CTA
+    int inc = n;
+#pragma unroll
+    for (int d = 1; d < GB_LANES; d <<= 1) {
+        const int t = __shfl_up_sync(FULL, inc, d, GB_LANES);
+        if (o.lane >= d) inc += t;
+    }
+    const int n_op = __shfl_sync(FULL, inc, GB_LANES - 1, GB_LANES);
     int tot;
-    const int loc = block_excl_sum(n, tmp, tot);
-    if (i < G.n_ops) G.opi[i] = make_int2(lpc, loc);
+    const int ex = block_excl_sum(o.lane == 0 ? n_op : 0, tmp, tot);
+    if (o.i < G.n_ops) {
+        G.opl[o.i * GB_LANES + o.lane] = inc - n;
+        if (o.lane == 0) G.opi[o.i].y = ex;
+    }
     if (tid == 0) G.opn[blockIdx.x] = tot;
     if (!gb_last_block(&G.done[1])) return;
-    // exclusive sum over the blocks, in place; the total is the path's raw vertex count
+    // exclusive sum over the CTAs, in place; the total is the path's raw vertex count
     const int nb = (int)gridDim.x;
     long long carry = 0;
     for (int b0 = 0; b0 < nb; b0 += BLOCK) {
         const int b = b0 + tid;
         long long t;
-        const long long ex = block_excl_sum_ll(b < nb ? __ldcg(&G.opn[b]) : 0ll, ltmp, t);
-        if (b < nb) G.opn[b] = carry + ex;
+        const long long e = block_excl_sum_ll(b < nb ? __ldcg(&G.opn[b]) : 0ll, ltmp, t);
+        if (b < nb) G.opn[b] = carry + e;
         carry += t;
     }
     if (tid == 0) *G.n_raw = carry;
@@ -3036,30 +3149,23 @@ __global__ void __launch_bounds__(BLOCK) k_gb_emit(KParams P) {
     const GridBuildBufs& G = P.gb;
     const long long n_raw = *G.n_raw;
     if (n_raw > G.raw_cap) return;  // every CTA: the caller grows the arrays
-    const int tid = threadIdx.x, i = blockIdx.x * BLOCK + tid;
-    if (i < G.n_ops) {
-        const ft_op op = gb_op(G.ops, i);
-        const int kind = op.kind;
-        if (kind >= FT_OP_MOVE && kind <= FT_OP_CUBIC) {
-            const int2 oi = G.opi[i];
-            const int off = (int)(G.opn[blockIdx.x] + oi.y);
-            float px, py;
-            int pk;
-            gb_pen(G.ops, oi.x, px, py, pk);
-            // the first vertex of this op starts a sub-figure after a close event
-            const int rs = kind == FT_OP_MOVE || pk == FT_OP_CLOSE || pk == -1;
-            int flags = 0;
-            int2* raw = G.raw;
-            unsigned char* fl = G.fl;
-            const int cap = G.raw_cap;
-            gb_walk(P, op, kind, px, py, flags, [&](int k, int2 q) {
-                if (ck(off + k < cap, 13) && off + k < cap) {
-                    raw[off + k] = q;
-                    fl[off + k] = k == 0 ? (unsigned char)rs : (unsigned char)0;
-                }
-            });
-            if (rs && ck(off < cap, 13) && off < cap) atomicMax(&G.tr[off / GB_TILE], off);
-        }
+    const int tid = threadIdx.x;
+    int flags = 0;
+    const GbOp o = gb_op_of(G, flags);
+    if (o.kind >= FT_OP_MOVE && o.kind <= FT_OP_CUBIC) {
+        const long long off0 = G.opn[blockIdx.x] + G.opi[o.i].y;
+        const int off = (int)(off0 + G.opl[o.i * GB_LANES + o.lane]);
+        int2* raw = G.raw;
+        unsigned char* fl = G.fl;
+        const int cap = G.raw_cap;
+        const unsigned char rs0 = (o.lane == 0 && o.rs) ? 1 : 0;
+        gb_walk(P, o.op, o.kind, o.px, o.py, o.lane, flags, [&](int k, int2 q) {
+            if (ck(off + k < cap, 13) && off + k < cap) {
+                raw[off + k] = q;
+                fl[off + k] = k == 0 ? rs0 : (unsigned char)0;
+            }
+        });
+        if (rs0 && ck(off < cap, 13) && off < cap) atomicMax(&G.tr[off / GB_TILE], off);
     }
     if (!gb_last_block(&G.done[2])) return;
     // exclusive max of the tiles' last sub-figure starts, in place
@@ -3256,24 +3362,44 @@ __global__ void __launch_bounds__(BLOCK) k_gb_top(KParams P) {
         G.top[blockIdx.x] = b;
     }
     if (!gb_last_block(&G.done[4])) return;
-    if (tid == 0) {
-        int4 b = make_int4(INT_MAX, INT_MAX, INT_MAX, 0);
-        for (int k = 0; k < (int)gridDim.x; k++) {
-            const int4 o = __ldcg(&G.top[k]);
-            if (top_less(o.x, o.y, o.z, b.x, b.y, b.z)) b = o;
+    by = bx = bi = INT_MAX;
+    for (int k = tid; k < (int)gridDim.x; k += BLOCK) {
+        const int4 o = __ldcg(&G.top[k]);
+        if (top_less(o.x, o.y, o.z, by, bx, bi)) {
+            by = o.x;
+            bx = o.y;
+            bi = o.z;
         }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const int oy = __shfl_down_sync(FULL, by, o), ox = __shfl_down_sync(FULL, bx, o),
+                  oi = __shfl_down_sync(FULL, bi, o);
+        if (top_less(oy, ox, oi, by, bx, bi)) {
+            by = oy;
+            bx = ox;
+            bi = oi;
+        }
+    }
+    __syncthreads();
+    if (lane == 0) wb[w] = make_int4(by, bx, bi, 0);
+    __syncthreads();
+    if (tid == 0) {
+        int4 b = wb[0];
+        for (int k = 1; k < NWARP; k++)
+            if (top_less(wb[k].x, wb[k].y, wb[k].z, b.x, b.y, b.z)) b = wb[k];
         P.fig_state[0] = count > 0 ? make_int4(count, fig_dir(b.z, count, pts, ss), b.x >> 16, 0)
                                    : make_int4(0, 0, 0, 0);
     }
 }
 
 cudaError_t launch_grid_build(const KParams& p, int sm_count, cudaStream_t s) {
-    const int nbo = (p.gb.n_ops + BLOCK - 1) / BLOCK;
+    const int nbo = (p.gb.n_ops + BLOCK - 1) / BLOCK, nbw = (p.gb.n_ops + GB_OPB - 1) / GB_OPB;
     if (nbo <= 0 || p.gb.raw_cap % GB_TILE || p.gb.raw_cap > GB_RAW_MAX) return cudaErrorInvalidValue;
     const int gt = std::max(1, 4 * sm_count);
     k_gb_ops<<<nbo, BLOCK, 0, s>>>(p);
-    k_gb_count<<<nbo, BLOCK, 0, s>>>(p);
-    k_gb_emit<<<nbo, BLOCK, 0, s>>>(p);
+    k_gb_count<<<nbw, BLOCK, 0, s>>>(p);
+    k_gb_emit<<<nbw, BLOCK, 0, s>>>(p);
     k_gb_keep<<<gt, BLOCK, 0, s>>>(p);
     k_gb_write<<<gt, BLOCK, 0, s>>>(p);
     k_gb_top<<<GB_TOP_BLOCKS, BLOCK, 0, s>>>(p);

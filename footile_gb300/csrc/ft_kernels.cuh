@@ -105,6 +105,9 @@ static_assert(NWARP * WS_BYTES <= SCRATCH_BYTES_PER_CTA, "warp scratch layout");
 constexpr int GB_PER = 4;                      // raw vertices per thread of the tile kernels
 constexpr int GB_TILE = GB_PER * BLOCK;        // raw vertices per tile
 constexpr int GB_TOP_BLOCKS = 512;             // CTAs of the top-vertex search
+constexpr int GB_D0 = 3;                       // an op's curve walk is split at this depth
+constexpr int GB_LANES = 1 << GB_D0;           // threads per op of the count and emit walks
+constexpr int GB_OPB = BLOCK / GB_LANES;       // ops per CTA of the count and emit walks
 constexpr long long GB_RAW_MAX = 1ll << 29;    // raw vertices the grid build takes at most
 struct GridBuildBufs {
     const ft_op* ops;   // the path's ops
@@ -114,9 +117,10 @@ struct GridBuildBufs {
     unsigned* done;     // [8] tickets: the last CTA of a kernel to finish runs its scan
     long long* n_raw;   // raw vertices of the path
     int* count;         // vertices kept
-    int2* opa;          // per block of 256 ops: last Move/Line/Quad/Cubic/Close op, last PenWidth op
-    long long* opn;     // per block of 256 ops: raw vertices
-    int2* opi;          // per op: last Move/Line/Quad/Cubic/Close op before it, raw offset in its block
+    int2* opa;          // per 256 ops: last Move/Line/Quad/Cubic/Close op, last PenWidth op
+    long long* opn;     // per GB_OPB ops: raw vertices
+    int2* opi;          // per op: last Move/Line/Quad/Cubic/Close op before it in its 256, raw offset in its GB_OPB
+    int* opl;           // per op and lane: the lane's raw offset in the op
     int2* raw;          // raw vertices, 16.16
     unsigned char* fl;  // per raw vertex: 1 = starts a sub-figure
     unsigned char* kp;  // per raw vertex: 1 = kept, 2 = pops its sub-figure's first vertex
@@ -126,16 +130,18 @@ struct GridBuildBufs {
     int4* top;          // per CTA of the top-vertex search: min (y, x, id)
 };
 struct GbLayout {
-    size_t state, opa, opn, opi, raw, fl, kp, rk, tr, tp, top, bytes;
+    size_t state, opa, opn, opi, opl, raw, fl, kp, rk, tr, tp, top, bytes;
 };
 constexpr GbLayout gb_layout(size_t n_ops, size_t raw_cap) {
     GbLayout g{};
-    const size_t nbo = (n_ops + BLOCK - 1) / BLOCK, ntiles = raw_cap / GB_TILE;
+    const size_t nbo = (n_ops + BLOCK - 1) / BLOCK, nbw = (n_ops + GB_OPB - 1) / GB_OPB,
+                 ntiles = raw_cap / GB_TILE;
     g.state = 0;  // done[8] at 0, n_raw at 32, count at 40
     g.opa = 256;
     g.opn = align256(g.opa + nbo * 8);
-    g.opi = align256(g.opn + nbo * 8);
-    g.raw = align256(g.opi + n_ops * 8);
+    g.opi = align256(g.opn + nbw * 8);
+    g.opl = align256(g.opi + n_ops * 8);
+    g.raw = align256(g.opl + n_ops * GB_LANES * 4);
     g.fl = align256(g.raw + raw_cap * 8);
     g.kp = align256(g.fl + raw_cap);
     g.rk = align256(g.kp + raw_cap);
