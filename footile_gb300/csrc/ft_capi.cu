@@ -1127,13 +1127,14 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
             p.bin_hist = reinterpret_cast<int*>(static_cast<char*>(c->figbins.p) + 16);
         }
         const size_t raw_cap = c->gb_raw_cap;
+        bool use_probe = false;
+        ftk::KParams pp;  // the probe's parameters
         if (grid_build) {
             const ftk::GbLayout G = ftk::gb_layout(paths[0].n_ops, raw_cap);
             FT_CU(c->gbuf.ensure(G.bytes), "alloc grid build");
             unsigned char* gb = static_cast<unsigned char*>(c->gbuf.p);
             FT_CU(cudaMemsetAsync(gb, 0, 256, c->stream), "reset grid build");
-            FT_CU(cudaMemsetAsync(gb + G.tr, 0xFF, raw_cap / ftk::GB_TILE * sizeof(int), c->stream),
-                  "reset grid build");
+            FT_CU(cudaMemsetAsync(gb + G.tr, 0xFF, G.tp - G.tr, c->stream), "reset grid build");  // tr, tr2
             ftk::GridBuildBufs& g = p.gb;
             g.ops = ops_d + paths[0].op_begin;
             g.n_ops = (int)paths[0].n_ops;
@@ -1153,14 +1154,32 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
             g.tr = reinterpret_cast<int*>(gb + G.tr);
             g.tp = reinterpret_cast<int4*>(gb + G.tp);
             g.top = reinterpret_cast<int4*>(gb + G.top);
+            g.final_flag = nullptr;
+            g.skip = nullptr;
+            // a probe over the first ops: a capped figure usually reaches its cap there, and
+            // the build over all ops is then skipped
+            const int probe_ops = std::max(4096, p.pt_cap / 8);
+            use_probe = (int)paths[0].n_ops > 2 * probe_ops;
+            if (use_probe) {
+                pp = p;
+                ftk::GridBuildBufs& q = pp.gb;
+                q.n_ops = probe_ops;
+                q.done = reinterpret_cast<unsigned*>(gb + 128);
+                q.n_raw = reinterpret_cast<long long*>(gb + 160);
+                q.count = reinterpret_cast<int*>(gb + 168);
+                q.final_flag = reinterpret_cast<int*>(gb + 172);
+                q.tr = reinterpret_cast<int*>(gb + G.tr2);
+                g.skip = q.final_flag;
+            }
         }
         c->comp_timed = false;
         FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
         if (n_paths) {
             Stage st_build("figure build and edge binning");
             if (grid_build) {
-                FT_CU(ftk::launch_grid_build(p, c->sm_count, c->stream), "launch grid figure build");
-                c->launches += 6;
+                FT_CU(ftk::launch_grid_build(p, c->sm_count, c->stream, use_probe ? &pp : nullptr),
+                      "launch grid figure build");
+                c->launches += use_probe ? 11 : 6;
             } else {
                 FT_CU(ftk::launch_composite_build(p, grid, smem_a, c->stream, grid <= c->sm_count),
                       "launch composite build");
@@ -1176,10 +1195,14 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
         FT_CU(cudaMemcpyAsync(&used, c->pool_used.p, sizeof(used), cudaMemcpyDeviceToHost, c->stream), "pool size");
         if (n_paths == 1)
             FT_CU(cudaMemcpyAsync(&cr0, c->crec.p, sizeof(int4), cudaMemcpyDeviceToHost, c->stream), "path record");
-        long long n_raw = 0;
+        long long n_raw = 0, n_raw_probe = 0;
         if (grid_build)
             FT_CU(cudaMemcpyAsync(&n_raw, p.gb.n_raw, sizeof(n_raw), cudaMemcpyDeviceToHost, c->stream), "raw count");
+        if (use_probe)
+            FT_CU(cudaMemcpyAsync(&n_raw_probe, pp.gb.n_raw, sizeof(n_raw_probe), cudaMemcpyDeviceToHost, c->stream),
+                  "raw count");
         FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
+        n_raw = std::max(n_raw, n_raw_probe);  // the full build is skipped after a complete probe
         if (grid_build && n_raw > (long long)raw_cap) {
             // more raw vertices than the arrays hold: grow them, or build on one CTA
             if (n_raw > ftk::GB_RAW_MAX) {

@@ -3107,6 +3107,7 @@ __global__ void __launch_bounds__(BLOCK) k_gb_count(KParams P) {
     __shared__ int tmp[2 * NWARP + 2];
     __shared__ long long ltmp[NWARP];
     const GridBuildBufs& G = P.gb;
+    if (G.skip && *G.skip) return;  // a probe over a prefix of the ops completed the figure
     const int tid = threadIdx.x;
     int flags = 0;
     const GbOp o = gb_op_of(G, flags);
@@ -3147,6 +3148,7 @@ __global__ void __launch_bounds__(BLOCK) k_gb_emit(KParams P) {
     __shared__ int tmp[2 * NWARP + 2];
     __shared__ int s_c;
     const GridBuildBufs& G = P.gb;
+    if (G.skip && *G.skip) return;  // a probe over a prefix of the ops completed the figure
     const long long n_raw = *G.n_raw;
     if (n_raw > G.raw_cap) return;  // every CTA: the caller grows the arrays
     const int tid = threadIdx.x;
@@ -3187,6 +3189,7 @@ __global__ void __launch_bounds__(BLOCK) k_gb_keep(KParams P) {
     __shared__ int tmp[2 * NWARP + 2];
     __shared__ PAgg wt[NWARP];
     const GridBuildBufs& G = P.gb;
+    if (G.skip && *G.skip) return;  // a probe over a prefix of the ops completed the figure
     const long long n_raw = *G.n_raw;
     if (n_raw > G.raw_cap) return;
     const int M = (int)n_raw, nt = (M + GB_TILE - 1) / GB_TILE, tid = threadIdx.x;
@@ -3261,6 +3264,7 @@ __global__ void __launch_bounds__(BLOCK) k_gb_write(KParams P) {
     __shared__ PAgg wt[NWARP];
     __shared__ int s_l;
     const GridBuildBufs& G = P.gb;
+    if (G.skip && *G.skip) return;  // a probe over a prefix of the ops completed the figure
     const long long n_raw = *G.n_raw;
     if (n_raw > G.raw_cap) return;
     const int M = (int)n_raw, nt = (M + GB_TILE - 1) / GB_TILE, tid = threadIdx.x, cap = P.pt_cap;
@@ -3322,6 +3326,7 @@ __global__ void __launch_bounds__(BLOCK) k_gb_write(KParams P) {
             // the close after the cap pops the last vertex if it equals its sub-figure's first
             const int2 v = G.raw[l - 1], f = G.raw[G.rk[l - 1]];
             *G.count = cap - ((!(G.fl[l] & 1) && v.x == f.x && v.y == f.y) ? 1 : 0);
+            if (G.final_flag) *G.final_flag = 1;
         }
         __syncthreads();
     }
@@ -3330,6 +3335,7 @@ __global__ void __launch_bounds__(BLOCK) k_gb_write(KParams P) {
 __global__ void __launch_bounds__(BLOCK) k_gb_top(KParams P) {
     __shared__ int4 wb[NWARP];
     const GridBuildBufs& G = P.gb;
+    if (G.skip && *G.skip) return;  // a probe over a prefix of the ops completed the figure
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int count = *G.n_raw > G.raw_cap ? 0 : *G.count;
     const int2* pts = reinterpret_cast<const int2*>(P.scratch + P.L.pts);
@@ -3393,16 +3399,21 @@ __global__ void __launch_bounds__(BLOCK) k_gb_top(KParams P) {
     }
 }
 
-cudaError_t launch_grid_build(const KParams& p, int sm_count, cudaStream_t s) {
-    const int nbo = (p.gb.n_ops + BLOCK - 1) / BLOCK, nbw = (p.gb.n_ops + GB_OPB - 1) / GB_OPB;
+cudaError_t launch_grid_build(const KParams& p, int sm_count, cudaStream_t s, const KParams* probe) {
+    const int nbo = (p.gb.n_ops + BLOCK - 1) / BLOCK;
     if (nbo <= 0 || p.gb.raw_cap % GB_TILE || p.gb.raw_cap > GB_RAW_MAX) return cudaErrorInvalidValue;
+    if (probe && (probe->gb.n_ops <= 0 || probe->gb.n_ops > p.gb.n_ops)) return cudaErrorInvalidValue;
     const int gt = std::max(1, 4 * sm_count);
-    k_gb_ops<<<nbo, BLOCK, 0, s>>>(p);
-    k_gb_count<<<nbw, BLOCK, 0, s>>>(p);
-    k_gb_emit<<<nbw, BLOCK, 0, s>>>(p);
-    k_gb_keep<<<gt, BLOCK, 0, s>>>(p);
-    k_gb_write<<<gt, BLOCK, 0, s>>>(p);
-    k_gb_top<<<GB_TOP_BLOCKS, BLOCK, 0, s>>>(p);
+    k_gb_ops<<<nbo, BLOCK, 0, s>>>(p);  // pens of every op (the probe's too) and the pen width after
+    for (const KParams* q : {probe, &p}) {
+        if (!q) continue;
+        const int nbw = (q->gb.n_ops + GB_OPB - 1) / GB_OPB;
+        k_gb_count<<<nbw, BLOCK, 0, s>>>(*q);
+        k_gb_emit<<<nbw, BLOCK, 0, s>>>(*q);
+        k_gb_keep<<<gt, BLOCK, 0, s>>>(*q);
+        k_gb_write<<<gt, BLOCK, 0, s>>>(*q);
+        k_gb_top<<<GB_TOP_BLOCKS, BLOCK, 0, s>>>(*q);
+    }
     return cudaGetLastError();
 }
 

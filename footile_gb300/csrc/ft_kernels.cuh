@@ -128,15 +128,17 @@ struct GridBuildBufs {
     int* tr;            // per tile: last sub-figure start
     int4* tp;           // per tile: position aggregate (kept - popped, runs, max prefix)
     int4* top;          // per CTA of the top-vertex search: min (y, x, id)
+    int* final_flag;    // nullable: set when the cap is reached (the figure is complete)
+    const int* skip;    // nullable: the kernels after k_gb_ops do nothing when *skip is set
 };
 struct GbLayout {
-    size_t state, opa, opn, opi, opl, raw, fl, kp, rk, tr, tp, top, bytes;
+    size_t state, opa, opn, opi, opl, raw, fl, kp, rk, tr, tr2, tp, top, bytes;
 };
 constexpr GbLayout gb_layout(size_t n_ops, size_t raw_cap) {
     GbLayout g{};
     const size_t nbo = (n_ops + BLOCK - 1) / BLOCK, nbw = (n_ops + GB_OPB - 1) / GB_OPB,
                  ntiles = raw_cap / GB_TILE;
-    g.state = 0;  // done[8] at 0, n_raw at 32, count at 40
+    g.state = 0;  // two builds' done[8] at 0 / 128, n_raw at 32 / 160, count at 40 / 168, final at 44 / 172
     g.opa = 256;
     g.opn = align256(g.opa + nbo * 8);
     g.opi = align256(g.opn + nbw * 8);
@@ -146,7 +148,8 @@ constexpr GbLayout gb_layout(size_t n_ops, size_t raw_cap) {
     g.kp = align256(g.fl + raw_cap);
     g.rk = align256(g.kp + raw_cap);
     g.tr = align256(g.rk + raw_cap * 4);
-    g.tp = align256(g.tr + ntiles * 4);
+    g.tr2 = align256(g.tr + ntiles * 4);
+    g.tp = align256(g.tr2 + ntiles * 4);
     g.top = align256(g.tp + ntiles * 16);
     g.bytes = align256(g.top + (size_t)GB_TOP_BLOCKS * 16);
     return g;
@@ -224,8 +227,11 @@ cudaError_t launch_figure_bins(const KParams& p, int grid, cudaStream_t s);
 // width after the path and the path's status.  p.gb's state (done, n_raw, count) must be
 // zero and tr all -1 (bytes 0xFF) before the launch.  When the path has more raw
 // vertices than p.gb.raw_cap, *n_raw says how many and nothing else is written but a
-// figure of no vertices; the caller grows the arrays and builds again.
-cudaError_t launch_grid_build(const KParams& p, int sm_count, cudaStream_t s);
+// figure of no vertices; the caller grows the arrays and builds again.  `probe`
+// (nullable): the same build over a prefix of the ops first (its own state and tr, its
+// final_flag the full build's skip): when the cap is reached within the prefix the figure
+// is complete and the full build does nothing.
+cudaError_t launch_grid_build(const KParams& p, int sm_count, cudaStream_t s, const KParams* probe = nullptr);
 int composite_bands_smem(int band_rows, int width);
 int composite_build_blocks_per_sm(int smem_bytes, bool stroke);
 

@@ -130,3 +130,24 @@ def test_raw_arrays_grow(ctx):
     ops = ops_array(ops)
     got, want, *_ = gpu_vs_oracle(ctx, ops, 1000, 900, tolerance=0.05)
     assert_same(got, want, "long cubics")
+
+
+@pytest.mark.parametrize("lead", [14, 17, 19, 20, 21, 22, 24])
+def test_cap_near_the_probe_boundary(ctx, lead):
+    """Long paths are built first over their first 8,192 ops; when the cap is reached
+    there, the build over all ops is skipped.  After `lead` lines come 20 quads of 16
+    leaves and quads of 8 leaves, every vertex distinct: the first 8,192 ops hold
+    65,682 - 7 * lead raw vertices, so the 65,535th vertex falls inside them for
+    lead <= 20, on their last vertex for lead 21, and after them beyond."""
+    ctx.tune(split_px=1, fig_build=2)
+    ops = [PathOp.Move(0.0, 30.0)]
+    ops += [PathOp.Line(0.125 + 0.0625 * k, 30.0 - 0.125 * k) for k in range(lead)]
+    x, y = 0.125 + 0.0625 * lead, 30.0
+    ops.append(PathOp.Line(x, y))
+    for k in range(20000):
+        h = 80.0 if k < 20 else 20.0
+        ops.append(PathOp.Quad(x + 0.125, y + h, x + 0.25, y))
+        x += 0.25
+    ops = ops_array(ops)
+    got, want, *_ = gpu_vs_oracle(ctx, ops, 5010, 72, rule=_abi.EVENODD)
+    assert_same(got, want, f"lead {lead}")

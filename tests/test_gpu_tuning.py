@@ -54,7 +54,8 @@ def test_autotune_and_cache(ctx, tmp_path):
     t, ms = ctx.autotune(ops_d, paths, _abi.MATTE8, ras_d, cache_path=cache)
     assert ms > 0 and ctx.tuning() == t
     line = open(cache).read().split()
-    assert len(line) == 12 and [int(v) for v in line[1:11]] == list(t.values())
+    # the cache keeps the batch plan's ten knobs (not the single-path fig_build)
+    assert len(line) == 12 and [int(v) for v in line[1:11]] == list(t.values())[:10] and t["fig_build"] == 0
     # the tuned plan draws the same bytes
     b = PreparedBatch(ctx, paths, _abi.MATTE8)
     ras_d.zero_()
