@@ -1046,7 +1046,11 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
     } else if ((reinterpret_cast<uintptr_t>(ops) & 15) || (fmt == FT_RGBA8P && (reinterpret_cast<uintptr_t>(raster) & 3))) {
         return fail(c, FT_ERR_ARG, "device ops need 16-byte alignment, Rgba8p rasters 4-byte alignment");
     }
-    const int R = composite_band_rows(c, w, fmt);
+    // a single Rgba8p call is composited from its Matte8 coverage (the mask route below):
+    // its bands are the Matte8 compositor's
+    const bool mask_route = fmt == FT_RGBA8P && n_paths == 1 && !(c->tuned && c->tune.tile_stage > 0) &&
+                            ftk::composite_bands_smem(composite_band_rows(c, w, FT_MATTE8), (int)w) <= c->max_smem;
+    const int R = composite_band_rows(c, w, mask_route ? FT_MATTE8 : fmt);
     const int n_bands = (int)((h + R - 1) / R);
     const int tile_w = composite_tile_w(c, w);
     const int stage = (c->tuned && c->tune.tile_stage > 0) ? c->tune.tile_stage : 1;
@@ -1225,7 +1229,7 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
             const uint32_t mstride = (w + 15) & ~15u;
             const int smem_m = ftk::composite_bands_smem(R, (int)w);
             bool streamed = false;
-            if (fmt == FT_RGBA8P && n_paths == 1 && !(c->tuned && c->tune.tile_stage > 0) && smem_m <= c->max_smem) {
+            if (mask_route && smem_m <= c->max_smem) {
                 FT_CU(c->mask.ensure((size_t)mstride * h), "alloc mask");
                 CUtensorMap tc, tmk;
                 if (canvas_tensor_map(&tc, ras_d, w, h, stride, ftk::SO_COLS, ftk::SO_ROWS) &&
