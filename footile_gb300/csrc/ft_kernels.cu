@@ -2111,16 +2111,31 @@ __device__ __forceinline__ void matte_row(int* row, unsigned* spans, int W, int 
     __syncwarp();
 }
 
+// (edge, row) items of one band spread over a whole compositor CTA (a single call): the
+// band's edges 256 at a time, each edge's rows in the band counted, a block scan and a
+// run-length item map (as raster_rows).
+struct BandStage {
+    EdgeRec edges[BLOCK];
+    int ya[BLOCK];
+    int off[BLOCK];
+    int scan[2 * NWARP + 2];
+    unsigned char map[MAP_CAP];
+};
+constexpr int BAND_STAGE_BYTES = (int)((sizeof(BandStage) + 255) & ~(size_t)255);
+
 // Matte8 ordered composite: every call overwrites its rows from its top row down
 // (fig.rs:629-636), so a raster row shows only the last call that reaches it.  One CTA per
-// band of P.band_rows rows, one warp per row: the warp finds that call and draws it.
+// band of P.band_rows rows, one warp per row: the warp finds that call and draws it.  A
+// single call on bands of 8 rows spreads the band's (edge, row) items over the whole CTA
+// (each edge read once, not once per row-warp).
 __global__ void __launch_bounds__(BLOCK) k_cbands(KParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int W = (int)P.canvas_w, H = (int)P.canvas_h, Wp = (W + 3) & ~3;
     const int R = P.band_rows, nb = P.n_bands, b = blockIdx.x;
     const int r = b * R + warp;  // this warp's raster row
-    if (warp >= R || r >= H) return;
+    const bool whole = P.n_items == 1 && R == NWARP && blockDim.x == BLOCK;
+    if (!whole && (warp >= R || r >= H)) return;
     unsigned char* mine = smem + (size_t)warp * row_smem_bytes(W);
     int* row = reinterpret_cast<int*>(mine);
     unsigned* spans = reinterpret_cast<unsigned*>(row + Wp);
@@ -2129,6 +2144,52 @@ __global__ void __launch_bounds__(BLOCK) k_cbands(KParams P) {
     for (int k = lane; k < n_words; k += 32) spans[k] = 0;
     __syncwarp();
     uint8_t* drow = P.rasters + (size_t)r * P.canvas_stride;
+    if (whole) {
+        BandStage& Bs = *reinterpret_cast<BandStage*>(smem + (size_t)R * row_smem_bytes(W));
+        const int4 cr = P.crec[0];
+        const int rlo = max(b * R, cr.x), rhi = min(b * R + R, H);  // rows the call draws here
+        if (rlo >= rhi) return;
+        const int o0 = P.bandoff[b], o1 = P.bandoff[b + 1];
+        const EdgeRec* edges =
+            P.pool + ((unsigned long long)(unsigned)cr.z | ((unsigned long long)(unsigned)cr.w << 32)) + o0;
+        const int ne = o1 - o0, yb0 = rlo + cr.y, yb1 = rhi + cr.y;  // scan rows yb0 .. yb1 - 1
+        __syncthreads();  // every row buffer cleared
+        for (int e0 = 0; e0 < ne; e0 += BLOCK) {
+            const int e = e0 + threadIdx.x;
+            int nrow = 0, ya = 0;
+            EdgeRec E;
+            E.ed = 0;
+            if (e < ne) {
+                E = edges[e];
+                if (E.ed) {
+                    ya = max(E.start_row, yb0);
+                    nrow = max(min(E.end_row, yb1 - 1) - ya + 1, 0);
+                }
+            }
+            Bs.edges[threadIdx.x] = E;
+            Bs.ya[threadIdx.x] = ya;
+            int tot;
+            const int o = block_excl_sum(nrow, Bs.scan, tot);
+            Bs.off[threadIdx.x] = o;
+            for (int m0 = 0; m0 < tot; m0 += MAP_CAP) {
+                const int ia = max(o, m0), ib = min(o + nrow, m0 + MAP_CAP);
+                for (int k = ia; k < ib; k++) Bs.map[k - m0] = (unsigned char)threadIdx.x;
+                __syncthreads();
+                const int nm = min(MAP_CAP, tot - m0);
+                for (int it = threadIdx.x; it < nm; it += BLOCK) {
+                    const int jj = Bs.map[it];
+                    const int y = Bs.ya[jj] + (m0 + it - Bs.off[jj]);
+                    const int ri = y - cr.y - b * R;  // band row of scan row y
+                    if (ck(ri >= 0 && ri < R, 15))
+                        scan_item(Bs.edges[jj], y,
+                                  reinterpret_cast<int*>(smem + (size_t)ri * row_smem_bytes(W)), W);
+                }
+                __syncthreads();
+            }
+        }
+        if (r >= rlo && r < rhi) matte_row(row, spans, W, Wp, drow, P.rule);
+        return;
+    }
     const int n = (int)P.n_items;
     int found = -1;
     for (int c1 = n; c1 > 0 && found < 0; c1 -= 32) {
@@ -2141,7 +2202,7 @@ __global__ void __launch_bounds__(BLOCK) k_cbands(KParams P) {
     const int4 cr = P.crec[found];
     const int o0 = P.bandoff[(size_t)b * n + found], o1 = P.bandoff[(size_t)(b + 1) * n + found];
     const unsigned long long first = ((unsigned long long)(unsigned)cr.z | ((unsigned long long)(unsigned)cr.w << 32)) + o0;
-    row_items(P.pool + first, o1 - o0, r + cr.y, row, W, spans);
+    row_items(P.pool + first, o1 - o0, r + cr.y, row, W, nullptr);
     __syncwarp();
     matte_row(row, spans, W, Wp, drow, P.rule);
 }
@@ -2689,7 +2750,7 @@ cudaError_t launch_composite_tiles(const KParams& p, const CUtensorMap& tmap, cu
     return cudaGetLastError();
 }
 
-int composite_bands_smem(int band_rows, int width) { return band_rows * row_smem_bytes(width); }
+int composite_bands_smem(int band_rows, int width) { return band_rows * row_smem_bytes(width) + BAND_STAGE_BYTES; }
 
 // ---- edges and band bins of one path's figure over the whole GPU (split_bin); the
 //      figure was built by CTA 0 of k_cbuild.  Band rows follow bin_edges.
