@@ -79,6 +79,7 @@ struct ft_ctx {
     DevBuf mask;                            // a single large Rgba8p call's Matte8 coverage
     DevBuf gbuf;                            // one fill path's grid-wide figure build
     size_t gb_raw_cap = 0;                  // its raw vertex capacity (grows on demand)
+    size_t gs_sraw_cap = 0;                 // a stroke path's raw stroke point capacity (grows on demand)
     DevBuf srgb_lut, conv_src, conv_dst;    // ft_convert
     PlanSlot plan;                                   // the last batch's plan
     std::vector<std::unique_ptr<PlanSlot>> chunk_plans;  // host batches in pipelined chunks
@@ -1079,13 +1080,16 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
     // one fill path: its figure is built over the whole GPU (the grid build, whose raw
     // vertex arrays grow until the path's raw vertices fit) or by one CTA of k_cbuild
     const int fig_build = c->tuned ? c->tune.fig_build : 0;
-    bool grid_build = !stroke && n_paths == 1 && paths[0].n_ops > 0 &&
+    bool grid_build = n_paths == 1 && paths[0].n_ops > 0 &&
                       (fig_build == 2 || (fig_build == 0 && paths[0].n_ops >= FT_GRID_BUILD_OPS));
-    if (grid_build && c->gb_raw_cap == 0) {
+    auto first_cap = [&](size_t& cap) {
+        if (cap) return;
         const uint64_t est = std::max<uint64_t>((uint64_t)paths[0].n_ops * 64, 1u << 20);
-        c->gb_raw_cap = (size_t)std::min<uint64_t>((est + ftk::GB_TILE - 1) / ftk::GB_TILE * ftk::GB_TILE,
-                                                   (uint64_t)ftk::GB_RAW_MAX);
-    }
+        cap = (size_t)std::min<uint64_t>((est + ftk::GB_TILE - 1) / ftk::GB_TILE * ftk::GB_TILE,
+                                         (uint64_t)ftk::GB_RAW_MAX);
+    };
+    if (grid_build) first_cap(c->gb_raw_cap);
+    if (grid_build && stroke) first_cap(c->gs_sraw_cap);
     // edge pool: grows until every path's binned edges fit
     // first pool size in edges (it grows on demand)
     const bool penv = c->tuned && c->tune.pool_edges > 0;
@@ -1130,11 +1134,11 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
             p.fig_state = static_cast<int4*>(c->figbins.p);
             p.bin_hist = reinterpret_cast<int*>(static_cast<char*>(c->figbins.p) + 16);
         }
-        const size_t raw_cap = c->gb_raw_cap;
+        const size_t raw_cap = c->gb_raw_cap, sraw_cap = stroke ? c->gs_sraw_cap : 0;
         bool use_probe = false;
         ftk::KParams pp;  // the probe's parameters
         if (grid_build) {
-            const ftk::GbLayout G = ftk::gb_layout(paths[0].n_ops, raw_cap);
+            const ftk::GbLayout G = ftk::gb_layout(paths[0].n_ops, raw_cap, sraw_cap);
             FT_CU(c->gbuf.ensure(G.bytes), "alloc grid build");
             unsigned char* gb = static_cast<unsigned char*>(c->gbuf.p);
             FT_CU(cudaMemsetAsync(gb, 0, 256, c->stream), "reset grid build");
@@ -1147,7 +1151,8 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
             g.done = reinterpret_cast<unsigned*>(gb);
             g.n_raw = reinterpret_cast<long long*>(gb + 32);
             g.count = reinterpret_cast<int*>(gb + 40);
-            g.opa = reinterpret_cast<int2*>(gb + G.opa);
+            g.opa = reinterpret_cast<int4*>(gb + G.opa);
+            g.opw = reinterpret_cast<int*>(gb + G.opw);
             g.opn = reinterpret_cast<long long*>(gb + G.opn);
             g.opi = reinterpret_cast<int2*>(gb + G.opi);
             g.opl = reinterpret_cast<int*>(gb + G.opl);
@@ -1160,10 +1165,24 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
             g.top = reinterpret_cast<int4*>(gb + G.top);
             g.final_flag = nullptr;
             g.skip = nullptr;
+            if (stroke) {
+                ftk::GridStrokeBufs& q = p.gs;
+                q.sraw_cap = (int)sraw_cap;
+                q.st = reinterpret_cast<int*>(gb + 128);
+                q.n_sraw = reinterpret_cast<long long*>(gb + 160);
+                q.done = reinterpret_cast<unsigned*>(gb + 192);
+                q.raw4 = reinterpret_cast<float4*>(gb + G.raw4);
+                q.sfl = gb + G.sfl;
+                q.sopi = reinterpret_cast<int*>(gb + G.sopi);
+                q.stile = reinterpret_cast<int2*>(gb + G.stile);
+                q.subt = reinterpret_cast<int*>(gb + G.subt);
+                q.itoff = reinterpret_cast<int*>(gb + G.itoff);
+                q.itc = reinterpret_cast<int*>(gb + G.itc);
+            }
             // a probe over the first ops: a capped figure usually reaches its cap there, and
             // the build over all ops is then skipped
             const int probe_ops = std::max(4096, p.pt_cap / 8);
-            use_probe = (int)paths[0].n_ops > 2 * probe_ops;
+            use_probe = !stroke && (int)paths[0].n_ops > 2 * probe_ops;
             if (use_probe) {
                 pp = p;
                 ftk::GridBuildBufs& q = pp.gb;
@@ -1180,7 +1199,10 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
         FT_CU(cudaEventRecord(c->ev0, c->stream), "event");
         if (n_paths) {
             Stage st_build("figure build and edge binning");
-            if (grid_build) {
+            if (grid_build && stroke) {
+                FT_CU(ftk::launch_grid_stroke(p, c->sm_count, c->stream), "launch grid stroke build");
+                c->launches += 11;
+            } else if (grid_build) {
                 FT_CU(ftk::launch_grid_build(p, c->sm_count, c->stream, use_probe ? &pp : nullptr),
                       "launch grid figure build");
                 c->launches += use_probe ? 11 : 6;
@@ -1199,14 +1221,28 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
         FT_CU(cudaMemcpyAsync(&used, c->pool_used.p, sizeof(used), cudaMemcpyDeviceToHost, c->stream), "pool size");
         if (n_paths == 1)
             FT_CU(cudaMemcpyAsync(&cr0, c->crec.p, sizeof(int4), cudaMemcpyDeviceToHost, c->stream), "path record");
-        long long n_raw = 0, n_raw_probe = 0;
+        long long n_raw = 0, n_raw_probe = 0, n_sraw = 0;
         if (grid_build)
             FT_CU(cudaMemcpyAsync(&n_raw, p.gb.n_raw, sizeof(n_raw), cudaMemcpyDeviceToHost, c->stream), "raw count");
+        if (grid_build && stroke)
+            FT_CU(cudaMemcpyAsync(&n_sraw, p.gs.n_sraw, sizeof(n_sraw), cudaMemcpyDeviceToHost, c->stream),
+                  "stroke point count");
         if (use_probe)
             FT_CU(cudaMemcpyAsync(&n_raw_probe, pp.gb.n_raw, sizeof(n_raw_probe), cudaMemcpyDeviceToHost, c->stream),
                   "raw count");
         FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
         n_raw = std::max(n_raw, n_raw_probe);  // the full build is skipped after a complete probe
+        if (grid_build && stroke && n_sraw > (long long)sraw_cap) {
+            // more raw stroke points than the arrays hold: grow them, or build on one CTA
+            if (n_sraw > ftk::GB_RAW_MAX) {
+                grid_build = false;
+            } else {
+                const long long want_raw = std::min<long long>(n_sraw + n_sraw / 8, ftk::GB_RAW_MAX);
+                c->gs_sraw_cap = (size_t)((want_raw + ftk::GB_TILE - 1) / ftk::GB_TILE * ftk::GB_TILE);
+            }
+            attempt--;
+            continue;
+        }
         if (grid_build && n_raw > (long long)raw_cap) {
             // more raw vertices than the arrays hold: grow them, or build on one CTA
             if (n_raw > ftk::GB_RAW_MAX) {

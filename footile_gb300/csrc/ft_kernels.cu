@@ -3104,35 +3104,48 @@ __device__ int gb_walk(const KParams& P, const ft_op& op, int kind, float px, fl
 
 __global__ void __launch_bounds__(BLOCK) k_gb_ops(KParams P) {
     __shared__ int tmp[2 * NWARP + 2];
-    __shared__ int s_pc, s_pw;
+    __shared__ int s_tot[3];
     const GridBuildBufs& G = P.gb;
     const int tid = threadIdx.x, i = blockIdx.x * BLOCK + tid;
     const int kind = i < G.n_ops ? __ldg(&G.ops[i].kind) : -1;
     int mpc, lpc;
     block_max_scan((kind >= FT_OP_CLOSE && kind <= FT_OP_CUBIC) ? i : -1, tmp, mpc, lpc);
     const int mpw = block_incl_max(kind == FT_OP_PEN_WIDTH ? i : -1, tmp);
-    if (i < G.n_ops) G.opi[i].x = lpc;  // the block's part; k_gb_count adds the blocks before
-    if (tid == BLOCK - 1) G.opa[blockIdx.x] = make_int2(mpc, mpw);
+    const int mcm = block_incl_max((kind == FT_OP_CLOSE || kind == FT_OP_MOVE) ? i : -1, tmp);
+    if (i < G.n_ops) {
+        G.opi[i].x = lpc;  // the block's part; k_gb_count adds the blocks before
+        G.opw[i] = mpw;
+    }
+    if (tid == BLOCK - 1) G.opa[blockIdx.x] = make_int4(mpc, mpw, mcm, 0);
     if (!gb_last_block(&G.done[0])) return;
     // exclusive max over the blocks, in place
     const int nb = (int)gridDim.x;
-    int cpc = -1, cpw = -1;
+    int cpc = -1, cpw = -1, ccm = -1;
     for (int b0 = 0; b0 < nb; b0 += BLOCK) {
         const int b = b0 + tid;
-        const int2 a = b < nb ? __ldcg(&G.opa[b]) : make_int2(-1, -1);
-        int ipc, epc, ipw, epw;
+        const int4 a = b < nb ? __ldcg(&G.opa[b]) : make_int4(-1, -1, -1, 0);
+        int ipc, epc, ipw, epw, icm, ecm;
         block_max_scan(a.x, tmp, ipc, epc);
-        if (tid == BLOCK - 1) s_pc = ipc;
+        if (tid == BLOCK - 1) s_tot[0] = ipc;
         block_max_scan(a.y, tmp, ipw, epw);
-        if (tid == BLOCK - 1) s_pw = ipw;
+        if (tid == BLOCK - 1) s_tot[1] = ipw;
+        block_max_scan(a.z, tmp, icm, ecm);
+        if (tid == BLOCK - 1) s_tot[2] = icm;
         __syncthreads();
-        if (b < nb) G.opa[b] = make_int2(max(cpc, epc), max(cpw, epw));
-        cpc = max(cpc, s_pc);
-        cpw = max(cpw, s_pw);
+        if (b < nb) G.opa[b] = make_int4(max(cpc, epc), max(cpw, epw), max(ccm, ecm), 0);
+        cpc = max(cpc, s_tot[0]);
+        cpw = max(cpw, s_tot[1]);
+        ccm = max(ccm, s_tot[2]);
         __syncthreads();
     }
-    // pen width after the call: the last PenWidth op of the path
-    if (tid == 0 && P.sw_out) P.sw_out[0] = cpw >= 0 ? G.ops[cpw].v[0] : G.s_width;
+    if (tid == 0) {
+        // pen width after the call: the last PenWidth op of the path
+        if (P.sw_out) P.sw_out[0] = cpw >= 0 ? G.ops[cpw].v[0] : G.s_width;
+        if (P.gs.st) {
+            P.gs.st[3] = cpc;
+            P.gs.st[4] = ccm;
+        }
+    }
 }
 
 // Op i of a CTA of k_gb_count / k_gb_emit (GB_OPB ops, GB_LANES lanes each) and its pen.
@@ -3205,6 +3218,22 @@ __global__ void __launch_bounds__(BLOCK) k_gb_count(KParams P) {
     if (tid == 0) *G.n_raw = carry;
 }
 
+// Exclusive max of the tiles' last sub-figure starts, in place (one CTA).
+__device__ void gb_scan_tr(const GridBuildBufs& G, long long n_raw, int* tmp, int& s_c) {
+    const int tid = threadIdx.x, nt = (int)((n_raw + GB_TILE - 1) / GB_TILE);
+    int carry = -1;
+    for (int b0 = 0; b0 < nt; b0 += BLOCK) {
+        const int b = b0 + tid;
+        int inc, exc;
+        block_max_scan(b < nt ? __ldcg(&G.tr[b]) : -1, tmp, inc, exc);
+        if (tid == BLOCK - 1) s_c = inc;
+        __syncthreads();
+        if (b < nt) G.tr[b] = max(carry, exc);
+        carry = max(carry, s_c);
+        __syncthreads();
+    }
+}
+
 __global__ void __launch_bounds__(BLOCK) k_gb_emit(KParams P) {
     __shared__ int tmp[2 * NWARP + 2];
     __shared__ int s_c;
@@ -3231,19 +3260,7 @@ __global__ void __launch_bounds__(BLOCK) k_gb_emit(KParams P) {
         if (rs0 && ck(off < cap, 13) && off < cap) atomicMax(&G.tr[off / GB_TILE], off);
     }
     if (!gb_last_block(&G.done[2])) return;
-    // exclusive max of the tiles' last sub-figure starts, in place
-    const int nt = (int)((n_raw + GB_TILE - 1) / GB_TILE);
-    int carry = -1;
-    for (int b0 = 0; b0 < nt; b0 += BLOCK) {
-        const int b = b0 + tid;
-        int inc, exc;
-        block_max_scan(b < nt ? __ldcg(&G.tr[b]) : -1, tmp, inc, exc);
-        if (tid == BLOCK - 1) s_c = inc;
-        __syncthreads();
-        if (b < nt) G.tr[b] = max(carry, exc);
-        carry = max(carry, s_c);
-        __syncthreads();
-    }
+    gb_scan_tr(G, n_raw, tmp, s_c);
 }
 
 __global__ void __launch_bounds__(BLOCK) k_gb_keep(KParams P) {
@@ -3475,6 +3492,462 @@ cudaError_t launch_grid_build(const KParams& p, int sm_count, cudaStream_t s, co
         k_gb_write<<<gt, BLOCK, 0, s>>>(*q);
         k_gb_top<<<GB_TOP_BLOCKS, BLOCK, 0, s>>>(*q);
     }
+    return cudaGetLastError();
+}
+
+// ---- grid-wide build of one stroke path
+//
+// Plotter::stroke (plotter.rs:356-365) collects the stroke points (Stroke::add_point and
+// close, stroker.rs:204-236), makes every sub-stroke's outline (stroker.rs:239-416) and
+// fills it NonZero.  Over the whole GPU, in stream order:
+//   k_gb_ops    pens, the last PenWidth op at or before each op, the last Close/Move op
+//   k_gs_count  every op's raw stroke points (the walk carrying widths, GB_LANES lanes
+//               per op), scanned
+//   k_gs_emit   the raw points (x, y, width), whether each starts a sub-stroke, its op
+//   k_gs_keep   per raw point: kept when it starts a sub-stroke or its f32 position
+//               differs from the raw point before it (no closing point is popped); per
+//               tile the kept points and sub-stroke starts, scanned
+//   k_gs_write  a kept point's position is the kept points before it and its sub-stroke
+//               the starts before it; points from 65,535 on are dropped and start
+//               nothing; a start sets its sub-stroke's first point and the joined flag the
+//               close events before it leave on the sub-stroke before
+//   k_gs_subs   per sub-stroke: its points, the last one's joined flag (the last Close or
+//               Move op after its last point when the cap stopped the points, else the
+//               path's last Move/Line/Quad/Cubic/Close op), SubStroke::len in u16
+//               arithmetic and 2 len + 2 outline items, scanned
+//   k_go_count  every outline item's points (outline_item), scanned
+//   k_go_emit   the outline's raw vertices through the second transform (plotter.rs:
+//               219-224), the figure runs' starts per tile, scanned
+// then k_gb_keep, k_gb_write and k_gb_top build the outline's figure as they do a fill's.
+
+// width in effect at op j: its path's last PenWidth op at or before it, else the width
+// the path starts with
+__device__ __forceinline__ float gs_width(const GridBuildBufs& G, int j) {
+    if (j < 0) return G.s_width;
+    const int lpw = max(G.opw[j], G.opa[j / BLOCK].y);
+    return lpw >= 0 ? __ldg(&G.ops[lpw].v[0]) : G.s_width;
+}
+
+// Raw stroke points of a Move/Line/Quad/Cubic op with the pen at (px, py) and widths
+// pen_w (at the pen) and sw (at the op), as build_fill's STROKE walk makes them
+// (plotter.rs:233-236, 294-298), split over GB_LANES lanes as gb_walk splits a fill's:
+// emit(k, point, width) for the lane's k-th leaf; returns the lane's leaf count.
+template <class Emit>
+__device__ int gs_walk(const KParams& P, const ft_op& op, int kind, float px, float py, float pen_w, float sw,
+                       int lane, int& flags, Emit emit) {
+    if (kind == FT_OP_MOVE || kind == FT_OP_LINE) {
+        if (lane) return 0;
+        emit(0, xform(P.xf, p2(op.v[0], op.v[1])), sw);
+        return 1;
+    }
+    P2 a = xform(P.xf, p2(px, py)), b = xform(P.xf, p2(op.v[0], op.v[1])), c = xform(P.xf, p2(op.v[2], op.v[3]));
+    const float tol_sq = P.tol_sq;
+    int dh = 0, n;
+    if (kind == FT_OP_QUAD) {
+        float wa = pen_w, wb = __fmul_rn(__fadd_rn(pen_w, sw), 0.5f), wc = sw;
+        if (!pfinite(a) || !pfinite(b) || !pfinite(c)) {
+            if (lane) return 0;
+            flags |= 2;
+            emit(0, c, wc);
+            return 1;
+        }
+        for (int d = 0; d < GB_D0; d++) {
+            const P2 ab = pmid(a, b), bc = pmid(b, c), abbc = pmid(ab, bc), ac = pmid(a, c);
+            const bool within = pdist_sq(abbc, ac) <= tol_sq;
+            if (within || d >= FT_MAX_DEPTH) {
+                if (lane & ((1 << (GB_D0 - d)) - 1)) return 0;
+                if (!within) flags |= 1;
+                emit(0, c, wc);
+                return 1;
+            }
+            const float wab = fmid(wa, wb), wbc = fmid(wb, wc), wabbc = fmid(wab, wbc);
+            if ((lane >> (GB_D0 - 1 - d)) & 1) {
+                a = abbc;
+                b = bc;
+                wa = wabbc;
+                wb = wbc;
+            } else {
+                b = ab;
+                c = abbc;
+                wb = wab;
+                wc = wabbc;
+            }
+        }
+        n = quad_walk<true>(a, b, c, wa, wb, wc, tol_sq, 0, INT_MAX, &dh, emit, GB_D0);
+    } else {
+        P2 e = xform(P.xf, p2(op.v[4], op.v[5]));
+        float wa = pen_w, wb = __fadd_rn(sw, __fmul_rn(__fsub_rn(pen_w, sw), 1.0f / 3.0f)),
+              wc = __fadd_rn(sw, __fmul_rn(__fsub_rn(pen_w, sw), 2.0f / 3.0f)), we = sw;
+        if (!pfinite(a) || !pfinite(b) || !pfinite(c) || !pfinite(e)) {
+            if (lane) return 0;
+            flags |= 2;
+            emit(0, e, we);
+            return 1;
+        }
+        for (int d = 0; d < GB_D0; d++) {
+            const P2 ab = pmid(a, b), bc = pmid(b, c), cd = pmid(c, e);
+            const P2 abbc = pmid(ab, bc), bccd = pmid(bc, cd);
+            const P2 pe = pmid(abbc, bccd), ad = pmid(a, e);
+            const bool within = pdist_sq(pe, ad) <= tol_sq;
+            if (within || d >= FT_MAX_DEPTH) {
+                if (lane & ((1 << (GB_D0 - d)) - 1)) return 0;
+                if (!within) flags |= 1;
+                emit(0, e, we);
+                return 1;
+            }
+            const float wab = fmid(wa, wb), wbc = fmid(wb, wc), wcd = fmid(wc, we);
+            const float wabbc = fmid(wab, wbc), wbccd = fmid(wbc, wcd), wpe = fmid(wabbc, wbccd);
+            if ((lane >> (GB_D0 - 1 - d)) & 1) {
+                a = pe;
+                b = bccd;
+                c = cd;
+                wa = wpe;
+                wb = wbccd;
+                wc = wcd;
+            } else {
+                b = ab;
+                c = abbc;
+                e = pe;
+                wb = wab;
+                wc = wabbc;
+                we = wpe;
+            }
+        }
+        n = cubic_walk<true>(a, b, c, e, wa, wb, wc, we, tol_sq, 0, INT_MAX, &dh, emit, GB_D0);
+    }
+    if (dh) flags |= 1;
+    return n;
+}
+
+__device__ __forceinline__ bool gs_over(const GridStrokeBufs& S) { return *S.n_sraw > S.sraw_cap; }
+
+__global__ void __launch_bounds__(BLOCK) k_gs_count(KParams P) {
+    __shared__ int tmp[2 * NWARP + 2];
+    __shared__ long long ltmp[NWARP];
+    const GridBuildBufs& G = P.gb;
+    const GridStrokeBufs& S = P.gs;
+    const int tid = threadIdx.x;
+    int flags = 0;
+    const GbOp o = gb_op_of(G, flags);
+    int n = 0;
+    if (o.kind >= FT_OP_MOVE && o.kind <= FT_OP_CUBIC)
+        n = gs_walk(P, o.op, o.kind, o.px, o.py, gs_width(G, o.lpc), gs_width(G, o.i), o.lane, flags,
+                    [](int, P2, float) {});
+    if (flags) atomicMax(&P.status[0], (flags & 1) ? FT_ERR_DEPTH : FT_ERR_ARG);
+    int inc = n;
+#pragma unroll
+    for (int d = 1; d < GB_LANES; d <<= 1) {
+        const int t = __shfl_up_sync(FULL, inc, d, GB_LANES);
+        if (o.lane >= d) inc += t;
+    }
+    const int n_op = __shfl_sync(FULL, inc, GB_LANES - 1, GB_LANES);
+    int tot;
+    const int ex = block_excl_sum(o.lane == 0 ? n_op : 0, tmp, tot);
+    if (o.i < G.n_ops) {
+        G.opl[o.i * GB_LANES + o.lane] = inc - n;
+        if (o.lane == 0) G.opi[o.i].y = ex;
+    }
+    if (tid == 0) G.opn[blockIdx.x] = tot;
+    if (!gb_last_block(&S.done[0])) return;
+    const int nb = (int)gridDim.x;
+    long long carry = 0;
+    for (int b0 = 0; b0 < nb; b0 += BLOCK) {
+        const int b = b0 + tid;
+        long long t;
+        const long long e = block_excl_sum_ll(b < nb ? __ldcg(&G.opn[b]) : 0ll, ltmp, t);
+        if (b < nb) G.opn[b] = carry + e;
+        carry += t;
+    }
+    if (tid == 0) *S.n_sraw = carry;
+}
+
+__global__ void __launch_bounds__(BLOCK) k_gs_emit(KParams P) {
+    const GridBuildBufs& G = P.gb;
+    const GridStrokeBufs& S = P.gs;
+    if (gs_over(S)) return;  // every CTA: the caller grows the arrays
+    int flags = 0;
+    const GbOp o = gb_op_of(G, flags);
+    if (o.kind < FT_OP_MOVE || o.kind > FT_OP_CUBIC) return;
+    const long long off0 = G.opn[blockIdx.x] + G.opi[o.i].y;
+    const int off = (int)(off0 + G.opl[o.i * GB_LANES + o.lane]);
+    const int cap = S.sraw_cap;
+    // a Move ends the sub-stroke before it open, a Close joined (stroker.rs:87-96)
+    const unsigned char f0 = (unsigned char)(((o.lane == 0 && o.rs) ? 1 : 0) | (o.kind != FT_OP_MOVE ? 2 : 0));
+    const unsigned char f1 = (unsigned char)(o.kind != FT_OP_MOVE ? 2 : 0);
+    float4* raw4 = S.raw4;
+    unsigned char* sfl = S.sfl;
+    int* sopi = S.sopi;
+    const int i = o.i;
+    gs_walk(P, o.op, o.kind, o.px, o.py, gs_width(G, o.lpc), gs_width(G, o.i), o.lane, flags,
+            [&](int k, P2 q, float w) {
+                if (ck(off + k < cap, 13) && off + k < cap) {
+                    raw4[off + k] = make_float4(q.x, q.y, w, 0.f);
+                    sfl[off + k] = k == 0 ? f0 : f1;
+                    sopi[off + k] = i;
+                }
+            });
+}
+
+// Kept raw stroke points and sub-stroke starts per tile, packed (kept << 32 | starts).
+__global__ void __launch_bounds__(BLOCK) k_gs_keep(KParams P) {
+    __shared__ long long ltmp[NWARP];
+    const GridStrokeBufs& S = P.gs;
+    if (gs_over(S)) return;
+    const int M = (int)*S.n_sraw, nt = (M + GB_TILE - 1) / GB_TILE, tid = threadIdx.x;
+    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+        const int k0 = t * GB_TILE + GB_PER * tid;
+        long long v = 0;
+        float2 q = make_float2(0.f, 0.f);
+        if (k0 > 0 && k0 <= M) {
+            const float4 p = S.raw4[k0 - 1];
+            q = make_float2(p.x, p.y);
+        }
+#pragma unroll
+        for (int j = 0; j < GB_PER; j++) {
+            const int k = k0 + j;
+            if (k >= M) break;
+            const float4 p = S.raw4[k];
+            const int rs = S.sfl[k] & 1;
+            const bool keep = rs || !(p.x == q.x && p.y == q.y);
+            v += ((long long)(keep ? 1 : 0) << 32) | rs;
+            q = make_float2(p.x, p.y);
+        }
+        long long tot;
+        block_excl_sum_ll(v, ltmp, tot);
+        if (tid == 0) S.stile[t] = make_int2((int)(tot >> 32), (int)(tot & 0xFFFFFFFFll));
+    }
+    if (!gb_last_block(&S.done[1])) return;
+    long long carry = 0;
+    for (int b0 = 0; b0 < nt; b0 += BLOCK) {
+        const int b = b0 + tid;
+        long long x = 0;
+        if (b < nt) {
+            const int2 a = __ldcg(&S.stile[b]);
+            x = ((long long)a.x << 32) | (unsigned)a.y;
+        }
+        long long t;
+        const long long e = carry + block_excl_sum_ll(x, ltmp, t);
+        if (b < nt) S.stile[b] = make_int2((int)(e >> 32), (int)(e & 0xFFFFFFFFll));
+        carry += t;
+    }
+    if (tid == 0) {
+        const int kept = (int)(carry >> 32);
+        S.st[0] = min(kept, PT_CAP);
+        S.st[6] = kept > PT_CAP ? 1 : 0;
+    }
+}
+
+__global__ void __launch_bounds__(BLOCK) k_gs_write(KParams P) {
+    __shared__ long long ltmp[NWARP];
+    const GridStrokeBufs& S = P.gs;
+    if (gs_over(S)) return;
+    const int M = (int)*S.n_sraw, nt = (M + GB_TILE - 1) / GB_TILE, tid = threadIdx.x;
+    const int count = S.st[0];
+    float4* spts = reinterpret_cast<float4*>(P.scratch + P.L.spts);
+    SubRec* subs = reinterpret_cast<SubRec*>(P.scratch + P.L.subs);
+    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+        const int2 c = S.stile[t];
+        const int k0 = t * GB_TILE + GB_PER * tid;
+        float4 p[GB_PER];
+        int f[GB_PER], keep = 0;
+        long long v = 0;
+        float2 q = make_float2(0.f, 0.f);
+        if (k0 > 0 && k0 <= M) {
+            const float4 pp = S.raw4[k0 - 1];
+            q = make_float2(pp.x, pp.y);
+        }
+#pragma unroll
+        for (int j = 0; j < GB_PER; j++) {
+            const int k = k0 + j;
+            p[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+            f[j] = 0;
+            if (k < M) {
+                p[j] = S.raw4[k];
+                f[j] = S.sfl[k];
+                const int rs = f[j] & 1;
+                if (rs || !(p[j].x == q.x && p[j].y == q.y)) keep |= 1 << j;
+                v += ((long long)((keep >> j) & 1) << 32) | rs;
+                q = make_float2(p[j].x, p[j].y);
+            }
+        }
+        long long tot;
+        const long long e = block_excl_sum_ll(v, ltmp, tot);
+        int pos = c.x + (int)(e >> 32), sid = c.y + (int)(e & 0xFFFFFFFFll);
+#pragma unroll
+        for (int j = 0; j < GB_PER; j++) {
+            if (!((keep >> j) & 1)) continue;
+            const int rs = f[j] & 1;
+            if (pos < PT_CAP) {
+                spts[pos] = p[j];
+                if (rs) {
+                    subs[sid].start = pos;
+                    if (sid > 0) subs[sid - 1].joined = (f[j] >> 1) & 1;
+                    atomicMax(&S.st[1], sid + 1);
+                }
+                if (pos == count - 1) S.st[2] = S.sopi[k0 + j];  // the op of the last kept point
+            }
+            pos++;
+            sid += rs;
+        }
+    }
+}
+
+// Sub-strokes (stroker.rs:87-96, 239-262), GB_TILE... 256 per chunk.
+__global__ void __launch_bounds__(BLOCK) k_gs_subs(KParams P) {
+    __shared__ int tmp[2 * NWARP + 2];
+    __shared__ int s_c;
+    const GridBuildBufs& G = P.gb;
+    const GridStrokeBufs& S = P.gs;
+    if (gs_over(S)) return;
+    const int tid = threadIdx.x, nsub = S.st[1], count = S.st[0];
+    SubRec* subs = reinterpret_cast<SubRec*>(P.scratch + P.L.subs);
+    const int nc = (nsub + BLOCK - 1) / BLOCK;
+    for (int c = blockIdx.x; c < nc; c += gridDim.x) {
+        const int si = c * BLOCK + tid;
+        int items = 0;
+        if (si < nsub) {
+            const SubRec r = subs[si];
+            const int n = (si + 1 < nsub ? subs[si + 1].start : count) - r.start;
+            int joined = r.joined;
+            if (si == nsub - 1) {
+                // the last sub-stroke: the close events after its last point
+                const int cm = S.st[4], pc = S.st[3];
+                if (S.st[6])
+                    joined = cm > S.st[2] ? (__ldg(&G.ops[cm].kind) == FT_OP_CLOSE) : 0;
+                else
+                    joined = pc >= 0 ? (__ldg(&G.ops[pc].kind) == FT_OP_CLOSE) : 0;
+                subs[si].joined = joined;
+            }
+            // SubStroke::len with u16 arithmetic: n + 1 wraps at 65,536
+            const int len = joined ? ((n + 1) & 0xFFFF) : (n > 0 ? n - 1 : 0);
+            items = len > 0 ? 2 * len + 2 : 0;
+            subs[si].n = n;
+            subs[si].len = len;
+        }
+        int tot;
+        const int off = block_excl_sum(items, tmp, tot);
+        if (si < nsub) subs[si].item_off = off;
+        if (tid == 0) S.subt[c] = tot;
+    }
+    if (!gb_last_block(&S.done[2])) return;
+    int carry = 0;
+    for (int b0 = 0; b0 < nc; b0 += BLOCK) {
+        const int b = b0 + tid;
+        int tot;
+        const int e = block_excl_sum(b < nc ? __ldcg(&S.subt[b]) : 0, tmp, tot);
+        if (b < nc) S.subt[b] = carry + e;
+        carry += tot;
+    }
+    if (tid == 0) S.st[5] = carry;
+    (void)s_c;
+}
+
+// Outline item t: its sub-stroke (the last with item offset <= t: empty sub-strokes share
+// the next one's offset and come before it) and its index u in it.
+__device__ __forceinline__ SubRec go_item(const GridStrokeBufs& S, const SubRec* subs, int nsub, int t, int& u) {
+    int lo = 0, hi = nsub - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (subs[mid].item_off + S.subt[mid / BLOCK] <= t)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    SubRec sr = subs[lo];
+    sr.item_off += S.subt[lo / BLOCK];
+    u = t - sr.item_off;
+    return sr;
+}
+
+__global__ void __launch_bounds__(BLOCK) k_go_count(KParams P) {
+    __shared__ int tmp[2 * NWARP + 2];
+    __shared__ long long ltmp[NWARP];
+    const GridBuildBufs& G = P.gb;
+    const GridStrokeBufs& S = P.gs;
+    if (gs_over(S)) return;
+    const int tid = threadIdx.x, nsub = S.st[1], n_items = min(S.st[5], GS_ITEMS_CAP);
+    const float4* spts = reinterpret_cast<const float4*>(P.scratch + P.L.spts);
+    const SubRec* subs = reinterpret_cast<const SubRec*>(P.scratch + P.L.subs);
+    const int nc = (n_items + BLOCK - 1) / BLOCK;
+    int depth_hit = 0;
+    for (int c = blockIdx.x; c < nc; c += gridDim.x) {
+        const int t = c * BLOCK + tid;
+        int n = 0;
+        if (t < n_items) {
+            int u;
+            const SubRec sr = go_item(S, subs, nsub, t, u);
+            n = outline_item(P, spts, sr, u, INT_MAX, INT_MAX, &depth_hit, [](int, P2) {});
+        }
+        int tot;
+        const int off = block_excl_sum(n, tmp, tot);
+        if (t < n_items) S.itoff[t] = off;
+        if (tid == 0) S.itc[c] = tot;
+    }
+    if (depth_hit) atomicMax(&P.status[0], FT_ERR_DEPTH);
+    if (!gb_last_block(&S.done[3])) return;
+    long long carry = 0;
+    for (int b0 = 0; b0 < nc; b0 += BLOCK) {
+        const int b = b0 + tid;
+        long long t;
+        const long long e = block_excl_sum_ll(b < nc ? (long long)__ldcg(&S.itc[b]) : 0ll, ltmp, t);
+        if (b < nc) S.itc[b] = (int)min(carry + e, (long long)INT_MAX);
+        carry += t;
+    }
+    if (tid == 0) *G.n_raw = carry;
+}
+
+__global__ void __launch_bounds__(BLOCK) k_go_emit(KParams P) {
+    __shared__ int tmp[2 * NWARP + 2];
+    __shared__ int s_c;
+    const GridBuildBufs& G = P.gb;
+    const GridStrokeBufs& S = P.gs;
+    if (gs_over(S)) return;
+    const long long n_raw = *G.n_raw;
+    if (n_raw > G.raw_cap) return;
+    const int tid = threadIdx.x, nsub = S.st[1], n_items = min(S.st[5], GS_ITEMS_CAP), cap = G.raw_cap;
+    const float4* spts = reinterpret_cast<const float4*>(P.scratch + P.L.spts);
+    const SubRec* subs = reinterpret_cast<const SubRec*>(P.scratch + P.L.subs);
+    for (int t = blockIdx.x * BLOCK + tid; t < n_items; t += gridDim.x * BLOCK) {
+        int u;
+        const SubRec sr = go_item(S, subs, nsub, t, u);
+        const int off = S.itc[t / BLOCK] + S.itoff[t];
+        // a figure run starts at each side's first point after a Close: the forward side
+        // always (after the previous sub-stroke's Close, or first), the reverse side when
+        // the sub-stroke is joined (stroker.rs:255-260)
+        const bool rev = u > sr.len, joined = sr.joined != 0;
+        const int j = rev ? u - sr.len - 1 : u;
+        const int rsk = ((!rev && ((!joined && j == 0) || (joined && j == 1))) || (rev && joined && j == 1)) ? 0 : -1;
+        int dh = 0;
+        const int n = outline_item(P, spts, sr, u, 0, INT_MAX, &dh, [&](int k, P2 q) {
+            const P2 tq = xform(P.xf, q);  // the outline is transformed again (F9)
+            if (ck(off + k < cap, 16) && off + k < cap) {
+                G.raw[off + k] = make_int2(f2fx(tq.x), f2fx(tq.y));
+                G.fl[off + k] = k == rsk ? (unsigned char)1 : (unsigned char)0;
+            }
+        });
+        if (rsk == 0 && n > 0 && off < cap) atomicMax(&G.tr[off / GB_TILE], off);
+    }
+    if (!gb_last_block(&G.done[2])) return;
+    gb_scan_tr(G, n_raw, tmp, s_c);
+}
+
+cudaError_t launch_grid_stroke(const KParams& p, int sm_count, cudaStream_t s) {
+    const int nbo = (p.gb.n_ops + BLOCK - 1) / BLOCK, nbw = (p.gb.n_ops + GB_OPB - 1) / GB_OPB;
+    if (nbo <= 0 || p.gb.raw_cap % GB_TILE || p.gb.raw_cap > GB_RAW_MAX || p.gs.sraw_cap % GB_TILE ||
+        p.gs.sraw_cap > GB_RAW_MAX || !p.gs.st || p.pt_cap != PT_CAP)
+        return cudaErrorInvalidValue;
+    const int gt = std::max(1, 4 * sm_count);
+    k_gb_ops<<<nbo, BLOCK, 0, s>>>(p);
+    k_gs_count<<<nbw, BLOCK, 0, s>>>(p);
+    k_gs_emit<<<nbw, BLOCK, 0, s>>>(p);
+    k_gs_keep<<<gt, BLOCK, 0, s>>>(p);
+    k_gs_write<<<gt, BLOCK, 0, s>>>(p);
+    k_gs_subs<<<std::max(1, std::min(gt, PT_CAP / BLOCK + 1)), BLOCK, 0, s>>>(p);
+    k_go_count<<<gt, BLOCK, 0, s>>>(p);
+    k_go_emit<<<gt, BLOCK, 0, s>>>(p);
+    k_gb_keep<<<gt, BLOCK, 0, s>>>(p);
+    k_gb_write<<<gt, BLOCK, 0, s>>>(p);
+    k_gb_top<<<GB_TOP_BLOCKS, BLOCK, 0, s>>>(p);
     return cudaGetLastError();
 }
 

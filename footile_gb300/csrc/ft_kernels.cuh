@@ -117,7 +117,8 @@ struct GridBuildBufs {
     unsigned* done;     // [8] tickets: the last CTA of a kernel to finish runs its scan
     long long* n_raw;   // raw vertices of the path
     int* count;         // vertices kept
-    int2* opa;          // per 256 ops: last Move/Line/Quad/Cubic/Close op, last PenWidth op
+    int4* opa;          // per 256 ops: last Move/Line/Quad/Cubic/Close op, last PenWidth op, last Close/Move op
+    int* opw;           // per op: last PenWidth op at or before it in its 256 (strokes)
     long long* opn;     // per GB_OPB ops: raw vertices
     int2* opi;          // per op: last Move/Line/Quad/Cubic/Close op before it in its 256, raw offset in its GB_OPB
     int* opl;           // per op and lane: the lane's raw offset in the op
@@ -131,16 +132,38 @@ struct GridBuildBufs {
     int* final_flag;    // nullable: set when the cap is reached (the figure is complete)
     const int* skip;    // nullable: the kernels after k_gb_ops do nothing when *skip is set
 };
-struct GbLayout {
-    size_t state, opa, opn, opi, opl, raw, fl, kp, rk, tr, tr2, tp, top, bytes;
+// Grid-wide build of one stroke path (the stroker's points, sub-strokes and outline, then
+// the outline's figure through the fill build's k_gb_keep / k_gb_write / k_gb_top).
+constexpr int GS_ITEMS_CAP = 6 * PT_CAP + 256;  // outline items of 65,535 stroke points at most
+struct GridStrokeBufs {
+    int sraw_cap;        // raw stroke points the arrays hold (a multiple of GB_TILE)
+    long long* n_sraw;   // raw stroke points of the path
+    int* st;             // [0] points kept, [1] sub-strokes, [2] op of the last kept point, [3] last
+                         // Move/Line/Quad/Cubic/Close op, [4] last Close/Move op, [5] outline items,
+                         // [6] the 65,535-point cap was reached
+    unsigned* done;      // [8] tickets
+    float4* raw4;        // raw stroke points: x, y, width
+    unsigned char* sfl;  // per raw point: 1 starts a sub-stroke, 2 its op is not a Move
+    int* sopi;           // per raw point: its op
+    int2* stile;         // per tile of raw points: kept, sub-stroke starts
+    int* subt;           // per 256 sub-strokes: outline items
+    int* itoff;          // per outline item: raw offset in its 256
+    int* itc;            // per 256 outline items: raw vertices
 };
-constexpr GbLayout gb_layout(size_t n_ops, size_t raw_cap) {
+struct GbLayout {
+    size_t state, opa, opw, opn, opi, opl, raw, fl, kp, rk, tr, tr2, tp, top;
+    size_t raw4, sfl, sopi, stile, subt, itoff, itc, bytes;
+};
+constexpr GbLayout gb_layout(size_t n_ops, size_t raw_cap, size_t sraw_cap = 0) {
     GbLayout g{};
     const size_t nbo = (n_ops + BLOCK - 1) / BLOCK, nbw = (n_ops + GB_OPB - 1) / GB_OPB,
                  ntiles = raw_cap / GB_TILE;
-    g.state = 0;  // two builds' done[8] at 0 / 128, n_raw at 32 / 160, count at 40 / 168, final at 44 / 172
+    // two builds' done[8] at 0 / 128, n_raw at 32 / 160, count at 40 / 168, final at 44 / 172;
+    // a stroke build's st[] at 128, n_sraw at 160, done[] at 192
+    g.state = 0;
     g.opa = 256;
-    g.opn = align256(g.opa + nbo * 8);
+    g.opw = align256(g.opa + nbo * 16);
+    g.opn = align256(g.opw + n_ops * 4);
     g.opi = align256(g.opn + nbw * 8);
     g.opl = align256(g.opi + n_ops * 8);
     g.raw = align256(g.opl + n_ops * GB_LANES * 4);
@@ -151,7 +174,14 @@ constexpr GbLayout gb_layout(size_t n_ops, size_t raw_cap) {
     g.tr2 = align256(g.tr + ntiles * 4);
     g.tp = align256(g.tr2 + ntiles * 4);
     g.top = align256(g.tp + ntiles * 16);
-    g.bytes = align256(g.top + (size_t)GB_TOP_BLOCKS * 16);
+    g.raw4 = align256(g.top + (size_t)GB_TOP_BLOCKS * 16);
+    g.sfl = align256(g.raw4 + sraw_cap * 16);
+    g.sopi = align256(g.sfl + sraw_cap);
+    g.stile = align256(g.sopi + sraw_cap * 4);
+    g.subt = align256(g.stile + sraw_cap / GB_TILE * 8);
+    g.itoff = align256(g.subt + (sraw_cap ? (size_t)(PT_CAP / BLOCK + 1) * 4 : 0));
+    g.itc = align256(g.itoff + (sraw_cap ? (size_t)GS_ITEMS_CAP * 4 : 0));
+    g.bytes = align256(g.itc + (sraw_cap ? (size_t)(GS_ITEMS_CAP / BLOCK + 1) * 4 : 0));
     return g;
 }
 
@@ -202,6 +232,7 @@ struct KParams {
     int use_tma;
     // one fill path built over the whole GPU (launch_grid_build) instead of by k_cbuild
     GridBuildBufs gb;
+    GridStrokeBufs gs;  // and the stroker's part of one stroke path (launch_grid_stroke)
 };
 
 // Ordered composite: per-path figure build and edge binning, then one CTA per band.
@@ -232,6 +263,12 @@ cudaError_t launch_figure_bins(const KParams& p, int grid, cudaStream_t s);
 // final_flag the full build's skip): when the cap is reached within the prefix the figure
 // is complete and the full build does nothing.
 cudaError_t launch_grid_build(const KParams& p, int sm_count, cudaStream_t s, const KParams* probe = nullptr);
+// The same for one stroke path (p.gb and p.gs): stroke points, sub-strokes and outline over
+// the whole GPU, then the outline's figure as launch_grid_build builds a fill's.  p.gs's
+// state (st, n_sraw, done) must be zero before the launch, as p.gb's.  When the path has
+// more raw stroke points than p.gs.sraw_cap, or its outline more raw vertices than
+// p.gb.raw_cap, *n_sraw / *n_raw say how many and the figure is empty.
+cudaError_t launch_grid_stroke(const KParams& p, int sm_count, cudaStream_t s);
 int composite_bands_smem(int band_rows, int width);
 int composite_build_blocks_per_sm(int smem_bytes, bool stroke);
 
