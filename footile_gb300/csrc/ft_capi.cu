@@ -1141,7 +1141,7 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
             const ftk::GbLayout G = ftk::gb_layout(paths[0].n_ops, raw_cap, sraw_cap);
             FT_CU(c->gbuf.ensure(G.bytes), "alloc grid build");
             unsigned char* gb = static_cast<unsigned char*>(c->gbuf.p);
-            FT_CU(cudaMemsetAsync(gb, 0, 256, c->stream), "reset grid build");
+            FT_CU(cudaMemsetAsync(gb, 0, 512, c->stream), "reset grid build");
             FT_CU(cudaMemsetAsync(gb + G.tr, 0xFF, G.tp - G.tr, c->stream), "reset grid build");  // tr, tr2
             ftk::GridBuildBufs& g = p.gb;
             g.ops = ops_d + paths[0].op_begin;
@@ -1178,12 +1178,23 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
                 q.subt = reinterpret_cast<int*>(gb + G.subt);
                 q.itoff = reinterpret_cast<int*>(gb + G.itoff);
                 q.itc = reinterpret_cast<int*>(gb + G.itc);
+                q.final_flag = nullptr;
+                q.skip = nullptr;
             }
             // a probe over the first ops: a capped figure usually reaches its cap there, and
             // the build over all ops is then skipped
             const int probe_ops = std::max(4096, p.pt_cap / 8);
-            use_probe = !stroke && (int)paths[0].n_ops > 2 * probe_ops;
-            if (use_probe) {
+            use_probe = (int)paths[0].n_ops > 2 * probe_ops;
+            if (use_probe && stroke) {
+                // the stroke points over the first ops: the 65,535-point cap is usually reached there
+                pp = p;
+                pp.gb.n_ops = probe_ops;
+                ftk::GridStrokeBufs& q = pp.gs;
+                q.n_sraw = reinterpret_cast<long long*>(gb + 256);
+                q.done = reinterpret_cast<unsigned*>(gb + 288);
+                q.final_flag = reinterpret_cast<int*>(gb + 320);
+                p.gs.skip = q.final_flag;
+            } else if (use_probe) {
                 pp = p;
                 ftk::GridBuildBufs& q = pp.gb;
                 q.n_ops = probe_ops;
@@ -1200,8 +1211,9 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
         if (n_paths) {
             Stage st_build("figure build and edge binning");
             if (grid_build && stroke) {
-                FT_CU(ftk::launch_grid_stroke(p, c->sm_count, c->stream), "launch grid stroke build");
-                c->launches += 11;
+                FT_CU(ftk::launch_grid_stroke(p, c->sm_count, c->stream, use_probe ? &pp : nullptr),
+                      "launch grid stroke build");
+                c->launches += use_probe ? 15 : 11;
             } else if (grid_build) {
                 FT_CU(ftk::launch_grid_build(p, c->sm_count, c->stream, use_probe ? &pp : nullptr),
                       "launch grid figure build");
@@ -1224,14 +1236,20 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
         long long n_raw = 0, n_raw_probe = 0, n_sraw = 0;
         if (grid_build)
             FT_CU(cudaMemcpyAsync(&n_raw, p.gb.n_raw, sizeof(n_raw), cudaMemcpyDeviceToHost, c->stream), "raw count");
+        long long n_sraw_probe = 0;
         if (grid_build && stroke)
             FT_CU(cudaMemcpyAsync(&n_sraw, p.gs.n_sraw, sizeof(n_sraw), cudaMemcpyDeviceToHost, c->stream),
+                  "stroke point count");
+        if (grid_build && stroke && use_probe)
+            FT_CU(cudaMemcpyAsync(&n_sraw_probe, pp.gs.n_sraw, sizeof(n_sraw_probe), cudaMemcpyDeviceToHost,
+                                  c->stream),
                   "stroke point count");
         if (use_probe)
             FT_CU(cudaMemcpyAsync(&n_raw_probe, pp.gb.n_raw, sizeof(n_raw_probe), cudaMemcpyDeviceToHost, c->stream),
                   "raw count");
         FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
         n_raw = std::max(n_raw, n_raw_probe);  // the full build is skipped after a complete probe
+        n_sraw = std::max(n_sraw, n_sraw_probe);
         if (grid_build && stroke && n_sraw > (long long)sraw_cap) {
             // more raw stroke points than the arrays hold: grow them, or build on one CTA
             if (n_sraw > ftk::GB_RAW_MAX) {

@@ -3626,6 +3626,7 @@ __global__ void __launch_bounds__(BLOCK) k_gs_count(KParams P) {
     __shared__ long long ltmp[NWARP];
     const GridBuildBufs& G = P.gb;
     const GridStrokeBufs& S = P.gs;
+    if (S.skip && *S.skip) return;  // a probe over a prefix of the ops completed the points
     const int tid = threadIdx.x;
     int flags = 0;
     const GbOp o = gb_op_of(G, flags);
@@ -3664,6 +3665,7 @@ __global__ void __launch_bounds__(BLOCK) k_gs_count(KParams P) {
 __global__ void __launch_bounds__(BLOCK) k_gs_emit(KParams P) {
     const GridBuildBufs& G = P.gb;
     const GridStrokeBufs& S = P.gs;
+    if (S.skip && *S.skip) return;  // a probe over a prefix of the ops completed the points
     if (gs_over(S)) return;  // every CTA: the caller grows the arrays
     int flags = 0;
     const GbOp o = gb_op_of(G, flags);
@@ -3692,6 +3694,7 @@ __global__ void __launch_bounds__(BLOCK) k_gs_emit(KParams P) {
 __global__ void __launch_bounds__(BLOCK) k_gs_keep(KParams P) {
     __shared__ long long ltmp[NWARP];
     const GridStrokeBufs& S = P.gs;
+    if (S.skip && *S.skip) return;  // a probe over a prefix of the ops completed the points
     if (gs_over(S)) return;
     const int M = (int)*S.n_sraw, nt = (M + GB_TILE - 1) / GB_TILE, tid = threadIdx.x;
     for (int t = blockIdx.x; t < nt; t += gridDim.x) {
@@ -3734,12 +3737,14 @@ __global__ void __launch_bounds__(BLOCK) k_gs_keep(KParams P) {
         const int kept = (int)(carry >> 32);
         S.st[0] = min(kept, PT_CAP);
         S.st[6] = kept > PT_CAP ? 1 : 0;
+        if (S.final_flag && kept > PT_CAP) *S.final_flag = 1;
     }
 }
 
 __global__ void __launch_bounds__(BLOCK) k_gs_write(KParams P) {
     __shared__ long long ltmp[NWARP];
     const GridStrokeBufs& S = P.gs;
+    if (S.skip && *S.skip) return;  // a probe over a prefix of the ops completed the points
     if (gs_over(S)) return;
     const int M = (int)*S.n_sraw, nt = (M + GB_TILE - 1) / GB_TILE, tid = threadIdx.x;
     const int count = S.st[0];
@@ -3931,17 +3936,22 @@ __global__ void __launch_bounds__(BLOCK) k_go_emit(KParams P) {
     gb_scan_tr(G, n_raw, tmp, s_c);
 }
 
-cudaError_t launch_grid_stroke(const KParams& p, int sm_count, cudaStream_t s) {
-    const int nbo = (p.gb.n_ops + BLOCK - 1) / BLOCK, nbw = (p.gb.n_ops + GB_OPB - 1) / GB_OPB;
+cudaError_t launch_grid_stroke(const KParams& p, int sm_count, cudaStream_t s, const KParams* probe) {
+    const int nbo = (p.gb.n_ops + BLOCK - 1) / BLOCK;
     if (nbo <= 0 || p.gb.raw_cap % GB_TILE || p.gb.raw_cap > GB_RAW_MAX || p.gs.sraw_cap % GB_TILE ||
         p.gs.sraw_cap > GB_RAW_MAX || !p.gs.st || p.pt_cap != PT_CAP)
         return cudaErrorInvalidValue;
+    if (probe && (probe->gb.n_ops <= 0 || probe->gb.n_ops > p.gb.n_ops)) return cudaErrorInvalidValue;
     const int gt = std::max(1, 4 * sm_count);
-    k_gb_ops<<<nbo, BLOCK, 0, s>>>(p);
-    k_gs_count<<<nbw, BLOCK, 0, s>>>(p);
-    k_gs_emit<<<nbw, BLOCK, 0, s>>>(p);
-    k_gs_keep<<<gt, BLOCK, 0, s>>>(p);
-    k_gs_write<<<gt, BLOCK, 0, s>>>(p);
+    k_gb_ops<<<nbo, BLOCK, 0, s>>>(p);  // pens and widths of every op (the probe's too)
+    for (const KParams* q : {probe, &p}) {
+        if (!q) continue;
+        const int nbw = (q->gb.n_ops + GB_OPB - 1) / GB_OPB;
+        k_gs_count<<<nbw, BLOCK, 0, s>>>(*q);
+        k_gs_emit<<<nbw, BLOCK, 0, s>>>(*q);
+        k_gs_keep<<<gt, BLOCK, 0, s>>>(*q);
+        k_gs_write<<<gt, BLOCK, 0, s>>>(*q);
+    }
     k_gs_subs<<<std::max(1, std::min(gt, PT_CAP / BLOCK + 1)), BLOCK, 0, s>>>(p);
     k_go_count<<<gt, BLOCK, 0, s>>>(p);
     k_go_emit<<<gt, BLOCK, 0, s>>>(p);

@@ -149,6 +149,8 @@ struct GridStrokeBufs {
     int* subt;           // per 256 sub-strokes: outline items
     int* itoff;          // per outline item: raw offset in its 256
     int* itc;            // per 256 outline items: raw vertices
+    int* final_flag;     // nullable: set when the 65,535-point cap is reached (the points are complete)
+    const int* skip;     // nullable: the stroke point kernels do nothing when *skip is set
 };
 struct GbLayout {
     size_t state, opa, opw, opn, opi, opl, raw, fl, kp, rk, tr, tr2, tp, top;
@@ -159,9 +161,10 @@ constexpr GbLayout gb_layout(size_t n_ops, size_t raw_cap, size_t sraw_cap = 0) 
     const size_t nbo = (n_ops + BLOCK - 1) / BLOCK, nbw = (n_ops + GB_OPB - 1) / GB_OPB,
                  ntiles = raw_cap / GB_TILE;
     // two builds' done[8] at 0 / 128, n_raw at 32 / 160, count at 40 / 168, final at 44 / 172;
-    // a stroke build's st[] at 128, n_sraw at 160, done[] at 192
+    // a stroke build's st[] at 128, n_sraw at 160, done[] at 192, its probe's n_sraw at 256,
+    // done[] at 288, final at 320
     g.state = 0;
-    g.opa = 256;
+    g.opa = 512;
     g.opw = align256(g.opa + nbo * 16);
     g.opn = align256(g.opw + n_ops * 4);
     g.opi = align256(g.opn + nbw * 8);
@@ -268,7 +271,10 @@ cudaError_t launch_grid_build(const KParams& p, int sm_count, cudaStream_t s, co
 // state (st, n_sraw, done) must be zero before the launch, as p.gb's.  When the path has
 // more raw stroke points than p.gs.sraw_cap, or its outline more raw vertices than
 // p.gb.raw_cap, *n_sraw / *n_raw say how many and the figure is empty.
-cudaError_t launch_grid_stroke(const KParams& p, int sm_count, cudaStream_t s);
+// `probe` (nullable): the stroke points first over a prefix of the ops (its own n_sraw,
+// done and final_flag, the full build's skip): when the point cap is reached there the
+// points are complete and the full build's point kernels do nothing.
+cudaError_t launch_grid_stroke(const KParams& p, int sm_count, cudaStream_t s, const KParams* probe = nullptr);
 int composite_bands_smem(int band_rows, int width);
 int composite_build_blocks_per_sm(int smem_bytes, bool stroke);
 

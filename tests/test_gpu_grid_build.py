@@ -233,3 +233,24 @@ def test_stroke_outline_grows_raw_arrays(ctx):
     got, want, *_ = gpu_vs_oracle(ctx, ops_array(ops), 500, 500, stroke=True, join=_abi.JOIN_ROUND,
                                   tolerance=0.05)
     assert_same(got, want, "wide round joins")
+
+
+@pytest.mark.parametrize("lead", [14, 20, 21, 22])
+def test_stroke_point_cap_near_the_probe_boundary(ctx, lead):
+    """Long stroke paths collect their points first over their first 8,192 ops; when the
+    65,535-point cap is reached there the points are complete.  The quads of
+    test_cap_near_the_probe_boundary put the 65,536th point inside those ops for
+    lead <= 20 and after them from 21 on."""
+    ctx.tune(split_px=1, fig_build=2)
+    ops = [PathOp.Move(0.0, 30.0)]
+    ops += [PathOp.Line(0.125 + 0.0625 * k, 30.0 - 0.125 * k) for k in range(lead)]
+    x, y = 0.125 + 0.0625 * lead, 30.0
+    ops.append(PathOp.Line(x, y))
+    for k in range(20000):
+        h = 80.0 if k < 20 else 20.0
+        ops.append(PathOp.Quad(x + 0.125, y + h, x + 0.25, y))
+        x += 0.25
+    ops.append(PathOp.Close())
+    got, want, *_ = gpu_vs_oracle(ctx, ops_array(ops), 5010, 72, stroke=True, join=_abi.JOIN_BEVEL,
+                                  s_width=0.5)
+    assert_same(got, want, f"stroke lead {lead}")
