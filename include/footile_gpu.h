@@ -42,8 +42,8 @@ enum {
 /* Maximum De Casteljau / round-join arc recursion depth.  footile recurses without
  * a limit (README.md:32-33); deeper subdivisions are emitted as leaves and flagged. */
 #define FT_MAX_DEPTH 22
-/* Single fill paths of at least this many ops build their figure over the whole GPU
- * (ft_tuning.fig_build). */
+/* Single fill and stroke paths of at least this many ops build their figure over the
+ * whole GPU (ft_tuning.fig_build). */
 #define FT_GRID_BUILD_OPS 2048
 
 /* Vertices kept per figure, from `Vid(u16)` (src/vid.rs:9-18, src/fig.rs:428-442). */
@@ -209,9 +209,10 @@ FT_API void ft_batch_destroy(ft_batch* batch);
  * memory by TMA (when the canvas base and row stride are 16-byte aligned), 2 = read and
  * written in place, 0 = built-in; `pool_edges`, the first size of the binned-edge pool in edges (it
  * grows on demand; 0 = built-in); `fig_build`, who builds the figure of a single fill
- * path (ft_fill of at least split_px pixels, or an ft_composite_batch of one path):
- * 1 = one CTA, 2 = the whole GPU (scans over the path's ops and raw vertices), 0 =
- * built-in: the whole GPU from FT_GRID_BUILD_OPS ops.  Host batches (ft_fill_batch with
+ * or stroke path (ft_fill / ft_stroke of at least split_px pixels, or an
+ * ft_composite_batch of one path): 1 = one CTA, 2 = the whole GPU (scans over the path's
+ * ops, stroke points and raw vertices), 0 = built-in: the whole GPU from
+ * FT_GRID_BUILD_OPS ops.  Host batches (ft_fill_batch with
  * FT_HOST): `host_chunks`, chunks of the copy pipeline (1..16, 0 = built-in: 2 from
  * 64 MB of rasters); `host_mapped`, 0 = page-locked Matte8 rasters are written and
  * page-locked ops read in place (built-in), 1 = rasters and ops are copied, 2 = rasters
