@@ -1995,8 +1995,10 @@ __device__ void bin_edges(const KParams& P, uint32_t path, const CState& S, cons
     __syncthreads();
 }
 
+// Four CTAs per SM (56 registers for strokes, no spills; 101 unbounded, two CTAs): the
+// builds of an ordered composite are latency-bound chains of block scans.
 template <bool STROKE>
-__global__ void __launch_bounds__(BLOCK) k_cbuild(KParams P) {
+__global__ void __launch_bounds__(BLOCK, 4) k_cbuild(KParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ CState S;
     __shared__ int s_item;
