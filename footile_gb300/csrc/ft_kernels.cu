@@ -829,6 +829,7 @@ __device__ void build_outline(const KParams& P, CState& S, const float4* spts, c
         int n = 0, si = -1, u = 0, rsk = -1;  // rsk: index of this item's point that starts a figure run
         SubRec sr;
         int depth_hit = 0;
+        P2 c0 = p2(0.f, 0.f), c1 = p2(0.f, 0.f);  // the item's first two points, kept for the emit pass
         if (t < total_items) {
             // the last sub-stroke with item_off <= t owns item t (empty ones share the
             // next one's offset and come before it)
@@ -843,7 +844,10 @@ __device__ void build_outline(const KParams& P, CState& S, const float4* spts, c
             si = lo;
             sr = subs[si];
             u = t - sr.item_off;
-            n = outline_item(P, spts, sr, u, INT_MAX, INT_MAX, &depth_hit, [](int, P2) {});
+            n = outline_item(P, spts, sr, u, 0, INT_MAX, &depth_hit, [&](int k, P2 q) {
+                if (k == 0) c0 = q;
+                if (k == 1) c1 = q;
+            });
             // a figure run starts at each side's first point after a Close: the forward
             // side always (after the previous sub-stroke's Close, or first), the reverse
             // side when the sub-stroke is joined (stroker.rs:255-260)
@@ -860,13 +864,18 @@ __device__ void build_outline(const KParams& P, CState& S, const float4* spts, c
             const int w1 = min(w0 + RAW_CAP, total);
             if (n > 0 && off < w1 && off + n > w0) {
                 const int lo = max(w0, off) - off, hi = min(w1, off + n) - off;
-                int dh = 0;
-                outline_item(P, spts, sr, u, lo, hi, &dh, [&](int k, P2 q) {
+                auto put = [&](int k, P2 q) {
                     const int idx = off + k - w0;
                     const P2 tq = xform(P.xf, q);  // the outline is transformed again (F9)
                     B.raw[idx] = make_int2(f2fx(tq.x), f2fx(tq.y));
                     B.rs[idx] = (k == rsk) ? (unsigned char)1 : (unsigned char)0;
-                });
+                };
+                if (n <= 2) {  // an end, a miter or a bevel: the points of the count pass
+                    for (int k = lo; k < hi; k++) put(k, k == 0 ? c0 : c1);
+                } else {
+                    int dh = 0;
+                    outline_item(P, spts, sr, u, lo, hi, &dh, put);
+                }
             }
             __syncthreads();
             compact_window_block(S, B.raw, B.rs, w1 - w0, pts, ss, Cs);
