@@ -1,6 +1,7 @@
 """The bounds-check build (-DFT_CHECK=1): the library compiled with device index checks
 runs small cases of every kernel family — glyph batches (warp and CTA rasterisers), a
-single large fill and stroke (mask compositor), ordered stroke and fill composites (tile
+single large fill and stroke (figure built by one CTA and by the whole GPU, mask
+compositor), ordered stroke and fill composites (tile
 compositor, every tile width), Matte8 composites — with no failed check and the oracle's
 bytes.  It stands in for a memory checker, which this project does not run."""
 import os
@@ -38,11 +39,14 @@ CASES = textwrap.dedent("""
     ctx.set_tuning(None)
     rng = np.random.default_rng(3)
     ops = workloads.random_path(rng, 1200, 200, n_sub=2)
-    for stroke in (False, True):
-        init = rng.integers(0, 256, (1000, 1200, 4)).astype(np.uint8)
-        got, want, *_ = gpu_vs_oracle(ctx, ops, 1200, 1000, fmt=_abi.RGBA8P, clr=(20, 40, 60, 200), init=init,
-                                      stroke=stroke)
-        assert np.array_equal(got, want), "large call"
+    for fig_build in (1, 2):  # the figure (and a stroke's points and outline) on one CTA, on the whole GPU
+        ctx.tune(fig_build=fig_build)
+        for stroke in (False, True):
+            init = rng.integers(0, 256, (1000, 1200, 4)).astype(np.uint8)
+            got, want, *_ = gpu_vs_oracle(ctx, ops, 1200, 1000, fmt=_abi.RGBA8P, clr=(20, 40, 60, 200), init=init,
+                                          stroke=stroke)
+            assert np.array_equal(got, want), "large call"
+    ctx.set_tuning(None)
     paths_ops, _, clrs, side = workloads.strokes_16384(n_paths=64, side=700)
     o, p, _ = pack_batch(paths_ops, [side] * 64, _abi.RGBA8P, clrs)
     for tw in (128, 256, 512, 1024):
