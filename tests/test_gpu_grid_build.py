@@ -254,3 +254,30 @@ def test_stroke_point_cap_near_the_probe_boundary(ctx, lead):
     got, want, *_ = gpu_vs_oracle(ctx, ops_array(ops), 5010, 72, stroke=True, join=_abi.JOIN_BEVEL,
                                   s_width=0.5)
     assert_same(got, want, f"stroke lead {lead}")
+
+
+@pytest.mark.parametrize("stroke", [False, True])
+def test_composite_batch_of_one_offset_path(ctx, stroke):
+    """ft_composite_batch of one path whose ops start after 500 ops of another path: the
+    grid-wide build reads the path's ops from its op_begin; the canvas starts random."""
+    from footile_gb300.plotter import composite_batch
+    ctx.tune(fig_build=2)
+    rng = np.random.default_rng(31)
+    junk = workloads.random_path(rng, 300, 500, n_sub=1)
+    path = workloads.random_path(rng, 300, 700, n_sub=9, close=not stroke)
+    if stroke:
+        path = np.concatenate([ops_array([PathOp.PenWidth(3.5)]), path])
+    ops = np.concatenate([junk, path])
+    paths = np.zeros(1, dtype=_abi.PATH_DTYPE)
+    paths[0]["op_begin"] = len(junk)
+    paths[0]["n_ops"] = len(path)
+    paths[0]["width"] = 320
+    paths[0]["height"] = 300
+    paths[0]["clr"] = (90, 30, 160, 200)
+    init = rng.integers(0, 256, (300, 320, 4)).astype(np.uint8)
+    want = init.copy()
+    oracle.composite(int(stroke), _abi.EVENODD, ops, paths, _abi.RGBA8P, want, s_width=1.0)
+    got = init.copy()
+    ctx.set_pen_width(1.0)
+    composite_batch(ctx, ops, paths, _abi.RGBA8P, got, rule=_abi.EVENODD, stroke=stroke)
+    assert_same(got, want, f"one offset path, stroke {stroke}")
