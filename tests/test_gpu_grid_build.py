@@ -281,3 +281,17 @@ def test_composite_batch_of_one_offset_path(ctx, stroke):
     ctx.set_pen_width(1.0)
     composite_batch(ctx, ops, paths, _abi.RGBA8P, got, rule=_abi.EVENODD, stroke=stroke)
     assert_same(got, want, f"one offset path, stroke {stroke}")
+
+
+@pytest.mark.parametrize("stroke,join", [(False, None), (True, _abi.JOIN_MITER), (True, _abi.JOIN_ROUND)])
+def test_built_in_route_large_paths(ctx, stroke, join):
+    """No tuning: a path of more than FT_GRID_BUILD_OPS ops on a 1024x1024 canvas takes the
+    grid-wide build by default (with its probe), against the oracle."""
+    rng = np.random.default_rng(41 + int(stroke))
+    ops = workloads.random_path(rng, 1024, 300, n_sub=10, close=not stroke)
+    assert len(ops) > 2048
+    kw = dict(stroke=True, join=join, s_width=2.5) if stroke else dict(rule=_abi.NONZERO)
+    got, want, st, sw, err = gpu_vs_oracle(ctx, ops, 1024, 1024, fmt=_abi.RGBA8P, clr=(10, 200, 120, 180),
+                                           init=5, **kw)
+    assert_same(got, want, f"built-in route, stroke {stroke}")
+    assert (err.code if err else 0) == st
