@@ -2782,11 +2782,29 @@ __device__ __forceinline__ FigBins fig_bins(const KParams& P) {
 }
 
 // Bands counted in shared memory by each CTA of the edge binning (one global atomic per
-// CTA and band instead of one per edge and band); more bands count in global memory.
+// CTA and band instead of one per edge and band); more bands count in global memory.  In
+// shared memory an edge adds +1 at its first band and -1 after its last (a difference
+// array, two atomics per edge), and a prefix sum gives the counts.
 constexpr int BIN_SMEM_BANDS = 8192;
 
+// Counts of this CTA's edges per band: sh[0 .. nb] difference array -> counts in sh[0 .. nb).
+__device__ void fig_bin_prefix(int* sh, int nb, int* tmp) {
+    __syncthreads();
+    int carry = 0;
+    for (int b0 = 0; b0 < nb; b0 += BLOCK) {
+        const int b = b0 + threadIdx.x;
+        int tot;
+        const int v = b < nb ? sh[b] : 0;
+        const int ex = block_excl_sum(v, tmp, tot);
+        if (b < nb) sh[b] = carry + ex + v;
+        carry += tot;
+    }
+    __syncthreads();
+}
+
 __global__ void __launch_bounds__(BLOCK) k_fig_edges(KParams P) {
-    extern __shared__ int sh_bins[];  // n_bands counts (when n_bands <= BIN_SMEM_BANDS)
+    extern __shared__ int sh_bins[];  // n_bands + 1 differences (when n_bands <= BIN_SMEM_BANDS)
+    __shared__ int tmp[2 * NWARP + 2];
     const FigBins f = fig_bins(P);
     const bool local = f.nb <= BIN_SMEM_BANDS;
     const unsigned char* scr = P.scratch;
@@ -2794,19 +2812,24 @@ __global__ void __launch_bounds__(BLOCK) k_fig_edges(KParams P) {
     const int* ss = reinterpret_cast<const int*>(scr + P.L.ss);
     EdgeRec* edges = reinterpret_cast<EdgeRec*>(P.scratch + P.L.edges);
     if (local) {
-        for (int b = threadIdx.x; b < f.nb; b += BLOCK) sh_bins[b] = 0;
+        for (int b = threadIdx.x; b <= f.nb; b += BLOCK) sh_bins[b] = 0;
         __syncthreads();
     }
-    int* hist = local ? sh_bins : P.bin_hist;
     for (int e = blockIdx.x * BLOCK + threadIdx.x; e < f.count; e += gridDim.x * BLOCK) {
         const EdgeRec E = edge_rec(e, f.count, f.figdir, pts, ss);
         edges[e] = E;
         if (!E.ed) continue;
         const int lo = max(E.start_row - f.tmin, f.rb), hi = min(E.end_row - f.tmin, f.H - 1);
-        for (int b = lo / f.R; lo <= hi && b <= hi / f.R; b++) atomicAdd(&hist[b], 1);
+        if (lo > hi) continue;
+        if (local) {
+            atomicAdd(&sh_bins[lo / f.R], 1);
+            atomicAdd(&sh_bins[hi / f.R + 1], -1);
+        } else {
+            for (int b = lo / f.R; b <= hi / f.R; b++) atomicAdd(&P.bin_hist[b], 1);
+        }
     }
     if (local) {
-        __syncthreads();
+        fig_bin_prefix(sh_bins, f.nb, tmp);
         for (int b = threadIdx.x; b < f.nb; b += BLOCK)
             if (sh_bins[b]) atomicAdd(&P.bin_hist[b], sh_bins[b]);
     }
@@ -2837,8 +2860,19 @@ __global__ void __launch_bounds__(BLOCK) k_fig_bin_scan(KParams P) {
     }
 }
 
+// (edge, band) pairs of 256 edges at a time spread over the CTA (run-length item map):
+// an edge spanning many bands no longer holds one thread for all of them.
+struct BinStage {
+    int4 q[2 * BLOCK];  // the edges' two halves
+    int b0[BLOCK];      // first band
+    int off[BLOCK];
+    int scan[2 * NWARP + 2];
+    unsigned char map[MAP_CAP];
+};
+
 __global__ void __launch_bounds__(BLOCK) k_fig_bin_fill(KParams P) {
-    extern __shared__ int sh_bins[];  // n_bands counts, then n_bands cursors (n_bands <= BIN_SMEM_BANDS)
+    // n_bands + 1 counts, then n_bands cursors (n_bands <= BIN_SMEM_BANDS), then the stage
+    extern __shared__ __align__(16) int sh_bins[];
     const FigBins f = fig_bins(P);
     if (!P.fig_state[0].w) return;
     const bool local = f.nb <= BIN_SMEM_BANDS;
@@ -2846,42 +2880,91 @@ __global__ void __launch_bounds__(BLOCK) k_fig_bin_fill(KParams P) {
     const unsigned long long base = (unsigned long long)(unsigned)cr.z | ((unsigned long long)(unsigned)cr.w << 32);
     const int4* erec = reinterpret_cast<const int4*>(P.scratch + P.L.edges);
     int* cursor = P.bin_hist + f.nb;
-    if (local) {
-        // this CTA's edges per band, then one run of slots per band taken from the cursors
-        for (int b = threadIdx.x; b < f.nb; b += BLOCK) sh_bins[b] = 0;
-        __syncthreads();
+    auto rows_of = [&](const int4& q1, int& lo, int& hi) {
+        lo = max(q1.z - f.tmin, f.rb);
+        hi = min(q1.w - f.tmin, f.H - 1);
+        return q1.y != 0 && lo <= hi;
+    };
+    if (!local) {
         for (int e = blockIdx.x * BLOCK + threadIdx.x; e < f.count; e += gridDim.x * BLOCK) {
-            const int4 q1 = erec[2 * e + 1];
-            if (!q1.y) continue;
-            const int lo = max(q1.z - f.tmin, f.rb), hi = min(q1.w - f.tmin, f.H - 1);
-            for (int b = lo / f.R; lo <= hi && b <= hi / f.R; b++) atomicAdd(&sh_bins[b], 1);
+            const int4 q1 = erec[2 * e + 1];  // step_pix, ed, start_row, end_row
+            int lo, hi;
+            if (!rows_of(q1, lo, hi)) continue;
+            const int4 q0 = erec[2 * e];
+            for (int b = lo / f.R; b <= hi / f.R; b++) {
+                const unsigned long long k = base + (unsigned)atomicAdd(&cursor[b], 1);
+                if (!ck(k < P.pool_cap, 12)) continue;
+                int4* dst = reinterpret_cast<int4*>(P.pool + k);
+                dst[0] = q0;
+                dst[1] = q1;
+            }
         }
-        __syncthreads();
-        for (int b = threadIdx.x; b < f.nb; b += BLOCK)
-            sh_bins[f.nb + b] = sh_bins[b] ? atomicAdd(&cursor[b], sh_bins[b]) : 0;
-        __syncthreads();
-        cursor = sh_bins + f.nb;
+        return;
     }
+    const int stage_at = (2 * f.nb + 1 + 3) & ~3;  // ints, 16-byte aligned
+    BinStage& Bs = *reinterpret_cast<BinStage*>(sh_bins + stage_at);
+    // this CTA's edges per band, then one run of slots per band taken from the cursors
+    for (int b = threadIdx.x; b <= f.nb; b += BLOCK) sh_bins[b] = 0;
+    __syncthreads();
     for (int e = blockIdx.x * BLOCK + threadIdx.x; e < f.count; e += gridDim.x * BLOCK) {
-        const int4 q1 = erec[2 * e + 1];  // step_pix, ed, start_row, end_row
-        if (!q1.y) continue;
-        const int4 q0 = erec[2 * e];
-        const int lo = max(q1.z - f.tmin, f.rb), hi = min(q1.w - f.tmin, f.H - 1);
-        for (int b = lo / f.R; lo <= hi && b <= hi / f.R; b++) {
-            const unsigned long long k = base + (unsigned)atomicAdd(&cursor[b], 1);
-            if (!ck(k < P.pool_cap, 12)) continue;
-            int4* dst = reinterpret_cast<int4*>(P.pool + k);
-            dst[0] = q0;
-            dst[1] = q1;
+        int lo, hi;
+        if (!rows_of(erec[2 * e + 1], lo, hi)) continue;
+        atomicAdd(&sh_bins[lo / f.R], 1);
+        atomicAdd(&sh_bins[hi / f.R + 1], -1);
+    }
+    fig_bin_prefix(sh_bins, f.nb, Bs.scan);
+    for (int b = threadIdx.x; b < f.nb; b += BLOCK)
+        sh_bins[f.nb + 1 + b] = sh_bins[b] ? atomicAdd(&cursor[b], sh_bins[b]) : 0;
+    __syncthreads();
+    int* lcur = sh_bins + f.nb + 1;
+    for (int e0 = blockIdx.x * BLOCK; e0 < f.count; e0 += gridDim.x * BLOCK) {
+        const int e = e0 + threadIdx.x;
+        int n = 0, b0 = 0;
+        int4 q0 = make_int4(0, 0, 0, 0), q1 = q0;
+        if (e < f.count) {
+            q1 = erec[2 * e + 1];
+            int lo, hi;
+            if (rows_of(q1, lo, hi)) {
+                q0 = erec[2 * e];
+                b0 = lo / f.R;
+                n = hi / f.R - b0 + 1;
+            }
+        }
+        Bs.q[2 * threadIdx.x] = q0;
+        Bs.q[2 * threadIdx.x + 1] = q1;
+        Bs.b0[threadIdx.x] = b0;
+        int tot;
+        const int o = block_excl_sum(n, Bs.scan, tot);
+        Bs.off[threadIdx.x] = o;
+        for (int m0 = 0; m0 < tot; m0 += MAP_CAP) {
+            const int ia = max(o, m0), ib = min(o + n, m0 + MAP_CAP);
+            for (int k = ia; k < ib; k++) Bs.map[k - m0] = (unsigned char)threadIdx.x;
+            __syncthreads();
+            const int nm = min(MAP_CAP, tot - m0);
+            for (int it = threadIdx.x; it < nm; it += BLOCK) {
+                const int jj = Bs.map[it];
+                const int b = Bs.b0[jj] + (m0 + it - Bs.off[jj]);
+                if (!ck(b >= 0 && b < f.nb, 12)) continue;
+                const unsigned long long k = base + (unsigned)atomicAdd(&lcur[b], 1);
+                if (!ck(k < P.pool_cap, 12)) continue;
+                int4* dst = reinterpret_cast<int4*>(P.pool + k);
+                dst[0] = Bs.q[2 * jj];
+                dst[1] = Bs.q[2 * jj + 1];
+            }
+            __syncthreads();
         }
     }
 }
 
 cudaError_t launch_figure_bins(const KParams& p, int grid, cudaStream_t s) {
     const bool local = p.n_bands <= BIN_SMEM_BANDS;
-    const int sm_e = local ? p.n_bands * (int)sizeof(int) : 0, sm_f = 2 * sm_e;
+    const int sm_e = local ? (p.n_bands + 1) * (int)sizeof(int) : 0;
+    const int sm_f = local ? ((2 * p.n_bands + 1 + 3) & ~3) * (int)sizeof(int) + (int)sizeof(BinStage) : 0;
     cudaError_t e = cudaFuncSetAttribute(k_fig_bin_fill, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         2 * BIN_SMEM_BANDS * (int)sizeof(int));
+                                         ((2 * BIN_SMEM_BANDS + 1 + 3) & ~3) * (int)sizeof(int) + (int)sizeof(BinStage));
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_fig_edges, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (BIN_SMEM_BANDS + 1) * (int)sizeof(int));
     if (e != cudaSuccess) return e;
     k_fig_edges<<<grid, BLOCK, sm_e, s>>>(p);
     e = cudaGetLastError();
