@@ -94,3 +94,44 @@ def test_noalloc_rejects_too_wide(gpu_lib):
     rc = fill(_abi.NONZERO, None, 0, _abi.MATTE8, None, ctypes.c_void_p(16), _abi.MAX_WIDTH + 1, 1,
               _abi.MAX_WIDTH + 1, None, 0.3, 1.0, None, None)
     assert rc == _abi.ERR_CAP
+
+
+def test_noalloc_in_a_captured_graph(cuda_ok, gpu_lib):
+    """The use the declaration describes: one call made eagerly first (the per-device
+    setup), then a call recorded into a CUDA graph during stream capture, replayed onto a
+    fresh raster: bit for bit the context fill's raster."""
+    torch = pytest.importorskip("torch")
+    fill = _noalloc(gpu_lib)
+    rng = np.random.default_rng(5)
+    clr = (200, 10, 70, 255)
+    c = (ctypes.c_uint8 * 4)(*clr)
+    s = torch.cuda.Stream()
+    warm_ops = torch.from_numpy(workloads.random_path(rng, 64, 20).view(np.uint8)).cuda()
+    warm_ras = torch.zeros((64, 64), dtype=torch.uint8, device="cuda")
+    rc = fill(_abi.NONZERO, ctypes.c_void_p(warm_ops.data_ptr()), warm_ops.numel() // 32, _abi.MATTE8, c,
+              ctypes.c_void_p(warm_ras.data_ptr()), 64, 64, 64, None, 0.3, 1.0, None, ctypes.c_void_p(s.cuda_stream))
+    assert rc == _abi.OK
+    torch.cuda.synchronize()
+    ops = workloads.random_path(rng, 240, 80, n_sub=3)
+    ops_d = torch.from_numpy(ops.view(np.uint8)).cuda()
+    ras_d = torch.full((240, 240), 9, dtype=torch.uint8, device="cuda")
+    st_d = torch.full((1,), -1, dtype=torch.int32, device="cuda")
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        rc = fill(_abi.EVENODD, ctypes.c_void_p(ops_d.data_ptr()), len(ops), _abi.MATTE8, c,
+                  ctypes.c_void_p(ras_d.data_ptr()), 240, 240, 240, None, 0.3, 1.0,
+                  ctypes.c_void_p(st_d.data_ptr()), ctypes.c_void_p(s.cuda_stream))
+    assert rc == _abi.OK
+    ras_d.fill_(9)
+    torch.cuda.synchronize()
+    g.replay()
+    torch.cuda.synchronize()
+    assert int(st_d.item()) == _abi.OK
+    ctx = _lib.Context(0)
+    want = np.full((240, 240), 9, np.uint8)
+    ctx.set_pen_width(1.0)
+    Plotter(want, context=ctx).fill(_abi.EVENODD, ops, clr)
+    ctx.close()
+    got = ras_d.cpu().numpy()
+    bad = np.argwhere(got != want)
+    assert len(bad) == 0, f"{len(bad)} bytes differ from ft_fill"
