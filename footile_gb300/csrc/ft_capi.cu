@@ -1183,8 +1183,8 @@ static int composite_impl(ft_ctx* c, int32_t stroke, int32_t rule, const ft_op* 
             }
             // a probe over the first ops: a capped figure usually reaches its cap there, and
             // the build over all ops is then skipped
-            const int probe_ops = std::max(4096, p.pt_cap / 8);
-            use_probe = (int)paths[0].n_ops > 2 * probe_ops;
+            const int probe_ops = std::max(2048, p.pt_cap / 32);
+            use_probe = (int)paths[0].n_ops > 8 * probe_ops;
             if (use_probe && stroke) {
                 // the stroke points over the first ops: the 65,535-point cap is usually reached there
                 pp = p;

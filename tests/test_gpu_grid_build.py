@@ -132,90 +132,34 @@ def test_raw_arrays_grow(ctx):
     assert_same(got, want, "long cubics")
 
 
-@pytest.mark.parametrize("lead", [14, 17, 19, 20, 21, 22, 24])
-def test_cap_near_the_probe_boundary(ctx, lead):
-    """Long paths are built first over their first 8,192 ops; when the cap is reached
-    there, the build over all ops is skipped.  After `lead` lines come 20 quads of 16
-    leaves and quads of 8 leaves, every vertex distinct: the first 8,192 ops hold
-    65,682 - 7 * lead raw vertices, so the 65,535th vertex falls inside them for
-    lead <= 20, on their last vertex for lead 21, and after them beyond."""
-    ctx.tune(split_px=1, fig_build=2)
-    ops = [PathOp.Move(0.0, 30.0)]
-    ops += [PathOp.Line(0.125 + 0.0625 * k, 30.0 - 0.125 * k) for k in range(lead)]
-    x, y = 0.125 + 0.0625 * lead, 30.0
+def probe_boundary_ops(lead, big, n_quads=20000):
+    """Lines and quads whose every raw vertex is distinct: after `lead` lines, `big` quads of
+    64 leaves, then quads of 32.  The first 2,048 ops (the probe of a long path) hold
+    65,474 - 31 * lead + 32 * big raw vertices."""
+    ops = [PathOp.Move(0.0, 700.0)]
+    ops += [PathOp.Line(0.125 + 0.0625 * k, 700.0 - 0.125 * k) for k in range(lead)]
+    x, y = 0.125 + 0.0625 * lead, 700.0
     ops.append(PathOp.Line(x, y))
-    for k in range(20000):
-        h = 80.0 if k < 20 else 20.0
-        ops.append(PathOp.Quad(x + 0.125, y + h, x + 0.25, y))
+    for k in range(n_quads):
+        h = 1280.0 if k < big else 320.0
+        ops.append(PathOp.Quad(x + 0.125, y - h, x + 0.25, y))
         x += 0.25
-    ops = ops_array(ops)
-    got, want, *_ = gpu_vs_oracle(ctx, ops, 5010, 72, rule=_abi.EVENODD)
-    assert_same(got, want, f"lead {lead}")
+    return ops
 
 
-# ---- strokes: the stroker's points, sub-strokes and outline built by the whole GPU
-
-def random_stroke_ops(rng, n_ops, side, grid=None):
-    """Moves, lines, quads, cubics, closes and pen widths; with `grid`, points on a coarse
-    grid so that coincident stroke points and one-point sub-strokes occur."""
-    ops = []
-    for _ in range(n_ops):
-        u = rng.random()
-        pt = (lambda: (float(rng.integers(0, grid)) * side / grid, float(rng.integers(0, grid)) * side / grid)) \
-            if grid else (lambda: tuple(float(v) for v in rng.random(2) * side))
-        if u < 0.1 or not ops:
-            ops.append(PathOp.Move(*pt()))
-        elif u < 0.18:
-            ops.append(PathOp.Close())
-        elif u < 0.22:
-            ops.append(PathOp.PenWidth(float(rng.uniform(0.5, 9.0))))
-        elif u < 0.55:
-            ops.append(PathOp.Line(*pt()))
-        elif u < 0.8:
-            ops.append(PathOp.Quad(*pt(), *pt()))
-        else:
-            ops.append(PathOp.Cubic(*pt(), *pt(), *pt()))
-    return ops_array(ops)
+# (lead, big): the probe's raw vertices 65,804 / 65,556 (the cap inside), 65,525 (after it),
+# 65,503, 65,535 (its last vertex: the cap just after it) and 65,567
+PROBE_CASES = [(10, 20), (18, 20), (19, 20), (29, 29), (29, 30), (29, 31)]
 
 
-@pytest.mark.parametrize("join", [_abi.JOIN_MITER, _abi.JOIN_BEVEL, _abi.JOIN_ROUND])
-@pytest.mark.parametrize("seed", range(4))
-def test_random_strokes(ctx, build, join, seed):
-    rng = np.random.default_rng(300 + seed)
-    ops = random_stroke_ops(rng, int(rng.integers(5, 600)), 200.0, grid=(6 if seed % 2 else None))
-    xf = (1.25, 0.125, 5.0, -0.25, 0.75, 9.0) if seed == 2 else _abi.IDENTITY
-    fmt = _abi.RGBA8P if seed % 2 else _abi.MATTE8
-    got, want, st, sw, err = gpu_vs_oracle(ctx, ops, 256, 230, fmt=fmt, clr=(40, 90, 200, 230), init=11,
-                                           stroke=True, join=join, miter_limit=(4.0, 1.5, 10.0, 2.0)[seed],
-                                           s_width=(1.0, 3.5, 6.0, 0.75)[seed], transform=xf,
-                                           tolerance=(0.3, 0.1, 0.5, 1.0)[seed])
-    assert_same(got, want, f"stroke {join} {seed}")
-    assert (err.code if err else 0) == st
-    assert ctx.pen_width() == sw
-
-
-@pytest.mark.parametrize("tail", ["close", "move", "line", "closes_after"])
-@pytest.mark.parametrize("extra", [-1, 0, 2])
-def test_stroke_point_cap(ctx, build, tail, extra):
-    """More stroke points than 65,535: points from the cap on are dropped, and the last
-    sub-stroke's joined flag comes from the close events after its last kept point."""
-    n = _abi.MAX_POINTS + extra
-    k = np.arange(n)
-    ops = np.zeros(n + 4, dtype=_abi.OP_DTYPE)
-    ops["kind"][0] = _abi.OP_MOVE
-    ops["kind"][1:n] = _abi.OP_LINE
-    ops["v"][:n, 0] = ((k * 7919) % 200).astype(np.float32) * np.float32(0.5) + np.float32(8)
-    ops["v"][:n, 1] = ((k * 104729) % 180).astype(np.float32) * np.float32(0.5) + np.float32(8)
-    t = ops_array({
-        "close": [PathOp.Close(), PathOp.Line(30.0, 30.0)],
-        "move": [PathOp.Move(5.0, 5.0), PathOp.Line(40.0, 9.0)],
-        "line": [PathOp.Line(3.0, 7.0), PathOp.Line(50.0, 70.0)],
-        "closes_after": [PathOp.Line(60.0, 20.0), PathOp.Move(1.0, 1.0), PathOp.Close()],
-    }[tail])
-    ops[n:n + len(t)] = t
-    ops = ops[:n + len(t)]
-    got, want, *_ = gpu_vs_oracle(ctx, ops, 116, 106, stroke=True, join=_abi.JOIN_ROUND, s_width=0.8)
-    assert_same(got, want, f"stroke cap {tail} {extra}")
+@pytest.mark.parametrize("lead,big", PROBE_CASES)
+def test_cap_near_the_probe_boundary(ctx, lead, big):
+    """Long paths are built first over their first 2,048 ops; when the cap is reached
+    there, the build over all ops is skipped."""
+    ctx.tune(split_px=1, fig_build=2)
+    ops = ops_array(probe_boundary_ops(lead, big))
+    got, want, *_ = gpu_vs_oracle(ctx, ops, 5010, 720, rule=_abi.EVENODD)
+    assert_same(got, want, f"lead {lead} big {big}")
 
 
 def test_stroke_outline_grows_raw_arrays(ctx):
@@ -235,25 +179,15 @@ def test_stroke_outline_grows_raw_arrays(ctx):
     assert_same(got, want, "wide round joins")
 
 
-@pytest.mark.parametrize("lead", [14, 20, 21, 22])
-def test_stroke_point_cap_near_the_probe_boundary(ctx, lead):
-    """Long stroke paths collect their points first over their first 8,192 ops; when the
-    65,535-point cap is reached there the points are complete.  The quads of
-    test_cap_near_the_probe_boundary put the 65,536th point inside those ops for
-    lead <= 20 and after them from 21 on."""
+@pytest.mark.parametrize("lead,big", PROBE_CASES)
+def test_stroke_point_cap_near_the_probe_boundary(ctx, lead, big):
+    """Long stroke paths collect their points first over their first 2,048 ops; when the
+    65,535-point cap is reached there the points are complete."""
     ctx.tune(split_px=1, fig_build=2)
-    ops = [PathOp.Move(0.0, 30.0)]
-    ops += [PathOp.Line(0.125 + 0.0625 * k, 30.0 - 0.125 * k) for k in range(lead)]
-    x, y = 0.125 + 0.0625 * lead, 30.0
-    ops.append(PathOp.Line(x, y))
-    for k in range(20000):
-        h = 80.0 if k < 20 else 20.0
-        ops.append(PathOp.Quad(x + 0.125, y + h, x + 0.25, y))
-        x += 0.25
-    ops.append(PathOp.Close())
-    got, want, *_ = gpu_vs_oracle(ctx, ops_array(ops), 5010, 72, stroke=True, join=_abi.JOIN_BEVEL,
+    ops = probe_boundary_ops(lead, big) + [PathOp.Close()]
+    got, want, *_ = gpu_vs_oracle(ctx, ops_array(ops), 5010, 720, stroke=True, join=_abi.JOIN_BEVEL,
                                   s_width=0.5)
-    assert_same(got, want, f"stroke lead {lead}")
+    assert_same(got, want, f"stroke lead {lead} big {big}")
 
 
 @pytest.mark.parametrize("stroke", [False, True])
