@@ -229,3 +229,16 @@ def test_built_in_route_large_paths(ctx, stroke, join):
                                            init=5, **kw)
     assert_same(got, want, f"built-in route, stroke {stroke}")
     assert (err.code if err else 0) == st
+
+
+def test_stroke_points_grow_raw_arrays(ctx):
+    """8,000 long cubics at tolerance 0.01: over a million raw stroke points, more than the
+    arrays first hold (64 per op, at least 2^20); the build grows them and runs again."""
+    ctx.tune(split_px=1, fig_build=2)
+    rng = np.random.default_rng(19)
+    ops = [PathOp.Move(10.0, 10.0)]
+    for _ in range(8000):
+        ops.append(PathOp.Cubic(*(rng.random(6) * 990 + 5).astype(np.float32).tolist()))
+    got, want, *_ = gpu_vs_oracle(ctx, ops_array(ops), 1000, 1000, stroke=True, join=_abi.JOIN_MITER,
+                                  tolerance=0.01, s_width=1.5)
+    assert_same(got, want, "many stroke points")
