@@ -162,6 +162,71 @@ def test_cap_near_the_probe_boundary(ctx, lead, big):
     assert_same(got, want, f"lead {lead} big {big}")
 
 
+# ---- strokes: the stroker's points, sub-strokes and outline built by the whole GPU
+
+def random_stroke_ops(rng, n_ops, side, grid=None):
+    """Moves, lines, quads, cubics, closes and pen widths; with `grid`, points on a coarse
+    grid so that coincident stroke points and one-point sub-strokes occur."""
+    ops = []
+    for _ in range(n_ops):
+        u = rng.random()
+        pt = (lambda: (float(rng.integers(0, grid)) * side / grid, float(rng.integers(0, grid)) * side / grid)) \
+            if grid else (lambda: tuple(float(v) for v in rng.random(2) * side))
+        if u < 0.1 or not ops:
+            ops.append(PathOp.Move(*pt()))
+        elif u < 0.18:
+            ops.append(PathOp.Close())
+        elif u < 0.22:
+            ops.append(PathOp.PenWidth(float(rng.uniform(0.5, 9.0))))
+        elif u < 0.55:
+            ops.append(PathOp.Line(*pt()))
+        elif u < 0.8:
+            ops.append(PathOp.Quad(*pt(), *pt()))
+        else:
+            ops.append(PathOp.Cubic(*pt(), *pt(), *pt()))
+    return ops_array(ops)
+
+
+@pytest.mark.parametrize("join", [_abi.JOIN_MITER, _abi.JOIN_BEVEL, _abi.JOIN_ROUND])
+@pytest.mark.parametrize("seed", range(4))
+def test_random_strokes(ctx, build, join, seed):
+    rng = np.random.default_rng(300 + seed)
+    ops = random_stroke_ops(rng, int(rng.integers(5, 600)), 200.0, grid=(6 if seed % 2 else None))
+    xf = (1.25, 0.125, 5.0, -0.25, 0.75, 9.0) if seed == 2 else _abi.IDENTITY
+    fmt = _abi.RGBA8P if seed % 2 else _abi.MATTE8
+    got, want, st, sw, err = gpu_vs_oracle(ctx, ops, 256, 230, fmt=fmt, clr=(40, 90, 200, 230), init=11,
+                                           stroke=True, join=join, miter_limit=(4.0, 1.5, 10.0, 2.0)[seed],
+                                           s_width=(1.0, 3.5, 6.0, 0.75)[seed], transform=xf,
+                                           tolerance=(0.3, 0.1, 0.5, 1.0)[seed])
+    assert_same(got, want, f"stroke {join} {seed}")
+    assert (err.code if err else 0) == st
+    assert ctx.pen_width() == sw
+
+
+@pytest.mark.parametrize("tail", ["close", "move", "line", "closes_after"])
+@pytest.mark.parametrize("extra", [-1, 0, 2])
+def test_stroke_point_cap(ctx, build, tail, extra):
+    """More stroke points than 65,535: points from the cap on are dropped, and the last
+    sub-stroke's joined flag comes from the close events after its last kept point."""
+    n = _abi.MAX_POINTS + extra
+    k = np.arange(n)
+    ops = np.zeros(n + 4, dtype=_abi.OP_DTYPE)
+    ops["kind"][0] = _abi.OP_MOVE
+    ops["kind"][1:n] = _abi.OP_LINE
+    ops["v"][:n, 0] = ((k * 7919) % 200).astype(np.float32) * np.float32(0.5) + np.float32(8)
+    ops["v"][:n, 1] = ((k * 104729) % 180).astype(np.float32) * np.float32(0.5) + np.float32(8)
+    t = ops_array({
+        "close": [PathOp.Close(), PathOp.Line(30.0, 30.0)],
+        "move": [PathOp.Move(5.0, 5.0), PathOp.Line(40.0, 9.0)],
+        "line": [PathOp.Line(3.0, 7.0), PathOp.Line(50.0, 70.0)],
+        "closes_after": [PathOp.Line(60.0, 20.0), PathOp.Move(1.0, 1.0), PathOp.Close()],
+    }[tail])
+    ops[n:n + len(t)] = t
+    ops = ops[:n + len(t)]
+    got, want, *_ = gpu_vs_oracle(ctx, ops, 116, 106, stroke=True, join=_abi.JOIN_ROUND, s_width=0.8)
+    assert_same(got, want, f"stroke cap {tail} {extra}")
+
+
 def test_stroke_outline_grows_raw_arrays(ctx):
     """A small stroke sizes the arrays; then wide round joins on 70,000 short segments give
     an outline of far more raw vertices than that, and the build grows its arrays and
