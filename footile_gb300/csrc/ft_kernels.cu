@@ -1195,7 +1195,7 @@ __device__ void build_fill(const KParams& P, const ft_path_desc& d, float sw0, B
                     }
                 }
                 G::sync();
-                if (STROKE) {
+                if constexpr (STROKE) {
                     compact_stroke_block(S, reinterpret_cast<const float4*>(B.raw), B.rs, B.rs + SRAW, opi, w1 - w0,
                                          spts, subs, *Cs);
                 } else if (N == 32) {
@@ -2143,7 +2143,7 @@ __global__ void __launch_bounds__(BLOCK) k_cbands(KParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int W = (int)P.canvas_w, H = (int)P.canvas_h, Wp = (W + 3) & ~3;
-    const int R = P.band_rows, nb = P.n_bands, b = blockIdx.x;
+    const int R = P.band_rows, b = blockIdx.x;
     const int r = b * R + warp;  // this warp's raster row
     const bool whole = P.n_items == 1 && R == NWARP && blockDim.x == BLOCK;
     if (!whole && (warp >= R || r >= H)) return;
@@ -2369,9 +2369,10 @@ __device__ __forceinline__ unsigned warp_sum_u(unsigned v) {
 
 template <bool STAGED>
 __global__ void __launch_bounds__(BLOCK, 4) k_ctile(KParams P, const __grid_constant__ CUtensorMap tmap) {
-    extern __shared__ __align__(128) unsigned char smem[];
+    extern __shared__ __align__(128) unsigned char smem_tma[];  // TMA destinations: 128-byte aligned
+    unsigned char* smem = smem_tma;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int W = (int)P.canvas_w, H = (int)P.canvas_h, R = P.band_rows, nb = P.n_bands, sw = P.seg_w;
+    const int W = (int)P.canvas_w, H = (int)P.canvas_h, R = P.band_rows, sw = P.seg_w;
     const int nseg = (W + sw - 1) / sw;
     const int b = (int)blockIdx.x / nseg, x0 = ((int)blockIdx.x % nseg) * sw;
     const int r = b * R + warp;
@@ -2632,7 +2633,8 @@ constexpr int SO_THREADS = 32 * (SO_CWARPS + 1);
 __global__ void __launch_bounds__(SO_THREADS, 6) k_srcover_mask(const __grid_constant__ CUtensorMap tm_canvas,
                                                                  const __grid_constant__ CUtensorMap tm_mask, int W,
                                                                  int H, int r0, unsigned clr, int32_t* status) {
-    extern __shared__ __align__(128) unsigned char smem[];
+    extern __shared__ __align__(128) unsigned char smem_tma[];  // TMA destinations: 128-byte aligned
+    unsigned char* smem = smem_tma;
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + SO_STAGES * SO_STAGE_BYTES);
     uint64_t* done = full + SO_STAGES;
     // src[a]: the colour's four channels times coverage a (pix's ch8_mul), packed; its
@@ -3335,7 +3337,6 @@ __global__ void __launch_bounds__(BLOCK) k_gb_emit(KParams P) {
     if (G.skip && *G.skip) return;  // a probe over a prefix of the ops completed the figure
     const long long n_raw = *G.n_raw;
     if (n_raw > G.raw_cap) return;  // every CTA: the caller grows the arrays
-    const int tid = threadIdx.x;
     int flags = 0;
     const GbOp o = gb_op_of(G, flags);
     if (o.kind >= FT_OP_MOVE && o.kind <= FT_OP_CUBIC) {
@@ -3891,10 +3892,9 @@ __global__ void __launch_bounds__(BLOCK) k_gs_write(KParams P) {
     }
 }
 
-// Sub-strokes (stroker.rs:87-96, 239-262), GB_TILE... 256 per chunk.
+// Sub-strokes (stroker.rs:87-96, 239-262), 256 a CTA step.
 __global__ void __launch_bounds__(BLOCK) k_gs_subs(KParams P) {
     __shared__ int tmp[2 * NWARP + 2];
-    __shared__ int s_c;
     const GridBuildBufs& G = P.gb;
     const GridStrokeBufs& S = P.gs;
     if (gs_over(S)) return;
@@ -3938,7 +3938,6 @@ __global__ void __launch_bounds__(BLOCK) k_gs_subs(KParams P) {
         carry += tot;
     }
     if (tid == 0) S.st[5] = carry;
-    (void)s_c;
 }
 
 // Outline item t: its sub-stroke (the last with item offset <= t: empty sub-strokes share
