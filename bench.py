@@ -151,6 +151,11 @@ def extra_scene(ctx, stream, dev, cpu=True):
             fill(_abi.NONZERO, _abi.MATTE8, m_d, w)
             fb[f"{name}_{cap_name}_nonzero_matte8_ms"] = _events_ms(
                 stream, lambda: fill(_abi.NONZERO, _abi.MATTE8, m_d, w), 3)
+        ctx.set_figure_cap(0)
+        ctx.set_join(_abi.JOIN_ROUND, 0.0)
+        stroke()
+        fb[f"{name}_stroke_w8_round_matte8_ms"] = _events_ms(stream, stroke, 3)
+        ctx.set_join(_abi.JOIN_MITER, 4.0)
     ctx.set_tuning(None)
     out["figure_build"] = fb
     ctx.set_figure_cap(0)
