@@ -1861,8 +1861,13 @@ cudaError_t launch_raster(const KParams& p, int grid, int smem_bytes, cudaStream
     return cudaGetLastError();
 }
 
+// The occupancy query honours the kernel's carve-out preference: a launch of at most one
+// CTA per SM leaves FEW_CTAS_CARVEOUT set, under which the query would report one CTA per
+// SM, the next grid would again be one CTA per SM and keep that carve-out for good.  The
+// query is made with no preference; each launch then sets its own.
 int raster_blocks_per_sm(int smem_bytes, bool stroke) {
     auto kern = stroke ? k_raster<true> : k_raster<false>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutDefault);
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, BLOCK, smem_bytes) != cudaSuccess) return 1;
@@ -4064,8 +4069,10 @@ cudaError_t launch_composite_build(const KParams& p, int grid, int smem_bytes, c
     return cudaGetLastError();
 }
 
+// As raster_blocks_per_sm: the query is made with no carve-out preference.
 int composite_build_blocks_per_sm(int smem_bytes, bool stroke) {
     auto kern = stroke ? k_cbuild<true> : k_cbuild<false>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutDefault);
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, BLOCK, smem_bytes) != cudaSuccess) return 1;

@@ -198,7 +198,8 @@ FT_API void ft_batch_destroy(ft_batch* batch);
  * The knobs of a batch plan: `warp_max_side`, the largest canvas side given whole to
  * one warp (0..512, 0 sends every path to the CTA rasteriser); `cta_smem_bytes`, the
  * CTA rasteriser's shared memory, which sets its tile: bands of as many full-width rows
- * as fit (0 = built-in choice); `split_px`, paths of at least this many pixels are
+ * as fit (0 = built-in choice; the ordered composite's figure builds keep their own
+ * 48 KB); `split_px`, paths of at least this many pixels are
  * split into row ranges, the queue grain of large paths (0 = 1 Mpx); `grid_per_sm`,
  * resident CTAs per SM of the persistent kernels (0 = occupancy maximum).
  * Ordered composites (ft_composite_batch, and single calls of at least split_px pixels):
@@ -235,7 +236,9 @@ FT_API int ft_set_tuning(ft_ctx* ctx, const ft_tuning* tuning);
 FT_API int ft_get_tuning(ft_ctx* ctx, ft_tuning* tuning);
 
 /* Autotuner: times candidate plans of this batch (prepared batches, graph replay, CUDA
- * events on the context stream) and keeps the fastest as the context's tuning.  With
+ * events on the context stream), the built-in plan first, and keeps the fastest as the
+ * context's tuning; a candidate displaces the plan in hand only when it is more than 1 %
+ * faster, so knobs the batch does not exercise keep their built-in values.  With
  * `cache_path` (may be NULL) the choice is looked up first and appended after tuning,
  * keyed by the GPU (name, SM count), the call kind and a signature of the batch
  * (path count, mean and largest canvas side, mean op count, in powers of two).  `ops`
