@@ -72,6 +72,7 @@ struct ft_ctx {
     float miter_limit = 4.0f;
     float s_width = 1.0f;   // host copy, valid unless sw_on_device
     bool sw_on_device = false;
+    int sw_cur = 0;         // the current slot of sw_chain
     // device buffers
     DevBuf ops, paths, overflow, status, sw_out, rasters, queue, scratch, sw_chain;
     DevBuf pool, pool_used, bandoff, crec;  // ordered composite
@@ -397,11 +398,14 @@ int single(ft_ctx* c, int stroke, int32_t rule, const ft_op* ops, uint32_t n_ops
     const uint64_t raster_bytes = h ? (uint64_t)(h - 1) * stride + (uint64_t)w * bpp : 0;
     int st = check_path(c, d, fmt, raster_bytes, n_ops);
     if (st != FT_OK) return st;
-    // pen-width chain: [0] current value, [1] value after this call
+    // pen-width chain (plotter.rs:151-153): two slots used in turn, the call reads the
+    // current one and its kernels write the width after the call into the other, which
+    // becomes current when the call is enqueued (no copy between calls)
     FT_CU(c->sw_chain.ensure(2 * sizeof(float)), "alloc pen width");
-    float* swd = static_cast<float*>(c->sw_chain.p);
+    float* sw_in = static_cast<float*>(c->sw_chain.p) + c->sw_cur;
+    float* sw_next = static_cast<float*>(c->sw_chain.p) + (c->sw_cur ^ 1);
     if (!c->sw_on_device) {
-        FT_CU(cudaMemcpyAsync(swd, &c->s_width, sizeof(float), cudaMemcpyHostToDevice, c->stream), "pen width");
+        FT_CU(cudaMemcpyAsync(sw_in, &c->s_width, sizeof(float), cudaMemcpyHostToDevice, c->stream), "pen width");
         c->sw_on_device = true;
     }
     const ft_op* ops_d = ops;
@@ -426,15 +430,15 @@ int single(ft_ctx* c, int stroke, int32_t rule, const ft_op* ops, uint32_t n_ops
         // a large canvas, or an un-capped fill: build the figure once and bin its edges,
         // then one CTA per band of rows (the ordered compositor with a single call)
         float sw0 = c->s_width;
-        FT_CU(cudaMemcpyAsync(&sw0, swd, sizeof(float), cudaMemcpyDeviceToHost, c->stream), "pen width");
+        FT_CU(cudaMemcpyAsync(&sw0, sw_in, sizeof(float), cudaMemcpyDeviceToHost, c->stream), "pen width");
         FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
         d.s_width = sw0;
-        st = composite_impl(c, stroke, rule, ops_d, n_ops, &d, 1, fmt, ras_d, w, h, stride, FT_DEVICE, swd + 1);
+        st = composite_impl(c, stroke, rule, ops_d, n_ops, &d, 1, fmt, ras_d, w, h, stride, FT_DEVICE, sw_next);
     } else {
-        st = run(c, stroke, rule, ops_d, &d, 1, fmt, ras_d, swd, swd + 1);
+        st = run(c, stroke, rule, ops_d, &d, 1, fmt, ras_d, sw_in, sw_next);
     }
     if (st != FT_OK) return st;
-    FT_CU(cudaMemcpyAsync(swd, swd + 1, sizeof(float), cudaMemcpyDeviceToDevice, c->stream), "pen width");
+    c->sw_cur ^= 1;
     if (where == FT_HOST) {
         if (raster_bytes)
             FT_CU(cudaMemcpyAsync(raster, c->rasters.p, raster_bytes, cudaMemcpyDeviceToHost, c->stream),
@@ -746,7 +750,9 @@ FT_API int ft_get_pen_width(ft_ctx* c, float* w) {
     if (!c || !w) return FT_ERR_ARG;
     if (c->sw_on_device && c->sw_chain.p) {
         FT_CU(cudaStreamSynchronize(c->stream), "synchronize");
-        FT_CU(cudaMemcpy(&c->s_width, c->sw_chain.p, sizeof(float), cudaMemcpyDeviceToHost), "pen width");
+        FT_CU(cudaMemcpy(&c->s_width, static_cast<float*>(c->sw_chain.p) + c->sw_cur, sizeof(float),
+                         cudaMemcpyDeviceToHost),
+              "pen width");
     }
     *w = c->s_width;
     return FT_OK;

@@ -71,6 +71,44 @@ def test_random_strokes(ctx, seed):
     assert ctx.pen_width() == sw
 
 
+def test_pen_width_chain_on_device(ctx):
+    """Consecutive strokes on device buffers hand the pen width from call to call on the
+    device (plotter.rs:151-153), with no host read in between; one call on a 1024² canvas
+    takes the large-canvas route (the figure built once, bands composited)."""
+    import ctypes
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(17)
+    calls = []
+    for k in range(6):
+        side = 1024 if k == 2 else 96
+        ops = workloads.random_path(rng, 96, int(rng.integers(2, 12)), n_sub=1, close=bool(k % 2))
+        if k in (0, 3, 4):
+            ops = np.concatenate([ops_array([PathOp.PenWidth(float(2 + 2.5 * k))]), ops])
+        calls.append((ops, side))
+    ctx.set_tolerance(0.3)
+    ctx.set_transform(_abi.IDENTITY)
+    ctx.set_join(_abi.JOIN_ROUND, 0.0)
+    ctx.set_pen_width(1.5)
+    clr = (ctypes.c_uint8 * 4)(0, 0, 0, 255)
+    keep = []
+    for ops, side in calls:
+        ops_d = torch.from_numpy(ops.view(np.uint8)).cuda()
+        r_d = torch.zeros((side, side), dtype=torch.uint8, device="cuda")
+        torch.cuda.synchronize()
+        ctx.check(ctx.L.ft_stroke(ctx.h, ctypes.c_void_p(ops_d.data_ptr()), len(ops), _abi.MATTE8, clr,
+                                  ctypes.c_void_p(r_d.data_ptr()), side, side, side, _abi.DEVICE))
+        keep.append((ops_d, r_d))
+    torch.cuda.synchronize()
+    sw = 1.5
+    for k, ((ops, side), (_, r_d)) in enumerate(zip(calls, keep)):
+        want = np.zeros((side, side), np.uint8)
+        st, sw = oracle.stroke(ops, want, _abi.MATTE8, (0, 0, 0, 255), s_width=sw, tolerance=0.3,
+                               transform=_abi.IDENTITY, join=_abi.JOIN_ROUND, miter_limit=0.0)
+        assert st == 0
+        assert_same(r_d.cpu().numpy(), want, f"call {k} (pen width {sw})")
+    assert ctx.pen_width() == sw
+
+
 def test_close_then_move_unjoins(ctx):
     # stroker.rs:230-236 — Close then Move leaves the first sub-stroke open
     ops = (Path2D().absolute().pen_width(4.0).move_to(10, 10).line_to(50, 12).line_to(30, 40).close()
