@@ -61,6 +61,9 @@ def lib():
             L.orc_stroke.restype = ctypes.c_int
             L.orc_stroke_outline.argtypes = [P, u32, ctypes.POINTER(Params), ctypes.c_float, P, u32]
             L.orc_stroke_outline.restype = u32
+            L.orc_stroke_points.argtypes = [P, u32, ctypes.POINTER(Params), ctypes.c_float, P, P,
+                                            ctypes.POINTER(u32), P, ctypes.POINTER(u32), u32]
+            L.orc_stroke_points.restype = u32
             L.orc_join_decisions.argtypes = [P, u32, ctypes.POINTER(Params), ctypes.c_float, i32, P, P, u32]
             L.orc_join_decisions.restype = u32
             L.orc_fig_points.argtypes = [P, u32, ctypes.POINTER(Params), P, u32]
@@ -151,6 +154,25 @@ def stroke_outline(ops, s_width=1.0, **params):
         if n <= cap:
             return out[:n]
         cap = n
+
+
+def stroke_points(ops, s_width=1.0, **params):
+    """The stroker's input and result for `ops` (stroker.rs:204-236): the events the
+    plotter hands it, an (n, 4) f32 array of (x, y, width, 0) per add_point and
+    (0, 0, 0, 1 + joined) per close; the kept stroke points, (m, 3) f32 (x, y, width);
+    and the sub-strokes, (k, 4) int32 (start, points, joined, done)."""
+    ops = np.ascontiguousarray(ops, dtype=_abi.OP_DTYPE)
+    cap = 1 << 16
+    while True:
+        ev = np.zeros((cap, 4), np.float32)
+        pts = np.zeros((cap, 3), np.float32)
+        subs = np.zeros((cap, 4), np.int32)
+        n_pts, n_subs = ctypes.c_uint32(0), ctypes.c_uint32(0)
+        n = lib().orc_stroke_points(_ptr(ops), len(ops), ctypes.byref(make_params(**params)), s_width, _ptr(ev),
+                                    _ptr(pts), ctypes.byref(n_pts), _ptr(subs), ctypes.byref(n_subs), cap)
+        if max(n, n_pts.value, n_subs.value) <= cap:
+            return ev[:n].copy(), pts[:n_pts.value].copy(), subs[:n_subs.value].copy()
+        cap = max(n, n_pts.value, n_subs.value)
 
 
 def join_decisions(ops, s_width=1.0, libm=False, with_uv=False, **params):

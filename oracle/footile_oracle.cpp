@@ -896,6 +896,56 @@ __attribute__((visibility("default"))) uint32_t orc_stroke_outline(const ft_op* 
     return (uint32_t)outline.size();
 }
 
+// The stream the plotter hands the stroker (plotter.rs:175-224 into stroker.rs:204-236)
+// and what the stroker keeps of it: `ev` gets 4 floats per event, (x, y, width, 0) for an
+// add_point and (0, 0, 0, 1 + joined) for a close; `pts` 3 floats per kept stroke point;
+// `subs` 4 ints per sub-stroke (start, points, joined, done).  Returns the event count;
+// n_pts / n_subs get the other two counts.  Each array holds `cap` entries at most.
+struct StrokeTee : orc::PlotDest {
+    orc::Stroke& st;
+    std::vector<float> ev;
+    explicit StrokeTee(orc::Stroke& s) : st(s) {}
+    void add_point(orc::WidePt p) override {
+        ev.insert(ev.end(), {p.p.x, p.p.y, p.w, 0.0f});
+        st.add_point(p);
+    }
+    void close(bool joined) override {
+        ev.insert(ev.end(), {0.0f, 0.0f, 0.0f, joined ? 2.0f : 1.0f});
+        st.close(joined);
+    }
+};
+
+__attribute__((visibility("default"))) uint32_t orc_stroke_points(const ft_op* ops, uint32_t n_ops,
+                                                                  const orc_params* prm, float s_width, float* ev,
+                                                                  float* pts, uint32_t* n_pts, int32_t* subs,
+                                                                  uint32_t* n_subs, uint32_t cap) {
+    uint8_t dummy = 0;
+    orc::Raster r{&dummy, 1, 1, 1, FT_MATTE8};
+    float tol = prm ? prm->tolerance : 0.3f;
+    const float* m = prm ? prm->transform : ORC_IDENTITY;
+    orc::Plotter p(r, tol, m, prm ? prm->join : FT_JOIN_MITER, prm ? prm->miter_limit : 4.0f, s_width);
+    orc::Stroke st(p.join, p.miter_limit, p.tol_sq, &p.status);
+    StrokeTee tee(st);
+    p.add_ops(ops, n_ops, tee);
+    const uint32_t n_ev = (uint32_t)(tee.ev.size() / 4);
+    for (uint32_t i = 0; i < n_ev && i < cap; i++)
+        for (int k = 0; k < 4; k++) ev[4 * i + k] = tee.ev[4 * i + k];
+    *n_pts = (uint32_t)st.points.size();
+    for (uint32_t i = 0; i < *n_pts && i < cap; i++) {
+        pts[3 * i] = st.points[i].p.x;
+        pts[3 * i + 1] = st.points[i].p.y;
+        pts[3 * i + 2] = st.points[i].w;
+    }
+    *n_subs = (uint32_t)st.subs.size();
+    for (uint32_t i = 0; i < *n_subs && i < cap; i++) {
+        subs[4 * i] = st.subs[i].start;
+        subs[4 * i + 1] = st.subs[i].n_points;
+        subs[4 * i + 2] = st.subs[i].joined;
+        subs[4 * i + 3] = st.subs[i].done;
+    }
+    return n_ev;
+}
+
 // The join decisions of the stroke outline of `ops` (stroker.rs:340-396), one byte per
 // join in outline order: 0 bevel, 1 miter, 2 round arc.  `libm` 0 takes the angle and
 // the miter sine from ft_fmath.h (as the CUDA path does), 1 from the C library's
