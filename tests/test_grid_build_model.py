@@ -17,6 +17,8 @@ import oracle
 from footile_gb300 import _abi
 from footile_gb300.path import PathOp, ops_array
 
+CAP = _abi.MAX_POINTS
+
 
 def raw_stream(ops):
     """Raw vertices of a Move/Line/Close/PenWidth path (identity transform, coordinates
@@ -158,3 +160,48 @@ def test_cap_with_many_subfigures():
     """Many short sub-figures that pop, crossing the cap."""
     rng = np.random.default_rng(7)
     check(random_lines(rng, 90000, grid=40, p_move=0.2, p_close=0.2, p_back=0.2))
+
+
+def cap_index(raw, rs, cap):
+    """The first raw vertex whose position reaches the cap (len(raw) when none does)."""
+    M = len(raw)
+    if M == 0:
+        return 0
+    idx = np.arange(M)
+    R = np.maximum.accumulate(np.where(rs, idx, -1))
+    same_prev = np.zeros(M, bool)
+    same_prev[1:] = np.all(raw[1:] == raw[:-1], axis=1)
+    keep = rs | ~same_prev
+    pop = np.append(rs[1:], True) & np.all(raw == raw[R], axis=1)
+    pos = np.concatenate([[0], np.cumsum(keep.astype(np.int64) - pop)[:-1]])
+    over = np.flatnonzero(pos >= cap)
+    return int(over[0]) if len(over) else M
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_probe_prefix_completes(seed):
+    """A figure built over a prefix of the ops is final once the cap falls inside the
+    prefix's raw vertices (the probe of k_gb_write sets its flag only then): every
+    decision before the cap vertex, and the count at it, depend on raw vertices up to it.
+    Prefixes ending just before, on and after the op that reaches the cap are built and
+    compared with the figure of the whole path."""
+    rng = np.random.default_rng(40 + seed)
+    ops = random_lines(rng, 76000, grid=300, p_move=0.04, p_close=0.04, p_back=0.05)
+    raw, rs = raw_stream(ops)
+    want = grid_figure(raw, rs, CAP)
+    l_full = cap_index(raw, rs, CAP)
+    assert l_full < len(raw), "the path must reach the cap"
+    # the op that emits raw vertex l_full
+    emits = np.isin(ops["kind"], [_abi.OP_MOVE, _abi.OP_LINE])
+    op_of = np.flatnonzero(emits)
+    j = int(op_of[l_full])
+    final = 0
+    for P in list(range(max(1, j - 3), min(len(ops), j + 5))) + [len(ops) - 1]:
+        rp, rsp = raw_stream(ops[:P])
+        if cap_index(rp, rsp, CAP) >= len(rp):
+            continue  # the cap is not inside this prefix: the probe is not final
+        final += 1
+        pts, ss = grid_figure(rp, rsp, CAP)
+        np.testing.assert_array_equal(pts, want[0])
+        np.testing.assert_array_equal(ss, want[1])
+    assert final >= 4
