@@ -22,8 +22,10 @@ from footile_gb300.path import PathOp, ops_array
 CAP = _abi.MAX_POINTS
 
 
-def grid_points(ev, cap=CAP):
-    """Kept stroke points (x, y, width) and sub-strokes (start, points, joined, done)."""
+def grid_points(ev, cap=CAP, ev_all=None):
+    """Kept stroke points (x, y, width) and sub-strokes (start, points, joined, done).
+    `ev_all` (a stream that `ev` is a prefix of): the last sub-stroke's flags come from
+    its closes, as the probe takes them from the ops of the whole path."""
     is_pt = ev[:, 3] == 0
     raw = ev[is_pt, :3]
     M = len(raw)
@@ -60,7 +62,7 @@ def grid_points(ev, cap=CAP):
     subs[-1, 1] = count - subs[-1, 0]
     # the last sub-stroke: the closes after the last point written
     last = int(ev_idx[np.flatnonzero(written)[-1]])
-    tail = ev[last + 1:, 3]
+    tail = (ev if ev_all is None else ev_all)[last + 1:, 3]
     tail = tail[tail > 0]
     if len(tail):
         subs[-1, 2] = int(tail[-1]) - 1
@@ -145,3 +147,62 @@ def test_point_cap(tail, extra):
     n_pts, _ = check(ops)
     if extra >= 0:
         assert n_pts == CAP
+
+
+def kept_count(ev):
+    """Stroke points a stream keeps before the cap applies."""
+    raw = ev[ev[:, 3] == 0]
+    if not len(raw):
+        return 0
+    ev_idx = np.flatnonzero(ev[:, 3] == 0)
+    starts = np.array([k == 0 or bool((ev[(ev_idx[k - 1] + 1 if k else 0):ev_idx[k], 3] > 0).any())
+                       for k in range(len(raw))])
+    same = np.zeros(len(raw), bool)
+    same[1:] = (raw[1:, 0] == raw[:-1, 0]) & (raw[1:, 1] == raw[:-1, 1])
+    return int((starts | ~same).sum())
+
+
+@pytest.mark.parametrize("tail", ["close_move", "line", "move_close"])
+def test_probe_prefix_completes(tail):
+    """The stroke points over a prefix of the ops are final once the prefix keeps more
+    than 65,535 (the probe of k_gs_keep sets its flag only then): the points and
+    sub-stroke starts come from the prefix, the last sub-stroke's joined and done flags
+    from the closes of the whole path.  Prefixes ending around the op whose point is the
+    65,536th kept are compared with the whole path."""
+    rng = np.random.default_rng(77)
+    n = CAP + 1200
+    ops = np.zeros(n, dtype=_abi.OP_DTYPE)
+    ops["kind"][:] = _abi.OP_LINE
+    ops["kind"][rng.integers(0, n, 300)] = _abi.OP_MOVE
+    ops["kind"][rng.integers(0, n, 300)] = _abi.OP_CLOSE
+    ops["kind"][0] = _abi.OP_MOVE
+    ops["v"][:, 0] = rng.integers(0, 200, n).astype(np.float32)
+    ops["v"][:, 1] = rng.integers(0, 200, n).astype(np.float32)
+    extra = {"close_move": [PathOp.Close(), PathOp.Move(3, 3), PathOp.Close()],
+             "line": [PathOp.Line(4, 4), PathOp.Line(8, 4)],
+             "move_close": [PathOp.Move(3, 3), PathOp.Close()]}[tail]
+    ops = np.concatenate([ops, ops_array(extra)])
+    ev, want_pts, want_subs = oracle.stroke_points(ops)
+    assert len(want_pts) == CAP
+    # the op that emits the 65,536th kept point
+    emits = np.flatnonzero(np.isin(ops["kind"], [_abi.OP_MOVE, _abi.OP_LINE]))
+    lo, hi = 1, len(ops)
+    while lo < hi:  # the shortest prefix keeping more than the cap
+        mid = (lo + hi) // 2
+        if kept_count(oracle.stroke_points(ops[:mid])[0]) > CAP:
+            hi = mid
+        else:
+            lo = mid
+            lo += 1
+    assert ops["kind"][lo - 1] in (_abi.OP_MOVE, _abi.OP_LINE) and lo - 1 in emits
+    final = 0
+    for P in list(range(lo - 3, min(lo + 4, len(ops) + 1))) + [len(ops)]:
+        ev_p = oracle.stroke_points(ops[:P])[0]
+        assert np.array_equal(ev_p, ev[:len(ev_p)])
+        if kept_count(ev_p) <= CAP:
+            continue  # the probe is not final
+        final += 1
+        pts, subs = grid_points(ev_p, ev_all=ev)
+        np.testing.assert_array_equal(pts, want_pts)
+        np.testing.assert_array_equal(subs, want_subs)
+    assert final >= 4
